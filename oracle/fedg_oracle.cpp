@@ -1,0 +1,1019 @@
+// fedg_oracle.cpp -- FP64 CPU restatement of the SCALE-DG 3D nonhydrostatic DG
+// dynamics step of FElib (ywkawai/FE-Project), used ONLY as test infrastructure:
+// the parity checker of the CUDA path and the timed CPU baseline.  Nothing in the
+// product library links or calls this file.
+//
+// Scope (flat cube domain: Gsqrt = 1, GI3 = 0, periodic in x/y, slip lids in z;
+// dry air: Rtot = Rdry, CVtot = CVdry, CPtot = CPdry; PRES_hyd_ref = 0 so
+// DPhydDx = DPhydDy = 0; constant Coriolis parameter f):
+//   * reference element: LGL nodes, orthonormal Legendre Vandermonde, D1D, exact
+//     (non-lumped) mass matrix -> tensor-product Lift, VPOrdM1 truncation,
+//     exponential modal filter
+//       FElib/src/element/scale_element_hexahedral.F90:102-404
+//       FElib/src/element/scale_element_operation_tensorprod3D.F90:5464-5569
+//       FElib/src/element/scale_element_modalfilter.F90:204-236
+//       FElib/src/common/scale_polynomial.F90:250-373
+//   * DRHOT -> PRES/DPRES      FElib/src/fluid_dyn_solver/scale_atm_dyn_dgm_nonhydro3d_common.F90:428-479
+//   * HEVE cal_tend            ..._nonhydro3d_rhot_heve.F90:292-489
+//     HEVE Rusanov face flux   ..._nonhydro3d_rhot_heve_numflux.F90:946-1139
+//   * HEVI cal_tend            ..._nonhydro3d_rhot_hevi.F90:289-482
+//     HEVI Rusanov face flux   ..._nonhydro3d_rhot_hevi_numflux.F90:232-418
+//   * HEVI cal_vi              ..._nonhydro3d_rhot_hevi.F90:772-965
+//     eval_Ax / solve / matbnd ..._nonhydro3d_rhot_hevi_common_2.F90:111-1328
+//     batched LU (partial piv) ..._hevi_common_linalgebra.F90:2296-2445
+//   * slip lid BC              ..._dgm_bnd.F90:270-367
+//   * modal filter apply       ..._dgm_modalfilter.F90:49-130
+//   * SSP-RK3 / IMEX ARK232    FElib/src/common/scale_timeint_rk.F90:1182-1278, 2201-2565
+//                              FElib/src/common/scale_timeint_rk_butcher_tab.F90:200-274
+//   * driver stage loop        ..._driver_nonhydro3d.F90:614-963
+//
+// Layout: every field is column-major (Np, Ne) like FElib, node n = i + N1*j + N1^2*k,
+// element ke = ex + NeX*ey + NeX*NeY*ez.  Exterior (halo) values are produced in place
+// from the neighbour element (periodic) or from the element itself with MOMZ reflected
+// (slip lid), which is what FElib's halo exchange + ApplyBC produce on one rank.
+//
+// The Newton solve of cal_vi has two modes: max_iter = 1 restates FElib exactly (one
+// linearised solve from the guess var0); max_iter > 1 iterates the same Newton step
+// until the scaled update is below tol (the iterated method this build adds).
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+#include <algorithm>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+enum { VD = 0, VMX = 1, VMY = 2, VMZ = 3, VRT = 4 };  // argument order of cal_tend_ex
+
+struct Const {
+  double grav = 9.80616, rdry = 287.04, cpdry = 1004.64, cvdry = 717.6, pres00 = 100000.0;
+};
+
+// ---------------------------------------------------------------------------------
+// 1D reference element on LGL nodes
+// ---------------------------------------------------------------------------------
+static double legendre(int n, double x) {
+  if (n == 0) return 1.0;
+  double p0 = 1.0, p1 = x;
+  for (int m = 1; m < n; ++m) {
+    double p2 = ((2.0 * m + 1.0) * x * p1 - m * p0) / (m + 1.0);
+    p0 = p1; p1 = p2;
+  }
+  return p1;
+}
+// derivative of P_n
+static double dlegendre(int n, double x) {
+  if (n == 0) return 0.0;
+  // (1-x^2) P_n' = n (P_{n-1} - x P_n); at interior points only
+  return n * (legendre(n - 1, x) - x * legendre(n, x)) / (1.0 - x * x);
+}
+
+// LGL nodes: +-1 and the zeros of P_N' (FElib obtains them as Jacobi(1,1) Gauss points by
+// dstev, scale_polynomial.F90:250-373); here by Newton iteration on P_N'.
+static void lgl_nodes(int N, std::vector<double>& x, std::vector<double>& w) {
+  x.assign(N + 1, 0.0); w.assign(N + 1, 0.0);
+  x[0] = -1.0; x[N] = 1.0;
+  for (int i = 1; i < N; ++i) {
+    double xi = -std::cos(M_PI * i / N);
+    for (int it = 0; it < 100; ++it) {
+      // f = P_N'(x); f' = P_N''(x) = (2x P_N' - N(N+1) P_N)/(1-x^2)
+      double f = dlegendre(N, xi);
+      double fp = (2.0 * xi * f - N * (N + 1.0) * legendre(N, xi)) / (1.0 - xi * xi);
+      double dx = f / fp;
+      xi -= dx;
+      if (std::fabs(dx) < 1e-17) break;
+    }
+    x[i] = xi;
+  }
+  for (int i = 0; i <= N; ++i) {
+    double pn = legendre(N, x[i]);
+    w[i] = 2.0 / (N * (N + 1.0) * pn * pn);  // scale_polynomial.F90:271-287
+  }
+}
+
+static void mat_inverse(int n, std::vector<double> a, std::vector<double>& inv) {
+  inv.assign(n * n, 0.0);
+  for (int i = 0; i < n; ++i) inv[i * n + i] = 1.0;
+  for (int c = 0; c < n; ++c) {
+    int piv = c;
+    for (int r = c + 1; r < n; ++r)
+      if (std::fabs(a[r * n + c]) > std::fabs(a[piv * n + c])) piv = r;
+    if (piv != c)
+      for (int k = 0; k < n; ++k) { std::swap(a[c * n + k], a[piv * n + k]); std::swap(inv[c * n + k], inv[piv * n + k]); }
+    double d = 1.0 / a[c * n + c];
+    for (int k = 0; k < n; ++k) { a[c * n + k] *= d; inv[c * n + k] *= d; }
+    for (int r = 0; r < n; ++r) {
+      if (r == c) continue;
+      double f = a[r * n + c];
+      if (f == 0.0) continue;
+      for (int k = 0; k < n; ++k) { a[r * n + k] -= f * a[c * n + k]; inv[r * n + k] -= f * inv[c * n + k]; }
+    }
+  }
+}
+
+struct Elem1D {
+  int N = 0, N1 = 0;
+  std::vector<double> x, w;
+  std::vector<double> V, invV;   // V(i,m) = P_m(x_i) sqrt(m+1/2)   (row-major, [i*N1+m])
+  std::vector<double> D;         // D(i,l) = l_l'(x_i)
+  std::vector<double> Minv;      // inverse of the exact 1D mass matrix = V V^T
+  std::vector<double> F;         // modal filter V diag(sigma) V^-1
+  std::vector<double> T;         // truncation of the highest mode V diag(1..1,0) V^-1
+
+  void init(int porder, double etac, double alpha, int ord) {
+    N = porder; N1 = porder + 1;
+    lgl_nodes(N, x, w);
+    V.assign(N1 * N1, 0.0);
+    for (int i = 0; i < N1; ++i)
+      for (int m = 0; m < N1; ++m) V[i * N1 + m] = legendre(m, x[i]) * std::sqrt(m + 0.5);
+    mat_inverse(N1, V, invV);
+    // derivative of the Lagrange basis at the LGL nodes (scale_element_hexahedral.F90:256-258)
+    D.assign(N1 * N1, 0.0);
+    for (int i = 0; i < N1; ++i)
+      for (int l = 0; l < N1; ++l) {
+        if (i != l) D[i * N1 + l] = legendre(N, x[i]) / (legendre(N, x[l]) * (x[i] - x[l]));
+      }
+    D[0] = -N * (N + 1.0) / 4.0;
+    D[N * N1 + N] = N * (N + 1.0) / 4.0;
+    // exact mass matrix M = (V V^T)^-1 (scale_element_base.F90:221-239), so M^-1 = V V^T
+    Minv.assign(N1 * N1, 0.0);
+    for (int i = 0; i < N1; ++i)
+      for (int j = 0; j < N1; ++j) {
+        double s = 0.0;
+        for (int m = 0; m < N1; ++m) s += V[i * N1 + m] * V[j * N1 + m];
+        Minv[i * N1 + j] = s;
+      }
+    // exponential filter (scale_element_modalfilter.F90:204-236, 60-95)
+    std::vector<double> sig(N1, 1.0);
+    for (int m = 0; m < N1; ++m) {
+      double eta = double(m) / double(N);
+      if (eta > etac && m != 0) sig[m] = std::exp(-alpha * std::pow((eta - etac) / (1.0 - etac), ord));
+    }
+    F.assign(N1 * N1, 0.0);
+    T.assign(N1 * N1, 0.0);
+    for (int i = 0; i < N1; ++i)
+      for (int j = 0; j < N1; ++j) {
+        double s = 0.0, t = 0.0;
+        for (int m = 0; m < N1; ++m) {
+          s += V[i * N1 + m] * sig[m] * invV[m * N1 + j];
+          if (m < N1 - 1) t += V[i * N1 + m] * invV[m * N1 + j];  // tensorprod3D.F90:5560-5563
+        }
+        F[i * N1 + j] = s;
+        T[i * N1 + j] = t;
+      }
+  }
+};
+
+// ---------------------------------------------------------------------------------
+// the oracle context
+// ---------------------------------------------------------------------------------
+struct Oracle {
+  Const c;
+  Elem1D e;
+  int N1, Np, Nfp, NfpTot;
+  int NeX, NeY, NeZ, Ne;
+  double xmin, xmax, ymin, ymax, zmin, zmax, dx, dy, dz;
+  double coriolis_f = 0.0;
+  int filter_on = 1;
+  // base state, (Np, Ne)
+  std::vector<double> dens_hyd, pres_hyd, therm_hyd;
+  double newton_cref = 340.0;  // velocity scale of the MOMZ convergence test
+
+  size_t nid(int i, int j, int k) const { return (size_t)i + (size_t)N1 * j + (size_t)N1 * N1 * k; }
+  size_t eid(int ex, int ey, int ez) const { return (size_t)ex + (size_t)NeX * ey + (size_t)NeX * NeY * ez; }
+};
+
+// face node -> (i,j,k) in the element; a,b are the face-local indices
+static inline void face_node(int N1, int f, int a, int b, int& i, int& j, int& k) {
+  const int N = N1 - 1;
+  switch (f) {
+    case 0: i = a; j = 0; k = b; break;      // y- (south)
+    case 1: i = N; j = a; k = b; break;      // x+ (east)
+    case 2: i = a; j = N; k = b; break;      // y+ (north)
+    case 3: i = 0; j = a; k = b; break;      // x- (west)
+    case 4: i = a; j = b; k = 0; break;      // z- (bottom)
+    default: i = a; j = b; k = N; break;     // z+ (top)
+  }
+}
+static const double NX[6] = {0, 1, 0, -1, 0, 0};
+static const double NY[6] = {-1, 0, 1, 0, 0, 0};
+static const double NZ[6] = {0, 0, 0, 0, -1, 1};
+
+// neighbour element across face f (periodic x/y); returns -1 at a lid
+static inline long neighbour(const Oracle& o, int ex, int ey, int ez, int f) {
+  switch (f) {
+    case 0: return (long)o.eid(ex, (ey - 1 + o.NeY) % o.NeY, ez);
+    case 1: return (long)o.eid((ex + 1) % o.NeX, ey, ez);
+    case 2: return (long)o.eid(ex, (ey + 1) % o.NeY, ez);
+    case 3: return (long)o.eid((ex - 1 + o.NeX) % o.NeX, ey, ez);
+    case 4: return ez > 0 ? (long)o.eid(ex, ey, ez - 1) : -1;
+    default: return ez < o.NeZ - 1 ? (long)o.eid(ex, ey, ez + 1) : -1;
+  }
+}
+static inline int opposite_face(int f) {
+  static const int opp[6] = {2, 3, 0, 1, 5, 4};
+  return opp[f];
+}
+
+// ---------------------------------------------------------------------------------
+// DRHOT -> DPRES (nonhydro3d_common.F90:428-479, CPU branch)
+// ---------------------------------------------------------------------------------
+static void drhot2pres(const Oracle& o, const double* drhot, double* pres, double* dpres) {
+  const double rP0 = 1.0 / o.c.pres00, kap = o.c.cpdry / o.c.cvdry;
+  const size_t n = (size_t)o.Np * o.Ne;
+#pragma omp parallel for
+  for (size_t p = 0; p < n; ++p) {
+    double rhot = o.therm_hyd[p] + drhot[p];
+    double pr = o.c.pres00 * std::pow(o.c.rdry * rP0 * rhot, kap);
+    if (pres) pres[p] = pr;
+    dpres[p] = pr - o.pres_hyd[p];
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// explicit tendency: HEVE (hevi = 0) or HEVI (hevi = 1)
+// ---------------------------------------------------------------------------------
+static void cal_tend(const Oracle& o, int hevi, const double* const q[5], const double* dpres, double* const t[5]) {
+  const int N1 = o.N1, Np = o.Np, Nfp = o.Nfp;
+  const double gamm = o.c.cpdry / o.c.cvdry;
+  const double E11 = 2.0 / o.dx, E22 = 2.0 / o.dy, E33 = 2.0 / o.dz;
+  const double FS[6] = {2.0 / o.dy, 2.0 / o.dx, 2.0 / o.dy, 2.0 / o.dx, 2.0 / o.dz, 2.0 / o.dz};
+  const std::vector<double>& D = o.e.D;
+  const std::vector<double>& Mi = o.e.Minv;
+  const std::vector<double>& T = o.e.T;
+  const int N = N1 - 1;
+
+#pragma omp parallel
+  {
+    std::vector<double> flux((size_t)Np * 3 * 5), dfl((size_t)Np * 4 * 5), delf((size_t)Nfp * 6 * 5);
+#pragma omp for schedule(static)
+    for (long ke = 0; ke < o.Ne; ++ke) {
+      const int ex = ke % o.NeX, ey = (ke / o.NeX) % o.NeY, ez = ke / (o.NeX * o.NeY);
+      const size_t off = (size_t)ke * Np;
+      // --- face flux (numflux get_generalvc) ---
+      for (int f = 0; f < 6; ++f) {
+        const long kn = neighbour(o, ex, ey, ez, f);
+        const int fo = opposite_face(f);
+        const double nx = NX[f], ny = NY[f], nz = NZ[f];
+        for (int b = 0; b < N1; ++b)
+          for (int a = 0; a < N1; ++a) {
+            int i, j, k; face_node(N1, f, a, b, i, j, k);
+            const size_t iM = off + o.nid(i, j, k);
+            size_t iP; double msign = 1.0;
+            if (kn >= 0) { int i2, j2, k2; face_node(N1, fo, a, b, i2, j2, k2); iP = (size_t)kn * Np + o.nid(i2, j2, k2); }
+            else { iP = iM; msign = -1.0; }  // slip lid: MOMZ reflected (dgm_bnd.F90:323-341)
+            const double ddM = q[VD][iM], ddP = q[VD][iP];
+            const double mxM = q[VMX][iM], mxP = q[VMX][iP];
+            const double myM = q[VMY][iM], myP = q[VMY][iP];
+            const double mzM = q[VMZ][iM], mzP = msign * q[VMZ][iP];
+            const double drM = q[VRT][iM], drP = q[VRT][iP];
+            const double dpM = dpres[iM], dpP = dpres[iP];
+            const double densM = ddM + o.dens_hyd[iM], densP = ddP + o.dens_hyd[iP];
+            const double rhotM = o.therm_hyd[iM] + drM, rhotP = o.therm_hyd[iP] + drP;
+            const double phM = o.pres_hyd[iM], phP = o.pres_hyd[iP];
+            const double tmp1 = FS[f] * 0.5;
+            const int fp = a + N1 * b;
+            double* df = &delf[(size_t)(f * Nfp + fp) * 5];
+            if (!hevi) {
+              const double velM = (mxM * nx + myM * ny + mzM * nz) / densM;
+              const double velP = (mxP * nx + myP * ny + mzP * nz) / densP;
+              const double gnn = std::fabs(nx) + std::fabs(ny) + std::fabs(nz);
+              const double alpha = std::max(std::sqrt(gnn * gamm * (phM + dpM) / densM) + std::fabs(velM),
+                                            std::sqrt(gnn * gamm * (phP + dpP) / densP) + std::fabs(velP));
+              df[VD] = tmp1 * (densP * velP - densM * velM - alpha * (ddP - ddM));
+              df[VRT] = tmp1 * (rhotP * velP - rhotM * velM - alpha * (drP - drM));
+              df[VMZ] = tmp1 * (mzP * velP - mzM * velM + (dpP - dpM) * nz - alpha * (mzP - mzM));
+              df[VMX] = tmp1 * (mxP * velP - mxM * velM + nx * (dpP - dpM) - alpha * (mxP - mxM));
+              df[VMY] = tmp1 * (myP * velP - myM * velM + ny * (dpP - dpM) - alpha * (myP - myM));
+            } else {
+              const double velhM = (mxM * nx + myM * ny) / densM;
+              const double velhP = (mxP * nx + myP * ny) / densP;
+              const double velM = velhM + mzM * nz / densM;
+              const double velP = velhP + mzP * nz / densP;
+              const double swV = 1.0 - nz * nz;
+              const double alpha = swV * std::max(std::sqrt(gamm * (phM + dpM) / densM) + std::fabs(velM),
+                                                  std::sqrt(gamm * (phP + dpP) / densP) + std::fabs(velP));
+              df[VD] = tmp1 * (densP * velhP - densM * velhM - alpha * (ddP - ddM));
+              df[VRT] = tmp1 * (rhotP * velhP - rhotM * velhM - alpha * (drP - drM));
+              df[VMZ] = tmp1 * (mzP * velP - mzM * velM - alpha * (mzP - mzM));
+              df[VMX] = tmp1 * (mxP * velP - mxM * velM + nx * (dpP - dpM) - alpha * (mxP - mxM));
+              df[VMY] = tmp1 * (myP * velP - myM * velM + ny * (dpP - dpM) - alpha * (myP - myM));
+            }
+          }
+      }
+      // --- volume fluxes (cal_tend flux build) ---
+      for (int p = 0; p < Np; ++p) {
+        const size_t g = off + p;
+        const double dd = q[VD][g], mx = q[VMX][g], my = q[VMY][g], mz = q[VMZ][g], dr = q[VRT][g], dp = dpres[g];
+        const double rdens = 1.0 / (dd + o.dens_hyd[g]);
+        double* F = &flux[(size_t)p * 15];  // [dir*5 + var]
+        F[0 * 5 + VD] = mx; F[1 * 5 + VD] = my; F[2 * 5 + VD] = mz;
+        const double pt = (o.therm_hyd[g] + dr) * rdens;
+        F[0 * 5 + VRT] = mx * pt; F[1 * 5 + VRT] = my * pt; F[2 * 5 + VRT] = hevi ? 0.0 : mz * pt;
+        const double w = mz * rdens;
+        F[0 * 5 + VMZ] = mx * w; F[1 * 5 + VMZ] = my * w; F[2 * 5 + VMZ] = mz * w + (hevi ? 0.0 : dp);
+        const double u = mx * rdens, v = my * rdens;
+        F[0 * 5 + VMX] = mx * u + dp; F[1 * 5 + VMX] = my * u; F[2 * 5 + VMX] = mz * u;
+        F[0 * 5 + VMY] = mx * v; F[1 * 5 + VMY] = my * v + dp; F[2 * 5 + VMY] = mz * v;
+      }
+      // --- Div_var5: D1D along x, y, z; tensor-product Lift ---
+      for (int k = 0; k < N1; ++k)
+        for (int j = 0; j < N1; ++j)
+          for (int i = 0; i < N1; ++i) {
+            const int p = (int)o.nid(i, j, k);
+            for (int v = 0; v < 5; ++v) {
+              double sx = 0, sy = 0, sz = 0;
+              for (int l = 0; l < N1; ++l) {
+                sx += D[i * N1 + l] * flux[(size_t)o.nid(l, j, k) * 15 + 0 * 5 + v];
+                sy += D[j * N1 + l] * flux[(size_t)o.nid(i, l, k) * 15 + 1 * 5 + v];
+                sz += D[k * N1 + l] * flux[(size_t)o.nid(i, j, l) * 15 + 2 * 5 + v];
+              }
+              // Lift_hexahedral (tensorprod3D_kernel.F90:2316-2339 with Lift_mat of :5512-5569)
+              const double lf =
+                  Mi[j * N1 + 0] * delf[(size_t)(0 * Nfp + i + N1 * k) * 5 + v] +
+                  Mi[i * N1 + N] * delf[(size_t)(1 * Nfp + j + N1 * k) * 5 + v] +
+                  Mi[j * N1 + N] * delf[(size_t)(2 * Nfp + i + N1 * k) * 5 + v] +
+                  Mi[i * N1 + 0] * delf[(size_t)(3 * Nfp + j + N1 * k) * 5 + v] +
+                  Mi[k * N1 + 0] * delf[(size_t)(4 * Nfp + i + N1 * j) * 5 + v] +
+                  Mi[k * N1 + N] * delf[(size_t)(5 * Nfp + i + N1 * j) * 5 + v];
+              double* d = &dfl[(size_t)p * 20 + v * 4];
+              d[0] = sx; d[1] = sy; d[2] = sz; d[3] = lf;
+            }
+          }
+      // --- combine (heve.F90:424-465, hevi.F90:416-478) ---
+      for (int k = 0; k < N1; ++k)
+        for (int j = 0; j < N1; ++j)
+          for (int i = 0; i < N1; ++i) {
+            const int p = (int)o.nid(i, j, k);
+            const size_t g = off + p;
+            const double* d = &dfl[(size_t)p * 20];
+            auto full = [&](int v) { return E11 * d[v * 4 + 0] + E22 * d[v * 4 + 1] + E33 * d[v * 4 + 2] + d[v * 4 + 3]; };
+            auto horiz = [&](int v) { return E11 * d[v * 4 + 0] + E22 * d[v * 4 + 1] + d[v * 4 + 3]; };
+            if (!hevi) {
+              t[VD][g] = -full(VD);
+              t[VRT][g] = -full(VRT);
+              double drho = 0.0;  // VFilterPM1(DDENS) along z
+              for (int l = 0; l < N1; ++l) drho += T[k * N1 + l] * q[VD][off + o.nid(i, j, l)];
+              t[VMZ][g] = -full(VMZ) - o.c.grav * drho;
+            } else {
+              t[VD][g] = -horiz(VD);
+              t[VRT][g] = -horiz(VRT);
+              t[VMZ][g] = -full(VMZ);
+            }
+            t[VMX][g] = o.coriolis_f * q[VMY][g] - full(VMX);
+            t[VMY][g] = -o.coriolis_f * q[VMX][g] - full(VMY);
+          }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// modal filter (dgm_modalfilter.F90:49-130, Gsqrt = 1)
+// ---------------------------------------------------------------------------------
+static void modal_filter(const Oracle& o, double* const q[5]) {
+  const int N1 = o.N1, Np = o.Np;
+  const std::vector<double>& F = o.e.F;
+#pragma omp parallel
+  {
+    std::vector<double> a(Np), b(Np);
+#pragma omp for schedule(static)
+    for (long ke = 0; ke < o.Ne; ++ke)
+      for (int v = 0; v < 5; ++v) {
+        double* x = q[v] + (size_t)ke * Np;
+        for (int k = 0; k < N1; ++k)
+          for (int j = 0; j < N1; ++j)
+            for (int i = 0; i < N1; ++i) {
+              double s = 0;
+              for (int l = 0; l < N1; ++l) s += F[i * N1 + l] * x[o.nid(l, j, k)];
+              a[o.nid(i, j, k)] = s;
+            }
+        for (int k = 0; k < N1; ++k)
+          for (int j = 0; j < N1; ++j)
+            for (int i = 0; i < N1; ++i) {
+              double s = 0;
+              for (int l = 0; l < N1; ++l) s += F[j * N1 + l] * a[o.nid(i, l, k)];
+              b[o.nid(i, j, k)] = s;
+            }
+        for (int k = 0; k < N1; ++k)
+          for (int j = 0; j < N1; ++j)
+            for (int i = 0; i < N1; ++i) {
+              double s = 0;
+              for (int l = 0; l < N1; ++l) s += F[k * N1 + l] * b[o.nid(i, j, l)];
+              x[o.nid(i, j, k)] = s;
+            }
+      }
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// HEVI vertical-implicit solve, one horizontal node column at a time.
+// ---------------------------------------------------------------------------------
+// LU with partial pivoting of an n x n row-major matrix, solving nrhs right-hand sides
+// stored row-major in R (n x nrhs)  (linalgebra.F90:2296-2445 does the same per column).
+static void lu_solve(int n, double* A, double* R, int nrhs) {
+  for (int k = 0; k < n; ++k) {
+    int piv = k;
+    double amax = std::fabs(A[k * n + k]);
+    for (int r = k + 1; r < n; ++r)
+      if (std::fabs(A[r * n + k]) > amax) { amax = std::fabs(A[r * n + k]); piv = r; }
+    if (piv != k) {
+      for (int c = 0; c < n; ++c) std::swap(A[k * n + c], A[piv * n + c]);
+      for (int c = 0; c < nrhs; ++c) std::swap(R[k * nrhs + c], R[piv * nrhs + c]);
+    }
+    const double rd = 1.0 / A[k * n + k];
+    for (int r = k + 1; r < n; ++r) {
+      const double f = A[r * n + k] * rd;
+      if (f == 0.0) continue;
+      A[r * n + k] = f;
+      for (int c = k + 1; c < n; ++c) A[r * n + c] -= f * A[k * n + c];
+      for (int c = 0; c < nrhs; ++c) R[r * nrhs + c] -= f * R[k * nrhs + c];
+    }
+  }
+  for (int k = n - 1; k >= 0; --k) {
+    const double rd = 1.0 / A[k * n + k];
+    for (int c = 0; c < nrhs; ++c) {
+      double s = R[k * nrhs + c];
+      for (int m = k + 1; m < n; ++m) s -= A[k * n + m] * R[m * nrhs + c];
+      R[k * nrhs + c] = s * rd;
+    }
+  }
+}
+
+struct ColumnWork {
+  // per level (L = NeZ*N1): prognostic iterate, stage input, guess var0, base state
+  std::vector<double> P[5], Q[5], Z[5], dh, ph, rh;
+  std::vector<double> alphB, alphT;      // vertical-face alph per element (bottom, top)
+  std::vector<double> A3;                // eval_Ax output (3, L)
+  std::vector<double> b, G, D, Lm, Um, Guv, Duv, Luv, Uuv, buv;
+  std::vector<double> W, WT, POT, DPDRHOT;
+};
+
+struct ColumnParams {
+  double impl_fac, dt, tol;
+  int max_iter;
+};
+
+// eval_Ax (var3) for the whole column at the current iterate P; fills A3 (-> tendencies),
+// and the linearisation fields.  common_2.F90:111-326 and vi_cal_del_flux_dyn :1171-1328.
+static void column_eval_Ax(const Oracle& o, ColumnWork& w) {
+  const int N1 = o.N1, NeZ = o.NeZ, L = NeZ * N1, N = N1 - 1;
+  const double E33 = 2.0 / o.dz, FSz = 2.0 / o.dz;
+  const double rP0 = 1.0 / o.c.pres00, kap = o.c.cpdry / o.c.cvdry;
+  const std::vector<double>& D = o.e.D;
+  const std::vector<double>& Mi = o.e.Minv;
+  const std::vector<double>& T = o.e.T;
+  std::vector<double> fd(L), fr(L), fm(L), pot(L), dens(L);
+  for (int l = 0; l < L; ++l) {
+    dens[l] = w.dh[l] + w.P[VD][l];
+    const double rhot = w.rh[l] + w.P[VRT][l];
+    pot[l] = rhot / dens[l];
+    fd[l] = w.P[VMZ][l];                       // MOMW (flat)
+    fr[l] = pot[l] * fd[l];
+    const double pr = o.c.pres00 * std::pow(o.c.rdry * rP0 * rhot, kap);
+    fm[l] = pr - w.ph[l];                      // DPRES
+    w.POT[l] = pot[l];
+    w.W[l] = w.P[VMZ][l] / dens[l];
+    w.WT[l] = fd[l] / dens[l];
+    w.DPDRHOT[l] = kap * pr / rhot;
+  }
+  for (int ez = 0; ez < NeZ; ++ez) {
+    // face values: 0 = bottom (nz=-1), 1 = top (nz=+1)
+    double del[2][3];
+    for (int s = 0; s < 2; ++s) {
+      const int lM = ez * N1 + (s == 0 ? 0 : N);
+      int lP; bool lid = false;
+      if (s == 0) { if (ez > 0) lP = (ez - 1) * N1 + N; else { lP = lM; lid = true; } }
+      else { if (ez < NeZ - 1) lP = (ez + 1) * N1; else { lP = lM; lid = true; } }
+      const double nz = s == 0 ? -1.0 : 1.0;
+      const double alph = s == 0 ? w.alphB[ez] : w.alphT[ez];
+      const double ddM = w.P[VD][lM], ddP = w.P[VD][lP];
+      const double mzM = w.P[VMZ][lM];
+      const double mzP = lid ? -mzM : w.P[VMZ][lP];
+      const double mwM = mzM, mwP = lid ? -mzM : w.P[VMZ][lP];
+      const double drM = w.P[VRT][lM], drP = w.P[VRT][lP];
+      const double tmp1 = 0.5 * FSz;
+      del[s][0] = tmp1 * ((mwP - mwM) * nz - alph * (ddP - ddM));
+      del[s][1] = tmp1 * ((fm[lP] - fm[lM]) * nz - alph * (mzP - mzM));
+      del[s][2] = tmp1 * ((pot[lP] * mwP - pot[lM] * mwM) * nz - alph * (drP - drM));
+    }
+    for (int k = 0; k < N1; ++k) {
+      const int l = ez * N1 + k;
+      double sd = 0, sr = 0, sm = 0, drho = 0;
+      for (int m = 0; m < N1; ++m) {
+        sd += D[k * N1 + m] * fd[ez * N1 + m];
+        sr += D[k * N1 + m] * fr[ez * N1 + m];
+        sm += D[k * N1 + m] * fm[ez * N1 + m];
+        drho += T[k * N1 + m] * w.P[VD][ez * N1 + m];
+      }
+      const double lb = Mi[k * N1 + 0], lt = Mi[k * N1 + N];
+      w.A3[0 * L + l] = -(E33 * sd + lb * del[0][0] + lt * del[1][0]);
+      w.A3[1 * L + l] = -(E33 * sm + lb * del[0][1] + lt * del[1][1]) - o.c.grav * drho;
+      w.A3[2 * L + l] = -(E33 * sr + lb * del[0][2] + lt * del[1][2]);
+    }
+  }
+}
+
+// MOMX/MOMY implicit tendency -Lift(del_flux_uv) at iterate P (eval_Ax_uv, common_2.F90:482-586)
+static void column_eval_Ax_uv(const Oracle& o, ColumnWork& w, std::vector<double>& tx, std::vector<double>& ty) {
+  const int N1 = o.N1, NeZ = o.NeZ, N = N1 - 1;
+  const double FSz = 2.0 / o.dz;
+  const std::vector<double>& Mi = o.e.Minv;
+  for (int ez = 0; ez < NeZ; ++ez) {
+    double dx_[2], dy_[2];
+    for (int s = 0; s < 2; ++s) {
+      const int lM = ez * N1 + (s == 0 ? 0 : N);
+      int lP;
+      if (s == 0) lP = ez > 0 ? (ez - 1) * N1 + N : lM;
+      else lP = ez < NeZ - 1 ? (ez + 1) * N1 : lM;
+      const double alph = s == 0 ? w.alphB[ez] : w.alphT[ez];
+      const double tmp1 = -0.5 * FSz * alph;
+      dx_[s] = tmp1 * (w.P[VMX][lP] - w.P[VMX][lM]);
+      dy_[s] = tmp1 * (w.P[VMY][lP] - w.P[VMY][lM]);
+    }
+    for (int k = 0; k < N1; ++k) {
+      const double lb = Mi[k * N1 + 0], lt = Mi[k * N1 + N];
+      tx[ez * N1 + k] = -(lb * dx_[0] + lt * dx_[1]);
+      ty[ez * N1 + k] = -(lb * dy_[0] + lt * dy_[1]);
+    }
+  }
+}
+
+// returns the number of Newton iterations used (or -1 if not converged within max_iter)
+static int column_solve(const Oracle& o, ColumnWork& w, const ColumnParams& cp, double* tend_out[5], int L) {
+  const int N1 = o.N1, NeZ = o.NeZ, N = N1 - 1, n3 = 3 * N1;
+  const double E33 = 2.0 / o.dz, FSz = 2.0 / o.dz;
+  const double rP0 = 1.0 / o.c.pres00, kap = o.c.cpdry / o.c.cvdry;
+  const std::vector<double>& Dm = o.e.D;
+  const std::vector<double>& Mi = o.e.Minv;
+  const std::vector<double>& T = o.e.T;
+  const double impl_fac = cp.impl_fac;
+
+  // alph from var0 (vi_cal_del_flux_dyn_uv :1149-1155; Gnn = |nz| = 1 on vertical faces)
+  std::vector<double> s0(L);
+  for (int l = 0; l < L; ++l) {
+    const double rdens0 = 1.0 / (w.dh[l] + w.Z[VD][l]);
+    const double wt0 = w.Z[VMZ][l] * rdens0;
+    const double pres0 = o.c.pres00 * std::pow(o.c.rdry * rP0 * (w.rh[l] + w.Z[VRT][l]), kap);
+    s0[l] = std::fabs(wt0) + std::sqrt(kap * pres0 * rdens0);
+  }
+  for (int ez = 0; ez < NeZ; ++ez) {
+    const int lb = ez * N1, lt = ez * N1 + N;
+    const int lbP = ez > 0 ? (ez - 1) * N1 + N : lb;
+    const int ltP = ez < NeZ - 1 ? (ez + 1) * N1 : lt;
+    w.alphB[ez] = std::max(s0[lb], s0[lbP]);
+    w.alphT[ez] = std::max(s0[lt], s0[ltP]);
+  }
+
+  for (int v = 0; v < 5; ++v) w.P[v] = w.Z[v];  // PROG_VARS = var0 (hevi.F90:852-872)
+
+  std::vector<double> tx(L), ty(L);
+  if (impl_fac == 0.0) {  // hevi.F90:943-961: tendencies of the implicit operator at var0
+    column_eval_Ax_uv(o, w, tx, ty);
+    column_eval_Ax(o, w);
+    for (int l = 0; l < L; ++l) {
+      tend_out[VD][l] = w.A3[0 * L + l];
+      tend_out[VMZ][l] = w.A3[1 * L + l];
+      tend_out[VRT][l] = w.A3[2 * L + l];
+      tend_out[VMX][l] = tx[l];
+      tend_out[VMY][l] = ty[l];
+    }
+    return 0;
+  }
+
+  // ---- MOMX/MOMY: one linear solve (eval_Ax_uv + solve_uv, common_2.F90:482-689) ----
+  column_eval_Ax_uv(o, w, tx, ty);
+  {
+    const int n = N1;
+    std::vector<double>& buv = w.buv;   // (L, 2)
+    for (int l = 0; l < L; ++l) {
+      buv[l * 2 + 0] = impl_fac * tx[l] - w.P[VMX][l] + w.Q[VMX][l];
+      buv[l * 2 + 1] = impl_fac * ty[l] - w.P[VMY][l] + w.Q[VMY][l];
+    }
+    std::vector<double> Dd(n * n), R(n * 3), Lc(n), Uc(n);
+    std::vector<double>& Guv = w.Guv;   // (NeZ, n)
+    for (int ez = 0; ez < NeZ; ++ez) {
+      std::fill(Dd.begin(), Dd.end(), 0.0);
+      for (int p = 0; p < n; ++p) Dd[p * n + p] = 1.0;
+      for (int f = 0; f < 2; ++f) {
+        const bool bc = (ez == 0 && f == 0) || (ez == NeZ - 1 && f == 1);
+        const int pv1 = f == 0 ? 0 : N;
+        const double alph = f == 0 ? w.alphB[ez] : w.alphT[ez];
+        for (int p = 0; p < n; ++p) {
+          const double lift = f == 0 ? Mi[p * N1 + 0] : Mi[p * N1 + N];
+          const double tmp1 = 0.5 * impl_fac * lift * FSz * alph;
+          if (!bc) {
+            Dd[p * n + pv1] += tmp1;
+            if (f == 0) Lc[p] = -tmp1; else Uc[p] = -tmp1;
+          }
+        }
+      }
+      for (int p = 0; p < n; ++p) {
+        const int l = ez * N1 + p;
+        if (ez > 0) {
+          const double Lv = Lc[p];
+          Dd[p * n + 0] -= Lv * Guv[(ez - 1) * n + N];
+          buv[l * 2 + 0] -= Lv * buv[((ez - 1) * N1 + N) * 2 + 0];
+          buv[l * 2 + 1] -= Lv * buv[((ez - 1) * N1 + N) * 2 + 1];
+        }
+        R[p * 3 + 0] = buv[l * 2 + 0];
+        R[p * 3 + 1] = buv[l * 2 + 1];
+        R[p * 3 + 2] = (ez < NeZ - 1) ? Uc[p] : 0.0;
+      }
+      lu_solve(n, Dd.data(), R.data(), 3);
+      for (int p = 0; p < n; ++p) {
+        const int l = ez * N1 + p;
+        buv[l * 2 + 0] = R[p * 3 + 0];
+        buv[l * 2 + 1] = R[p * 3 + 1];
+        Guv[ez * n + p] = R[p * 3 + 2];
+      }
+    }
+    for (int ez = NeZ - 2; ez >= 0; --ez)
+      for (int p = 0; p < n; ++p) {
+        const int l = ez * N1 + p;
+        const double g = Guv[ez * n + p];
+        buv[l * 2 + 0] -= g * buv[((ez + 1) * N1) * 2 + 0];
+        buv[l * 2 + 1] -= g * buv[((ez + 1) * N1) * 2 + 1];
+      }
+    for (int l = 0; l < L; ++l) { w.P[VMX][l] += buv[l * 2 + 0]; w.P[VMY][l] += buv[l * 2 + 1]; }
+  }
+
+  // ---- DENS/MOMZ/RHOT: Newton iterations (eval_Ax + solve, common_2.F90:111-479) ----
+  int iters_used = -1;
+  for (int it = 1; it <= cp.max_iter; ++it) {
+    column_eval_Ax(o, w);
+    std::vector<double>& b = w.b;  // (NeZ, n3) row index v + 3*pv
+    for (int ez = 0; ez < NeZ; ++ez)
+      for (int k = 0; k < N1; ++k) {
+        const int l = ez * N1 + k;
+        b[ez * n3 + 3 * k + 0] = impl_fac * w.A3[0 * L + l] - w.P[VD][l] + w.Q[VD][l];
+        b[ez * n3 + 3 * k + 1] = impl_fac * w.A3[1 * L + l] - w.P[VMZ][l] + w.Q[VMZ][l];
+        b[ez * n3 + 3 * k + 2] = impl_fac * w.A3[2 * L + l] - w.P[VRT][l] + w.Q[VRT][l];
+      }
+    std::vector<double>& G = w.G;           // (NeZ, n3, 3)
+    std::vector<double> Dd(n3 * n3), R(n3 * 4), Lc(n3 * 3), Uc(n3 * 3);
+    for (int ez = 0; ez < NeZ; ++ez) {
+      // construct_matbnd (common_2.F90:693-901)
+      std::fill(Dd.begin(), Dd.end(), 0.0);
+      std::fill(Lc.begin(), Lc.end(), 0.0);
+      std::fill(Uc.begin(), Uc.end(), 0.0);
+      auto Dat = [&](int v, int pv, int v2, int pv2) -> double& { return Dd[(v + 3 * pv) * n3 + v2 + 3 * pv2]; };
+      for (int pv = 0; pv < N1; ++pv)
+        for (int pv2 = 0; pv2 < N1; ++pv2) {
+          const int l2 = ez * N1 + pv2;
+          const double fdz = E33 * impl_fac * Dm[pv * N1 + pv2];
+          const double id = pv == pv2 ? 1.0 : 0.0;
+          Dat(0, pv, 0, pv2) = id;
+          Dat(0, pv, 1, pv2) = fdz;
+          Dat(0, pv, 2, pv2) = 0.0;
+          Dat(1, pv, 1, pv2) = id;
+          Dat(1, pv, 0, pv2) = impl_fac * o.c.grav * T[pv * N1 + pv2];
+          Dat(1, pv, 2, pv2) = fdz * w.DPDRHOT[l2];
+          Dat(2, pv, 0, pv2) = -fdz * w.POT[l2] * w.WT[l2];
+          Dat(2, pv, 1, pv2) = fdz * w.POT[l2];
+          Dat(2, pv, 2, pv2) = id + fdz * w.WT[l2];
+        }
+      for (int f = 0; f < 2; ++f) {
+        const bool bc = (ez == 0 && f == 0) || (ez == NeZ - 1 && f == 1);
+        const int pv1 = f == 0 ? 0 : N;
+        const int ezn = f == 0 ? std::max(ez - 1, 0) : std::min(ez + 1, NeZ - 1);
+        const int pvn = bc ? pv1 : (f == 0 ? N : 0);
+        const int l1 = ez * N1 + pv1, ln = ezn * N1 + pvn;
+        const double nz = f == 0 ? -1.0 : 1.0;
+        const double alph = f == 0 ? w.alphB[ez] : w.alphT[ez];
+        for (int pv = 0; pv < N1; ++pv) {
+          const double lift = f == 0 ? Mi[pv * N1 + 0] : Mi[pv * N1 + N];
+          const double fac = 0.5 * impl_fac * lift * FSz;
+          const double tmp1 = fac * alph, tmp2 = fac * nz;
+          if (bc) {
+            Dat(2, pv, 0, pv1) += 2.0 * tmp2 * w.POT[l1] * w.WT[l1];
+            Dat(0, pv, 1, pv1) -= 2.0 * tmp2;
+            Dat(1, pv, 1, pv1) += 2.0 * tmp1;
+            Dat(2, pv, 1, pv1) -= 2.0 * tmp2 * w.POT[l1];
+            Dat(2, pv, 2, pv1) -= 2.0 * tmp2 * w.WT[l1];
+          } else {
+            Dat(0, pv, 0, pv1) += tmp1;
+            Dat(2, pv, 0, pv1) += tmp2 * w.POT[l1] * w.WT[l1];
+            Dat(0, pv, 1, pv1) -= tmp2;
+            Dat(1, pv, 1, pv1) += tmp1;
+            Dat(2, pv, 1, pv1) -= tmp2 * w.POT[l1];
+            Dat(1, pv, 2, pv1) -= tmp2 * w.DPDRHOT[l1];
+            Dat(2, pv, 2, pv1) += tmp1 - tmp2 * w.WT[l1];
+            std::vector<double>& C = f == 0 ? Lc : Uc;  // (n3, 3): [row*3 + var of the neighbour node]
+            C[(0 + 3 * pv) * 3 + 0] = -tmp1;
+            C[(1 + 3 * pv) * 3 + 0] = 0.0;
+            C[(2 + 3 * pv) * 3 + 0] = -tmp2 * w.POT[ln] * w.WT[ln];
+            C[(0 + 3 * pv) * 3 + 1] = tmp2;
+            C[(1 + 3 * pv) * 3 + 1] = -tmp1;
+            C[(2 + 3 * pv) * 3 + 1] = tmp2 * w.POT[ln];
+            C[(0 + 3 * pv) * 3 + 2] = 0.0;
+            C[(1 + 3 * pv) * 3 + 2] = tmp2 * w.DPDRHOT[ln];
+            C[(2 + 3 * pv) * 3 + 2] = -tmp1 + tmp2 * w.WT[ln];
+          }
+        }
+      }
+      // block-Thomas forward elimination (common_2.F90:390-430)
+      if (ez > 0) {
+        const int p1 = 3 * N;
+        for (int r = 0; r < n3; ++r) {
+          for (int c2 = 0; c2 < 3; ++c2) {
+            double s = 0;
+            for (int m = 0; m < 3; ++m) s += Lc[r * 3 + m] * G[((ez - 1) * n3 + p1 + m) * 3 + c2];
+            Dd[r * n3 + c2] -= s;
+          }
+          double s = 0;
+          for (int m = 0; m < 3; ++m) s += Lc[r * 3 + m] * b[(ez - 1) * n3 + p1 + m];
+          b[ez * n3 + r] -= s;
+        }
+      }
+      for (int r = 0; r < n3; ++r) {
+        R[r * 4 + 0] = b[ez * n3 + r];
+        for (int m = 0; m < 3; ++m) R[r * 4 + 1 + m] = (ez < NeZ - 1) ? Uc[r * 3 + m] : 0.0;
+      }
+      lu_solve(n3, Dd.data(), R.data(), 4);
+      for (int r = 0; r < n3; ++r) {
+        b[ez * n3 + r] = R[r * 4 + 0];
+        for (int m = 0; m < 3; ++m) G[(ez * n3 + r) * 3 + m] = R[r * 4 + 1 + m];
+      }
+    }
+    for (int ez = NeZ - 2; ez >= 0; --ez)  // back substitution (common_2.F90:443-458)
+      for (int r = 0; r < n3; ++r) {
+        double s = 0;
+        for (int m = 0; m < 3; ++m) s += G[(ez * n3 + r) * 3 + m] * b[(ez + 1) * n3 + m];
+        b[ez * n3 + r] -= s;
+      }
+    double err = 0.0;
+    for (int ez = 0; ez < NeZ; ++ez)
+      for (int k = 0; k < N1; ++k) {
+        const int l = ez * N1 + k;
+        const double dd = b[ez * n3 + 3 * k + 0], dm = b[ez * n3 + 3 * k + 1], dr = b[ez * n3 + 3 * k + 2];
+        w.P[VD][l] += dd;
+        w.P[VMZ][l] += dm;
+        w.P[VRT][l] += dr;
+        err = std::max(err, std::fabs(dd) / w.dh[l]);
+        err = std::max(err, std::fabs(dm) / (w.dh[l] * o.newton_cref));
+        err = std::max(err, std::fabs(dr) / w.rh[l]);
+      }
+    if (cp.max_iter == 1 || err <= cp.tol) { iters_used = it; break; }
+  }
+  // tend_im = (PROG - q)/impl_fac  (hevi.F90:931-942)
+  for (int v = 0; v < 5; ++v)
+    for (int l = 0; l < L; ++l) tend_out[v][l] = (w.P[v][l] - w.Q[v][l]) / impl_fac;
+  return iters_used;
+}
+
+// cal_vi over all columns; returns #non-converged columns; iters histogram optional
+static long cal_vi(const Oracle& o, const double* const q[5], const double* const q0[5], double impl_fac,
+                   double dt, int max_iter, double tol, double* const tend[5], int* col_iters) {
+  const int N1 = o.N1, NeZ = o.NeZ, L = NeZ * N1, n3 = 3 * N1;
+  const double rgamm = o.c.cvdry / o.c.cpdry;
+  const long ncol = (long)o.NeX * o.NeY * N1 * N1;
+  long nfail = 0;
+  ColumnParams cp{impl_fac, dt, tol, max_iter};
+#pragma omp parallel reduction(+ : nfail)
+  {
+    ColumnWork w;
+    for (int v = 0; v < 5; ++v) { w.P[v].resize(L); w.Q[v].resize(L); w.Z[v].resize(L); }
+    w.dh.resize(L); w.ph.resize(L); w.rh.resize(L);
+    w.alphB.resize(NeZ); w.alphT.resize(NeZ);
+    w.A3.resize(3 * L); w.b.resize(NeZ * n3); w.G.resize(NeZ * n3 * 3);
+    w.buv.resize(L * 2); w.Guv.resize(NeZ * N1);
+    w.W.resize(L); w.WT.resize(L); w.POT.resize(L); w.DPDRHOT.resize(L);
+    std::vector<double> tout[5];
+    for (int v = 0; v < 5; ++v) tout[v].resize(L);
+    double* tp[5];
+    for (int v = 0; v < 5; ++v) tp[v] = tout[v].data();
+    std::vector<size_t> gidx(L);
+#pragma omp for schedule(dynamic, 16)
+    for (long c = 0; c < ncol; ++c) {
+      const int ij = c % (N1 * N1);
+      const long exy = c / (N1 * N1);
+      const int i = ij % N1, j = ij / N1;
+      const int ex = exy % o.NeX, ey = exy / o.NeX;
+      for (int ez = 0; ez < NeZ; ++ez)
+        for (int k = 0; k < N1; ++k) gidx[ez * N1 + k] = o.eid(ex, ey, ez) * o.Np + o.nid(i, j, k);
+      for (int l = 0; l < L; ++l) {
+        const size_t g = gidx[l];
+        for (int v = 0; v < 5; ++v) { w.Q[v][l] = q[v][g]; w.Z[v][l] = q0[v][g]; }
+        w.dh[l] = o.dens_hyd[g];
+        w.ph[l] = o.pres_hyd[g];
+        w.rh[l] = o.c.pres00 / o.c.rdry * std::pow(w.ph[l] / o.c.pres00, rgamm);
+      }
+      const int its = column_solve(o, w, cp, tp, L);
+      if (its < 0) ++nfail;
+      if (col_iters) col_iters[c] = its;
+      for (int l = 0; l < L; ++l)
+        for (int v = 0; v < 5; ++v) tend[v][gidx[l]] = tout[v][l];
+    }
+  }
+  return nfail;
+}
+
+}  // namespace
+
+// =================================================================================
+// C API (ctypes)
+// =================================================================================
+extern "C" {
+
+typedef struct {
+  int porder;
+  int NeX, NeY, NeZ;
+  double xmin, xmax, ymin, ymax, zmin, zmax;
+  double grav, rdry, cpdry, cvdry, pres00;
+  double coriolis_f;
+  int filter_on;
+  double mf_etac, mf_alpha;
+  int mf_order;
+  double newton_cref;
+} orc_desc;
+
+void* orc_create(const orc_desc* d) {
+  if (!d || d->porder < 1 || d->porder > 15 || d->NeX < 1 || d->NeY < 1 || d->NeZ < 1) return nullptr;
+  Oracle* o = new Oracle();
+  o->c.grav = d->grav; o->c.rdry = d->rdry; o->c.cpdry = d->cpdry; o->c.cvdry = d->cvdry; o->c.pres00 = d->pres00;
+  o->e.init(d->porder, d->mf_etac, d->mf_alpha, d->mf_order);
+  o->N1 = d->porder + 1; o->Np = o->N1 * o->N1 * o->N1; o->Nfp = o->N1 * o->N1; o->NfpTot = 6 * o->Nfp;
+  o->NeX = d->NeX; o->NeY = d->NeY; o->NeZ = d->NeZ; o->Ne = d->NeX * d->NeY * d->NeZ;
+  o->xmin = d->xmin; o->xmax = d->xmax; o->ymin = d->ymin; o->ymax = d->ymax; o->zmin = d->zmin; o->zmax = d->zmax;
+  o->dx = (d->xmax - d->xmin) / d->NeX; o->dy = (d->ymax - d->ymin) / d->NeY; o->dz = (d->zmax - d->zmin) / d->NeZ;
+  o->coriolis_f = d->coriolis_f;
+  o->filter_on = d->filter_on;
+  o->newton_cref = d->newton_cref > 0 ? d->newton_cref : 340.0;
+  const size_t n = (size_t)o->Np * o->Ne;
+  o->dens_hyd.assign(n, 0.0); o->pres_hyd.assign(n, 0.0); o->therm_hyd.assign(n, 0.0);
+  return o;
+}
+
+void orc_destroy(void* h) { delete static_cast<Oracle*>(h); }
+
+int orc_num_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+void orc_set_num_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+
+// 1D operators: x, w (N1); D, Minv, F, T, V, invV (N1*N1 row-major)
+void orc_get_1d(void* h, double* x, double* w, double* D, double* Minv, double* F, double* T, double* V, double* invV) {
+  Oracle* o = static_cast<Oracle*>(h);
+  const int n = o->N1;
+  if (x) std::memcpy(x, o->e.x.data(), n * sizeof(double));
+  if (w) std::memcpy(w, o->e.w.data(), n * sizeof(double));
+  if (D) std::memcpy(D, o->e.D.data(), n * n * sizeof(double));
+  if (Minv) std::memcpy(Minv, o->e.Minv.data(), n * n * sizeof(double));
+  if (F) std::memcpy(F, o->e.F.data(), n * n * sizeof(double));
+  if (T) std::memcpy(T, o->e.T.data(), n * n * sizeof(double));
+  if (V) std::memcpy(V, o->e.V.data(), n * n * sizeof(double));
+  if (invV) std::memcpy(invV, o->e.invV.data(), n * n * sizeof(double));
+}
+
+// node coordinates (Np, Ne)
+void orc_node_coords(void* h, double* x, double* y, double* z) {
+  Oracle* o = static_cast<Oracle*>(h);
+  for (int ez = 0; ez < o->NeZ; ++ez)
+    for (int ey = 0; ey < o->NeY; ++ey)
+      for (int ex = 0; ex < o->NeX; ++ex) {
+        const size_t ke = o->eid(ex, ey, ez);
+        for (int k = 0; k < o->N1; ++k)
+          for (int j = 0; j < o->N1; ++j)
+            for (int i = 0; i < o->N1; ++i) {
+              const size_t g = ke * o->Np + o->nid(i, j, k);
+              if (x) x[g] = o->xmin + (ex + 0.5 * (o->e.x[i] + 1.0)) * o->dx;
+              if (y) y[g] = o->ymin + (ey + 0.5 * (o->e.x[j] + 1.0)) * o->dy;
+              if (z) z[g] = o->zmin + (ez + 0.5 * (o->e.x[k] + 1.0)) * o->dz;
+            }
+      }
+}
+
+// base state (Np, Ne): DENS_hyd, PRES_hyd; THERM_hyd = P00/Rd (PRES_hyd/P00)^(cv/cp)
+void orc_set_base_state(void* h, const double* dens_hyd, const double* pres_hyd) {
+  Oracle* o = static_cast<Oracle*>(h);
+  const size_t n = (size_t)o->Np * o->Ne;
+  const double rgamm = o->c.cvdry / o->c.cpdry;
+  for (size_t p = 0; p < n; ++p) {
+    o->dens_hyd[p] = dens_hyd[p];
+    o->pres_hyd[p] = pres_hyd[p];
+    o->therm_hyd[p] = o->c.pres00 / o->c.rdry * std::pow(pres_hyd[p] / o->c.pres00, rgamm);
+  }
+}
+
+void orc_get_therm_hyd(void* h, double* out) {
+  Oracle* o = static_cast<Oracle*>(h);
+  std::memcpy(out, o->therm_hyd.data(), o->therm_hyd.size() * sizeof(double));
+}
+
+void orc_drhot2pres(void* h, const double* drhot, double* pres, double* dpres) {
+  drhot2pres(*static_cast<Oracle*>(h), drhot, pres, dpres);
+}
+
+// q = {DDENS, MOMX, MOMY, MOMZ, DRHOT}; dpres may be NULL (computed here)
+void orc_cal_tend(void* h, int hevi, const double* const* q, const double* dpres, double* const* tend) {
+  Oracle* o = static_cast<Oracle*>(h);
+  std::vector<double> dp;
+  if (!dpres) { dp.resize((size_t)o->Np * o->Ne); drhot2pres(*o, q[VRT], nullptr, dp.data()); dpres = dp.data(); }
+  cal_tend(*o, hevi, q, dpres, tend);
+}
+
+long orc_cal_vi(void* h, const double* const* q, const double* const* q0, double impl_fac, double dt,
+                int max_iter, double tol, double* const* tend, int* col_iters) {
+  return cal_vi(*static_cast<Oracle*>(h), q, q0, impl_fac, dt, max_iter, tol, tend, col_iters);
+}
+
+void orc_modalfilter(void* h, double* const* q) { modal_filter(*static_cast<Oracle*>(h), q); }
+
+// HEVE + SSP-RK3 (ERK_SSP_3s3o), modal filter after each step if enabled
+void orc_step_heve(void* h, double* const* q, double dt, int nsteps) {
+  Oracle* o = static_cast<Oracle*>(h);
+  const size_t n = (size_t)o->Np * o->Ne;
+  std::vector<double> q0[5], tmp[5], t[5], dp(n);
+  for (int v = 0; v < 5; ++v) { q0[v].resize(n); tmp[v].resize(n); t[v].resize(n); }
+  double* tp[5]; for (int v = 0; v < 5; ++v) tp[v] = t[v].data();
+  for (int s = 0; s < nsteps; ++s) {
+    for (int v = 0; v < 5; ++v) std::memcpy(q0[v].data(), q[v], n * sizeof(double));
+    for (int st = 1; st <= 3; ++st) {
+      drhot2pres(*o, q[VRT], nullptr, dp.data());
+      cal_tend(*o, 0, q, dp.data(), tp);
+      for (int v = 0; v < 5; ++v) {
+        double* x = q[v]; const double* x0 = q0[v].data(); double* vt = tmp[v].data(); const double* tt = t[v].data();
+#pragma omp parallel for
+        for (size_t p = 0; p < n; ++p) {
+          if (st == 1) { vt[p] = x0[p] / 3.0; x[p] = x[p] + dt * tt[p]; }
+          else if (st == 2) { x[p] = 0.75 * x0[p] + 0.25 * x[p] + 0.25 * dt * tt[p]; }
+          else { x[p] = vt[p] + (2.0 / 3.0) * x[p] + (2.0 / 3.0) * dt * tt[p]; }
+        }
+      }
+    }
+    if (o->filter_on) modal_filter(*o, q);
+  }
+}
+
+// HEVI + IMEX ARK(2,3,2); returns #non-converged column solves; iteration stats optional
+long orc_step_hevi(void* h, double* const* q, double dt, int nsteps, int max_iter, double tol, double* mean_iters) {
+  Oracle* o = static_cast<Oracle*>(h);
+  const size_t n = (size_t)o->Np * o->Ne;
+  const double alp = (3.0 + 2.0 * std::sqrt(2.0)) / 6.0, gam = 1.0 - 1.0 / std::sqrt(2.0), del = 1.0 / (2.0 * std::sqrt(2.0));
+  const double aex[4][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}, {0, 2 * gam, 0, 0}, {0, 1 - alp, alp, 0}};
+  const double aim[4][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}, {0, gam, gam, 0}, {0, del, del, gam}};
+  const double bb[4] = {0, del, del, gam};
+  std::vector<double> var0[5], vtmp[5], tex[4][5], tim[4][5], dp(n);
+  for (int v = 0; v < 5; ++v) {
+    var0[v].resize(n); vtmp[v].resize(n);
+    for (int s = 1; s <= 3; ++s) { tex[s][v].resize(n); tim[s][v].resize(n); }
+  }
+  const long ncol = (long)o->NeX * o->NeY * o->N1 * o->N1;
+  std::vector<int> its(ncol);
+  long nfail = 0; double itsum = 0; long itcnt = 0;
+  for (int step = 0; step < nsteps; ++step) {
+    for (int v = 0; v < 5; ++v) std::memcpy(var0[v].data(), q[v], n * sizeof(double));  // StoreVar0
+    for (int st = 1; st <= 3; ++st) {
+      const double impl_fac = aim[st][st] * dt;
+      const double* qc[5]; const double* z0[5]; double* tip[5]; double* tep[5];
+      for (int v = 0; v < 5; ++v) { qc[v] = q[v]; z0[v] = var0[v].data(); tip[v] = tim[st][v].data(); tep[v] = tex[st][v].data(); }
+      nfail += cal_vi(*o, qc, z0, impl_fac, dt, max_iter, tol, tip, its.data());
+      if (impl_fac != 0.0) { for (long c = 0; c < ncol; ++c) if (its[c] > 0) { itsum += its[c]; ++itcnt; } }
+      for (int v = 0; v < 5; ++v) {  // StoreImplicit (timeint_rk.F90:2510-2565)
+        double* x = q[v];
+        if (st == 1) { std::memcpy(var0[v].data(), x, n * sizeof(double)); std::memcpy(vtmp[v].data(), x, n * sizeof(double)); }
+        const double* ti = tim[st][v].data();
+#pragma omp parallel for
+        for (size_t p = 0; p < n; ++p) x[p] = x[p] + impl_fac * ti[p];
+      }
+      drhot2pres(*o, q[VRT], nullptr, dp.data());
+      cal_tend(*o, 1, q, dp.data(), tep);
+      for (int v = 0; v < 5; ++v) {  // Advance (rk_advance_general2D, timeint_rk.F90:2201-2360)
+        double* x = q[v]; double* vt = vtmp[v].data(); const double* x0 = var0[v].data();
+        const double* te = tex[st][v].data(); const double* ti = tim[st][v].data();
+        if (st == 3) {
+#pragma omp parallel for
+          for (size_t p = 0; p < n; ++p) x[p] = vt[p] + bb[3] * dt * te[p] + bb[3] * dt * ti[p];
+        } else {
+#pragma omp parallel for
+          for (size_t p = 0; p < n; ++p) {
+            vt[p] = vt[p] + bb[st] * dt * te[p] + bb[st] * dt * ti[p];
+            double s = x0[p];
+            for (int j = 1; j <= st; ++j) s = s + aex[st + 1][j] * dt * tex[j][v][p] + aim[st + 1][j] * dt * tim[j][v][p];
+            x[p] = s;
+          }
+        }
+      }
+    }
+    if (o->filter_on) modal_filter(*o, q);
+  }
+  if (mean_iters) *mean_iters = itcnt ? itsum / itcnt : 0.0;
+  return nfail;
+}
+
+}  // extern "C"

@@ -1,0 +1,193 @@
+"""ctypes wrapper of the FP64 CPU oracle (``fedg_oracle.cpp``).
+
+Test infrastructure only: the checker used by ``tests/``, ``__graft_entry__.smoke()``
+and the ``cpu_baseline`` leg of ``bench.py``.  The product path never imports this.
+
+Every routine follows FElib (ywkawai/FE-Project); the per-function citations are in
+``fedg_oracle.cpp``.  Fields are numpy float64 arrays of shape ``(Ne, Np)`` in C order,
+which is the same memory as FElib's column-major ``(Np, Ne)``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libfedg_oracle.so")
+_lib = None
+
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+class OrcDesc(ctypes.Structure):
+    _fields_ = [
+        ("porder", ctypes.c_int),
+        ("NeX", ctypes.c_int), ("NeY", ctypes.c_int), ("NeZ", ctypes.c_int),
+        ("xmin", ctypes.c_double), ("xmax", ctypes.c_double),
+        ("ymin", ctypes.c_double), ("ymax", ctypes.c_double),
+        ("zmin", ctypes.c_double), ("zmax", ctypes.c_double),
+        ("grav", ctypes.c_double), ("rdry", ctypes.c_double), ("cpdry", ctypes.c_double),
+        ("cvdry", ctypes.c_double), ("pres00", ctypes.c_double),
+        ("coriolis_f", ctypes.c_double),
+        ("filter_on", ctypes.c_int),
+        ("mf_etac", ctypes.c_double), ("mf_alpha", ctypes.c_double), ("mf_order", ctypes.c_int),
+        ("newton_cref", ctypes.c_double),
+    ]
+
+
+def build() -> str:
+    """Compile the oracle with its Makefile (gcc + OpenMP); returns the .so path."""
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def _load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(
+        os.path.join(_HERE, "fedg_oracle.cpp")
+    ):
+        build()
+    lib = ctypes.CDLL(_LIB_PATH)
+    lib.orc_create.restype = ctypes.c_void_p
+    lib.orc_create.argtypes = [ctypes.POINTER(OrcDesc)]
+    lib.orc_destroy.argtypes = [ctypes.c_void_p]
+    lib.orc_num_threads.restype = ctypes.c_int
+    lib.orc_set_num_threads.argtypes = [ctypes.c_int]
+    lib.orc_get_1d.argtypes = [ctypes.c_void_p] + [_dp] * 8
+    lib.orc_node_coords.argtypes = [ctypes.c_void_p, _dp, _dp, _dp]
+    lib.orc_set_base_state.argtypes = [ctypes.c_void_p, _dp, _dp]
+    lib.orc_get_therm_hyd.argtypes = [ctypes.c_void_p, _dp]
+    lib.orc_drhot2pres.argtypes = [ctypes.c_void_p, _dp, _dp, _dp]
+    pp = ctypes.POINTER(_dp)
+    lib.orc_cal_tend.argtypes = [ctypes.c_void_p, ctypes.c_int, pp, _dp, pp]
+    lib.orc_cal_vi.restype = ctypes.c_long
+    lib.orc_cal_vi.argtypes = [ctypes.c_void_p, pp, pp, ctypes.c_double, ctypes.c_double,
+                               ctypes.c_int, ctypes.c_double, pp, ctypes.POINTER(ctypes.c_int)]
+    lib.orc_modalfilter.argtypes = [ctypes.c_void_p, pp]
+    lib.orc_step_heve.argtypes = [ctypes.c_void_p, pp, ctypes.c_double, ctypes.c_int]
+    lib.orc_step_hevi.restype = ctypes.c_long
+    lib.orc_step_hevi.argtypes = [ctypes.c_void_p, pp, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                  ctypes.c_double, _dp]
+    _lib = lib
+    return lib
+
+
+def _ptr(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(_dp)
+
+
+def _pp(arrs):
+    arr = (_dp * len(arrs))(*[_ptr(a) for a in arrs])
+    return ctypes.cast(arr, ctypes.POINTER(_dp)), arrs
+
+
+def set_num_threads(n: int) -> None:
+    _load().orc_set_num_threads(int(n))
+
+
+def num_threads() -> int:
+    return int(_load().orc_num_threads())
+
+
+class Oracle:
+    """FP64 CPU restatement of FElib's nonhydro3d HEVE/HEVI dynamics on a flat cube domain."""
+
+    def __init__(self, porder, NeX, NeY, NeZ, dom, *, grav=9.80616, rdry=287.04, cpdry=1004.64,
+                 cvdry=717.6, pres00=1.0e5, coriolis_f=0.0, filter_on=True, mf_etac=2.0 / 3.0,
+                 mf_alpha=36.0, mf_order=16, newton_cref=340.0):
+        lib = _load()
+        xmin, xmax, ymin, ymax, zmin, zmax = dom
+        d = OrcDesc(porder, NeX, NeY, NeZ, xmin, xmax, ymin, ymax, zmin, zmax, grav, rdry, cpdry,
+                    cvdry, pres00, coriolis_f, int(filter_on), mf_etac, mf_alpha, mf_order, newton_cref)
+        self._h = lib.orc_create(ctypes.byref(d))
+        if not self._h:
+            raise ValueError("oracle: invalid descriptor")
+        self.lib = lib
+        self.N1 = porder + 1
+        self.Np = self.N1 ** 3
+        self.Ne = NeX * NeY * NeZ
+        self.shape = (self.Ne, self.Np)
+        self.NeX, self.NeY, self.NeZ = NeX, NeY, NeZ
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            self.lib.orc_destroy(h)
+            self._h = None
+
+    def operators_1d(self):
+        n = self.N1
+        x, w = np.zeros(n), np.zeros(n)
+        D, Mi, F, T, V, iV = (np.zeros((n, n)) for _ in range(6))
+        self.lib.orc_get_1d(self._h, _ptr(x), _ptr(w), _ptr(D), _ptr(Mi), _ptr(F), _ptr(T), _ptr(V), _ptr(iV))
+        return dict(x=x, w=w, D=D, Minv=Mi, F=F, T=T, V=V, invV=iV)
+
+    def coords(self):
+        x, y, z = (np.zeros(self.shape) for _ in range(3))
+        self.lib.orc_node_coords(self._h, _ptr(x), _ptr(y), _ptr(z))
+        return x, y, z
+
+    def set_base_state(self, dens_hyd, pres_hyd):
+        self.lib.orc_set_base_state(self._h, _ptr(np.ascontiguousarray(dens_hyd, np.float64)),
+                                    _ptr(np.ascontiguousarray(pres_hyd, np.float64)))
+
+    def therm_hyd(self):
+        out = np.zeros(self.shape)
+        self.lib.orc_get_therm_hyd(self._h, _ptr(out))
+        return out
+
+    def drhot2pres(self, drhot):
+        pres, dpres = np.zeros(self.shape), np.zeros(self.shape)
+        self.lib.orc_drhot2pres(self._h, _ptr(np.ascontiguousarray(drhot)), _ptr(pres), _ptr(dpres))
+        return pres, dpres
+
+    def cal_tend(self, q, hevi, dpres=None):
+        """q: list of 5 arrays (DDENS, MOMX, MOMY, MOMZ, DRHOT) -> 5 tendencies."""
+        qs = [np.ascontiguousarray(a, np.float64) for a in q]
+        out = [np.zeros(self.shape) for _ in range(5)]
+        pq, _k1 = _pp(qs)
+        po, _k2 = _pp(out)
+        dp = _ptr(np.ascontiguousarray(dpres, np.float64)) if dpres is not None else None
+        self.lib.orc_cal_tend(self._h, int(hevi), pq, dp, po)
+        return out
+
+    def cal_vi(self, q, q0, impl_fac, dt, max_iter=1, tol=0.0, want_iters=False):
+        qs = [np.ascontiguousarray(a, np.float64) for a in q]
+        q0s = [np.ascontiguousarray(a, np.float64) for a in q0]
+        out = [np.zeros(self.shape) for _ in range(5)]
+        ncol = self.NeX * self.NeY * self.N1 * self.N1
+        its = np.zeros(ncol, np.int32)
+        pq, _k1 = _pp(qs)
+        pz, _k2 = _pp(q0s)
+        po, _k3 = _pp(out)
+        nfail = self.lib.orc_cal_vi(self._h, pq, pz, float(impl_fac), float(dt), int(max_iter), float(tol), po,
+                                    its.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+        if want_iters:
+            return out, int(nfail), its
+        return out
+
+    def modalfilter(self, q):
+        qs = [np.ascontiguousarray(a, np.float64).copy() for a in q]
+        pq, _k = _pp(qs)
+        self.lib.orc_modalfilter(self._h, pq)
+        return qs
+
+    def step_heve(self, q, dt, nsteps):
+        qs = [np.ascontiguousarray(a, np.float64).copy() for a in q]
+        pq, _k = _pp(qs)
+        self.lib.orc_step_heve(self._h, pq, float(dt), int(nsteps))
+        return qs
+
+    def step_hevi(self, q, dt, nsteps, max_iter=1, tol=0.0):
+        qs = [np.ascontiguousarray(a, np.float64).copy() for a in q]
+        pq, _k = _pp(qs)
+        mi = ctypes.c_double(0.0)
+        nfail = self.lib.orc_step_hevi(self._h, pq, float(dt), int(nsteps), int(max_iter), float(tol),
+                                       ctypes.byref(mi))
+        return qs, int(nfail), float(mi.value)
