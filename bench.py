@@ -1,0 +1,326 @@
+#!/usr/bin/env python
+"""Benchmark of the SCALE-DG nonhydrostatic 3D DG dynamics step on one GB300.
+
+Workload (default): p=7, 128x128x16 elements over 12.8 x 12.8 x 3.2 km, periodic in x/y,
+slip lids, constant Brunt-Vaisala base state (N = 0.01 1/s, theta_sfc = 300 K), i.i.d.
++-0.1 K potential-temperature noise below 500 m (seed 0), u = 5 m/s, HEVI with IMEX
+ARK(2,3,2) and the column Newton solve to tol 1e-10.  134,217,728 nodes x 5 variables.
+
+A "step" is one full time step (3 RK stages) of the whole domain; the metric is
+DOF-stage updates per second = 5 * Np * Ne * 3 * steps / time.
+
+  python bench.py [--steps K] [--warmup W] [--path mixed|fp64] [--impl fedg|reference]
+
+--impl reference times the CPU implementation of the same step (the FP64 oracle port of
+FElib's routines, all host cores) on a bounded sample of the workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for p in (os.path.join(ROOT, "fe-project_gb300"), os.path.join(ROOT, "oracle")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+METRIC = "DOF-stage/s on 1 GB300: learned+FP32 vs plain FP64 HEVI, rel L2 err <=1e-6"
+UNIT = "DOF-stage/s"
+DT_STABLE = 0.005  # C5 geometry (h = 100 m, p = 7): the oracle is stable at 0.005 s, not at 0.01 s
+
+
+def _env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(
+        os.environ.get("LOCAL_RANK", "0"))
+
+
+# ----------------------------------------------------------------------------------------
+# clocks during the timed region
+# ----------------------------------------------------------------------------------------
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+# ----------------------------------------------------------------------------------------
+# CPU leg: the FP64 oracle on a bounded sample of the workload
+# ----------------------------------------------------------------------------------------
+def cpu_sample(path_kind, seconds_target=15.0):
+    """Times the oracle's HEVI ARK232 step on an 8x8x16-element sample of the C5 workload
+    (same p, same column depth, same base state and noise); returns DOF-stage/s."""
+    import oracle as orc
+    from fedg import cases
+
+    case = cases.C5().scaled(8, 8, 16)
+    q, b = cases.initial_state(case)
+    o = orc.Oracle(case.porder, case.NeX, case.NeY, case.NeZ, case.dom)
+    o.set_base_state(b["dens_hyd"], b["pres_hyd"])
+    threads = orc.num_threads()
+    max_iter, tol = (20, 1e-10)
+    t0 = time.perf_counter()
+    o.step_hevi(q, DT_STABLE, 1, max_iter=max_iter, tol=tol)
+    t1 = time.perf_counter()
+    nsteps = max(1, int(seconds_target / max(t1 - t0, 1e-3)))
+    nsteps = min(nsteps, 20)
+    t2 = time.perf_counter()
+    o.step_hevi(q, DT_STABLE, nsteps, max_iter=max_iter, tol=tol)
+    t3 = time.perf_counter()
+    value = case.dofs * 3 * nsteps / (t3 - t2)
+    return {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"FP64 oracle (C++/OpenMP restatement of FElib), HEVI ARK232 Newton tol 1e-10, "
+                      f"{nsteps} steps of an 8x8x16-element p=7 sample of the 128x128x16 workload "
+                      f"({case.dofs} DOF), {t3 - t2:.1f} s"}
+
+
+# ----------------------------------------------------------------------------------------
+def run_reference(args):
+    rank, world, _ = _env_rank()
+    if rank != 0:
+        return 0
+    cb = cpu_sample("reference", seconds_target=max(5.0, 10.0 * max(args.steps, 1) / 5.0))
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "C5 p=7 128x128x16 HEVI IMEX-ARK232 (8x8x16-element sample on the host cores)",
+                       "dt": DT_STABLE},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def fp64_dgemm_tflops(torch, dev):
+    """Measured FP64 matrix throughput (cuBLAS DGEMM 4096^3, best of 3) -- the FP64 roofline."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device=dev)
+    b = torch.randn(n, n, dtype=torch.float64, device=dev)
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, b
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def run_fedg(args):
+    import numpy as np
+    import torch
+
+    import __graft_entry__ as ge
+    rank, world, local = _env_rank()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    if rank == 0:
+        ge.build()
+    if world > 1:
+        dist.barrier()
+    from fedg import cases
+    from fedg import lib as fl
+
+    case = cases.C5()
+    if args.small:
+        case = case.scaled(32, 32, 16)
+    path = args.path
+    prec = fl.PREC_MIXED if path == "mixed" else fl.PREC_FP64
+    q, b = cases.initial_state(case)
+    ctx = fl.Context(case, device=local)
+    ctx.set_base_state(b["dens_hyd"], b["pres_hyd"], b["therm_hyd"])
+    dens_norm = float(np.linalg.norm(b["dens_hyd"]))
+    therm_norm = float(np.linalg.norm(b["therm_hyd"]))
+    del b
+    qd = [ctx.tensor(a) for a in q]
+    q_host = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in q]
+    del q
+    stream = torch.cuda.ExternalStream(ctx.stream_handle)
+    opts = dict(prec=prec, dt=DT_STABLE, max_iter=20, tol=1e-10, use_guess=(path == "mixed" and args.guess))
+
+    # warm-up
+    nfail_w, its_w = ctx.update(qd, args.warmup, **opts)
+    # timed region: K steps of the whole domain, inputs (5.4 GB state) larger than L2
+    fl.prof_reset(ctx)
+    fl.prof_enable(ctx, True)
+    clk = Clocks(local)
+    clk.start()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    nfail, its = ctx.update(qd, args.steps, sync=False, **opts)
+    e1.record(stream)
+    ctx.sync()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    clocks = clk.stop()
+    fl.prof_enable(ctx, False)
+    prof = fl.prof_read(ctx)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    dofs_stage = case.dofs * 3
+    value = dofs_stage * args.steps / (ms * 1e-3) * world
+
+    # dominant kernel and its roofline
+    peaks, peak_src = measured_peaks()
+    kname = max(prof, key=lambda k: prof[k][0])
+    ktime, klaunch = prof[kname]
+    nodes = case.Np * case.Ne
+    # algorithmic bytes per node per launch (one read/write of each array element)
+    bytes_per_node = {
+        "vi_fp64": 8 * (5 + 5 + 5),          # q*, var0 in; tend_im out
+        "tend_fp64": 8 * (6 + 5),            # 5 fields + DPRES in; 5 tendencies out
+        "rk": 8 * 20,                        # general IMEX advance (upper bound of the stage kinds)
+        "stage_mixed": 0, "vi_mixed": 0, "filter": 8 * 10, "drhot2pres": 8 * 2, "mlp": 0, "aux": 0,
+    }
+    try:
+        from fedg import mixed_bytes
+        bytes_per_node.update(mixed_bytes.BYTES_PER_NODE)
+    except Exception:
+        pass
+    avg_ms = ktime / max(klaunch, 1)
+    achieved = bytes_per_node.get(kname, 0) * nodes / (avg_ms * 1e-3) / 1e9 if avg_ms > 0 else 0.0
+    roof = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peaks.get("hbm_gbs", 6800.0),
+            "unit": "GB/s", "frac": achieved / peaks.get("hbm_gbs", 6800.0), "traffic": None,
+            "peak_source": peak_src, "avg_launch_ms": avg_ms, "algorithmic_bytes_per_node": bytes_per_node.get(kname)}
+    fp64_tf = fp64_dgemm_tflops(torch, ctx.dev) if rank == 0 else 0.0
+    gpu_launches = sum(v[1] for v in prof.values())
+
+    # end to end through the public API with host buffers: H2D of the state, one step, D2H
+    e2e = None
+    if rank == 0 and not args.no_e2e:
+        ke = max(1, min(args.steps, 2))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            for dst, src in zip(qd, q_host):
+                dst.copy_(src, non_blocking=True)
+            torch.cuda.synchronize()
+            ctx.update(qd, 1, sync=False, **opts)
+            ctx.sync()
+            for dst, src in zip(q_host, qd):
+                dst.copy_(src, non_blocking=True)
+            torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        nb = sum(t.numel() * 8 for t in qd)
+        e2e = {"value": dofs_stage * ke / (t1 - t0), "unit": UNIT, "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb,
+               "steps": ke}
+
+    cb = None
+    if rank == 0 and not args.no_cpu:
+        cb = cpu_sample(path)
+
+    finite = all(bool(torch.isfinite(t).all().item()) for t in qd)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if prec == fl.PREC_FP64 else "f32+f64", "data": "synthetic",
+            "config": {"workload": f"{case.name}: p=7 {case.NeX}x{case.NeY}x{case.NeZ} elements, HEVI IMEX-ARK232, "
+                                   f"constBVFreq N=0.01, +-0.1K noise below 500 m, u=5 m/s",
+                       "path": "plain_fp64" if prec == fl.PREC_FP64 else ("learned+fp32" if opts["use_guess"] else "fp32"),
+                       "dt": DT_STABLE, "dt_baseline": 0.5, "newton_tol": opts["tol"], "newton_max_iter": opts["max_iter"],
+                       "mean_newton_solves": its, "nonconverged_columns": nfail, "finite": finite,
+                       "l2": "inputs larger than L2 (FP64 state %.1f GB)" % (case.dofs * 8 / 1e9),
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "roofline": roof,
+            "roofline_fp64": {"bound": "fp64", "peak_tflops": fp64_tf, "peak_source": "measured cuBLAS DGEMM 4096^3"},
+            "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items() if v[1]},
+            "cpu_baseline": cb, "e2e": e2e, "gpu_launches": gpu_launches, "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["fedg", "reference"], default="fedg")
+    ap.add_argument("--path", choices=["mixed", "fp64"], default=os.environ.get("FEDG_BENCH_PATH", "fp64"))
+    ap.add_argument("--guess", type=int, default=1)
+    ap.add_argument("--small", action="store_true", help="32x32x16 elements instead of 128x128x16 (profiling)")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_fedg(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

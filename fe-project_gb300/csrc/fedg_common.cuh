@@ -1,0 +1,60 @@
+// fedg_common.cuh -- shared definitions of the GB300 SCALE-DG dynamics kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#define FEDG_MAXN1 8
+
+namespace fedg {
+
+enum { VD = 0, VMX = 1, VMY = 2, VMZ = 3, VRT = 4 };  // cal_tend_ex argument order
+
+// Everything a kernel needs about the element and the mesh, passed by value (it lands in the
+// kernel-parameter constant bank, so every thread of a warp reads the same word: broadcast).
+struct Ops {
+  double D[FEDG_MAXN1 * FEDG_MAXN1];  // D1D(i,l) = l_l'(x_i), row-major [i*N1+l]
+  double F[FEDG_MAXN1 * FEDG_MAXN1];  // modal filter (h == v parameters by default)
+  double Fv[FEDG_MAXN1 * FEDG_MAXN1]; // vertical modal filter
+  double T[FEDG_MAXN1 * FEDG_MAXN1];  // VPOrdM1 truncation
+  double Lb[FEDG_MAXN1];              // Lift coefficient from the -1 face: Minv(k,0)
+  double Lt[FEDG_MAXN1];              // Lift coefficient from the +1 face: Minv(k,N)
+  double E11, E22, E33;               // Escale of the flat cube
+  double FSx, FSy, FSz;               // Fscale per face orientation
+  double grav, rdry, cpdry, cvdry, pres00;
+  double kap;    // cp/cv
+  double rgamm;  // cv/cp
+  double coriolis_f;
+  int NeX, NeY, NeZ;
+  int N1, Np, L;  // L = NeZ*N1 levels
+};
+
+// column profiles of the horizontally homogeneous base state, [L] each
+struct Prof {
+  const double* dens;   // DENS_hyd
+  const double* pres;   // PRES_hyd
+  const double* therm;  // THERM_hyd (cal_tend_ex)
+  const double* rhyd;   // P00/Rd (PRES_hyd/P00)^(cv/cp) (cal_vi recomputes it, hevi_common_2.F90:236-237)
+};
+
+__host__ __device__ inline int face_opp(int f) { return f ^ ((f < 4) ? 2 : 1); }
+
+template <int N1>
+__device__ __forceinline__ void face_node(int f, int a, int b, int& i, int& j, int& k) {
+  constexpr int N = N1 - 1;
+  switch (f) {
+    case 0: i = a; j = 0; k = b; break;   // y-
+    case 1: i = N; j = a; k = b; break;   // x+
+    case 2: i = a; j = N; k = b; break;   // y+
+    case 3: i = 0; j = a; k = b; break;   // x-
+    case 4: i = a; j = b; k = 0; break;   // z-
+    default: i = a; j = b; k = N; break;  // z+
+  }
+}
+
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+}  // namespace fedg

@@ -1,0 +1,312 @@
+"""ctypes binding of ``libfedg.so`` (the C ABI declared in ``include/fedg.h``).
+
+This is the host-side mirror of FElib's operator interface for the dynamics hot path:
+``cal_tend_ex`` / ``cal_vi`` (FElib/src/fluid_dyn_solver/scale_atm_dyn_dgm_driver_nonhydro3d.F90:
+152-250), the ``timeint_rk`` stage methods (FElib/src/common/scale_timeint_rk.F90:81-104) and
+the driver's ``update`` loop (:614-963).  Device memory is held in torch CUDA tensors; the
+library only sees raw device pointers.  There is no CPU fallback: constructing a
+:class:`Context` without the compiled library or without a GPU raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+PKG_ROOT = os.path.dirname(_HERE)
+LIB_PATH = os.path.join(PKG_ROOT, "_build", "libfedg.so")
+
+HEVE, HEVI = 0, 1
+SSP_RK3, IMEX_ARK232 = 0, 1
+PREC_FP64, PREC_MIXED = 0, 1
+
+EXPORTED = [
+    "fedg_last_error", "fedg_ctx_create", "fedg_ctx_destroy", "fedg_ctx_stream", "fedg_synchronize",
+    "fedg_set_base_state", "fedg_drhot2pres", "fedg_cal_tend_ex", "fedg_cal_vi", "fedg_modalfilter",
+    "fedg_tint_create", "fedg_tint_destroy", "fedg_tint_nstage", "fedg_tint_implicit_diagfac",
+    "fedg_tint_tend_ex", "fedg_tint_tend_im", "fedg_tint_var0", "fedg_tint_store_var0",
+    "fedg_tint_store_implicit", "fedg_tint_advance", "fedg_update",
+    "fedg_prof_enable", "fedg_prof_reset", "fedg_prof_read",
+]
+
+# kernel classes of fedg_prof_read (include/fedg.h)
+K_TEND, K_VI, K_RK, K_FILTER, K_PRES, K_MTEND, K_MVI, K_MLP, K_AUX, K_COUNT = range(10)
+KERNEL_NAMES = ["tend_fp64", "vi_fp64", "rk", "filter", "drhot2pres", "stage_mixed", "vi_mixed", "mlp", "aux"]
+
+
+class MeshDesc(ctypes.Structure):
+    _fields_ = [
+        ("porder", ctypes.c_int),
+        ("NeX", ctypes.c_int), ("NeY", ctypes.c_int), ("NeZ", ctypes.c_int),
+        ("xmin", ctypes.c_double), ("xmax", ctypes.c_double),
+        ("ymin", ctypes.c_double), ("ymax", ctypes.c_double),
+        ("zmin", ctypes.c_double), ("zmax", ctypes.c_double),
+        ("periodic_x", ctypes.c_int), ("periodic_y", ctypes.c_int),
+        ("grav", ctypes.c_double), ("rdry", ctypes.c_double), ("cpdry", ctypes.c_double),
+        ("cvdry", ctypes.c_double), ("pres00", ctypes.c_double),
+        ("mf_on", ctypes.c_int),
+        ("mf_etac_h", ctypes.c_double), ("mf_alpha_h", ctypes.c_double), ("mf_order_h", ctypes.c_int),
+        ("mf_etac_v", ctypes.c_double), ("mf_alpha_v", ctypes.c_double), ("mf_order_v", ctypes.c_int),
+        ("device", ctypes.c_int),
+    ]
+
+
+class UpdateOpts(ctypes.Structure):
+    _fields_ = [("eqs", ctypes.c_int), ("prec", ctypes.c_int), ("max_iter", ctypes.c_int),
+                ("use_guess", ctypes.c_int), ("dt", ctypes.c_double), ("tol", ctypes.c_double)]
+
+
+_lib = None
+_vp = ctypes.c_void_p
+_P5 = ctypes.c_void_p * 5
+
+
+def load():
+    """Load libfedg.so; raises if it has not been built (no silent fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"libfedg.so not built ({LIB_PATH}); run __graft_entry__.build()")
+    lib = ctypes.CDLL(LIB_PATH)
+    lib.fedg_last_error.restype = ctypes.c_char_p
+    lib.fedg_ctx_create.argtypes = [ctypes.POINTER(MeshDesc), ctypes.POINTER(_vp)]
+    lib.fedg_ctx_destroy.argtypes = [_vp]
+    lib.fedg_ctx_stream.restype = _vp
+    lib.fedg_ctx_stream.argtypes = [_vp]
+    lib.fedg_synchronize.argtypes = [_vp]
+    lib.fedg_set_base_state.argtypes = [_vp] + [_vp] * 9
+    lib.fedg_drhot2pres.argtypes = [_vp, _vp, _vp, _vp]
+    lib.fedg_cal_tend_ex.argtypes = [_vp, ctypes.c_void_p * 16, _P5, ctypes.c_int]
+    lib.fedg_cal_vi.argtypes = [_vp, ctypes.c_void_p * 12, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                ctypes.c_double, _P5, _vp]
+    lib.fedg_modalfilter.argtypes = [_vp, _P5]
+    lib.fedg_tint_create.argtypes = [_vp, ctypes.c_int, ctypes.c_double, ctypes.POINTER(_vp)]
+    lib.fedg_tint_destroy.argtypes = [_vp]
+    lib.fedg_tint_nstage.argtypes = [_vp]
+    lib.fedg_tint_implicit_diagfac.restype = ctypes.c_double
+    lib.fedg_tint_implicit_diagfac.argtypes = [_vp, ctypes.c_int]
+    for nm in ("fedg_tint_tend_ex", "fedg_tint_tend_im"):
+        getattr(lib, nm).restype = _vp
+        getattr(lib, nm).argtypes = [_vp, ctypes.c_int, ctypes.c_int]
+    lib.fedg_tint_var0.restype = _vp
+    lib.fedg_tint_var0.argtypes = [_vp, ctypes.c_int]
+    lib.fedg_tint_store_var0.argtypes = [_vp, _P5]
+    lib.fedg_tint_store_implicit.argtypes = [_vp, ctypes.c_int, _P5]
+    lib.fedg_tint_advance.argtypes = [_vp, ctypes.c_int, _P5]
+    lib.fedg_update.argtypes = [_vp, _P5, ctypes.c_int, ctypes.POINTER(UpdateOpts), ctypes.POINTER(ctypes.c_double)]
+    lib.fedg_prof_enable.argtypes = [_vp, ctypes.c_int]
+    lib.fedg_prof_reset.argtypes = [_vp]
+    lib.fedg_prof_read.argtypes = [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                   ctypes.POINTER(ctypes.c_longlong)]
+    _lib = lib
+    return lib
+
+
+def last_error() -> str:
+    return load().fedg_last_error().decode()
+
+
+class FedgError(RuntimeError):
+    pass
+
+
+def _check(rc: int, what: str) -> int:
+    if rc < 0:
+        raise FedgError(f"{what} failed ({rc}): {last_error()}")
+    return rc
+
+
+def _ptr(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def _p5(ts):
+    return _P5(*[t.data_ptr() for t in ts])
+
+
+class Context:
+    """One fedg context (mesh, operators, base state, CUDA stream) on one GPU."""
+
+    def __init__(self, case, device: int = 0, filter_on=None):
+        import torch
+
+        if not torch.cuda.is_available():
+            raise RuntimeError("fedg: no CUDA device (the library has no CPU fallback)")
+        self.lib = load()
+        self.case = case
+        self.torch = torch
+        self.dev = torch.device("cuda", device)
+        xmin, xmax, ymin, ymax, zmin, zmax = case.dom
+        from .cases import CPDRY, CVDRY, GRAV, PRES00, RDRY
+
+        fo = case.filter_on if filter_on is None else filter_on
+        d = MeshDesc(case.porder, case.NeX, case.NeY, case.NeZ, xmin, xmax, ymin, ymax, zmin, zmax, 1, 1,
+                     GRAV, RDRY, CPDRY, CVDRY, PRES00, int(fo), 2.0 / 3.0, 36.0, 16, 2.0 / 3.0, 36.0, 16, device)
+        h = _vp()
+        _check(self.lib.fedg_ctx_create(ctypes.byref(d), ctypes.byref(h)), "fedg_ctx_create")
+        self.h = h
+        self.shape = (case.Ne, case.Np)
+        self.ncol = case.NeX * case.NeY * case.N1 * case.N1
+        self._base = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fedg_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- helpers --
+    def tensor(self, a):
+        t = self.torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64)).to(self.dev)
+        return t.contiguous()
+
+    def empty(self):
+        return self.torch.empty(self.shape, dtype=self.torch.float64, device=self.dev)
+
+    def sync(self):
+        _check(self.lib.fedg_synchronize(self.h), "fedg_synchronize")
+
+    @property
+    def stream_handle(self):
+        return self.lib.fedg_ctx_stream(self.h)
+
+    # -- FElib interface --
+    def set_base_state(self, dens_hyd, pres_hyd, therm_hyd):
+        b = [self.tensor(dens_hyd), self.tensor(pres_hyd), self.tensor(therm_hyd)]
+        self.torch.cuda.synchronize()
+        _check(self.lib.fedg_set_base_state(self.h, _ptr(b[0]), _ptr(b[1]), _ptr(b[2]), None, None, None, None,
+                                            None, None), "fedg_set_base_state")
+        self._base = b
+        return b
+
+    def drhot2pres(self, drhot):
+        pres, dpres = self.empty(), self.empty()
+        self.torch.cuda.synchronize()
+        _check(self.lib.fedg_drhot2pres(self.h, _ptr(drhot), _ptr(pres), _ptr(dpres)), "fedg_drhot2pres")
+        self.sync()
+        return pres, dpres
+
+    def cal_tend_ex(self, q, eqs, dpres=None):
+        out = [self.empty() for _ in range(5)]
+        b = self._base
+        ins = (ctypes.c_void_p * 16)(*[t.data_ptr() for t in q], dpres.data_ptr() if dpres is not None else None,
+                                     b[0].data_ptr(), b[1].data_ptr(), None, b[2].data_ptr(),
+                                     None, None, None, None, None, None)
+        self.torch.cuda.synchronize()
+        _check(self.lib.fedg_cal_tend_ex(self.h, ins, _p5(out), int(eqs)), "fedg_cal_tend_ex")
+        self.sync()
+        return out
+
+    def cal_vi(self, q, q0, impl_fac, dt, max_iter=1, tol=0.0, want_status=False):
+        out = [self.empty() for _ in range(5)]
+        b = self._base
+        ins = (ctypes.c_void_p * 12)(*[t.data_ptr() for t in q], b[0].data_ptr(), b[1].data_ptr(),
+                                     *[t.data_ptr() for t in q0])
+        st = self.torch.zeros(self.ncol, dtype=self.torch.int32, device=self.dev)
+        self.torch.cuda.synchronize()
+        nfail = _check(self.lib.fedg_cal_vi(self.h, ins, float(impl_fac), float(dt), int(max_iter), float(tol),
+                                            _p5(out), _ptr(st)), "fedg_cal_vi")
+        self.sync()
+        if want_status:
+            return out, nfail, st
+        return out
+
+    def modalfilter(self, q):
+        self.torch.cuda.synchronize()
+        _check(self.lib.fedg_modalfilter(self.h, _p5(q)), "fedg_modalfilter")
+        self.sync()
+        return q
+
+    def update(self, q, nsteps, *, eqs=None, prec=PREC_FP64, dt=None, max_iter=1, tol=0.0, use_guess=False,
+               sync=True):
+        eqs = (HEVE if self.case.eqs == "HEVE" else HEVI) if eqs is None else eqs
+        o = UpdateOpts(int(eqs), int(prec), int(max_iter), int(bool(use_guess)),
+                       float(self.case.dt if dt is None else dt), float(tol))
+        mi = ctypes.c_double(0.0)
+        if sync:
+            self.torch.cuda.synchronize()
+        nfail = _check(self.lib.fedg_update(self.h, _p5(q), int(nsteps), ctypes.byref(o), ctypes.byref(mi)),
+                       "fedg_update")
+        if sync:
+            self.sync()
+        return nfail, float(mi.value)
+
+
+def prof_enable(ctx, on=True):
+    _check(ctx.lib.fedg_prof_enable(ctx.h, int(bool(on))), "fedg_prof_enable")
+
+
+def prof_reset(ctx):
+    _check(ctx.lib.fedg_prof_reset(ctx.h), "fedg_prof_reset")
+
+
+def prof_read(ctx):
+    """{kernel_name: (total_ms, launches)} for every kernel class of the context."""
+    out = {}
+    for k, nm in enumerate(KERNEL_NAMES):
+        t = ctypes.c_double(0.0)
+        n = ctypes.c_longlong(0)
+        _check(ctx.lib.fedg_prof_read(ctx.h, k, ctypes.byref(t), ctypes.byref(n)), "fedg_prof_read")
+        out[nm] = (float(t.value), int(n.value))
+    return out
+
+
+class TimeInt:
+    """fedg_tint: FElib's timeint_rk object (var0, varTmp, tendency buffers) on the device."""
+
+    def __init__(self, ctx: Context, scheme: int, dt: float):
+        self.ctx = ctx
+        h = _vp()
+        _check(ctx.lib.fedg_tint_create(ctx.h, int(scheme), float(dt), ctypes.byref(h)), "fedg_tint_create")
+        self.h = h
+        self.nstage = ctx.lib.fedg_tint_nstage(h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.fedg_tint_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def implicit_diagfac(self, s):
+        return self.ctx.lib.fedg_tint_implicit_diagfac(self.h, int(s))
+
+    def _wrap(self, ptr):
+        """A torch view of a library-owned device buffer (Ne, Np) float64."""
+        torch = self.ctx.torch
+        n = self.ctx.shape[0] * self.ctx.shape[1]
+        # build a tensor from the raw pointer via __cuda_array_interface__
+        class _CAI:
+            __cuda_array_interface__ = {"shape": (n,), "typestr": "<f8", "data": (int(ptr), False), "version": 3,
+                                        "strides": None}
+        return torch.as_tensor(_CAI(), device=self.ctx.dev).view(self.ctx.shape)
+
+    def tend_ex(self, s, v):
+        return self._wrap(self.ctx.lib.fedg_tint_tend_ex(self.h, int(s), int(v)))
+
+    def tend_im(self, s, v):
+        return self._wrap(self.ctx.lib.fedg_tint_tend_im(self.h, int(s), int(v)))
+
+    def var0(self, v):
+        return self._wrap(self.ctx.lib.fedg_tint_var0(self.h, int(v)))
+
+    def store_var0(self, q):
+        _check(self.ctx.lib.fedg_tint_store_var0(self.h, _p5(q)), "fedg_tint_store_var0")
+
+    def store_implicit(self, s, q):
+        _check(self.ctx.lib.fedg_tint_store_implicit(self.h, int(s), _p5(q)), "fedg_tint_store_implicit")
+
+    def advance(self, s, q):
+        _check(self.ctx.lib.fedg_tint_advance(self.h, int(s), _p5(q)), "fedg_tint_advance")

@@ -1,0 +1,163 @@
+/*
+ * fedg.h -- C ABI of the GB300-native SCALE-DG nonhydrostatic 3D DG dynamics step.
+ *
+ * Drop-in boundary for FElib's dynamics hot path (ywkawai/FE-Project):
+ *   - explicit tendency      atm_dyn_nonhydro3d_cal_tend_ex
+ *                            FElib/src/fluid_dyn_solver/scale_atm_dyn_dgm_driver_nonhydro3d.F90:152-199
+ *                            implementations ..._nonhydro3d_rhot_heve.F90:292-489 (HEVE),
+ *                            ..._nonhydro3d_rhot_hevi.F90:289-482 (HEVI)
+ *   - vertical-implicit solve atm_dyn_nonhydro3d_cal_vi
+ *                            ..._driver_nonhydro3d.F90:201-250, ..._rhot_hevi.F90:772-965
+ *   - RK stage methods       timeint_rk%StoreVar0 / StoreImplicit / Advance / Get_implicit_diagfac
+ *                            FElib/src/common/scale_timeint_rk.F90:81-104, 304-317, 536-585, 2201-2565
+ *   - modal filter           atm_dyn_dgm_modalfilter_apply, ..._dgm_modalfilter.F90:49-130
+ *   - pressure               atm_dyn_dgm_nonhydro3d_common_DRHOT2PRES, ..._nonhydro3d_common.F90:428-479
+ *   - driver stage loop      AtmDynDGMDriver_nonhydro3d_update, ..._driver_nonhydro3d.F90:614-963
+ *
+ * Conventions
+ *   - Every field is an FElib array real(RP) :: q(Np, NeA), column-major, passed as a
+ *     DEVICE pointer (the Fortran side passes it under `!$acc host_data use_device`).
+ *     Only the first Np*Ne entries (the local elements) are read or written: exterior
+ *     values of periodic faces and of the slip lids are formed inside the kernels, so no
+ *     halo exchange is needed on one GPU.
+ *   - Element order ke = i + (j-1)*NeX + (k-1)*NeX*NeY, node order p = i + (j-1)*N1 + (k-1)*N1^2.
+ *   - Return codes: 0 ok; > 0 number of columns whose Newton iteration did not converge;
+ *     < 0 error (fedg_last_error() gives the text).  No entry point traps the GPU.
+ *   - One CUDA stream per context; every call is stream-ordered and returns without a
+ *     device synchronisation unless it has to read a result back (status counts).
+ */
+#ifndef FEDG_H
+#define FEDG_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct fedg_ctx fedg_ctx;
+typedef struct fedg_tint fedg_tint;
+
+/* Flat cube domain: the MeshCubeDom3D parameters FElib reads from &PARAM_ATMOS_MESH
+ * (scale_mesh_cubedom3d.F90) plus the SCALE constants (&PARAM_CONST) and the modal
+ * filter parameters (&PARAM_ATMOS_DYN_MODALFILTER, ..._driver_nonhydro3d.F90:1249-1294). */
+typedef struct {
+  int porder;                 /* PolyOrder_h == PolyOrder_v, 1..7                         */
+  int NeX, NeY, NeZ;          /* local elements per direction                            */
+  double xmin, xmax, ymin, ymax, zmin, zmax;
+  int periodic_x, periodic_y; /* must be 1: periodic lateral boundaries                  */
+  double grav, rdry, cpdry, cvdry, pres00;
+  int mf_on;                  /* MODALFILTER_FLAG                                        */
+  double mf_etac_h, mf_alpha_h; int mf_order_h;
+  double mf_etac_v, mf_alpha_v; int mf_order_v;
+  int device;                 /* CUDA device ordinal                                     */
+} fedg_mesh_desc;
+
+enum { FEDG_HEVE = 0, FEDG_HEVI = 1 };
+enum { FEDG_SSP_RK3 = 0, FEDG_IMEX_ARK232 = 1 };
+/* precision of the fused update path (fedg_update) */
+enum { FEDG_PREC_FP64 = 0, FEDG_PREC_MIXED = 1 };
+
+const char* fedg_last_error(void);
+
+/* Context: builds the reference-element operators (D1D, exact-mass Lift, filters, VPOrdM1
+ * truncation) and owns one CUDA stream and the scratch of the fused paths.
+ * Replaces MeshCubeDom3D + HexahedralElement + ElementOperationTensorProd3D set-up
+ * (scale_element_hexahedral.F90:102-404, scale_element_operation_tensorprod3D.F90:5512-5569). */
+int fedg_ctx_create(const fedg_mesh_desc* desc, fedg_ctx** out);
+void fedg_ctx_destroy(fedg_ctx* ctx);
+/* the CUDA stream (cudaStream_t) every call of this context is ordered on */
+void* fedg_ctx_stream(fedg_ctx* ctx);
+int fedg_synchronize(fedg_ctx* ctx);
+
+/* Base state (AUX_VARS DENS_hyd, PRES_hyd, THERM_hyd, Rtot, CVtot, CPtot, DPhydDx, DPhydDy and
+ * the 2D CORIOLIS(Np2D, NeA2D)); device pointers in FElib layout.  The library keeps the
+ * state as per-level column profiles: it checks on the GPU that the fields are horizontally
+ * homogeneous, that Rtot/CVtot/CPtot are the dry constants, DPhydDx/DPhydDy vanish and
+ * CORIOLIS is constant, and returns < 0 otherwise.  CORIOLIS and DPhyd* may be NULL (zero). */
+int fedg_set_base_state(fedg_ctx* ctx, const double* DENS_hyd, const double* PRES_hyd,
+                        const double* THERM_hyd, const double* Rtot, const double* CVtot,
+                        const double* CPtot, const double* DPhydDx, const double* DPhydDy,
+                        const double* CORIOLIS);
+
+/* atm_dyn_dgm_nonhydro3d_common_DRHOT2PRES (nonhydro3d_common.F90:428-479). */
+int fedg_drhot2pres(fedg_ctx* ctx, const double* DRHOT, double* PRES, double* DPRES);
+
+/* atm_dyn_nonhydro3d_cal_tend_ex (driver_nonhydro3d.F90:152-199).
+ *   in[16]  = DDENS_, MOMX_, MOMY_, MOMZ_, DRHOT_, DPRES_, DENS_hyd, PRES_hyd, PRES_hyd_ref,
+ *             THERM_hyd, CORIOLIS, Rtot, CVtot, CPtot, DPhydDx, DPhydDy
+ *   out[5]  = DENS_dt, MOMX_dt, MOMY_dt, MOMZ_dt, RHOT_dt
+ *   eqs     = FEDG_HEVE (rhot_heve_cal_tend) or FEDG_HEVI (rhot_hevi_cal_tend)
+ * The base-state inputs are registered with fedg_set_base_state when their pointers differ
+ * from the registered ones.  DPRES_ may be NULL: it is then formed from DRHOT_ inside the kernel. */
+int fedg_cal_tend_ex(fedg_ctx* ctx, const double* const in[16], double* const out[5], int eqs);
+
+/* atm_dyn_nonhydro3d_cal_vi (driver_nonhydro3d.F90:201-250; rhot_hevi.F90:772-965).
+ *   in[12]  = DDENS_, MOMX_, MOMY_, MOMZ_, DRHOT_, DENS_hyd, PRES_hyd,
+ *             DDENS0_, MOMX0_, MOMY0_, MOMZ0_, DRHOT0_       (Rtot/CVtot/CPtot: registered)
+ *   out[5]  = DENS_dt, MOMX_dt, MOMY_dt, MOMZ_dt, RHOT_dt  = (q_new - q)/impl_fac, or A(var0)
+ *             when impl_fac == 0 (rhot_hevi.F90:943-961)
+ *   max_iter = 1 reproduces FElib's single linearised solve from the guess var0;
+ *   max_iter > 1 iterates Newton until the scaled residual is below tol.
+ *   col_status (optional, device, NeX*NeY*N1*N1 ints): Newton solves used per column,
+ *   -1 = not converged, -2 = non-finite.  Returns the number of non-converged columns. */
+int fedg_cal_vi(fedg_ctx* ctx, const double* const in[12], double impl_fac, double dt,
+                int max_iter, double tol, double* const out[5], int* col_status);
+
+/* atm_dyn_dgm_modalfilter_apply with do_weight_Gsqrt (dgm_modalfilter.F90:49-130), in place. */
+int fedg_modalfilter(fedg_ctx* ctx, double* const q[5]);
+
+/* timeint_rk (scale_timeint_rk.F90).  The object owns var0, varTmp and the explicit and
+ * implicit tendency buffers tend_buf2D_ex/im(Np, Ne, 5, nstage) on the device. */
+int fedg_tint_create(fedg_ctx* ctx, int scheme, double dt, fedg_tint** out);
+void fedg_tint_destroy(fedg_tint* t);
+int fedg_tint_nstage(const fedg_tint* t);
+double fedg_tint_implicit_diagfac(const fedg_tint* t, int stage);           /* :304-317   */
+/* device pointer of tend_buf2D_ex/_im(:, :, var, stage) (var in out[] order, stage 1-based) */
+double* fedg_tint_tend_ex(fedg_tint* t, int stage, int var);
+double* fedg_tint_tend_im(fedg_tint* t, int stage, int var);
+double* fedg_tint_var0(fedg_tint* t, int var);
+int fedg_tint_store_var0(fedg_tint* t, double* const q[5]);                   /* driver :703-713 */
+int fedg_tint_store_implicit(fedg_tint* t, int stage, double* const q[5]);    /* :2510-2565 */
+int fedg_tint_advance(fedg_tint* t, int stage, double* const q[5]);           /* :536-585, 1182-1278, 2201-2360 */
+
+/* AtmDynDGMDriver_nonhydro3d_update (driver_nonhydro3d.F90:614-963): nsteps full time steps
+ * of q (5 device fields) with the fused GPU stage kernels.  eqs FEDG_HEVE uses SSP-RK3,
+ * FEDG_HEVI uses IMEX ARK232 with the column Newton solve (max_iter, tol).
+ * prec: FEDG_PREC_FP64, or FEDG_PREC_MIXED (FP32 explicit arithmetic on deviations from the
+ * hydrostatic state with 3xTF32 tensor-core derivative contractions; FP64 pressure deviation,
+ * Newton residual, linear solve and RK accumulation).  use_guess != 0 takes the initial
+ * Newton iterate from the column-guess network loaded with fedg_guess_load.
+ * iters_out (optional, host): mean Newton solves per implicit column solve. */
+typedef struct {
+  int eqs, prec, max_iter, use_guess;
+  double dt, tol;
+} fedg_update_opts;
+int fedg_update(fedg_ctx* ctx, double* const q[5], int nsteps, const fedg_update_opts* opts,
+                double* iters_out);
+
+/* Kernel timers: the analogue of FElib's PROF_rapstart/PROF_rapend regions
+ * (e.g. 'ATM_DYN_cal_vi', 'cal_dyn_tend_interior'; scale_prof of the SCALE library).
+ * When enabled, every launch of the context records a pair of CUDA events on the context
+ * stream; fedg_prof_read synchronises and returns the summed device time and the launch
+ * count of one kernel class.  Launch counts are kept even when timing is off. */
+enum {
+  FEDG_K_TEND = 0,      /* explicit tendency (volume + face + Lift), FP64          */
+  FEDG_K_VI = 1,        /* column Newton solve, FP64                                */
+  FEDG_K_RK = 2,        /* RK stage arithmetic                                      */
+  FEDG_K_FILTER = 3,    /* modal filter                                             */
+  FEDG_K_PRES = 4,      /* DRHOT -> DPRES                                           */
+  FEDG_K_MTEND = 5,     /* fused mixed-precision stage kernel (tendency + RK)       */
+  FEDG_K_MVI = 6,       /* mixed-precision column solve                             */
+  FEDG_K_MLP = 7,       /* column-guess network (inference / training)              */
+  FEDG_K_AUX = 8,       /* status reductions, base-state checks                     */
+  FEDG_K_COUNT = 9
+};
+int fedg_prof_enable(fedg_ctx* ctx, int on);
+int fedg_prof_reset(fedg_ctx* ctx);
+int fedg_prof_read(fedg_ctx* ctx, int kernel, double* total_ms, long long* launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FEDG_H */

@@ -643,17 +643,31 @@ static int column_solve(const Oracle& o, ColumnWork& w, const ColumnParams& cp, 
   }
 
   // ---- DENS/MOMZ/RHOT: Newton iterations (eval_Ax + solve, common_2.F90:111-479) ----
+  // The FP64 residual b = impl_fac*A(P) - P + q* is evaluated before every solve; with
+  // max_iter > 1 the iteration stops once max |b|/scale <= tol (scale: DENS_hyd,
+  // DENS_hyd*cref, RHOT_hyd).  max_iter == 1 is FElib's single solve without a test.
   int iters_used = -1;
-  for (int it = 1; it <= cp.max_iter; ++it) {
+  int nsolve = 0;
+  for (;;) {
     column_eval_Ax(o, w);
     std::vector<double>& b = w.b;  // (NeZ, n3) row index v + 3*pv
+    double err = 0.0;
     for (int ez = 0; ez < NeZ; ++ez)
       for (int k = 0; k < N1; ++k) {
         const int l = ez * N1 + k;
-        b[ez * n3 + 3 * k + 0] = impl_fac * w.A3[0 * L + l] - w.P[VD][l] + w.Q[VD][l];
-        b[ez * n3 + 3 * k + 1] = impl_fac * w.A3[1 * L + l] - w.P[VMZ][l] + w.Q[VMZ][l];
-        b[ez * n3 + 3 * k + 2] = impl_fac * w.A3[2 * L + l] - w.P[VRT][l] + w.Q[VRT][l];
+        const double bd = impl_fac * w.A3[0 * L + l] - w.P[VD][l] + w.Q[VD][l];
+        const double bm = impl_fac * w.A3[1 * L + l] - w.P[VMZ][l] + w.Q[VMZ][l];
+        const double br = impl_fac * w.A3[2 * L + l] - w.P[VRT][l] + w.Q[VRT][l];
+        b[ez * n3 + 3 * k + 0] = bd;
+        b[ez * n3 + 3 * k + 1] = bm;
+        b[ez * n3 + 3 * k + 2] = br;
+        err = std::max(err, std::fabs(bd) / w.dh[l]);
+        err = std::max(err, std::fabs(bm) / (w.dh[l] * o.newton_cref));
+        err = std::max(err, std::fabs(br) / w.rh[l]);
       }
+    if (!std::isfinite(err)) { iters_used = -2; break; }
+    if (cp.max_iter > 1 && err <= cp.tol) { iters_used = nsolve; break; }
+    if (nsolve >= cp.max_iter) { iters_used = -1; break; }
     std::vector<double>& G = w.G;           // (NeZ, n3, 3)
     std::vector<double> Dd(n3 * n3), R(n3 * 4), Lc(n3 * 3), Uc(n3 * 3);
     for (int ez = 0; ez < NeZ; ++ez) {
@@ -746,19 +760,15 @@ static int column_solve(const Oracle& o, ColumnWork& w, const ColumnParams& cp, 
         for (int m = 0; m < 3; ++m) s += G[(ez * n3 + r) * 3 + m] * b[(ez + 1) * n3 + m];
         b[ez * n3 + r] -= s;
       }
-    double err = 0.0;
     for (int ez = 0; ez < NeZ; ++ez)
       for (int k = 0; k < N1; ++k) {
         const int l = ez * N1 + k;
-        const double dd = b[ez * n3 + 3 * k + 0], dm = b[ez * n3 + 3 * k + 1], dr = b[ez * n3 + 3 * k + 2];
-        w.P[VD][l] += dd;
-        w.P[VMZ][l] += dm;
-        w.P[VRT][l] += dr;
-        err = std::max(err, std::fabs(dd) / w.dh[l]);
-        err = std::max(err, std::fabs(dm) / (w.dh[l] * o.newton_cref));
-        err = std::max(err, std::fabs(dr) / w.rh[l]);
+        w.P[VD][l] += b[ez * n3 + 3 * k + 0];
+        w.P[VMZ][l] += b[ez * n3 + 3 * k + 1];
+        w.P[VRT][l] += b[ez * n3 + 3 * k + 2];
       }
-    if (cp.max_iter == 1 || err <= cp.tol) { iters_used = it; break; }
+    ++nsolve;
+    if (cp.max_iter == 1) { iters_used = 1; break; }
   }
   // tend_im = (PROG - q)/impl_fac  (hevi.F90:931-942)
   for (int v = 0; v < 5; ++v)
@@ -983,7 +993,7 @@ long orc_step_hevi(void* h, double* const* q, double dt, int nsteps, int max_ite
       const double* qc[5]; const double* z0[5]; double* tip[5]; double* tep[5];
       for (int v = 0; v < 5; ++v) { qc[v] = q[v]; z0[v] = var0[v].data(); tip[v] = tim[st][v].data(); tep[v] = tex[st][v].data(); }
       nfail += cal_vi(*o, qc, z0, impl_fac, dt, max_iter, tol, tip, its.data());
-      if (impl_fac != 0.0) { for (long c = 0; c < ncol; ++c) if (its[c] > 0) { itsum += its[c]; ++itcnt; } }
+      if (impl_fac != 0.0) { for (long c = 0; c < ncol; ++c) if (its[c] >= 0) { itsum += its[c]; ++itcnt; } }
       for (int v = 0; v < 5; ++v) {  // StoreImplicit (timeint_rk.F90:2510-2565)
         double* x = q[v];
         if (st == 1) { std::memcpy(var0[v].data(), x, n * sizeof(double)); std::memcpy(vtmp[v].data(), x, n * sizeof(double)); }
