@@ -10,6 +10,7 @@
 #include "fedg_common.cuh"
 #include "fedg_kernels.cuh"
 #include "fedg_mixed.cuh"
+#include "fedg_ctx.cuh"
 
 using namespace fedg;
 
@@ -23,6 +24,12 @@ int cuda_fail(cudaError_t e, const char* where) {
   g_err = std::string(where) + ": " + cudaGetErrorString(e);
   return -2;
 }
+}  // namespace
+namespace fedg {
+int api_fail(const std::string& m) { return fail(m); }
+int api_cuda_fail(cudaError_t e, const char* where) { return cuda_fail(e, where); }
+}  // namespace fedg
+namespace {
 #define CK(call)                                              \
   do {                                                        \
     cudaError_t e_ = (call);                                  \
@@ -234,61 +241,6 @@ __global__ void k_rk(RKPtrs P, int kind, int stage, int nst, RKC c, size_t n, in
 
 }  // namespace
 
-// =====================================================================================
-struct fedg_ctx {
-  fedg_mesh_desc d;
-  Ops op;
-  int N1, Np, Ne, L, ncol;
-  size_t nxy, n;  // n = Np*Ne
-  cudaStream_t stream = nullptr;
-  double* d_prof = nullptr;  // [4][L]: dens, pres, therm, rhyd
-  bool base_set = false;
-  const void* base_ptr[10] = {};
-  int* d_status = nullptr;
-  unsigned long long* d_cnt = nullptr;
-  unsigned long long* h_cnt = nullptr;  // pinned [3]
-  // fused-update scratch
-  double* work = nullptr;
-  size_t work_doubles = 0;
-  MixedState* mixed = nullptr;
-  fedg_tint* upd_tint = nullptr;  // RK buffers of fedg_update, kept between calls
-  // kernel timers / launch counters
-  bool prof_on = false;
-  long long nlaunch[FEDG_K_COUNT] = {};
-  struct Rec { int id; cudaEvent_t a, b; };
-  std::vector<Rec> recs;
-  Prof prof() const { return Prof{d_prof, d_prof + L, d_prof + 2 * L, d_prof + 3 * L}; }
-};
-
-// Runs one launch f() of kernel class id on the context stream, counting it and, when the
-// timers are on, bracketing it with a pair of CUDA events.
-template <class Fn>
-static int tracked(fedg_ctx* c, int id, Fn&& f) {
-  c->nlaunch[id]++;
-  if (!c->prof_on) return f();
-  fedg_ctx::Rec r{id, nullptr, nullptr};
-  cudaEventCreate(&r.a);
-  cudaEventCreate(&r.b);
-  cudaEventRecord(r.a, c->stream);
-  const int rc = f();
-  cudaEventRecord(r.b, c->stream);
-  c->recs.push_back(r);
-  return rc;
-}
-
-struct fedg_tint {
-  fedg_ctx* ctx;
-  int scheme, nstage;
-  double dt;
-  double a_ex[3][3], a_im[3][3], b_ex[3], b_im[3];
-  double sig[4][3], gam[4][3];
-  double* buf = nullptr;  // var0, vtmp, tex[ns], tim[ns] : each 5*n
-  double* var0(int v) { return buf + (size_t)v * ctx->n; }
-  double* vtmp(int v) { return buf + (size_t)(5 + v) * ctx->n; }
-  double* tex(int s, int v) { return buf + (size_t)(10 + 5 * s + v) * ctx->n; }
-  double* tim(int s, int v) { return buf + (size_t)(10 + 5 * nstage + 5 * s + v) * ctx->n; }
-};
-
 extern "C" {
 
 const char* fedg_last_error(void) { return g_err.c_str(); }
@@ -399,6 +351,8 @@ int fedg_set_base_state(fedg_ctx* c, const double* DENS_hyd, const double* PRES_
   CK(cudaStreamSynchronize(c->stream));
   c->op.coriolis_f = f;
   c->base_set = true;
+  mixed_free(c->mixed);  // FP32 profiles of the mixed path are rebuilt from the new base state
+  c->mixed = nullptr;
   const void* ptrs[10] = {DENS_hyd, PRES_hyd, THERM_hyd, Rtot, CVtot, CPtot, DPhydDx, DPhydDy, CORIOLIS, nullptr};
   std::memcpy(c->base_ptr, ptrs, sizeof(ptrs));
   return 0;

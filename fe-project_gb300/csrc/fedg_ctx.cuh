@@ -1,0 +1,70 @@
+// fedg_ctx.cuh -- context and RK objects shared by the translation units.
+#pragma once
+#include <string>
+#include <vector>
+
+#include "../../include/fedg.h"
+#include "fedg_common.cuh"
+#include "fedg_kernels.cuh"
+#include "fedg_mixed.cuh"
+
+namespace fedg {
+int api_fail(const std::string& m);
+int api_cuda_fail(cudaError_t e, const char* where);
+}  // namespace fedg
+using namespace fedg;
+
+struct fedg_ctx {
+  fedg_mesh_desc d;
+  Ops op;
+  int N1, Np, Ne, L, ncol;
+  size_t nxy, n;  // n = Np*Ne
+  cudaStream_t stream = nullptr;
+  double* d_prof = nullptr;  // [4][L]: dens, pres, therm, rhyd
+  bool base_set = false;
+  const void* base_ptr[10] = {};
+  int* d_status = nullptr;
+  unsigned long long* d_cnt = nullptr;
+  unsigned long long* h_cnt = nullptr;  // pinned [3]
+  // fused-update scratch
+  double* work = nullptr;
+  size_t work_doubles = 0;
+  MixedState* mixed = nullptr;
+  fedg_tint* upd_tint = nullptr;  // RK buffers of fedg_update, kept between calls
+  // kernel timers / launch counters
+  bool prof_on = false;
+  long long nlaunch[FEDG_K_COUNT] = {};
+  struct Rec { int id; cudaEvent_t a, b; };
+  std::vector<Rec> recs;
+  Prof prof() const { return Prof{d_prof, d_prof + L, d_prof + 2 * L, d_prof + 3 * L}; }
+};
+
+// Runs one launch f() of kernel class id on the context stream, counting it and, when the
+// timers are on, bracketing it with a pair of CUDA events.
+template <class Fn>
+static int tracked(fedg_ctx* c, int id, Fn&& f) {
+  c->nlaunch[id]++;
+  if (!c->prof_on) return f();
+  fedg_ctx::Rec r{id, nullptr, nullptr};
+  cudaEventCreate(&r.a);
+  cudaEventCreate(&r.b);
+  cudaEventRecord(r.a, c->stream);
+  const int rc = f();
+  cudaEventRecord(r.b, c->stream);
+  c->recs.push_back(r);
+  return rc;
+}
+
+struct fedg_tint {
+  fedg_ctx* ctx;
+  int scheme, nstage;
+  double dt;
+  double a_ex[3][3], a_im[3][3], b_ex[3], b_im[3];
+  double sig[4][3], gam[4][3];
+  double* buf = nullptr;  // var0, vtmp, tex[ns], tim[ns] : each 5*n
+  double* var0(int v) { return buf + (size_t)v * ctx->n; }
+  double* vtmp(int v) { return buf + (size_t)(5 + v) * ctx->n; }
+  double* tex(int s, int v) { return buf + (size_t)(10 + 5 * s + v) * ctx->n; }
+  double* tim(int s, int v) { return buf + (size_t)(10 + 5 * nstage + 5 * s + v) * ctx->n; }
+};
+
