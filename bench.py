@@ -241,13 +241,13 @@ def run_fedg(args):
         "vi_fp64": 8 * (5 + 5 + 5),          # q*, var0 in; tend_im out
         "tend_fp64": 8 * (6 + 5),            # 5 fields + DPRES in; 5 tendencies out
         "rk": 8 * 20,                        # general IMEX advance (upper bound of the stage kinds)
-        "stage_mixed": 0, "vi_mixed": 0, "filter": 8 * 10, "drhot2pres": 8 * 2, "mlp": 0, "aux": 0,
+        # fused stage kernels, mean of the three: S1 q^n in -> q*_2, S3, SF out (120 B);
+        # S2 Q_2, t_im, q^n, S3, SF in -> q*_3, SF out (200 B); S3 Q_3, t_im, q^n, SF in -> q^n+1 (160 B)
+        "stage_mixed": 160,
+        # column solve: q*, var0 in (FP64) -> Q (FP64), t_im (FP32) out
+        "vi_mixed": 8 * 5 + 8 * 5 + 8 * 5 + 4 * 5,
+        "filter": 8 * 10, "drhot2pres": 8 * 2, "mlp": 0, "aux": 0,
     }
-    try:
-        from fedg import mixed_bytes
-        bytes_per_node.update(mixed_bytes.BYTES_PER_NODE)
-    except Exception:
-        pass
     avg_ms = ktime / max(klaunch, 1)
     achieved = bytes_per_node.get(kname, 0) * nodes / (avg_ms * 1e-3) / 1e9 if avg_ms > 0 else 0.0
     roof = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peaks.get("hbm_gbs", 6800.0),
@@ -276,6 +276,24 @@ def run_fedg(args):
         e2e = {"value": dofs_stage * ke / (t1 - t0), "unit": UNIT, "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb,
                "steps": ke}
 
+    plain = None
+    if rank == 0 and prec != fl.PREC_FP64 and not args.no_plain:
+        # the plain FP64 path on the same workload and state (FElib's algorithm in FP64 on the GPU)
+        o64 = dict(opts)
+        o64.update(prec=fl.PREC_FP64, use_guess=False)
+        ctx.update(qd, 1, **o64)
+        torch.cuda.synchronize()
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        kp = 2
+        p0.record(stream)
+        nf64, its64 = ctx.update(qd, kp, sync=False, **o64)
+        p1.record(stream)
+        ctx.sync()
+        torch.cuda.synchronize()
+        pms = p0.elapsed_time(p1)
+        plain = {"value": dofs_stage * kp / (pms * 1e-3), "unit": UNIT, "ms_per_step": pms / kp, "steps": kp,
+                 "mean_newton_solves": its64, "nonconverged_columns": nf64}
+
     cb = None
     if rank == 0 and not args.no_cpu:
         cb = cpu_sample(path)
@@ -297,6 +315,8 @@ def run_fedg(args):
             "roofline_fp64": {"bound": "fp64", "peak_tflops": fp64_tf, "peak_source": "measured cuBLAS DGEMM 4096^3"},
             "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items() if v[1]},
             "cpu_baseline": cb, "e2e": e2e, "gpu_launches": gpu_launches, "clocks": clocks,
+            "plain_fp64": plain,
+            "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -311,11 +331,12 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["fedg", "reference"], default="fedg")
-    ap.add_argument("--path", choices=["mixed", "fp64"], default=os.environ.get("FEDG_BENCH_PATH", "fp64"))
-    ap.add_argument("--guess", type=int, default=1)
+    ap.add_argument("--path", choices=["mixed", "fp64"], default=os.environ.get("FEDG_BENCH_PATH", "mixed"))
+    ap.add_argument("--guess", type=int, default=0)
     ap.add_argument("--small", action="store_true", help="32x32x16 elements instead of 128x128x16 (profiling)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison run")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

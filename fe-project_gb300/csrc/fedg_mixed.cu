@@ -30,7 +30,9 @@ struct MixCoef {
 };
 
 struct StageBufs {
-  const double* qs[5];  // state of the explicit tendency (q^n at stage 1, Q_s afterwards)
+  const float* qsf[5];  // state of the explicit tendency as FP32 deviations (q^n at stage 1, Q_s after):
+                        // DDENS, MOMX - DENS_hyd*Uref, MOMY - DENS_hyd*Vref, MOMZ, DRHOT
+  float* qnf[5];        // stage 3: FP32 deviation copy of q^{n+1} (next step's stage-1 state)
   double* qn[5];        // q^n; stage 3 overwrites it with q^{n+1}
   double* qi[5];        // next stage input q*_{s+1} (stages 1, 2)
   float* S3[5];         // stage-3 input accumulator
@@ -84,25 +86,14 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
   float* di = s_di + le * 5 * 2 * NF;
   const size_t g = (size_t)ke * Np + p;
   const int lev = ez * N1 + k;
-
-  // State as deviations in FP32: DDENS, DRHOT are deviations already; MOMX/MOMY are taken
-  // relative to the horizontally uniform reference DENS_hyd(z)*(U, V) (subtracted in FP64),
-  // whose fluxes have zero divergence and cancel across every face.
-  double qd[5];
-  float qv[5], dp = 0.f;
-  if (valid) {
-#pragma unroll
-    for (int v = 0; v < 5; ++v) qd[v] = __ldg(B.qs[v] + g);
-  } else {
-#pragma unroll
-    for (int v = 0; v < 5; ++v) qd[v] = 0.0;
-  }
   const double dh64 = valid ? __ldg(dens64 + lev) : 1.0;
-  qv[VD] = (float)qd[VD];
-  qv[VMX] = (float)(qd[VMX] - dh64 * cf.Uref);
-  qv[VMY] = (float)(qd[VMY] - dh64 * cf.Vref);
-  qv[VMZ] = (float)qd[VMZ];
-  qv[VRT] = (float)qd[VRT];
+
+  // The state arrives as FP32 deviations: DDENS, DRHOT are deviations already; MOMX/MOMY are
+  // taken relative to the horizontally uniform reference DENS_hyd(z)*(Uref, Vref) (subtracted in
+  // FP64 by the producer), whose fluxes have zero divergence and cancel across every face.
+  float qv[5], dp = 0.f;
+#pragma unroll
+  for (int v = 0; v < 5; ++v) qv[v] = valid ? __ldg(B.qsf[v] + g) : 0.f;
   const float dh = valid ? __ldg(pf.dens + lev) : 1.f;
   const float th = valid ? __ldg(pf.therm + lev) : 0.f;
   if (valid) dp = dpres_f(qv[VRT], __ldg(pf.rtherm + lev), __ldg(pf.pres + lev), op.kap);
@@ -155,11 +146,8 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
         int i2, j2, k2;
         face_node<N1>(face_opp(f), a, b, i2, j2, k2);
         const size_t gP = (size_t)kn * Np + i2 + N1 * j2 + NF * k2;
-        const double dhP = __ldg(dens64 + levP);
-        ddP = (float)__ldg(B.qs[VD] + gP);
-        mxP = (float)(__ldg(B.qs[VMX] + gP) - dhP * cf.Uref);
-        myP = (float)(__ldg(B.qs[VMY] + gP) - dhP * cf.Vref);
-        mzP = (float)__ldg(B.qs[VMZ] + gP); drP = (float)__ldg(B.qs[VRT] + gP);
+        ddP = __ldg(B.qsf[VD] + gP); mxP = __ldg(B.qsf[VMX] + gP); myP = __ldg(B.qsf[VMY] + gP);
+        mzP = __ldg(B.qsf[VMZ] + gP); drP = __ldg(B.qsf[VRT] + gP);
         dpP = dpres_f(drP, __ldg(pf.rtherm + levP), __ldg(pf.pres + levP), op.kap);
       } else {
         levP = levM;
@@ -244,8 +232,8 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
       const bool horiz_only = (v == VD || v == VRT);
       tex[v] = -(op.E11 * sx + op.E22 * sy + (horiz_only ? 0.f : op.E33 * sz) + lf);
     }
-    tex[VMX] += op.coriolis_f * (float)qd[VMY];
-    tex[VMY] -= op.coriolis_f * (float)qd[VMX];
+    tex[VMX] += op.coriolis_f * (qv[VMY] + dh * op.Vref);
+    tex[VMY] -= op.coriolis_f * (qv[VMX] + dh * op.Uref);
     if (STAGE == 1) {
       float sdp = 0.f, drho = 0.f;
 #pragma unroll
@@ -271,7 +259,7 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
     if (valid) {
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
-        B.qi[v][g] = qd[v] + cf.dt * (double)(float(cf.a21e) * tex[v] + float(cf.a21i) * tim[v]);
+        B.qi[v][g] = __ldg(B.qn[v] + g) + cf.dt * (double)(float(cf.a21e) * tex[v] + float(cf.a21i) * tim[v]);
         B.S3[v][g] = float(cf.a31e) * tex[v] + float(cf.a31i) * tim[v];
         B.SF[v][g] = float(cf.b1) * (tex[v] + tim[v]);
       }
@@ -290,58 +278,56 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
     }
     return;
   }
-  // STAGE 3: q^{n+1}, then the modal filter on the deviation from the element mean
+  // STAGE 3: q^{n+1} = q^n + dt (SF + b3 (t_ex + t_im)) in FP64, then the modal filter applied to
+  // the deviation from the reference state (DENS_hyd*(Uref,Vref) for MOMX/MOMY, 0 otherwise; the
+  // filter leaves that smooth reference unchanged), q^{n+1} = ref + F(deviation).
   double qnew[5];
+  float dev[5];
 #pragma unroll
   for (int v = 0; v < 5; ++v) {
     qnew[v] = 0.0;
+    dev[v] = 0.f;
     if (valid) {
-      const double qn = __ldg(B.qn[v] + g);
-      qnew[v] = qn + cf.dt * (double)(__ldg(B.SF[v] + g) + float(cf.b3) * (tex[v] + tim[v]));
+      qnew[v] = __ldg(B.qn[v] + g) + cf.dt * (double)(__ldg(B.SF[v] + g) + float(cf.b3) * (tex[v] + tim[v]));
+      const double ref = v == VMX ? dh64 * cf.Uref : (v == VMY ? dh64 * cf.Vref : 0.0);
+      dev[v] = (float)(qnew[v] - ref);
     }
   }
   if (!filter_on) {
     if (valid) {
 #pragma unroll
-      for (int v = 0; v < 5; ++v) B.qn[v][g] = qnew[v];
+      for (int v = 0; v < 5; ++v) {
+        B.qn[v][g] = qnew[v];
+        B.qnf[v][g] = dev[v];
+      }
     }
     return;
   }
   __syncthreads();  // everyone is done with the shared arrays
-  double* red = reinterpret_cast<double*>(s_fl);  // [EPB][5][NW]
-  const int lane = tid & 31, wie = p >> 5;
-#pragma unroll
-  for (int v = 0; v < 5; ++v) {
-    double s = qnew[v];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) red[(le * 5 + v) * NW + wie] = s;
-  }
-  __syncthreads();
   float* fa = s_st + le * 6 * Np;
   float* fb = fa + Np;
   for (int v = 0; v < 5; ++v) {
-    double mean = 0.0;
-#pragma unroll
-    for (int w = 0; w < NW; ++w) mean += red[(le * 5 + v) * NW + w];
-    mean *= 1.0 / Np;
-    fa[p] = (float)(qnew[v] - mean);
+    fa[p] = dev[v];
     __syncthreads();
-    float s = 0.f;
+    float sacc = 0.f;
 #pragma unroll
-    for (int l = 0; l < N1; ++l) s = fmaf(op.F[i * N1 + l], fa[l + N1 * j + NF * k], s);
-    fb[p] = s;
+    for (int l = 0; l < N1; ++l) sacc = fmaf(op.F[i * N1 + l], fa[l + N1 * j + NF * k], sacc);
+    fb[p] = sacc;
     __syncthreads();
-    s = 0.f;
+    sacc = 0.f;
 #pragma unroll
-    for (int l = 0; l < N1; ++l) s = fmaf(op.F[j * N1 + l], fb[i + N1 * l + NF * k], s);
+    for (int l = 0; l < N1; ++l) sacc = fmaf(op.F[j * N1 + l], fb[i + N1 * l + NF * k], sacc);
     __syncthreads();
-    fa[p] = s;
+    fa[p] = sacc;
     __syncthreads();
-    s = 0.f;
+    sacc = 0.f;
 #pragma unroll
-    for (int l = 0; l < N1; ++l) s = fmaf(op.Fv[k * N1 + l], fa[i + N1 * j + NF * l], s);
-    if (valid) B.qn[v][g] = mean + (double)s;
+    for (int l = 0; l < N1; ++l) sacc = fmaf(op.Fv[k * N1 + l], fa[i + N1 * j + NF * l], sacc);
+    if (valid) {
+      const double ref = v == VMX ? dh64 * cf.Uref : (v == VMY ? dh64 * cf.Vref : 0.0);
+      B.qn[v][g] = ref + (double)sacc;
+      B.qnf[v][g] = sacc;
+    }
     __syncthreads();
   }
 }
@@ -441,12 +427,16 @@ __device__ __forceinline__ void warp_lu_t(T (&a)[n], T (&rhs)[nr], T* prow, int*
   __syncwarp();
 }
 
-// (1+r)^kappa - 1 by its binomial series (|r| <= rmax), else from pow()
-__device__ __forceinline__ double binom_pm1(double r, const PresSeries& ps, double kap) {
+// (1+r)^kappa - 1 by its binomial series (|r| <= rmax), else from pow().  nt terms: the caller
+// picks nt warp-uniformly from max|r| so the remainder stays below 1e-16 relative.
+__device__ __forceinline__ double binom_pm1(double r, const PresSeries& ps, double kap, int nt) {
   if (fabs(r) > ps.rmax) return pow(1.0 + r, kap) - 1.0;
-  double s = ps.c[ps.nterm - 1];
-  for (int m = ps.nterm - 2; m >= 0; --m) s = fma(s, r, ps.c[m]);
+  double s = ps.c[nt - 1];
+  for (int m = nt - 2; m >= 0; --m) s = fma(s, r, ps.c[m]);
   return s * r;
+}
+__device__ __forceinline__ int binom_terms(float amax) {
+  return amax <= 1e-4f ? 4 : (amax <= 1e-3f ? 5 : (amax <= 1e-2f ? 8 : 12));
 }
 
 struct ColMix {
@@ -490,8 +480,10 @@ __device__ double mix_residual(const Ops& op, ColMix& c, const PresSeries& ps, d
                                bool fp64) {
   constexpr int n3 = 3 * N1;
   const float kap = (float)op.kap;
-  // level quantities, lanes over levels
-  for (int l = c.lane; l < c.L; l += 32) {
+  // level quantities, lanes over levels (warp-uniform trip count: the FP64 branch shuffles)
+  for (int base = 0; base < c.L; base += 32) {
+    const bool lact = base + c.lane < c.L;
+    const int l = lact ? base + c.lane : c.L - 1;
     const double Pd = c.P[3 * l], Pm = c.P[3 * l + 1], Pr = c.P[3 * l + 2];
     const float densf = __ldg(c.dhf + l) + (float)Pd;
     const float rhotf = __ldg(c.rhf + l) + (float)Pr;
@@ -504,21 +496,29 @@ __device__ double mix_residual(const Ops& op, ColMix& c, const PresSeries& ps, d
       rd = rd * fma(-dens, rd, 2.0);
       rd = rd * fma(-dens, rd, 2.0);
       const double pot = rhot * rd;
-      const double fm = __ldg(c.ph + l) * binom_pm1(Pr * __ldg(c.rhinv + l), ps, op.kap);
-      c.pot64[l] = pot;
-      c.fm64[l] = fm;
-      c.fr64[l] = pot * Pm;
+      const double rr = Pr * __ldg(c.rhinv + l);
+      float ra = fabsf((float)rr);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) ra = fmaxf(ra, __shfl_xor_sync(0xffffffffu, ra, o));
+      const double fm = __ldg(c.ph + l) * binom_pm1(rr, ps, op.kap, binom_terms(ra));
+      if (lact) {
+        c.pot64[l] = pot;
+        c.fm64[l] = fm;
+        c.fr64[l] = pot * Pm;
+      }
       fmf = (float)fm;
       potf = (float)pot;
     } else {
       potf = rhotf * rdf;
       fmf = __ldg(c.phf + l) * expm1f(kap * log1pf((float)Pr * __ldg(c.rhinvf + l)));
     }
-    c.pot[l] = potf;
-    c.fm[l] = fmf;
-    c.fr[l] = potf * (float)Pm;
-    c.wt[l] = (float)Pm * rdf;
-    c.dpd[l] = kap * (__ldg(c.phf + l) + fmf) / rhotf;
+    if (lact) {
+      c.pot[l] = potf;
+      c.fm[l] = fmf;
+      c.fr[l] = potf * (float)Pm;
+      c.wt[l] = (float)Pm * rdf;
+      c.dpd[l] = kap * (__ldg(c.phf + l) + fmf) / rhotf;
+    }
   }
   __syncwarp();
   // vertical-face fluxes, lanes over (element, side, variable)
@@ -528,7 +528,7 @@ __device__ double mix_residual(const Ops& op, ColMix& c, const PresSeries& ps, d
     else c.del[it] = mix_face<N1, float>(c, ez, s, v, c.fm, c.pot, 0.5f * (float)op.FSz);
   }
   __syncwarp();
-  double err = 0.0;
+  float errf = 0.f;
   for (int l = c.lane; l < c.L; l += 32) {
     const int ez = l / N1, k = l - ez * N1;
     double A[3];
@@ -564,23 +564,24 @@ __device__ double mix_residual(const Ops& op, ColMix& c, const PresSeries& ps, d
       A[1] = -(E33 * sm + lb * dl[1] + lt * dl[4]) - (float)op.grav * drho;
       A[2] = -(E33 * sr + lb * dl[2] + lt * dl[5]);
     }
-    const double sc[3] = {__ldg(c.dh + l), __ldg(c.dh + l) * cref, __ldg(c.rh + l)};
+    const float isc[3] = {1.f / __ldg(c.dhf + l), 1.f / (__ldg(c.dhf + l) * (float)cref), 1.f / __ldg(c.rhf + l)};
 #pragma unroll
     for (int v = 0; v < 3; ++v) {
       const double b = fma(impl_fac, A[v], c.Q[3 * l + v] - c.P[3 * l + v]);
-      c.bf[3 * l + v] = (float)b;
-      err = fmax(err, fabs(b) / sc[v]);
-      if (!(fabs(b) < 1e300)) err = __longlong_as_double(0x7ff8000000000000LL);
+      const float bfl = (float)b;
+      c.bf[3 * l + v] = bfl;
+      errf = fmaxf(errf, fabsf(bfl) * isc[v]);
+      if (!(fabsf(bfl) < 3.0e38f)) errf = __int_as_float(0x7fc00000);
     }
   }
   __syncwarp();
-  double e = err;
+  float e = errf;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    const double oe = __shfl_xor_sync(0xffffffffu, e, o);
-    e = (e != e || oe != oe) ? __longlong_as_double(0x7ff8000000000000LL) : fmax(e, oe);
+    const float oe = __shfl_xor_sync(0xffffffffu, e, o);
+    e = (e != e || oe != oe) ? __int_as_float(0x7fc00000) : fmaxf(e, oe);
   }
-  return e;
+  return (double)e;
 }
 
 // one correction: construct_matbnd + block-Thomas + warp LU, all FP32; P += correction (FP64)
@@ -683,7 +684,8 @@ __device__ void mix_solve(const Ops& op, ColMix& c, double impl_fac) {
 }
 
 struct MixViArgs {
-  double impl_fac, tol, cref;
+  double impl_fac, inv_impl_fac, tol, cref;
+  double Uref, Vref;  // reference wind of the FP32 deviation copy of Q
   int max_iter;
   int check64;  // 1: convergence judged by the FP64 residual; 0: by the split residual
 };
@@ -702,7 +704,7 @@ template <int N1>
 __global__ void __launch_bounds__(128) k_vi_mixed(const Ops op, const Prof pf, const ProfF pff,
                                                    const double* __restrict__ rhinv, const PresSeries ps,
                                                    const F5c qin, const F5c z, const float* const* guess,
-                                                   const F5 qout, float* const* tout, int* status,
+                                                   float* const* qsf, float* const* tout, int* status,
                                                    unsigned long long* cnt, const MixViArgs args, int ncol) {
   constexpr int N = N1 - 1, NF = N1 * N1, Np = N1 * N1 * N1;
   extern __shared__ double sm[];
@@ -775,24 +777,29 @@ __global__ void __launch_bounds__(128) k_vi_mixed(const Ops op, const Prof pf, c
       Qu[2 * l + 1] = __ldg(qin.v[VMY] + g);
     }
     __syncwarp();
-    const double tm = -0.5 * op.FSz;
+    const float tmf = (float)(-0.5 * op.FSz);
     for (int it = 0; it < 4; ++it) {
-      double err = 0.0;
+      float err = 0.f;
       for (int l = lane; l < L; l += 32) {
         const int ez = l / N1, pv = l - ez * N1;
+        const float iscu = 1.f / (__ldg(pff.dens + l) * (float)args.cref);
         const int lb = ez * N1, lt = ez * N1 + N;
         const int lbP = ez > 0 ? lb - 1 : lb, ltP = ez < NeZ - 1 ? lt + 1 : lt;
 #pragma unroll
         for (int m = 0; m < 2; ++m) {
-          const double dB = tm * (double)c.alB[ez] * (Pu[2 * lbP + m] - Pu[2 * lb + m]);
-          const double dT = tm * (double)c.alT[ez] * (Pu[2 * ltP + m] - Pu[2 * lt + m]);
-          const double b = impl_fac * (-(op.Lb[pv] * dB + op.Lt[pv] * dT)) + (Qu[2 * l + m] - Pu[2 * l + m]);
-          bu[2 * l + m] = (float)b;
-          err = fmax(err, fabs(b) / (__ldg(pf.dens + l) * args.cref));
+          // the operator acts on the face jumps only: jumps in FP64, the rest in FP32
+          const float jB = (float)(Pu[2 * lbP + m] - Pu[2 * lb + m]);
+          const float jT = (float)(Pu[2 * ltP + m] - Pu[2 * lt + m]);
+          const float Af = -((float)op.Lb[pv] * tmf * c.alB[ez] * jB + (float)op.Lt[pv] * tmf * c.alT[ez] * jT);
+          const double b = fma(impl_fac, (double)Af, Qu[2 * l + m] - Pu[2 * l + m]);
+          const float bfl = (float)b;
+          bu[2 * l + m] = bfl;
+          err = fmaxf(err, fabsf(bfl) * iscu);
         }
       }
-      err = warp_max(err);
-      if (err <= args.tol || it == 3) break;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) err = fmaxf(err, __shfl_xor_sync(0xffffffffu, err, o));
+      if ((double)err <= args.tol || it == 3) break;
       for (int ez = 0; ez < NeZ; ++ez) {
         float a[N1];
         float rhs[3];
@@ -843,10 +850,11 @@ __global__ void __launch_bounds__(128) k_vi_mixed(const Ops op, const Prof pf, c
     }
     for (int l = lane; l < L; l += 32) {
       const size_t g = gidx(l);
-      qout.v[VMX][g] = Pu[2 * l];
-      qout.v[VMY][g] = Pu[2 * l + 1];
-      tout[VMX][g] = (float)((Pu[2 * l] - Qu[2 * l]) / impl_fac);
-      tout[VMY][g] = (float)((Pu[2 * l + 1] - Qu[2 * l + 1]) / impl_fac);
+      const double dh64 = __ldg(pf.dens + l);
+      qsf[VMX][g] = (float)fma(-dh64, args.Uref, Pu[2 * l]);
+      qsf[VMY][g] = (float)fma(-dh64, args.Vref, Pu[2 * l + 1]);
+      tout[VMX][g] = (float)(Pu[2 * l] - Qu[2 * l]) * (float)args.inv_impl_fac;
+      tout[VMY][g] = (float)(Pu[2 * l + 1] - Qu[2 * l + 1]) * (float)args.inv_impl_fac;
     }
     __syncwarp();
   }
@@ -870,8 +878,8 @@ __global__ void __launch_bounds__(128) k_vi_mixed(const Ops op, const Prof pf, c
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
       const double pnew = c.P[3 * l + m];
-      qout.v[gv[m]][g] = pnew;
-      tout[gv[m]][g] = (float)((pnew - c.Q[3 * l + m]) / impl_fac);
+      qsf[gv[m]][g] = (float)pnew;
+      tout[gv[m]][g] = (float)(pnew - c.Q[3 * l + m]) * (float)args.inv_impl_fac;
     }
   }
   if (lane == 0) {
@@ -882,6 +890,22 @@ __global__ void __launch_bounds__(128) k_vi_mixed(const Ops op, const Prof pf, c
       atomicAdd(cnt + 2, 1ull);
     }
   }
+}
+
+// FP32 deviation copy of a state (DDENS, MOMX - DENS_hyd*Uref, MOMY - DENS_hyd*Vref, MOMZ, DRHOT)
+struct Dev5 { float* v[5]; };
+__global__ void k_to_dev(F5c q, Dev5 out, const double* __restrict__ dens_prof, double Uref, double Vref, int Np,
+                         int N1, size_t nxy, size_t n) {
+  const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n) return;
+  const size_t ke = g / Np;
+  const int ez = (int)(ke / nxy), k = (int)(g - ke * Np) / (N1 * N1);
+  const double dh = dens_prof[ez * N1 + k];
+  out.v[VD][g] = (float)q.v[VD][g];
+  out.v[VMX][g] = (float)fma(-dh, Uref, q.v[VMX][g]);
+  out.v[VMY][g] = (float)fma(-dh, Vref, q.v[VMY][g]);
+  out.v[VMZ][g] = (float)q.v[VMZ][g];
+  out.v[VRT][g] = (float)q.v[VRT][g];
 }
 
 // sums of MOMX, MOMY and DENS over the domain (FP64) for the reference wind
@@ -934,7 +958,7 @@ static int launch_stage_m(int stage, const OpsF& op, const ProfF& pf, const doub
 
 template <int N1>
 static int launch_vi_m(const Ops& op, const Prof& pf, const ProfF& pff, const double* rhinv, const PresSeries& ps,
-                       const F5c& qin, const F5c& z, const float* const* guess, const F5& qout, float* const* tout,
+                       const F5c& qin, const F5c& z, const float* const* guess, float* const* qsf, float* const* tout,
                        int* status, unsigned long long* cnt, const MixViArgs& a, cudaStream_t s) {
   const int per_warp = vi_mixed_doubles<N1>(op.L, op.NeZ);
   const int ncol = op.NeX * op.NeY * N1 * N1;
@@ -944,7 +968,7 @@ static int launch_vi_m(const Ops& op, const Prof& pf, const ProfF& pff, const do
   if (smem > 227 * 1024) return (int)cudaErrorInvalidValue;
   auto kfn = k_vi_mixed<N1>;
   cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  kfn<<<(ncol + wpb - 1) / wpb, 32 * wpb, smem, s>>>(op, pf, pff, rhinv, ps, qin, z, guess, qout, tout, status, cnt,
+  kfn<<<(ncol + wpb - 1) / wpb, 32 * wpb, smem, s>>>(op, pf, pff, rhinv, ps, qin, z, guess, qsf, tout, status, cnt,
                                                        a, ncol);
   return (int)cudaGetLastError();
 }
@@ -954,22 +978,23 @@ static int launch_vi_m(const Ops& op, const Prof& pf, const ProfF& pff, const do
 // =====================================================================================
 struct MixedState {
   size_t n = 0;
-  double* dbuf = nullptr;   // qs (5n) | qi (5n)
-  float* fbuf = nullptr;    // S3 (5n) | SF (5n) | TI (5n) | guess (3n)
+  double* dbuf = nullptr;   // qi (5n): next stage input, FP64
+  float* fbuf = nullptr;    // S3 | SF | TI (5n each) | guess (3n) | QSF (5n) | QNF (5n)
   float* prof = nullptr;    // [4][L]
   double* rhinv = nullptr;  // [L]
-  float** d_ptrs = nullptr; // device arrays of float pointers: TI[5], guess[3]
+  float** d_ptrs = nullptr; // device arrays of float pointers: TI[5], guess[3], QSF[5]
   OpsF opf;
   PresSeries ps;
   double Uref = 0.0, Vref = 0.0;
   bool wind_set = false;
   MlpState* mlp = nullptr;
-  double* qs(int v) { return dbuf + (size_t)v * n; }
-  double* qi(int v) { return dbuf + (size_t)(5 + v) * n; }
+  double* qi(int v) { return dbuf + (size_t)v * n; }
   float* S3(int v) { return fbuf + (size_t)v * n; }
   float* SF(int v) { return fbuf + (size_t)(5 + v) * n; }
   float* TI(int v) { return fbuf + (size_t)(10 + v) * n; }
   float* GU(int v) { return fbuf + (size_t)(15 + v) * n; }
+  float* QSF(int v) { return fbuf + (size_t)(18 + v) * n; }
+  float* QNF(int v) { return fbuf + (size_t)(23 + v) * n; }
 };
 
 void mixed_free(MixedState* m) {
@@ -990,11 +1015,11 @@ static int mixed_setup(fedg_ctx* c) {
   m->n = c->n;
   const int L = c->L;
   cudaError_t e;
-  if ((e = cudaMalloc(&m->dbuf, sizeof(double) * 10 * c->n)) != cudaSuccess ||
-      (e = cudaMalloc(&m->fbuf, sizeof(float) * 18 * c->n)) != cudaSuccess ||
+  if ((e = cudaMalloc(&m->dbuf, sizeof(double) * 5 * c->n)) != cudaSuccess ||
+      (e = cudaMalloc(&m->fbuf, sizeof(float) * 28 * c->n)) != cudaSuccess ||
       (e = cudaMalloc(&m->prof, sizeof(float) * 4 * L)) != cudaSuccess ||
       (e = cudaMalloc(&m->rhinv, sizeof(double) * L)) != cudaSuccess ||
-      (e = cudaMalloc(&m->d_ptrs, sizeof(float*) * 8)) != cudaSuccess) {
+      (e = cudaMalloc(&m->d_ptrs, sizeof(float*) * 13)) != cudaSuccess) {
     mixed_free(m);
     return api_cuda_fail(e, "fedg_update(mixed): allocation");
   }
@@ -1031,12 +1056,13 @@ static int mixed_setup(fedg_ctx* c) {
     pfh[3 * L + l] = (float)(1.0 / hp[2 * L + l]);
     rinv[l] = 1.0 / hp[3 * L + l];
   }
-  float* hptr[8];
+  float* hptr[13];
   for (int v = 0; v < 5; ++v) hptr[v] = m->TI(v);
   for (int v = 0; v < 3; ++v) hptr[5 + v] = m->GU(v);
+  for (int v = 0; v < 5; ++v) hptr[8 + v] = m->QSF(v);
   if ((e = cudaMemcpy(m->prof, pfh.data(), sizeof(float) * 4 * L, cudaMemcpyHostToDevice)) != cudaSuccess ||
       (e = cudaMemcpy(m->rhinv, rinv.data(), sizeof(double) * L, cudaMemcpyHostToDevice)) != cudaSuccess ||
-      (e = cudaMemcpy(m->d_ptrs, hptr, sizeof(float*) * 8, cudaMemcpyHostToDevice)) != cudaSuccess) {
+      (e = cudaMemcpy(m->d_ptrs, hptr, sizeof(float*) * 13, cudaMemcpyHostToDevice)) != cudaSuccess) {
     mixed_free(m);
     return api_cuda_fail(e, "fedg_update(mixed): upload");
   }
@@ -1065,6 +1091,7 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
   std::memset(&B, 0, sizeof(B));
   for (int v = 0; v < 5; ++v) {
     B.qn[v] = q[v];
+    B.qnf[v] = m->QNF(v);
     B.qi[v] = m->qi(v);
     B.S3[v] = m->S3(v);
     B.SF[v] = m->SF(v);
@@ -1091,7 +1118,17 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
   cf.Uref = m->Uref;
   cf.Vref = m->Vref;
   const double impl_fac = gam * o->dt;
-  MixViArgs va{impl_fac, o->tol, 340.0, o->max_iter, 1};
+  MixViArgs va{impl_fac, 1.0 / impl_fac, o->tol, 340.0, m->Uref, m->Vref, o->max_iter, 1};
+  {  // FP32 deviation copy of the incoming state for the first stage-1 tendency
+    F5c qc{{q[0], q[1], q[2], q[3], q[4]}};
+    Dev5 dv{{m->QNF(0), m->QNF(1), m->QNF(2), m->QNF(3), m->QNF(4)}};
+    r = tracked(c, FEDG_K_AUX, [&] {
+      k_to_dev<<<(unsigned)((c->n + 255) / 256), 256, 0, c->stream>>>(qc, dv, c->d_prof, m->Uref, m->Vref, c->Np,
+                                                                     c->N1, c->nxy, c->n);
+      return (int)cudaGetLastError();
+    });
+    if (r) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): deviation copy");
+  }
   if (cudaMemsetAsync(c->d_cnt, 0, sizeof(unsigned long long) * 3, c->stream) != cudaSuccess)
     return api_fail("fedg_update: memset");
   const int filt = c->d.mf_on;
@@ -1107,7 +1144,7 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
   auto vi = [&]() -> int {
     F5c qin{{m->qi(0), m->qi(1), m->qi(2), m->qi(3), m->qi(4)}};
     F5c z{{q[0], q[1], q[2], q[3], q[4]}};
-    F5 qo{{m->qs(0), m->qs(1), m->qs(2), m->qs(3), m->qs(4)}};
+    float* const* qo = m->d_ptrs + 8;
     const float* const* gptr = nullptr;
     if (o->use_guess) {
       const int rg = tracked(c, FEDG_K_MLP, [&] {
@@ -1125,10 +1162,10 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
     });
   };
   for (int step = 0; step < nsteps; ++step) {
-    for (int v = 0; v < 5; ++v) B.qs[v] = q[v];
+    for (int v = 0; v < 5; ++v) B.qsf[v] = m->QNF(v);
     if ((r = stage(1))) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): stage 1");
     if ((r = vi())) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): column solve 2");
-    for (int v = 0; v < 5; ++v) B.qs[v] = m->qs(v);
+    for (int v = 0; v < 5; ++v) B.qsf[v] = m->QSF(v);
     if ((r = stage(2))) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): stage 2");
     if ((r = vi())) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): column solve 3");
     if ((r = stage(3))) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): stage 3");
