@@ -647,6 +647,64 @@ int fedg_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_o
   return nfail;
 }
 
+// ---------------- column-guess network ----------------
+int fedg_guess_create(int levels, int hidden, fedg_guess** out) {
+  if (!out) return fail("fedg_guess_create: null argument");
+  MlpState* m = nullptr;
+  const int r = mlp_create(levels, hidden, &m);
+  if (r) return r == (int)cudaErrorInvalidValue ? fail("fedg_guess_create: levels >= 1 and hidden % 64 == 0 required")
+                                                 : cuda_fail((cudaError_t)r, "fedg_guess_create");
+  *out = reinterpret_cast<fedg_guess*>(m);
+  return 0;
+}
+void fedg_guess_destroy(fedg_guess* g) { mlp_free(reinterpret_cast<MlpState*>(g)); }
+long long fedg_guess_num_params(const fedg_guess* g) {
+  return g ? mlp_num_params(reinterpret_cast<const MlpState*>(g)) : -1;
+}
+int fedg_guess_set_scales(fedg_guess* g, const float in_scale[4], const float out_scale[3]) {
+  if (!g || !in_scale || !out_scale) return fail("fedg_guess_set_scales: null argument");
+  return mlp_set_scales(reinterpret_cast<MlpState*>(g), in_scale, out_scale);
+}
+int fedg_guess_set_params(fedg_guess* g, const float* host, long long n) {
+  if (!g || !host) return fail("fedg_guess_set_params: null argument");
+  const int r = mlp_set_params(reinterpret_cast<MlpState*>(g), host, n, 0);
+  return r ? (r == (int)cudaErrorInvalidValue ? fail("fedg_guess_set_params: wrong parameter count")
+                                              : cuda_fail((cudaError_t)r, "fedg_guess_set_params"))
+           : 0;
+}
+int fedg_guess_get_params(fedg_guess* g, float* host, long long n) {
+  if (!g || !host) return fail("fedg_guess_get_params: null argument");
+  const int r = mlp_get_params(reinterpret_cast<MlpState*>(g), host, n, 0);
+  return r ? (r == (int)cudaErrorInvalidValue ? fail("fedg_guess_get_params: wrong parameter count")
+                                              : cuda_fail((cudaError_t)r, "fedg_guess_get_params"))
+           : 0;
+}
+int fedg_guess_train_step(fedg_guess* g, const float* X, const float* T, int batch, float lr, float* loss) {
+  if (!g || !X || !T || batch < 1) return fail("fedg_guess_train_step: bad argument");
+  const int r = mlp_train_step(reinterpret_cast<MlpState*>(g), X, T, batch, lr, loss, 0);
+  return r ? cuda_fail((cudaError_t)r, "fedg_guess_train_step") : 0;
+}
+int fedg_guess_loss_grad(fedg_guess* g, const float* X, const float* T, int batch, float* loss, float* grad) {
+  if (!g || !X || !T || batch < 1 || !loss) return fail("fedg_guess_loss_grad: bad argument");
+  const int r = mlp_loss_grad(reinterpret_cast<MlpState*>(g), X, T, batch, loss, grad, 0);
+  return r ? cuda_fail((cudaError_t)r, "fedg_guess_loss_grad") : 0;
+}
+int fedg_guess_predict(fedg_guess* g, const float* X, float* Y, int n) {
+  if (!g || !X || !Y || n < 1) return fail("fedg_guess_predict: bad argument");
+  const int r = mlp_predict(reinterpret_cast<MlpState*>(g), X, Y, n, 0);
+  return r ? cuda_fail((cudaError_t)r, "fedg_guess_predict") : 0;
+}
+int fedg_guess_load(fedg_ctx* c, fedg_guess* g) {
+  if (!c) return fail("fedg_guess_load: null ctx");
+  MlpState* m = reinterpret_cast<MlpState*>(g);
+  if (m) {
+    if (mlp_num_params(m) <= 0) return fail("fedg_guess_load: empty network");
+    mlp_set_ready(m, 1);
+  }
+  c->guess = m;
+  return 0;
+}
+
 int fedg_prof_enable(fedg_ctx* c, int on) {
   if (!c) return fail("null ctx");
   c->prof_on = on != 0;

@@ -7,6 +7,7 @@
 #include "fedg_common.cuh"
 #include "fedg_kernels.cuh"
 #include "fedg_mixed.cuh"
+#include "fedg_mlp.cuh"
 
 namespace fedg {
 int api_fail(const std::string& m);
@@ -31,6 +32,7 @@ struct fedg_ctx {
   size_t work_doubles = 0;
   MixedState* mixed = nullptr;
   fedg_tint* upd_tint = nullptr;  // RK buffers of fedg_update, kept between calls
+  MlpState* guess = nullptr;      // column-guess network attached with fedg_guess_load (not owned)
   // kernel timers / launch counters
   bool prof_on = false;
   long long nlaunch[FEDG_K_COUNT] = {};

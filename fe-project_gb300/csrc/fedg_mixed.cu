@@ -987,7 +987,6 @@ struct MixedState {
   PresSeries ps;
   double Uref = 0.0, Vref = 0.0;
   bool wind_set = false;
-  MlpState* mlp = nullptr;
   double* qi(int v) { return dbuf + (size_t)v * n; }
   float* S3(int v) { return fbuf + (size_t)v * n; }
   float* SF(int v) { return fbuf + (size_t)(5 + v) * n; }
@@ -1004,7 +1003,6 @@ void mixed_free(MixedState* m) {
   cudaFree(m->prof);
   cudaFree(m->rhinv);
   cudaFree(m->d_ptrs);
-  mlp_free(m->mlp);
   delete m;
 }
 
@@ -1070,19 +1068,13 @@ static int mixed_setup(fedg_ctx* c) {
   return 0;
 }
 
-MlpState*& ctx_mlp(fedg_ctx* c) {
-  static MlpState* none = nullptr;
-  if (mixed_setup(c) != 0) return none;
-  return c->mixed->mlp;
-}
-
 int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_opts* o, double* iters_out) {
   if (o->eqs != FEDG_HEVI) return api_fail("fedg_update: the mixed-precision path implements HEVI (IMEX ARK232)");
   if (o->max_iter < 1) return api_fail("fedg_update: max_iter must be >= 1");
   int r = mixed_setup(c);
   if (r) return r;
   MixedState* m = c->mixed;
-  if (o->use_guess && !mlp_ready(m->mlp)) return api_fail("fedg_update: use_guess set but no column-guess network is loaded");
+  if (o->use_guess && !mlp_ready(c->guess)) return api_fail("fedg_update: use_guess set but no trained column-guess network is loaded (fedg_guess_load)");
   const double alp = (3.0 + 2.0 * std::sqrt(2.0)) / 6.0, gam = 1.0 - 1.0 / std::sqrt(2.0), del = 1.0 / (2.0 * std::sqrt(2.0));
   MixCoef cf{o->dt, 2.0 * gam, gam, 1.0 - alp, del, alp, del, del, del, gam, 0.0, 0.0};
   const ProfF pff{m->prof, m->prof + c->L, m->prof + 2 * c->L, m->prof + 3 * c->L};
@@ -1148,7 +1140,7 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
     const float* const* gptr = nullptr;
     if (o->use_guess) {
       const int rg = tracked(c, FEDG_K_MLP, [&] {
-        return mlp_infer(m->mlp, c->op, m->qi(0), m->qi(3), m->qi(4), impl_fac, m->GU(0), m->GU(1), m->GU(2), c->stream);
+        return mlp_infer(c->guess, c->op, m->qi(0), m->qi(3), m->qi(4), impl_fac, m->GU(0), m->GU(1), m->GU(2), c->stream);
       });
       if (rg) return rg;
       gptr = (const float* const*)(m->d_ptrs + 5);

@@ -29,6 +29,9 @@ EXPORTED = [
     "fedg_tint_tend_ex", "fedg_tint_tend_im", "fedg_tint_var0", "fedg_tint_store_var0",
     "fedg_tint_store_implicit", "fedg_tint_advance", "fedg_update",
     "fedg_prof_enable", "fedg_prof_reset", "fedg_prof_read",
+    "fedg_guess_create", "fedg_guess_destroy", "fedg_guess_num_params", "fedg_guess_set_scales",
+    "fedg_guess_set_params", "fedg_guess_get_params", "fedg_guess_train_step", "fedg_guess_loss_grad",
+    "fedg_guess_predict", "fedg_guess_load",
 ]
 
 # kernel classes of fedg_prof_read (include/fedg.h)
@@ -97,6 +100,18 @@ def load():
     lib.fedg_tint_store_implicit.argtypes = [_vp, ctypes.c_int, _P5]
     lib.fedg_tint_advance.argtypes = [_vp, ctypes.c_int, _P5]
     lib.fedg_update.argtypes = [_vp, _P5, ctypes.c_int, ctypes.POINTER(UpdateOpts), ctypes.POINTER(ctypes.c_double)]
+    _fp = ctypes.POINTER(ctypes.c_float)
+    lib.fedg_guess_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(_vp)]
+    lib.fedg_guess_destroy.argtypes = [_vp]
+    lib.fedg_guess_num_params.restype = ctypes.c_longlong
+    lib.fedg_guess_num_params.argtypes = [_vp]
+    lib.fedg_guess_set_scales.argtypes = [_vp, _fp, _fp]
+    lib.fedg_guess_set_params.argtypes = [_vp, _fp, ctypes.c_longlong]
+    lib.fedg_guess_get_params.argtypes = [_vp, _fp, ctypes.c_longlong]
+    lib.fedg_guess_train_step.argtypes = [_vp, _vp, _vp, ctypes.c_int, ctypes.c_float, _fp]
+    lib.fedg_guess_loss_grad.argtypes = [_vp, _vp, _vp, ctypes.c_int, _fp, _fp]
+    lib.fedg_guess_predict.argtypes = [_vp, _vp, _vp, ctypes.c_int]
+    lib.fedg_guess_load.argtypes = [_vp, _vp]
     lib.fedg_prof_enable.argtypes = [_vp, ctypes.c_int]
     lib.fedg_prof_reset.argtypes = [_vp]
     lib.fedg_prof_read.argtypes = [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
@@ -310,3 +325,97 @@ class TimeInt:
 
     def advance(self, s, q):
         _check(self.ctx.lib.fedg_tint_advance(self.h, int(s), _p5(q)), "fedg_tint_advance")
+
+
+class Guess:
+    """fedg_guess: the column-guess MLP (levels -> din = 3*levels+1, dout = 3*levels)."""
+
+    def __init__(self, levels: int, hidden: int = 256):
+        self.lib = load()
+        h = _vp()
+        _check(self.lib.fedg_guess_create(int(levels), int(hidden), ctypes.byref(h)), "fedg_guess_create")
+        self.h = h
+        self.levels, self.hidden = levels, hidden
+        self.din, self.dout = 3 * levels + 1, 3 * levels
+        self.n = int(self.lib.fedg_guess_num_params(h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fedg_guess_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def shapes(self):
+        h, di, do = self.hidden, self.din, self.dout
+        return [(h, di), (h,), (h, h), (h,), (do, h), (do,)]
+
+    def set_scales(self, in_scale, out_scale):
+        a = (ctypes.c_float * 4)(*[float(x) for x in in_scale])
+        b = (ctypes.c_float * 3)(*[float(x) for x in out_scale])
+        _check(self.lib.fedg_guess_set_scales(self.h, a, b), "fedg_guess_set_scales")
+        self.in_scale, self.out_scale = list(in_scale), list(out_scale)
+
+    def set_params(self, flat):
+        flat = np.ascontiguousarray(flat, dtype=np.float32)
+        assert flat.size == self.n
+        _check(self.lib.fedg_guess_set_params(self.h, flat.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), self.n),
+               "fedg_guess_set_params")
+
+    def get_params(self):
+        out = np.zeros(self.n, np.float32)
+        _check(self.lib.fedg_guess_get_params(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), self.n),
+               "fedg_guess_get_params")
+        return out
+
+    def init_params(self, seed=0):
+        rng = np.random.default_rng(seed)
+        parts = []
+        for shp in self.shapes():
+            if len(shp) == 2:
+                parts.append((rng.standard_normal(shp) * np.sqrt(2.0 / (shp[0] + shp[1]))).ravel())
+            else:
+                parts.append(np.zeros(shp))
+        self.set_params(np.concatenate(parts).astype(np.float32))
+
+    def train_step(self, X, T, lr=1e-3):
+        loss = ctypes.c_float(0.0)
+        import torch
+
+        torch.cuda.synchronize()
+        _check(self.lib.fedg_guess_train_step(self.h, _ptr(X), _ptr(T), int(X.shape[0]), float(lr),
+                                              ctypes.byref(loss)), "fedg_guess_train_step")
+        return float(loss.value)
+
+    def loss_grad(self, X, T):
+        import torch
+
+        loss = ctypes.c_float(0.0)
+        g = np.zeros(self.n, np.float32)
+        torch.cuda.synchronize()
+        _check(self.lib.fedg_guess_loss_grad(self.h, _ptr(X), _ptr(T), int(X.shape[0]), ctypes.byref(loss),
+                                             g.ctypes.data_as(ctypes.POINTER(ctypes.c_float))),
+               "fedg_guess_loss_grad")
+        return float(loss.value), g
+
+    def predict(self, X):
+        import torch
+
+        Y = torch.empty((X.shape[0], self.dout), dtype=torch.float32, device=X.device)
+        torch.cuda.synchronize()
+        _check(self.lib.fedg_guess_predict(self.h, _ptr(X), _ptr(Y), int(X.shape[0])), "fedg_guess_predict")
+        torch.cuda.synchronize()
+        return Y
+
+    def attach(self, ctx):
+        _check(self.lib.fedg_guess_load(ctx.h, self.h), "fedg_guess_load")
+        ctx._guess = self
+
+
+def detach_guess(ctx):
+    _check(ctx.lib.fedg_guess_load(ctx.h, None), "fedg_guess_load")
+    ctx._guess = None

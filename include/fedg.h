@@ -136,6 +136,31 @@ typedef struct {
 int fedg_update(fedg_ctx* ctx, double* const q[5], int nsteps, const fedg_update_opts* opts,
                 double* iters_out);
 
+/* Column-guess network for the HEVI Newton solve (the learned initial iterate): a GELU MLP
+ * (3L+1) -> hidden -> hidden -> 3L mapping a column's stage input (DDENS', MOMZ, DRHOT' at its
+ * L = NeZ*N1 levels, then impl_fac, each times in_scale[var]) to the implicit increment
+ * Q - q* (times out_scale[var]).  BF16 weights, FP32 accumulation; trained on the GPU by the
+ * library's own forward/backward/Adam kernels.  No counterpart in FElib: FElib's guess is
+ * var0 (rhot_hevi.F90:857-861); with fedg_update(use_guess) the plain Newton solve still
+ * runs to tol from this iterate, so the network only changes how many solves are needed.
+ * X, T, Y are device arrays (row per sample, FP32); parameters in host memory, logical order
+ * W1 (hidden x din) | b1 | W2 | b2 | W3 (dout x hidden) | b3. */
+typedef struct fedg_guess fedg_guess;
+int fedg_guess_create(int levels, int hidden, fedg_guess** out);
+void fedg_guess_destroy(fedg_guess* g);
+long long fedg_guess_num_params(const fedg_guess* g);
+int fedg_guess_set_scales(fedg_guess* g, const float in_scale[4], const float out_scale[3]);
+int fedg_guess_set_params(fedg_guess* g, const float* host, long long n);
+int fedg_guess_get_params(fedg_guess* g, float* host, long long n);
+/* one Adam step (beta 0.9/0.999, eps 1e-8) on the mean-square loss of a batch */
+int fedg_guess_train_step(fedg_guess* g, const float* X, const float* T, int batch, float lr, float* loss);
+/* loss and gradient (host, logical order) without updating the parameters */
+int fedg_guess_loss_grad(fedg_guess* g, const float* X, const float* T, int batch, float* loss, float* grad);
+/* inference through the BF16 tensor-core GEMM path */
+int fedg_guess_predict(fedg_guess* g, const float* X, float* Y, int n);
+/* attach (g != NULL) or detach (g == NULL) the network used by fedg_update(use_guess = 1) */
+int fedg_guess_load(fedg_ctx* ctx, fedg_guess* g);
+
 /* Kernel timers: the analogue of FElib's PROF_rapstart/PROF_rapend regions
  * (e.g. 'ATM_DYN_cal_vi', 'cal_dyn_tend_interior'; scale_prof of the SCALE library).
  * When enabled, every launch of the context records a pair of CUDA events on the context
