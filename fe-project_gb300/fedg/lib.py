@@ -31,7 +31,7 @@ EXPORTED = [
     "fedg_prof_enable", "fedg_prof_reset", "fedg_prof_read",
     "fedg_guess_create", "fedg_guess_destroy", "fedg_guess_num_params", "fedg_guess_set_scales",
     "fedg_guess_set_params", "fedg_guess_get_params", "fedg_guess_train_step", "fedg_guess_loss_grad",
-    "fedg_guess_predict", "fedg_guess_load",
+    "fedg_guess_predict", "fedg_guess_load", "fedg_cal_tend_ex_noalloc",
 ]
 
 # kernel classes of fedg_prof_read (include/fedg.h)
@@ -83,6 +83,7 @@ def load():
     lib.fedg_set_base_state.argtypes = [_vp] + [_vp] * 9
     lib.fedg_drhot2pres.argtypes = [_vp, _vp, _vp, _vp]
     lib.fedg_cal_tend_ex.argtypes = [_vp, ctypes.c_void_p * 16, _P5, ctypes.c_int]
+    lib.fedg_cal_tend_ex_noalloc.argtypes = [_vp, ctypes.c_void_p * 16, _P5, ctypes.c_int]
     lib.fedg_cal_vi.argtypes = [_vp, ctypes.c_void_p * 12, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                 ctypes.c_double, _P5, _vp]
     lib.fedg_modalfilter.argtypes = [_vp, _P5]

@@ -92,6 +92,19 @@ int fedg_drhot2pres(fedg_ctx* ctx, const double* DRHOT, double* PRES, double* DP
  * from the registered ones.  DPRES_ may be NULL: it is then formed from DRHOT_ inside the kernel. */
 int fedg_cal_tend_ex(fedg_ctx* ctx, const double* const in[16], double* const out[5], int eqs);
 
+/* fedg_cal_tend_ex without any device allocation.  No counterpart in the reference: FElib
+ * passes DPRES in, and fedg_cal_tend_ex allocates a scratch field on first use when it forms
+ * DPRES itself.  This variant is for callers that cannot allow a cudaMalloc once their set-up is
+ * over (a Fortran model whose device memory belongs to its OpenACC runtime, or any host whose
+ * device allocator has already claimed the memory): it forms DPRES in a static device array of
+ * 2,097,152 doubles (16 MiB, held by every GPU that loads the library) and returns < 0 with a
+ * message if Np*Ne exceeds that.  Same arguments as fedg_cal_tend_ex (in[5] is ignored); the
+ * base state must already be registered with fedg_set_base_state.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress), so make that first call before
+ * any stream capture.  All calls share the one array: calls whose kernels overlap on the GPU
+ * (two contexts, two streams) race on it and must be ordered by the caller. */
+int fedg_cal_tend_ex_noalloc(fedg_ctx* ctx, const double* const in[16], double* const out[5], int eqs);
+
 /* atm_dyn_nonhydro3d_cal_vi (driver_nonhydro3d.F90:201-250; rhot_hevi.F90:772-965).
  *   in[12]  = DDENS_, MOMX_, MOMY_, MOMZ_, DRHOT_, DENS_hyd, PRES_hyd,
  *             DDENS0_, MOMX0_, MOMY0_, MOMZ0_, DRHOT0_       (Rtot/CVtot/CPtot: registered)
