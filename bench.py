@@ -169,6 +169,34 @@ def fp64_dgemm_tflops(torch, dev):
     return 2.0 * n ** 3 / (best * 1e-3) / 1e12
 
 
+def _timed_update(ctx, torch, stream, qd, steps, opts):
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    nfail, its = ctx.update(qd, steps, sync=False, **opts)
+    e1.record(stream)
+    ctx.sync()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1), nfail, its
+
+
+def _full_field_errors(np, got, ref, dens_hyd_norm_sq, dens_hyd, therm_hyd):
+    """rel L2 per variable of DENS, MOMX, MOMY, MOMZ, RHOT (momentum against at least 1 m/s of
+    hydrostatic momentum) between two device states, computed on the device."""
+    out = {}
+    names = ["DENS", "MOMX", "MOMY", "MOMZ", "RHOT"]
+    for v, nm in enumerate(names):
+        d = float((got[v] - ref[v]).double().norm().item())
+        if v == 0:
+            den = float((ref[0] + dens_hyd).norm().item())
+        elif v == 4:
+            den = float((ref[4] + therm_hyd).norm().item())
+        else:
+            den = max(float(ref[v].norm().item()), dens_hyd_norm_sq ** 0.5)
+        out[nm] = d / den
+    return out
+
+
 def run_fedg(args):
     import numpy as np
     import torch
@@ -192,35 +220,43 @@ def run_fedg(args):
         case = case.scaled(32, 32, 16)
     path = args.path
     prec = fl.PREC_MIXED if path == "mixed" else fl.PREC_FP64
+    use_guess = path == "mixed" and bool(args.guess)
+    net, ginfo = None, None
+    if use_guess:
+        # the C5 column network (128 levels: 385 -> 256 -> 256 -> 384), trained on the GPU with the
+        # library's kernels on (stage input, converged increment) pairs of the plain solver on a
+        # 16x16x16-element slice of the same geometry, 8 noise/wind seeds
+        from fedg import guess
+
+        t0 = time.perf_counter()
+        net, ginfo = guess.build_guess(cases.C5().scaled(16, 16, 16), DT_STABLE, seeds=range(100, 108), nsteps=3,
+                                       per_stage_keep=4096, train_steps=args.train_steps, batch=4096, lr=1e-3)
+        ginfo["build_s"] = time.perf_counter() - t0
     q, b = cases.initial_state(case)
     ctx = fl.Context(case, device=local)
     ctx.set_base_state(b["dens_hyd"], b["pres_hyd"], b["therm_hyd"])
-    dens_norm = float(np.linalg.norm(b["dens_hyd"]))
-    therm_norm = float(np.linalg.norm(b["therm_hyd"]))
+    dens_hyd = ctx.tensor(b["dens_hyd"])
+    therm_hyd = ctx.tensor(b["therm_hyd"])
+    dnorm2 = float((dens_hyd * dens_hyd).sum().item())
     del b
     qd = [ctx.tensor(a) for a in q]
     q_host = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in q]
     del q
+    if net is not None:
+        net.attach(ctx)
     stream = torch.cuda.ExternalStream(ctx.stream_handle)
-    opts = dict(prec=prec, dt=DT_STABLE, max_iter=20, tol=1e-10, use_guess=(path == "mixed" and args.guess))
+    opts = dict(prec=prec, dt=DT_STABLE, max_iter=20, tol=1e-10, use_guess=use_guess)
 
     # warm-up
-    nfail_w, its_w = ctx.update(qd, args.warmup, **opts)
-    # timed region: K steps of the whole domain, inputs (5.4 GB state) larger than L2
+    ctx.update(qd, args.warmup, **opts)
+    # timed region: K steps of the whole domain; the inputs (FP64 state 5.4 GB) are larger than L2
     fl.prof_reset(ctx)
     fl.prof_enable(ctx, True)
     clk = Clocks(local)
     clk.start()
     if world > 1:
         dist.barrier()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    nfail, its = ctx.update(qd, args.steps, sync=False, **opts)
-    e1.record(stream)
-    ctx.sync()
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
+    ms, nfail, its = _timed_update(ctx, torch, stream, qd, args.steps, opts)
     clocks = clk.stop()
     fl.prof_enable(ctx, False)
     prof = fl.prof_read(ctx)
@@ -241,11 +277,12 @@ def run_fedg(args):
         "vi_fp64": 8 * (5 + 5 + 5),          # q*, var0 in; tend_im out
         "tend_fp64": 8 * (6 + 5),            # 5 fields + DPRES in; 5 tendencies out
         "rk": 8 * 20,                        # general IMEX advance (upper bound of the stage kinds)
-        # fused stage kernels, mean of the three: S1 q^n in -> q*_2, S3, SF out (120 B);
-        # S2 Q_2, t_im, q^n, S3, SF in -> q*_3, SF out (200 B); S3 Q_3, t_im, q^n, SF in -> q^n+1 (160 B)
-        "stage_mixed": 160,
-        # column solve: q*, var0 in (FP64) -> Q (FP64), t_im (FP32) out
-        "vi_mixed": 8 * 5 + 8 * 5 + 8 * 5 + 4 * 5,
+        # fused stage kernels, mean of the three (FP32 deviation state in, FP64 q^n / q* ):
+        # S1 q^n(f32) + q^n(f64) in -> q*_2, S3, SF out; S2 Q_2(f32), t_im, q^n, S3, SF in -> q*_3, SF out;
+        # S3 Q_3(f32), t_im, q^n, SF in -> q^n+1 (f64) + its f32 copy out
+        "stage_mixed": (20 + 40 + 40 + 20 + 20 + 20 + 20 + 40 + 20 + 20 + 40 + 20 + 20 + 40 + 20 + 40 + 20) / 3,
+        # column solve: q*, var0 in (FP64) -> Q (FP32 deviation copy), t_im (FP32) out
+        "vi_mixed": 8 * 5 + 8 * 5 + 4 * 5 + 4 * 5,
         "filter": 8 * 10, "drhot2pres": 8 * 2, "mlp": 0, "aux": 0,
     }
     avg_ms = ktime / max(klaunch, 1)
@@ -260,39 +297,49 @@ def run_fedg(args):
     e2e = None
     if rank == 0 and not args.no_e2e:
         ke = max(1, min(args.steps, 2))
+        q_e = [torch.empty_like(t) for t in qd]
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(ke):
-            for dst, src in zip(qd, q_host):
+            for dst, src in zip(q_e, q_host):
                 dst.copy_(src, non_blocking=True)
             torch.cuda.synchronize()
-            ctx.update(qd, 1, sync=False, **opts)
+            ctx.update(q_e, 1, sync=False, **opts)
             ctx.sync()
-            for dst, src in zip(q_host, qd):
+            for dst, src in zip(q_host, q_e):
                 dst.copy_(src, non_blocking=True)
             torch.cuda.synchronize()
         t1 = time.perf_counter()
         nb = sum(t.numel() * 8 for t in qd)
         e2e = {"value": dofs_stage * ke / (t1 - t0), "unit": UNIT, "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb,
                "steps": ke}
+        del q_e
 
-    plain = None
+    # the same path without the learned guess, and the plain FP64 path, on the same state
+    noguess, plain, acc = None, None, None
+    if rank == 0 and use_guess:
+        o2 = dict(opts, use_guess=False)
+        ms2, nf2, its2 = _timed_update(ctx, torch, stream, qd, args.steps, o2)
+        noguess = {"value": dofs_stage * args.steps / (ms2 * 1e-3), "unit": UNIT, "ms_per_step": ms2 / args.steps,
+                   "mean_newton_solves": its2, "nonconverged_columns": nf2}
     if rank == 0 and prec != fl.PREC_FP64 and not args.no_plain:
-        # the plain FP64 path on the same workload and state (FElib's algorithm in FP64 on the GPU)
-        o64 = dict(opts)
-        o64.update(prec=fl.PREC_FP64, use_guess=False)
-        ctx.update(qd, 1, **o64)
-        torch.cuda.synchronize()
-        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        kp = 2
-        p0.record(stream)
-        nf64, its64 = ctx.update(qd, kp, sync=False, **o64)
-        p1.record(stream)
-        ctx.sync()
-        torch.cuda.synchronize()
-        pms = p0.elapsed_time(p1)
-        plain = {"value": dofs_stage * kp / (pms * 1e-3), "unit": UNIT, "ms_per_step": pms / kp, "steps": kp,
+        # FElib's algorithm in FP64 on the GPU from the same initial state, and the error of the
+        # timed path against it after the same number of steps
+        q_ref = [torch.empty_like(t) for t in qd]
+        q_mix = [torch.empty_like(t) for t in qd]
+        for a, h in zip(q_ref, q_host):
+            a.copy_(h)
+        for a, h in zip(q_mix, q_host):
+            a.copy_(h)
+        ncmp = args.compare_steps
+        o64 = dict(opts, prec=fl.PREC_FP64, use_guess=False)
+        ctx.update(q_ref, max(ncmp - 2, 0), **o64)
+        pms, nf64, its64 = _timed_update(ctx, torch, stream, q_ref, 2, o64)
+        plain = {"value": dofs_stage * 2 / (pms * 1e-3), "unit": UNIT, "ms_per_step": pms / 2, "steps": 2,
                  "mean_newton_solves": its64, "nonconverged_columns": nf64}
+        ctx.update(q_mix, ncmp, **opts)
+        acc = {"steps": ncmp, "rel_l2_vs_plain_fp64": _full_field_errors(np, q_mix, q_ref, dnorm2, dens_hyd, therm_hyd)}
+        del q_ref, q_mix
 
     cb = None
     if rank == 0 and not args.no_cpu:
@@ -306,7 +353,7 @@ def run_fedg(args):
             "vs_baseline": None, "dtype": "f64" if prec == fl.PREC_FP64 else "f32+f64", "data": "synthetic",
             "config": {"workload": f"{case.name}: p=7 {case.NeX}x{case.NeY}x{case.NeZ} elements, HEVI IMEX-ARK232, "
                                    f"constBVFreq N=0.01, +-0.1K noise below 500 m, u=5 m/s",
-                       "path": "plain_fp64" if prec == fl.PREC_FP64 else ("learned+fp32" if opts["use_guess"] else "fp32"),
+                       "path": "plain_fp64" if prec == fl.PREC_FP64 else ("learned+fp32" if use_guess else "fp32"),
                        "dt": DT_STABLE, "dt_baseline": 0.5, "newton_tol": opts["tol"], "newton_max_iter": opts["max_iter"],
                        "mean_newton_solves": its, "nonconverged_columns": nfail, "finite": finite,
                        "l2": "inputs larger than L2 (FP64 state %.1f GB)" % (case.dofs * 8 / 1e9),
@@ -315,8 +362,11 @@ def run_fedg(args):
             "roofline_fp64": {"bound": "fp64", "peak_tflops": fp64_tf, "peak_source": "measured cuBLAS DGEMM 4096^3"},
             "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items() if v[1]},
             "cpu_baseline": cb, "e2e": e2e, "gpu_launches": gpu_launches, "clocks": clocks,
+            "guess_training": ginfo,
+            "fp32_without_guess": noguess,
             "plain_fp64": plain,
             "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
+            "accuracy": acc,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -332,7 +382,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["fedg", "reference"], default="fedg")
     ap.add_argument("--path", choices=["mixed", "fp64"], default=os.environ.get("FEDG_BENCH_PATH", "mixed"))
-    ap.add_argument("--guess", type=int, default=0)
+    ap.add_argument("--guess", type=int, default=1)
+    ap.add_argument("--train-steps", type=int, default=2000)
+    ap.add_argument("--compare-steps", type=int, default=4,
+                    help="steps of the accuracy comparison against the plain FP64 path")
     ap.add_argument("--small", action="store_true", help="32x32x16 elements instead of 128x128x16 (profiling)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")

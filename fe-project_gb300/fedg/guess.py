@@ -115,8 +115,12 @@ def generate(base_case, seeds, dt, nsteps, per_stage_keep, spinup=0):
     Xs, Ys, sp = [], [], []
     for sd in seeds:
         rng = np.random.default_rng(sd)
-        case = random_case(base_case, rng) if base_case.bubble else dataclasses.replace(
-            base_case, noise=dict(base_case.noise, seed=int(sd)))
+        if base_case.bubble:
+            case = random_case(base_case, rng)
+        else:  # noise-driven workloads: new noise field, amplitude and background wind per seed
+            case = dataclasses.replace(base_case, u0=rng.uniform(0.0, 10.0),
+                                       noise=dict(base_case.noise, seed=int(sd),
+                                                  amp=base_case.noise.get("amp", 0.1) * rng.uniform(0.5, 2.0)))
         q, b = cases.initial_state(case)
         ps = capture_pairs(case, q, b, dt, nsteps, keep=per_stage_keep, seed=int(sd))
         Xs.append(ps.X)
