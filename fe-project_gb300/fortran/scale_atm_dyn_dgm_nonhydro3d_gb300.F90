@@ -1,0 +1,216 @@
+!-------------------------------------------------------------------------------
+!> module FElib / Fluid dyn solver / Atmosphere / Nonhydrostatic model / GB300 binding
+!!
+!! ISO_C_BINDING shim that points FElib's cal_tend_ex / cal_vi procedure pointers
+!! (FElib/src/fluid_dyn_solver/scale_atm_dyn_dgm_driver_nonhydro3d.F90:152-250) at the
+!! GB300 library libfedg.so (C ABI: include/fedg.h).  The arrays are the driver's own
+!! OpenACC-resident fields; their device addresses are passed under host_data use_device.
+!! Not compiled in this repository (no Fortran compiler in its build image); built with the
+!! model by a maintainer, linked with -lfedg.
+!-------------------------------------------------------------------------------
+#include "scaleFElib.h"
+module scale_atm_dyn_dgm_nonhydro3d_gb300
+  use iso_c_binding
+  use scale_precision
+  use scale_prc, only: PRC_abort
+  use scale_const, only: GRAV => CONST_GRAV, Rdry => CONST_Rdry, CPdry => CONST_CPdry, &
+                         CVdry => CONST_CVdry, PRES00 => CONST_PRE00
+  use scale_element_base, only: ElementBase2D, ElementBase3D
+  use scale_element_operation_base, only: ElementOperationBase3D
+  use scale_localmesh_2d, only: LocalMesh2D
+  use scale_localmesh_3d, only: LocalMesh3D
+  use scale_sparsemat, only: SparseMat
+  implicit none
+  private
+
+  public :: atm_dyn_dgm_nonhydro3d_gb300_Init
+  public :: atm_dyn_dgm_nonhydro3d_gb300_Final
+  public :: atm_dyn_dgm_nonhydro3d_gb300_cal_tend_heve
+  public :: atm_dyn_dgm_nonhydro3d_gb300_cal_tend_hevi
+  public :: atm_dyn_dgm_nonhydro3d_gb300_cal_vi
+
+  integer(c_int), parameter :: FEDG_HEVE = 0, FEDG_HEVI = 1
+
+  type, bind(C) :: fedg_mesh_desc
+    integer(c_int) :: porder, NeX, NeY, NeZ
+    real(c_double) :: xmin, xmax, ymin, ymax, zmin, zmax
+    integer(c_int) :: periodic_x, periodic_y
+    real(c_double) :: grav, rdry, cpdry, cvdry, pres00
+    integer(c_int) :: mf_on
+    real(c_double) :: mf_etac_h, mf_alpha_h
+    integer(c_int) :: mf_order_h
+    real(c_double) :: mf_etac_v, mf_alpha_v
+    integer(c_int) :: mf_order_v
+    integer(c_int) :: device
+  end type
+
+  interface
+    integer(c_int) function fedg_ctx_create(desc, ctx) bind(C, name="fedg_ctx_create")
+      import :: c_int, c_ptr, fedg_mesh_desc
+      type(fedg_mesh_desc), intent(in) :: desc
+      type(c_ptr), intent(out) :: ctx
+    end function
+    subroutine fedg_ctx_destroy(ctx) bind(C, name="fedg_ctx_destroy")
+      import :: c_ptr
+      type(c_ptr), value :: ctx
+    end subroutine
+    integer(c_int) function fedg_cal_tend_ex(ctx, inp, outp, eqs) bind(C, name="fedg_cal_tend_ex")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+      type(c_ptr), intent(in) :: inp(16), outp(5)
+      integer(c_int), value :: eqs
+    end function
+    integer(c_int) function fedg_cal_vi(ctx, inp, impl_fac, dt, max_iter, tol, outp, status) &
+        bind(C, name="fedg_cal_vi")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      type(c_ptr), intent(in) :: inp(12), outp(5)
+      real(c_double), value :: impl_fac, dt, tol
+      integer(c_int), value :: max_iter
+      type(c_ptr), value :: status
+    end function
+    integer(c_int) function fedg_synchronize(ctx) bind(C, name="fedg_synchronize")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+    end function
+  end interface
+
+  type(c_ptr), save :: ctx = c_null_ptr
+  integer, save :: vi_max_iter = 1           ! 1: FElib's single linearised solve
+  real(RP), save :: vi_tol = 1.0E-10_RP
+
+contains
+
+  !> Create the library context from the cube-domain mesh (call once, after the mesh).
+  subroutine atm_dyn_dgm_nonhydro3d_gb300_Init( porder, NeX, NeY, NeZ, dom_xmin, dom_xmax, &
+      dom_ymin, dom_ymax, dom_zmin, dom_zmax, modalfilter_flag, max_iter, tol )
+    integer, intent(in) :: porder, NeX, NeY, NeZ
+    real(RP), intent(in) :: dom_xmin, dom_xmax, dom_ymin, dom_ymax, dom_zmin, dom_zmax
+    logical, intent(in) :: modalfilter_flag
+    integer, intent(in), optional :: max_iter
+    real(RP), intent(in), optional :: tol
+    type(fedg_mesh_desc) :: d
+    integer(c_int) :: ierr
+    d = fedg_mesh_desc(porder, NeX, NeY, NeZ, dom_xmin, dom_xmax, dom_ymin, dom_ymax, dom_zmin, dom_zmax, &
+                       1, 1, GRAV, Rdry, CPdry, CVdry, PRES00, merge(1, 0, modalfilter_flag),          &
+                       2.0_RP/3.0_RP, 36.0_RP, 16, 2.0_RP/3.0_RP, 36.0_RP, 16, 0)
+    ierr = fedg_ctx_create(d, ctx)
+    if (ierr < 0) call PRC_abort
+    if (present(max_iter)) vi_max_iter = max_iter
+    if (present(tol)) vi_tol = tol
+  end subroutine atm_dyn_dgm_nonhydro3d_gb300_Init
+
+  subroutine atm_dyn_dgm_nonhydro3d_gb300_Final()
+    if (c_associated(ctx)) call fedg_ctx_destroy(ctx)
+    ctx = c_null_ptr
+  end subroutine atm_dyn_dgm_nonhydro3d_gb300_Final
+
+  !> atm_dyn_nonhydro3d_cal_tend_ex for EQS_TYPE = "NONHYDRO3D_HEVE_GB300"
+  subroutine atm_dyn_dgm_nonhydro3d_gb300_cal_tend_heve( &
+    DENS_dt, MOMX_dt, MOMY_dt, MOMZ_dt, RHOT_dt, DDENS_, MOMX_, MOMY_, MOMZ_, THERM_, DPRES_, &
+    DENS_hyd, PRES_hyd, PRES_hyd_ref, THERM_hyd, CORIOLIS, Rtot, CVtot, CPtot, DPhydDx, DPhydDy, &
+    element3D_operation, Dx, Dy, Dz, Sx, Sy, Sz, Lift, lmesh, elem, lmesh2D, elem2D )
+    class(LocalMesh3D), intent(in) :: lmesh
+    class(ElementBase3D), intent(in) :: elem
+    class(LocalMesh2D), intent(in) :: lmesh2D
+    class(ElementBase2D), intent(in) :: elem2D
+    class(ElementOperationBase3D), intent(in) :: element3D_operation
+    type(SparseMat), intent(in) :: Dx, Dy, Dz, Sx, Sy, Sz, Lift
+    real(RP), intent(out), target :: DENS_dt(elem%Np,lmesh%NeA), MOMX_dt(elem%Np,lmesh%NeA), &
+      MOMY_dt(elem%Np,lmesh%NeA), MOMZ_dt(elem%Np,lmesh%NeA), RHOT_dt(elem%Np,lmesh%NeA)
+    real(RP), intent(in), target :: DDENS_(elem%Np,lmesh%NeA), MOMX_(elem%Np,lmesh%NeA), &
+      MOMY_(elem%Np,lmesh%NeA), MOMZ_(elem%Np,lmesh%NeA), THERM_(elem%Np,lmesh%NeA),      &
+      DPRES_(elem%Np,lmesh%NeA), DENS_hyd(elem%Np,lmesh%NeA), PRES_hyd(elem%Np,lmesh%NeA), &
+      PRES_hyd_ref(elem%Np,lmesh%NeA), THERM_hyd(elem%Np,lmesh%NeA),                       &
+      CORIOLIS(elem2D%Np,lmesh2D%NeA), Rtot(elem%Np,lmesh%NeA), CVtot(elem%Np,lmesh%NeA),   &
+      CPtot(elem%Np,lmesh%NeA), DPhydDx(elem%Np,lmesh%NeA), DPhydDy(elem%Np,lmesh%NeA)
+    call cal_tend( FEDG_HEVE )
+  contains
+    subroutine cal_tend( eqs )
+      integer(c_int), intent(in) :: eqs
+      type(c_ptr) :: inp(16), outp(5)
+      integer(c_int) :: ierr
+      !$acc host_data use_device(DENS_dt, MOMX_dt, MOMY_dt, MOMZ_dt, RHOT_dt, DDENS_, MOMX_, MOMY_, &
+      !$acc   MOMZ_, THERM_, DPRES_, DENS_hyd, PRES_hyd, PRES_hyd_ref, THERM_hyd, CORIOLIS, Rtot,      &
+      !$acc   CVtot, CPtot, DPhydDx, DPhydDy)
+      inp = [ c_loc(DDENS_), c_loc(MOMX_), c_loc(MOMY_), c_loc(MOMZ_), c_loc(THERM_), c_loc(DPRES_), &
+              c_loc(DENS_hyd), c_loc(PRES_hyd), c_loc(PRES_hyd_ref), c_loc(THERM_hyd), c_loc(CORIOLIS), &
+              c_loc(Rtot), c_loc(CVtot), c_loc(CPtot), c_loc(DPhydDx), c_loc(DPhydDy) ]
+      outp = [ c_loc(DENS_dt), c_loc(MOMX_dt), c_loc(MOMY_dt), c_loc(MOMZ_dt), c_loc(RHOT_dt) ]
+      !$acc end host_data
+      ierr = fedg_cal_tend_ex( ctx, inp, outp, eqs )
+      if (ierr < 0) call PRC_abort
+      ierr = fedg_synchronize( ctx )   ! FElib's next statement may touch the tendencies on another queue
+    end subroutine cal_tend
+  end subroutine atm_dyn_dgm_nonhydro3d_gb300_cal_tend_heve
+
+  !> atm_dyn_nonhydro3d_cal_tend_ex for EQS_TYPE = "NONHYDRO3D_HEVI_GB300"
+  subroutine atm_dyn_dgm_nonhydro3d_gb300_cal_tend_hevi( &
+    DENS_dt, MOMX_dt, MOMY_dt, MOMZ_dt, RHOT_dt, DDENS_, MOMX_, MOMY_, MOMZ_, THERM_, DPRES_, &
+    DENS_hyd, PRES_hyd, PRES_hyd_ref, THERM_hyd, CORIOLIS, Rtot, CVtot, CPtot, DPhydDx, DPhydDy, &
+    element3D_operation, Dx, Dy, Dz, Sx, Sy, Sz, Lift, lmesh, elem, lmesh2D, elem2D )
+    class(LocalMesh3D), intent(in) :: lmesh
+    class(ElementBase3D), intent(in) :: elem
+    class(LocalMesh2D), intent(in) :: lmesh2D
+    class(ElementBase2D), intent(in) :: elem2D
+    class(ElementOperationBase3D), intent(in) :: element3D_operation
+    type(SparseMat), intent(in) :: Dx, Dy, Dz, Sx, Sy, Sz, Lift
+    real(RP), intent(out), target :: DENS_dt(elem%Np,lmesh%NeA), MOMX_dt(elem%Np,lmesh%NeA), &
+      MOMY_dt(elem%Np,lmesh%NeA), MOMZ_dt(elem%Np,lmesh%NeA), RHOT_dt(elem%Np,lmesh%NeA)
+    real(RP), intent(in), target :: DDENS_(elem%Np,lmesh%NeA), MOMX_(elem%Np,lmesh%NeA), &
+      MOMY_(elem%Np,lmesh%NeA), MOMZ_(elem%Np,lmesh%NeA), THERM_(elem%Np,lmesh%NeA),      &
+      DPRES_(elem%Np,lmesh%NeA), DENS_hyd(elem%Np,lmesh%NeA), PRES_hyd(elem%Np,lmesh%NeA), &
+      PRES_hyd_ref(elem%Np,lmesh%NeA), THERM_hyd(elem%Np,lmesh%NeA),                       &
+      CORIOLIS(elem2D%Np,lmesh2D%NeA), Rtot(elem%Np,lmesh%NeA), CVtot(elem%Np,lmesh%NeA),   &
+      CPtot(elem%Np,lmesh%NeA), DPhydDx(elem%Np,lmesh%NeA), DPhydDy(elem%Np,lmesh%NeA)
+    type(c_ptr) :: inp(16), outp(5)
+    integer(c_int) :: ierr
+    !$acc host_data use_device(DENS_dt, MOMX_dt, MOMY_dt, MOMZ_dt, RHOT_dt, DDENS_, MOMX_, MOMY_, &
+    !$acc   MOMZ_, THERM_, DPRES_, DENS_hyd, PRES_hyd, PRES_hyd_ref, THERM_hyd, CORIOLIS, Rtot,      &
+    !$acc   CVtot, CPtot, DPhydDx, DPhydDy)
+    inp = [ c_loc(DDENS_), c_loc(MOMX_), c_loc(MOMY_), c_loc(MOMZ_), c_loc(THERM_), c_loc(DPRES_), &
+            c_loc(DENS_hyd), c_loc(PRES_hyd), c_loc(PRES_hyd_ref), c_loc(THERM_hyd), c_loc(CORIOLIS), &
+            c_loc(Rtot), c_loc(CVtot), c_loc(CPtot), c_loc(DPhydDx), c_loc(DPhydDy) ]
+    outp = [ c_loc(DENS_dt), c_loc(MOMX_dt), c_loc(MOMY_dt), c_loc(MOMZ_dt), c_loc(RHOT_dt) ]
+    !$acc end host_data
+    ierr = fedg_cal_tend_ex( ctx, inp, outp, FEDG_HEVI )
+    if (ierr < 0) call PRC_abort
+    ierr = fedg_synchronize( ctx )
+  end subroutine atm_dyn_dgm_nonhydro3d_gb300_cal_tend_hevi
+
+  !> atm_dyn_nonhydro3d_cal_vi for EQS_TYPE = "NONHYDRO3D_HEVI_GB300"
+  subroutine atm_dyn_dgm_nonhydro3d_gb300_cal_vi( &
+    DENS_dt, MOMX_dt, MOMY_dt, MOMZ_dt, RHOT_dt, DDENS_, MOMX_, MOMY_, MOMZ_, THERM_, DENS_hyd, PRES_hyd, &
+    DDENS0_, MOMX0_, MOMY0_, MOMZ0_, THERM0_, Rtot, CVtot, CPtot, element3D_operation, Dz, Lift,          &
+    impl_fac, dt, lmesh, elem, lmesh2D, elem2D )
+    class(LocalMesh3D), intent(in) :: lmesh
+    class(ElementBase3D), intent(in) :: elem
+    class(LocalMesh2D), intent(in) :: lmesh2D
+    class(ElementBase2D), intent(in) :: elem2D
+    class(ElementOperationBase3D), intent(in) :: element3D_operation
+    class(SparseMat), intent(in) :: Dz, Lift
+    real(RP), intent(out), target :: DENS_dt(elem%Np,lmesh%NeA), MOMX_dt(elem%Np,lmesh%NeA), &
+      MOMY_dt(elem%Np,lmesh%NeA), MOMZ_dt(elem%Np,lmesh%NeA), RHOT_dt(elem%Np,lmesh%NeA)
+    real(RP), intent(in), target :: DDENS_(elem%Np,lmesh%NeA), MOMX_(elem%Np,lmesh%NeA),        &
+      MOMY_(elem%Np,lmesh%NeA), MOMZ_(elem%Np,lmesh%NeA), THERM_(elem%Np,lmesh%NeA),             &
+      DENS_hyd(elem%Np,lmesh%NeA), PRES_hyd(elem%Np,lmesh%NeA), DDENS0_(elem%Np,lmesh%NeA),      &
+      MOMX0_(elem%Np,lmesh%NeA), MOMY0_(elem%Np,lmesh%NeA), MOMZ0_(elem%Np,lmesh%NeA),          &
+      THERM0_(elem%Np,lmesh%NeA), Rtot(elem%Np,lmesh%NeA), CVtot(elem%Np,lmesh%NeA),            &
+      CPtot(elem%Np,lmesh%NeA)
+    real(RP), intent(in) :: impl_fac, dt
+    type(c_ptr) :: inp(12), outp(5)
+    integer(c_int) :: ierr
+    !$acc host_data use_device(DENS_dt, MOMX_dt, MOMY_dt, MOMZ_dt, RHOT_dt, DDENS_, MOMX_, MOMY_, MOMZ_, &
+    !$acc   THERM_, DENS_hyd, PRES_hyd, DDENS0_, MOMX0_, MOMY0_, MOMZ0_, THERM0_)
+    inp = [ c_loc(DDENS_), c_loc(MOMX_), c_loc(MOMY_), c_loc(MOMZ_), c_loc(THERM_), c_loc(DENS_hyd), &
+            c_loc(PRES_hyd), c_loc(DDENS0_), c_loc(MOMX0_), c_loc(MOMY0_), c_loc(MOMZ0_), c_loc(THERM0_) ]
+    outp = [ c_loc(DENS_dt), c_loc(MOMX_dt), c_loc(MOMY_dt), c_loc(MOMZ_dt), c_loc(RHOT_dt) ]
+    !$acc end host_data
+    ierr = fedg_cal_vi( ctx, inp, impl_fac, dt, vi_max_iter, vi_tol, outp, c_null_ptr )
+    if (ierr < 0) call PRC_abort
+    if (ierr > 0) then
+      LOG_INFO("atm_dyn_dgm_nonhydro3d_gb300_cal_vi",*) 'Newton not converged in columns:', ierr
+    end if
+  end subroutine atm_dyn_dgm_nonhydro3d_gb300_cal_vi
+
+end module scale_atm_dyn_dgm_nonhydro3d_gb300
