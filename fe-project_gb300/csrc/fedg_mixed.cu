@@ -332,566 +332,6 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
   }
 }
 
-// =====================================================================================
-// column Newton solve, mixed precision: FP64 residual, FP32 Jacobian + LU, FP64 update
-// =====================================================================================
-// LU without pivoting: row k stays in lane k.  The mixed path's Jacobian is
-// I + impl_fac*J_A (diagonally dominant at stable time steps); a failed factorisation shows
-// up as a non-finite or non-converging FP64 residual and is reported per column.
-template <typename T, int n, int nr>
-__device__ __forceinline__ void warp_lu_np(T (&a)[n], T (&rhs)[nr], T* prow, int lane) {
-#pragma unroll
-  for (int k = 0; k < n; ++k) {
-    if (lane == k) {
-#pragma unroll
-      for (int c = k; c < n; ++c) prow[c] = a[c];
-#pragma unroll
-      for (int m = 0; m < nr; ++m) prow[n + m] = rhs[m];
-      prow[n + nr] = T(1) / a[k];
-    }
-    __syncwarp();
-    if (lane > k && lane < n) {
-      const T f = a[k] * prow[n + nr];
-#pragma unroll
-      for (int c = k + 1; c < n; ++c) a[c] = fma(-f, prow[c], a[c]);
-#pragma unroll
-      for (int m = 0; m < nr; ++m) rhs[m] = fma(-f, prow[n + m], rhs[m]);
-    }
-    __syncwarp();
-  }
-#pragma unroll
-  for (int k = n - 1; k >= 0; --k) {
-    if (lane == k) {
-      const T rd = T(1) / a[k];
-#pragma unroll
-      for (int m = 0; m < nr; ++m) rhs[m] *= rd;
-    }
-#pragma unroll
-    for (int m = 0; m < nr; ++m) {
-      const T xk = __shfl_sync(0xffffffffu, rhs[m], k);
-      if (lane < k) rhs[m] = fma(-a[k], xk, rhs[m]);
-    }
-  }
-  __syncwarp();
-}
-
-template <typename T, int n, int nr>
-__device__ __forceinline__ void warp_lu_t(T (&a)[n], T (&rhs)[nr], T* prow, int* plane, int lane, int& mypiv) {
-  bool done = lane >= n;
-  mypiv = -1;
-#pragma unroll
-  for (int k = 0; k < n; ++k) {
-    float bv = done ? -1.f : fabsf((float)a[k]);
-    int best = lane;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
-      const int ol = __shfl_xor_sync(0xffffffffu, best, o);
-      if (ov > bv || (ov == bv && ol < best)) { bv = ov; best = ol; }
-    }
-    const bool piv = (lane == best);
-    if (piv) {
-#pragma unroll
-      for (int c = k; c < n; ++c) prow[c] = a[c];
-#pragma unroll
-      for (int m = 0; m < nr; ++m) prow[n + m] = rhs[m];
-      prow[n + nr] = T(1) / a[k];
-      plane[k] = lane;
-      mypiv = k;
-    }
-    __syncwarp();
-    if (!done && !piv) {
-      const T f = a[k] * prow[n + nr];
-#pragma unroll
-      for (int c = k + 1; c < n; ++c) a[c] = fma(-f, prow[c], a[c]);
-#pragma unroll
-      for (int m = 0; m < nr; ++m) rhs[m] = fma(-f, prow[n + m], rhs[m]);
-    }
-    done = done || piv;
-    __syncwarp();
-  }
-#pragma unroll
-  for (int k = n - 1; k >= 0; --k) {
-    if (mypiv == k) {
-      const T rd = T(1) / a[k];
-#pragma unroll
-      for (int m = 0; m < nr; ++m) rhs[m] *= rd;
-    }
-    const int src = plane[k];
-#pragma unroll
-    for (int m = 0; m < nr; ++m) {
-      const T xk = __shfl_sync(0xffffffffu, rhs[m], src);
-      if (mypiv >= 0 && mypiv < k) rhs[m] = fma(-a[k], xk, rhs[m]);
-    }
-  }
-  __syncwarp();
-}
-
-// (1+r)^kappa - 1 by its binomial series (|r| <= rmax), else from pow().  nt terms: the caller
-// picks nt warp-uniformly from max|r| so the remainder stays below 1e-16 relative.
-__device__ __forceinline__ double binom_pm1(double r, const PresSeries& ps, double kap, int nt) {
-  if (fabs(r) > ps.rmax) return pow(1.0 + r, kap) - 1.0;
-  double s = ps.c[nt - 1];
-  for (int m = nt - 2; m >= 0; --m) s = fma(s, r, ps.c[m]);
-  return s * r;
-}
-__device__ __forceinline__ int binom_terms(float amax) {
-  return amax <= 1e-4f ? 4 : (amax <= 1e-3f ? 5 : (amax <= 1e-2f ? 8 : 12));
-}
-
-struct ColMix {
-  double *P, *Q;                     // [3L] iterate and stage input, row 3l+v (v: DENS, MOMZ, RHOT)
-  double *fm64, *fr64, *pot64;       // [L] FP64 level quantities of the certifying residual
-  double* del64;                     // [NeZ][2][3] FP64 vertical-face fluxes
-  float *fm, *fr, *pot, *wt, *dpd;   // [L] FP32 level quantities (split residual, Jacobian)
-  float* del;                        // [NeZ][2][3]
-  float* bf;                         // [3L] residual = right-hand side of the correction
-  float *xh, *Gh;                    // [3L], [9L] block-Thomas history
-  float *alB, *alT;                  // [NeZ] frozen vertical Rusanov speed
-  float* prow;
-  int* plane;
-  int L, NeZ, lane;
-  const double *dh, *ph, *rh, *rhinv;
-  const float *dhf, *phf, *rhf, *rhinvf;
-};
-
-// vertical face flux of element ez, side s (0 bottom, 1 top), variable v from the level arrays
-// (vi_cal_del_flux_dyn, hevi_common_2.F90:1294-1323); T = float or double
-template <int N1, typename T>
-__device__ __forceinline__ T mix_face(const ColMix& c, int ez, int s, int v, const T* fm, const T* pot, T tmp1) {
-  constexpr int N = N1 - 1;
-  const int lM = ez * N1 + (s == 0 ? 0 : N);
-  const bool lid = s == 0 ? (ez == 0) : (ez == c.NeZ - 1);
-  const int lP = lid ? lM : (s == 0 ? lM - 1 : lM + 1);
-  const T nz = s == 0 ? T(-1) : T(1);
-  const T al = (T)(s == 0 ? c.alB[ez] : c.alT[ez]);
-  const T mzM = (T)c.P[3 * lM + 1];
-  const T mzP = lid ? -mzM : (T)c.P[3 * lP + 1];
-  if (v == 0) return tmp1 * ((mzP - mzM) * nz - al * (T)(c.P[3 * lP] - c.P[3 * lM]));
-  if (v == 1) return tmp1 * ((fm[lP] - fm[lM]) * nz - al * (mzP - mzM));
-  return tmp1 * ((pot[lP] * mzP - pot[lM] * mzM) * nz - al * (T)(c.P[3 * lP + 2] - c.P[3 * lM + 2]));
-}
-
-// Newton residual b = impl_fac A(P) + (q* - P) of the whole column into c.bf; returns the
-// warp-wide max of |b|/scale.  fp64: the operator A in FP64 (the certifying residual);
-// otherwise A in FP32 and only the difference q* - P in FP64 (the split residual).
-template <int N1>
-__device__ double mix_residual(const Ops& op, ColMix& c, const PresSeries& ps, double impl_fac, double cref,
-                               bool fp64) {
-  constexpr int n3 = 3 * N1;
-  const float kap = (float)op.kap;
-  // level quantities, lanes over levels (warp-uniform trip count: the FP64 branch shuffles)
-  for (int base = 0; base < c.L; base += 32) {
-    const bool lact = base + c.lane < c.L;
-    const int l = lact ? base + c.lane : c.L - 1;
-    const double Pd = c.P[3 * l], Pm = c.P[3 * l + 1], Pr = c.P[3 * l + 2];
-    const float densf = __ldg(c.dhf + l) + (float)Pd;
-    const float rhotf = __ldg(c.rhf + l) + (float)Pr;
-    const float rdf = 1.f / densf;
-    float fmf, potf;
-    if (fp64) {
-      const double dens = __ldg(c.dh + l) + Pd;
-      const double rhot = __ldg(c.rh + l) + Pr;
-      double rd = (double)rdf;  // two Newton steps on 1/dens from the FP32 reciprocal
-      rd = rd * fma(-dens, rd, 2.0);
-      rd = rd * fma(-dens, rd, 2.0);
-      const double pot = rhot * rd;
-      const double rr = Pr * __ldg(c.rhinv + l);
-      float ra = fabsf((float)rr);
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) ra = fmaxf(ra, __shfl_xor_sync(0xffffffffu, ra, o));
-      const double fm = __ldg(c.ph + l) * binom_pm1(rr, ps, op.kap, binom_terms(ra));
-      if (lact) {
-        c.pot64[l] = pot;
-        c.fm64[l] = fm;
-        c.fr64[l] = pot * Pm;
-      }
-      fmf = (float)fm;
-      potf = (float)pot;
-    } else {
-      potf = rhotf * rdf;
-      fmf = __ldg(c.phf + l) * expm1f(kap * log1pf((float)Pr * __ldg(c.rhinvf + l)));
-    }
-    if (lact) {
-      c.pot[l] = potf;
-      c.fm[l] = fmf;
-      c.fr[l] = potf * (float)Pm;
-      c.wt[l] = (float)Pm * rdf;
-      c.dpd[l] = kap * (__ldg(c.phf + l) + fmf) / rhotf;
-    }
-  }
-  __syncwarp();
-  // vertical-face fluxes, lanes over (element, side, variable)
-  for (int it = c.lane; it < c.NeZ * 6; it += 32) {
-    const int ez = it / 6, s = (it / 3) % 2, v = it % 3;
-    if (fp64) c.del64[it] = mix_face<N1, double>(c, ez, s, v, c.fm64, c.pot64, 0.5 * op.FSz);
-    else c.del[it] = mix_face<N1, float>(c, ez, s, v, c.fm, c.pot, 0.5f * (float)op.FSz);
-  }
-  __syncwarp();
-  float errf = 0.f;
-  for (int l = c.lane; l < c.L; l += 32) {
-    const int ez = l / N1, k = l - ez * N1;
-    double A[3];
-    if (fp64) {
-      double sd = 0.0, sm = 0.0, sr = 0.0, drho = 0.0;
-#pragma unroll
-      for (int m = 0; m < N1; ++m) {
-        const int lm = ez * N1 + m;
-        const double dk = op.D[k * N1 + m];
-        sd = fma(dk, c.P[3 * lm + 1], sd);
-        sm = fma(dk, c.fm64[lm], sm);
-        sr = fma(dk, c.fr64[lm], sr);
-        drho = fma(op.T[k * N1 + m], c.P[3 * lm], drho);
-      }
-      const double* dl = c.del64 + ez * 6;
-      A[0] = -(op.E33 * sd + op.Lb[k] * dl[0] + op.Lt[k] * dl[3]);
-      A[1] = -(op.E33 * sm + op.Lb[k] * dl[1] + op.Lt[k] * dl[4]) - op.grav * drho;
-      A[2] = -(op.E33 * sr + op.Lb[k] * dl[2] + op.Lt[k] * dl[5]);
-    } else {
-      float sd = 0.f, sm = 0.f, sr = 0.f, drho = 0.f;
-#pragma unroll
-      for (int m = 0; m < N1; ++m) {
-        const int lm = ez * N1 + m;
-        const float dk = (float)op.D[k * N1 + m];
-        sd = fmaf(dk, (float)c.P[3 * lm + 1], sd);
-        sm = fmaf(dk, c.fm[lm], sm);
-        sr = fmaf(dk, c.fr[lm], sr);
-        drho = fmaf((float)op.T[k * N1 + m], (float)c.P[3 * lm], drho);
-      }
-      const float* dl = c.del + ez * 6;
-      const float E33 = (float)op.E33, lb = (float)op.Lb[k], lt = (float)op.Lt[k];
-      A[0] = -(E33 * sd + lb * dl[0] + lt * dl[3]);
-      A[1] = -(E33 * sm + lb * dl[1] + lt * dl[4]) - (float)op.grav * drho;
-      A[2] = -(E33 * sr + lb * dl[2] + lt * dl[5]);
-    }
-    const float isc[3] = {1.f / __ldg(c.dhf + l), 1.f / (__ldg(c.dhf + l) * (float)cref), 1.f / __ldg(c.rhf + l)};
-#pragma unroll
-    for (int v = 0; v < 3; ++v) {
-      const double b = fma(impl_fac, A[v], c.Q[3 * l + v] - c.P[3 * l + v]);
-      const float bfl = (float)b;
-      c.bf[3 * l + v] = bfl;
-      errf = fmaxf(errf, fabsf(bfl) * isc[v]);
-      if (!(fabsf(bfl) < 3.0e38f)) errf = __int_as_float(0x7fc00000);
-    }
-  }
-  __syncwarp();
-  float e = errf;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const float oe = __shfl_xor_sync(0xffffffffu, e, o);
-    e = (e != e || oe != oe) ? __int_as_float(0x7fc00000) : fmaxf(e, oe);
-  }
-  return (double)e;
-}
-
-// one correction: construct_matbnd + block-Thomas + warp LU, all FP32; P += correction (FP64)
-template <int N1>
-__device__ void mix_solve(const Ops& op, ColMix& c, double impl_fac) {
-  constexpr int N = N1 - 1, n3 = 3 * N1;
-  const int lane = c.lane;
-  const int v = lane % 3, pv = lane / 3;
-  const bool act = lane < n3;
-  const int pvr = act ? pv : 0;
-  const float fi = (float)impl_fac;
-  const float E33 = (float)op.E33, FSz = (float)op.FSz, gr = (float)op.grav;
-  for (int ez = 0; ez < c.NeZ; ++ez) {
-    float a[n3];
-    float rhs[4];
-    float Lc[3] = {0.f, 0.f, 0.f}, Uc[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-    for (int cc = 0; cc < n3; ++cc) {
-      const int v2 = cc % 3, pv2 = cc / 3;
-      const int l2 = ez * N1 + pv2;
-      const float fdz = E33 * fi * (float)op.D[pvr * N1 + pv2];
-      const float id = (pvr == pv2) ? 1.f : 0.f;
-      float x;
-      if (v == 0) x = v2 == 0 ? id : (v2 == 1 ? fdz : 0.f);
-      else if (v == 1) x = v2 == 1 ? id : (v2 == 0 ? fi * gr * (float)op.T[pvr * N1 + pv2] : fdz * c.dpd[l2]);
-      else x = v2 == 0 ? -fdz * c.pot[l2] * c.wt[l2] : (v2 == 1 ? fdz * c.pot[l2] : id + fdz * c.wt[l2]);
-      a[cc] = x;
-    }
-#pragma unroll
-    for (int f = 0; f < 2; ++f) {
-      const bool bc = (f == 0) ? (ez == 0) : (ez == c.NeZ - 1);
-      const int pv1 = f == 0 ? 0 : N;
-      const int l1 = ez * N1 + pv1;
-      const int ln = bc ? l1 : (f == 0 ? l1 - 1 : l1 + 1);
-      const float nz = f == 0 ? -1.f : 1.f;
-      const float al = f == 0 ? c.alB[ez] : c.alT[ez];
-      const float fac = 0.5f * fi * (float)(f == 0 ? op.Lb[pvr] : op.Lt[pvr]) * FSz;
-      const float tmp1 = fac * al, tmp2 = fac * nz;
-      const float pot1 = c.pot[l1], wt1 = c.wt[l1];
-      const int c0 = 3 * (f == 0 ? 0 : N);
-      if (bc) {
-        if (v == 2) a[c0 + 0] += 2.f * tmp2 * pot1 * wt1;
-        if (v == 0) a[c0 + 1] -= 2.f * tmp2;
-        if (v == 1) a[c0 + 1] += 2.f * tmp1;
-        if (v == 2) a[c0 + 1] -= 2.f * tmp2 * pot1;
-        if (v == 2) a[c0 + 2] -= 2.f * tmp2 * wt1;
-      } else {
-        if (v == 0) a[c0 + 0] += tmp1;
-        if (v == 2) a[c0 + 0] += tmp2 * pot1 * wt1;
-        if (v == 0) a[c0 + 1] -= tmp2;
-        if (v == 1) a[c0 + 1] += tmp1;
-        if (v == 2) a[c0 + 1] -= tmp2 * pot1;
-        if (v == 1) a[c0 + 2] -= tmp2 * c.dpd[l1];
-        if (v == 2) a[c0 + 2] += tmp1 - tmp2 * wt1;
-        const float potn = c.pot[ln], wtn = c.wt[ln];
-        float cc0, cc1, cc2;
-        if (v == 0) { cc0 = -tmp1; cc1 = tmp2; cc2 = 0.f; }
-        else if (v == 1) { cc0 = 0.f; cc1 = -tmp1; cc2 = tmp2 * c.dpd[ln]; }
-        else { cc0 = -tmp2 * potn * wtn; cc1 = tmp2 * potn; cc2 = -tmp1 + tmp2 * wtn; }
-        if (f == 0) { Lc[0] = cc0; Lc[1] = cc1; Lc[2] = cc2; }
-        else { Uc[0] = cc0; Uc[1] = cc1; Uc[2] = cc2; }
-      }
-    }
-    rhs[0] = act ? c.bf[ez * n3 + lane] : 0.f;
-    if (ez > 0) {
-      const float* Gp = c.Gh + ((ez - 1) * n3 + 3 * N) * 3;
-      const float* bp = c.xh + (ez - 1) * n3 + 3 * N;
-#pragma unroll
-      for (int c2 = 0; c2 < 3; ++c2) a[c2] -= Lc[0] * Gp[0 * 3 + c2] + Lc[1] * Gp[1 * 3 + c2] + Lc[2] * Gp[2 * 3 + c2];
-      rhs[0] -= Lc[0] * bp[0] + Lc[1] * bp[1] + Lc[2] * bp[2];
-    }
-    const bool last = ez == c.NeZ - 1;
-    rhs[1] = last ? 0.f : Uc[0];
-    rhs[2] = last ? 0.f : Uc[1];
-    rhs[3] = last ? 0.f : Uc[2];
-    if (!act) {
-#pragma unroll
-      for (int cc = 0; cc < n3; ++cc) a[cc] = 0.f;
-    }
-    __syncwarp();
-    warp_lu_np<float, n3, 4>(a, rhs, c.prow, lane);
-    if (act) {
-      c.xh[ez * n3 + lane] = rhs[0];
-      c.Gh[(ez * n3 + lane) * 3 + 0] = rhs[1];
-      c.Gh[(ez * n3 + lane) * 3 + 1] = rhs[2];
-      c.Gh[(ez * n3 + lane) * 3 + 2] = rhs[3];
-    }
-    __syncwarp();
-  }
-  for (int ez = c.NeZ - 2; ez >= 0; --ez) {
-    if (act) {
-      const float* bn = c.xh + (ez + 1) * n3;
-      const float* G = c.Gh + (ez * n3 + lane) * 3;
-      c.xh[ez * n3 + lane] -= G[0] * bn[0] + G[1] * bn[1] + G[2] * bn[2];
-    }
-    __syncwarp();
-  }
-  for (int idx = lane; idx < 3 * c.L; idx += 32) c.P[idx] += (double)c.xh[idx];
-  __syncwarp();
-}
-
-struct MixViArgs {
-  double impl_fac, inv_impl_fac, tol, cref;
-  double Uref, Vref;  // reference wind of the FP32 deviation copy of Q
-  int max_iter;
-  int check64;  // 1: convergence judged by the FP64 residual; 0: by the split residual
-};
-
-// per-warp shared memory in doubles
-template <int N1>
-__host__ __device__ constexpr int vi_mixed_doubles(int L, int NeZ) {
-  // doubles: P, Q (6L), del64 (6NeZ), G history (9L floats) shared with fm64/fr64/pot64 (3L doubles)
-  // floats:  fm, fr, pot, wt, dpd (5L), bf (3L), xh (3L), del (6NeZ), alB/alT (2NeZ), prow (3N1+8)
-  return 6 * L + 6 * NeZ + (9 * L + 1) / 2 + 1 + (11 * L + 8 * NeZ + 3 * N1 + 8 + 1) / 2 + 2;
-}
-
-// qin: stage input q*; z: var0 (alph and the plain initial iterate); guess: FP32 increments
-// of (DENS, MOMZ, RHOT) over q*, or NULL.  qout: Q; tout: (Q - q*)/impl_fac in FP32.
-template <int N1>
-__global__ void __launch_bounds__(128) k_vi_mixed(const Ops op, const Prof pf, const ProfF pff,
-                                                   const double* __restrict__ rhinv, const PresSeries ps,
-                                                   const F5c qin, const F5c z, const float* const* guess,
-                                                   float* const* qsf, float* const* tout, int* status,
-                                                   unsigned long long* cnt, const MixViArgs args, int ncol) {
-  constexpr int N = N1 - 1, NF = N1 * N1, Np = N1 * N1 * N1;
-  extern __shared__ double sm[];
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const int col = blockIdx.x * (blockDim.x >> 5) + wib;
-  if (col >= ncol) return;
-  const int L = op.L, NeZ = op.NeZ;
-  double* W = sm + (size_t)wib * vi_mixed_doubles<N1>(L, NeZ);
-  ColMix c;
-  c.L = L; c.NeZ = NeZ; c.lane = lane;
-  c.dh = pf.dens; c.ph = pf.pres; c.rh = pf.rhyd; c.rhinv = rhinv;
-  c.dhf = pff.dens; c.phf = pff.pres; c.rhf = pff.therm; c.rhinvf = pff.rtherm;
-  c.P = W; c.Q = c.P + 3 * L; c.del64 = c.Q + 3 * L;
-  double* gbase = c.del64 + 6 * NeZ;  // 9L floats of G history == 3L doubles of FP64 level arrays
-  c.Gh = reinterpret_cast<float*>(gbase);
-  c.fm64 = gbase; c.fr64 = c.fm64 + L; c.pot64 = c.fr64 + L;
-  float* fb = reinterpret_cast<float*>(gbase + (9 * L + 1) / 2 + 1);
-  c.fm = fb; c.fr = c.fm + L; c.pot = c.fr + L; c.wt = c.pot + L; c.dpd = c.wt + L;
-  c.bf = c.dpd + L; c.xh = c.bf + 3 * L; c.del = c.xh + 3 * L;
-  c.alB = c.del + 6 * NeZ; c.alT = c.alB + NeZ; c.prow = c.alT + NeZ;
-  c.plane = nullptr;
-  const int ij = col % NF, exy = col / NF;
-  const int ci = ij % N1, cj = ij / N1;
-  const size_t nxy = (size_t)op.NeX * op.NeY;
-  auto gidx = [&](int l) -> size_t {
-    const int ez = l / N1, k = l - ez * N1;
-    return ((size_t)ez * nxy + exy) * Np + ci + N1 * cj + NF * k;
-  };
-  const int gv[3] = {VD, VMZ, VRT};
-  const double impl_fac = args.impl_fac;
-  const float kap = (float)op.kap;
-
-  for (int l = lane; l < L; l += 32) {
-    const size_t g = gidx(l);
-#pragma unroll
-    for (int m = 0; m < 3; ++m) {
-      const double qv = __ldg(qin.v[gv[m]] + g);
-      c.Q[3 * l + m] = qv;
-      c.P[3 * l + m] = guess ? qv + (double)__ldg(guess[m] + g) : __ldg(z.v[gv[m]] + g);
-    }
-    // |w| + c of var0 in FP32: the frozen vertical Rusanov speed (hevi_common_2.F90:1149-1155)
-    const float dd0 = (float)__ldg(z.v[VD] + g), dr0 = (float)__ldg(z.v[VRT] + g);
-    const float rdens0 = 1.f / (__ldg(pff.dens + l) + dd0);
-    const float wt0 = (float)__ldg(z.v[VMZ] + g) * rdens0;
-    const float pres0 = __ldg(pff.pres + l) * (1.f + expm1f(kap * log1pf(dr0 * __ldg(pff.rtherm + l))));
-    c.fm[l] = fabsf(wt0) + sqrtf(kap * pres0 * rdens0);
-  }
-  __syncwarp();
-  for (int ez = lane; ez < NeZ; ez += 32) {
-    const int lb = ez * N1, lt = ez * N1 + N;
-    c.alB[ez] = fmaxf(c.fm[lb], c.fm[ez > 0 ? lb - 1 : lb]);
-    c.alT[ez] = fmaxf(c.fm[lt], c.fm[ez < NeZ - 1 ? lt + 1 : lt]);
-  }
-  __syncwarp();
-
-  // ---- MOMX/MOMY: linear vertical-dissipation system; FP64 residual, FP32 LU ----
-  {
-    // the var3 arrays are loaded already; the uv system borrows the G history (4.5L doubles)
-    // for its iterate and input and the float scratch for its right-hand side / solution
-    double* Pu = reinterpret_cast<double*>(c.Gh);     // [2L]
-    double* Qu = Pu + 2 * L;                          // [2L]
-    float* Gu = reinterpret_cast<float*>(Qu + 2 * L); // [L] (4L doubles + L floats <= 9L floats)
-    float* bu = c.bf;                                 // [2L] (bf has 3L)
-    float* xu = c.xh;                                 // [2L]
-    for (int l = lane; l < L; l += 32) {
-      const size_t g = gidx(l);
-      Pu[2 * l + 0] = __ldg(z.v[VMX] + g);
-      Pu[2 * l + 1] = __ldg(z.v[VMY] + g);
-      Qu[2 * l + 0] = __ldg(qin.v[VMX] + g);
-      Qu[2 * l + 1] = __ldg(qin.v[VMY] + g);
-    }
-    __syncwarp();
-    const float tmf = (float)(-0.5 * op.FSz);
-    for (int it = 0; it < 4; ++it) {
-      float err = 0.f;
-      for (int l = lane; l < L; l += 32) {
-        const int ez = l / N1, pv = l - ez * N1;
-        const float iscu = 1.f / (__ldg(pff.dens + l) * (float)args.cref);
-        const int lb = ez * N1, lt = ez * N1 + N;
-        const int lbP = ez > 0 ? lb - 1 : lb, ltP = ez < NeZ - 1 ? lt + 1 : lt;
-#pragma unroll
-        for (int m = 0; m < 2; ++m) {
-          // the operator acts on the face jumps only: jumps in FP64, the rest in FP32
-          const float jB = (float)(Pu[2 * lbP + m] - Pu[2 * lb + m]);
-          const float jT = (float)(Pu[2 * ltP + m] - Pu[2 * lt + m]);
-          const float Af = -((float)op.Lb[pv] * tmf * c.alB[ez] * jB + (float)op.Lt[pv] * tmf * c.alT[ez] * jT);
-          const double b = fma(impl_fac, (double)Af, Qu[2 * l + m] - Pu[2 * l + m]);
-          const float bfl = (float)b;
-          bu[2 * l + m] = bfl;
-          err = fmaxf(err, fabsf(bfl) * iscu);
-        }
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) err = fmaxf(err, __shfl_xor_sync(0xffffffffu, err, o));
-      if ((double)err <= args.tol || it == 3) break;
-      for (int ez = 0; ez < NeZ; ++ez) {
-        float a[N1];
-        float rhs[3];
-        const bool act = lane < N1;
-        const int pv = act ? lane : 0;
-        const int l = ez * N1 + pv;
-        const bool bcB = ez == 0, bcT = ez == NeZ - 1;
-        const float t1b = (float)(0.5 * impl_fac * op.Lb[pv] * op.FSz) * c.alB[ez];
-        const float t1t = (float)(0.5 * impl_fac * op.Lt[pv] * op.FSz) * c.alT[ez];
-#pragma unroll
-        for (int cc = 0; cc < N1; ++cc) a[cc] = (cc == pv) ? 1.f : 0.f;
-        if (!bcB) a[0] += t1b;
-        if (!bcT) a[N] += t1t;
-        const float Lc = bcB ? 0.f : -t1b;
-        const float Uc = bcT ? 0.f : -t1t;
-        float bx = bu[2 * l], by = bu[2 * l + 1];
-        if (ez > 0) {
-          a[0] -= Lc * Gu[(ez - 1) * N1 + N];
-          bx -= Lc * xu[2 * ((ez - 1) * N1 + N)];
-          by -= Lc * xu[2 * ((ez - 1) * N1 + N) + 1];
-        }
-        rhs[0] = bx; rhs[1] = by; rhs[2] = bcT ? 0.f : Uc;
-        if (!act) {
-#pragma unroll
-          for (int cc = 0; cc < N1; ++cc) a[cc] = 0.f;
-          rhs[0] = rhs[1] = rhs[2] = 0.f;
-        }
-        __syncwarp();
-        warp_lu_np<float, N1, 3>(a, rhs, c.prow, lane);
-        if (act) {
-          xu[2 * (ez * N1 + lane)] = rhs[0];
-          xu[2 * (ez * N1 + lane) + 1] = rhs[1];
-          Gu[ez * N1 + lane] = rhs[2];
-        }
-        __syncwarp();
-      }
-      for (int ez = NeZ - 2; ez >= 0; --ez) {
-        if (lane < N1) {
-          const int l = ez * N1 + lane;
-          const float gg = Gu[l];
-          xu[2 * l] -= gg * xu[2 * ((ez + 1) * N1)];
-          xu[2 * l + 1] -= gg * xu[2 * ((ez + 1) * N1) + 1];
-        }
-        __syncwarp();
-      }
-      for (int idx = lane; idx < 2 * L; idx += 32) Pu[idx] += (double)xu[idx];
-      __syncwarp();
-    }
-    for (int l = lane; l < L; l += 32) {
-      const size_t g = gidx(l);
-      const double dh64 = __ldg(pf.dens + l);
-      qsf[VMX][g] = (float)fma(-dh64, args.Uref, Pu[2 * l]);
-      qsf[VMY][g] = (float)fma(-dh64, args.Vref, Pu[2 * l + 1]);
-      tout[VMX][g] = (float)(Pu[2 * l] - Qu[2 * l]) * (float)args.inv_impl_fac;
-      tout[VMY][g] = (float)(Pu[2 * l + 1] - Qu[2 * l + 1]) * (float)args.inv_impl_fac;
-    }
-    __syncwarp();
-  }
-
-  // ---- DENS/MOMZ/RHOT Newton: first correction from the split residual, then the
-  //      certifying residual before every further correction ----
-  int st, nsolve = 0;
-  mix_residual<N1>(op, c, ps, impl_fac, args.cref, false);
-  mix_solve<N1>(op, c, impl_fac);
-  nsolve = 1;
-  while (true) {
-    const double err = mix_residual<N1>(op, c, ps, impl_fac, args.cref, args.check64 != 0);
-    if (err != err) { st = -2; break; }
-    if (err <= args.tol) { st = nsolve; break; }
-    if (nsolve >= args.max_iter) { st = -1; break; }
-    mix_solve<N1>(op, c, impl_fac);
-    ++nsolve;
-  }
-  for (int l = lane; l < L; l += 32) {
-    const size_t g = gidx(l);
-#pragma unroll
-    for (int m = 0; m < 3; ++m) {
-      const double pnew = c.P[3 * l + m];
-      qsf[gv[m]][g] = (float)pnew;
-      tout[gv[m]][g] = (float)(pnew - c.Q[3 * l + m]) * (float)args.inv_impl_fac;
-    }
-  }
-  if (lane == 0) {
-    if (status) status[col] = st;
-    if (st < 0) atomicAdd(cnt, 1ull);
-    else {
-      atomicAdd(cnt + 1, (unsigned long long)st);
-      atomicAdd(cnt + 2, 1ull);
-    }
-  }
-}
-
 // FP32 deviation copy of a state (DDENS, MOMX - DENS_hyd*Uref, MOMY - DENS_hyd*Vref, MOMZ, DRHOT)
 struct Dev5 { float* v[5]; };
 __global__ void k_to_dev(F5c q, Dev5 out, const double* __restrict__ dens_prof, double Uref, double Vref, int Np,
@@ -956,23 +396,6 @@ static int launch_stage_m(int stage, const OpsF& op, const ProfF& pf, const doub
   return launch_stage_n<N1, 3>(op, pf, dens64, B, cf, Ne, filt, s);
 }
 
-template <int N1>
-static int launch_vi_m(const Ops& op, const Prof& pf, const ProfF& pff, const double* rhinv, const PresSeries& ps,
-                       const F5c& qin, const F5c& z, const float* const* guess, float* const* qsf, float* const* tout,
-                       int* status, unsigned long long* cnt, const MixViArgs& a, cudaStream_t s) {
-  const int per_warp = vi_mixed_doubles<N1>(op.L, op.NeZ);
-  const int ncol = op.NeX * op.NeY * N1 * N1;
-  int wpb = 4;
-  size_t smem = sizeof(double) * (size_t)per_warp * wpb;
-  while (wpb > 1 && smem > 200 * 1024) { wpb >>= 1; smem = sizeof(double) * (size_t)per_warp * wpb; }
-  if (smem > 227 * 1024) return (int)cudaErrorInvalidValue;
-  auto kfn = k_vi_mixed<N1>;
-  cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  kfn<<<(ncol + wpb - 1) / wpb, 32 * wpb, smem, s>>>(op, pf, pff, rhinv, ps, qin, z, guess, qsf, tout, status, cnt,
-                                                       a, ncol);
-  return (int)cudaGetLastError();
-}
-
 }  // namespace fedg
 
 // =====================================================================================
@@ -983,6 +406,7 @@ struct MixedState {
   float* prof = nullptr;    // [4][L]
   double* rhinv = nullptr;  // [L]
   float** d_ptrs = nullptr; // device arrays of float pointers: TI[5], guess[3], QSF[5]
+  float* gsc = nullptr;     // block-Thomas history of the column solve
   OpsF opf;
   PresSeries ps;
   double Uref = 0.0, Vref = 0.0;
@@ -1003,6 +427,7 @@ void mixed_free(MixedState* m) {
   cudaFree(m->prof);
   cudaFree(m->rhinv);
   cudaFree(m->d_ptrs);
+  cudaFree(m->gsc);
   delete m;
 }
 
@@ -1017,7 +442,8 @@ static int mixed_setup(fedg_ctx* c) {
       (e = cudaMalloc(&m->fbuf, sizeof(float) * 28 * c->n)) != cudaSuccess ||
       (e = cudaMalloc(&m->prof, sizeof(float) * 4 * L)) != cudaSuccess ||
       (e = cudaMalloc(&m->rhinv, sizeof(double) * L)) != cudaSuccess ||
-      (e = cudaMalloc(&m->d_ptrs, sizeof(float*) * 13)) != cudaSuccess) {
+      (e = cudaMalloc(&m->d_ptrs, sizeof(float*) * 13)) != cudaSuccess ||
+      (e = cudaMalloc(&m->gsc, sizeof(float) * vi_cols_scratch_floats(c->n))) != cudaSuccess) {
     mixed_free(m);
     return api_cuda_fail(e, "fedg_update(mixed): allocation");
   }
@@ -1146,11 +572,8 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
       gptr = (const float* const*)(m->d_ptrs + 5);
     }
     return tracked(c, FEDG_K_MVI, [&] {
-      switch (c->N1) {
-        case 4: return launch_vi_m<4>(c->op, pf, pff, m->rhinv, m->ps, qin, z, gptr, qo, m->d_ptrs, c->d_status, c->d_cnt, va, c->stream);
-        case 8: return launch_vi_m<8>(c->op, pf, pff, m->rhinv, m->ps, qin, z, gptr, qo, m->d_ptrs, c->d_status, c->d_cnt, va, c->stream);
-      }
-      return (int)cudaErrorInvalidValue;
+      return launch_vi_cols(c->N1, c->op, pf, pff, m->rhinv, m->ps, qin, z, gptr, qo, m->d_ptrs, m->gsc, c->d_status,
+                            c->d_cnt, va, c->stream);
     });
   };
   for (int step = 0; step < nsteps; ++step) {

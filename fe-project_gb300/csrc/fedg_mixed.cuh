@@ -2,6 +2,7 @@
 #pragma once
 #include "../../include/fedg.h"
 #include "fedg_common.cuh"
+#include "fedg_kernels.cuh"
 
 namespace fedg {
 
@@ -32,6 +33,24 @@ struct PresSeries {
   int nterm;
   double rmax;  // |r| above which pow() is used instead
 };
+
+// controls of the mixed-precision column solve
+struct MixViArgs {
+  double impl_fac, inv_impl_fac, tol, cref;
+  double Uref, Vref;  // reference wind of the FP32 deviation copy of Q
+  int max_iter;
+  int check64;  // 1: convergence judged by the FP64 residual; 0: by the split residual
+};
+
+// Mixed-precision column solve (fedg_vicol.cu).  qin: stage input q* (FP64); z: var0 (alph and
+// the plain initial iterate); guess: FP32 increments of (DENS, MOMZ, RHOT) over q*, or NULL.
+// qsf: FP32 deviation copy of Q (MOMX/MOMY relative to DENS_hyd*(Uref, Vref)); tout: (Q - q*)/
+// impl_fac in FP32; gsc: vi_cols_scratch_floats(n) floats of block-Thomas history; status[ncol]:
+// solves used, -1 not converged, -2 non-finite; cnt[3]: failed columns, solves, converged columns.
+size_t vi_cols_scratch_floats(size_t nodes);
+int launch_vi_cols(int N1, const Ops& op, const Prof& pf, const ProfF& pff, const double* rhinv, const PresSeries& ps,
+                   const F5c& qin, const F5c& z, const float* const* guess, float* const* qsf, float* const* tout,
+                   float* gsc, int* status, unsigned long long* cnt, const MixViArgs& a, cudaStream_t s);
 
 }  // namespace fedg
 

@@ -1,0 +1,695 @@
+// fedg_vicol.cu -- HEVI column Newton solve of the mixed-precision path (cal_vi), N1 lanes per
+// column and 32/N1 columns per warp.
+//
+// FElib's cal_vi (FElib/src/atmosphere/dynamics/scale_atm_dyn_dgm_nonhydro3d_rhot_hevi.F90:
+// 772-965, the operators of scale_atm_dyn_dgm_nonhydro3d_hevi_common_2.F90) solves, column by
+// column, Q - q* - impl_fac A(Q) = 0 for the vertical acoustic/buoyancy operator A with the
+// vertical Rusanov speed frozen at var0:
+//   MOMX, MOMY: a linear system (vertical face dissipation only, eval_Ax_uv/solve_uv)
+//   DENS, MOMZ, RHOT: Newton on a block-tridiagonal system with 3*N1 x 3*N1 element blocks
+//   (construct_matbnd, block-Thomas, block LU).
+//
+// Thread layout: lane k of a column group owns node k of every element of the column (level
+// l = ez*N1 + k) and, in the solve, the three rows (DENS, MOMZ, RHOT) of that node in each
+// element block.  The columns of one warp are neighbours in x (same element, consecutive i),
+// so every global load of a level touches whole 32-byte sectors.
+//
+// Precision (see fedg_mixed.cu for the whole path):
+//   - the iterate P is FP64 (shared memory); the convergence test is on the FP64 residual
+//     b = impl_fac A(P) + q* - P (FP64 operator, "certifying" residual);
+//   - the first correction of every column uses the split residual (FP32 operator, FP64 q* - P);
+//   - Jacobian, block-Thomas and the element LU (no pivoting: I + impl_fac J is diagonally
+//     dominant at stable time steps; a failure shows as a non-converging or non-finite FP64
+//     residual, reported per column) are FP32;
+//   - MOMX/MOMY: the element blocks are I plus two rank-one face terms, so the system reduces
+//     exactly to a scalar tridiagonal system in the NeZ-1 interface jumps, solved in FP32; the
+//     residual (FP64 jumps and q* - P, FP32 operator) is accurate far below the tolerance
+//     because the operator only sees the jumps.
+#include <algorithm>
+
+#include "fedg_ctx.cuh"
+#include "fedg_mixed.cuh"
+
+namespace fedg {
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+// per-column shared-memory layout (bytes); the column stride is padded so that the C columns
+// of a warp start on different banks
+struct ColLayout {
+  int oP, oJq, oRing, oDel, oBf, oProw, oBc, oAl, oJb, stride;
+  __host__ __device__ ColLayout(int N1, int NeZ) {
+    const int L = N1 * NeZ;
+    const int prw = ((3 * N1 + 5 + 3) / 4) * 4;
+    int o = 0;
+    oP = o;    o += 24 * L;                    // double P[3L] (uv phase: P[2L])
+    oJq = o;   o += 16 * L;                    // float4 Jq[L]: pot, wt, dpd of the Jacobian
+    oRing = o; o += 72 * N1;                   // 3 element slots x N1 nodes x 3 doubles
+    oDel = o;  o += 48;                        // 6 face fluxes of the current element
+    oBf = o;   o += 12 * L;                    // float b / y / x [3L] (uv phase: [2L])
+    oProw = o; o += 4 * prw;                   // pivot row + right-hand sides + 1/pivot
+    oBc = o;   o += 64;                        // block-Thomas coupling from the element below
+    oAl = o;   o += ((8 * NeZ + 15) / 16) * 16; // alB, alT per element
+    oJb = o;   o += ((12 * (NeZ + 1) + 15) / 16) * 16;  // uv: c' and the two interface jumps
+    const int words = o / 4;
+    const int C = 32 / N1;
+    stride = 4 * (((words + 31) / 32) * 32 + 32 / C);
+  }
+};
+
+template <int N1>
+struct Col {
+  static constexpr int PRW = ((3 * N1 + 5 + 3) / 4) * 4;
+  double* P;
+  float4* Jq;
+  double* ring;  // [3][3][N1]: slot, quantity (fm, fr, pot), node
+  double* del;
+  float* Bf;
+  float* prow;
+  float* bc;
+  float* al;
+  float* jb;
+  int k, NeZ, L;
+  size_t gb, gs;  // global index of node (0, k) of this column and the element-layer stride
+  __device__ size_t g(int e) const { return gb + (size_t)e * gs; }
+  __device__ float alB(int e) const { return al[2 * e]; }
+  __device__ float alT(int e) const { return al[2 * e + 1]; }
+};
+
+__device__ __forceinline__ float grp_max_nan(float e, int width) {
+  for (int o = width / 2; o > 0; o >>= 1) {
+    const float oe = __shfl_xor_sync(FULL, e, o);
+    e = (e != e || oe != oe) ? __int_as_float(0x7fc00000) : fmaxf(e, oe);
+  }
+  return e;
+}
+
+// (1+r)^kappa - 1 by its binomial series for |r| <= rmax (NT terms, compile-time indices into
+// the coefficient table so it stays in the parameter bank), else pow(); nt chosen from max|r|
+template <int NT>
+__device__ __forceinline__ double binom_horner(double r, const PresSeries& ps) {
+  double s = ps.c[NT - 1];
+#pragma unroll
+  for (int m = NT - 2; m >= 0; --m) s = fma(s, r, ps.c[m]);
+  return s * r;
+}
+__device__ __forceinline__ double binom_pm1c(double r, const PresSeries& ps, double kap, int nt) {
+  if (fabs(r) > ps.rmax) return pow(1.0 + r, kap) - 1.0;
+  switch (nt) {
+    case 4: return binom_horner<4>(r, ps);
+    case 5: return binom_horner<5>(r, ps);
+    case 8: return binom_horner<8>(r, ps);
+    default: return binom_horner<12>(r, ps);
+  }
+}
+__device__ __forceinline__ int binom_nterm(float amax) {
+  return amax <= 1e-4f ? 4 : (amax <= 1e-3f ? 5 : (amax <= 1e-2f ? 8 : 12));
+}
+
+struct ResIn {
+  const double *dh, *ph, *rh, *rhinv;   // FP64 profiles
+  const float *dhf, *phf, *rhf, *rhinvf; // FP32 profiles
+};
+
+// ---------------------------------------------------------------------------------------------
+// residual b = impl_fac A(P) + q* - P of the DENS/MOMZ/RHOT system into c.Bf (FP32), the FP32
+// Jacobian level quantities into c.Jq; returns the column max of |b|/scale (NaN if not finite).
+// CERT: the operator A in FP64 (eval_Ax, hevi_common_2.F90:1177-1292, with the vertical face
+// flux vi_cal_del_flux_dyn :1294-1323); otherwise A in FP32 with only q* - P in FP64.
+// Element by element, with the level quantities of elements e-1, e, e+1 in a ring of 3 slots.
+template <int N1, bool CERT>
+__device__ float col_residual(const Ops& op, const Col<N1>& c, const ResIn& pr, const PresSeries& ps,
+                              const F5c& qin, double impl_fac, double cref) {
+  using T = typename std::conditional<CERT, double, float>::type;
+  constexpr int N = N1 - 1;
+  const int k = c.k;
+  T Dk[N1], Tk[N1];
+#pragma unroll
+  for (int m = 0; m < N1; ++m) {
+    Dk[m] = (T)op.D[k * N1 + m];
+    Tk[m] = (T)op.T[k * N1 + m];
+  }
+  const T E33 = (T)op.E33, lbk = (T)op.Lb[k], ltk = (T)op.Lt[k], grav = (T)op.grav;
+  const T tmp1 = (T)(0.5 * op.FSz);
+  const float kapf = (float)op.kap;
+  // ring [slot][q][node]: q 0 fm, 1 fr, 2 pot; FP32 mode also 3 MOMZ, 4 DDENS (as floats, so the
+  // FP32 sums read no FP64 value); 3 slots x 5 x N1 floats fit the 3 x 3 x N1 doubles
+  constexpr int NQ = CERT ? 3 : 5;
+  T* rg = reinterpret_cast<T*>(c.ring);
+  auto R = [&](int slot, int q, int m) -> T& { return rg[(slot * NQ + q) * N1 + m]; };
+
+  auto fill = [&](int e) {  // level quantities of node (e, k) into slot e % 3 (all lanes)
+    const int l = e * N1 + k;
+    const double Pd = c.P[3 * l], Pm = c.P[3 * l + 1], Pr = c.P[3 * l + 2];
+    const float densf = __ldg(pr.dhf + l) + (float)Pd;
+    const float rhotf = __ldg(pr.rhf + l) + (float)Pr;
+    const float rdf = 1.f / densf;
+    float fmf, potf;
+    const int s = e % 3;
+    if constexpr (CERT) {
+      const double dens = __ldg(pr.dh + l) + Pd;
+      const double rhot = __ldg(pr.rh + l) + Pr;
+      double rd = (double)rdf;  // one Newton step on 1/dens from the FP32 reciprocal
+      rd = rd * fma(-dens, rd, 2.0);
+      rd = rd * fma(-dens, rd, 2.0);
+      const double pot = rhot * rd;
+      const double rr = Pr * __ldg(pr.rhinv + l);
+      float ra = fabsf((float)rr);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) ra = fmaxf(ra, __shfl_xor_sync(FULL, ra, o));
+      const double fm = __ldg(pr.ph + l) * binom_pm1c(rr, ps, op.kap, binom_nterm(ra));
+      R(s, 0, k) = fm;
+      R(s, 1, k) = pot * Pm;
+      R(s, 2, k) = pot;
+      fmf = (float)fm;
+      potf = (float)pot;
+    } else {
+      potf = rhotf * rdf;
+      fmf = __ldg(pr.phf + l) * expm1f(kapf * log1pf((float)Pr * __ldg(pr.rhinvf + l)));
+      R(s, 0, k) = fmf;
+      R(s, 1, k) = potf * (float)Pm;
+      R(s, 2, k) = potf;
+      R(s, 3, k) = (float)Pm;
+      R(s, 4, k) = (float)Pd;
+    }
+    c.Jq[l] = make_float4(potf, (float)Pm * rdf, kapf * (__ldg(pr.phf + l) + fmf) / rhotf, 0.f);
+  };
+
+  fill(0);
+  if (c.NeZ > 1) fill(1);
+  __syncwarp();
+  float errf = 0.f;
+  const int gv[3] = {VD, VMZ, VRT};
+  for (int e = 0; e < c.NeZ; ++e) {
+    const int sc = e % 3, sb = (e + 2) % 3, st = (e + 1) % 3;
+    // vertical-face fluxes of element e: lanes over (side, variable)
+    for (int t = k; t < 6; t += N1) {
+      const int s = t / 3, v = t - 3 * s;
+      const int nM = s == 0 ? 0 : N;
+      const int lM = e * N1 + nM;
+      const bool lid = s == 0 ? (e == 0) : (e == c.NeZ - 1);
+      const int lP = lid ? lM : (s == 0 ? lM - 1 : lM + 1);
+      const int sP = lid ? sc : (s == 0 ? sb : st), nP = lid ? nM : (s == 0 ? N : 0);
+      const T nz = s == 0 ? T(-1) : T(1);
+      const T al = (T)(s == 0 ? c.alB(e) : c.alT(e));
+      const double mzMd = c.P[3 * lM + 1];
+      const double mzPd = lid ? -mzMd : c.P[3 * lP + 1];
+      const T mzM = (T)mzMd, mzP = (T)mzPd;
+      const T dmz = (T)(mzPd - mzMd);
+      T val;
+      if (v == 0) val = tmp1 * (dmz * nz - al * (T)(c.P[3 * lP] - c.P[3 * lM]));
+      else if (v == 1) val = tmp1 * ((R(sP, 0, nP) - R(sc, 0, nM)) * nz - al * dmz);
+      else val = tmp1 * ((R(sP, 2, nP) * mzP - R(sc, 2, nM) * mzM) * nz - al * (T)(c.P[3 * lP + 2] - c.P[3 * lM + 2]));
+      reinterpret_cast<T*>(c.del)[t] = val;
+    }
+    __syncwarp();
+    {
+      const int l = e * N1 + k;
+      T sd = 0, sm = 0, sr = 0, drho = 0;
+#pragma unroll
+      for (int m = 0; m < N1; ++m) {
+        T mz, dd;
+        if constexpr (CERT) {
+          mz = c.P[3 * (e * N1 + m) + 1];
+          dd = c.P[3 * (e * N1 + m)];
+        } else {
+          mz = R(sc, 3, m);
+          dd = R(sc, 4, m);
+        }
+        sd += Dk[m] * mz;
+        sm += Dk[m] * R(sc, 0, m);
+        sr += Dk[m] * R(sc, 1, m);
+        drho += Tk[m] * dd;
+      }
+      const T* dl = reinterpret_cast<const T*>(c.del);
+      T A[3];
+      A[0] = -(E33 * sd + lbk * dl[0] + ltk * dl[3]);
+      A[1] = -(E33 * sm + lbk * dl[1] + ltk * dl[4]) - grav * drho;
+      A[2] = -(E33 * sr + lbk * dl[2] + ltk * dl[5]);
+      const size_t gi = c.g(e);
+      const float isc[3] = {1.f / __ldg(pr.dhf + l), 1.f / (__ldg(pr.dhf + l) * (float)cref), 1.f / __ldg(pr.rhf + l)};
+#pragma unroll
+      for (int v = 0; v < 3; ++v) {
+        const double qmp = __ldg(qin.v[gv[v]] + gi) - c.P[3 * l + v];
+        float bfl;
+        if constexpr (CERT) bfl = (float)fma(impl_fac, A[v], qmp);
+        else bfl = fmaf((float)impl_fac, A[v], (float)qmp);
+        c.Bf[3 * l + v] = bfl;
+        errf = fmaxf(errf, fabsf(bfl) * isc[v]);
+        if (!(fabsf(bfl) < 3.0e38f)) errf = __int_as_float(0x7fc00000);
+      }
+    }
+    __syncwarp();
+    if (e + 2 < c.NeZ) fill(e + 2);
+    __syncwarp();
+  }
+  return grp_max_nan(errf, N1);
+}
+
+// ---------------------------------------------------------------------------------------------
+// element LU without pivoting of the 3*N1 rows held 3 per lane (row 3k+v in lane k), with four
+// right-hand sides; on return r = A^-1 r.  The pivot row goes through the group's shared buffer.
+template <int N1>
+__device__ __forceinline__ void lu_rows(float (&a)[3][3 * N1], float (&r)[3][4], float* prow, int k) {
+  constexpr int n = 3 * N1, PRW = Col<N1>::PRW;
+  float4* p4 = reinterpret_cast<float4*>(prow);
+#pragma unroll
+  for (int kk = 0; kk < n; ++kk) {
+    const int owner = kk / 3, vv = kk % 3;
+    const int q0 = kk / 4;
+    if (k == owner) {
+      float t[PRW];
+#pragma unroll
+      for (int cc = 0; cc < PRW; ++cc) t[cc] = 0.f;
+#pragma unroll
+      for (int cc = 4 * q0; cc < n; ++cc) t[cc] = a[vv][cc];
+#pragma unroll
+      for (int m = 0; m < 4; ++m) t[n + m] = r[vv][m];
+      t[n + 4] = __fdividef(1.f, a[vv][kk]);
+#pragma unroll
+      for (int q = q0; q < PRW / 4; ++q) p4[q] = make_float4(t[4 * q], t[4 * q + 1], t[4 * q + 2], t[4 * q + 3]);
+    }
+    __syncwarp();
+    float pr[PRW];
+#pragma unroll
+    for (int q = q0; q < PRW / 4; ++q) {
+      const float4 x = p4[q];
+      pr[4 * q] = x.x; pr[4 * q + 1] = x.y; pr[4 * q + 2] = x.z; pr[4 * q + 3] = x.w;
+    }
+#pragma unroll
+    for (int v = 0; v < 3; ++v) {
+      if (3 * k + v > kk) {
+        const float f = a[v][kk] * pr[n + 4];
+#pragma unroll
+        for (int cc = kk + 1; cc < n; ++cc) a[v][cc] = fmaf(-f, pr[cc], a[v][cc]);
+#pragma unroll
+        for (int m = 0; m < 4; ++m) r[v][m] = fmaf(-f, pr[n + m], r[v][m]);
+      }
+    }
+    __syncwarp();
+  }
+  // back substitution U x = r
+#pragma unroll
+  for (int kk = n - 1; kk >= 0; --kk) {
+    const int owner = kk / 3, vv = kk % 3;
+    if (k == owner) {
+      const float rd = __fdividef(1.f, a[vv][kk]);
+#pragma unroll
+      for (int m = 0; m < 4; ++m) r[vv][m] *= rd;
+      p4[0] = make_float4(r[vv][0], r[vv][1], r[vv][2], r[vv][3]);
+    }
+    __syncwarp();
+    const float4 x = p4[0];
+#pragma unroll
+    for (int v = 0; v < 3; ++v) {
+      if (3 * k + v < kk) {
+        const float av = a[v][kk];
+        r[v][0] = fmaf(-av, x.x, r[v][0]);
+        r[v][1] = fmaf(-av, x.y, r[v][1]);
+        r[v][2] = fmaf(-av, x.z, r[v][2]);
+        r[v][3] = fmaf(-av, x.w, r[v][3]);
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// one Newton correction of the DENS/MOMZ/RHOT system from the residual in c.Bf and the Jacobian
+// quantities in c.Jq: construct_matbnd (hevi_common_2.F90:1325-1480), block-Thomas with the
+// 3x3 couplings of the face nodes, element LU; P += correction where apply.  G history in gscr.
+template <int N1>
+__device__ void col_solve(const Ops& op, const Col<N1>& c, double impl_fac, float* __restrict__ gsc, size_t gcol,
+                          size_t glayer, bool apply) {
+  constexpr int N = N1 - 1, n3 = 3 * N1;
+  const int k = c.k;
+  const float fi = (float)impl_fac;
+  const float fdzs = (float)op.E33 * fi;
+  float Dk[N1], Tk[N1];
+#pragma unroll
+  for (int m = 0; m < N1; ++m) {
+    Dk[m] = fdzs * (float)op.D[k * N1 + m];
+    Tk[m] = fi * (float)op.grav * (float)op.T[k * N1 + m];
+  }
+  const float facB = 0.5f * fi * (float)op.Lb[k] * (float)op.FSz;
+  const float facT = 0.5f * fi * (float)op.Lt[k] * (float)op.FSz;
+  for (int e = 0; e < c.NeZ; ++e) {
+    float a[3][n3];
+    float r[3][4];
+    float4 J[N1];
+#pragma unroll
+    for (int m = 0; m < N1; ++m) J[m] = c.Jq[e * N1 + m];
+#pragma unroll
+    for (int m = 0; m < N1; ++m) {
+      const float fdz = Dk[m];
+      const float id = (m == k) ? 1.f : 0.f;
+      a[0][3 * m + 0] = id;
+      a[0][3 * m + 1] = fdz;
+      a[0][3 * m + 2] = 0.f;
+      a[1][3 * m + 0] = Tk[m];
+      a[1][3 * m + 1] = id;
+      a[1][3 * m + 2] = fdz * J[m].z;
+      a[2][3 * m + 0] = -fdz * J[m].x * J[m].y;
+      a[2][3 * m + 1] = fdz * J[m].x;
+      a[2][3 * m + 2] = id + fdz * J[m].y;
+    }
+    float Lc[3][3], Uc[3][3];
+#pragma unroll
+    for (int f = 0; f < 2; ++f) {
+      const bool bnd = (f == 0) ? (e == 0) : (e == c.NeZ - 1);
+      const int pv1 = f == 0 ? 0 : N;
+      const int l1 = e * N1 + pv1;
+      const float nz = f == 0 ? -1.f : 1.f;
+      const float al = f == 0 ? c.alB(e) : c.alT(e);
+      const float fac = f == 0 ? facB : facT;
+      const float t1 = fac * al, t2 = fac * nz;
+      const float pot1 = J[pv1].x, wt1 = J[pv1].y, dpd1 = J[pv1].z;
+      const int c0 = 3 * pv1;
+      float cc[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+      if (bnd) {  // slip lid: exterior MOMZ = -interior
+        a[2][c0 + 0] += 2.f * t2 * pot1 * wt1;
+        a[0][c0 + 1] -= 2.f * t2;
+        a[1][c0 + 1] += 2.f * t1;
+        a[2][c0 + 1] -= 2.f * t2 * pot1;
+        a[2][c0 + 2] -= 2.f * t2 * wt1;
+      } else {
+        a[0][c0 + 0] += t1;
+        a[2][c0 + 0] += t2 * pot1 * wt1;
+        a[0][c0 + 1] -= t2;
+        a[1][c0 + 1] += t1;
+        a[2][c0 + 1] -= t2 * pot1;
+        a[1][c0 + 2] -= t2 * dpd1;
+        a[2][c0 + 2] += t1 - t2 * wt1;
+        const float4 Jn = c.Jq[f == 0 ? l1 - 1 : l1 + 1];
+        cc[0][0] = -t1; cc[0][1] = t2;
+        cc[1][1] = -t1; cc[1][2] = t2 * Jn.z;
+        cc[2][0] = -t2 * Jn.x * Jn.y; cc[2][1] = t2 * Jn.x; cc[2][2] = -t1 + t2 * Jn.y;
+      }
+#pragma unroll
+      for (int v = 0; v < 3; ++v)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          if (f == 0) Lc[v][j] = cc[v][j];
+          else Uc[v][j] = cc[v][j];
+        }
+    }
+    const int l = e * N1 + k;
+#pragma unroll
+    for (int v = 0; v < 3; ++v) r[v][0] = c.Bf[3 * l + v];
+    if (e > 0) {  // A_e -= L_e G_{e-1}, b_e -= L_e y_{e-1} (rows of node N of element e-1)
+      const float4 b0 = reinterpret_cast<const float4*>(c.bc)[0];
+      const float4 b1 = reinterpret_cast<const float4*>(c.bc)[1];
+      const float4 b2 = reinterpret_cast<const float4*>(c.bc)[2];
+      const float Gp[3][3] = {{b0.x, b0.y, b0.z}, {b1.x, b1.y, b1.z}, {b2.x, b2.y, b2.z}};
+      const float yp[3] = {b0.w, b1.w, b2.w};
+#pragma unroll
+      for (int v = 0; v < 3; ++v) {
+#pragma unroll
+        for (int c2 = 0; c2 < 3; ++c2)
+          a[v][c2] -= Lc[v][0] * Gp[0][c2] + Lc[v][1] * Gp[1][c2] + Lc[v][2] * Gp[2][c2];
+        r[v][0] -= Lc[v][0] * yp[0] + Lc[v][1] * yp[1] + Lc[v][2] * yp[2];
+      }
+    }
+    const bool last = e == c.NeZ - 1;
+#pragma unroll
+    for (int v = 0; v < 3; ++v)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) r[v][1 + j] = last ? 0.f : Uc[v][j];
+    __syncwarp();  // everyone has read c.bc
+    lu_rows<N1>(a, r, c.prow, k);
+#pragma unroll
+    for (int v = 0; v < 3; ++v) c.Bf[3 * l + v] = r[v][0];
+    float4* gp = reinterpret_cast<float4*>(gsc + (gcol + (size_t)e * glayer) * 12 * N1 + 12 * k);
+    gp[0] = make_float4(r[0][1], r[0][2], r[0][3], r[1][1]);
+    gp[1] = make_float4(r[1][2], r[1][3], r[2][1], r[2][2]);
+    gp[2] = make_float4(r[2][3], 0.f, 0.f, 0.f);
+    if (k == N) {
+      float4* b4 = reinterpret_cast<float4*>(c.bc);
+      b4[0] = make_float4(r[0][1], r[0][2], r[0][3], r[0][0]);
+      b4[1] = make_float4(r[1][1], r[1][2], r[1][3], r[1][0]);
+      b4[2] = make_float4(r[2][1], r[2][2], r[2][3], r[2][0]);
+    }
+    __syncwarp();
+  }
+  // back sweep: x_e = y_e - G_e x_{e+1}(node 0)
+  for (int e = c.NeZ - 2; e >= 0; --e) {
+    const int l = e * N1 + k;
+    const float* x1 = c.Bf + 3 * (e + 1) * N1;
+    const float xa = x1[0], xb = x1[1], xc = x1[2];
+    const float4* gp = reinterpret_cast<const float4*>(gsc + (gcol + (size_t)e * glayer) * 12 * N1 + 12 * k);
+    const float4 g0 = gp[0], g1 = gp[1], g2 = gp[2];
+    c.Bf[3 * l + 0] -= g0.x * xa + g0.y * xb + g0.z * xc;
+    c.Bf[3 * l + 1] -= g0.w * xa + g1.x * xb + g1.y * xc;
+    c.Bf[3 * l + 2] -= g1.z * xa + g1.w * xb + g2.x * xc;
+    __syncwarp();
+  }
+  if (apply) {
+    for (int e = 0; e < c.NeZ; ++e) {
+      const int l = e * N1 + k;
+#pragma unroll
+      for (int v = 0; v < 3; ++v) c.P[3 * l + v] += (double)c.Bf[3 * l + v];
+    }
+  }
+  __syncwarp();
+}
+
+// ---------------------------------------------------------------------------------------------
+template <int N1>
+__global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const Prof pf, const ProfF pff, const double* __restrict__ rhinv,
+                                                const PresSeries ps, const F5c qin, const F5c z,
+                                                const float* const* guess, float* const* qsf, float* const* tout,
+                                                float* __restrict__ gsc, int* status, unsigned long long* cnt,
+                                                const MixViArgs args, int ncol) {
+  constexpr int N = N1 - 1, C = 32 / N1, NF = N1 * N1, Np = N1 * N1 * N1;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int lane = threadIdx.x & 31;
+  const int grp = lane / N1, k = lane % N1;
+  const int col0 = blockIdx.x * C;
+  if (col0 >= ncol) return;  // ncol is a multiple of C: warps are all-valid or all-invalid
+  const int col = col0 + grp;
+  const int NeZ = op.NeZ, L = op.L;
+  const ColLayout lay(N1, NeZ);
+  unsigned char* base = smraw + (size_t)grp * lay.stride;
+  Col<N1> c;
+  c.P = reinterpret_cast<double*>(base + lay.oP);
+  c.Jq = reinterpret_cast<float4*>(base + lay.oJq);
+  c.ring = reinterpret_cast<double*>(base + lay.oRing);
+  c.del = reinterpret_cast<double*>(base + lay.oDel);
+  c.Bf = reinterpret_cast<float*>(base + lay.oBf);
+  c.prow = reinterpret_cast<float*>(base + lay.oProw);
+  c.bc = reinterpret_cast<float*>(base + lay.oBc);
+  c.al = reinterpret_cast<float*>(base + lay.oAl);
+  c.jb = reinterpret_cast<float*>(base + lay.oJb);
+  c.k = k; c.NeZ = NeZ; c.L = L;
+  {
+    const int ij = col % NF, exy = col / NF;
+    const int ci = ij % N1, cj = ij / N1;
+    const size_t nxy = (size_t)op.NeX * op.NeY;
+    c.gb = (size_t)exy * Np + ci + N1 * cj + NF * k;
+    c.gs = nxy * Np;
+  }
+  const double impl_fac = args.impl_fac;
+  const float kapf = (float)op.kap;
+
+  // ---- frozen vertical Rusanov speed |w| + c of var0 (hevi_common_2.F90:1149-1155) ----
+  float* atmp = c.Bf;  // [L]
+  for (int e = 0; e < NeZ; ++e) {
+    const int l = e * N1 + k;
+    const size_t gi = c.g(e);
+    const float dd0 = (float)__ldg(z.v[VD] + gi), dr0 = (float)__ldg(z.v[VRT] + gi);
+    const float rdens0 = 1.f / (__ldg(pff.dens + l) + dd0);
+    const float wt0 = (float)__ldg(z.v[VMZ] + gi) * rdens0;
+    const float pres0 = __ldg(pff.pres + l) * (1.f + expm1f(kapf * log1pf(dr0 * __ldg(pff.rtherm + l))));
+    atmp[l] = fabsf(wt0) + sqrtf(kapf * pres0 * rdens0);
+  }
+  __syncwarp();
+  for (int e = k; e < NeZ; e += N1) {
+    const int lb = e * N1, lt = e * N1 + N;
+    c.al[2 * e] = fmaxf(atmp[lb], atmp[e > 0 ? lb - 1 : lb]);
+    c.al[2 * e + 1] = fmaxf(atmp[lt], atmp[e < NeZ - 1 ? lt + 1 : lt]);
+  }
+  __syncwarp();
+
+  // ---- MOMX/MOMY (eval_Ax_uv / solve_uv): residual with FP64 jumps, interface reduction ----
+  {
+    double* Pu = c.P;   // [2L]
+    float* bu = c.Bf;   // [2L]
+    for (int e = 0; e < NeZ; ++e) {
+      const int l = e * N1 + k;
+      const size_t gi = c.g(e);
+      Pu[2 * l] = __ldg(z.v[VMX] + gi);
+      Pu[2 * l + 1] = __ldg(z.v[VMY] + gi);
+    }
+    __syncwarp();
+    const float cfs = (float)(0.5 * impl_fac * op.FSz);
+    const float lbk = (float)op.Lb[k], ltk = (float)op.Lt[k];
+    const float lb0 = (float)op.Lb[0], lbN = (float)op.Lb[N], lt0 = (float)op.Lt[0], ltN = (float)op.Lt[N];
+    const float iscu_c = 1.f / (float)args.cref;
+    float* jdel = reinterpret_cast<float*>(c.del);  // 4 jumps of the current element
+    bool active = true;
+    for (int it = 0; it < 4; ++it) {
+      float err = 0.f;
+      for (int e = 0; e < NeZ; ++e) {
+        // bottom and top jumps (neighbour - own) of both components: lanes t < 4
+        for (int t = k; t < 4; t += N1) {
+          const int s = t >> 1, m = t & 1;
+          const int lM = e * N1 + (s == 0 ? 0 : N);
+          const bool lid = s == 0 ? (e == 0) : (e == NeZ - 1);
+          const int lP = lid ? lM : (s == 0 ? lM - 1 : lM + 1);
+          jdel[t] = (float)(Pu[2 * lP + m] - Pu[2 * lM + m]);
+        }
+        __syncwarp();
+        const int l = e * N1 + k;
+        const size_t gi = c.g(e);
+        const float iscu = iscu_c / __ldg(pff.dens + l);
+        const float aB = lbk * c.alB(e), aT = ltk * c.alT(e);
+#pragma unroll
+        for (int m = 0; m < 2; ++m) {
+          const float Af = cfs * (aB * jdel[m] + aT * jdel[2 + m]);  // impl_fac * A(P)
+          const double qmp = __ldg(qin.v[VMX + m] + gi) - Pu[2 * l + m];
+          const float b = Af + (float)qmp;
+          bu[2 * l + m] = b;
+          err = fmaxf(err, fabsf(b) * iscu);
+        }
+        __syncwarp();
+      }
+      err = grp_max_nan(err, N1);
+      const bool need = active && !(err <= args.tol) && it < 3;
+      if (!__any_sync(FULL, need)) break;
+      // interface jumps J_e = d_e0 - d_{e-1,N} (e = 1..NeZ-1) from the scalar tridiagonal system
+      //   (1 + beta_e0 + tau_{e-1,N}) J_e - tau_e0 J_{e+1} - beta_{e-1,N} J_{e-1} = b_e0 - b_{e-1,N}
+      // with beta_ep = cfs Lb[p] alB_e, tau_ep = cfs Lt[p] alT_e; then
+      //   d_ep = b_ep - beta_ep J_e + tau_ep J_{e+1}   (J_0 = J_NeZ = 0: slip lids)
+      float* cp = c.jb;             // [NeZ+1]
+      float* Jx = c.jb + (NeZ + 1); // [NeZ+1]
+      float* Jy = Jx + (NeZ + 1);   // [NeZ+1]
+      if (k == 0) {
+        Jx[0] = Jy[0] = 0.f;
+        Jx[NeZ] = Jy[NeZ] = 0.f;
+        float cprev = 0.f, rxp = 0.f, ryp = 0.f;
+        for (int e = 1; e < NeZ; ++e) {
+          const float aa = e >= 2 ? -cfs * lbN * c.alB(e - 1) : 0.f;  // -beta_{e-1,N}
+          const float dd = 1.f + cfs * lb0 * c.alB(e) + cfs * ltN * c.alT(e - 1);
+          const float cc = e < NeZ - 1 ? -cfs * lt0 * c.alT(e) : 0.f;  // -tau_{e,0}
+          const float ip = __fdividef(1.f, dd - aa * cprev);
+          const float rx = bu[2 * (e * N1)] - bu[2 * ((e - 1) * N1 + N)];
+          const float ry = bu[2 * (e * N1) + 1] - bu[2 * ((e - 1) * N1 + N) + 1];
+          cprev = cc * ip;
+          rxp = (rx - aa * rxp) * ip;
+          ryp = (ry - aa * ryp) * ip;
+          cp[e] = cprev;
+          Jx[e] = rxp;
+          Jy[e] = ryp;
+        }
+        for (int e = NeZ - 2; e >= 1; --e) {
+          Jx[e] -= cp[e] * Jx[e + 1];
+          Jy[e] -= cp[e] * Jy[e + 1];
+        }
+      }
+      __syncwarp();
+      if (need) {
+        for (int e = 0; e < NeZ; ++e) {
+          const int l = e * N1 + k;
+          const float beta = e > 0 ? cfs * lbk * c.alB(e) : 0.f;
+          const float tau = e < NeZ - 1 ? cfs * ltk * c.alT(e) : 0.f;
+          Pu[2 * l] += (double)(bu[2 * l] - beta * Jx[e] + tau * Jx[e + 1]);
+          Pu[2 * l + 1] += (double)(bu[2 * l + 1] - beta * Jy[e] + tau * Jy[e + 1]);
+        }
+      }
+      active = need;
+      __syncwarp();
+    }
+    for (int e = 0; e < NeZ; ++e) {
+      const int l = e * N1 + k;
+      const size_t gi = c.g(e);
+      const double dh64 = __ldg(pf.dens + l);
+      const double px = Pu[2 * l], py = Pu[2 * l + 1];
+      qsf[VMX][gi] = (float)fma(-dh64, args.Uref, px);
+      qsf[VMY][gi] = (float)fma(-dh64, args.Vref, py);
+      tout[VMX][gi] = (float)(px - __ldg(qin.v[VMX] + gi)) * (float)args.inv_impl_fac;
+      tout[VMY][gi] = (float)(py - __ldg(qin.v[VMY] + gi)) * (float)args.inv_impl_fac;
+    }
+    __syncwarp();
+  }
+
+  // ---- DENS/MOMZ/RHOT Newton ----
+  const int gv[3] = {VD, VMZ, VRT};
+  for (int e = 0; e < NeZ; ++e) {
+    const int l = e * N1 + k;
+    const size_t gi = c.g(e);
+#pragma unroll
+    for (int m = 0; m < 3; ++m)
+      c.P[3 * l + m] = guess ? __ldg(qin.v[gv[m]] + gi) + (double)__ldg(guess[m] + gi) : __ldg(z.v[gv[m]] + gi);
+  }
+  __syncwarp();
+  const ResIn rin{pf.dens, pf.pres, pf.rhyd, rhinv, pff.dens, pff.pres, pff.therm, pff.rtherm};
+  const size_t gcolumn = (size_t)col, glayer = (size_t)ncol;  // G history rows of this column
+  col_residual<N1, false>(op, c, rin, ps, qin, impl_fac, args.cref);
+  col_solve<N1>(op, c, impl_fac, gsc, gcolumn, glayer, true);
+  int nsolve = 1, st = 0;
+  bool active = true;
+  while (true) {
+    const float err = args.check64 ? col_residual<N1, true>(op, c, rin, ps, qin, impl_fac, args.cref)
+                                   : col_residual<N1, false>(op, c, rin, ps, qin, impl_fac, args.cref);
+    if (active) {
+      if (err != err) { st = -2; active = false; }
+      else if ((double)err <= args.tol) { st = nsolve; active = false; }
+      else if (nsolve >= args.max_iter) { st = -1; active = false; }
+    }
+    if (!__any_sync(FULL, active)) break;
+    col_solve<N1>(op, c, impl_fac, gsc, gcolumn, glayer, active);
+    ++nsolve;
+  }
+  for (int e = 0; e < NeZ; ++e) {
+    const int l = e * N1 + k;
+    const size_t gi = c.g(e);
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      const double pnew = c.P[3 * l + m];
+      qsf[gv[m]][gi] = (float)pnew;
+      tout[gv[m]][gi] = (float)(pnew - __ldg(qin.v[gv[m]] + gi)) * (float)args.inv_impl_fac;
+    }
+  }
+  if (k == 0 && status) status[col] = st;
+  const unsigned nfail = __reduce_add_sync(FULL, (k == 0 && st < 0) ? 1u : 0u);
+  const unsigned nsol = __reduce_add_sync(FULL, (k == 0 && st >= 0) ? (unsigned)st : 0u);
+  const unsigned nok = __reduce_add_sync(FULL, (k == 0 && st >= 0) ? 1u : 0u);
+  if (lane == 0) {
+    if (nfail) atomicAdd(cnt, (unsigned long long)nfail);
+    if (nok) {
+      atomicAdd(cnt + 1, (unsigned long long)nsol);
+      atomicAdd(cnt + 2, (unsigned long long)nok);
+    }
+  }
+}
+
+template <int N1>
+int launch_n(const Ops& op, const Prof& pf, const ProfF& pff, const double* rhinv, const PresSeries& ps,
+             const F5c& qin, const F5c& z, const float* const* guess, float* const* qsf, float* const* tout, float* gsc,
+             int* status, unsigned long long* cnt, const MixViArgs& a, cudaStream_t s) {
+  constexpr int C = 32 / N1;
+  const ColLayout lay(N1, op.NeZ);
+  const size_t smem = (size_t)lay.stride * C;
+  if (smem > 227 * 1024) return (int)cudaErrorInvalidValue;
+  const int ncol = op.NeX * op.NeY * N1 * N1;
+  auto kfn = k_vi_cols<N1>;
+  cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  kfn<<<(ncol + C - 1) / C, 32, smem, s>>>(op, pf, pff, rhinv, ps, qin, z, guess, qsf, tout, gsc, status, cnt, a, ncol);
+  return (int)cudaGetLastError();
+}
+
+}  // namespace
+
+size_t vi_cols_scratch_floats(size_t nodes) { return (size_t)12 * nodes; }
+
+int launch_vi_cols(int N1, const Ops& op, const Prof& pf, const ProfF& pff, const double* rhinv, const PresSeries& ps,
+                   const F5c& qin, const F5c& z, const float* const* guess, float* const* qsf, float* const* tout,
+                   float* gsc, int* status, unsigned long long* cnt, const MixViArgs& a, cudaStream_t s) {
+  switch (N1) {
+    case 4: return launch_n<4>(op, pf, pff, rhinv, ps, qin, z, guess, qsf, tout, gsc, status, cnt, a, s);
+    case 8: return launch_n<8>(op, pf, pff, rhinv, ps, qin, z, guess, qsf, tout, gsc, status, cnt, a, s);
+  }
+  return (int)cudaErrorInvalidValue;
+}
+
+}  // namespace fedg
