@@ -38,17 +38,15 @@ constexpr unsigned FULL = 0xffffffffu;
 // per-column shared-memory layout (bytes); the column stride is padded so that the C columns
 // of a warp start on different banks
 struct ColLayout {
-  int oP, oJq, oRing, oDel, oBf, oProw, oBc, oAl, oJb, stride;
+  int oP, oJq, oRing, oDel, oBf, oBc, oAl, oJb, stride;
   __host__ __device__ ColLayout(int N1, int NeZ) {
     const int L = N1 * NeZ;
-    const int prw = ((3 * N1 + 5 + 3) / 4) * 4;
     int o = 0;
     oP = o;    o += 24 * L;                    // double P[3L] (uv phase: P[2L])
     oJq = o;   o += 16 * L;                    // float4 Jq[L]: pot, wt, dpd of the Jacobian
     oRing = o; o += 72 * N1;                   // 3 element slots x N1 nodes x 3 doubles
     oDel = o;  o += 48;                        // 6 face fluxes of the current element
     oBf = o;   o += 12 * L;                    // float b / y / x [3L] (uv phase: [2L])
-    oProw = o; o += 4 * prw;                   // pivot row + right-hand sides + 1/pivot
     oBc = o;   o += 64;                        // block-Thomas coupling from the element below
     oAl = o;   o += ((8 * NeZ + 15) / 16) * 16; // alB, alT per element
     oJb = o;   o += ((12 * (NeZ + 1) + 15) / 16) * 16;  // uv: c' and the two interface jumps
@@ -60,13 +58,11 @@ struct ColLayout {
 
 template <int N1>
 struct Col {
-  static constexpr int PRW = ((3 * N1 + 5 + 3) / 4) * 4;
   double* P;
   float4* Jq;
   double* ring;  // [3][3][N1]: slot, quantity (fm, fr, pot), node
   double* del;
   float* Bf;
-  float* prow;
   float* bc;
   float* al;
   float* jb;
@@ -248,71 +244,58 @@ __device__ float col_residual(const Ops& op, const Col<N1>& c, const ResIn& pr, 
 }
 
 // ---------------------------------------------------------------------------------------------
-// element LU without pivoting of the 3*N1 rows held 3 per lane (row 3k+v in lane k), with four
-// right-hand sides; on return r = A^-1 r.  The pivot row goes through the group's shared buffer.
+// Element LU without pivoting of the 3*N1 rows held 3 per lane (row 3k+v in lane k), with four
+// right-hand sides; on return r = A^-1 r.  The pivot row reaches the other lanes of the column
+// group by shuffles (width N1), and rows that a step does not touch get a zero multiplier, so
+// the factorisation is branch-free and needs neither shared memory nor barriers.  The pivot
+// index is a template parameter so every register index is a compile-time constant.
+template <int N1, int kk>
+__device__ __forceinline__ void shfl_fwd(float (&a)[3][3 * N1], float (&r)[3][4], int k) {
+  constexpr int n = 3 * N1;
+  if constexpr (kk < n) {
+    constexpr int owner = kk / 3, vv = kk % 3;
+    const float piv = __shfl_sync(FULL, a[vv][kk], owner, N1);
+    const float inv = __fdividef(1.f, piv);
+    float f[3];
+#pragma unroll
+    for (int v = 0; v < 3; ++v) f[v] = (3 * k + v > kk) ? a[v][kk] * inv : 0.f;
+#pragma unroll
+    for (int cc = kk + 1; cc < n; ++cc) {
+      const float p = __shfl_sync(FULL, a[vv][cc], owner, N1);
+#pragma unroll
+      for (int v = 0; v < 3; ++v) a[v][cc] = fmaf(-f[v], p, a[v][cc]);
+    }
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const float p = __shfl_sync(FULL, r[vv][m], owner, N1);
+#pragma unroll
+      for (int v = 0; v < 3; ++v) r[v][m] = fmaf(-f[v], p, r[v][m]);
+    }
+    shfl_fwd<N1, kk + 1>(a, r, k);
+  }
+}
+template <int N1, int kk>
+__device__ __forceinline__ void shfl_bwd(float (&a)[3][3 * N1], float (&r)[3][4], int k) {
+  if constexpr (kk >= 0) {
+    constexpr int owner = kk / 3, vv = kk % 3;
+    const float inv = __fdividef(1.f, __shfl_sync(FULL, a[vv][kk], owner, N1));
+    float x[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) x[m] = __shfl_sync(FULL, r[vv][m], owner, N1) * inv;
+#pragma unroll
+    for (int v = 0; v < 3; ++v) {
+      const int row = 3 * k + v;
+      const float g = row < kk ? a[v][kk] : 0.f;
+#pragma unroll
+      for (int m = 0; m < 4; ++m) r[v][m] = row == kk ? x[m] : fmaf(-g, x[m], r[v][m]);
+    }
+    shfl_bwd<N1, kk - 1>(a, r, k);
+  }
+}
 template <int N1>
-__device__ __forceinline__ void lu_rows(float (&a)[3][3 * N1], float (&r)[3][4], float* prow, int k) {
-  constexpr int n = 3 * N1, PRW = Col<N1>::PRW;
-  float4* p4 = reinterpret_cast<float4*>(prow);
-#pragma unroll
-  for (int kk = 0; kk < n; ++kk) {
-    const int owner = kk / 3, vv = kk % 3;
-    const int q0 = kk / 4;
-    if (k == owner) {
-      float t[PRW];
-#pragma unroll
-      for (int cc = 0; cc < PRW; ++cc) t[cc] = 0.f;
-#pragma unroll
-      for (int cc = 4 * q0; cc < n; ++cc) t[cc] = a[vv][cc];
-#pragma unroll
-      for (int m = 0; m < 4; ++m) t[n + m] = r[vv][m];
-      t[n + 4] = __fdividef(1.f, a[vv][kk]);
-#pragma unroll
-      for (int q = q0; q < PRW / 4; ++q) p4[q] = make_float4(t[4 * q], t[4 * q + 1], t[4 * q + 2], t[4 * q + 3]);
-    }
-    __syncwarp();
-    float pr[PRW];
-#pragma unroll
-    for (int q = q0; q < PRW / 4; ++q) {
-      const float4 x = p4[q];
-      pr[4 * q] = x.x; pr[4 * q + 1] = x.y; pr[4 * q + 2] = x.z; pr[4 * q + 3] = x.w;
-    }
-#pragma unroll
-    for (int v = 0; v < 3; ++v) {
-      if (3 * k + v > kk) {
-        const float f = a[v][kk] * pr[n + 4];
-#pragma unroll
-        for (int cc = kk + 1; cc < n; ++cc) a[v][cc] = fmaf(-f, pr[cc], a[v][cc]);
-#pragma unroll
-        for (int m = 0; m < 4; ++m) r[v][m] = fmaf(-f, pr[n + m], r[v][m]);
-      }
-    }
-    __syncwarp();
-  }
-  // back substitution U x = r
-#pragma unroll
-  for (int kk = n - 1; kk >= 0; --kk) {
-    const int owner = kk / 3, vv = kk % 3;
-    if (k == owner) {
-      const float rd = __fdividef(1.f, a[vv][kk]);
-#pragma unroll
-      for (int m = 0; m < 4; ++m) r[vv][m] *= rd;
-      p4[0] = make_float4(r[vv][0], r[vv][1], r[vv][2], r[vv][3]);
-    }
-    __syncwarp();
-    const float4 x = p4[0];
-#pragma unroll
-    for (int v = 0; v < 3; ++v) {
-      if (3 * k + v < kk) {
-        const float av = a[v][kk];
-        r[v][0] = fmaf(-av, x.x, r[v][0]);
-        r[v][1] = fmaf(-av, x.y, r[v][1]);
-        r[v][2] = fmaf(-av, x.z, r[v][2]);
-        r[v][3] = fmaf(-av, x.w, r[v][3]);
-      }
-    }
-    __syncwarp();
-  }
+__device__ __forceinline__ void lu_rows(float (&a)[3][3 * N1], float (&r)[3][4], int k) {
+  shfl_fwd<N1, 0>(a, r, k);
+  shfl_bwd<N1, 3 * N1 - 1>(a, r, k);
 }
 
 // one Newton correction of the DENS/MOMZ/RHOT system from the residual in c.Bf and the Jacobian
@@ -416,7 +399,7 @@ __device__ void col_solve(const Ops& op, const Col<N1>& c, double impl_fac, floa
 #pragma unroll
       for (int j = 0; j < 3; ++j) r[v][1 + j] = last ? 0.f : Uc[v][j];
     __syncwarp();  // everyone has read c.bc
-    lu_rows<N1>(a, r, c.prow, k);
+    lu_rows<N1>(a, r, k);
 #pragma unroll
     for (int v = 0; v < 3; ++v) c.Bf[3 * l + v] = r[v][0];
     float4* gp = reinterpret_cast<float4*>(gsc + (gcol + (size_t)e * glayer) * 12 * N1 + 12 * k);
@@ -476,7 +459,6 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const Prof pf, con
   c.ring = reinterpret_cast<double*>(base + lay.oRing);
   c.del = reinterpret_cast<double*>(base + lay.oDel);
   c.Bf = reinterpret_cast<float*>(base + lay.oBf);
-  c.prow = reinterpret_cast<float*>(base + lay.oProw);
   c.bc = reinterpret_cast<float*>(base + lay.oBc);
   c.al = reinterpret_cast<float*>(base + lay.oAl);
   c.jb = reinterpret_cast<float*>(base + lay.oJb);
@@ -510,15 +492,46 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const Prof pf, con
   }
   __syncwarp();
 
-  // ---- MOMX/MOMY (eval_Ax_uv / solve_uv): residual with FP64 jumps, interface reduction ----
+  // ---- MOMX/MOMY (eval_Ax_uv / solve_uv) ----
+  // The operator is linear and acts on the face jumps only.  With P = P0 + D (P0 = var0 in FP64,
+  // D an FP32 increment), b(P) = [impl_fac A(P0) + (q* - P0)] + impl_fac A(D) - D.  The FP64 work is
+  // q* - P0, kept as an FP32 pair hi + lo so the residual has the accuracy of the FP64 difference,
+  // and the face jumps of P0, once per column; everything after that is FP32.
   {
-    double* Pu = c.P;   // [2L]
-    float* bu = c.Bf;   // [2L]
+    double* P0 = c.P;                                   // [2L] FP64, only while the jumps are formed
+    float* qh = reinterpret_cast<float*>(c.Jq);         // [2L] (q* - P0) hi
+    float* ql = qh + 2 * L;                             // [2L] (q* - P0) lo
+    float* D = reinterpret_cast<float*>(c.P);           // [2L] increment, once P0 is dead
+    float* j0 = reinterpret_cast<float*>(c.P) + 4 * L;  // [4 NeZ] face jumps of P0
+    float* bu = c.Bf;                                   // [2L] residual
     for (int e = 0; e < NeZ; ++e) {
       const int l = e * N1 + k;
       const size_t gi = c.g(e);
-      Pu[2 * l] = __ldg(z.v[VMX] + gi);
-      Pu[2 * l + 1] = __ldg(z.v[VMY] + gi);
+#pragma unroll
+      for (int m = 0; m < 2; ++m) {
+        const double p0 = __ldg(z.v[VMX + m] + gi);
+        const double d = __ldg(qin.v[VMX + m] + gi) - p0;
+        const float hi = (float)d;
+        P0[2 * l + m] = p0;
+        qh[2 * l + m] = hi;
+        ql[2 * l + m] = (float)(d - (double)hi);
+      }
+    }
+    __syncwarp();
+    for (int e = 0; e < NeZ; ++e) {
+      for (int t = k; t < 4; t += N1) {  // bottom/top jump (neighbour - own) of MOMX/MOMY
+        const int s = t >> 1, m = t & 1;
+        const int lM = e * N1 + (s == 0 ? 0 : N);
+        const bool lid = s == 0 ? (e == 0) : (e == NeZ - 1);
+        const int lP = lid ? lM : (s == 0 ? lM - 1 : lM + 1);
+        j0[4 * e + t] = (float)(P0[2 * lP + m] - P0[2 * lM + m]);
+      }
+    }
+    __syncwarp();
+    for (int e = 0; e < NeZ; ++e) {
+      const int l = e * N1 + k;
+      D[2 * l] = 0.f;
+      D[2 * l + 1] = 0.f;
     }
     __syncwarp();
     const float cfs = (float)(0.5 * impl_fac * op.FSz);
@@ -530,26 +543,24 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const Prof pf, con
     for (int it = 0; it < 4; ++it) {
       float err = 0.f;
       for (int e = 0; e < NeZ; ++e) {
-        // bottom and top jumps (neighbour - own) of both components: lanes t < 4
         for (int t = k; t < 4; t += N1) {
           const int s = t >> 1, m = t & 1;
           const int lM = e * N1 + (s == 0 ? 0 : N);
           const bool lid = s == 0 ? (e == 0) : (e == NeZ - 1);
           const int lP = lid ? lM : (s == 0 ? lM - 1 : lM + 1);
-          jdel[t] = (float)(Pu[2 * lP + m] - Pu[2 * lM + m]);
+          jdel[t] = j0[4 * e + t] + (D[2 * lP + m] - D[2 * lM + m]);
         }
         __syncwarp();
         const int l = e * N1 + k;
-        const size_t gi = c.g(e);
         const float iscu = iscu_c / __ldg(pff.dens + l);
         const float aB = lbk * c.alB(e), aT = ltk * c.alT(e);
 #pragma unroll
         for (int m = 0; m < 2; ++m) {
           const float Af = cfs * (aB * jdel[m] + aT * jdel[2 + m]);  // impl_fac * A(P)
-          const double qmp = __ldg(qin.v[VMX + m] + gi) - Pu[2 * l + m];
-          const float b = Af + (float)qmp;
+          const float b = ((qh[2 * l + m] - D[2 * l + m]) + ql[2 * l + m]) + Af;
           bu[2 * l + m] = b;
           err = fmaxf(err, fabsf(b) * iscu);
+          if (!(fabsf(b) < 3.0e38f)) err = __int_as_float(0x7fc00000);
         }
         __syncwarp();
       }
@@ -592,22 +603,22 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const Prof pf, con
           const int l = e * N1 + k;
           const float beta = e > 0 ? cfs * lbk * c.alB(e) : 0.f;
           const float tau = e < NeZ - 1 ? cfs * ltk * c.alT(e) : 0.f;
-          Pu[2 * l] += (double)(bu[2 * l] - beta * Jx[e] + tau * Jx[e + 1]);
-          Pu[2 * l + 1] += (double)(bu[2 * l + 1] - beta * Jy[e] + tau * Jy[e + 1]);
+          D[2 * l] += bu[2 * l] - beta * Jx[e] + tau * Jx[e + 1];
+          D[2 * l + 1] += bu[2 * l + 1] - beta * Jy[e] + tau * Jy[e + 1];
         }
       }
       active = need;
       __syncwarp();
     }
+    const float iif = (float)args.inv_impl_fac;
     for (int e = 0; e < NeZ; ++e) {
       const int l = e * N1 + k;
       const size_t gi = c.g(e);
       const double dh64 = __ldg(pf.dens + l);
-      const double px = Pu[2 * l], py = Pu[2 * l + 1];
-      qsf[VMX][gi] = (float)fma(-dh64, args.Uref, px);
-      qsf[VMY][gi] = (float)fma(-dh64, args.Vref, py);
-      tout[VMX][gi] = (float)(px - __ldg(qin.v[VMX] + gi)) * (float)args.inv_impl_fac;
-      tout[VMY][gi] = (float)(py - __ldg(qin.v[VMY] + gi)) * (float)args.inv_impl_fac;
+      qsf[VMX][gi] = (float)fma(-dh64, args.Uref, __ldg(z.v[VMX] + gi)) + D[2 * l];
+      qsf[VMY][gi] = (float)fma(-dh64, args.Vref, __ldg(z.v[VMY] + gi)) + D[2 * l + 1];
+      tout[VMX][gi] = ((D[2 * l] - qh[2 * l]) - ql[2 * l]) * iif;
+      tout[VMY][gi] = ((D[2 * l + 1] - qh[2 * l + 1]) - ql[2 * l + 1]) * iif;
     }
     __syncwarp();
   }
