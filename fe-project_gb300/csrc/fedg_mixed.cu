@@ -20,13 +20,15 @@
 #include <vector>
 
 #include "fedg_ctx.cuh"
+#include "fedg_f2.cuh"
 #include "fedg_mlp.cuh"
 
 namespace fedg {
 
 struct MixCoef {
   double dt, a21e, a21i, a31e, a31i, a32e, a32i, b1, b2, b3;
-  double Uref, Vref;  // reference wind of the FP32 momentum deviations
+  double Uref, Vref;    // reference wind of the FP32 momentum deviations
+  float2 Uref2, Vref2;  // the same as float pairs
 };
 
 struct StageBufs {
@@ -34,7 +36,7 @@ struct StageBufs {
                         // DDENS, MOMX - DENS_hyd*Uref, MOMY - DENS_hyd*Vref, MOMZ, DRHOT
   float* qnf[5];        // stage 3: FP32 deviation copy of q^{n+1} (next step's stage-1 state)
   double* qn[5];        // q^n; stage 3 overwrites it with q^{n+1}
-  double* qi[5];        // next stage input q*_{s+1} (stages 1, 2)
+  float2* qi[5];        // next stage input q*_{s+1} as float pairs (stages 1, 2)
   float* S3[5];         // stage-3 input accumulator
   float* SF[5];         // final-update accumulator
   const float* TI[5];   // implicit tendency of the stage (stages 2, 3)
@@ -254,12 +256,15 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
     }
   }
 
-  // --- fused RK epilogue (FP64 accumulation of the prognostic variables) ---
+  // --- fused RK epilogue: the prognostic variables accumulate in float pairs (about 48 bits;
+  // the FP64 state is split with integer instructions), the FP32 stage increments added exactly ---
+  const float dtf = (float)cf.dt;
   if (STAGE == 1) {
     if (valid) {
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
-        B.qi[v][g] = __ldg(B.qn[v] + g) + cf.dt * (double)(float(cf.a21e) * tex[v] + float(cf.a21i) * tim[v]);
+        const f2 qn = f2_split(__ldg(B.qn[v] + g));
+        B.qi[v][g] = f2_pack(f2_add_f(qn, dtf * (float(cf.a21e) * tex[v] + float(cf.a21i) * tim[v])));
         B.S3[v][g] = float(cf.a31e) * tex[v] + float(cf.a31i) * tim[v];
         B.SF[v][g] = float(cf.b1) * (tex[v] + tim[v]);
       }
@@ -270,34 +275,36 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
     if (valid) {
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
-        const double qn = __ldg(B.qn[v] + g);
+        const f2 qn = f2_split(__ldg(B.qn[v] + g));
         const float s3 = __ldg(B.S3[v] + g) + float(cf.a32e) * tex[v] + float(cf.a32i) * tim[v];
-        B.qi[v][g] = qn + cf.dt * (double)s3;
+        B.qi[v][g] = f2_pack(f2_add_f(qn, dtf * s3));
         B.SF[v][g] = __ldg(B.SF[v] + g) + float(cf.b2) * (tex[v] + tim[v]);
       }
     }
     return;
   }
-  // STAGE 3: q^{n+1} = q^n + dt (SF + b3 (t_ex + t_im)) in FP64, then the modal filter applied to
-  // the deviation from the reference state (DENS_hyd*(Uref,Vref) for MOMX/MOMY, 0 otherwise; the
-  // filter leaves that smooth reference unchanged), q^{n+1} = ref + F(deviation).
-  double qnew[5];
+  // STAGE 3: q^{n+1} = q^n + dt (SF + b3 (t_ex + t_im)) in float pairs, then the modal filter
+  // applied to the deviation from the reference state (DENS_hyd*(Uref,Vref) for MOMX/MOMY, 0
+  // otherwise; the filter leaves that smooth reference unchanged), q^{n+1} = ref + F(deviation).
+  f2 qnew[5];
   float dev[5];
+  const f2 dh2 = f2_split(dh64);
 #pragma unroll
   for (int v = 0; v < 5; ++v) {
-    qnew[v] = 0.0;
+    qnew[v] = f2{0.f, 0.f};
     dev[v] = 0.f;
     if (valid) {
-      qnew[v] = __ldg(B.qn[v] + g) + cf.dt * (double)(__ldg(B.SF[v] + g) + float(cf.b3) * (tex[v] + tim[v]));
-      const double ref = v == VMX ? dh64 * cf.Uref : (v == VMY ? dh64 * cf.Vref : 0.0);
-      dev[v] = (float)(qnew[v] - ref);
+      qnew[v] = f2_add_f(f2_split(__ldg(B.qn[v] + g)),
+                         dtf * (__ldg(B.SF[v] + g) + float(cf.b3) * (tex[v] + tim[v])));
+      const f2 ref = v == VMX ? f2_mul(dh2, f2_of(cf.Uref2)) : (v == VMY ? f2_mul(dh2, f2_of(cf.Vref2)) : f2{0.f, 0.f});
+      dev[v] = f2_to_f(f2_sub(qnew[v], ref));
     }
   }
   if (!filter_on) {
     if (valid) {
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
-        B.qn[v][g] = qnew[v];
+        B.qn[v][g] = (double)qnew[v].h + (double)qnew[v].l;
         B.qnf[v][g] = dev[v];
       }
     }
@@ -401,17 +408,17 @@ static int launch_stage_m(int stage, const OpsF& op, const ProfF& pf, const doub
 // =====================================================================================
 struct MixedState {
   size_t n = 0;
-  double* dbuf = nullptr;   // qi (5n): next stage input, FP64
+  float2* qpair = nullptr;  // qi (5n): next stage input as float pairs
   float* fbuf = nullptr;    // S3 | SF | TI (5n each) | guess (3n) | QSF (5n) | QNF (5n)
-  float* prof = nullptr;    // [4][L]
-  double* rhinv = nullptr;  // [L]
+  float* prof = nullptr;    // [4][L] FP32 DENS_hyd, PRES_hyd, THERM_hyd, 1/THERM_hyd
+  float2* prof2 = nullptr;  // [4][L] float pairs DENS_hyd, PRES_hyd, RHOT_hyd, 1/RHOT_hyd
   float** d_ptrs = nullptr; // device arrays of float pointers: TI[5], guess[3], QSF[5]
   float* gsc = nullptr;     // block-Thomas history of the column solve
   OpsF opf;
-  PresSeries ps;
+  OpsX opx;
   double Uref = 0.0, Vref = 0.0;
   bool wind_set = false;
-  double* qi(int v) { return dbuf + (size_t)v * n; }
+  float2* qi(int v) { return qpair + (size_t)v * n; }
   float* S3(int v) { return fbuf + (size_t)v * n; }
   float* SF(int v) { return fbuf + (size_t)(5 + v) * n; }
   float* TI(int v) { return fbuf + (size_t)(10 + v) * n; }
@@ -420,12 +427,17 @@ struct MixedState {
   float* QNF(int v) { return fbuf + (size_t)(23 + v) * n; }
 };
 
+static float2 split_host(double x) {
+  const float h = (float)x;
+  return make_float2(h, (float)(x - (double)h));
+}
+
 void mixed_free(MixedState* m) {
   if (!m) return;
-  cudaFree(m->dbuf);
+  cudaFree(m->qpair);
   cudaFree(m->fbuf);
   cudaFree(m->prof);
-  cudaFree(m->rhinv);
+  cudaFree(m->prof2);
   cudaFree(m->d_ptrs);
   cudaFree(m->gsc);
   delete m;
@@ -438,10 +450,10 @@ static int mixed_setup(fedg_ctx* c) {
   m->n = c->n;
   const int L = c->L;
   cudaError_t e;
-  if ((e = cudaMalloc(&m->dbuf, sizeof(double) * 5 * c->n)) != cudaSuccess ||
+  if ((e = cudaMalloc(&m->qpair, sizeof(float2) * 5 * c->n)) != cudaSuccess ||
       (e = cudaMalloc(&m->fbuf, sizeof(float) * 28 * c->n)) != cudaSuccess ||
       (e = cudaMalloc(&m->prof, sizeof(float) * 4 * L)) != cudaSuccess ||
-      (e = cudaMalloc(&m->rhinv, sizeof(double) * L)) != cudaSuccess ||
+      (e = cudaMalloc(&m->prof2, sizeof(float2) * 4 * L)) != cudaSuccess ||
       (e = cudaMalloc(&m->d_ptrs, sizeof(float*) * 13)) != cudaSuccess ||
       (e = cudaMalloc(&m->gsc, sizeof(float) * vi_cols_scratch_floats(c->n))) != cudaSuccess) {
     mixed_free(m);
@@ -459,33 +471,45 @@ static int mixed_setup(fedg_ctx* c) {
   f.FSx = (float)o.FSx; f.FSy = (float)o.FSy; f.FSz = (float)o.FSz;
   f.grav = (float)o.grav; f.kap = (float)o.kap; f.coriolis_f = (float)o.coriolis_f;
   f.NeX = o.NeX; f.NeY = o.NeY; f.NeZ = o.NeZ; f.N1 = o.N1; f.Np = o.Np; f.L = o.L;
-  // binomial series of (1+r)^kappa - 1: c_n = C(kappa, n); 12 terms are exact to roundoff for |r| <= 0.03
-  m->ps.nterm = 12;
-  m->ps.rmax = 0.03;
+  // float-pair operators of the column solve; binomial series of (1+r)^kappa - 1 with
+  // c_n = C(kappa, n): 12 terms are exact to roundoff for |r| <= 0.03
+  OpsX& x = m->opx;
+  std::memset(&x, 0, sizeof(x));
+  for (int k = 0; k < FEDG_MAXN1 * FEDG_MAXN1; ++k) { x.D[k] = split_host(o.D[k]); x.T[k] = split_host(o.T[k]); }
+  for (int k = 0; k < FEDG_MAXN1; ++k) { x.Lb[k] = split_host(o.Lb[k]); x.Lt[k] = split_host(o.Lt[k]); }
+  x.E33 = split_host(o.E33);
+  x.tmp1 = split_host(0.5 * o.FSz);
+  x.grav = split_host(o.grav);
+  x.kap = split_host(o.kap);
+  x.kap64 = o.kap;
+  x.rmax = 0.03f;
   double cn = 1.0;
   for (int n = 1; n <= 12; ++n) {
     cn *= (o.kap - (n - 1)) / n;
-    m->ps.c[n - 1] = cn;
+    x.cb[n - 1] = (float)cn;
   }
   // FP32 base-state profiles and 1/RHOT_hyd
   std::vector<double> hp(4 * L);
   e = cudaMemcpy(hp.data(), c->d_prof, sizeof(double) * 4 * L, cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) { mixed_free(m); return api_cuda_fail(e, "fedg_update(mixed): profile copy"); }
   std::vector<float> pfh(4 * L);
-  std::vector<double> rinv(L);
+  std::vector<float2> pf2(4 * L);
   for (int l = 0; l < L; ++l) {
     pfh[l] = (float)hp[l];
     pfh[L + l] = (float)hp[L + l];
     pfh[2 * L + l] = (float)hp[2 * L + l];
     pfh[3 * L + l] = (float)(1.0 / hp[2 * L + l]);
-    rinv[l] = 1.0 / hp[3 * L + l];
+    pf2[l] = split_host(hp[l]);
+    pf2[L + l] = split_host(hp[L + l]);
+    pf2[2 * L + l] = split_host(hp[3 * L + l]);
+    pf2[3 * L + l] = split_host(1.0 / hp[3 * L + l]);
   }
   float* hptr[13];
   for (int v = 0; v < 5; ++v) hptr[v] = m->TI(v);
   for (int v = 0; v < 3; ++v) hptr[5 + v] = m->GU(v);
   for (int v = 0; v < 5; ++v) hptr[8 + v] = m->QSF(v);
   if ((e = cudaMemcpy(m->prof, pfh.data(), sizeof(float) * 4 * L, cudaMemcpyHostToDevice)) != cudaSuccess ||
-      (e = cudaMemcpy(m->rhinv, rinv.data(), sizeof(double) * L, cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaMemcpy(m->prof2, pf2.data(), sizeof(float2) * 4 * L, cudaMemcpyHostToDevice)) != cudaSuccess ||
       (e = cudaMemcpy(m->d_ptrs, hptr, sizeof(float*) * 13, cudaMemcpyHostToDevice)) != cudaSuccess) {
     mixed_free(m);
     return api_cuda_fail(e, "fedg_update(mixed): upload");
@@ -502,9 +526,8 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
   MixedState* m = c->mixed;
   if (o->use_guess && !mlp_ready(c->guess)) return api_fail("fedg_update: use_guess set but no trained column-guess network is loaded (fedg_guess_load)");
   const double alp = (3.0 + 2.0 * std::sqrt(2.0)) / 6.0, gam = 1.0 - 1.0 / std::sqrt(2.0), del = 1.0 / (2.0 * std::sqrt(2.0));
-  MixCoef cf{o->dt, 2.0 * gam, gam, 1.0 - alp, del, alp, del, del, del, gam, 0.0, 0.0};
+  MixCoef cf{o->dt, 2.0 * gam, gam, 1.0 - alp, del, alp, del, del, del, gam, 0.0, 0.0, {0.f, 0.f}, {0.f, 0.f}};
   const ProfF pff{m->prof, m->prof + c->L, m->prof + 2 * c->L, m->prof + 3 * c->L};
-  const Prof pf = c->prof();
   StageBufs B;
   std::memset(&B, 0, sizeof(B));
   for (int v = 0; v < 5; ++v) {
@@ -531,12 +554,16 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
     m->Vref = hs[2] != 0.0 ? hs[1] / hs[2] : 0.0;
     m->opf.Uref = (float)m->Uref;
     m->opf.Vref = (float)m->Vref;
+    m->opx.Uref = split_host(m->Uref);
+    m->opx.Vref = split_host(m->Vref);
     m->wind_set = true;
   }
   cf.Uref = m->Uref;
   cf.Vref = m->Vref;
+  cf.Uref2 = m->opx.Uref;
+  cf.Vref2 = m->opx.Vref;
   const double impl_fac = gam * o->dt;
-  MixViArgs va{impl_fac, 1.0 / impl_fac, o->tol, 340.0, m->Uref, m->Vref, o->max_iter, 1};
+  MixViArgs va{impl_fac, 1.0 / impl_fac, o->tol, 340.0, split_host(impl_fac), o->max_iter, 1};
   {  // FP32 deviation copy of the incoming state for the first stage-1 tendency
     F5c qc{{q[0], q[1], q[2], q[3], q[4]}};
     Dev5 dv{{m->QNF(0), m->QNF(1), m->QNF(2), m->QNF(3), m->QNF(4)}};
@@ -560,7 +587,9 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
     });
   };
   auto vi = [&]() -> int {
-    F5c qin{{m->qi(0), m->qi(1), m->qi(2), m->qi(3), m->qi(4)}};
+    X5 qin{{m->qi(0), m->qi(1), m->qi(2), m->qi(3), m->qi(4)}};
+    const ProfX px{m->prof2, m->prof2 + c->L, m->prof2 + 2 * c->L, m->prof2 + 3 * c->L,
+                   m->prof, m->prof + c->L, m->prof + 2 * c->L, m->prof + 3 * c->L};
     F5c z{{q[0], q[1], q[2], q[3], q[4]}};
     float* const* qo = m->d_ptrs + 8;
     const float* const* gptr = nullptr;
@@ -572,8 +601,8 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
       gptr = (const float* const*)(m->d_ptrs + 5);
     }
     return tracked(c, FEDG_K_MVI, [&] {
-      return launch_vi_cols(c->N1, c->op, pf, pff, m->rhinv, m->ps, qin, z, gptr, qo, m->d_ptrs, m->gsc, c->d_status,
-                            c->d_cnt, va, c->stream);
+      return launch_vi_cols(c->N1, c->op, m->opx, px, qin, z, gptr, qo, m->d_ptrs, m->gsc, c->d_status, c->d_cnt, va,
+                            c->stream);
     });
   };
   for (int step = 0; step < nsteps; ++step) {
@@ -588,6 +617,8 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
   if (cudaMemcpyAsync(c->h_cnt, c->d_cnt, sizeof(unsigned long long) * 3, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
       cudaStreamSynchronize(c->stream) != cudaSuccess)
     return api_fail("fedg_update(mixed): status readback");
+  if (o->use_guess && mlp_take_error(c->guess, c->stream))
+    return api_fail("fedg_update(mixed): a column-guess tensor-core GEMM timed out waiting on its barrier");
   if (iters_out) *iters_out = c->h_cnt[2] ? double(c->h_cnt[1]) / double(c->h_cnt[2]) : 0.0;
   return (int)c->h_cnt[0];
 }

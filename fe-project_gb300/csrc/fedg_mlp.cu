@@ -1,5 +1,6 @@
-// fedg_mlp.cu -- column-guess network kernels: BF16 tensor-core inference GEMMs, FP32 training
-// forward/backward, Adam, and the column gather/scatter between (Np, Ne) fields and feature rows.
+// fedg_mlp.cu -- column-guess network kernels: BF16 inference GEMMs on the 5th-generation tensor
+// cores (tcgen05, TMEM accumulators) with the column gather/scatter between (Np, Ne) fields and
+// feature rows fused into the first and last layer, FP32 training forward/backward, Adam.
 //
 // Network: x (3L+1) -> 256 -> 256 -> 3L, GELU (erf form) after the two hidden layers.
 // Features (var-major): DDENS'(l), MOMZ(l), DRHOT'(l) for the L levels of the column, then
@@ -14,7 +15,9 @@ using bf16 = __nv_bfloat16;
 
 namespace {
 
-constexpr int BM = 128, BN = 64, BK = 32;
+// padding of the inference buffers: rows to the 128-row GEMM tile, inputs to the 32-wide K chunk,
+// outputs to a multiple of 64 columns
+constexpr int PAD_ROWS = 128, PAD_OUT = 64, PAD_K = 32;
 
 __host__ __device__ inline int rup(int x, int a) { return (x + a - 1) / a * a; }
 
@@ -23,91 +26,211 @@ __device__ __forceinline__ float gelu_d(float x) {
   return 0.5f * (1.f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
 }
 
-__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+struct ColMap {
+  int N1, Np, NeX, NeY, L;
+};
+__device__ __forceinline__ size_t col_gidx(const ColMap& cm, int c, int l) {
+  const int NF = cm.N1 * cm.N1;
+  const int ij = c % NF, exy = c / NF, ci = ij % cm.N1, cj = ij / cm.N1;
+  const int ez = l / cm.N1, k = l - ez * cm.N1;
+  return ((size_t)ez * cm.NeX * cm.NeY + exy) * cm.Np + ci + cm.N1 * cj + NF * k;
+}
+// column gather/scatter of the first and last inference layers: features (var-major) DDENS'(l),
+// MOMZ(l), DRHOT'(l) of the column's L levels, then impl_fac, each times its scale; outputs
+// (Q - q*)(l) per variable divided by its scale, written into (Np, Ne) fields
+struct ColIO {
+  ColMap cm;
+  const float2 *qd, *qm, *qr;  // stage input q* as float pairs
+  float s0, s1, s2, fac;       // input scales, scaled impl_fac
+  float *gd, *gm, *gr;         // guess fields
+  float r0, r1, r2;            // 1 / output scales
+};
+
+// ---------------------------------------------------------------------------------------------
+// Inference GEMM on the 5th-generation tensor cores:
+//   C[M x Np] = act(A[M x Kp] . W[Np x Kp]^T + bias), bf16 operands (both K-major), FP32 accumulate.
+// One CTA of 4 warps per 128 x BN output tile.  Each K chunk of 32 is staged in shared memory in
+// the no-swizzle K-major canonical layout, in 8-row x 16-byte core matrices.  K-adjacent core
+// matrices are 128 B apart (leading byte offset), 8-row groups 512 B apart (stride byte
+// offset).
+// One elected thread issues tcgen05.mma (M = 128, N = BN, K = 16) into a TMEM accumulator of
+// 128 lanes x BN columns and commits to an mbarrier.  Every wait on that barrier is bounded:
+// after the limit the kernel raises *err, skips the stores, waits once more (bounded) for
+// the MMAs in flight and releases its TMEM.  The epilogue reads the accumulator with
+// tcgen05.ld (warp w owns lanes 32w..32w+31, one output row per thread), adds the bias,
+// applies GELU and stores the row.
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
+         (1ull << 46);  // descriptor version 1, base offset 0, no swizzle
 }
 
-// C[M x Np] = act(A[M x Kp] . W[Np x Kp]^T + bias), A/W bf16 row-major, Kp % 32 == 0, Np % 64 == 0.
-// Block tile 128 x 64 x 32, four warps of 64 x 32, m16n8k16 BF16 tensor-core MMAs, FP32 accumulate.
-template <bool GELU, bool OUTBF16>
-__global__ void __launch_bounds__(128) k_gemm_bf16(const bf16* __restrict__ A, const bf16* __restrict__ W,
-                                                   const float* __restrict__ bias, void* __restrict__ out, int M,
-                                                   int Np, int Kp) {
-  __shared__ __align__(16) bf16 As[BM][BK + 8];
-  __shared__ __align__(16) bf16 Ws[BN][BK + 8];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int wm = warp >> 1, wn = warp & 1;
-  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
-  float acc[4][4][4];
-#pragma unroll
-  for (int a = 0; a < 4; ++a)
-#pragma unroll
-    for (int b = 0; b < 4; ++b)
-#pragma unroll
-      for (int c = 0; c < 4; ++c) acc[a][b][c] = 0.f;
-  for (int k0 = 0; k0 < Kp; k0 += BK) {
-    for (int i = threadIdx.x; i < BM * BK / 8; i += 128) {
-      const int r = i / (BK / 8), cv = i % (BK / 8);
-      const int gr = m0 + r;
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (gr < M) v = *reinterpret_cast<const uint4*>(A + (size_t)gr * Kp + k0 + cv * 8);
-      *reinterpret_cast<uint4*>(&As[r][cv * 8]) = v;
-    }
-    for (int i = threadIdx.x; i < BN * BK / 8; i += 128) {
-      const int r = i / (BK / 8), cv = i % (BK / 8);
-      *reinterpret_cast<uint4*>(&Ws[r][cv * 8]) =
-          *reinterpret_cast<const uint4*>(W + (size_t)(n0 + r) * Kp + k0 + cv * 8);
-    }
-    __syncthreads();
-#pragma unroll
-    for (int kk = 0; kk < BK; kk += 16) {
-      uint32_t af[4][4], bfr[4][2];
-      const int ar = lane >> 2, ac = kk + (lane & 3) * 2;
-#pragma unroll
-      for (int mt = 0; mt < 4; ++mt) {
-        const int row = wm * 64 + mt * 16 + ar;
-        af[mt][0] = *reinterpret_cast<const uint32_t*>(&As[row][ac]);
-        af[mt][1] = *reinterpret_cast<const uint32_t*>(&As[row + 8][ac]);
-        af[mt][2] = *reinterpret_cast<const uint32_t*>(&As[row][ac + 8]);
-        af[mt][3] = *reinterpret_cast<const uint32_t*>(&As[row + 8][ac + 8]);
-      }
-#pragma unroll
-      for (int nt = 0; nt < 4; ++nt) {
-        const int n = wn * 32 + nt * 8 + ar;
-        bfr[nt][0] = *reinterpret_cast<const uint32_t*>(&Ws[n][ac]);
-        bfr[nt][1] = *reinterpret_cast<const uint32_t*>(&Ws[n][ac + 8]);
-      }
-#pragma unroll
-      for (int mt = 0; mt < 4; ++mt)
-#pragma unroll
-        for (int nt = 0; nt < 4; ++nt) mma_bf16(acc[mt][nt], af[mt], bfr[nt]);
-    }
-    __syncthreads();
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t parity) {
+  for (int it = 0; it < (1 << 20); ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    if (done) return true;
   }
+  return false;
+}
+
+template <int BN, bool GATHER, int OMODE, bool GELU>
+__global__ void __launch_bounds__(128) k_gemm_tc(const bf16* __restrict__ A, const bf16* __restrict__ W,
+                                                 const float* __restrict__ bias, void* __restrict__ out, int M, int Np,
+                                                 int Kp, const ColIO io, int* err) {
+  constexpr int TM = 128, TK = 32;
+  constexpr uint32_t TCOLS = BN <= 32 ? 32 : (BN <= 64 ? 64 : (BN <= 128 ? 128 : 256));
+  static_assert(BN % 16 == 0 && BN <= 256, "tcgen05 M=128 needs N % 16 == 0, N <= 256");
+  __shared__ __align__(1024) bf16 sA[TM * TK];
+  __shared__ __align__(1024) bf16 sB[BN * TK];
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tmem_slot;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.x * TM, n0 = blockIdx.y * BN;
+  const uint32_t mb = smem_u32(&mbar);
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_slot)),
+                 "r"(TCOLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mb) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+  // instruction descriptor: D f32, A/B bf16, both K-major, N/8, M/16
+  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
+  uint32_t parity = 0;
+  bool ok = true;
+  for (int k0 = 0; k0 < Kp && ok; k0 += TK) {
+    for (int i = tid; i < TM * (TK / 8); i += 128) {  // A rows: 16-byte chunks to core-matrix slots
+      const int r = i >> 2, kc = i & 3;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (m0 + r < M) {
+        if constexpr (GATHER) {  // features of column m0 + r straight from the q* fields
+          const int L = io.cm.L;
+          __align__(16) bf16 x8[8];
 #pragma unroll
-  for (int mt = 0; mt < 4; ++mt)
+          for (int j = 0; j < 8; ++j) {
+            const int f = k0 + kc * 8 + j;
+            float x = 0.f;
+            if (f < 3 * L) {
+              const int vv = f / L, l = f - vv * L;
+              const size_t g = col_gidx(io.cm, m0 + r, l);
+              x = vv == 0 ? __ldg(io.qd + g).x * io.s0 : (vv == 1 ? __ldg(io.qm + g).x * io.s1 : __ldg(io.qr + g).x * io.s2);
+            } else if (f == 3 * L) {
+              x = io.fac;
+            }
+            x8[j] = __float2bfloat16_rn(x);
+          }
+          v = *reinterpret_cast<const uint4*>(x8);
+        } else {
+          v = *reinterpret_cast<const uint4*>(A + (size_t)(m0 + r) * Kp + k0 + kc * 8);
+        }
+      }
+      *reinterpret_cast<uint4*>(sA + ((r >> 3) * 4 + kc) * 64 + (r & 7) * 8) = v;
+    }
+    for (int i = tid; i < BN * (TK / 8); i += 128) {
+      const int r = i >> 2, kc = i & 3;
+      const uint4 v = *reinterpret_cast<const uint4*>(W + (size_t)(n0 + r) * Kp + k0 + kc * 8);
+      *reinterpret_cast<uint4*>(sB + ((r >> 3) * 4 + kc) * 64 + (r & 7) * 8) = v;
+    }
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // generic stores -> tensor-core reads
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
 #pragma unroll
-    for (int nt = 0; nt < 4; ++nt) {
-      const int col = n0 + wn * 32 + nt * 8 + (lane & 3) * 2;
-      const float b0 = bias[col], b1 = bias[col + 1];
+      for (int ks = 0; ks < TK / 16; ++ks) {
+        const uint64_t ad = umma_desc(smem_u32(sA) + ks * 256, 128, 512);
+        const uint64_t bd = umma_desc(smem_u32(sB) + ks * 256, 128, 512);
+        const uint32_t acc = (k0 > 0 || ks > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+            : "memory");
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mb)
+                   : "memory");
+    }
+    // the MMAs must have read sA/sB before the next chunk overwrites them
+    const bool got = mbar_wait_bounded(mb, parity);
+    parity ^= 1u;
+    ok = __syncthreads_and(got) != 0;
+  }
+  if (!ok) {  // give MMAs still in flight a second bounded wait before the accumulator is released
+    mbar_wait_bounded(mb, parity ^ 1u);
+    if (tid == 0) atomicExch(err, 1);
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const int row = m0 + 32 * warp + lane;
+  const uint32_t tl = tmem + ((uint32_t)(32 * warp) << 16);
+#pragma unroll 1
+  for (int c0 = 0; c0 < BN; c0 += 16) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(tl + (uint32_t)c0)
+        : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+    if (ok && row < M) {
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int row = m0 + wm * 64 + mt * 16 + (lane >> 2) + h * 8;
-        if (row >= M) continue;
-        float v0 = acc[mt][nt][2 * h] + b0, v1 = acc[mt][nt][2 * h + 1] + b1;
+      for (int j = 0; j < 16; j += 2) {
+        const int col = n0 + c0 + j;
+        float v0 = __uint_as_float(r[j]) + bias[col], v1 = __uint_as_float(r[j + 1]) + bias[col + 1];
         if (GELU) { v0 = gelu_f(v0); v1 = gelu_f(v1); }
-        if (OUTBF16) {
+        if constexpr (OMODE == 0) {
           *reinterpret_cast<__nv_bfloat162*>(reinterpret_cast<bf16*>(out) + (size_t)row * Np + col) =
               __floats2bfloat162_rn(v0, v1);
-        } else {
+        } else if constexpr (OMODE == 1) {
           *reinterpret_cast<float2*>(reinterpret_cast<float*>(out) + (size_t)row * Np + col) = make_float2(v0, v1);
+        } else {  // scatter: output feature -> (variable, level) of column `row`
+          const int L = io.cm.L;
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int f = col + h;
+            if (f < 3 * L) {
+              const int vv = f / L, l = f - vv * L;
+              const size_t g = col_gidx(io.cm, row, l);
+              const float y = h ? v1 : v0;
+              if (vv == 0) io.gd[g] = y * io.r0;
+              else if (vv == 1) io.gm[g] = y * io.r1;
+              else io.gr[g] = y * io.r2;
+            }
+          }
         }
       }
     }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TCOLS) : "memory");
+}
+
+template <bool GATHER, int OMODE, bool GELU>
+static void launch_gemm_tc(const bf16* A, const bf16* W, const float* bias, void* out, int M, int Np, int Kp,
+                           const ColIO& io, int* err, cudaStream_t s) {
+  const unsigned gm = (unsigned)((M + 127) / 128);
+  if (Np % 256 == 0)
+    k_gemm_tc<256, GATHER, OMODE, GELU><<<dim3(gm, Np / 256), 128, 0, s>>>(A, W, bias, out, M, Np, Kp, io, err);
+  else if (Np % 192 == 0)
+    k_gemm_tc<192, GATHER, OMODE, GELU><<<dim3(gm, Np / 192), 128, 0, s>>>(A, W, bias, out, M, Np, Kp, io, err);
+  else if (Np % 128 == 0)
+    k_gemm_tc<128, GATHER, OMODE, GELU><<<dim3(gm, Np / 128), 128, 0, s>>>(A, W, bias, out, M, Np, Kp, io, err);
+  else
+    k_gemm_tc<64, GATHER, OMODE, GELU><<<dim3(gm, Np / 64), 128, 0, s>>>(A, W, bias, out, M, Np, Kp, io, err);
 }
 
 // Generic FP32 SIMT GEMM for training: C(m,n) (+)= sum_k A(m,k) B(k,n) (+ bias[n]),
@@ -217,45 +340,6 @@ __global__ void k_copy_rows(const float* __restrict__ Yp, int doutp, float* __re
   Y[i] = Yp[(size_t)r * doutp + c];
 }
 
-// column c = (ex, ey, i, j): level l of variable v lives at ((ez*nxy + exy)*Np + i + N1 j + N1^2 k)
-struct ColMap {
-  int N1, Np, NeX, NeY, L;
-};
-__device__ __forceinline__ size_t col_gidx(const ColMap& cm, int c, int l) {
-  const int NF = cm.N1 * cm.N1;
-  const int ij = c % NF, exy = c / NF, ci = ij % cm.N1, cj = ij / cm.N1;
-  const int ez = l / cm.N1, k = l - ez * cm.N1;
-  return ((size_t)ez * cm.NeX * cm.NeY + exy) * cm.Np + ci + cm.N1 * cj + NF * k;
-}
-__global__ void k_gather_x(ColMap cm, const double* __restrict__ qd, const double* __restrict__ qm,
-                           const double* __restrict__ qr, float fac, float s0, float s1, float s2, bf16* __restrict__ X,
-                           int dinp, int ncol) {
-  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (size_t)ncol * dinp) return;
-  const int c = (int)(i / dinp), f = (int)(i % dinp);
-  float x = 0.f;
-  if (f < 3 * cm.L) {
-    const int v = f / cm.L, l = f - v * cm.L;
-    const size_t g = col_gidx(cm, c, l);
-    x = v == 0 ? (float)qd[g] * s0 : (v == 1 ? (float)qm[g] * s1 : (float)qr[g] * s2);
-  } else if (f == 3 * cm.L) {
-    x = fac;
-  }
-  X[i] = __float2bfloat16_rn(x);
-}
-__global__ void k_scatter_y(ColMap cm, const float* __restrict__ Y, int doutp, float r0, float r1, float r2,
-                            float* __restrict__ gd, float* __restrict__ gm, float* __restrict__ gr, int ncol) {
-  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (size_t)ncol * 3 * cm.L) return;
-  const int c = (int)(i / (3 * cm.L)), f = (int)(i % (3 * cm.L));
-  const int v = f / cm.L, l = f - v * cm.L;
-  const float y = Y[(size_t)c * doutp + f];
-  const size_t g = col_gidx(cm, c, l);
-  if (v == 0) gd[g] = y * r0;
-  else if (v == 1) gm[g] = y * r1;
-  else gr[g] = y * r2;
-}
-
 inline unsigned nblk(size_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 }  // namespace
@@ -280,6 +364,7 @@ struct MlpState {
   size_t icap = 0;
   bf16 *Xh = nullptr, *H1 = nullptr, *H2 = nullptr;
   float* Yf = nullptr;
+  int* err = nullptr;  // raised by a tensor-core GEMM whose barrier wait ran out
   int ready = 0;
 };
 
@@ -288,7 +373,7 @@ void mlp_free(MlpState* m) {
   cudaFree(m->P); cudaFree(m->G); cudaFree(m->Mo); cudaFree(m->Vo); cudaFree(m->Wh);
   cudaFree(m->Z1); cudaFree(m->A1); cudaFree(m->Z2); cudaFree(m->A2); cudaFree(m->Y); cudaFree(m->dY);
   cudaFree(m->dA); cudaFree(m->loss);
-  cudaFree(m->Xh); cudaFree(m->H1); cudaFree(m->H2); cudaFree(m->Yf);
+  cudaFree(m->Xh); cudaFree(m->H1); cudaFree(m->H2); cudaFree(m->Yf); cudaFree(m->err);
   delete m;
 }
 
@@ -306,9 +391,9 @@ int mlp_create(int levels, int hidden, MlpState** out) {
   m->din = 3 * levels + 1;
   m->h = hidden;
   m->dout = 3 * levels;
-  m->dinp = rup(m->din, BK);
+  m->dinp = rup(m->din, PAD_K);
   m->hp = hidden;
-  m->doutp = rup(m->dout, BN);
+  m->doutp = rup(m->dout, PAD_OUT);
   m->oW1 = 0;
   m->ob1 = m->oW1 + (size_t)m->hp * m->dinp;
   m->oW2 = m->ob1 + m->hp;
@@ -326,10 +411,12 @@ int mlp_create(int levels, int hidden, MlpState** out) {
       (e = cudaMalloc(&m->Mo, sizeof(float) * m->np)) != cudaSuccess ||
       (e = cudaMalloc(&m->Vo, sizeof(float) * m->np)) != cudaSuccess ||
       (e = cudaMalloc(&m->Wh, sizeof(bf16) * m->nh)) != cudaSuccess ||
-      (e = cudaMalloc(&m->loss, sizeof(float))) != cudaSuccess) {
+      (e = cudaMalloc(&m->loss, sizeof(float))) != cudaSuccess ||
+      (e = cudaMalloc(&m->err, sizeof(int))) != cudaSuccess) {
     mlp_free(m);
     return (int)e;
   }
+  cudaMemset(m->err, 0, sizeof(int));
   cudaMemset(m->P, 0, sizeof(float) * m->np);
   cudaMemset(m->G, 0, sizeof(float) * m->np);
   cudaMemset(m->Mo, 0, sizeof(float) * m->np);
@@ -488,7 +575,7 @@ static int ensure_infer(MlpState* m, size_t n) {
   if (n <= m->icap) return 0;
   cudaFree(m->Xh); cudaFree(m->H1); cudaFree(m->H2); cudaFree(m->Yf);
   m->icap = 0;
-  const size_t nr = (size_t)rup((int)std::min<size_t>(n, 1u << 30), BM);
+  const size_t nr = (size_t)rup((int)std::min<size_t>(n, 1u << 30), PAD_ROWS);
   cudaError_t e;
   if ((e = cudaMalloc(&m->Xh, sizeof(bf16) * nr * m->dinp)) != cudaSuccess ||
       (e = cudaMalloc(&m->H1, sizeof(bf16) * nr * m->hp)) != cudaSuccess ||
@@ -499,37 +586,51 @@ static int ensure_infer(MlpState* m, size_t n) {
   return 0;
 }
 
-static int run_layers(MlpState* m, int n, cudaStream_t s) {
-  const dim3 g1((n + BM - 1) / BM, m->hp / BN), g3((n + BM - 1) / BM, m->doutp / BN);
-  k_gemm_bf16<true, true><<<g1, 128, 0, s>>>(m->Xh, m->Wh + m->hW1, m->P + m->ob1, m->H1, n, m->hp, m->dinp);
-  k_gemm_bf16<true, true><<<g1, 128, 0, s>>>(m->H1, m->Wh + m->hW2, m->P + m->ob2, m->H2, n, m->hp, m->hp);
-  k_gemm_bf16<false, false><<<g3, 128, 0, s>>>(m->H2, m->Wh + m->hW3, m->P + m->ob3, m->Yf, n, m->doutp, m->hp);
+// the three layers on the tensor cores; with io.cm.L > 0 the first layer gathers its input rows
+// from the q* fields and the last scatters its outputs to the guess fields
+static int run_layers(MlpState* m, int n, const ColIO* io, cudaStream_t s) {
+  const ColIO none{};
+  if (io) launch_gemm_tc<true, 0, true>(nullptr, m->Wh + m->hW1, m->P + m->ob1, m->H1, n, m->hp, m->dinp, *io, m->err, s);
+  else launch_gemm_tc<false, 0, true>(m->Xh, m->Wh + m->hW1, m->P + m->ob1, m->H1, n, m->hp, m->dinp, none, m->err, s);
+  launch_gemm_tc<false, 0, true>(m->H1, m->Wh + m->hW2, m->P + m->ob2, m->H2, n, m->hp, m->hp, none, m->err, s);
+  if (io) launch_gemm_tc<false, 2, false>(m->H2, m->Wh + m->hW3, m->P + m->ob3, nullptr, n, m->doutp, m->hp, *io, m->err, s);
+  else launch_gemm_tc<false, 1, false>(m->H2, m->Wh + m->hW3, m->P + m->ob3, m->Yf, n, m->doutp, m->hp, none, m->err, s);
   return (int)cudaGetLastError();
+}
+
+int mlp_take_error(MlpState* m, cudaStream_t s) {
+  int h = 0;
+  cudaError_t e = cudaMemcpyAsync(&h, m->err, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return (int)e;
+  if (h) cudaMemsetAsync(m->err, 0, sizeof(int), s);
+  return h ? -1 : 0;
 }
 
 int mlp_predict(MlpState* m, const float* X, float* Y, int n, cudaStream_t s) {
   int r = ensure_infer(m, (size_t)n);
   if (r) return r;
   k_f32_to_bf16_rows<<<nblk((size_t)n * m->dinp, 256), 256, 0, s>>>(X, m->din, m->Xh, m->dinp, n);
-  if ((r = run_layers(m, n, s))) return r;
+  if ((r = run_layers(m, n, nullptr, s))) return r;
   k_copy_rows<<<nblk((size_t)n * m->dout, 256), 256, 0, s>>>(m->Yf, m->doutp, Y, m->dout, n);
-  return (int)cudaGetLastError();
+  if ((r = (int)cudaGetLastError())) return r;
+  return mlp_take_error(m, s) ? (int)cudaErrorLaunchTimeout : 0;
 }
 
-int mlp_infer(MlpState* m, const fedg::Ops& op, const double* qd, const double* qm, const double* qr, double impl_fac,
+int mlp_infer(MlpState* m, const fedg::Ops& op, const float2* qd, const float2* qm, const float2* qr, double impl_fac,
               float* gd, float* gm, float* gr, cudaStream_t s) {
   if (!m || !m->ready) return (int)cudaErrorNotReady;
   if (m->L != op.L) return (int)cudaErrorInvalidValue;
   const int ncol = op.NeX * op.NeY * op.N1 * op.N1;
   int r = ensure_infer(m, (size_t)ncol);
   if (r) return r;
-  ColMap cm{op.N1, op.Np, op.NeX, op.NeY, op.L};
-  k_gather_x<<<nblk((size_t)ncol * m->dinp, 256), 256, 0, s>>>(cm, qd, qm, qr, (float)impl_fac * m->in_scale[3],
-                                                               m->in_scale[0], m->in_scale[1], m->in_scale[2], m->Xh,
-                                                               m->dinp, ncol);
-  if ((r = run_layers(m, ncol, s))) return r;
-  k_scatter_y<<<nblk((size_t)ncol * 3 * m->L, 256), 256, 0, s>>>(cm, m->Yf, m->doutp, 1.f / m->out_scale[0],
-                                                                 1.f / m->out_scale[1], 1.f / m->out_scale[2], gd, gm,
-                                                                 gr, ncol);
+  ColIO io{};
+  io.cm = ColMap{op.N1, op.Np, op.NeX, op.NeY, op.L};
+  io.qd = qd; io.qm = qm; io.qr = qr;
+  io.s0 = m->in_scale[0]; io.s1 = m->in_scale[1]; io.s2 = m->in_scale[2];
+  io.fac = (float)impl_fac * m->in_scale[3];
+  io.gd = gd; io.gm = gm; io.gr = gr;
+  io.r0 = 1.f / m->out_scale[0]; io.r1 = 1.f / m->out_scale[1]; io.r2 = 1.f / m->out_scale[2];
+  if ((r = run_layers(m, ncol, &io, s))) return r;
   return (int)cudaGetLastError();
 }

@@ -12,8 +12,12 @@ void mlp_free(MlpState* m);
 bool mlp_ready(const MlpState* m);
 // Guess of Q - q* for every column from the stage input q* (DDENS, MOMZ, DRHOT fields, FP64) and
 // impl_fac; writes three FP32 (Np, Ne) fields.  Runs the three GEMMs on the tensor cores.
-int mlp_infer(MlpState* m, const fedg::Ops& op, const double* qd, const double* qm, const double* qr, double impl_fac,
+int mlp_infer(MlpState* m, const fedg::Ops& op, const float2* qd, const float2* qm, const float2* qr, double impl_fac,
               float* gd, float* gm, float* gr, cudaStream_t s);
+
+// 0, or -1 if a tensor-core GEMM of this network gave up waiting on its barrier since the last
+// call (synchronises the stream; clears the flag)
+int mlp_take_error(MlpState* m, cudaStream_t s);
 
 // host-side management used by the C ABI
 int mlp_create(int levels, int hidden, MlpState** out);

@@ -15,9 +15,11 @@
 // so every global load of a level touches whole 32-byte sectors.
 //
 // Precision (see fedg_mixed.cu for the whole path):
-//   - the iterate P is FP64 (shared memory); the convergence test is on the FP64 residual
-//     b = impl_fac A(P) + q* - P (FP64 operator, "certifying" residual);
-//   - the first correction of every column uses the split residual (FP32 operator, FP64 q* - P);
+//   - the iterate P and the stage input q* are float pairs (hi + lo, about 48 significant bits,
+//     fedg_f2.cuh); the convergence test is on the residual b = impl_fac A(P) + q* - P with the
+//     operator evaluated in float pairs ("certifying" residual), so the column reaches the
+//     FP64-class Newton solution while the kernel issues no FP64 arithmetic on its main path;
+//   - the first correction of every column uses the split residual (FP32 operator, q* - P in pairs);
 //   - Jacobian, block-Thomas and the element LU (no pivoting: I + impl_fac J is diagonally
 //     dominant at stable time steps; a failure shows as a non-converging or non-finite FP64
 //     residual, reported per column) are FP32;
@@ -28,6 +30,7 @@
 #include <algorithm>
 
 #include "fedg_ctx.cuh"
+#include "fedg_f2.cuh"
 #include "fedg_mixed.cuh"
 
 namespace fedg {
@@ -42,10 +45,10 @@ struct ColLayout {
   __host__ __device__ ColLayout(int N1, int NeZ) {
     const int L = N1 * NeZ;
     int o = 0;
-    oP = o;    o += 24 * L;                    // double P[3L] (uv phase: P[2L])
+    oP = o;    o += 24 * L;                    // float2 P[3L] (uv phase: var0 pairs [2L])
     oJq = o;   o += 16 * L;                    // float4 Jq[L]: pot, wt, dpd of the Jacobian
-    oRing = o; o += 72 * N1;                   // 3 element slots x N1 nodes x 3 doubles
-    oDel = o;  o += 48;                        // 6 face fluxes of the current element
+    oRing = o; o += 96 * N1;                   // 3 element slots x 4 quantities x N1 nodes x float2
+    oDel = o;  o += 48;                        // 6 face fluxes (float2) of the current element
     oBf = o;   o += 12 * L;                    // float b / y / x [3L] (uv phase: [2L])
     oBc = o;   o += 64;                        // block-Thomas coupling from the element below
     oAl = o;   o += ((8 * NeZ + 15) / 16) * 16; // alB, alT per element
@@ -58,10 +61,10 @@ struct ColLayout {
 
 template <int N1>
 struct Col {
-  double* P;
+  float2* P;     // iterate, float pairs, row 3l+v (v: DENS, MOMZ, RHOT)
   float4* Jq;
-  double* ring;  // [3][3][N1]: slot, quantity (fm, fr, pot), node
-  double* del;
+  void* ring;    // [3][4][N1]: slot, quantity (MOMZ, DDENS, fm, fr), node
+  void* del;
   float* Bf;
   float* bc;
   float* al;
@@ -81,95 +84,75 @@ __device__ __forceinline__ float grp_max_nan(float e, int width) {
   return e;
 }
 
-// (1+r)^kappa - 1 by its binomial series for |r| <= rmax (NT terms, compile-time indices into
-// the coefficient table so it stays in the parameter bank), else pow(); nt chosen from max|r|
-template <int NT>
-__device__ __forceinline__ double binom_horner(double r, const PresSeries& ps) {
-  double s = ps.c[NT - 1];
-#pragma unroll
-  for (int m = NT - 2; m >= 0; --m) s = fma(s, r, ps.c[m]);
-  return s * r;
-}
-__device__ __forceinline__ double binom_pm1c(double r, const PresSeries& ps, double kap, int nt) {
-  if (fabs(r) > ps.rmax) return pow(1.0 + r, kap) - 1.0;
-  switch (nt) {
-    case 4: return binom_horner<4>(r, ps);
-    case 5: return binom_horner<5>(r, ps);
-    case 8: return binom_horner<8>(r, ps);
-    default: return binom_horner<12>(r, ps);
-  }
-}
-__device__ __forceinline__ int binom_nterm(float amax) {
-  return amax <= 1e-4f ? 4 : (amax <= 1e-3f ? 5 : (amax <= 1e-2f ? 8 : 12));
-}
-
-struct ResIn {
-  const double *dh, *ph, *rh, *rhinv;   // FP64 profiles
-  const float *dhf, *phf, *rhf, *rhinvf; // FP32 profiles
-};
-
 // ---------------------------------------------------------------------------------------------
 // residual b = impl_fac A(P) + q* - P of the DENS/MOMZ/RHOT system into c.Bf (FP32), the FP32
 // Jacobian level quantities into c.Jq; returns the column max of |b|/scale (NaN if not finite).
-// CERT: the operator A in FP64 (eval_Ax, hevi_common_2.F90:1177-1292, with the vertical face
-// flux vi_cal_del_flux_dyn :1294-1323); otherwise A in FP32 with only q* - P in FP64.
+// CERT: the operator A in float pairs (eval_Ax, hevi_common_2.F90:1177-1292, with the vertical
+// face flux vi_cal_del_flux_dyn :1294-1323); otherwise A in FP32 with only q* - P in pairs.
 // Element by element, with the level quantities of elements e-1, e, e+1 in a ring of 3 slots.
+// The pressure deviation PRES_hyd ((1 + r)^kappa - 1), r = DRHOT/RHOT_hyd, is the binomial
+// series: its leading term kappa r in pairs, the rest (relative size |r|) in FP32, which keeps
+// the pair precision for |r| <= rmax; beyond that pow() in FP64.
 template <int N1, bool CERT>
-__device__ float col_residual(const Ops& op, const Col<N1>& c, const ResIn& pr, const PresSeries& ps,
-                              const F5c& qin, double impl_fac, double cref) {
-  using T = typename std::conditional<CERT, double, float>::type;
+__device__ float col_residual(const OpsX& ox, const Col<N1>& c, const ProfX& px, const X5& qin, float2 impl2,
+                              float cref) {
   constexpr int N = N1 - 1;
   const int k = c.k;
-  T Dk[N1], Tk[N1];
+  const float kapf = ox.kap.x;
+  float2* r2 = reinterpret_cast<float2*>(c.ring);
+  float* r1 = reinterpret_cast<float*>(c.ring);
+  auto ri = [](int s, int q, int m) { return (s * 4 + q) * N1 + m; };
+  f2 Dk[N1], Tk[N1];
 #pragma unroll
   for (int m = 0; m < N1; ++m) {
-    Dk[m] = (T)op.D[k * N1 + m];
-    Tk[m] = (T)op.T[k * N1 + m];
+    Dk[m] = f2_of(ox.D[k * N1 + m]);
+    Tk[m] = f2_of(ox.T[k * N1 + m]);
   }
-  const T E33 = (T)op.E33, lbk = (T)op.Lb[k], ltk = (T)op.Lt[k], grav = (T)op.grav;
-  const T tmp1 = (T)(0.5 * op.FSz);
-  const float kapf = (float)op.kap;
-  // ring [slot][q][node]: q 0 fm, 1 fr, 2 pot; FP32 mode also 3 MOMZ, 4 DDENS (as floats, so the
-  // FP32 sums read no FP64 value); 3 slots x 5 x N1 floats fit the 3 x 3 x N1 doubles
-  constexpr int NQ = CERT ? 3 : 5;
-  T* rg = reinterpret_cast<T*>(c.ring);
-  auto R = [&](int slot, int q, int m) -> T& { return rg[(slot * NQ + q) * N1 + m]; };
+  const f2 lbk = f2_of(ox.Lb[k]), ltk = f2_of(ox.Lt[k]);
+  const f2 E33 = f2_of(ox.E33), grav = f2_of(ox.grav), tmp1 = f2_of(ox.tmp1), impl = f2_of(impl2);
 
   auto fill = [&](int e) {  // level quantities of node (e, k) into slot e % 3 (all lanes)
     const int l = e * N1 + k;
-    const double Pd = c.P[3 * l], Pm = c.P[3 * l + 1], Pr = c.P[3 * l + 2];
-    const float densf = __ldg(pr.dhf + l) + (float)Pd;
-    const float rhotf = __ldg(pr.rhf + l) + (float)Pr;
-    const float rdf = 1.f / densf;
-    float fmf, potf;
+    const f2 Pd = f2_of(c.P[3 * l]), Pm = f2_of(c.P[3 * l + 1]), Pr = f2_of(c.P[3 * l + 2]);
     const int s = e % 3;
+    const float phf = __ldg(px.phf + l);
+    float potf, wtf, fmf, rhotf;
     if constexpr (CERT) {
-      const double dens = __ldg(pr.dh + l) + Pd;
-      const double rhot = __ldg(pr.rh + l) + Pr;
-      double rd = (double)rdf;  // one Newton step on 1/dens from the FP32 reciprocal
-      rd = rd * fma(-dens, rd, 2.0);
-      rd = rd * fma(-dens, rd, 2.0);
-      const double pot = rhot * rd;
-      const double rr = Pr * __ldg(pr.rhinv + l);
-      float ra = fabsf((float)rr);
+      const f2 dens = f2_add(f2_of(__ldg(px.dh + l)), Pd);
+      const f2 rhot = f2_add(f2_of(__ldg(px.rh + l)), Pr);
+      const f2 rd = f2_recip(dens);
+      const f2 pot = f2_mul(rhot, rd);
+      const f2 rr = f2_mul(Pr, f2_of(__ldg(px.rhinv + l)));
+      f2 S;
+      if (fabsf(rr.h) <= ox.rmax) {
+        float tl = ox.cb[11];
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) ra = fmaxf(ra, __shfl_xor_sync(FULL, ra, o));
-      const double fm = __ldg(pr.ph + l) * binom_pm1c(rr, ps, op.kap, binom_nterm(ra));
-      R(s, 0, k) = fm;
-      R(s, 1, k) = pot * Pm;
-      R(s, 2, k) = pot;
-      fmf = (float)fm;
-      potf = (float)pot;
+        for (int m = 10; m >= 1; --m) tl = fmaf(tl, rr.h, ox.cb[m]);
+        S = f2_add_f(f2_mul(f2_of(ox.kap), rr), __fmul_rn(__fmul_rn(rr.h, rr.h), tl));
+      } else {
+        S = f2_split(pow(1.0 + ((double)rr.h + (double)rr.l), ox.kap64) - 1.0);
+      }
+      const f2 fm = f2_mul(f2_of(__ldg(px.ph + l)), S);
+      r2[ri(s, 0, k)] = f2_pack(Pm);
+      r2[ri(s, 1, k)] = f2_pack(Pd);
+      r2[ri(s, 2, k)] = f2_pack(fm);
+      r2[ri(s, 3, k)] = f2_pack(f2_mul(pot, Pm));
+      potf = pot.h;
+      fmf = fm.h;
+      wtf = Pm.h * rd.h;
+      rhotf = rhot.h;
     } else {
+      const float rdf = 1.f / (__ldg(px.dhf + l) + Pd.h);
+      rhotf = __ldg(px.rhf + l) + Pr.h;
       potf = rhotf * rdf;
-      fmf = __ldg(pr.phf + l) * expm1f(kapf * log1pf((float)Pr * __ldg(pr.rhinvf + l)));
-      R(s, 0, k) = fmf;
-      R(s, 1, k) = potf * (float)Pm;
-      R(s, 2, k) = potf;
-      R(s, 3, k) = (float)Pm;
-      R(s, 4, k) = (float)Pd;
+      fmf = phf * expm1f(kapf * log1pf(Pr.h * __ldg(px.rthf + l)));
+      wtf = Pm.h * rdf;
+      r1[ri(s, 0, k)] = Pm.h;
+      r1[ri(s, 1, k)] = Pd.h;
+      r1[ri(s, 2, k)] = fmf;
+      r1[ri(s, 3, k)] = potf * Pm.h;
     }
-    c.Jq[l] = make_float4(potf, (float)Pm * rdf, kapf * (__ldg(pr.phf + l) + fmf) / rhotf, 0.f);
+    c.Jq[l] = make_float4(potf, wtf, kapf * (phf + fmf) / rhotf, 0.f);
   };
 
   fill(0);
@@ -187,53 +170,92 @@ __device__ float col_residual(const Ops& op, const Col<N1>& c, const ResIn& pr, 
       const bool lid = s == 0 ? (e == 0) : (e == c.NeZ - 1);
       const int lP = lid ? lM : (s == 0 ? lM - 1 : lM + 1);
       const int sP = lid ? sc : (s == 0 ? sb : st), nP = lid ? nM : (s == 0 ? N : 0);
-      const T nz = s == 0 ? T(-1) : T(1);
-      const T al = (T)(s == 0 ? c.alB(e) : c.alT(e));
-      const double mzMd = c.P[3 * lM + 1];
-      const double mzPd = lid ? -mzMd : c.P[3 * lP + 1];
-      const T mzM = (T)mzMd, mzP = (T)mzPd;
-      const T dmz = (T)(mzPd - mzMd);
-      T val;
-      if (v == 0) val = tmp1 * (dmz * nz - al * (T)(c.P[3 * lP] - c.P[3 * lM]));
-      else if (v == 1) val = tmp1 * ((R(sP, 0, nP) - R(sc, 0, nM)) * nz - al * dmz);
-      else val = tmp1 * ((R(sP, 2, nP) * mzP - R(sc, 2, nM) * mzM) * nz - al * (T)(c.P[3 * lP + 2] - c.P[3 * lM + 2]));
-      reinterpret_cast<T*>(c.del)[t] = val;
+      const float nz = s == 0 ? -1.f : 1.f;
+      const float al = s == 0 ? c.alB(e) : c.alT(e);
+      // jump of RHOT (the slip lid's exterior state is the interior one: no jump)
+      const f2 dth = lid ? f2{0.f, 0.f} : f2_sub(f2_of(c.P[3 * lP + 2]), f2_of(c.P[3 * lM + 2]));
+      if constexpr (CERT) {
+        const f2 mzM = f2_of(r2[ri(sc, 0, nM)]);
+        const f2 dmz = lid ? f2_add(f2_neg(mzM), f2_neg(mzM)) : f2_sub(f2_of(r2[ri(sP, 0, nP)]), mzM);
+        f2 x;
+        if (v == 0) {
+          const f2 dr = lid ? f2{0.f, 0.f} : f2_sub(f2_of(r2[ri(sP, 1, nP)]), f2_of(r2[ri(sc, 1, nM)]));
+          x = f2_sub(f2_mul_f(dmz, nz), f2_mul_f(dr, al));
+        } else if (v == 1) {
+          const f2 dfm = lid ? f2{0.f, 0.f} : f2_sub(f2_of(r2[ri(sP, 2, nP)]), f2_of(r2[ri(sc, 2, nM)]));
+          x = f2_sub(f2_mul_f(dfm, nz), f2_mul_f(dmz, al));
+        } else {
+          const f2 frM = f2_of(r2[ri(sc, 3, nM)]);
+          const f2 dfr = lid ? f2_add(f2_neg(frM), f2_neg(frM)) : f2_sub(f2_of(r2[ri(sP, 3, nP)]), frM);
+          x = f2_sub(f2_mul_f(dfr, nz), f2_mul_f(dth, al));
+        }
+        reinterpret_cast<float2*>(c.del)[t] = f2_pack(f2_mul(tmp1, x));
+      } else {
+        // MOMZ and density jumps from the float-pair iterate: the jumps of a DG solution are small
+        // against the values, so differencing FP32-rounded values would lose them
+        const float mzM = r1[ri(sc, 0, nM)];
+        const float dmz = lid ? -2.f * mzM : f2_to_f(f2_sub(f2_of(c.P[3 * lP + 1]), f2_of(c.P[3 * lM + 1])));
+        float x;
+        if (v == 0) x = dmz * nz - al * (lid ? 0.f : f2_to_f(f2_sub(f2_of(c.P[3 * lP]), f2_of(c.P[3 * lM]))));
+        else if (v == 1) x = (lid ? 0.f : r1[ri(sP, 2, nP)] - r1[ri(sc, 2, nM)]) * nz - al * dmz;
+        else {
+          const float frM = r1[ri(sc, 3, nM)];
+          x = (lid ? -2.f * frM : r1[ri(sP, 3, nP)] - frM) * nz - al * f2_to_f(dth);
+        }
+        reinterpret_cast<float*>(c.del)[t] = tmp1.h * x;
+      }
     }
     __syncwarp();
     {
       const int l = e * N1 + k;
-      T sd = 0, sm = 0, sr = 0, drho = 0;
-#pragma unroll
-      for (int m = 0; m < N1; ++m) {
-        T mz, dd;
-        if constexpr (CERT) {
-          mz = c.P[3 * (e * N1 + m) + 1];
-          dd = c.P[3 * (e * N1 + m)];
-        } else {
-          mz = R(sc, 3, m);
-          dd = R(sc, 4, m);
-        }
-        sd += Dk[m] * mz;
-        sm += Dk[m] * R(sc, 0, m);
-        sr += Dk[m] * R(sc, 1, m);
-        drho += Tk[m] * dd;
-      }
-      const T* dl = reinterpret_cast<const T*>(c.del);
-      T A[3];
-      A[0] = -(E33 * sd + lbk * dl[0] + ltk * dl[3]);
-      A[1] = -(E33 * sm + lbk * dl[1] + ltk * dl[4]) - grav * drho;
-      A[2] = -(E33 * sr + lbk * dl[2] + ltk * dl[5]);
       const size_t gi = c.g(e);
-      const float isc[3] = {1.f / __ldg(pr.dhf + l), 1.f / (__ldg(pr.dhf + l) * (float)cref), 1.f / __ldg(pr.rhf + l)};
+      const float isc[3] = {1.f / __ldg(px.dhf + l), 1.f / (__ldg(px.dhf + l) * cref), 1.f / __ldg(px.rhf + l)};
+      float bfl[3];
+      if constexpr (CERT) {
+        f2acc sd, sm, sr, drho;
+#pragma unroll
+        for (int m = 0; m < N1; ++m) {
+          sd.add(Dk[m], f2_of(r2[ri(sc, 0, m)]));
+          drho.add(Tk[m], f2_of(r2[ri(sc, 1, m)]));
+          sm.add(Dk[m], f2_of(r2[ri(sc, 2, m)]));
+          sr.add(Dk[m], f2_of(r2[ri(sc, 3, m)]));
+        }
+        const float2* dl = reinterpret_cast<const float2*>(c.del);
+        f2 A[3];
+        A[0] = f2_add(f2_add(f2_mul(E33, sd.get()), f2_mul(lbk, f2_of(dl[0]))), f2_mul(ltk, f2_of(dl[3])));
+        A[1] = f2_add(f2_add(f2_add(f2_mul(E33, sm.get()), f2_mul(lbk, f2_of(dl[1]))), f2_mul(ltk, f2_of(dl[4]))),
+                      f2_mul(grav, drho.get()));
+        A[2] = f2_add(f2_add(f2_mul(E33, sr.get()), f2_mul(lbk, f2_of(dl[2]))), f2_mul(ltk, f2_of(dl[5])));
+#pragma unroll
+        for (int v = 0; v < 3; ++v) {  // A[v] holds -A: b = q* - P - impl_fac (-A)
+          const f2 qmp = f2_sub(f2_of(__ldg(qin.v[gv[v]] + gi)), f2_of(c.P[3 * l + v]));
+          bfl[v] = f2_to_f(f2_sub(qmp, f2_mul(impl, A[v])));
+        }
+      } else {
+        float sd = 0.f, sm = 0.f, sr = 0.f, drho = 0.f;
+#pragma unroll
+        for (int m = 0; m < N1; ++m) {
+          sd = fmaf(Dk[m].h, r1[ri(sc, 0, m)], sd);
+          drho = fmaf(Tk[m].h, r1[ri(sc, 1, m)], drho);
+          sm = fmaf(Dk[m].h, r1[ri(sc, 2, m)], sm);
+          sr = fmaf(Dk[m].h, r1[ri(sc, 3, m)], sr);
+        }
+        const float* dl = reinterpret_cast<const float*>(c.del);
+        float A[3];
+        A[0] = E33.h * sd + lbk.h * dl[0] + ltk.h * dl[3];
+        A[1] = E33.h * sm + lbk.h * dl[1] + ltk.h * dl[4] + grav.h * drho;
+        A[2] = E33.h * sr + lbk.h * dl[2] + ltk.h * dl[5];
+#pragma unroll
+        for (int v = 0; v < 3; ++v) {
+          const float qmp = f2_to_f(f2_sub(f2_of(__ldg(qin.v[gv[v]] + gi)), f2_of(c.P[3 * l + v])));
+          bfl[v] = fmaf(-impl.h, A[v], qmp);
+        }
+      }
 #pragma unroll
       for (int v = 0; v < 3; ++v) {
-        const double qmp = __ldg(qin.v[gv[v]] + gi) - c.P[3 * l + v];
-        float bfl;
-        if constexpr (CERT) bfl = (float)fma(impl_fac, A[v], qmp);
-        else bfl = fmaf((float)impl_fac, A[v], (float)qmp);
-        c.Bf[3 * l + v] = bfl;
-        errf = fmaxf(errf, fabsf(bfl) * isc[v]);
-        if (!(fabsf(bfl) < 3.0e38f)) errf = __int_as_float(0x7fc00000);
+        c.Bf[3 * l + v] = bfl[v];
+        errf = fmaxf(errf, fabsf(bfl[v]) * isc[v]);
+        if (!(fabsf(bfl[v]) < 3.0e38f)) errf = __int_as_float(0x7fc00000);
       }
     }
     __syncwarp();
@@ -430,7 +452,7 @@ __device__ void col_solve(const Ops& op, const Col<N1>& c, double impl_fac, floa
     for (int e = 0; e < c.NeZ; ++e) {
       const int l = e * N1 + k;
 #pragma unroll
-      for (int v = 0; v < 3; ++v) c.P[3 * l + v] += (double)c.Bf[3 * l + v];
+      for (int v = 0; v < 3; ++v) c.P[3 * l + v] = f2_pack(f2_add_f(f2_of(c.P[3 * l + v]), c.Bf[3 * l + v]));
     }
   }
   __syncwarp();
@@ -438,8 +460,7 @@ __device__ void col_solve(const Ops& op, const Col<N1>& c, double impl_fac, floa
 
 // ---------------------------------------------------------------------------------------------
 template <int N1>
-__global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const Prof pf, const ProfF pff, const double* __restrict__ rhinv,
-                                                const PresSeries ps, const F5c qin, const F5c z,
+__global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const OpsX ox, const ProfX px, const X5 qin, const F5c z,
                                                 const float* const* guess, float* const* qsf, float* const* tout,
                                                 float* __restrict__ gsc, int* status, unsigned long long* cnt,
                                                 const MixViArgs args, int ncol) {
@@ -454,10 +475,10 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const Prof pf, con
   const ColLayout lay(N1, NeZ);
   unsigned char* base = smraw + (size_t)grp * lay.stride;
   Col<N1> c;
-  c.P = reinterpret_cast<double*>(base + lay.oP);
+  c.P = reinterpret_cast<float2*>(base + lay.oP);
   c.Jq = reinterpret_cast<float4*>(base + lay.oJq);
-  c.ring = reinterpret_cast<double*>(base + lay.oRing);
-  c.del = reinterpret_cast<double*>(base + lay.oDel);
+  c.ring = base + lay.oRing;
+  c.del = base + lay.oDel;
   c.Bf = reinterpret_cast<float*>(base + lay.oBf);
   c.bc = reinterpret_cast<float*>(base + lay.oBc);
   c.al = reinterpret_cast<float*>(base + lay.oAl);
@@ -470,18 +491,18 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const Prof pf, con
     c.gb = (size_t)exy * Np + ci + N1 * cj + NF * k;
     c.gs = nxy * Np;
   }
-  const double impl_fac = args.impl_fac;
-  const float kapf = (float)op.kap;
+  const float kapf = ox.kap.x;
+  const float iif = (float)args.inv_impl_fac;
 
   // ---- frozen vertical Rusanov speed |w| + c of var0 (hevi_common_2.F90:1149-1155) ----
   float* atmp = c.Bf;  // [L]
   for (int e = 0; e < NeZ; ++e) {
     const int l = e * N1 + k;
     const size_t gi = c.g(e);
-    const float dd0 = (float)__ldg(z.v[VD] + gi), dr0 = (float)__ldg(z.v[VRT] + gi);
-    const float rdens0 = 1.f / (__ldg(pff.dens + l) + dd0);
-    const float wt0 = (float)__ldg(z.v[VMZ] + gi) * rdens0;
-    const float pres0 = __ldg(pff.pres + l) * (1.f + expm1f(kapf * log1pf(dr0 * __ldg(pff.rtherm + l))));
+    const float dd0 = f2_split(__ldg(z.v[VD] + gi)).h, dr0 = f2_split(__ldg(z.v[VRT] + gi)).h;
+    const float rdens0 = 1.f / (__ldg(px.dhf + l) + dd0);
+    const float wt0 = f2_split(__ldg(z.v[VMZ] + gi)).h * rdens0;
+    const float pres0 = __ldg(px.phf + l) * (1.f + expm1f(kapf * log1pf(dr0 * __ldg(px.rthf + l))));
     atmp[l] = fabsf(wt0) + sqrtf(kapf * pres0 * rdens0);
   }
   __syncwarp();
@@ -493,12 +514,12 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const Prof pf, con
   __syncwarp();
 
   // ---- MOMX/MOMY (eval_Ax_uv / solve_uv) ----
-  // The operator is linear and acts on the face jumps only.  With P = P0 + D (P0 = var0 in FP64,
-  // D an FP32 increment), b(P) = [impl_fac A(P0) + (q* - P0)] + impl_fac A(D) - D.  The FP64 work is
-  // q* - P0, kept as an FP32 pair hi + lo so the residual has the accuracy of the FP64 difference,
-  // and the face jumps of P0, once per column; everything after that is FP32.
+  // The operator is linear and acts on the face jumps only.  With P = P0 + D (P0 = var0, D an
+  // FP32 increment), b(P) = [impl_fac A(P0) + (q* - P0)] + impl_fac A(D) - D.  q* - P0 is kept as
+  // an FP32 pair hi + lo and the face jumps of P0 are formed in pairs, once per column;
+  // everything after that is FP32.
   {
-    double* P0 = c.P;                                   // [2L] FP64, only while the jumps are formed
+    float2* P0 = c.P;                                   // [2L] var0 pairs, only while the jumps are formed
     float* qh = reinterpret_cast<float*>(c.Jq);         // [2L] (q* - P0) hi
     float* ql = qh + 2 * L;                             // [2L] (q* - P0) lo
     float* D = reinterpret_cast<float*>(c.P);           // [2L] increment, once P0 is dead
@@ -509,12 +530,11 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const Prof pf, con
       const size_t gi = c.g(e);
 #pragma unroll
       for (int m = 0; m < 2; ++m) {
-        const double p0 = __ldg(z.v[VMX + m] + gi);
-        const double d = __ldg(qin.v[VMX + m] + gi) - p0;
-        const float hi = (float)d;
-        P0[2 * l + m] = p0;
-        qh[2 * l + m] = hi;
-        ql[2 * l + m] = (float)(d - (double)hi);
+        const f2 p0 = f2_split(__ldg(z.v[VMX + m] + gi));
+        const f2 d = f2_sub(f2_of(__ldg(qin.v[VMX + m] + gi)), p0);
+        P0[2 * l + m] = f2_pack(p0);
+        qh[2 * l + m] = d.h;
+        ql[2 * l + m] = d.l;
       }
     }
     __syncwarp();
@@ -524,7 +544,7 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const Prof pf, con
         const int lM = e * N1 + (s == 0 ? 0 : N);
         const bool lid = s == 0 ? (e == 0) : (e == NeZ - 1);
         const int lP = lid ? lM : (s == 0 ? lM - 1 : lM + 1);
-        j0[4 * e + t] = (float)(P0[2 * lP + m] - P0[2 * lM + m]);
+        j0[4 * e + t] = f2_to_f(f2_sub(f2_of(P0[2 * lP + m]), f2_of(P0[2 * lM + m])));
       }
     }
     __syncwarp();
@@ -534,9 +554,9 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const Prof pf, con
       D[2 * l + 1] = 0.f;
     }
     __syncwarp();
-    const float cfs = (float)(0.5 * impl_fac * op.FSz);
-    const float lbk = (float)op.Lb[k], ltk = (float)op.Lt[k];
-    const float lb0 = (float)op.Lb[0], lbN = (float)op.Lb[N], lt0 = (float)op.Lt[0], ltN = (float)op.Lt[N];
+    const float cfs = (float)(0.5 * args.impl_fac * op.FSz);
+    const float lbk = ox.Lb[k].x, ltk = ox.Lt[k].x;
+    const float lb0 = ox.Lb[0].x, lbN = ox.Lb[N].x, lt0 = ox.Lt[0].x, ltN = ox.Lt[N].x;
     const float iscu_c = 1.f / (float)args.cref;
     float* jdel = reinterpret_cast<float*>(c.del);  // 4 jumps of the current element
     bool active = true;
@@ -552,7 +572,7 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const Prof pf, con
         }
         __syncwarp();
         const int l = e * N1 + k;
-        const float iscu = iscu_c / __ldg(pff.dens + l);
+        const float iscu = iscu_c / __ldg(px.dhf + l);
         const float aB = lbk * c.alB(e), aT = ltk * c.alT(e);
 #pragma unroll
         for (int m = 0; m < 2; ++m) {
@@ -610,15 +630,17 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const Prof pf, con
       active = need;
       __syncwarp();
     }
-    const float iif = (float)args.inv_impl_fac;
     for (int e = 0; e < NeZ; ++e) {
       const int l = e * N1 + k;
       const size_t gi = c.g(e);
-      const double dh64 = __ldg(pf.dens + l);
-      qsf[VMX][gi] = (float)fma(-dh64, args.Uref, __ldg(z.v[VMX] + gi)) + D[2 * l];
-      qsf[VMY][gi] = (float)fma(-dh64, args.Vref, __ldg(z.v[VMY] + gi)) + D[2 * l + 1];
-      tout[VMX][gi] = ((D[2 * l] - qh[2 * l]) - ql[2 * l]) * iif;
-      tout[VMY][gi] = ((D[2 * l + 1] - qh[2 * l + 1]) - ql[2 * l + 1]) * iif;
+      const f2 dh = f2_of(__ldg(px.dh + l));
+#pragma unroll
+      for (int m = 0; m < 2; ++m) {
+        const f2 ref = f2_mul(dh, f2_of(m == 0 ? ox.Uref : ox.Vref));
+        const f2 p0 = f2_split(__ldg(z.v[VMX + m] + gi));
+        qsf[VMX + m][gi] = f2_to_f(f2_sub(p0, ref)) + D[2 * l + m];
+        tout[VMX + m][gi] = ((D[2 * l + m] - qh[2 * l + m]) - ql[2 * l + m]) * iif;
+      }
     }
     __syncwarp();
   }
@@ -630,25 +652,26 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const Prof pf, con
     const size_t gi = c.g(e);
 #pragma unroll
     for (int m = 0; m < 3; ++m)
-      c.P[3 * l + m] = guess ? __ldg(qin.v[gv[m]] + gi) + (double)__ldg(guess[m] + gi) : __ldg(z.v[gv[m]] + gi);
+      c.P[3 * l + m] = f2_pack(guess ? f2_add_f(f2_of(__ldg(qin.v[gv[m]] + gi)), __ldg(guess[m] + gi))
+                                     : f2_split(__ldg(z.v[gv[m]] + gi)));
   }
   __syncwarp();
-  const ResIn rin{pf.dens, pf.pres, pf.rhyd, rhinv, pff.dens, pff.pres, pff.therm, pff.rtherm};
   const size_t gcolumn = (size_t)col, glayer = (size_t)ncol;  // G history rows of this column
-  col_residual<N1, false>(op, c, rin, ps, qin, impl_fac, args.cref);
-  col_solve<N1>(op, c, impl_fac, gsc, gcolumn, glayer, true);
+  const float cref = (float)args.cref;
+  col_residual<N1, false>(ox, c, px, qin, args.impl2, cref);
+  col_solve<N1>(op, c, args.impl_fac, gsc, gcolumn, glayer, true);
   int nsolve = 1, st = 0;
   bool active = true;
   while (true) {
-    const float err = args.check64 ? col_residual<N1, true>(op, c, rin, ps, qin, impl_fac, args.cref)
-                                   : col_residual<N1, false>(op, c, rin, ps, qin, impl_fac, args.cref);
+    const float err = args.check64 ? col_residual<N1, true>(ox, c, px, qin, args.impl2, cref)
+                                   : col_residual<N1, false>(ox, c, px, qin, args.impl2, cref);
     if (active) {
       if (err != err) { st = -2; active = false; }
       else if ((double)err <= args.tol) { st = nsolve; active = false; }
       else if (nsolve >= args.max_iter) { st = -1; active = false; }
     }
     if (!__any_sync(FULL, active)) break;
-    col_solve<N1>(op, c, impl_fac, gsc, gcolumn, glayer, active);
+    col_solve<N1>(op, c, args.impl_fac, gsc, gcolumn, glayer, active);
     ++nsolve;
   }
   for (int e = 0; e < NeZ; ++e) {
@@ -656,9 +679,9 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const Prof pf, con
     const size_t gi = c.g(e);
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
-      const double pnew = c.P[3 * l + m];
-      qsf[gv[m]][gi] = (float)pnew;
-      tout[gv[m]][gi] = (float)(pnew - __ldg(qin.v[gv[m]] + gi)) * (float)args.inv_impl_fac;
+      const f2 pnew = f2_of(c.P[3 * l + m]);
+      qsf[gv[m]][gi] = f2_to_f(pnew);
+      tout[gv[m]][gi] = f2_to_f(f2_sub(pnew, f2_of(__ldg(qin.v[gv[m]] + gi)))) * iif;
     }
   }
   if (k == 0 && status) status[col] = st;
@@ -675,9 +698,9 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const Prof pf, con
 }
 
 template <int N1>
-int launch_n(const Ops& op, const Prof& pf, const ProfF& pff, const double* rhinv, const PresSeries& ps,
-             const F5c& qin, const F5c& z, const float* const* guess, float* const* qsf, float* const* tout, float* gsc,
-             int* status, unsigned long long* cnt, const MixViArgs& a, cudaStream_t s) {
+int launch_n(const Ops& op, const OpsX& ox, const ProfX& px, const X5& qin, const F5c& z, const float* const* guess,
+             float* const* qsf, float* const* tout, float* gsc, int* status, unsigned long long* cnt,
+             const MixViArgs& a, cudaStream_t s) {
   constexpr int C = 32 / N1;
   const ColLayout lay(N1, op.NeZ);
   const size_t smem = (size_t)lay.stride * C;
@@ -685,7 +708,7 @@ int launch_n(const Ops& op, const Prof& pf, const ProfF& pff, const double* rhin
   const int ncol = op.NeX * op.NeY * N1 * N1;
   auto kfn = k_vi_cols<N1>;
   cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  kfn<<<(ncol + C - 1) / C, 32, smem, s>>>(op, pf, pff, rhinv, ps, qin, z, guess, qsf, tout, gsc, status, cnt, a, ncol);
+  kfn<<<(ncol + C - 1) / C, 32, smem, s>>>(op, ox, px, qin, z, guess, qsf, tout, gsc, status, cnt, a, ncol);
   return (int)cudaGetLastError();
 }
 
@@ -693,12 +716,12 @@ int launch_n(const Ops& op, const Prof& pf, const ProfF& pff, const double* rhin
 
 size_t vi_cols_scratch_floats(size_t nodes) { return (size_t)12 * nodes; }
 
-int launch_vi_cols(int N1, const Ops& op, const Prof& pf, const ProfF& pff, const double* rhinv, const PresSeries& ps,
-                   const F5c& qin, const F5c& z, const float* const* guess, float* const* qsf, float* const* tout,
-                   float* gsc, int* status, unsigned long long* cnt, const MixViArgs& a, cudaStream_t s) {
+int launch_vi_cols(int N1, const Ops& op, const OpsX& ox, const ProfX& px, const X5& qin, const F5c& z,
+                   const float* const* guess, float* const* qsf, float* const* tout, float* gsc, int* status,
+                   unsigned long long* cnt, const MixViArgs& a, cudaStream_t s) {
   switch (N1) {
-    case 4: return launch_n<4>(op, pf, pff, rhinv, ps, qin, z, guess, qsf, tout, gsc, status, cnt, a, s);
-    case 8: return launch_n<8>(op, pf, pff, rhinv, ps, qin, z, guess, qsf, tout, gsc, status, cnt, a, s);
+    case 4: return launch_n<4>(op, ox, px, qin, z, guess, qsf, tout, gsc, status, cnt, a, s);
+    case 8: return launch_n<8>(op, ox, px, qin, z, guess, qsf, tout, gsc, status, cnt, a, s);
   }
   return (int)cudaErrorInvalidValue;
 }

@@ -1,0 +1,152 @@
+"""One-hour precision run: the mixed-precision + learned-guess HEVI path against the plain FP64
+path, both on the GPU from the same initial state.  It reports the relative L2 error per variable
+at checkpoints.
+
+Workload: the density current on the p = 7 mesh with 800 m elements. This is the recipe of the
+medium HEVI case run in the precision form:
+
+  - isothermal 300 K base state;
+  - -15 K cosine bubble of 4 km x 2 km radius at z = 3 km;
+  - u = 10 m/s;
+  - periodic in x and y, slip lids;
+  - 8 vertical elements, i.e. 64-level columns.
+
+The default horizontal extent is 8 x 8 elements (6.4 km), so both paths finish an hour in a few
+GPU-minutes.  The time step is dt = 0.04 s. It is the stable step for this mesh: 0.08 s
+diverges, and the 0.5 s of the original recipe exceeds the horizontal acoustic limit of p = 7
+elements of 800 m. One simulated hour is therefore 90,000 steps.
+
+Paths:
+
+  plain    FP64 fused update (FElib's algorithm), Newton to tol 1e-10 (max 20 solves).
+  learned  Mixed-precision fused update.  The Newton starts from the column-guess MLP and is
+           certified by the FP64 residual to the same tol.  The MLP follows the learned-guess
+           recipe:
+             - 193 -> 256 -> 256 -> 192;
+             - trained on the GPU on pairs the plain solver generates from 20 random
+               density-current seeds, on 4 x 4 x 8 slices of the same mesh.
+
+Errors are computed on the full fields DENS, MOMX, MOMY, MOMZ, RHOT. Momentum is measured
+against at least 1 m/s of hydrostatic momentum. The deviation fields DDENS and DRHOT are also
+reported against their own norms.
+
+Usage (from the repository root):  PYTHONPATH=fe-project_gb300 python -m fedg.precision [--nex 8 ...]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import sys
+import time
+
+import numpy as np
+
+from . import cases
+from . import guess as fguess
+from . import lib as fl
+
+VARS = ("DENS", "MOMX", "MOMY", "MOMZ", "RHOT")
+
+
+def _errors(torch, got, ref, dens_hyd, therm_hyd):
+    full, dev = {}, {}
+    mfloor = float(dens_hyd.norm().item())
+    for v, nm in enumerate(VARS):
+        d = float((got[v] - ref[v]).norm().item())
+        if v == 0:
+            den = float((ref[0] + dens_hyd).norm().item())
+        elif v == 4:
+            den = float((ref[4] + therm_hyd).norm().item())
+        else:
+            den = max(float(ref[v].norm().item()), mfloor)
+        full[nm] = d / den
+    for v, nm in ((0, "DDENS"), (4, "DRHOT")):
+        dev[nm] = float((got[v] - ref[v]).norm().item()) / max(float(ref[v].norm().item()), 1e-300)
+    return full, dev
+
+
+def run(nex=8, ney=8, nez=8, dt=0.04, hours=1.0, checkpoint_min=10.0, chunk=250, use_guess=True, seeds=20,
+        train_steps=2000, out=sys.stdout):
+    import torch
+
+    base = cases.C2()
+    case = base.scaled(nex, ney, nez)
+    nsteps = int(round(hours * 3600.0 / dt))
+    ck_every = max(1, int(round(checkpoint_min * 60.0 / dt)))
+    info = {"workload": f"density current p=7 {nex}x{ney}x{nez} elements of 800 m, HEVI IMEX-ARK232",
+            "dt": dt, "steps": nsteps, "simulated_s": nsteps * dt, "newton_tol": 1e-10}
+    net = None
+    if use_guess:
+        t0 = time.perf_counter()
+        # learned-guess recipe: about 200k (stage input, converged increment) pairs from 20 seeds
+        # of 4x4x8 slices; 5 steps x 2 implicit stages x 1024 columns per seed
+        net, ginfo = fguess.build_guess(base.scaled(4, 4, nez), dt, seeds=range(seeds), nsteps=5,
+                                        per_stage_keep=None, train_steps=train_steps, batch=4096, lr=1e-3)
+        ginfo["build_s"] = time.perf_counter() - t0
+        info["guess_training"] = ginfo
+    q, b = cases.initial_state(case)
+    ctx = fl.Context(case)
+    ctx.set_base_state(b["dens_hyd"], b["pres_hyd"], b["therm_hyd"])
+    dens_hyd = ctx.tensor(b["dens_hyd"])
+    therm_hyd = ctx.tensor(b["therm_hyd"])
+    q64 = [ctx.tensor(a) for a in q]
+    qmx = [t.clone() for t in q64]
+    if net is not None:
+        net.attach(ctx)
+    o64 = dict(prec=fl.PREC_FP64, dt=dt, max_iter=20, tol=1e-10)
+    omx = dict(prec=fl.PREC_MIXED, dt=dt, max_iter=20, tol=1e-10, use_guess=net is not None)
+    stats = {"plain": {"s": 0.0, "fail": 0, "its": 0.0}, "learned": {"s": 0.0, "fail": 0, "its": 0.0}}
+    done, nchunk = 0, 0
+    print(json.dumps({"setup": info}), file=out, flush=True)
+    while done < nsteps:
+        n = min(chunk, nsteps - done, ck_every - done % ck_every)
+        for name, st, opts in (("plain", q64, o64), ("learned", qmx, omx)):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            nf, its = ctx.update(st, n, **opts)
+            torch.cuda.synchronize()
+            s = stats[name]
+            s["s"] += time.perf_counter() - t0
+            s["fail"] += nf
+            s["its"] += its * n
+        done += n
+        nchunk += 1
+        if done % ck_every == 0 or done == nsteps:
+            full, dev = _errors(torch, qmx, q64, dens_hyd, therm_hyd)
+            finite = all(bool(torch.isfinite(t).all().item()) for t in q64 + qmx)
+            rec = {"step": done, "t_s": done * dt, "rel_l2_full": full, "rel_l2_deviation": dev, "finite": finite,
+                   "plain_ms_per_step": 1e3 * stats["plain"]["s"] / done,
+                   "learned_ms_per_step": 1e3 * stats["learned"]["s"] / done,
+                   "plain_mean_solves": stats["plain"]["its"] / done,
+                   "learned_mean_solves": stats["learned"]["its"] / done,
+                   "plain_nonconverged": stats["plain"]["fail"], "learned_nonconverged": stats["learned"]["fail"]}
+            print(json.dumps(rec), file=out, flush=True)
+            if not finite:
+                break
+    ctx.close()
+    return rec
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--nex", type=int, default=8)
+    ap.add_argument("--ney", type=int, default=8)
+    ap.add_argument("--nez", type=int, default=8)
+    ap.add_argument("--dt", type=float, default=0.04)
+    ap.add_argument("--hours", type=float, default=1.0)
+    ap.add_argument("--checkpoint-min", type=float, default=10.0)
+    ap.add_argument("--chunk", type=int, default=250)
+    ap.add_argument("--no-guess", action="store_true")
+    ap.add_argument("--seeds", type=int, default=20)
+    ap.add_argument("--train-steps", type=int, default=2000)
+    a = ap.parse_args(argv)
+    import __graft_entry__ as ge  # noqa: F401  (repository root on sys.path when run from it)
+
+    ge.build()
+    run(a.nex, a.ney, a.nez, a.dt, a.hours, a.checkpoint_min, a.chunk, not a.no_guess, a.seeds, a.train_steps)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.path.insert(0, ".")
+    sys.exit(main())
