@@ -28,13 +28,8 @@ __device__ __forceinline__ float gelu_d(float x) {
 
 struct ColMap {
   int N1, Np, NeX, NeY, L;
+  int lgN1;  // log2(N1): N1 is a power of two
 };
-__device__ __forceinline__ size_t col_gidx(const ColMap& cm, int c, int l) {
-  const int NF = cm.N1 * cm.N1;
-  const int ij = c % NF, exy = c / NF, ci = ij % cm.N1, cj = ij / cm.N1;
-  const int ez = l / cm.N1, k = l - ez * cm.N1;
-  return ((size_t)ez * cm.NeX * cm.NeY + exy) * cm.Np + ci + cm.N1 * cj + NF * k;
-}
 // column gather/scatter of the first and last inference layers: features (var-major) DDENS'(l),
 // MOMZ(l), DRHOT'(l) of the column's L levels, then impl_fac, each times its scale; outputs
 // (Q - q*)(l) per variable divided by its scale, written into (Np, Ne) fields
@@ -49,7 +44,8 @@ struct ColIO {
 // ---------------------------------------------------------------------------------------------
 // Inference GEMM on the 5th-generation tensor cores:
 //   C[M x Np] = act(A[M x Kp] . W[Np x Kp]^T + bias), bf16 operands (both K-major), FP32 accumulate.
-// One CTA of 4 warps per 128 x BN output tile.  Each K chunk of 32 is staged in shared memory in
+// One CTA of 4 warps per 128 x BN output tile.  Each K chunk of 32 is prefetched into registers
+// while the previous chunk's MMAs run, then staged in one of two shared-memory buffers in
 // the no-swizzle K-major canonical layout, in 8-row x 16-byte core matrices.  K-adjacent core
 // matrices are 128 B apart (leading byte offset), 8-row groups 512 B apart (stride byte
 // offset).
@@ -79,101 +75,145 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t parity
   return false;
 }
 
+// element offset of level l of column c within an (Np, Ne) field, from the column's base index
+__device__ __forceinline__ size_t col_base(const ColMap& cm, int c) {
+  const int ij = c & ((1 << (2 * cm.lgN1)) - 1), exy = c >> (2 * cm.lgN1);
+  return (size_t)exy * cm.Np + (ij & (cm.N1 - 1)) + cm.N1 * (ij >> cm.lgN1);
+}
+__device__ __forceinline__ size_t col_off(const ColMap& cm, int l) {
+  return (size_t)(l >> cm.lgN1) * ((size_t)cm.NeX * cm.NeY * cm.Np) + (size_t)((l & (cm.N1 - 1)) << (2 * cm.lgN1));
+}
+
 template <int BN, bool GATHER, int OMODE, bool GELU>
 __global__ void __launch_bounds__(128) k_gemm_tc(const bf16* __restrict__ A, const bf16* __restrict__ W,
                                                  const float* __restrict__ bias, void* __restrict__ out, int M, int Np,
                                                  int Kp, const ColIO io, int* err) {
-  constexpr int TM = 128, TK = 32;
+  constexpr int TM = 128, TK = 32, NA = TM * (TK / 8) / 128, NB = BN * (TK / 8) / 128;
   constexpr uint32_t TCOLS = BN <= 32 ? 32 : (BN <= 64 ? 64 : (BN <= 128 ? 128 : 256));
-  static_assert(BN % 16 == 0 && BN <= 256, "tcgen05 M=128 needs N % 16 == 0, N <= 256");
-  __shared__ __align__(1024) bf16 sA[TM * TK];
-  __shared__ __align__(1024) bf16 sB[BN * TK];
-  __shared__ __align__(8) uint64_t mbar;
-  __shared__ uint32_t tmem_slot;
+  static_assert(BN % 32 == 0 && BN <= 256, "tcgen05 M=128 tile: N % 32 == 0 (16 for the MMA), N <= 256");
+  extern __shared__ __align__(1024) unsigned char gsm[];
+  bf16* sA = reinterpret_cast<bf16*>(gsm);                // [2][TM*TK]
+  bf16* sB = sA + 2 * TM * TK;                            // [2][BN*TK]
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(sB + 2 * BN * TK);  // [2]
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 2);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int m0 = blockIdx.x * TM, n0 = blockIdx.y * BN;
-  const uint32_t mb = smem_u32(&mbar);
   if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_slot)),
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
                  "r"(TCOLS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
   }
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mb) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(mbar)) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(mbar + 1)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-  const uint32_t tmem = tmem_slot;
+  const uint32_t tmem = *tmem_slot;
   // instruction descriptor: D f32, A/B bf16, both K-major, N/8, M/16
   const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
-  uint32_t parity = 0;
-  bool ok = true;
-  for (int k0 = 0; k0 < Kp && ok; k0 += TK) {
-    for (int i = tid; i < TM * (TK / 8); i += 128) {  // A rows: 16-byte chunks to core-matrix slots
-      const int r = i >> 2, kc = i & 3;
+
+  // one K chunk of this thread's A and B pieces in registers: prefetched while the previous
+  // chunk's MMAs run
+  uint4 ra[NA], rb[NB];
+  auto load_chunk = [&](int k0) {
+#pragma unroll
+    for (int q = 0; q < NA; ++q) {
+      const int i = tid + 128 * q, r = i >> 2, kc = i & 3;
       uint4 v = make_uint4(0, 0, 0, 0);
       if (m0 + r < M) {
         if constexpr (GATHER) {  // features of column m0 + r straight from the q* fields
           const int L = io.cm.L;
+          const size_t cb = col_base(io.cm, m0 + r);
+          int f = k0 + kc * 8;
+          int vv = f / L, l = f - vv * L;
           __align__(16) bf16 x8[8];
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
-            const int f = k0 + kc * 8 + j;
             float x = 0.f;
-            if (f < 3 * L) {
-              const int vv = f / L, l = f - vv * L;
-              const size_t g = col_gidx(io.cm, m0 + r, l);
+            if (vv < 3) {
+              const size_t g = cb + col_off(io.cm, l);
               x = vv == 0 ? __ldg(io.qd + g).x * io.s0 : (vv == 1 ? __ldg(io.qm + g).x * io.s1 : __ldg(io.qr + g).x * io.s2);
-            } else if (f == 3 * L) {
+            } else if (vv == 3 && l == 0) {
               x = io.fac;
             }
             x8[j] = __float2bfloat16_rn(x);
+            if (++l == L) { l = 0; ++vv; }
           }
           v = *reinterpret_cast<const uint4*>(x8);
         } else {
           v = *reinterpret_cast<const uint4*>(A + (size_t)(m0 + r) * Kp + k0 + kc * 8);
         }
       }
-      *reinterpret_cast<uint4*>(sA + ((r >> 3) * 4 + kc) * 64 + (r & 7) * 8) = v;
+      ra[q] = v;
     }
-    for (int i = tid; i < BN * (TK / 8); i += 128) {
-      const int r = i >> 2, kc = i & 3;
-      const uint4 v = *reinterpret_cast<const uint4*>(W + (size_t)(n0 + r) * Kp + k0 + kc * 8);
-      *reinterpret_cast<uint4*>(sB + ((r >> 3) * 4 + kc) * 64 + (r & 7) * 8) = v;
+#pragma unroll
+    for (int q = 0; q < NB; ++q) {
+      const int i = tid + 128 * q, r = i >> 2, kc = i & 3;
+      rb[q] = *reinterpret_cast<const uint4*>(W + (size_t)(n0 + r) * Kp + k0 + kc * 8);
     }
+  };
+  auto store_chunk = [&](int buf) {  // 16-byte pieces to their core-matrix slots
+#pragma unroll
+    for (int q = 0; q < NA; ++q) {
+      const int i = tid + 128 * q, r = i >> 2, kc = i & 3;
+      *reinterpret_cast<uint4*>(sA + buf * TM * TK + ((r >> 3) * 4 + kc) * 64 + (r & 7) * 8) = ra[q];
+    }
+#pragma unroll
+    for (int q = 0; q < NB; ++q) {
+      const int i = tid + 128 * q, r = i >> 2, kc = i & 3;
+      *reinterpret_cast<uint4*>(sB + buf * BN * TK + ((r >> 3) * 4 + kc) * 64 + (r & 7) * 8) = rb[q];
+    }
+  };
+
+  const int nch = Kp / TK;
+  bool ok = true;
+  int last = -1;  // last chunk whose MMAs were committed
+  load_chunk(0);
+  for (int c = 0; c < nch; ++c) {
+    const int buf = c & 1;
+    if (c >= 2) {  // the MMAs of chunk c-2 must have read this buffer
+      const bool got = mbar_wait_bounded(smem_u32(mbar + buf), (uint32_t)(((c - 2) >> 1) & 1));
+      ok = __syncthreads_and(got) != 0;
+      if (!ok) break;
+    }
+    store_chunk(buf);
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // generic stores -> tensor-core reads
     __syncthreads();
     if (tid == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
 #pragma unroll
       for (int ks = 0; ks < TK / 16; ++ks) {
-        const uint64_t ad = umma_desc(smem_u32(sA) + ks * 256, 128, 512);
-        const uint64_t bd = umma_desc(smem_u32(sB) + ks * 256, 128, 512);
-        const uint32_t acc = (k0 > 0 || ks > 0) ? 1u : 0u;
+        const uint64_t ad = umma_desc(smem_u32(sA + buf * TM * TK) + ks * 256, 128, 512);
+        const uint64_t bd = umma_desc(smem_u32(sB + buf * BN * TK) + ks * 256, 128, 512);
+        const uint32_t acc = (c > 0 || ks > 0) ? 1u : 0u;
         asm volatile(
             "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
             " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
             "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
             : "memory");
       }
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mb)
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                       smem_u32(mbar + buf))
                    : "memory");
     }
-    // the MMAs must have read sA/sB before the next chunk overwrites them
-    const bool got = mbar_wait_bounded(mb, parity);
-    parity ^= 1u;
-    ok = __syncthreads_and(got) != 0;
+    last = c;
+    if (c + 1 < nch) load_chunk((c + 1) * TK);
   }
-  if (!ok) {  // give MMAs still in flight a second bounded wait before the accumulator is released
-    mbar_wait_bounded(mb, parity ^ 1u);
-    if (tid == 0) atomicExch(err, 1);
+  // the last commit arrives once every MMA before it has completed
+  if (last >= 0) {
+    const bool got = mbar_wait_bounded(smem_u32(mbar + (last & 1)), (uint32_t)((last >> 1) & 1));
+    ok = (__syncthreads_and(got) != 0) && ok;
   }
+  if (!ok && tid == 0) atomicExch(err, 1);
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   const int row = m0 + 32 * warp + lane;
   const uint32_t tl = tmem + ((uint32_t)(32 * warp) << 16);
+  size_t rbase = 0;
+  if constexpr (OMODE == 2) rbase = col_base(io.cm, row < M ? row : 0);
 #pragma unroll 1
   for (int c0 = 0; c0 < BN; c0 += 16) {
     uint32_t r[16];
@@ -185,29 +225,32 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const bf16* __restrict__ A, con
         : "memory");
     asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
     if (ok && row < M) {
+      if constexpr (OMODE == 2) {  // scatter: output feature -> (variable, level) of column `row`
+        const int L = io.cm.L;
+        int f = n0 + c0;
+        int vv = f / L, l = f - vv * L;
 #pragma unroll
-      for (int j = 0; j < 16; j += 2) {
-        const int col = n0 + c0 + j;
-        float v0 = __uint_as_float(r[j]) + bias[col], v1 = __uint_as_float(r[j + 1]) + bias[col + 1];
-        if (GELU) { v0 = gelu_f(v0); v1 = gelu_f(v1); }
-        if constexpr (OMODE == 0) {
-          *reinterpret_cast<__nv_bfloat162*>(reinterpret_cast<bf16*>(out) + (size_t)row * Np + col) =
-              __floats2bfloat162_rn(v0, v1);
-        } else if constexpr (OMODE == 1) {
-          *reinterpret_cast<float2*>(reinterpret_cast<float*>(out) + (size_t)row * Np + col) = make_float2(v0, v1);
-        } else {  // scatter: output feature -> (variable, level) of column `row`
-          const int L = io.cm.L;
+        for (int j = 0; j < 16; ++j) {
+          if (vv < 3) {
+            const float y = __uint_as_float(r[j]) + bias[n0 + c0 + j];
+            const size_t g = rbase + col_off(io.cm, l);
+            if (vv == 0) io.gd[g] = y * io.r0;
+            else if (vv == 1) io.gm[g] = y * io.r1;
+            else io.gr[g] = y * io.r2;
+          }
+          if (++l == L) { l = 0; ++vv; }
+        }
+      } else {
 #pragma unroll
-          for (int h = 0; h < 2; ++h) {
-            const int f = col + h;
-            if (f < 3 * L) {
-              const int vv = f / L, l = f - vv * L;
-              const size_t g = col_gidx(io.cm, row, l);
-              const float y = h ? v1 : v0;
-              if (vv == 0) io.gd[g] = y * io.r0;
-              else if (vv == 1) io.gm[g] = y * io.r1;
-              else io.gr[g] = y * io.r2;
-            }
+        for (int j = 0; j < 16; j += 2) {
+          const int col = n0 + c0 + j;
+          float v0 = __uint_as_float(r[j]) + bias[col], v1 = __uint_as_float(r[j + 1]) + bias[col + 1];
+          if (GELU) { v0 = gelu_f(v0); v1 = gelu_f(v1); }
+          if constexpr (OMODE == 0) {
+            *reinterpret_cast<__nv_bfloat162*>(reinterpret_cast<bf16*>(out) + (size_t)row * Np + col) =
+                __floats2bfloat162_rn(v0, v1);
+          } else {
+            *reinterpret_cast<float2*>(reinterpret_cast<float*>(out) + (size_t)row * Np + col) = make_float2(v0, v1);
           }
         }
       }
@@ -219,18 +262,22 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const bf16* __restrict__ A, con
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TCOLS) : "memory");
 }
 
+template <int BN, bool GATHER, int OMODE, bool GELU>
+static void launch_tc_n(const bf16* A, const bf16* W, const float* bias, void* out, int M, int Np, int Kp,
+                        const ColIO& io, int* err, cudaStream_t s) {
+  const size_t smem = 2 * sizeof(bf16) * (128 * 32 + BN * 32) + 2 * sizeof(uint64_t) + 16;
+  auto kfn = k_gemm_tc<BN, GATHER, OMODE, GELU>;
+  cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  kfn<<<dim3((unsigned)((M + 127) / 128), (unsigned)(Np / BN)), 128, smem, s>>>(A, W, bias, out, M, Np, Kp, io, err);
+}
+
 template <bool GATHER, int OMODE, bool GELU>
 static void launch_gemm_tc(const bf16* A, const bf16* W, const float* bias, void* out, int M, int Np, int Kp,
                            const ColIO& io, int* err, cudaStream_t s) {
-  const unsigned gm = (unsigned)((M + 127) / 128);
-  if (Np % 256 == 0)
-    k_gemm_tc<256, GATHER, OMODE, GELU><<<dim3(gm, Np / 256), 128, 0, s>>>(A, W, bias, out, M, Np, Kp, io, err);
-  else if (Np % 192 == 0)
-    k_gemm_tc<192, GATHER, OMODE, GELU><<<dim3(gm, Np / 192), 128, 0, s>>>(A, W, bias, out, M, Np, Kp, io, err);
-  else if (Np % 128 == 0)
-    k_gemm_tc<128, GATHER, OMODE, GELU><<<dim3(gm, Np / 128), 128, 0, s>>>(A, W, bias, out, M, Np, Kp, io, err);
-  else
-    k_gemm_tc<64, GATHER, OMODE, GELU><<<dim3(gm, Np / 64), 128, 0, s>>>(A, W, bias, out, M, Np, Kp, io, err);
+  if (Np % 256 == 0) launch_tc_n<256, GATHER, OMODE, GELU>(A, W, bias, out, M, Np, Kp, io, err, s);
+  else if (Np % 192 == 0) launch_tc_n<192, GATHER, OMODE, GELU>(A, W, bias, out, M, Np, Kp, io, err, s);
+  else if (Np % 128 == 0) launch_tc_n<128, GATHER, OMODE, GELU>(A, W, bias, out, M, Np, Kp, io, err, s);
+  else launch_tc_n<64, GATHER, OMODE, GELU>(A, W, bias, out, M, Np, Kp, io, err, s);
 }
 
 // Generic FP32 SIMT GEMM for training: C(m,n) (+)= sum_k A(m,k) B(k,n) (+ bias[n]),
@@ -625,7 +672,8 @@ int mlp_infer(MlpState* m, const fedg::Ops& op, const float2* qd, const float2* 
   int r = ensure_infer(m, (size_t)ncol);
   if (r) return r;
   ColIO io{};
-  io.cm = ColMap{op.N1, op.Np, op.NeX, op.NeY, op.L};
+  io.cm = ColMap{op.N1, op.Np, op.NeX, op.NeY, op.L, op.N1 == 8 ? 3 : (op.N1 == 4 ? 2 : (op.N1 == 2 ? 1 : 0))};
+  if ((1 << io.cm.lgN1) != op.N1) return (int)cudaErrorInvalidValue;
   io.qd = qd; io.qm = qm; io.qr = qr;
   io.s0 = m->in_scale[0]; io.s1 = m->in_scale[1]; io.s2 = m->in_scale[2];
   io.fac = (float)impl_fac * m->in_scale[3];
