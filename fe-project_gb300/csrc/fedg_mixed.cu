@@ -40,6 +40,9 @@ struct StageBufs {
   float* S3[5];         // stage-3 input accumulator
   float* SF[5];         // final-update accumulator
   const float* TI[5];   // implicit tendency of the stage (stages 2, 3)
+  __nv_bfloat16* X;     // stages 1, 2: feature rows of the column-guess network (NULL: none)
+  int xdinp;            // row length of X
+  float xs[3];          // feature scales of DDENS', MOMZ, DRHOT'
 };
 
 // PRES - PRES_hyd = PRES_hyd ((1 + DRHOT/THERM_hyd)^kappa - 1)   (nonhydro3d_common.F90:470-474)
@@ -259,26 +262,42 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
   // --- fused RK epilogue: the prognostic variables accumulate in float pairs (about 48 bits;
   // the FP64 state is split with integer instructions), the FP32 stage increments added exactly ---
   const float dtf = (float)cf.dt;
-  if (STAGE == 1) {
+  if (STAGE == 1 || STAGE == 2) {
+    float xq[3] = {0.f, 0.f, 0.f};  // q* of DDENS, MOMZ, DRHOT for the guess network's rows
     if (valid) {
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
         const f2 qn = f2_split(__ldg(B.qn[v] + g));
-        B.qi[v][g] = f2_pack(f2_add_f(qn, dtf * (float(cf.a21e) * tex[v] + float(cf.a21i) * tim[v])));
-        B.S3[v][g] = float(cf.a31e) * tex[v] + float(cf.a31i) * tim[v];
-        B.SF[v][g] = float(cf.b1) * (tex[v] + tim[v]);
+        f2 qs;
+        if (STAGE == 1) {
+          qs = f2_add_f(qn, dtf * (float(cf.a21e) * tex[v] + float(cf.a21i) * tim[v]));
+          B.S3[v][g] = float(cf.a31e) * tex[v] + float(cf.a31i) * tim[v];
+          B.SF[v][g] = float(cf.b1) * (tex[v] + tim[v]);
+        } else {
+          const float s3 = __ldg(B.S3[v] + g) + float(cf.a32e) * tex[v] + float(cf.a32i) * tim[v];
+          qs = f2_add_f(qn, dtf * s3);
+          B.SF[v][g] = __ldg(B.SF[v] + g) + float(cf.b2) * (tex[v] + tim[v]);
+        }
+        B.qi[v][g] = f2_pack(qs);
+        if (v == VD) xq[0] = qs.h;
+        if (v == VMZ) xq[1] = qs.h;
+        if (v == VRT) xq[2] = qs.h;
       }
     }
-    return;
-  }
-  if (STAGE == 2) {
-    if (valid) {
+    if (B.X) {
+      // the element's q* as feature rows of the guess network: stage the N1 levels of each
+      // (column, variable) in shared memory, then write them as one vector per row segment
+      __syncthreads();  // the element's shared arrays are no longer read
+      __nv_bfloat16* sx = reinterpret_cast<__nv_bfloat16*>(st);  // [NF][3][N1]
 #pragma unroll
-      for (int v = 0; v < 5; ++v) {
-        const f2 qn = f2_split(__ldg(B.qn[v] + g));
-        const float s3 = __ldg(B.S3[v] + g) + float(cf.a32e) * tex[v] + float(cf.a32i) * tim[v];
-        B.qi[v][g] = f2_pack(f2_add_f(qn, dtf * s3));
-        B.SF[v][g] = __ldg(B.SF[v] + g) + float(cf.b2) * (tex[v] + tim[v]);
+      for (int v = 0; v < 3; ++v) sx[((i + N1 * j) * 3 + v) * N1 + k] = __float2bfloat16_rn(xq[v] * B.xs[v]);
+      __syncthreads();
+      if (valid && p < 3 * NF) {
+        const int cij = p / 3, v = p - 3 * cij;
+        const size_t row = (size_t)(ex + op.NeX * ey) * NF + cij;
+        __nv_bfloat16* dst = B.X + row * B.xdinp + v * op.L + ez * N1;
+        if constexpr (N1 == 8) *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<const uint4*>(sx + (cij * 3 + v) * N1);
+        else *reinterpret_cast<uint2*>(dst) = *reinterpret_cast<const uint2*>(sx + (cij * 3 + v) * N1);
       }
     }
     return;
@@ -586,6 +605,15 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
       return (int)cudaErrorInvalidValue;
     });
   };
+  B.X = nullptr;
+  if (o->use_guess) {  // the stage kernels write the guess network's feature rows
+    MlpRows rows;
+    r = tracked(c, FEDG_K_MLP, [&] { return mlp_rows(c->guess, (int)c->ncol, impl_fac, &rows, c->stream); });
+    if (r) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): guess feature rows");
+    B.X = rows.X;
+    B.xdinp = rows.dinp;
+    for (int v = 0; v < 3; ++v) B.xs[v] = rows.s[v];
+  }
   auto vi = [&]() -> int {
     X5 qin{{m->qi(0), m->qi(1), m->qi(2), m->qi(3), m->qi(4)}};
     const ProfX px{m->prof2, m->prof2 + c->L, m->prof2 + 2 * c->L, m->prof2 + 3 * c->L,
@@ -595,7 +623,7 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
     const float* const* gptr = nullptr;
     if (o->use_guess) {
       const int rg = tracked(c, FEDG_K_MLP, [&] {
-        return mlp_infer(c->guess, c->op, m->qi(0), m->qi(3), m->qi(4), impl_fac, m->GU(0), m->GU(1), m->GU(2), c->stream);
+        return mlp_infer(c->guess, c->op, m->GU(0), m->GU(1), m->GU(2), c->stream);
       });
       if (rg) return rg;
       gptr = (const float* const*)(m->d_ptrs + 5);

@@ -30,15 +30,12 @@ struct ColMap {
   int N1, Np, NeX, NeY, L;
   int lgN1;  // log2(N1): N1 is a power of two
 };
-// column gather/scatter of the first and last inference layers: features (var-major) DDENS'(l),
-// MOMZ(l), DRHOT'(l) of the column's L levels, then impl_fac, each times its scale; outputs
-// (Q - q*)(l) per variable divided by its scale, written into (Np, Ne) fields
+// column scatter of the last inference layer: outputs (Q - q*)(l) per variable (var-major over the
+// column's L levels) divided by its scale, written into (Np, Ne) fields
 struct ColIO {
   ColMap cm;
-  const float2 *qd, *qm, *qr;  // stage input q* as float pairs
-  float s0, s1, s2, fac;       // input scales, scaled impl_fac
-  float *gd, *gm, *gr;         // guess fields
-  float r0, r1, r2;            // 1 / output scales
+  float *gd, *gm, *gr;  // guess fields
+  float r0, r1, r2;     // 1 / output scales
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -84,7 +81,7 @@ __device__ __forceinline__ size_t col_off(const ColMap& cm, int l) {
   return (size_t)(l >> cm.lgN1) * ((size_t)cm.NeX * cm.NeY * cm.Np) + (size_t)((l & (cm.N1 - 1)) << (2 * cm.lgN1));
 }
 
-template <int BN, bool GATHER, int OMODE, bool GELU>
+template <int BN, int OMODE, bool GELU>
 __global__ void __launch_bounds__(128) k_gemm_tc(const bf16* __restrict__ A, const bf16* __restrict__ W,
                                                  const float* __restrict__ bias, void* __restrict__ out, int M, int Np,
                                                  int Kp, const ColIO io, int* err) {
@@ -124,30 +121,7 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const bf16* __restrict__ A, con
     for (int q = 0; q < NA; ++q) {
       const int i = tid + 128 * q, r = i >> 2, kc = i & 3;
       uint4 v = make_uint4(0, 0, 0, 0);
-      if (m0 + r < M) {
-        if constexpr (GATHER) {  // features of column m0 + r straight from the q* fields
-          const int L = io.cm.L;
-          const size_t cb = col_base(io.cm, m0 + r);
-          int f = k0 + kc * 8;
-          int vv = f / L, l = f - vv * L;
-          __align__(16) bf16 x8[8];
-#pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            float x = 0.f;
-            if (vv < 3) {
-              const size_t g = cb + col_off(io.cm, l);
-              x = vv == 0 ? __ldg(io.qd + g).x * io.s0 : (vv == 1 ? __ldg(io.qm + g).x * io.s1 : __ldg(io.qr + g).x * io.s2);
-            } else if (vv == 3 && l == 0) {
-              x = io.fac;
-            }
-            x8[j] = __float2bfloat16_rn(x);
-            if (++l == L) { l = 0; ++vv; }
-          }
-          v = *reinterpret_cast<const uint4*>(x8);
-        } else {
-          v = *reinterpret_cast<const uint4*>(A + (size_t)(m0 + r) * Kp + k0 + kc * 8);
-        }
-      }
+      if (m0 + r < M) v = *reinterpret_cast<const uint4*>(A + (size_t)(m0 + r) * Kp + k0 + kc * 8);
       ra[q] = v;
     }
 #pragma unroll
@@ -262,22 +236,22 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const bf16* __restrict__ A, con
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TCOLS) : "memory");
 }
 
-template <int BN, bool GATHER, int OMODE, bool GELU>
+template <int BN, int OMODE, bool GELU>
 static void launch_tc_n(const bf16* A, const bf16* W, const float* bias, void* out, int M, int Np, int Kp,
                         const ColIO& io, int* err, cudaStream_t s) {
   const size_t smem = 2 * sizeof(bf16) * (128 * 32 + BN * 32) + 2 * sizeof(uint64_t) + 16;
-  auto kfn = k_gemm_tc<BN, GATHER, OMODE, GELU>;
+  auto kfn = k_gemm_tc<BN, OMODE, GELU>;
   cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   kfn<<<dim3((unsigned)((M + 127) / 128), (unsigned)(Np / BN)), 128, smem, s>>>(A, W, bias, out, M, Np, Kp, io, err);
 }
 
-template <bool GATHER, int OMODE, bool GELU>
+template <int OMODE, bool GELU>
 static void launch_gemm_tc(const bf16* A, const bf16* W, const float* bias, void* out, int M, int Np, int Kp,
                            const ColIO& io, int* err, cudaStream_t s) {
-  if (Np % 256 == 0) launch_tc_n<256, GATHER, OMODE, GELU>(A, W, bias, out, M, Np, Kp, io, err, s);
-  else if (Np % 192 == 0) launch_tc_n<192, GATHER, OMODE, GELU>(A, W, bias, out, M, Np, Kp, io, err, s);
-  else if (Np % 128 == 0) launch_tc_n<128, GATHER, OMODE, GELU>(A, W, bias, out, M, Np, Kp, io, err, s);
-  else launch_tc_n<64, GATHER, OMODE, GELU>(A, W, bias, out, M, Np, Kp, io, err, s);
+  if (Np % 256 == 0) launch_tc_n<256, OMODE, GELU>(A, W, bias, out, M, Np, Kp, io, err, s);
+  else if (Np % 192 == 0) launch_tc_n<192, OMODE, GELU>(A, W, bias, out, M, Np, Kp, io, err, s);
+  else if (Np % 128 == 0) launch_tc_n<128, OMODE, GELU>(A, W, bias, out, M, Np, Kp, io, err, s);
+  else launch_tc_n<64, OMODE, GELU>(A, W, bias, out, M, Np, Kp, io, err, s);
 }
 
 // Generic FP32 SIMT GEMM for training: C(m,n) (+)= sum_k A(m,k) B(k,n) (+ bias[n]),
@@ -633,15 +607,36 @@ static int ensure_infer(MlpState* m, size_t n) {
   return 0;
 }
 
-// the three layers on the tensor cores; with io.cm.L > 0 the first layer gathers its input rows
-// from the q* fields and the last scatters its outputs to the guess fields
+// the three layers on the tensor cores over the feature rows in m->Xh; with io the last layer
+// scatters its outputs to the guess fields, otherwise it writes FP32 rows to m->Yf
 static int run_layers(MlpState* m, int n, const ColIO* io, cudaStream_t s) {
   const ColIO none{};
-  if (io) launch_gemm_tc<true, 0, true>(nullptr, m->Wh + m->hW1, m->P + m->ob1, m->H1, n, m->hp, m->dinp, *io, m->err, s);
-  else launch_gemm_tc<false, 0, true>(m->Xh, m->Wh + m->hW1, m->P + m->ob1, m->H1, n, m->hp, m->dinp, none, m->err, s);
-  launch_gemm_tc<false, 0, true>(m->H1, m->Wh + m->hW2, m->P + m->ob2, m->H2, n, m->hp, m->hp, none, m->err, s);
-  if (io) launch_gemm_tc<false, 2, false>(m->H2, m->Wh + m->hW3, m->P + m->ob3, nullptr, n, m->doutp, m->hp, *io, m->err, s);
-  else launch_gemm_tc<false, 1, false>(m->H2, m->Wh + m->hW3, m->P + m->ob3, m->Yf, n, m->doutp, m->hp, none, m->err, s);
+  launch_gemm_tc<0, true>(m->Xh, m->Wh + m->hW1, m->P + m->ob1, m->H1, n, m->hp, m->dinp, none, m->err, s);
+  launch_gemm_tc<0, true>(m->H1, m->Wh + m->hW2, m->P + m->ob2, m->H2, n, m->hp, m->hp, none, m->err, s);
+  if (io) launch_gemm_tc<2, false>(m->H2, m->Wh + m->hW3, m->P + m->ob3, nullptr, n, m->doutp, m->hp, *io, m->err, s);
+  else launch_gemm_tc<1, false>(m->H2, m->Wh + m->hW3, m->P + m->ob3, m->Yf, n, m->doutp, m->hp, none, m->err, s);
+  return (int)cudaGetLastError();
+}
+
+// impl_fac feature (times its scale) and zero padding of every feature row
+__global__ void k_rows_tail(bf16* __restrict__ X, int dinp, int f0, float fac, int ncol) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int w = dinp - f0;
+  if (i >= (size_t)ncol * w) return;
+  const int r = (int)(i / w), f = f0 + (int)(i % w);
+  X[(size_t)r * dinp + f] = __float2bfloat16_rn(f == f0 ? fac : 0.f);
+}
+
+int mlp_rows(MlpState* m, int ncol, double impl_fac, MlpRows* out, cudaStream_t s) {
+  if (!m || !m->ready) return (int)cudaErrorNotReady;
+  int r = ensure_infer(m, (size_t)ncol);
+  if (r) return r;
+  k_rows_tail<<<nblk((size_t)ncol * (m->dinp - 3 * m->L), 256), 256, 0, s>>>(m->Xh, m->dinp, 3 * m->L,
+                                                                             (float)impl_fac * m->in_scale[3], ncol);
+  out->X = m->Xh;
+  out->dinp = m->dinp;
+  out->L = m->L;
+  for (int v = 0; v < 3; ++v) out->s[v] = m->in_scale[v];
   return (int)cudaGetLastError();
 }
 
@@ -664,21 +659,15 @@ int mlp_predict(MlpState* m, const float* X, float* Y, int n, cudaStream_t s) {
   return mlp_take_error(m, s) ? (int)cudaErrorLaunchTimeout : 0;
 }
 
-int mlp_infer(MlpState* m, const fedg::Ops& op, const float2* qd, const float2* qm, const float2* qr, double impl_fac,
-              float* gd, float* gm, float* gr, cudaStream_t s) {
+int mlp_infer(MlpState* m, const fedg::Ops& op, float* gd, float* gm, float* gr, cudaStream_t s) {
   if (!m || !m->ready) return (int)cudaErrorNotReady;
   if (m->L != op.L) return (int)cudaErrorInvalidValue;
   const int ncol = op.NeX * op.NeY * op.N1 * op.N1;
-  int r = ensure_infer(m, (size_t)ncol);
-  if (r) return r;
+  if ((size_t)ncol > m->icap) return (int)cudaErrorInvalidValue;  // mlp_rows prepares the rows first
   ColIO io{};
   io.cm = ColMap{op.N1, op.Np, op.NeX, op.NeY, op.L, op.N1 == 8 ? 3 : (op.N1 == 4 ? 2 : (op.N1 == 2 ? 1 : 0))};
   if ((1 << io.cm.lgN1) != op.N1) return (int)cudaErrorInvalidValue;
-  io.qd = qd; io.qm = qm; io.qr = qr;
-  io.s0 = m->in_scale[0]; io.s1 = m->in_scale[1]; io.s2 = m->in_scale[2];
-  io.fac = (float)impl_fac * m->in_scale[3];
   io.gd = gd; io.gm = gm; io.gr = gr;
   io.r0 = 1.f / m->out_scale[0]; io.r1 = 1.f / m->out_scale[1]; io.r2 = 1.f / m->out_scale[2];
-  if ((r = run_layers(m, ncol, &io, s))) return r;
-  return (int)cudaGetLastError();
+  return run_layers(m, ncol, &io, s);
 }

@@ -10,10 +10,18 @@
 struct MlpState;
 void mlp_free(MlpState* m);
 bool mlp_ready(const MlpState* m);
-// Guess of Q - q* for every column from the stage input q* (DDENS, MOMZ, DRHOT fields, FP64) and
-// impl_fac; writes three FP32 (Np, Ne) fields.  Runs the three GEMMs on the tensor cores.
-int mlp_infer(MlpState* m, const fedg::Ops& op, const float2* qd, const float2* qm, const float2* qr, double impl_fac,
-              float* gd, float* gm, float* gr, cudaStream_t s);
+// Feature rows of the guess network, written by the producer of the stage input q* (the stage
+// kernels): row c (column c) holds DDENS'(l) s[0], MOMZ(l) s[1], DRHOT'(l) s[2] at
+// X[c*dinp + v*L + l] (bf16), followed by impl_fac and zero padding, which mlp_rows fills.
+struct MlpRows {
+  __nv_bfloat16* X;
+  int dinp, L;
+  float s[3];
+};
+int mlp_rows(MlpState* m, int ncol, double impl_fac, MlpRows* out, cudaStream_t s);
+// Guess of Q - q* for every column from the rows prepared by mlp_rows and the producer: three
+// GEMMs on the tensor cores, the last scattering into three FP32 (Np, Ne) fields.
+int mlp_infer(MlpState* m, const fedg::Ops& op, float* gd, float* gm, float* gr, cudaStream_t s);
 
 // 0, or -1 if a tensor-core GEMM of this network gave up waiting on its barrier since the last
 // call (synchronises the stream; clears the flag)
