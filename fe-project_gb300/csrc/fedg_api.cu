@@ -589,7 +589,7 @@ int fedg_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_o
   if (!c->base_set) return fail("fedg_update: base state not set");
   if (o->eqs != FEDG_HEVE && o->eqs != FEDG_HEVI) return fail("fedg_update: bad eqs");
   CK(cudaSetDevice(c->d.device));
-  if (o->prec == FEDG_PREC_MIXED) return mixed_update(c, q, nsteps, o, iters_out);
+  if (o->prec == FEDG_PREC_MIXED || o->prec == FEDG_PREC_PAIR) return mixed_update(c, q, nsteps, o, iters_out);
   if (o->prec != FEDG_PREC_FP64) return fail("fedg_update: bad prec");
   const int scheme = o->eqs == FEDG_HEVE ? FEDG_SSP_RK3 : FEDG_IMEX_ARK232;
   int r = 0;

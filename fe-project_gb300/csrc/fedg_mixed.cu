@@ -433,6 +433,11 @@ struct MixedState {
   float2* prof2 = nullptr;  // [4][L] float pairs DENS_hyd, PRES_hyd, RHOT_hyd, 1/RHOT_hyd
   float** d_ptrs = nullptr; // device arrays of float pointers: TI[5], guess[3], QSF[5]
   float* gsc = nullptr;     // block-Thomas history of the column solve
+  // float-pair mode (FEDG_PREC_PAIR), allocated on first use: S3 | SF | TI | QSF | QNF as pairs
+  float2* pbuf = nullptr;
+  void** d_pptrs = nullptr;  // device arrays of pointers: TI[5], QSF[5] (pairs)
+  float2* prof5 = nullptr;   // [5][L] DENS_hyd, PRES_hyd, THERM_hyd, 1/THERM_hyd, THERM_hyd/DENS_hyd
+  OpsP opp;
   OpsF opf;
   OpsX opx;
   double Uref = 0.0, Vref = 0.0;
@@ -444,6 +449,11 @@ struct MixedState {
   float* GU(int v) { return fbuf + (size_t)(15 + v) * n; }
   float* QSF(int v) { return fbuf + (size_t)(18 + v) * n; }
   float* QNF(int v) { return fbuf + (size_t)(23 + v) * n; }
+  float2* S3p(int v) { return pbuf + (size_t)v * n; }
+  float2* SFp(int v) { return pbuf + (size_t)(5 + v) * n; }
+  float2* TIp(int v) { return pbuf + (size_t)(10 + v) * n; }
+  float2* QSFp(int v) { return pbuf + (size_t)(15 + v) * n; }
+  float2* QNFp(int v) { return pbuf + (size_t)(20 + v) * n; }
 };
 
 static float2 split_host(double x) {
@@ -459,6 +469,9 @@ void mixed_free(MixedState* m) {
   cudaFree(m->prof2);
   cudaFree(m->d_ptrs);
   cudaFree(m->gsc);
+  cudaFree(m->pbuf);
+  cudaFree(m->d_pptrs);
+  cudaFree(m->prof5);
   delete m;
 }
 
@@ -537,12 +550,78 @@ static int mixed_setup(fedg_ctx* c) {
   return 0;
 }
 
+// float-pair deviation copy of a state (DDENS, MOMX - DENS_hyd*Uref, MOMY - DENS_hyd*Vref, MOMZ, DRHOT)
+struct Dev5p { float2* v[5]; };
+__global__ void k_to_dev2(F5c q, Dev5p out, const double* __restrict__ dens_prof, float2 U, float2 V, int Np, int N1,
+                          size_t nxy, size_t n) {
+  const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n) return;
+  const size_t ke = g / Np;
+  const int ez = (int)(ke / nxy), k = (int)(g - ke * Np) / (N1 * N1);
+  const f2 dh = f2_split(dens_prof[ez * N1 + k]);
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    f2 x = f2_split(q.v[v][g]);
+    if (v == VMX) x = f2_sub(x, f2_mul(dh, f2_of(U)));
+    if (v == VMY) x = f2_sub(x, f2_mul(dh, f2_of(V)));
+    out.v[v][g] = f2_pack(x);
+  }
+}
+
+static int pair_setup(fedg_ctx* c, MixedState* m) {
+  if (m->pbuf) return 0;
+  const int L = c->L;
+  cudaError_t e;
+  if ((e = cudaMalloc(&m->pbuf, sizeof(float2) * 25 * c->n)) != cudaSuccess ||
+      (e = cudaMalloc(&m->d_pptrs, sizeof(void*) * 10)) != cudaSuccess ||
+      (e = cudaMalloc(&m->prof5, sizeof(float2) * 5 * L)) != cudaSuccess) {
+    cudaFree(m->pbuf); cudaFree(m->d_pptrs); cudaFree(m->prof5);
+    m->pbuf = nullptr; m->d_pptrs = nullptr; m->prof5 = nullptr;
+    return api_cuda_fail(e, "fedg_update(pair): allocation");
+  }
+  const Ops& o = c->op;
+  OpsP& x = m->opp;
+  std::memset(&x, 0, sizeof(x));
+  for (int k = 0; k < FEDG_MAXN1 * FEDG_MAXN1; ++k) {
+    x.D[k] = split_host(o.D[k]); x.T[k] = split_host(o.T[k]);
+    x.F[k] = split_host(o.F[k]); x.Fv[k] = split_host(o.Fv[k]);
+  }
+  for (int k = 0; k < FEDG_MAXN1; ++k) { x.Lb[k] = split_host(o.Lb[k]); x.Lt[k] = split_host(o.Lt[k]); }
+  x.E11 = split_host(o.E11); x.E22 = split_host(o.E22); x.E33 = split_host(o.E33);
+  x.FSx = split_host(o.FSx); x.FSy = split_host(o.FSy); x.FSz = split_host(o.FSz);
+  x.grav = split_host(o.grav); x.kap = split_host(o.kap); x.cor = split_host(o.coriolis_f);
+  x.kap64 = o.kap;
+  x.rmax = m->opx.rmax;
+  for (int n = 0; n < 12; ++n) x.cb[n] = m->opx.cb[n];
+  x.NeX = o.NeX; x.NeY = o.NeY; x.NeZ = o.NeZ; x.N1 = o.N1; x.Np = o.Np; x.L = o.L;
+  std::vector<double> hp(4 * L);
+  e = cudaMemcpy(hp.data(), c->d_prof, sizeof(double) * 4 * L, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return api_cuda_fail(e, "fedg_update(pair): profile copy");
+  std::vector<float2> p5(5 * L);
+  for (int l = 0; l < L; ++l) {
+    p5[l] = split_host(hp[l]);
+    p5[L + l] = split_host(hp[L + l]);
+    p5[2 * L + l] = split_host(hp[2 * L + l]);
+    p5[3 * L + l] = split_host(1.0 / hp[2 * L + l]);
+    p5[4 * L + l] = split_host(hp[2 * L + l] / hp[l]);
+  }
+  void* hptr[10];
+  for (int v = 0; v < 5; ++v) hptr[v] = m->TIp(v);
+  for (int v = 0; v < 5; ++v) hptr[5 + v] = m->QSFp(v);
+  if ((e = cudaMemcpy(m->prof5, p5.data(), sizeof(float2) * 5 * L, cudaMemcpyHostToDevice)) != cudaSuccess ||
+      (e = cudaMemcpy(m->d_pptrs, hptr, sizeof(void*) * 10, cudaMemcpyHostToDevice)) != cudaSuccess)
+    return api_cuda_fail(e, "fedg_update(pair): upload");
+  return 0;
+}
+
 int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_opts* o, double* iters_out) {
   if (o->eqs != FEDG_HEVI) return api_fail("fedg_update: the mixed-precision path implements HEVI (IMEX ARK232)");
   if (o->max_iter < 1) return api_fail("fedg_update: max_iter must be >= 1");
   int r = mixed_setup(c);
   if (r) return r;
   MixedState* m = c->mixed;
+  const bool pair = o->prec == FEDG_PREC_PAIR;
+  if (pair && (r = pair_setup(c, m))) return r;
   if (o->use_guess && !mlp_ready(c->guess)) return api_fail("fedg_update: use_guess set but no trained column-guess network is loaded (fedg_guess_load)");
   const double alp = (3.0 + 2.0 * std::sqrt(2.0)) / 6.0, gam = 1.0 - 1.0 / std::sqrt(2.0), del = 1.0 / (2.0 * std::sqrt(2.0));
   MixCoef cf{o->dt, 2.0 * gam, gam, 1.0 - alp, del, alp, del, del, del, gam, 0.0, 0.0, {0.f, 0.f}, {0.f, 0.f}};
@@ -581,9 +660,34 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
   cf.Vref = m->Vref;
   cf.Uref2 = m->opx.Uref;
   cf.Vref2 = m->opx.Vref;
+  m->opp.Uref = m->opx.Uref;
+  m->opp.Vref = m->opx.Vref;
   const double impl_fac = gam * o->dt;
-  MixViArgs va{impl_fac, 1.0 / impl_fac, o->tol, 340.0, split_host(impl_fac), o->max_iter, 1};
-  {  // FP32 deviation copy of the incoming state for the first stage-1 tendency
+  MixViArgs va{impl_fac, 1.0 / impl_fac, o->tol, 340.0, split_host(impl_fac), split_host(1.0 / impl_fac), o->max_iter, 1};
+  const PairCoef pc{split_host(o->dt), split_host(2.0 * gam), split_host(gam), split_host(1.0 - alp), split_host(del),
+                    split_host(alp), split_host(del), split_host(del), split_host(del), split_host(gam)};
+  const ProfP pfp{m->prof5, m->prof5 + c->L, m->prof5 + 2 * c->L, m->prof5 + 3 * c->L, m->prof5 + 4 * c->L,
+                  m->prof + c->L};
+  StagePairBufs BP;
+  std::memset(&BP, 0, sizeof(BP));
+  if (pair) {
+    for (int v = 0; v < 5; ++v) {
+      BP.qn[v] = q[v];
+      BP.qnf[v] = m->QNFp(v);
+      BP.qi[v] = m->qi(v);
+      BP.S3[v] = m->S3p(v);
+      BP.SF[v] = m->SFp(v);
+      BP.TI[v] = m->TIp(v);
+    }
+    F5c qc{{q[0], q[1], q[2], q[3], q[4]}};
+    Dev5p dv{{m->QNFp(0), m->QNFp(1), m->QNFp(2), m->QNFp(3), m->QNFp(4)}};
+    r = tracked(c, FEDG_K_AUX, [&] {
+      k_to_dev2<<<(unsigned)((c->n + 255) / 256), 256, 0, c->stream>>>(qc, dv, c->d_prof, m->opx.Uref, m->opx.Vref,
+                                                                      c->Np, c->N1, c->nxy, c->n);
+      return (int)cudaGetLastError();
+    });
+    if (r) return api_cuda_fail((cudaError_t)r, "fedg_update(pair): deviation copy");
+  } else {  // FP32 deviation copy of the incoming state for the first stage-1 tendency
     F5c qc{{q[0], q[1], q[2], q[3], q[4]}};
     Dev5 dv{{m->QNF(0), m->QNF(1), m->QNF(2), m->QNF(3), m->QNF(4)}};
     r = tracked(c, FEDG_K_AUX, [&] {
@@ -598,6 +702,7 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
   const int filt = c->d.mf_on;
   auto stage = [&](int s) -> int {
     return tracked(c, FEDG_K_MTEND, [&] {
+      if (pair) return launch_stage_pair(c->N1, s, m->opp, pfp, c->d_prof, BP, pc, c->Ne, filt, c->stream);
       switch (c->N1) {
         case 4: return launch_stage_m<4>(s, m->opf, pff, c->d_prof, B, cf, c->Ne, filt, c->stream);
         case 8: return launch_stage_m<8>(s, m->opf, pff, c->d_prof, B, cf, c->Ne, filt, c->stream);
@@ -610,16 +715,17 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
     MlpRows rows;
     r = tracked(c, FEDG_K_MLP, [&] { return mlp_rows(c->guess, (int)c->ncol, impl_fac, &rows, c->stream); });
     if (r) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): guess feature rows");
-    B.X = rows.X;
-    B.xdinp = rows.dinp;
-    for (int v = 0; v < 3; ++v) B.xs[v] = rows.s[v];
+    B.X = BP.X = rows.X;
+    B.xdinp = BP.xdinp = rows.dinp;
+    for (int v = 0; v < 3; ++v) B.xs[v] = BP.xs[v] = rows.s[v];
   }
   auto vi = [&]() -> int {
     X5 qin{{m->qi(0), m->qi(1), m->qi(2), m->qi(3), m->qi(4)}};
     const ProfX px{m->prof2, m->prof2 + c->L, m->prof2 + 2 * c->L, m->prof2 + 3 * c->L,
                    m->prof, m->prof + c->L, m->prof + 2 * c->L, m->prof + 3 * c->L};
     F5c z{{q[0], q[1], q[2], q[3], q[4]}};
-    float* const* qo = m->d_ptrs + 8;
+    void* const* qo = pair ? m->d_pptrs + 5 : reinterpret_cast<void* const*>(m->d_ptrs + 8);
+    void* const* to = pair ? m->d_pptrs : reinterpret_cast<void* const*>(m->d_ptrs);
     const float* const* gptr = nullptr;
     if (o->use_guess) {
       const int rg = tracked(c, FEDG_K_MLP, [&] {
@@ -629,15 +735,21 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
       gptr = (const float* const*)(m->d_ptrs + 5);
     }
     return tracked(c, FEDG_K_MVI, [&] {
-      return launch_vi_cols(c->N1, c->op, m->opx, px, qin, z, gptr, qo, m->d_ptrs, m->gsc, c->d_status, c->d_cnt, va,
+      return launch_vi_cols(c->N1, c->op, m->opx, px, qin, z, gptr, qo, to, m->gsc, c->d_status, c->d_cnt, va, pair,
                             c->stream);
     });
   };
   for (int step = 0; step < nsteps; ++step) {
-    for (int v = 0; v < 5; ++v) B.qsf[v] = m->QNF(v);
+    for (int v = 0; v < 5; ++v) {
+      B.qsf[v] = m->QNF(v);
+      BP.qs[v] = pair ? m->QNFp(v) : nullptr;
+    }
     if ((r = stage(1))) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): stage 1");
     if ((r = vi())) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): column solve 2");
-    for (int v = 0; v < 5; ++v) B.qsf[v] = m->QSF(v);
+    for (int v = 0; v < 5; ++v) {
+      B.qsf[v] = m->QSF(v);
+      BP.qs[v] = pair ? m->QSFp(v) : nullptr;
+    }
     if ((r = stage(2))) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): stage 2");
     if ((r = vi())) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): column solve 3");
     if ((r = stage(3))) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): stage 3");

@@ -3,6 +3,7 @@
 #include "../../include/fedg.h"
 #include "fedg_common.cuh"
 #include "fedg_kernels.cuh"
+#include <cuda_bf16.h>
 
 namespace fedg {
 
@@ -53,10 +54,45 @@ struct X5 {
 // controls of the mixed-precision column solve
 struct MixViArgs {
   double impl_fac, inv_impl_fac, tol, cref;
-  float2 impl2;  // impl_fac as a float pair
+  float2 impl2;     // impl_fac as a float pair
+  float2 inv_impl2; // 1/impl_fac as a float pair
   int max_iter;
   int check64;  // 1: convergence judged by the float-pair residual; 0: by the split residual
 };
+
+// ---- float-pair precision mode (FEDG_PREC_PAIR, fedg_pair.cu) ----
+struct OpsP {
+  float2 D[FEDG_MAXN1 * FEDG_MAXN1], T[FEDG_MAXN1 * FEDG_MAXN1];
+  float2 F[FEDG_MAXN1 * FEDG_MAXN1], Fv[FEDG_MAXN1 * FEDG_MAXN1];
+  float2 Lb[FEDG_MAXN1], Lt[FEDG_MAXN1];
+  float2 E11, E22, E33, FSx, FSy, FSz, grav, kap, cor, Uref, Vref;
+  float cb[12];
+  float rmax;
+  double kap64;
+  int NeX, NeY, NeZ, N1, Np, L;
+};
+// base-state profiles for the pair stage kernels, [L] each
+struct ProfP {
+  const float2 *dh, *ph, *th, *rth, *ptr;  // DENS_hyd, PRES_hyd, THERM_hyd, 1/THERM_hyd, THERM_hyd/DENS_hyd
+  const float* phf;                         // PRES_hyd in FP32 (wave speed)
+};
+struct PairCoef {
+  float2 dt, a21e, a21i, a31e, a31i, a32e, a32i, b1, b2, b3;
+};
+struct StagePairBufs {
+  const float2* qs[5];  // deviation state of the explicit tendency (q^n at stage 1, Q_s after)
+  float2* qnf[5];       // stage 3: deviation copy of q^{n+1}
+  double* qn[5];        // q^n; stage 3 overwrites it with q^{n+1}
+  float2* qi[5];        // next stage input q*_{s+1}
+  float2* S3[5];        // stage-3 input accumulator
+  float2* SF[5];        // final-update accumulator
+  const float2* TI[5];  // implicit tendency of the stage (stages 2, 3)
+  __nv_bfloat16* X;     // stages 1, 2: feature rows of the column-guess network (NULL: none)
+  int xdinp;
+  float xs[3];
+};
+int launch_stage_pair(int N1, int stage, const OpsP& op, const ProfP& pf, const double* dens64,
+                      const StagePairBufs& B, const PairCoef& cf, int Ne, int filt, cudaStream_t s);
 
 // Mixed-precision column solve (fedg_vicol.cu).  qin: stage input q* (float pairs); z: var0
 // (FP64; alph and the plain initial iterate); guess: FP32 increments of (DENS, MOMZ, RHOT) over
@@ -65,9 +101,10 @@ struct MixViArgs {
 // impl_fac in FP32; gsc: vi_cols_scratch_floats(n) floats of block-Thomas history; status[ncol]:
 // solves used, -1 not converged, -2 non-finite; cnt[3]: failed columns, solves, converged columns.
 size_t vi_cols_scratch_floats(size_t nodes);
+// pair_out: qsf and tout are float-pair (float2) arrays instead of FP32 ones
 int launch_vi_cols(int N1, const Ops& op, const OpsX& ox, const ProfX& px, const X5& qin, const F5c& z,
-                   const float* const* guess, float* const* qsf, float* const* tout, float* gsc, int* status,
-                   unsigned long long* cnt, const MixViArgs& a, cudaStream_t s);
+                   const float* const* guess, void* const* qsf, void* const* tout, float* gsc, int* status,
+                   unsigned long long* cnt, const MixViArgs& a, bool pair_out, cudaStream_t s);
 
 }  // namespace fedg
 

@@ -459,9 +459,9 @@ __device__ void col_solve(const Ops& op, const Col<N1>& c, double impl_fac, floa
 }
 
 // ---------------------------------------------------------------------------------------------
-template <int N1>
+template <int N1, bool PO>
 __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const OpsX ox, const ProfX px, const X5 qin, const F5c z,
-                                                const float* const* guess, float* const* qsf, float* const* tout,
+                                                const float* const* guess, void* const* qsf, void* const* tout,
                                                 float* __restrict__ gsc, int* status, unsigned long long* cnt,
                                                 const MixViArgs args, int ncol) {
   constexpr int N = N1 - 1, C = 32 / N1, NF = N1 * N1, Np = N1 * N1 * N1;
@@ -515,14 +515,15 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const OpsX ox, con
 
   // ---- MOMX/MOMY (eval_Ax_uv / solve_uv) ----
   // The operator is linear and acts on the face jumps only.  With P = P0 + D (P0 = var0, D an
-  // FP32 increment), b(P) = [impl_fac A(P0) + (q* - P0)] + impl_fac A(D) - D.  q* - P0 is kept as
-  // an FP32 pair hi + lo and the face jumps of P0 are formed in pairs, once per column;
-  // everything after that is FP32.
+  // increment kept as a float pair), b(P) = [impl_fac A(P0) + (q* - P0)] + impl_fac A(D) - D.
+  // q* - P0 is kept as a pair hi + lo and the face jumps of P0 are formed in pairs, once per
+  // column; the corrections are FP32 and accumulate into D in pairs, so repeated corrections
+  // refine D to pair accuracy.
   {
     float2* P0 = c.P;                                   // [2L] var0 pairs, only while the jumps are formed
     float* qh = reinterpret_cast<float*>(c.Jq);         // [2L] (q* - P0) hi
     float* ql = qh + 2 * L;                             // [2L] (q* - P0) lo
-    float* D = reinterpret_cast<float*>(c.P);           // [2L] increment, once P0 is dead
+    float2* D = reinterpret_cast<float2*>(c.P);         // [2L] increment (float pair), once P0 is dead
     float* j0 = reinterpret_cast<float*>(c.P) + 4 * L;  // [4 NeZ] face jumps of P0
     float* bu = c.Bf;                                   // [2L] residual
     for (int e = 0; e < NeZ; ++e) {
@@ -550,8 +551,8 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const OpsX ox, con
     __syncwarp();
     for (int e = 0; e < NeZ; ++e) {
       const int l = e * N1 + k;
-      D[2 * l] = 0.f;
-      D[2 * l + 1] = 0.f;
+      D[2 * l] = make_float2(0.f, 0.f);
+      D[2 * l + 1] = make_float2(0.f, 0.f);
     }
     __syncwarp();
     const float cfs = (float)(0.5 * args.impl_fac * op.FSz);
@@ -568,7 +569,7 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const OpsX ox, con
           const int lM = e * N1 + (s == 0 ? 0 : N);
           const bool lid = s == 0 ? (e == 0) : (e == NeZ - 1);
           const int lP = lid ? lM : (s == 0 ? lM - 1 : lM + 1);
-          jdel[t] = j0[4 * e + t] + (D[2 * lP + m] - D[2 * lM + m]);
+          jdel[t] = j0[4 * e + t] + (D[2 * lP + m].x - D[2 * lM + m].x);
         }
         __syncwarp();
         const int l = e * N1 + k;
@@ -577,7 +578,7 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const OpsX ox, con
 #pragma unroll
         for (int m = 0; m < 2; ++m) {
           const float Af = cfs * (aB * jdel[m] + aT * jdel[2 + m]);  // impl_fac * A(P)
-          const float b = ((qh[2 * l + m] - D[2 * l + m]) + ql[2 * l + m]) + Af;
+          const float b = ((qh[2 * l + m] - D[2 * l + m].x) + (ql[2 * l + m] - D[2 * l + m].y)) + Af;
           bu[2 * l + m] = b;
           err = fmaxf(err, fabsf(b) * iscu);
           if (!(fabsf(b) < 3.0e38f)) err = __int_as_float(0x7fc00000);
@@ -623,8 +624,8 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const OpsX ox, con
           const int l = e * N1 + k;
           const float beta = e > 0 ? cfs * lbk * c.alB(e) : 0.f;
           const float tau = e < NeZ - 1 ? cfs * ltk * c.alT(e) : 0.f;
-          D[2 * l] += bu[2 * l] - beta * Jx[e] + tau * Jx[e + 1];
-          D[2 * l + 1] += bu[2 * l + 1] - beta * Jy[e] + tau * Jy[e + 1];
+          D[2 * l] = f2_pack(f2_add_f(f2_of(D[2 * l]), bu[2 * l] - beta * Jx[e] + tau * Jx[e + 1]));
+          D[2 * l + 1] = f2_pack(f2_add_f(f2_of(D[2 * l + 1]), bu[2 * l + 1] - beta * Jy[e] + tau * Jy[e + 1]));
         }
       }
       active = need;
@@ -638,8 +639,16 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const OpsX ox, con
       for (int m = 0; m < 2; ++m) {
         const f2 ref = f2_mul(dh, f2_of(m == 0 ? ox.Uref : ox.Vref));
         const f2 p0 = f2_split(__ldg(z.v[VMX + m] + gi));
-        qsf[VMX + m][gi] = f2_to_f(f2_sub(p0, ref)) + D[2 * l + m];
-        tout[VMX + m][gi] = ((D[2 * l + m] - qh[2 * l + m]) - ql[2 * l + m]) * iif;
+        const f2 d = f2_of(D[2 * l + m]);
+        const f2 pdev = f2_add(f2_sub(p0, ref), d);
+        const f2 inc = f2_sub(d, f2{qh[2 * l + m], ql[2 * l + m]});  // P - q*
+        if constexpr (PO) {
+          static_cast<float2*>(qsf[VMX + m])[gi] = f2_pack(pdev);
+          static_cast<float2*>(tout[VMX + m])[gi] = f2_pack(f2_mul(inc, f2_of(args.inv_impl2)));
+        } else {
+          static_cast<float*>(qsf[VMX + m])[gi] = f2_to_f(pdev);
+          static_cast<float*>(tout[VMX + m])[gi] = f2_to_f(inc) * iif;
+        }
       }
     }
     __syncwarp();
@@ -680,8 +689,14 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const OpsX ox, con
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
       const f2 pnew = f2_of(c.P[3 * l + m]);
-      qsf[gv[m]][gi] = f2_to_f(pnew);
-      tout[gv[m]][gi] = f2_to_f(f2_sub(pnew, f2_of(__ldg(qin.v[gv[m]] + gi)))) * iif;
+      const f2 inc = f2_sub(pnew, f2_of(__ldg(qin.v[gv[m]] + gi)));
+      if constexpr (PO) {
+        static_cast<float2*>(qsf[gv[m]])[gi] = f2_pack(pnew);
+        static_cast<float2*>(tout[gv[m]])[gi] = f2_pack(f2_mul(inc, f2_of(args.inv_impl2)));
+      } else {
+        static_cast<float*>(qsf[gv[m]])[gi] = f2_to_f(pnew);
+        static_cast<float*>(tout[gv[m]])[gi] = f2_to_f(inc) * iif;
+      }
     }
   }
   if (k == 0 && status) status[col] = st;
@@ -697,16 +712,16 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const OpsX ox, con
   }
 }
 
-template <int N1>
+template <int N1, bool PO>
 int launch_n(const Ops& op, const OpsX& ox, const ProfX& px, const X5& qin, const F5c& z, const float* const* guess,
-             float* const* qsf, float* const* tout, float* gsc, int* status, unsigned long long* cnt,
+             void* const* qsf, void* const* tout, float* gsc, int* status, unsigned long long* cnt,
              const MixViArgs& a, cudaStream_t s) {
   constexpr int C = 32 / N1;
   const ColLayout lay(N1, op.NeZ);
   const size_t smem = (size_t)lay.stride * C;
   if (smem > 227 * 1024) return (int)cudaErrorInvalidValue;
   const int ncol = op.NeX * op.NeY * N1 * N1;
-  auto kfn = k_vi_cols<N1>;
+  auto kfn = k_vi_cols<N1, PO>;
   cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   kfn<<<(ncol + C - 1) / C, 32, smem, s>>>(op, ox, px, qin, z, guess, qsf, tout, gsc, status, cnt, a, ncol);
   return (int)cudaGetLastError();
@@ -717,11 +732,13 @@ int launch_n(const Ops& op, const OpsX& ox, const ProfX& px, const X5& qin, cons
 size_t vi_cols_scratch_floats(size_t nodes) { return (size_t)12 * nodes; }
 
 int launch_vi_cols(int N1, const Ops& op, const OpsX& ox, const ProfX& px, const X5& qin, const F5c& z,
-                   const float* const* guess, float* const* qsf, float* const* tout, float* gsc, int* status,
-                   unsigned long long* cnt, const MixViArgs& a, cudaStream_t s) {
-  switch (N1) {
-    case 4: return launch_n<4>(op, ox, px, qin, z, guess, qsf, tout, gsc, status, cnt, a, s);
-    case 8: return launch_n<8>(op, ox, px, qin, z, guess, qsf, tout, gsc, status, cnt, a, s);
+                   const float* const* guess, void* const* qsf, void* const* tout, float* gsc, int* status,
+                   unsigned long long* cnt, const MixViArgs& a, bool pair_out, cudaStream_t s) {
+  switch (N1 * 2 + (pair_out ? 1 : 0)) {
+    case 8: return launch_n<4, false>(op, ox, px, qin, z, guess, qsf, tout, gsc, status, cnt, a, s);
+    case 9: return launch_n<4, true>(op, ox, px, qin, z, guess, qsf, tout, gsc, status, cnt, a, s);
+    case 16: return launch_n<8, false>(op, ox, px, qin, z, guess, qsf, tout, gsc, status, cnt, a, s);
+    case 17: return launch_n<8, true>(op, ox, px, qin, z, guess, qsf, tout, gsc, status, cnt, a, s);
   }
   return (int)cudaErrorInvalidValue;
 }

@@ -20,7 +20,7 @@ LIB_PATH = os.path.join(PKG_ROOT, "_build", "libfedg.so")
 
 HEVE, HEVI = 0, 1
 SSP_RK3, IMEX_ARK232 = 0, 1
-PREC_FP64, PREC_MIXED = 0, 1
+PREC_FP64, PREC_MIXED, PREC_PAIR = 0, 1, 2
 
 EXPORTED = [
     "fedg_last_error", "fedg_ctx_create", "fedg_ctx_destroy", "fedg_ctx_stream", "fedg_synchronize",

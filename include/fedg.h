@@ -56,7 +56,7 @@ typedef struct {
 enum { FEDG_HEVE = 0, FEDG_HEVI = 1 };
 enum { FEDG_SSP_RK3 = 0, FEDG_IMEX_ARK232 = 1 };
 /* precision of the fused update path (fedg_update) */
-enum { FEDG_PREC_FP64 = 0, FEDG_PREC_MIXED = 1 };
+enum { FEDG_PREC_FP64 = 0, FEDG_PREC_MIXED = 1, FEDG_PREC_PAIR = 2 };
 
 const char* fedg_last_error(void);
 
@@ -137,10 +137,16 @@ int fedg_tint_advance(fedg_tint* t, int stage, double* const q[5]);           /*
 /* AtmDynDGMDriver_nonhydro3d_update (driver_nonhydro3d.F90:614-963): nsteps full time steps
  * of q (5 device fields) with the fused GPU stage kernels.  eqs FEDG_HEVE uses SSP-RK3,
  * FEDG_HEVI uses IMEX ARK232 with the column Newton solve (max_iter, tol).
- * prec: FEDG_PREC_FP64, or FEDG_PREC_MIXED (FP32 explicit arithmetic on deviations from the
- * hydrostatic state with 3xTF32 tensor-core derivative contractions; FP64 pressure deviation,
- * Newton residual, linear solve and RK accumulation).  use_guess != 0 takes the initial
- * Newton iterate from the column-guess network loaded with fedg_guess_load.
+ * prec (HEVI only for the last two):
+ *   FEDG_PREC_FP64: FElib's arithmetic in FP64.
+ *   FEDG_PREC_MIXED: FP32 explicit arithmetic on deviations from the hydrostatic state and the
+ *     reference wind; the Newton iterate, its certifying residual and the RK accumulation in
+ *     float pairs (about 48 bits); FP32 Jacobian and LU.
+ *   FEDG_PREC_PAIR: as FEDG_PREC_MIXED with the explicit operator also in float pairs.
+ *     It is FP64-class end to end; use it with a Newton tol near 1e-13, so the FP32
+ *     corrections are refined to pair accuracy.
+ * use_guess != 0 takes the initial Newton iterate from the column-guess network loaded with
+ * fedg_guess_load.
  * iters_out (optional, host): mean Newton solves per implicit column solve. */
 typedef struct {
   int eqs, prec, max_iter, use_guess;
