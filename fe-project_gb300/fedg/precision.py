@@ -1,6 +1,6 @@
-"""One-hour precision run: the mixed-precision + learned-guess HEVI path against the plain FP64
-path, both on the GPU from the same initial state.  It reports the relative L2 error per variable
-at checkpoints.
+"""One-hour precision run: the learned-guess HEVI paths in the float-pair and FP32 precision modes
+against the plain FP64 path, all on the GPU from the same initial state.  It reports the relative
+L2 error per variable at checkpoints.
 
 Workload: the density current on the p = 7 mesh with 800 m elements. This is the recipe of the
 medium HEVI case run in the precision form:
@@ -11,24 +11,29 @@ medium HEVI case run in the precision form:
   - periodic in x and y, slip lids;
   - 8 vertical elements, i.e. 64-level columns.
 
-The default horizontal extent is 8 x 8 elements (6.4 km), so both paths finish an hour in a few
-GPU-minutes.  The time step is dt = 0.04 s. It is the stable step for this mesh: 0.08 s
+The default horizontal extent is 8 x 8 elements (6.4 km), so the four paths finish the hour in
+about half an hour of GPU time (almost all of it in the two FP64 paths).  The time step is dt = 0.04 s. It is the stable step for this mesh: 0.08 s
 diverges, and the 0.5 s of the original recipe exceeds the horizontal acoustic limit of p = 7
 elements of 800 m. One simulated hour is therefore 90,000 steps.
 
-Paths:
+Paths (all from the same initial state; the four HEVI paths at the same dt):
 
-  plain    FP64 fused update (FElib's algorithm), Newton to tol 1e-10 (max 20 solves).
-  learned  Mixed-precision fused update.  The Newton starts from the column-guess MLP and is
-           certified by the FP64 residual to the same tol.  The MLP follows the learned-guess
-           recipe:
-             - 193 -> 256 -> 256 -> 192;
-             - trained on the GPU on pairs the plain solver generates from 20 random
-               density-current seeds, on 4 x 4 x 8 slices of the same mesh.
+  plain_fp64_tol1e-13   FP64 fused update (FElib's algorithm), Newton to tol 1e-13: the
+                        implicit stages converged to roundoff; the reference of the comparison.
+  plain_fp64_tol1e-10   the same at the plain method's tolerance 1e-10.
+  learned_pair_tol1e-13 float-pair precision mode (FEDG_PREC_PAIR: explicit operator, Newton
+                        residual and RK accumulation in float pairs, FP32 Jacobian/LU), Newton from
+                        the column-guess MLP to tol 1e-13.
+  learned_fp32_tol1e-10 FP32 explicit mode (FEDG_PREC_MIXED), Newton from the MLP to tol 1e-10.
 
-Errors are computed on the full fields DENS, MOMX, MOMY, MOMZ, RHOT. Momentum is measured
-against at least 1 m/s of hydrostatic momentum. The deviation fields DDENS and DRHOT are also
-reported against their own norms.
+The MLP follows the learned-guess recipe:
+  - 193 -> 256 -> 256 -> 192;
+  - trained on the GPU on pairs the plain solver generates from 20 random density-current seeds,
+    on 4 x 4 x 8 slices of the same mesh.
+
+Errors are computed on the full fields DENS, MOMX, MOMY, MOMZ, RHOT, with momentum measured against
+at least 1 m/s of hydrostatic momentum. The deviation fields DDENS and DRHOT are also reported
+against their own norms.
 
 Usage (from the repository root):  PYTHONPATH=fe-project_gb300 python -m fedg.precision [--nex 8 ...]
 """
@@ -65,7 +70,16 @@ def _errors(torch, got, ref, dens_hyd, therm_hyd):
     return full, dev
 
 
-def run(nex=8, ney=8, nez=8, dt=0.04, hours=1.0, checkpoint_min=10.0, chunk=250, use_guess=True, seeds=20,
+PATHS = {
+    "plain_fp64_tol1e-13": (fl.PREC_FP64, 1e-13, False),
+    "plain_fp64_tol1e-10": (fl.PREC_FP64, 1e-10, False),
+    "learned_pair_tol1e-13": (fl.PREC_PAIR, 1e-13, True),
+    "learned_fp32_tol1e-10": (fl.PREC_MIXED, 1e-10, True),
+}
+REFS = ("plain_fp64_tol1e-13", "plain_fp64_tol1e-10")
+
+
+def run(nex=8, ney=8, nez=8, dt=0.04, hours=1.0, checkpoint_min=10.0, chunk=250, paths=tuple(PATHS), seeds=20,
         train_steps=2000, out=sys.stdout):
     import torch
 
@@ -74,9 +88,9 @@ def run(nex=8, ney=8, nez=8, dt=0.04, hours=1.0, checkpoint_min=10.0, chunk=250,
     nsteps = int(round(hours * 3600.0 / dt))
     ck_every = max(1, int(round(checkpoint_min * 60.0 / dt)))
     info = {"workload": f"density current p=7 {nex}x{ney}x{nez} elements of 800 m, HEVI IMEX-ARK232",
-            "dt": dt, "steps": nsteps, "simulated_s": nsteps * dt, "newton_tol": 1e-10}
+            "dt": dt, "steps": nsteps, "simulated_s": nsteps * dt, "paths": list(paths)}
     net = None
-    if use_guess:
+    if any(PATHS[p][2] for p in paths):
         t0 = time.perf_counter()
         # learned-guess recipe: about 200k (stage input, converged increment) pairs from 20 seeds
         # of 4x4x8 slices; 5 steps x 2 implicit stages x 1024 columns per seed
@@ -89,37 +103,41 @@ def run(nex=8, ney=8, nez=8, dt=0.04, hours=1.0, checkpoint_min=10.0, chunk=250,
     ctx.set_base_state(b["dens_hyd"], b["pres_hyd"], b["therm_hyd"])
     dens_hyd = ctx.tensor(b["dens_hyd"])
     therm_hyd = ctx.tensor(b["therm_hyd"])
-    q64 = [ctx.tensor(a) for a in q]
-    qmx = [t.clone() for t in q64]
+    q0 = [ctx.tensor(a) for a in q]
+    states = {p: [t.clone() for t in q0] for p in paths}
     if net is not None:
         net.attach(ctx)
-    o64 = dict(prec=fl.PREC_FP64, dt=dt, max_iter=20, tol=1e-10)
-    omx = dict(prec=fl.PREC_MIXED, dt=dt, max_iter=20, tol=1e-10, use_guess=net is not None)
-    stats = {"plain": {"s": 0.0, "fail": 0, "its": 0.0}, "learned": {"s": 0.0, "fail": 0, "its": 0.0}}
-    done, nchunk = 0, 0
+    stats = {p: {"s": 0.0, "fail": 0, "its": 0.0} for p in paths}
+    done = 0
     print(json.dumps({"setup": info}), file=out, flush=True)
+    rec = None
     while done < nsteps:
         n = min(chunk, nsteps - done, ck_every - done % ck_every)
-        for name, st, opts in (("plain", q64, o64), ("learned", qmx, omx)):
+        for p in paths:
+            prec, tol, guess = PATHS[p]
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            nf, its = ctx.update(st, n, **opts)
+            nf, its = ctx.update(states[p], n, prec=prec, dt=dt, max_iter=30, tol=tol, use_guess=guess)
             torch.cuda.synchronize()
-            s = stats[name]
+            s = stats[p]
             s["s"] += time.perf_counter() - t0
             s["fail"] += nf
             s["its"] += its * n
         done += n
-        nchunk += 1
         if done % ck_every == 0 or done == nsteps:
-            full, dev = _errors(torch, qmx, q64, dens_hyd, therm_hyd)
-            finite = all(bool(torch.isfinite(t).all().item()) for t in q64 + qmx)
-            rec = {"step": done, "t_s": done * dt, "rel_l2_full": full, "rel_l2_deviation": dev, "finite": finite,
-                   "plain_ms_per_step": 1e3 * stats["plain"]["s"] / done,
-                   "learned_ms_per_step": 1e3 * stats["learned"]["s"] / done,
-                   "plain_mean_solves": stats["plain"]["its"] / done,
-                   "learned_mean_solves": stats["learned"]["its"] / done,
-                   "plain_nonconverged": stats["plain"]["fail"], "learned_nonconverged": stats["learned"]["fail"]}
+            finite = all(bool(torch.isfinite(t).all().item()) for st in states.values() for t in st)
+            rec = {"step": done, "t_s": done * dt, "finite": finite, "errors": {}}
+            for ref in REFS:
+                if ref not in states:
+                    continue
+                for p in paths:
+                    if p == ref:
+                        continue
+                    full, dev = _errors(torch, states[p], states[ref], dens_hyd, therm_hyd)
+                    rec["errors"][f"{p} vs {ref}"] = {"rel_l2_full": full, "rel_l2_deviation": dev}
+            rec["ms_per_step"] = {p: 1e3 * stats[p]["s"] / done for p in paths}
+            rec["mean_solves"] = {p: stats[p]["its"] / done for p in paths}
+            rec["nonconverged"] = {p: stats[p]["fail"] for p in paths}
             print(json.dumps(rec), file=out, flush=True)
             if not finite:
                 break
@@ -136,14 +154,18 @@ def main(argv=None):
     ap.add_argument("--hours", type=float, default=1.0)
     ap.add_argument("--checkpoint-min", type=float, default=10.0)
     ap.add_argument("--chunk", type=int, default=250)
-    ap.add_argument("--no-guess", action="store_true")
+    ap.add_argument("--paths", default=",".join(PATHS), help="comma-separated subset of " + ", ".join(PATHS))
     ap.add_argument("--seeds", type=int, default=20)
     ap.add_argument("--train-steps", type=int, default=2000)
     a = ap.parse_args(argv)
     import __graft_entry__ as ge  # noqa: F401  (repository root on sys.path when run from it)
 
     ge.build()
-    run(a.nex, a.ney, a.nez, a.dt, a.hours, a.checkpoint_min, a.chunk, not a.no_guess, a.seeds, a.train_steps)
+    paths = tuple(p for p in a.paths.split(",") if p)
+    unknown = [p for p in paths if p not in PATHS]
+    if unknown:
+        ap.error(f"unknown paths {unknown}")
+    run(a.nex, a.ney, a.nez, a.dt, a.hours, a.checkpoint_min, a.chunk, paths, a.seeds, a.train_steps)
     return 0
 
 
