@@ -316,12 +316,21 @@ def run_fedg(args):
         del q_e
 
     # the same path without the learned guess, and the plain FP64 path, on the same state
-    noguess, plain, acc = None, None, None
+    noguess, plain, acc, pairp = None, None, None, None
     if rank == 0 and use_guess:
         o2 = dict(opts, use_guess=False)
         ms2, nf2, its2 = _timed_update(ctx, torch, stream, qd, args.steps, o2)
         noguess = {"value": dofs_stage * args.steps / (ms2 * 1e-3), "unit": UNIT, "ms_per_step": ms2 / args.steps,
                    "mean_newton_solves": its2, "nonconverged_columns": nf2}
+    if rank == 0 and prec == fl.PREC_MIXED and not args.no_pair:
+        # the float-pair precision mode (explicit operator in pairs as well; Newton to 1e-13), the
+        # mode that stays within 1e-6 of FP64 over a simulated hour of the density current
+        op_ = dict(opts, prec=fl.PREC_PAIR, tol=1e-13, max_iter=30)
+        ctx.update(qd, 1, **op_)
+        msp, nfp, itsp = _timed_update(ctx, torch, stream, qd, args.steps, op_)
+        pairp = {"value": dofs_stage * args.steps / (msp * 1e-3), "unit": UNIT, "ms_per_step": msp / args.steps,
+                 "newton_tol": 1e-13, "mean_newton_solves": itsp, "nonconverged_columns": nfp,
+                 "path": "learned+pair" if use_guess else "pair"}
     if rank == 0 and prec != fl.PREC_FP64 and not args.no_plain:
         # FElib's algorithm in FP64 on the GPU from the same initial state, and the error of the
         # timed path against it after the same number of steps
@@ -339,6 +348,11 @@ def run_fedg(args):
                  "mean_newton_solves": its64, "nonconverged_columns": nf64}
         ctx.update(q_mix, ncmp, **opts)
         acc = {"steps": ncmp, "rel_l2_vs_plain_fp64": _full_field_errors(np, q_mix, q_ref, dnorm2, dens_hyd, therm_hyd)}
+        if pairp is not None:
+            for a, h in zip(q_mix, q_host):
+                a.copy_(h)
+            ctx.update(q_mix, ncmp, **dict(opts, prec=fl.PREC_PAIR, tol=1e-13, max_iter=30))
+            pairp["rel_l2_vs_plain_fp64"] = _full_field_errors(np, q_mix, q_ref, dnorm2, dens_hyd, therm_hyd)
         del q_ref, q_mix
 
     cb = None
@@ -364,6 +378,7 @@ def run_fedg(args):
             "cpu_baseline": cb, "e2e": e2e, "gpu_launches": gpu_launches, "clocks": clocks,
             "guess_training": ginfo,
             "fp32_without_guess": noguess,
+            "learned_pair": pairp,
             "plain_fp64": plain,
             "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
             "accuracy": acc,
@@ -390,6 +405,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison run")
+    ap.add_argument("--no-pair", action="store_true", help="skip the float-pair precision mode run")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
