@@ -41,18 +41,18 @@ constexpr unsigned FULL = 0xffffffffu;
 // per-column shared-memory layout (bytes); the column stride is padded so that the C columns
 // of a warp start on different banks
 struct ColLayout {
-  int oP, oJq, oRing, oDel, oBf, oBc, oAl, oJb, stride;
+  int oP, oRing, oDel, oBf, oBc, oAl, oJb, oSJ, stride;
   __host__ __device__ ColLayout(int N1, int NeZ) {
     const int L = N1 * NeZ;
     int o = 0;
     oP = o;    o += 24 * L;                    // float2 P[3L] (uv phase: var0 pairs [2L])
-    oJq = o;   o += 16 * L;                    // float4 Jq[L]: pot, wt, dpd of the Jacobian
     oRing = o; o += 96 * N1;                   // 3 element slots x 4 quantities x N1 nodes x float2
     oDel = o;  o += 48;                        // 6 face fluxes (float2) of the current element
     oBf = o;   o += 12 * L;                    // float b / y / x [3L] (uv phase: [2L])
     oBc = o;   o += 64;                        // block-Thomas coupling from the element below
     oAl = o;   o += ((8 * NeZ + 15) / 16) * 16; // alB, alT per element
     oJb = o;   o += ((12 * (NeZ + 1) + 15) / 16) * 16;  // uv: c' and the two interface jumps
+    oSJ = o;   o += 16 * (N1 + 2);             // float4: pot, wt, dpd of the element's nodes + 2 neighbours
     const int words = o / 4;
     const int C = 32 / N1;
     stride = 4 * (((words + 31) / 32) * 32 + 32 / C);
@@ -62,7 +62,8 @@ struct ColLayout {
 template <int N1>
 struct Col {
   float2* P;     // iterate, float pairs, row 3l+v (v: DENS, MOMZ, RHOT)
-  float4* Jq;
+  float4* sJ;    // Jacobian level quantities of the current element's nodes, then node N of the
+                 // element below and node 0 of the element above
   void* ring;    // [3][4][N1]: slot, quantity (MOMZ, DDENS, fm, fr), node
   void* del;
   float* Bf;
@@ -85,8 +86,8 @@ __device__ __forceinline__ float grp_max_nan(float e, int width) {
 }
 
 // ---------------------------------------------------------------------------------------------
-// residual b = impl_fac A(P) + q* - P of the DENS/MOMZ/RHOT system into c.Bf (FP32), the FP32
-// Jacobian level quantities into c.Jq; returns the column max of |b|/scale (NaN if not finite).
+// residual b = impl_fac A(P) + q* - P of the DENS/MOMZ/RHOT system into c.Bf (FP32); returns the
+// column max of |b|/scale (NaN if not finite).
 // CERT: the operator A in float pairs (eval_Ax, hevi_common_2.F90:1177-1292, with the vertical
 // face flux vi_cal_del_flux_dyn :1294-1323); otherwise A in FP32 with only q* - P in pairs.
 // Element by element, with the level quantities of elements e-1, e, e+1 in a ring of 3 slots.
@@ -115,8 +116,6 @@ __device__ float col_residual(const OpsX& ox, const Col<N1>& c, const ProfX& px,
     const int l = e * N1 + k;
     const f2 Pd = f2_of(c.P[3 * l]), Pm = f2_of(c.P[3 * l + 1]), Pr = f2_of(c.P[3 * l + 2]);
     const int s = e % 3;
-    const float phf = __ldg(px.phf + l);
-    float potf, wtf, fmf, rhotf;
     if constexpr (CERT) {
       const f2 dens = f2_add(f2_of(__ldg(px.dh + l)), Pd);
       const f2 rhot = f2_add(f2_of(__ldg(px.rh + l)), Pr);
@@ -137,22 +136,14 @@ __device__ float col_residual(const OpsX& ox, const Col<N1>& c, const ProfX& px,
       r2[ri(s, 1, k)] = f2_pack(Pd);
       r2[ri(s, 2, k)] = f2_pack(fm);
       r2[ri(s, 3, k)] = f2_pack(f2_mul(pot, Pm));
-      potf = pot.h;
-      fmf = fm.h;
-      wtf = Pm.h * rd.h;
-      rhotf = rhot.h;
     } else {
       const float rdf = 1.f / (__ldg(px.dhf + l) + Pd.h);
-      rhotf = __ldg(px.rhf + l) + Pr.h;
-      potf = rhotf * rdf;
-      fmf = phf * expm1f(kapf * log1pf(Pr.h * __ldg(px.rthf + l)));
-      wtf = Pm.h * rdf;
+      const float potf = (__ldg(px.rhf + l) + Pr.h) * rdf;
       r1[ri(s, 0, k)] = Pm.h;
       r1[ri(s, 1, k)] = Pd.h;
-      r1[ri(s, 2, k)] = fmf;
+      r1[ri(s, 2, k)] = __ldg(px.phf + l) * expm1f(kapf * log1pf(Pr.h * __ldg(px.rthf + l)));
       r1[ri(s, 3, k)] = potf * Pm.h;
     }
-    c.Jq[l] = make_float4(potf, wtf, kapf * (phf + fmf) / rhotf, 0.f);
   };
 
   fill(0);
@@ -320,12 +311,23 @@ __device__ __forceinline__ void lu_rows(float (&a)[3][3 * N1], float (&r)[3][4],
   shfl_bwd<N1, 3 * N1 - 1>(a, r, k);
 }
 
+// FP32 Jacobian level quantities of level l from the iterate: pot = RHOT/DENS, wt = MOMZ/DENS,
+// dpd = dP/dRHOT = kappa PRES/RHOT
+__device__ __forceinline__ float4 jac_level(const ProfX& px, const float2* P, int l, float kapf) {
+  const float Pd = P[3 * l].x, Pm = P[3 * l + 1].x, Pr = P[3 * l + 2].x;
+  const float rdf = 1.f / (__ldg(px.dhf + l) + Pd);
+  const float rhotf = __ldg(px.rhf + l) + Pr;
+  const float phf = __ldg(px.phf + l);
+  const float fmf = phf * expm1f(kapf * log1pf(Pr * __ldg(px.rthf + l)));
+  return make_float4(rhotf * rdf, Pm * rdf, kapf * (phf + fmf) / rhotf, 0.f);
+}
+
 // one Newton correction of the DENS/MOMZ/RHOT system from the residual in c.Bf and the Jacobian
-// quantities in c.Jq: construct_matbnd (hevi_common_2.F90:1325-1480), block-Thomas with the
+// quantities of the iterate: construct_matbnd (hevi_common_2.F90:1325-1480), block-Thomas with the
 // 3x3 couplings of the face nodes, element LU; P += correction where apply.  G history in gscr.
 template <int N1>
-__device__ void col_solve(const Ops& op, const Col<N1>& c, double impl_fac, float* __restrict__ gsc, size_t gcol,
-                          size_t glayer, bool apply) {
+__device__ void col_solve(const Ops& op, const ProfX& px, float kapf, const Col<N1>& c, double impl_fac,
+                          float* __restrict__ gsc, size_t gcol, size_t glayer, bool apply) {
   constexpr int N = N1 - 1, n3 = 3 * N1;
   const int k = c.k;
   const float fi = (float)impl_fac;
@@ -341,9 +343,20 @@ __device__ void col_solve(const Ops& op, const Col<N1>& c, double impl_fac, floa
   for (int e = 0; e < c.NeZ; ++e) {
     float a[3][n3];
     float r[3][4];
+    {  // this element's level quantities, and the face neighbours' (lane 0: below, lane N: above)
+      const int l = e * N1 + k;
+      const float4 own = jac_level(px, c.P, l, kapf);
+      const bool below = k == 0 && e > 0, above = k == N && e < c.NeZ - 1;
+      const float4 nb = jac_level(px, c.P, below ? l - 1 : (above ? l + 1 : l), kapf);
+      __syncwarp();  // the previous element's quantities have been read
+      c.sJ[k] = own;
+      if (below) c.sJ[N1] = nb;
+      if (above) c.sJ[N1 + 1] = nb;
+      __syncwarp();
+    }
     float4 J[N1];
 #pragma unroll
-    for (int m = 0; m < N1; ++m) J[m] = c.Jq[e * N1 + m];
+    for (int m = 0; m < N1; ++m) J[m] = c.sJ[m];
 #pragma unroll
     for (int m = 0; m < N1; ++m) {
       const float fdz = Dk[m];
@@ -363,7 +376,6 @@ __device__ void col_solve(const Ops& op, const Col<N1>& c, double impl_fac, floa
     for (int f = 0; f < 2; ++f) {
       const bool bnd = (f == 0) ? (e == 0) : (e == c.NeZ - 1);
       const int pv1 = f == 0 ? 0 : N;
-      const int l1 = e * N1 + pv1;
       const float nz = f == 0 ? -1.f : 1.f;
       const float al = f == 0 ? c.alB(e) : c.alT(e);
       const float fac = f == 0 ? facB : facT;
@@ -385,7 +397,7 @@ __device__ void col_solve(const Ops& op, const Col<N1>& c, double impl_fac, floa
         a[2][c0 + 1] -= t2 * pot1;
         a[1][c0 + 2] -= t2 * dpd1;
         a[2][c0 + 2] += t1 - t2 * wt1;
-        const float4 Jn = c.Jq[f == 0 ? l1 - 1 : l1 + 1];
+        const float4 Jn = c.sJ[f == 0 ? N1 : N1 + 1];
         cc[0][0] = -t1; cc[0][1] = t2;
         cc[1][1] = -t1; cc[1][2] = t2 * Jn.z;
         cc[2][0] = -t2 * Jn.x * Jn.y; cc[2][1] = t2 * Jn.x; cc[2][2] = -t1 + t2 * Jn.y;
@@ -460,7 +472,7 @@ __device__ void col_solve(const Ops& op, const Col<N1>& c, double impl_fac, floa
 
 // ---------------------------------------------------------------------------------------------
 template <int N1, bool PO>
-__global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const OpsX ox, const ProfX px, const X5 qin, const F5c z,
+__global__ void __launch_bounds__(32, 9) k_vi_cols(const Ops op, const OpsX ox, const ProfX px, const X5 qin, const F5c z,
                                                 const float* const* guess, void* const* qsf, void* const* tout,
                                                 float* __restrict__ gsc, int* status, unsigned long long* cnt,
                                                 const MixViArgs args, int ncol) {
@@ -476,7 +488,7 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const OpsX ox, con
   unsigned char* base = smraw + (size_t)grp * lay.stride;
   Col<N1> c;
   c.P = reinterpret_cast<float2*>(base + lay.oP);
-  c.Jq = reinterpret_cast<float4*>(base + lay.oJq);
+  c.sJ = reinterpret_cast<float4*>(base + lay.oSJ);
   c.ring = base + lay.oRing;
   c.del = base + lay.oDel;
   c.Bf = reinterpret_cast<float*>(base + lay.oBf);
@@ -514,45 +526,29 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const OpsX ox, con
   __syncwarp();
 
   // ---- MOMX/MOMY (eval_Ax_uv / solve_uv) ----
-  // The operator is linear and acts on the face jumps only.  With P = P0 + D (P0 = var0, D an
-  // increment kept as a float pair), b(P) = [impl_fac A(P0) + (q* - P0)] + impl_fac A(D) - D.
-  // q* - P0 is kept as a pair hi + lo and the face jumps of P0 are formed in pairs, once per
-  // column; the corrections are FP32 and accumulate into D in pairs, so repeated corrections
-  // refine D to pair accuracy.
+  // The operator is linear and acts on the face jumps only.  The unknown is E = P - q*, a float
+  // pair per node, starting from var0 - q*: b(P) = impl_fac A(q* + E) - E.  The face jumps of q*
+  // are formed in pairs once per column; the corrections are FP32 and accumulate into E in pairs,
+  // so repeated corrections refine E to pair accuracy.
   {
-    float2* P0 = c.P;                                   // [2L] var0 pairs, only while the jumps are formed
-    float* qh = reinterpret_cast<float*>(c.Jq);         // [2L] (q* - P0) hi
-    float* ql = qh + 2 * L;                             // [2L] (q* - P0) lo
-    float2* D = reinterpret_cast<float2*>(c.P);         // [2L] increment (float pair), once P0 is dead
-    float* j0 = reinterpret_cast<float*>(c.P) + 4 * L;  // [4 NeZ] face jumps of P0
+    float2* E = reinterpret_cast<float2*>(c.P);         // [2L] P - q* (float pair)
+    float* jq = reinterpret_cast<float*>(c.P) + 4 * L;  // [4 NeZ] face jumps of q*
     float* bu = c.Bf;                                   // [2L] residual
+    const size_t g0 = c.gb - (size_t)NF * k;            // node (0, 0) of this column
+    auto gl = [&](int l) { return g0 + (size_t)(l / N1) * c.gs + (size_t)NF * (l % N1); };
     for (int e = 0; e < NeZ; ++e) {
       const int l = e * N1 + k;
       const size_t gi = c.g(e);
 #pragma unroll
-      for (int m = 0; m < 2; ++m) {
-        const f2 p0 = f2_split(__ldg(z.v[VMX + m] + gi));
-        const f2 d = f2_sub(f2_of(__ldg(qin.v[VMX + m] + gi)), p0);
-        P0[2 * l + m] = f2_pack(p0);
-        qh[2 * l + m] = d.h;
-        ql[2 * l + m] = d.l;
-      }
-    }
-    __syncwarp();
-    for (int e = 0; e < NeZ; ++e) {
-      for (int t = k; t < 4; t += N1) {  // bottom/top jump (neighbour - own) of MOMX/MOMY
+      for (int m = 0; m < 2; ++m)
+        E[2 * l + m] = f2_pack(f2_sub(f2_split(__ldg(z.v[VMX + m] + gi)), f2_of(__ldg(qin.v[VMX + m] + gi))));
+      for (int t = k; t < 4; t += N1) {  // bottom/top jump (neighbour - own) of q* MOMX/MOMY
         const int s = t >> 1, m = t & 1;
         const int lM = e * N1 + (s == 0 ? 0 : N);
         const bool lid = s == 0 ? (e == 0) : (e == NeZ - 1);
         const int lP = lid ? lM : (s == 0 ? lM - 1 : lM + 1);
-        j0[4 * e + t] = f2_to_f(f2_sub(f2_of(P0[2 * lP + m]), f2_of(P0[2 * lM + m])));
+        jq[4 * e + t] = lid ? 0.f : f2_to_f(f2_sub(f2_of(__ldg(qin.v[VMX + m] + gl(lP))), f2_of(__ldg(qin.v[VMX + m] + gl(lM)))));
       }
-    }
-    __syncwarp();
-    for (int e = 0; e < NeZ; ++e) {
-      const int l = e * N1 + k;
-      D[2 * l] = make_float2(0.f, 0.f);
-      D[2 * l + 1] = make_float2(0.f, 0.f);
     }
     __syncwarp();
     const float cfs = (float)(0.5 * args.impl_fac * op.FSz);
@@ -569,7 +565,7 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const OpsX ox, con
           const int lM = e * N1 + (s == 0 ? 0 : N);
           const bool lid = s == 0 ? (e == 0) : (e == NeZ - 1);
           const int lP = lid ? lM : (s == 0 ? lM - 1 : lM + 1);
-          jdel[t] = j0[4 * e + t] + (D[2 * lP + m].x - D[2 * lM + m].x);
+          jdel[t] = jq[4 * e + t] + (E[2 * lP + m].x - E[2 * lM + m].x);
         }
         __syncwarp();
         const int l = e * N1 + k;
@@ -578,7 +574,7 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const OpsX ox, con
 #pragma unroll
         for (int m = 0; m < 2; ++m) {
           const float Af = cfs * (aB * jdel[m] + aT * jdel[2 + m]);  // impl_fac * A(P)
-          const float b = ((qh[2 * l + m] - D[2 * l + m].x) + (ql[2 * l + m] - D[2 * l + m].y)) + Af;
+          const float b = (Af - E[2 * l + m].x) - E[2 * l + m].y;
           bu[2 * l + m] = b;
           err = fmaxf(err, fabsf(b) * iscu);
           if (!(fabsf(b) < 3.0e38f)) err = __int_as_float(0x7fc00000);
@@ -624,8 +620,8 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const OpsX ox, con
           const int l = e * N1 + k;
           const float beta = e > 0 ? cfs * lbk * c.alB(e) : 0.f;
           const float tau = e < NeZ - 1 ? cfs * ltk * c.alT(e) : 0.f;
-          D[2 * l] = f2_pack(f2_add_f(f2_of(D[2 * l]), bu[2 * l] - beta * Jx[e] + tau * Jx[e + 1]));
-          D[2 * l + 1] = f2_pack(f2_add_f(f2_of(D[2 * l + 1]), bu[2 * l + 1] - beta * Jy[e] + tau * Jy[e + 1]));
+          E[2 * l] = f2_pack(f2_add_f(f2_of(E[2 * l]), bu[2 * l] - beta * Jx[e] + tau * Jx[e + 1]));
+          E[2 * l + 1] = f2_pack(f2_add_f(f2_of(E[2 * l + 1]), bu[2 * l + 1] - beta * Jy[e] + tau * Jy[e + 1]));
         }
       }
       active = need;
@@ -638,10 +634,8 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const OpsX ox, con
 #pragma unroll
       for (int m = 0; m < 2; ++m) {
         const f2 ref = f2_mul(dh, f2_of(m == 0 ? ox.Uref : ox.Vref));
-        const f2 p0 = f2_split(__ldg(z.v[VMX + m] + gi));
-        const f2 d = f2_of(D[2 * l + m]);
-        const f2 pdev = f2_add(f2_sub(p0, ref), d);
-        const f2 inc = f2_sub(d, f2{qh[2 * l + m], ql[2 * l + m]});  // P - q*
+        const f2 inc = f2_of(E[2 * l + m]);  // P - q*
+        const f2 pdev = f2_add(f2_sub(f2_of(__ldg(qin.v[VMX + m] + gi)), ref), inc);
         if constexpr (PO) {
           static_cast<float2*>(qsf[VMX + m])[gi] = f2_pack(pdev);
           static_cast<float2*>(tout[VMX + m])[gi] = f2_pack(f2_mul(inc, f2_of(args.inv_impl2)));
@@ -668,7 +662,7 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const OpsX ox, con
   const size_t gcolumn = (size_t)col, glayer = (size_t)ncol;  // G history rows of this column
   const float cref = (float)args.cref;
   col_residual<N1, false>(ox, c, px, qin, args.impl2, cref);
-  col_solve<N1>(op, c, args.impl_fac, gsc, gcolumn, glayer, true);
+  col_solve<N1>(op, px, kapf, c, args.impl_fac, gsc, gcolumn, glayer, true);
   int nsolve = 1, st = 0;
   bool active = true;
   while (true) {
@@ -680,7 +674,7 @@ __global__ void __launch_bounds__(32) k_vi_cols(const Ops op, const OpsX ox, con
       else if (nsolve >= args.max_iter) { st = -1; active = false; }
     }
     if (!__any_sync(FULL, active)) break;
-    col_solve<N1>(op, c, args.impl_fac, gsc, gcolumn, glayer, active);
+    col_solve<N1>(op, px, kapf, c, args.impl_fac, gsc, gcolumn, glayer, active);
     ++nsolve;
   }
   for (int e = 0; e < NeZ; ++e) {
