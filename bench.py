@@ -122,7 +122,7 @@ def cpu_sample(path_kind, seconds_target=15.0):
     o.step_hevi(q, DT_STABLE, 1, max_iter=max_iter, tol=tol)
     t1 = time.perf_counter()
     nsteps = max(1, int(seconds_target / max(t1 - t0, 1e-3)))
-    nsteps = min(nsteps, 20)
+    nsteps = min(nsteps, 400)
     t2 = time.perf_counter()
     o.step_hevi(q, DT_STABLE, nsteps, max_iter=max_iter, tol=tol)
     t3 = time.perf_counter()
@@ -287,8 +287,14 @@ def run_fedg(args):
     }
     avg_ms = ktime / max(klaunch, 1)
     achieved = bytes_per_node.get(kname, 0) * nodes / (avg_ms * 1e-3) / 1e9 if avg_ms > 0 else 0.0
+    # DRAM bytes per node of one launch from ncu (dram__bytes_read.sum + dram__bytes_write.sum of the
+    # kernel on the 32x32x16-element slice, profiles/mixed_kernels_C5small_p7_32x32x16.md), scaled to
+    # this workload's node count
+    ncu_bytes_per_node = {"vi_mixed": (847.3e6 + 728.2e6) / (32 * 32 * 16 * 512)}
+    traffic = ncu_bytes_per_node[kname] * nodes / 1e9 if kname in ncu_bytes_per_node else None
     roof = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peaks.get("hbm_gbs", 6800.0),
-            "unit": "GB/s", "frac": achieved / peaks.get("hbm_gbs", 6800.0), "traffic": None,
+            "unit": "GB/s", "frac": achieved / peaks.get("hbm_gbs", 6800.0), "traffic": traffic,
+            "traffic_unit": "GB per launch (ncu DRAM read+write, 32x32x16 capture scaled by nodes)",
             "peak_source": peak_src, "avg_launch_ms": avg_ms, "algorithmic_bytes_per_node": bytes_per_node.get(kname)}
     fp64_tf = fp64_dgemm_tflops(torch, ctx.dev) if rank == 0 else 0.0
     gpu_launches = sum(v[1] for v in prof.values())
