@@ -9,7 +9,16 @@ ARK(2,3,2) and the column Newton solve to tol 1e-10.  134,217,728 nodes x 5 vari
 A "step" is one full time step (3 RK stages) of the whole domain; the metric is
 DOF-stage updates per second = 5 * Np * Ne * 3 * steps / time.
 
-  python bench.py [--steps K] [--warmup W] [--path mixed|fp64] [--impl fedg|reference]
+Paths (--path):
+  pair   (default) the learned Newton guess with the FP32-pipe float-pair arithmetic
+         (FEDG_PREC_PAIR) and the Newton solve to tol 1e-13: the path that stays within 1e-6
+         relative L2 of converged FP64 over a simulated hour;
+  mixed  the learned guess with FP32 explicit arithmetic (FEDG_PREC_MIXED), Newton tol 1e-10;
+  fp64   FElib's algorithm in FP64 on the GPU, Newton tol 1e-10.
+The default run also times learned+FP32, the headline path without the guess and the plain
+FP64 path on the same state, and reports the error of each against plain FP64.
+
+  python bench.py [--steps K] [--warmup W] [--path pair|mixed|fp64] [--impl fedg|reference]
 
 --impl reference times the CPU implementation of the same step (the FP64 oracle port of
 FElib's routines, all host cores) on a bounded sample of the workload.
@@ -33,6 +42,19 @@ for p in (os.path.join(ROOT, "fe-project_gb300"), os.path.join(ROOT, "oracle")):
 METRIC = "DOF-stage/s on 1 GB300: learned+FP32 vs plain FP64 HEVI, rel L2 err <=1e-6"
 UNIT = "DOF-stage/s"
 DT_STABLE = 0.005  # C5 geometry (h = 100 m, p = 7): the oracle is stable at 0.005 s, not at 0.01 s
+
+# precision mode (fedg.lib PREC_*), Newton tolerance and iteration cap of each path
+PATH_PREC = {"pair": 2, "mixed": 1, "fp64": 0}
+PATH_TOL = {"pair": 1e-13, "mixed": 1e-10, "fp64": 1e-10}
+PATH_ITER = {"pair": 30, "mixed": 20, "fp64": 20}
+PATH_NAME = {"pair": "learned+pair", "mixed": "learned+fp32", "fp64": "plain_fp64"}
+PATH_DTYPE = {"pair": "f32x2", "mixed": "f32+f32x2", "fp64": "f64"}
+# DRAM bytes per node of one launch of the dominant kernel from ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum on the 32x32x16-element slice, 8,388,608 nodes; profiles/), per path
+NCU_BYTES_PER_NODE = {
+    "pair": {"vi_mixed": (936.96e6 + 1159.80e6) / (32 * 32 * 16 * 512)},
+    "mixed": {"vi_mixed": (847.3e6 + 728.2e6) / (32 * 32 * 16 * 512)},
+}
 
 
 def _env_rank():
@@ -219,8 +241,8 @@ def run_fedg(args):
     if args.small:
         case = case.scaled(32, 32, 16)
     path = args.path
-    prec = fl.PREC_MIXED if path == "mixed" else fl.PREC_FP64
-    use_guess = path == "mixed" and bool(args.guess)
+    prec = PATH_PREC[path]
+    use_guess = path != "fp64" and bool(args.guess)
     net, ginfo = None, None
     if use_guess:
         # the C5 column network (128 levels: 385 -> 256 -> 256 -> 384), trained on the GPU with the
@@ -245,7 +267,7 @@ def run_fedg(args):
     if net is not None:
         net.attach(ctx)
     stream = torch.cuda.ExternalStream(ctx.stream_handle)
-    opts = dict(prec=prec, dt=DT_STABLE, max_iter=20, tol=1e-10, use_guess=use_guess)
+    opts = dict(prec=prec, dt=DT_STABLE, max_iter=PATH_ITER[path], tol=PATH_TOL[path], use_guess=use_guess)
 
     # warm-up
     ctx.update(qd, args.warmup, **opts)
@@ -281,8 +303,9 @@ def run_fedg(args):
         # S1 q^n(f32) + q^n(f64) in -> q*_2, S3, SF out; S2 Q_2(f32), t_im, q^n, S3, SF in -> q*_3, SF out;
         # S3 Q_3(f32), t_im, q^n, SF in -> q^n+1 (f64) + its f32 copy out
         "stage_mixed": (20 + 40 + 40 + 20 + 20 + 20 + 20 + 40 + 20 + 20 + 40 + 20 + 20 + 40 + 20 + 40 + 20) / 3,
-        # column solve: q*, var0 in (FP64) -> Q (FP32 deviation copy), t_im (FP32) out
-        "vi_mixed": 8 * 5 + 8 * 5 + 4 * 5 + 4 * 5,
+        # column solve: q* (float pairs) and var0 (FP64) in -> Q and t_im out, FP32 in the FP32 mode and
+        # float pairs in the pair mode; plus the three guess fields (FP32) when the guess is on
+        "vi_mixed": 8 * 5 + 8 * 5 + (8 if prec == fl.PREC_PAIR else 4) * 10 + (12 if use_guess else 0),
         "filter": 8 * 10, "drhot2pres": 8 * 2, "mlp": 0, "aux": 0,
     }
     avg_ms = ktime / max(klaunch, 1)
@@ -290,11 +313,11 @@ def run_fedg(args):
     # DRAM bytes per node of one launch from ncu (dram__bytes_read.sum + dram__bytes_write.sum of the
     # kernel on the 32x32x16-element slice, profiles/mixed_kernels_C5small_p7_32x32x16.md), scaled to
     # this workload's node count
-    ncu_bytes_per_node = {"vi_mixed": (847.3e6 + 728.2e6) / (32 * 32 * 16 * 512)}
+    ncu_bytes_per_node = NCU_BYTES_PER_NODE.get(path, {})
     traffic = ncu_bytes_per_node[kname] * nodes / 1e9 if kname in ncu_bytes_per_node else None
     roof = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peaks.get("hbm_gbs", 6800.0),
             "unit": "GB/s", "frac": achieved / peaks.get("hbm_gbs", 6800.0), "traffic": traffic,
-            "traffic_unit": "GB per launch (ncu DRAM read+write, 32x32x16 capture scaled by nodes)",
+            "traffic_unit": "GB per launch (ncu DRAM read+write of the same path on the 32x32x16 slice, scaled by nodes)",
             "peak_source": peak_src, "avg_launch_ms": avg_ms, "algorithmic_bytes_per_node": bytes_per_node.get(kname)}
     fp64_tf = fp64_dgemm_tflops(torch, ctx.dev) if rank == 0 else 0.0
     gpu_launches = sum(v[1] for v in prof.values())
@@ -321,25 +344,25 @@ def run_fedg(args):
                "steps": ke}
         del q_e
 
-    # the same path without the learned guess, and the plain FP64 path, on the same state
-    noguess, plain, acc, pairp = None, None, None, None
+    # the headline path without the learned guess, the other precision mode, and the plain FP64 path, on
+    # the same state
+    noguess, plain, acc, other = None, None, None, None
     if rank == 0 and use_guess:
         o2 = dict(opts, use_guess=False)
         ms2, nf2, its2 = _timed_update(ctx, torch, stream, qd, args.steps, o2)
         noguess = {"value": dofs_stage * args.steps / (ms2 * 1e-3), "unit": UNIT, "ms_per_step": ms2 / args.steps,
-                   "mean_newton_solves": its2, "nonconverged_columns": nf2}
-    if rank == 0 and prec == fl.PREC_MIXED and not args.no_pair:
-        # the float-pair precision mode (explicit operator in pairs as well; Newton to 1e-13), the
-        # mode that stays within 1e-6 of FP64 over a simulated hour of the density current
-        op_ = dict(opts, prec=fl.PREC_PAIR, tol=1e-13, max_iter=30)
+                   "newton_tol": opts["tol"], "mean_newton_solves": its2, "nonconverged_columns": nf2}
+    other_path = {"pair": "mixed", "mixed": "pair"}.get(path)
+    if rank == 0 and other_path and not args.no_other:
+        op_ = dict(opts, prec=PATH_PREC[other_path], tol=PATH_TOL[other_path], max_iter=PATH_ITER[other_path])
         ctx.update(qd, 1, **op_)
-        msp, nfp, itsp = _timed_update(ctx, torch, stream, qd, args.steps, op_)
-        pairp = {"value": dofs_stage * args.steps / (msp * 1e-3), "unit": UNIT, "ms_per_step": msp / args.steps,
-                 "newton_tol": 1e-13, "mean_newton_solves": itsp, "nonconverged_columns": nfp,
-                 "path": "learned+pair" if use_guess else "pair"}
+        mso, nfo, itso = _timed_update(ctx, torch, stream, qd, args.steps, op_)
+        other = {"value": dofs_stage * args.steps / (mso * 1e-3), "unit": UNIT, "ms_per_step": mso / args.steps,
+                 "newton_tol": op_["tol"], "mean_newton_solves": itso, "nonconverged_columns": nfo,
+                 "path": PATH_NAME[other_path] if use_guess else PATH_NAME[other_path].replace("learned+", "")}
     if rank == 0 and prec != fl.PREC_FP64 and not args.no_plain:
-        # FElib's algorithm in FP64 on the GPU from the same initial state, and the error of the
-        # timed path against it after the same number of steps
+        # FElib's algorithm in FP64 on the GPU from the same initial state, and the error of each
+        # precision mode against it after the same number of steps
         q_ref = [torch.empty_like(t) for t in qd]
         q_mix = [torch.empty_like(t) for t in qd]
         for a, h in zip(q_ref, q_host):
@@ -347,18 +370,19 @@ def run_fedg(args):
         for a, h in zip(q_mix, q_host):
             a.copy_(h)
         ncmp = args.compare_steps
-        o64 = dict(opts, prec=fl.PREC_FP64, use_guess=False)
+        o64 = dict(opts, prec=fl.PREC_FP64, use_guess=False, tol=1e-10, max_iter=20)
         ctx.update(q_ref, max(ncmp - 2, 0), **o64)
         pms, nf64, its64 = _timed_update(ctx, torch, stream, q_ref, 2, o64)
         plain = {"value": dofs_stage * 2 / (pms * 1e-3), "unit": UNIT, "ms_per_step": pms / 2, "steps": 2,
-                 "mean_newton_solves": its64, "nonconverged_columns": nf64}
+                 "newton_tol": 1e-10, "mean_newton_solves": its64, "nonconverged_columns": nf64}
         ctx.update(q_mix, ncmp, **opts)
         acc = {"steps": ncmp, "rel_l2_vs_plain_fp64": _full_field_errors(np, q_mix, q_ref, dnorm2, dens_hyd, therm_hyd)}
-        if pairp is not None:
+        if other is not None:
             for a, h in zip(q_mix, q_host):
                 a.copy_(h)
-            ctx.update(q_mix, ncmp, **dict(opts, prec=fl.PREC_PAIR, tol=1e-13, max_iter=30))
-            pairp["rel_l2_vs_plain_fp64"] = _full_field_errors(np, q_mix, q_ref, dnorm2, dens_hyd, therm_hyd)
+            ctx.update(q_mix, ncmp, **dict(opts, prec=PATH_PREC[other_path], tol=PATH_TOL[other_path],
+                                           max_iter=PATH_ITER[other_path]))
+            other["rel_l2_vs_plain_fp64"] = _full_field_errors(np, q_mix, q_ref, dnorm2, dens_hyd, therm_hyd)
         del q_ref, q_mix
 
     cb = None
@@ -370,10 +394,11 @@ def run_fedg(args):
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64" if prec == fl.PREC_FP64 else "f32+f64", "data": "synthetic",
+            "vs_baseline": None, "dtype": PATH_DTYPE[path], "data": "synthetic",
             "config": {"workload": f"{case.name}: p=7 {case.NeX}x{case.NeY}x{case.NeZ} elements, HEVI IMEX-ARK232, "
                                    f"constBVFreq N=0.01, +-0.1K noise below 500 m, u=5 m/s",
-                       "path": "plain_fp64" if prec == fl.PREC_FP64 else ("learned+fp32" if use_guess else "fp32"),
+                       "path": PATH_NAME[path] if use_guess or path == "fp64" else PATH_NAME[path].replace("learned+", ""),
+                       "one_hour_accuracy": "fe-project_gb300/fedg/precision.py (C1 warm bubble and C2 density current)",
                        "dt": DT_STABLE, "dt_baseline": 0.5, "newton_tol": opts["tol"], "newton_max_iter": opts["max_iter"],
                        "mean_newton_solves": its, "nonconverged_columns": nfail, "finite": finite,
                        "l2": "inputs larger than L2 (FP64 state %.1f GB)" % (case.dofs * 8 / 1e9),
@@ -383,8 +408,8 @@ def run_fedg(args):
             "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items() if v[1]},
             "cpu_baseline": cb, "e2e": e2e, "gpu_launches": gpu_launches, "clocks": clocks,
             "guess_training": ginfo,
-            "fp32_without_guess": noguess,
-            "learned_pair": pairp,
+            "without_guess": noguess,
+            ("learned_fp32" if other_path == "mixed" else "learned_pair"): other,
             "plain_fp64": plain,
             "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
             "accuracy": acc,
@@ -402,7 +427,7 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["fedg", "reference"], default="fedg")
-    ap.add_argument("--path", choices=["mixed", "fp64"], default=os.environ.get("FEDG_BENCH_PATH", "mixed"))
+    ap.add_argument("--path", choices=["pair", "mixed", "fp64"], default=os.environ.get("FEDG_BENCH_PATH", "pair"))
     ap.add_argument("--guess", type=int, default=1)
     ap.add_argument("--train-steps", type=int, default=2000)
     ap.add_argument("--compare-steps", type=int, default=4,
@@ -411,7 +436,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison run")
-    ap.add_argument("--no-pair", action="store_true", help="skip the float-pair precision mode run")
+    ap.add_argument("--no-other", action="store_true", help="skip the run of the other precision mode")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -80,14 +80,18 @@ REFS = ("plain_fp64_tol1e-13", "plain_fp64_tol1e-10")
 
 
 def run(nex=8, ney=8, nez=8, dt=0.04, hours=1.0, checkpoint_min=10.0, chunk=250, paths=tuple(PATHS), seeds=20,
-        train_steps=2000, out=sys.stdout):
+        train_steps=2000, case_name="C2", out=sys.stdout):
+    import dataclasses
+
     import torch
 
-    base = cases.C2()
+    # C2: the density current (default); C1: the +2 K warm bubble of the small case, run with the
+    # HEVI IMEX scheme of the precision form
+    base = cases.C2() if case_name == "C2" else dataclasses.replace(cases.C1(), eqs="HEVI")
     case = base.scaled(nex, ney, nez)
     nsteps = int(round(hours * 3600.0 / dt))
     ck_every = max(1, int(round(checkpoint_min * 60.0 / dt)))
-    info = {"workload": f"density current p=7 {nex}x{ney}x{nez} elements of 800 m, HEVI IMEX-ARK232",
+    info = {"workload": f"{case_name} recipe p={case.porder} {nex}x{ney}x{nez} elements, HEVI IMEX-ARK232",
             "dt": dt, "steps": nsteps, "simulated_s": nsteps * dt, "paths": list(paths)}
     net = None
     if any(PATHS[p][2] for p in paths):
@@ -147,6 +151,7 @@ def run(nex=8, ney=8, nez=8, dt=0.04, hours=1.0, checkpoint_min=10.0, chunk=250,
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--case", choices=["C2", "C1"], default="C2")
     ap.add_argument("--nex", type=int, default=8)
     ap.add_argument("--ney", type=int, default=8)
     ap.add_argument("--nez", type=int, default=8)
@@ -165,7 +170,7 @@ def main(argv=None):
     unknown = [p for p in paths if p not in PATHS]
     if unknown:
         ap.error(f"unknown paths {unknown}")
-    run(a.nex, a.ney, a.nez, a.dt, a.hours, a.checkpoint_min, a.chunk, paths, a.seeds, a.train_steps)
+    run(a.nex, a.ney, a.nez, a.dt, a.hours, a.checkpoint_min, a.chunk, paths, a.seeds, a.train_steps, a.case)
     return 0
 
 
