@@ -95,6 +95,24 @@ void invert(int n, std::vector<double> a, std::vector<double>& inv) {
   }
 }
 
+// exponential modal filter V diag(sigma) V^-1, sigma_m = exp(-alpha ((m/N - etac)/(1 - etac))^ord) for
+// m/N > etac (scale_element_modalfilter.F90:204-236)
+void filter_1d(int N, const std::vector<double>& V, const std::vector<double>& iV, double etac, double alpha, int ord,
+               double* F) {
+  const int n1 = N + 1;
+  std::vector<double> sig(n1, 1.0);
+  for (int m = 1; m < n1; ++m) {
+    const double eta = double(m) / N;
+    if (eta > etac) sig[m] = std::exp(-alpha * std::pow((eta - etac) / (1.0 - etac), ord));
+  }
+  for (int i = 0; i < n1; ++i)
+    for (int j = 0; j < n1; ++j) {
+      double s = 0.0;
+      for (int m = 0; m < n1; ++m) s += V[i * n1 + m] * sig[m] * iV[m * n1 + j];
+      F[i * n1 + j] = s;
+    }
+}
+
 // 1D operators of the tensor-product element (scale_element_hexahedral.F90:102-404,
 // scale_element_operation_tensorprod3D.F90:5464-5569, scale_element_modalfilter.F90:204-236)
 void build_ops_1d(int N, double etac_h, double alpha_h, int ord_h, double etac_v, double alpha_v, int ord_v,
@@ -119,21 +137,12 @@ void build_ops_1d(int N, double etac_h, double alpha_h, int ord_h, double etac_v
     op.Lb[k] = sb;
     op.Lt[k] = st;
   }
-  auto filt = [&](double etac, double alpha, int ord, double* F) {
-    std::vector<double> sig(n1, 1.0);
-    for (int m = 1; m < n1; ++m) {
-      const double eta = double(m) / N;
-      if (eta > etac) sig[m] = std::exp(-alpha * std::pow((eta - etac) / (1.0 - etac), ord));
-    }
-    for (int i = 0; i < n1; ++i)
-      for (int j = 0; j < n1; ++j) {
-        double s = 0.0;
-        for (int m = 0; m < n1; ++m) s += V[i * n1 + m] * sig[m] * iV[m * n1 + j];
-        F[i * n1 + j] = s;
-      }
-  };
-  filt(etac_h, alpha_h, ord_h, op.F);
-  filt(etac_v, alpha_v, ord_v, op.Fv);
+  for (int i = 0; i < n1; ++i) {
+    const double pn = legendre(N, x[i]);
+    op.w[i] = 2.0 / (N * (N + 1.0) * pn * pn);
+  }
+  filter_1d(N, V, iV, etac_h, alpha_h, ord_h, op.F);
+  filter_1d(N, V, iV, etac_v, alpha_v, ord_v, op.Fv);
   for (int i = 0; i < n1; ++i)
     for (int j = 0; j < n1; ++j) {
       double s = 0.0;
@@ -141,6 +150,20 @@ void build_ops_1d(int N, double etac_h, double alpha_h, int ord_h, double etac_v
       op.T[i * n1 + j] = s;
     }
 }
+
+}  // namespace
+namespace fedg {
+void modal_filter_1d(int N, double etac, double alpha, int ord, double* F) {
+  const int n1 = N + 1;
+  const std::vector<double> x = lgl(N);
+  std::vector<double> V(n1 * n1), iV;
+  for (int i = 0; i < n1; ++i)
+    for (int m = 0; m < n1; ++m) V[i * n1 + m] = legendre(m, x[i]) * std::sqrt(m + 0.5);
+  invert(n1, V, iV);
+  filter_1d(N, V, iV, etac, alpha, ord, F);
+}
+}  // namespace fedg
+namespace {
 
 // ---------------- small device kernels ----------------
 __global__ void k_extract_profile(const double* __restrict__ a, double* __restrict__ prof, int N1, int Np, int L,
@@ -268,6 +291,7 @@ int fedg_ctx_create(const fedg_mesh_desc* d, fedg_ctx** out) {
   const double dx = (d->xmax - d->xmin) / d->NeX, dy = (d->ymax - d->ymin) / d->NeY, dz = (d->zmax - d->zmin) / d->NeZ;
   op.E11 = 2.0 / dx; op.E22 = 2.0 / dy; op.E33 = 2.0 / dz;
   op.FSx = 2.0 / dx; op.FSy = 2.0 / dy; op.FSz = 2.0 / dz;
+  op.Jac = dx * dy * dz / 8.0;
   op.grav = d->grav; op.rdry = d->rdry; op.cpdry = d->cpdry; op.cvdry = d->cvdry; op.pres00 = d->pres00;
   op.kap = d->cpdry / d->cvdry;
   op.rgamm = d->cvdry / d->cpdry;
@@ -296,6 +320,7 @@ void fedg_ctx_destroy(fedg_ctx* c) {
   cudaFree(c->d_status);
   cudaFree(c->d_cnt);
   cudaFree(c->work);
+  cudaFree(c->trc_buf);
   if (c->h_cnt) cudaFreeHost(c->h_cnt);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -369,6 +394,7 @@ int fedg_drhot2pres(fedg_ctx* c, const double* DRHOT, double* PRES, double* DPRE
 static double* ensure_work(fedg_ctx* c, size_t ndouble) {
   if (c->work_doubles >= ndouble) return c->work;
   cudaFree(c->work);
+  cudaFree(c->trc_buf);
   c->work = nullptr;
   c->work_doubles = 0;
   if (cudaMalloc(&c->work, sizeof(double) * ndouble) != cudaSuccess) return nullptr;

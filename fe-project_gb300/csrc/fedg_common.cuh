@@ -18,8 +18,10 @@ struct Ops {
   double T[FEDG_MAXN1 * FEDG_MAXN1];  // VPOrdM1 truncation
   double Lb[FEDG_MAXN1];              // Lift coefficient from the -1 face: Minv(k,0)
   double Lt[FEDG_MAXN1];              // Lift coefficient from the +1 face: Minv(k,N)
+  double w[FEDG_MAXN1];               // LGL quadrature weights (scale_polynomial.F90:271-287)
   double E11, E22, E33;               // Escale of the flat cube
   double FSx, FSy, FSz;               // Fscale per face orientation
+  double Jac;                         // volume Jacobian J = dx dy dz / 8
   double grav, rdry, cpdry, cvdry, pres00;
   double kap;    // cp/cv
   double rgamm;  // cv/cp

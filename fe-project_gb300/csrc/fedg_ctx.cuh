@@ -33,6 +33,7 @@ struct fedg_ctx {
   MixedState* mixed = nullptr;
   fedg_tint* upd_tint = nullptr;  // RK buffers of fedg_update, kept between calls
   MlpState* guess = nullptr;      // column-guess network attached with fedg_guess_load (not owned)
+  double* trc_buf = nullptr;      // tracer update scratch: two stage fields, var0, varTmp, FCT per element
   // kernel timers / launch counters
   bool prof_on = false;
   long long nlaunch[FEDG_K_COUNT] = {};

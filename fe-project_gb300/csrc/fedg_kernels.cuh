@@ -14,6 +14,9 @@ struct ViArgs {
   double cref;  // velocity scale of the MOMZ convergence test [m/s]
 };
 
+// host: 1D exponential modal filter matrix (row-major N1 x N1) of order N
+void modal_filter_1d(int N, double etac, double alpha, int ord, double* F);
+
 int launch_tend_fp64(const Ops& op, const Prof& pf, const F5c& q, const double* dpres, const F5& t, int Ne,
                      int hevi, cudaStream_t s);
 int launch_filter_fp64(const Ops& op, const F5& q, int Ne, cudaStream_t s);

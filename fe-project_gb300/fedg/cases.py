@@ -50,6 +50,9 @@ class Case:
     noise: dict = field(default_factory=dict)  # amp, zmax, seed
     filter_on: bool = True
     newton_tol: float = 1e-10
+    grav: float = GRAV
+    v0: float = 0.0
+    tracer: dict = field(default_factory=dict)  # cosine-bell tracer: qmax, rx, ry, rz, xc, yc, zc
 
     @property
     def N1(self):
@@ -82,8 +85,13 @@ class Case:
         if b and not keep_extent:
             b["xc"] = 0.5 * (xmin + xmax)
             b["yc"] = 0.5 * (ymin + ymax)
+        tr = dict(self.tracer)
+        if tr and not keep_extent:  # keep the tracer's position and size relative to the domain
+            fx, fy, fz = NeX / self.NeX, NeY / self.NeY, NeZ / self.NeZ
+            tr.update(xc=xmin + (tr["xc"] - xmin) * fx, yc=ymin + (tr["yc"] - ymin) * fy,
+                      zc=zmin + (tr["zc"] - zmin) * fz, rx=tr["rx"] * fx, ry=tr["ry"] * fy, rz=tr["rz"] * fz)
         return replace(self, NeX=NeX, NeY=NeY, NeZ=NeZ, porder=porder or self.porder,
-                       dom=(xmin, xmax, ymin, ymax, zmin, zmax), bubble=b)
+                       dom=(xmin, xmax, ymin, ymax, zmin, zmax), bubble=b, tracer=tr)
 
 
 def C1():
@@ -113,7 +121,18 @@ def C5():
                 noise=dict(amp=0.1, zmax=500.0, seed=0))
 
 
-CASES = {"C1": C1, "C2": C2, "C3": C3, "C5": C5}
+def T1():
+    """Tracer advection test (model/atm_nonhydro3d/test/case/tracer_advection/{init,run}.conf):
+    p=3, 20x20x5 elements over 60x60x20 km, constPT 300 K base state with g = 0 (uniform density),
+    uniform wind (u, v) = (-35, -40) m/s, cosine-bell tracer of peak 1 and radii 10 km at
+    (12, 12, 5) km; tracer SSP-RK3, dt = 2 s, 900 s; no modal filter; FCT + TMAR on."""
+    return Case("T1_p3_20x20x5_trcadv", 3, 20, 20, 5, (0.0, 60000.0, 0.0, 60000.0, 0.0, 20000.0), "HEVE",
+                dt=2.0, nsteps=450, base="constPT", T0=300.0, psfc=101325.0, grav=0.0, u0=-35.0, v0=-40.0,
+                filter_on=False,
+                tracer=dict(qmax=1.0, rx=10000.0, ry=10000.0, rz=10000.0, xc=12000.0, yc=12000.0, zc=5000.0))
+
+
+CASES = {"C1": C1, "C2": C2, "C3": C3, "C5": C5, "T1": T1}
 
 
 def node_coords(case: Case):
@@ -138,20 +157,20 @@ def base_state(case: Case, z):
     """(DENS_hyd, PRES_hyd, PT_hyd) at heights z."""
     rovcp = RDRY / CPDRY
     if case.base == "constT":
-        H0 = RDRY * case.T0 / GRAV
+        H0 = RDRY * case.T0 / case.grav
         pres = case.psfc * np.exp(-z / H0)
         dens = pres / (RDRY * case.T0)
         pt = case.T0 * (PRES00 / pres) ** rovcp
     elif case.base == "constPT":
         exner_sfc = (case.psfc / PRES00) ** rovcp
-        exner = exner_sfc - GRAV / (CPDRY * case.T0) * z
+        exner = exner_sfc - case.grav / (CPDRY * case.T0) * z
         pres = PRES00 * exner ** (CPDRY / RDRY)
         dens = pres / (RDRY * exner * case.T0)
         pt = np.full_like(z, case.T0)
     elif case.base == "constBVFreq":
         exner_sfc = (case.psfc / PRES00) ** rovcp
-        pt = case.T0 * np.exp(case.bvf ** 2 / GRAV * z)
-        exner = exner_sfc + GRAV ** 2 / (CPDRY * case.bvf ** 2) * (1.0 / pt - 1.0 / case.T0)
+        pt = case.T0 * np.exp(case.bvf ** 2 / case.grav * z)
+        exner = exner_sfc + case.grav ** 2 / (CPDRY * case.bvf ** 2) * (1.0 / pt - 1.0 / case.T0)
         pres = PRES00 * exner ** (CPDRY / RDRY)
         dens = pres / (RDRY * exner * pt)
     else:
@@ -180,8 +199,17 @@ def initial_state(case: Case, seed=None):
     ddens = dens - dens_hyd
     drhot = dens * pt - therm_hyd
     momx = dens * case.u0
-    momy = np.zeros_like(z)
+    momy = dens * case.v0
     momz = np.zeros_like(z)
     q = [ddens, momx, momy, momz, drhot]
     base = dict(dens_hyd=dens_hyd, pres_hyd=pres_hyd, therm_hyd=therm_hyd, pt_hyd=pt_hyd, x=x, y=y, z=z)
     return q, base
+
+
+def tracer_state(case: Case):
+    """Initial tracer mixing ratio of a case with a ``tracer`` bell: qmax (0.5 (1 + cos(pi r)))
+    inside r <= 1 (mkinitutil_calc_cosinebell, exponent 1), sampled at the nodes."""
+    x, y, z = node_coords(case)
+    tr = case.tracer
+    r = np.sqrt(((x - tr["xc"]) / tr["rx"]) ** 2 + ((y - tr["yc"]) / tr["ry"]) ** 2 + ((z - tr["zc"]) / tr["rz"]) ** 2)
+    return np.where(r <= 1.0, tr["qmax"] * 0.5 * (1.0 + np.cos(np.pi * np.minimum(r, 1.0))), 0.0)

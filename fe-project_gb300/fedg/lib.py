@@ -32,11 +32,15 @@ EXPORTED = [
     "fedg_guess_create", "fedg_guess_destroy", "fedg_guess_num_params", "fedg_guess_set_scales",
     "fedg_guess_set_params", "fedg_guess_get_params", "fedg_guess_train_step", "fedg_guess_loss_grad",
     "fedg_guess_predict", "fedg_guess_load", "fedg_cal_tend_ex_noalloc",
+    "fedg_trc_alphdens_advtest", "fedg_trc_save_massflux", "fedg_trc_fct_coef", "fedg_trc_cal_tend",
+    "fedg_trc_tmar", "fedg_trc_modalfilter", "fedg_trc_update",
 ]
 
 # kernel classes of fedg_prof_read (include/fedg.h)
-K_TEND, K_VI, K_RK, K_FILTER, K_PRES, K_MTEND, K_MVI, K_MLP, K_AUX, K_COUNT = range(10)
-KERNEL_NAMES = ["tend_fp64", "vi_fp64", "rk", "filter", "drhot2pres", "stage_mixed", "vi_mixed", "mlp", "aux"]
+K_TEND, K_VI, K_RK, K_FILTER, K_PRES, K_MTEND, K_MVI, K_MLP, K_AUX, K_TRC_FCT, K_TRC_TEND, K_TRC_AUX, K_COUNT = \
+    range(13)
+KERNEL_NAMES = ["tend_fp64", "vi_fp64", "rk", "filter", "drhot2pres", "stage_mixed", "vi_mixed", "mlp", "aux",
+                "trc_fct", "trc_stage", "trc_aux"]
 
 
 class MeshDesc(ctypes.Structure):
@@ -54,6 +58,13 @@ class MeshDesc(ctypes.Structure):
         ("mf_etac_v", ctypes.c_double), ("mf_alpha_v", ctypes.c_double), ("mf_order_v", ctypes.c_int),
         ("device", ctypes.c_int),
     ]
+
+
+class TrcOpts(ctypes.Structure):
+    _fields_ = [("scheme", ctypes.c_int), ("dt", ctypes.c_double), ("nsteps", ctypes.c_int),
+                ("limiter", ctypes.c_int), ("tmar", ctypes.c_int), ("filter", ctypes.c_int),
+                ("mf_etac_h", ctypes.c_double), ("mf_alpha_h", ctypes.c_double), ("mf_order_h", ctypes.c_int),
+                ("mf_etac_v", ctypes.c_double), ("mf_alpha_v", ctypes.c_double), ("mf_order_v", ctypes.c_int)]
 
 
 class UpdateOpts(ctypes.Structure):
@@ -113,6 +124,16 @@ def load():
     lib.fedg_guess_loss_grad.argtypes = [_vp, _vp, _vp, ctypes.c_int, _fp, _fp]
     lib.fedg_guess_predict.argtypes = [_vp, _vp, _vp, ctypes.c_int]
     lib.fedg_guess_load.argtypes = [_vp, _vp]
+    _P3 = ctypes.c_void_p * 3
+    lib.fedg_trc_alphdens_advtest.argtypes = [_vp] + [_vp] * 6
+    lib.fedg_trc_save_massflux.argtypes = [_vp, ctypes.c_int, _P5, _vp, ctypes.c_double, ctypes.c_double,
+                                           ctypes.c_int, _P3, _vp, _vp]
+    lib.fedg_trc_fct_coef.argtypes = [_vp, _vp, _P3, _vp, _vp, _vp, _vp, _vp, ctypes.c_double, ctypes.c_double, _vp]
+    lib.fedg_trc_cal_tend.argtypes = [_vp, _vp, _P3, _vp, _vp, _vp, _vp, _vp]
+    lib.fedg_trc_tmar.argtypes = [_vp, _vp, _vp]
+    lib.fedg_trc_modalfilter.argtypes = [_vp, _vp, _vp, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                         ctypes.c_double, ctypes.c_double, ctypes.c_int]
+    lib.fedg_trc_update.argtypes = [_vp, _vp, _P3, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.POINTER(TrcOpts)]
     lib.fedg_prof_enable.argtypes = [_vp, ctypes.c_int]
     lib.fedg_prof_reset.argtypes = [_vp]
     lib.fedg_prof_read.argtypes = [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
@@ -160,7 +181,8 @@ class Context:
 
         fo = case.filter_on if filter_on is None else filter_on
         d = MeshDesc(case.porder, case.NeX, case.NeY, case.NeZ, xmin, xmax, ymin, ymax, zmin, zmax, 1, 1,
-                     GRAV, RDRY, CPDRY, CVDRY, PRES00, int(fo), 2.0 / 3.0, 36.0, 16, 2.0 / 3.0, 36.0, 16, device)
+                     getattr(case, "grav", GRAV), RDRY, CPDRY, CVDRY, PRES00, int(fo), 2.0 / 3.0, 36.0, 16,
+                     2.0 / 3.0, 36.0, 16, device)
         h = _vp()
         _check(self.lib.fedg_ctx_create(ctypes.byref(d), ctypes.byref(h)), "fedg_ctx_create")
         self.h = h
@@ -254,6 +276,79 @@ class Context:
         if sync:
             self.sync()
         return nfail, float(mi.value)
+
+    # -- tracer advection (trcadvect3d_heve.F90, driver_trcadv3d.F90) --
+    @property
+    def face_shape(self):
+        return (self.case.Ne, 6, self.case.N1 * self.case.N1)
+
+    def empty_face(self):
+        return self.torch.empty(self.face_shape, dtype=self.torch.float64, device=self.dev)
+
+    def trc_alphdens_advtest(self, ddens, momx, momy, momz):
+        aM, aP = self.empty_face(), self.empty_face()
+        self.torch.cuda.synchronize()
+        _check(self.lib.fedg_trc_alphdens_advtest(self.h, _ptr(ddens), _ptr(momx), _ptr(momy), _ptr(momz), _ptr(aM),
+                                                  _ptr(aP)), "fedg_trc_alphdens_advtest")
+        self.sync()
+        return aM, aP
+
+    def trc_save_massflux(self, rkstage, q, w_h, w_v, is_hevi, mflx, aM, aP, dpres=None):
+        self.torch.cuda.synchronize()
+        _check(self.lib.fedg_trc_save_massflux(self.h, int(rkstage), _p5(q), _ptr(dpres), float(w_h), float(w_v),
+                                               int(is_hevi), (ctypes.c_void_p * 3)(*[m.data_ptr() for m in mflx]),
+                                               _ptr(aM), _ptr(aP)), "fedg_trc_save_massflux")
+        self.sync()
+
+    def trc_fct_coef(self, Q, mflx, aM, aP, ddens, ddens0, c_ssm1, dt, rhoq_tp=None):
+        fct = self.empty()
+        self.torch.cuda.synchronize()
+        _check(self.lib.fedg_trc_fct_coef(self.h, _ptr(Q), (ctypes.c_void_p * 3)(*[m.data_ptr() for m in mflx]),
+                                          _ptr(rhoq_tp), _ptr(aM), _ptr(aP), _ptr(ddens), _ptr(ddens0),
+                                          float(c_ssm1), float(dt), _ptr(fct)), "fedg_trc_fct_coef")
+        self.sync()
+        return fct
+
+    def trc_cal_tend(self, Q, mflx, aM, aP, fct=None, rhoq_tp=None):
+        out = self.empty()
+        self.torch.cuda.synchronize()
+        _check(self.lib.fedg_trc_cal_tend(self.h, _ptr(Q), (ctypes.c_void_p * 3)(*[m.data_ptr() for m in mflx]),
+                                          _ptr(aM), _ptr(aP), _ptr(fct), _ptr(rhoq_tp), _ptr(out)),
+               "fedg_trc_cal_tend")
+        self.sync()
+        return out
+
+    def trc_tmar(self, Q, ddens):
+        self.torch.cuda.synchronize()
+        _check(self.lib.fedg_trc_tmar(self.h, _ptr(Q), _ptr(ddens)), "fedg_trc_tmar")
+        self.sync()
+        return Q
+
+    def trc_modalfilter(self, Q, ddens, etac_h=2.0 / 3.0, alpha_h=36.0, ord_h=16, etac_v=2.0 / 3.0, alpha_v=36.0,
+                        ord_v=16):
+        self.torch.cuda.synchronize()
+        _check(self.lib.fedg_trc_modalfilter(self.h, _ptr(Q), _ptr(ddens), float(etac_h), float(alpha_h), int(ord_h),
+                                             float(etac_v), float(alpha_v), int(ord_v)), "fedg_trc_modalfilter")
+        self.sync()
+        return Q
+
+    def trc_update(self, Q, mflx, aM, aP, ddens_trc, ddens0_trc, dt, nsteps=1, ddens=None, rhoq_tp=None,
+                   limiter=True, tmar=True, filter=None, sync=True):
+        """nsteps tracer steps in place on Q (ERK_SSP_3s3o); filter = None or a dict of the six tracer
+        filter parameters (etac_h, alpha_h, ord_h, etac_v, alpha_v, ord_v)."""
+        fp = dict(etac_h=2.0 / 3.0, alpha_h=36.0, ord_h=16, etac_v=2.0 / 3.0, alpha_v=36.0, ord_v=16)
+        if filter:
+            fp.update(filter)
+        o = TrcOpts(SSP_RK3, float(dt), int(nsteps), int(bool(limiter)), int(bool(tmar)), int(bool(filter)),
+                    fp["etac_h"], fp["alpha_h"], int(fp["ord_h"]), fp["etac_v"], fp["alpha_v"], int(fp["ord_v"]))
+        if sync:
+            self.torch.cuda.synchronize()
+        _check(self.lib.fedg_trc_update(self.h, _ptr(Q), (ctypes.c_void_p * 3)(*[m.data_ptr() for m in mflx]),
+                                        _ptr(aM), _ptr(aP), _ptr(ddens_trc), _ptr(ddens0_trc), _ptr(ddens),
+                                        _ptr(rhoq_tp), ctypes.byref(o)), "fedg_trc_update")
+        if sync:
+            self.sync()
+        return Q
 
 
 def prof_enable(ctx, on=True):

@@ -28,6 +28,7 @@ module scale_atm_dyn_dgm_nonhydro3d_gb300
   public :: atm_dyn_dgm_nonhydro3d_gb300_cal_tend_heve
   public :: atm_dyn_dgm_nonhydro3d_gb300_cal_tend_hevi
   public :: atm_dyn_dgm_nonhydro3d_gb300_cal_vi
+  public :: atm_dyn_dgm_nonhydro3d_gb300_ctx
 
   integer(c_int), parameter :: FEDG_HEVE = 0, FEDG_HEVI = 1
 
@@ -99,6 +100,12 @@ contains
     if (present(max_iter)) vi_max_iter = max_iter
     if (present(tol)) vi_tol = tol
   end subroutine atm_dyn_dgm_nonhydro3d_gb300_Init
+
+  !> the library context (shared with the tracer-advection shim)
+  function atm_dyn_dgm_nonhydro3d_gb300_ctx() result(c)
+    type(c_ptr) :: c
+    c = ctx
+  end function atm_dyn_dgm_nonhydro3d_gb300_ctx
 
   subroutine atm_dyn_dgm_nonhydro3d_gb300_Final()
     if (c_associated(ctx)) call fedg_ctx_destroy(ctx)

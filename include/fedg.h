@@ -180,6 +180,63 @@ int fedg_guess_predict(fedg_guess* g, const float* X, float* Y, int n);
 /* attach (g != NULL) or detach (g == NULL) the network used by fedg_update(use_guess = 1) */
 int fedg_guess_load(fedg_ctx* ctx, fedg_guess* g);
 
+/* ---- Tracer advection -------------------------------------------------------------------
+ * HEVE DG transport of a tracer mixing ratio q by a mass flux, with the nonnegativity limiter of
+ * Light and Durran (2016): FCT on the lowest mode, then truncation and mass-aware rescaling (TMAR).
+ * FElib/src/fluid_dyn_solver/scale_atm_dyn_dgm_trcadvect3d_heve.F90 and the tracer driver
+ * ..._driver_trcadv3d.F90.  FP64, device pointers in FElib layout like every other entry point;
+ * the base state (DENS_hyd) must be registered with fedg_set_base_state.
+ *   mflx[3]        = MFLX_x_tavg, MFLX_y_tavg, MFLX_z_tavg (Np, NeA)
+ *   alph_M/alph_P  = alphaDensM/P face values (NfpTot, Ne): face f = 1..6 (south, east, north,
+ *                    west, bottom, top), face node i + (k-1) N1 on the lateral faces and
+ *                    i + (j-1) N1 on the bottom/top faces
+ *   fct_coef       = AUX_TRCVARS3D TRCADV_FCTCOEF (Np, NeA), one value per element */
+
+/* atm_dyn_dgm_trcadvect3d_heve_cal_alphdens_advtest (trcadvect3d_heve.F90:404-455): the Rusanov
+ * coefficients of the advection test (ONLY_TRACERADV_FLAG), max(|v_n-|, |v_n+|) dens on each side. */
+int fedg_trc_alphdens_advtest(fedg_ctx* ctx, const double* DDENS, const double* MOMX, const double* MOMY,
+                              const double* MOMZ, double* alph_M, double* alph_P);
+/* atm_dyn_dgm_trcadvect3d_save_massflux (trcadvect3d_heve.F90:343-401, called from the dynamics
+ * stage loop, driver_nonhydro3d.F90:900-917): rkstage 1 sets, later stages add
+ * MFLX += w_h (MOMX, MOMY), w_v MOMZ and the dynamics' Rusanov coefficients
+ * (w_h (|nx|+|ny|) + w_v |nz|) alpha dens (cal_alphdens_dyn, :460-551).
+ *   q[5] = DDENS, MOMX, MOMY, MOMZ, DRHOT; DPRES may be NULL (formed from DRHOT). */
+int fedg_trc_save_massflux(fedg_ctx* ctx, int rkstage, const double* const q[5], const double* DPRES, double w_h,
+                           double w_v, int is_hevi, double* const mflx[3], double* alph_M, double* alph_P);
+/* atm_dyn_dgm_trcadvect3d_heve_calc_fct_coef (trcadvect3d_heve.F90:234-306).  RHOQ_tp may be NULL. */
+int fedg_trc_fct_coef(fedg_ctx* ctx, const double* QTRC, const double* const mflx[3], const double* RHOQ_tp,
+                      const double* alph_M, const double* alph_P, const double* DDENS_TRC,
+                      const double* DDENS0_TRC, double rk_c_ssm1, double dt, double* fct_coef);
+/* atm_dyn_dgm_trcadvect3d_heve_cal_tend (trcadvect3d_heve.F90:149-231): QTRC_dt = d(dens q)/dt.
+ * fct_coef NULL means no limiter (coefficient 1); RHOQ_tp may be NULL. */
+int fedg_trc_cal_tend(fedg_ctx* ctx, const double* QTRC, const double* const mflx[3], const double* alph_M,
+                      const double* alph_P, const double* fct_coef, const double* RHOQ_tp, double* QTRC_dt);
+/* atm_dyn_dgm_trcadvect3d_TMAR (trcadvect3d_heve.F90:311-340), in place; DDENS = DDENS_TRC. */
+int fedg_trc_tmar(fedg_ctx* ctx, double* QTRC, const double* DDENS);
+/* atm_dyn_dgm_tracer_modalfilter_apply (dgm_modalfilter.F90:232-270) with the tracer filter
+ * parameters (&PARAM_ATMOS_DYN_TRACER_MODALFILTER, driver_trcadv3d.F90:720-765), in place. */
+int fedg_trc_modalfilter(fedg_ctx* ctx, double* QTRC, const double* DDENS, double etac_h, double alpha_h,
+                         int order_h, double etac_v, double alpha_v, int order_v);
+/* AtmDynDGMDriver_trcadv3d_update for one tracer (driver_trcadv3d.F90:420-545): nsteps tracer
+ * steps with the mass flux, Rusanov coefficients and densities held fixed.  Each stage: the FCT
+ * coefficient (limiter), the tendency and the density-weighted low-storage advance
+ * (rk_advance_trcvar_low_storage2D, timeint_rk.F90:1390-1498); after the last stage the tracer
+ * filter (filter), TMAR (limiter && tmar: FElib's ONLY_TRACERADV_FLAG) and the rescale
+ * QTRC = (DENS_hyd + DDENS_TRC) / (DENS_hyd + DDENS) QTRC (DDENS NULL: DDENS_TRC).  In place on QTRC. */
+typedef struct {
+  int scheme;          /* FEDG_SSP_RK3 (ERK_SSP_3s3o, FElib's default TINTEG_TYPE_TRACER) */
+  double dt;
+  int nsteps;
+  int limiter;         /* !TRACERADV_DISABLE_LIMITER */
+  int tmar;
+  int filter;          /* MODALFILTER_FLAG */
+  double mf_etac_h, mf_alpha_h; int mf_order_h;
+  double mf_etac_v, mf_alpha_v; int mf_order_v;
+} fedg_trc_opts;
+int fedg_trc_update(fedg_ctx* ctx, double* QTRC, const double* const mflx[3], const double* alph_M,
+                    const double* alph_P, const double* DDENS_TRC, const double* DDENS0_TRC, const double* DDENS,
+                    const double* RHOQ_tp, const fedg_trc_opts* opts);
+
 /* Kernel timers: the analogue of FElib's PROF_rapstart/PROF_rapend regions
  * (e.g. 'ATM_DYN_cal_vi', 'cal_dyn_tend_interior'; scale_prof of the SCALE library).
  * When enabled, every launch of the context records a pair of CUDA events on the context
@@ -195,7 +252,10 @@ enum {
   FEDG_K_MVI = 6,       /* mixed-precision column solve                             */
   FEDG_K_MLP = 7,       /* column-guess network (inference / training)              */
   FEDG_K_AUX = 8,       /* status reductions, base-state checks                     */
-  FEDG_K_COUNT = 9
+  FEDG_K_TRC_FCT = 9,   /* tracer FCT coefficient (calc_fct_coef)                   */
+  FEDG_K_TRC_TEND = 10, /* tracer tendency + RK stage (cal_tend, Advance_trcvar)    */
+  FEDG_K_TRC_AUX = 11,  /* tracer Rusanov coefficients, mass flux, TMAR, filter     */
+  FEDG_K_COUNT = 12
 };
 int fedg_prof_enable(fedg_ctx* ctx, int on);
 int fedg_prof_reset(fedg_ctx* ctx);

@@ -26,6 +26,8 @@
 //   * SSP-RK3 / IMEX ARK232    FElib/src/common/scale_timeint_rk.F90:1182-1278, 2201-2565
 //                              FElib/src/common/scale_timeint_rk_butcher_tab.F90:200-274
 //   * driver stage loop        ..._driver_nonhydro3d.F90:614-963
+//   * tracer advection (FCT + TMAR, mass-flux averaging, tracer RK, tracer filter)
+//                              ..._trcadvect3d_heve.F90, ..._driver_trcadv3d.F90:330-560
 //
 // Layout: every field is column-major (Np, Ne) like FElib, node n = i + N1*j + N1^2*k,
 // element ke = ex + NeX*ey + NeX*NeY*ez.  Exterior (halo) values are produced in place
@@ -823,6 +825,359 @@ static long cal_vi(const Oracle& o, const double* const q[5], const double* cons
   return nfail;
 }
 
+// ---------------------------------------------------------------------------------
+// Tracer advection: HEVE DG transport of a mixing ratio by a (time-averaged) mass flux, with the
+// nonnegativity limiter of Light and Durran (2016): FCT on the lowest mode, then truncation and
+// mass-aware rescaling (TMAR).
+//   alphDens (advection test)  FElib/src/fluid_dyn_solver/scale_atm_dyn_dgm_trcadvect3d_heve.F90:404-455
+//   save_massflux + alphDens   ..._trcadvect3d_heve.F90:343-401, 460-551
+//   FCT coefficient            ..._trcadvect3d_heve.F90:234-306, net outward flux :678-777
+//   cal_tend + del_flux        ..._trcadvect3d_heve.F90:149-231, 554-674
+//   TMAR                       ..._trcadvect3d_heve.F90:311-340
+//   face integration weights   ..._trcadvect3d_heve.F90:75-137
+//   tracer modal filter        ..._dgm_modalfilter.F90:232-270
+//   tracer RK (low storage)    FElib/src/common/scale_timeint_rk.F90:1390-1498
+//   driver (one tracer)        ..._driver_trcadv3d.F90:420-545
+// Flat cube: Gsqrt = GsqrtH = 1, G13 = G23 = 0, G11 = G22 = 1, J = dx dy dz / 8, and
+// J * Fscale = the face Jacobian (dy dz / 4 on x faces, ...).  Face-node arrays are FElib's
+// (NfpTot, Ne): face f, node a + N1*b (the face_node order above).  At a slip lid the exterior
+// node is the element's own node with the vertical mass flux / momentum reflected.
+// ---------------------------------------------------------------------------------
+struct TrcFilter {
+  std::vector<double> Fh, Fv;  // 1D tracer modal filters (horizontal, vertical)
+};
+
+static void exp_filter_matrix(const Elem1D& e, double etac, double alpha, int ord, std::vector<double>& F) {
+  const int N1 = e.N1, N = e.N;
+  std::vector<double> sig(N1, 1.0);
+  for (int m = 0; m < N1; ++m) {
+    const double eta = double(m) / double(N);
+    if (eta > etac && m != 0) sig[m] = std::exp(-alpha * std::pow((eta - etac) / (1.0 - etac), ord));
+  }
+  F.assign(N1 * N1, 0.0);
+  for (int i = 0; i < N1; ++i)
+    for (int j = 0; j < N1; ++j) {
+      double s = 0.0;
+      for (int m = 0; m < N1; ++m) s += e.V[i * N1 + m] * sig[m] * e.invV[m * N1 + j];
+      F[i * N1 + j] = s;
+    }
+}
+
+// exterior node of face node (f, a, b) of element ke; lid = slip lid (own node, reflected)
+static inline size_t ext_node(const Oracle& o, long ke, int f, int a, int b, bool& lid) {
+  const int ex = (int)(ke % o.NeX), ey = (int)((ke / o.NeX) % o.NeY), ez = (int)(ke / ((long)o.NeX * o.NeY));
+  const long kn = neighbour(o, ex, ey, ez, f);
+  int i, j, k;
+  if (kn >= 0) {
+    lid = false;
+    face_node(o.N1, opposite_face(f), a, b, i, j, k);
+    return (size_t)kn * o.Np + o.nid(i, j, k);
+  }
+  lid = true;
+  face_node(o.N1, f, a, b, i, j, k);
+  return (size_t)ke * o.Np + o.nid(i, j, k);
+}
+
+// cal_alphdens_advtest: alph_dens = max(|v_n^-|, |v_n^+|) * dens * Gsqrt on each side
+static void trc_alphdens_advtest(const Oracle& o, const double* ddens, const double* momx, const double* momy,
+                                 const double* momz, double* aM, double* aP) {
+  const int N1 = o.N1, Nfp = o.Nfp;
+#pragma omp parallel for schedule(static)
+  for (long ke = 0; ke < o.Ne; ++ke)
+    for (int f = 0; f < 6; ++f)
+      for (int b = 0; b < N1; ++b)
+        for (int a = 0; a < N1; ++a) {
+          int i, j, k; face_node(N1, f, a, b, i, j, k);
+          const size_t iM = (size_t)ke * o.Np + o.nid(i, j, k);
+          bool lid; const size_t iP = ext_node(o, ke, f, a, b, lid);
+          const double densM = ddens[iM] + o.dens_hyd[iM], densP = ddens[iP] + o.dens_hyd[iP];
+          const double mzP = lid ? -momz[iP] : momz[iP];
+          const double velM = (momx[iM] * NX[f] + momy[iM] * NY[f] + momz[iM] * NZ[f]) / densM;
+          const double velP = (momx[iP] * NX[f] + momy[iP] * NY[f] + mzP * NZ[f]) / densP;
+          const double alpha = std::max(std::fabs(velM), std::fabs(velP));
+          const size_t fi = (size_t)ke * 6 * Nfp + f * Nfp + a + N1 * b;
+          aM[fi] = alpha * densM;
+          aP[fi] = alpha * densP;
+        }
+}
+
+// save_massflux: time average of the mass flux over the dynamics RK stages and of the Rusanov
+// coefficient of the dynamics (alphdens_dyn), weights w_h (horizontal) and w_v (vertical)
+static void trc_save_massflux(const Oracle& o, int rkstage, const double* const q[5], const double* dpres,
+                              double w_h, double w_v, int is_hevi, double* const mflx[3], double* aM, double* aP) {
+  const int N1 = o.N1, Nfp = o.Nfp;
+  const size_t n = (size_t)o.Np * o.Ne;
+  const double gamm = o.c.cpdry / o.c.cvdry;
+#pragma omp parallel for schedule(static)
+  for (size_t p = 0; p < n; ++p) {
+    if (rkstage == 1) {
+      mflx[0][p] = w_h * q[VMX][p]; mflx[1][p] = w_h * q[VMY][p]; mflx[2][p] = w_v * q[VMZ][p];
+    } else {
+      mflx[0][p] += w_h * q[VMX][p]; mflx[1][p] += w_h * q[VMY][p]; mflx[2][p] += w_v * q[VMZ][p];
+    }
+  }
+#pragma omp parallel for schedule(static)
+  for (long ke = 0; ke < o.Ne; ++ke)
+    for (int f = 0; f < 6; ++f)
+      for (int b = 0; b < N1; ++b)
+        for (int a = 0; a < N1; ++a) {
+          int i, j, k; face_node(N1, f, a, b, i, j, k);
+          const size_t iM = (size_t)ke * o.Np + o.nid(i, j, k);
+          bool lid; const size_t iP = ext_node(o, ke, f, a, b, lid);
+          const double nx = NX[f], ny = NY[f], nz = NZ[f];
+          const double densM = q[VD][iM] + o.dens_hyd[iM], densP = q[VD][iP] + o.dens_hyd[iP];
+          const double gnn = std::fabs(nx) + std::fabs(ny) + (is_hevi ? 0.0 : std::fabs(nz));
+          const double mzP = lid ? -q[VMZ][iP] : q[VMZ][iP];
+          const double velM = (q[VMX][iM] * nx + q[VMY][iM] * ny + q[VMZ][iM] * nz) / densM;
+          const double velP = (q[VMX][iP] * nx + q[VMY][iP] * ny + mzP * nz) / densP;
+          const double alpha = std::max(std::sqrt(gnn * gamm * (o.pres_hyd[iM] + dpres[iM]) / densM) + std::fabs(velM),
+                                        std::sqrt(gnn * gamm * (o.pres_hyd[iP] + dpres[iP]) / densP) + std::fabs(velP));
+          const double tw = w_h * (std::fabs(nx) + std::fabs(ny)) + w_v * std::fabs(nz);
+          const size_t fi = (size_t)ke * 6 * Nfp + f * Nfp + a + N1 * b;
+          if (rkstage == 1) { aM[fi] = 0.0; aP[fi] = 0.0; }
+          aM[fi] += tw * alpha * densM;
+          aP[fi] += tw * alpha * densP;
+        }
+}
+
+// Rusanov numerical flux of the tracer at every face node of element ke, the outward normal mass
+// flux of the interior side, and the face integrals of J*Fscale*numflux (FaceIntMat)
+static void trc_face(const Oracle& o, long ke, const double* Q, const double* const mflx[3], const double* aM,
+                     const double* aP, double* numflux, double* momflxM, double* outflux) {
+  const int N1 = o.N1, Nfp = o.Nfp;
+  const double J = o.dx * o.dy * o.dz / 8.0;
+  const double FS[6] = {2.0 / o.dy, 2.0 / o.dx, 2.0 / o.dy, 2.0 / o.dx, 2.0 / o.dz, 2.0 / o.dz};
+  const std::vector<double>& w = o.e.w;
+  for (int f = 0; f < 6; ++f) {
+    double s = 0.0;
+    for (int b = 0; b < N1; ++b)
+      for (int a = 0; a < N1; ++a) {
+        int i, j, k; face_node(N1, f, a, b, i, j, k);
+        const size_t iM = (size_t)ke * o.Np + o.nid(i, j, k);
+        bool lid; const size_t iP = ext_node(o, ke, f, a, b, lid);
+        const double mzP = lid ? -mflx[2][iP] : mflx[2][iP];
+        const double mfM = mflx[0][iM] * NX[f] + mflx[1][iM] * NY[f] + mflx[2][iM] * NZ[f];
+        const double mfP = mflx[0][iP] * NX[f] + mflx[1][iP] * NY[f] + mzP * NZ[f];
+        const int fp = f * Nfp + a + N1 * b;
+        const size_t fi = (size_t)ke * 6 * Nfp + fp;
+        const double qM = Q[iM], qP = Q[iP];
+        const double nf = 0.5 * ((qP * mfP + qM * mfM) - aP[fi] * qP + aM[fi] * qM);
+        numflux[fp] = nf;
+        momflxM[fp] = mfM;
+        s += w[a] * w[b] * (J * FS[f] * nf);
+      }
+    outflux[f] = s;
+  }
+}
+
+// calc_fct_coef: the largest fraction of the element's outflow its own mass can supply in one
+// stage, written to all Np nodes of the element (a nodal field, as in FElib)
+static void trc_fct_coef(const Oracle& o, const double* Q, const double* const mflx[3], const double* rhoq_tp,
+                         const double* aM, const double* aP, const double* ddens, const double* ddens0, double c_ssm1,
+                         double dt, double* fct) {
+  const int N1 = o.N1, Np = o.Np, Nfp = o.Nfp;
+  const double J = o.dx * o.dy * o.dz / 8.0;
+  const std::vector<double>& w = o.e.w;
+#pragma omp parallel
+  {
+    std::vector<double> nf(6 * Nfp), mf(6 * Nfp);
+    double out[6];
+#pragma omp for schedule(static)
+    for (long ke = 0; ke < o.Ne; ++ke) {
+      trc_face(o, ke, Q, mflx, aM, aP, nf.data(), mf.data(), out);
+      double net = 0.0;
+      for (int f = 0; f < 6; ++f) net += std::max(0.0, out[f]);
+      double qe = 0.0;
+      for (int k = 0; k < N1; ++k)
+        for (int j = 0; j < N1; ++j)
+          for (int i = 0; i < N1; ++i) {
+            const size_t g = (size_t)ke * Np + o.nid(i, j, k);
+            const double dens = o.dens_hyd[g] + (1.0 - c_ssm1) * ddens0[g] + c_ssm1 * ddens[g];
+            qe += J * (w[i] * w[j] * w[k]) * (dens * Q[g] / dt + (rhoq_tp ? rhoq_tp[g] : 0.0));
+          }
+      const double r = std::max(0.0, std::min(1.0, qe / (net + 1.0e-10)));
+      for (int p = 0; p < Np; ++p) fct[(size_t)ke * Np + p] = r;
+    }
+  }
+}
+
+// cal_tend with the FCT-limited del_flux: d(dens q)/dt.  fct is the nodal coefficient field; the
+// face value on each side is read at the face node (at a lid both sides are the element's own node)
+static void trc_cal_tend(const Oracle& o, const double* Q, const double* const mflx[3], const double* aM,
+                         const double* aP, const double* fct, const double* rhoq_tp, double* Qdt) {
+  const int N1 = o.N1, Np = o.Np, Nfp = o.Nfp, N = N1 - 1;
+  const double E11 = 2.0 / o.dx, E22 = 2.0 / o.dy, E33 = 2.0 / o.dz;
+  const double FS[6] = {2.0 / o.dy, 2.0 / o.dx, 2.0 / o.dy, 2.0 / o.dx, 2.0 / o.dz, 2.0 / o.dz};
+  const std::vector<double>& D = o.e.D;
+  const std::vector<double>& Mi = o.e.Minv;
+#pragma omp parallel
+  {
+    std::vector<double> nf(6 * Nfp), mf(6 * Nfp), delf(6 * Nfp), fl(3 * (size_t)Np);
+    double out[6];
+#pragma omp for schedule(static)
+    for (long ke = 0; ke < o.Ne; ++ke) {
+      trc_face(o, ke, Q, mflx, aM, aP, nf.data(), mf.data(), out);
+      for (int f = 0; f < 6; ++f) {
+        // 0.5 (R+ + R- - (R+ - R-) sign(1, outflux)): R- on outflow faces, R+ on inflow faces
+        const double sg = std::signbit(out[f]) ? -1.0 : 1.0;
+        for (int b = 0; b < N1; ++b)
+          for (int a = 0; a < N1; ++a) {
+            int i, j, k; face_node(N1, f, a, b, i, j, k);
+            const size_t iM = (size_t)ke * Np + o.nid(i, j, k);
+            bool lid; const size_t iP = ext_node(o, ke, f, a, b, lid);
+            const double RM = fct[iM], RP = fct[iP];
+            const int fp = f * Nfp + a + N1 * b;
+            delf[fp] = FS[f] * (nf[fp] * (0.5 * (RP + RM - (RP - RM) * sg)) - Q[iM] * mf[fp]);
+          }
+      }
+      for (int p = 0; p < Np; ++p) {
+        const size_t g = (size_t)ke * Np + p;
+        fl[p] = mflx[0][g] * Q[g];
+        fl[Np + p] = mflx[1][g] * Q[g];
+        fl[2 * Np + p] = mflx[2][g] * Q[g];
+      }
+      for (int k = 0; k < N1; ++k)
+        for (int j = 0; j < N1; ++j)
+          for (int i = 0; i < N1; ++i) {
+            double sx = 0, sy = 0, sz = 0;
+            for (int l = 0; l < N1; ++l) {
+              sx += D[i * N1 + l] * fl[o.nid(l, j, k)];
+              sy += D[j * N1 + l] * fl[Np + o.nid(i, l, k)];
+              sz += D[k * N1 + l] * fl[2 * Np + o.nid(i, j, l)];
+            }
+            const double lf = Mi[j * N1 + 0] * delf[0 * Nfp + i + N1 * k] + Mi[i * N1 + N] * delf[1 * Nfp + j + N1 * k] +
+                              Mi[j * N1 + N] * delf[2 * Nfp + i + N1 * k] + Mi[i * N1 + 0] * delf[3 * Nfp + j + N1 * k] +
+                              Mi[k * N1 + 0] * delf[4 * Nfp + i + N1 * j] + Mi[k * N1 + N] * delf[5 * Nfp + i + N1 * j];
+            const size_t g = (size_t)ke * Np + o.nid(i, j, k);
+            Qdt[g] = -(E11 * sx + E22 * sy + E33 * sz + lf) + (rhoq_tp ? rhoq_tp[g] : 0.0);
+          }
+    }
+  }
+}
+
+// TMAR: truncate negative values, rescale to keep the element's tracer mass
+static void trc_tmar(const Oracle& o, double* Q, const double* ddens) {
+  const int N1 = o.N1, Np = o.Np;
+  const std::vector<double>& w = o.e.w;
+  const double J = o.dx * o.dy * o.dz / 8.0;
+#pragma omp parallel for schedule(static)
+  for (long ke = 0; ke < o.Ne; ++ke) {
+    double q0 = 0.0, q1 = 0.0;
+    for (int k = 0; k < N1; ++k)
+      for (int j = 0; j < N1; ++j)
+        for (int i = 0; i < N1; ++i) {
+          const size_t g = (size_t)ke * Np + o.nid(i, j, k);
+          const double wd = J * (w[i] * w[j] * w[k]) * (o.dens_hyd[g] + ddens[g]);
+          q0 += wd * Q[g];
+          q1 += wd * std::max(0.0, Q[g]);
+        }
+    const double r = q0 / (q1 + 1.0e-32);
+    for (int p = 0; p < Np; ++p) {
+      const size_t g = (size_t)ke * Np + p;
+      Q[g] = r * std::max(0.0, Q[g]);
+    }
+  }
+}
+
+// tracer modal filter: Q <- F(dens Q) / dens with dens = Gsqrt (DENS_hyd + DDENS)
+static void trc_filter(const Oracle& o, const TrcFilter& tf, double* Q, const double* ddens) {
+  const int N1 = o.N1, Np = o.Np;
+#pragma omp parallel
+  {
+    std::vector<double> a(Np), b(Np), wt(Np);
+#pragma omp for schedule(static)
+    for (long ke = 0; ke < o.Ne; ++ke) {
+      double* x = Q + (size_t)ke * Np;
+      for (int p = 0; p < Np; ++p) {
+        const size_t g = (size_t)ke * Np + p;
+        wt[p] = o.dens_hyd[g] + ddens[g];
+        b[p] = wt[p] * x[p];
+      }
+      for (int k = 0; k < N1; ++k)
+        for (int j = 0; j < N1; ++j)
+          for (int i = 0; i < N1; ++i) {
+            double s = 0;
+            for (int l = 0; l < N1; ++l) s += tf.Fh[i * N1 + l] * b[o.nid(l, j, k)];
+            a[o.nid(i, j, k)] = s;
+          }
+      for (int k = 0; k < N1; ++k)
+        for (int j = 0; j < N1; ++j)
+          for (int i = 0; i < N1; ++i) {
+            double s = 0;
+            for (int l = 0; l < N1; ++l) s += tf.Fh[j * N1 + l] * a[o.nid(i, l, k)];
+            b[o.nid(i, j, k)] = s;
+          }
+      for (int k = 0; k < N1; ++k)
+        for (int j = 0; j < N1; ++j)
+          for (int i = 0; i < N1; ++i) {
+            double s = 0;
+            for (int l = 0; l < N1; ++l) s += tf.Fv[k * N1 + l] * b[o.nid(i, j, l)];
+            x[o.nid(i, j, k)] = s / wt[o.nid(i, j, k)];
+          }
+    }
+  }
+}
+
+// One tracer time step of the tracer driver with a low-storage explicit RK scheme given by its
+// Shu-Osher coefficients sig(s+1, s'), gam(s+1, s') (row-major [(nstage+1) x nstage], rows 1..nstage
+// used) and nodes c(s): the FCT coefficient, the tendency, the density-weighted advance
+// (rk_advance_trcvar_low_storage), then after the last stage the tracer filter and TMAR, and the
+// final rescale QTRC = (DENS_hyd + DDENS_TRC) / (DENS_hyd + DDENS) QTRC_tmp.
+struct TrcStepArgs {
+  int nstage;
+  const double* sig;  // [(nstage+1)*nstage]
+  const double* gam;
+  const double* c;    // [nstage]
+  double dt;
+  int limiter, tmar, filter;
+};
+
+static void trc_step(const Oracle& o, const TrcFilter& tf, const TrcStepArgs& A, double* QTRC,
+                     const double* const mflx[3], const double* aM, const double* aP, const double* ddens_trc,
+                     const double* ddens0_trc, const double* ddens, const double* rhoq_tp) {
+  const size_t n = (size_t)o.Np * o.Ne;
+  const int ns = A.nstage;
+  auto SIG = [&](int r, int s) { return A.sig[(size_t)(r - 1) * ns + (s - 1)]; };  // 1-based (row, col)
+  auto GAM = [&](int r, int s) { return A.gam[(size_t)(r - 1) * ns + (s - 1)]; };
+  std::vector<double> q(QTRC, QTRC + n), var0(n), vtmp(n), tend(n), fct(n, 1.0);
+  for (int s = 1; s <= ns; ++s) {
+    const double c_ssm1 = A.c[s - 1];
+    if (A.limiter) {
+      const double dttmp = A.dt * GAM(s + 1, s) / SIG(s + 1, s);
+      trc_fct_coef(o, q.data(), mflx, rhoq_tp, aM, aP, ddens_trc, ddens0_trc, c_ssm1, dttmp, fct.data());
+    }
+    trc_cal_tend(o, q.data(), mflx, aM, aP, fct.data(), rhoq_tp, tend.data());
+    const double sig_ss = SIG(s + 1, s), gam_ss = A.dt * GAM(s + 1, s);
+    if (s == ns) {
+#pragma omp parallel for
+      for (size_t p = 0; p < n; ++p) {
+        const double d0 = o.dens_hyd[p] + ddens0_trc[p];
+        const double dssm1 = d0 + c_ssm1 * (ddens_trc[p] - ddens0_trc[p]);
+        q[p] = (vtmp[p] + sig_ss * q[p] * dssm1 + gam_ss * tend[p]) / (o.dens_hyd[p] + ddens_trc[p]);
+      }
+    } else {
+      const double sig_Ns = SIG(ns + 1, s), gam_Ns = A.dt * GAM(ns + 1, s);
+      const double c_ss = A.c[s];
+      const bool acc = std::fabs(sig_Ns) > 1.0e-16 || std::fabs(gam_Ns) > 1.0e-16;  // CONST_EPS
+#pragma omp parallel for
+      for (size_t p = 0; p < n; ++p) {
+        const double d0 = o.dens_hyd[p] + ddens0_trc[p];
+        if (s == 1) { var0[p] = q[p] * d0; vtmp[p] = 0.0; }
+        const double dssm1 = d0 + c_ssm1 * (ddens_trc[p] - ddens0_trc[p]);
+        const double dss = d0 + c_ss * (ddens_trc[p] - ddens0_trc[p]);
+        if (acc) vtmp[p] = vtmp[p] + sig_Ns * q[p] * dssm1 + gam_Ns * tend[p];
+        q[p] = ((1.0 - sig_ss) * var0[p] + sig_ss * q[p] * dssm1 + gam_ss * tend[p]) / dss;
+      }
+    }
+  }
+  if (A.filter) trc_filter(o, tf, q.data(), ddens_trc);
+  if (A.limiter && A.tmar) trc_tmar(o, q.data(), ddens_trc);
+  const double* dd = ddens ? ddens : ddens_trc;
+#pragma omp parallel for
+  for (size_t p = 0; p < n; ++p)
+    QTRC[p] = (o.dens_hyd[p] + ddens_trc[p]) / (o.dens_hyd[p] + dd[p]) * q[p];
+}
+
 }  // namespace
 
 // =================================================================================
@@ -1024,6 +1379,55 @@ long orc_step_hevi(void* h, double* const* q, double dt, int nsteps, int max_ite
   }
   if (mean_iters) *mean_iters = itcnt ? itsum / itcnt : 0.0;
   return nfail;
+}
+
+
+// ---- tracer advection ----
+// face-node arrays are (NfpTot, Ne); mflx = {MFLX_x, MFLX_y, MFLX_z}; fct is a nodal (Np, Ne) field
+void orc_trc_alphdens_advtest(void* h, const double* ddens, const double* momx, const double* momy,
+                              const double* momz, double* aM, double* aP) {
+  trc_alphdens_advtest(*static_cast<Oracle*>(h), ddens, momx, momy, momz, aM, aP);
+}
+// q = {DDENS, MOMX, MOMY, MOMZ, DRHOT}; dpres may be NULL (formed from DRHOT)
+void orc_trc_save_massflux(void* h, int rkstage, const double* const* q, const double* dpres, double w_h,
+                           double w_v, int is_hevi, double* const* mflx, double* aM, double* aP) {
+  Oracle* o = static_cast<Oracle*>(h);
+  std::vector<double> dp;
+  if (!dpres) { dp.resize((size_t)o->Np * o->Ne); drhot2pres(*o, q[VRT], nullptr, dp.data()); dpres = dp.data(); }
+  trc_save_massflux(*o, rkstage, q, dpres, w_h, w_v, is_hevi, mflx, aM, aP);
+}
+void orc_trc_fct_coef(void* h, const double* Q, const double* const* mflx, const double* rhoq_tp, const double* aM,
+                      const double* aP, const double* ddens, const double* ddens0, double c_ssm1, double dt,
+                      double* fct) {
+  trc_fct_coef(*static_cast<Oracle*>(h), Q, mflx, rhoq_tp, aM, aP, ddens, ddens0, c_ssm1, dt, fct);
+}
+void orc_trc_cal_tend(void* h, const double* Q, const double* const* mflx, const double* aM, const double* aP,
+                      const double* fct, const double* rhoq_tp, double* Qdt) {
+  trc_cal_tend(*static_cast<Oracle*>(h), Q, mflx, aM, aP, fct, rhoq_tp, Qdt);
+}
+void orc_trc_tmar(void* h, double* Q, const double* ddens) { trc_tmar(*static_cast<Oracle*>(h), Q, ddens); }
+void orc_trc_filter(void* h, double* Q, const double* ddens, double etac_h, double alpha_h, int ord_h,
+                    double etac_v, double alpha_v, int ord_v) {
+  Oracle* o = static_cast<Oracle*>(h);
+  TrcFilter tf;
+  exp_filter_matrix(o->e, etac_h, alpha_h, ord_h, tf.Fh);
+  exp_filter_matrix(o->e, etac_v, alpha_v, ord_v, tf.Fv);
+  trc_filter(*o, tf, Q, ddens);
+}
+// nsteps tracer steps with fixed mass flux, Rusanov coefficients and densities (the advection-test
+// configuration, ONLY_TRACERADV_FLAG); filt = {etac_h, alpha_h, ord_h, etac_v, alpha_v, ord_v}
+void orc_trc_step(void* h, double* QTRC, const double* const* mflx, const double* aM, const double* aP,
+                  const double* ddens_trc, const double* ddens0_trc, const double* ddens, const double* rhoq_tp,
+                  int nstage, const double* sig, const double* gam, const double* c, double dt, int limiter,
+                  int tmar, int filter, const double* filt, int nsteps) {
+  Oracle* o = static_cast<Oracle*>(h);
+  TrcFilter tf;
+  if (filter) {
+    exp_filter_matrix(o->e, filt[0], filt[1], (int)filt[2], tf.Fh);
+    exp_filter_matrix(o->e, filt[3], filt[4], (int)filt[5], tf.Fv);
+  }
+  TrcStepArgs A{nstage, sig, gam, c, dt, limiter, tmar, filter};
+  for (int s = 0; s < nsteps; ++s) trc_step(*o, tf, A, QTRC, mflx, aM, aP, ddens_trc, ddens0_trc, ddens, rhoq_tp);
 }
 
 }  // extern "C"

@@ -73,6 +73,17 @@ def _load():
     lib.orc_step_hevi.restype = ctypes.c_long
     lib.orc_step_hevi.argtypes = [ctypes.c_void_p, pp, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                   ctypes.c_double, _dp]
+    lib.orc_trc_alphdens_advtest.argtypes = [ctypes.c_void_p] + [_dp] * 6
+    lib.orc_trc_save_massflux.argtypes = [ctypes.c_void_p, ctypes.c_int, pp, _dp, ctypes.c_double, ctypes.c_double,
+                                          ctypes.c_int, pp, _dp, _dp]
+    lib.orc_trc_fct_coef.argtypes = [ctypes.c_void_p, _dp, pp, _dp, _dp, _dp, _dp, _dp, ctypes.c_double,
+                                     ctypes.c_double, _dp]
+    lib.orc_trc_cal_tend.argtypes = [ctypes.c_void_p, _dp, pp, _dp, _dp, _dp, _dp, _dp]
+    lib.orc_trc_tmar.argtypes = [ctypes.c_void_p, _dp, _dp]
+    lib.orc_trc_filter.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                   ctypes.c_double, ctypes.c_double, ctypes.c_int]
+    lib.orc_trc_step.argtypes = [ctypes.c_void_p, _dp, pp, _dp, _dp, _dp, _dp, _dp, _dp, ctypes.c_int, _dp, _dp,
+                                 _dp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, ctypes.c_int]
     _lib = lib
     return lib
 
@@ -80,6 +91,15 @@ def _load():
 def _ptr(a: np.ndarray):
     assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
     return a.ctypes.data_as(_dp)
+
+
+def _optr(a):
+    """pointer of an optional array (None -> NULL)"""
+    return None if a is None else _ptr(a)
+
+
+def _c64(a):
+    return None if a is None else np.ascontiguousarray(a, np.float64)
 
 
 def _pp(arrs):
@@ -191,3 +211,79 @@ class Oracle:
         nfail = self.lib.orc_step_hevi(self._h, pq, float(dt), int(nsteps), int(max_iter), float(tol),
                                        ctypes.byref(mi))
         return qs, int(nfail), float(mi.value)
+
+    # ---- tracer advection (trcadvect3d_heve.F90, driver_trcadv3d.F90) ----
+    # Face-node arrays (alph_dens) have shape (Ne, 6, N1*N1): FElib's (NfpTot, Ne).
+
+    @property
+    def face_shape(self):
+        return (self.Ne, 6, self.N1 * self.N1)
+
+    def trc_alphdens_advtest(self, ddens, momx, momy, momz):
+        aM, aP = np.zeros(self.face_shape), np.zeros(self.face_shape)
+        a = [_c64(x) for x in (ddens, momx, momy, momz)]
+        self.lib.orc_trc_alphdens_advtest(self._h, *[_ptr(x) for x in a], _ptr(aM), _ptr(aP))
+        return aM, aP
+
+    def trc_save_massflux(self, rkstage, q, w_h, w_v, is_hevi, mflx, aM, aP, dpres=None):
+        """Updates mflx (3 arrays) and aM, aP in place (stage 1 resets them)."""
+        qs = [_c64(x) for x in q]
+        pq, _k1 = _pp(qs)
+        pm, _k2 = _pp(mflx)
+        dp = _c64(dpres)
+        self.lib.orc_trc_save_massflux(self._h, int(rkstage), pq, _optr(dp), float(w_h), float(w_v), int(is_hevi),
+                                       pm, _ptr(aM), _ptr(aP))
+
+    def trc_fct_coef(self, Q, mflx, aM, aP, ddens, ddens0, c_ssm1, dt, rhoq_tp=None):
+        fct = np.zeros(self.shape)
+        ms = [_c64(x) for x in mflx]
+        pm, _k = _pp(ms)
+        rq = _c64(rhoq_tp)
+        self.lib.orc_trc_fct_coef(self._h, _ptr(_c64(Q)), pm, _optr(rq), _ptr(_c64(aM)), _ptr(_c64(aP)),
+                                  _ptr(_c64(ddens)), _ptr(_c64(ddens0)), float(c_ssm1), float(dt), _ptr(fct))
+        return fct
+
+    def trc_cal_tend(self, Q, mflx, aM, aP, fct, rhoq_tp=None):
+        out = np.zeros(self.shape)
+        ms = [_c64(x) for x in mflx]
+        pm, _k = _pp(ms)
+        rq = _c64(rhoq_tp)
+        self.lib.orc_trc_cal_tend(self._h, _ptr(_c64(Q)), pm, _ptr(_c64(aM)), _ptr(_c64(aP)), _ptr(_c64(fct)),
+                                  _optr(rq), _ptr(out))
+        return out
+
+    def trc_tmar(self, Q, ddens):
+        q = np.array(Q, np.float64, copy=True, order="C")
+        self.lib.orc_trc_tmar(self._h, _ptr(q), _ptr(_c64(ddens)))
+        return q
+
+    def trc_filter(self, Q, ddens, etac_h=2.0 / 3.0, alpha_h=36.0, ord_h=16, etac_v=2.0 / 3.0, alpha_v=36.0,
+                   ord_v=16):
+        q = np.array(Q, np.float64, copy=True, order="C")
+        self.lib.orc_trc_filter(self._h, _ptr(q), _ptr(_c64(ddens)), float(etac_h), float(alpha_h), int(ord_h),
+                                float(etac_v), float(alpha_v), int(ord_v))
+        return q
+
+    def trc_step(self, QTRC, mflx, aM, aP, ddens_trc, ddens0_trc, dt, nsteps=1, ddens=None, rhoq_tp=None,
+                 scheme="ERK_SSP_3s3o", limiter=True, tmar=True, filter=None):
+        """nsteps tracer steps (fixed mass flux and densities); filter = None or a dict of the six
+        tracer filter parameters (etac_h, alpha_h, ord_h, etac_v, alpha_v, ord_v)."""
+        from timeint_ref import tables
+
+        tb = tables(scheme)
+        q = np.array(QTRC, np.float64, copy=True, order="C")
+        ms = [_c64(x) for x in mflx]
+        pm, _k = _pp(ms)
+        sig = np.ascontiguousarray(tb["sig"], np.float64)
+        gam = np.ascontiguousarray(tb["gam"], np.float64)
+        c = np.ascontiguousarray(tb["c"], np.float64)
+        fp = dict(etac_h=2.0 / 3.0, alpha_h=36.0, ord_h=16, etac_v=2.0 / 3.0, alpha_v=36.0, ord_v=16)
+        if filter:
+            fp.update(filter)
+        filt = np.array([fp["etac_h"], fp["alpha_h"], fp["ord_h"], fp["etac_v"], fp["alpha_v"], fp["ord_v"]],
+                        np.float64)
+        self.lib.orc_trc_step(self._h, _ptr(q), pm, _ptr(_c64(aM)), _ptr(_c64(aP)), _ptr(_c64(ddens_trc)),
+                              _ptr(_c64(ddens0_trc)), _optr(_c64(ddens)), _optr(_c64(rhoq_tp)), int(tb["nstage"]),
+                              _ptr(sig), _ptr(gam), _ptr(c), float(dt), int(bool(limiter)), int(bool(tmar)),
+                              int(bool(filter)), _ptr(filt), int(nsteps))
+        return q

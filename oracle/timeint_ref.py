@@ -36,7 +36,9 @@ def tables(name: str):
         gmm[1, 0] = 1.0
         gmm[2, 1] = 0.25
         gmm[3, 2] = 2.0 / 3.0
-        return dict(kind="lowstorage", nstage=3, sig=sig, gam=gmm)
+        # stage nodes of the equivalent Butcher form (a21 = 1, a31 = a32 = 1/4)
+        c = np.array([0.0, 1.0, 0.5])
+        return dict(kind="lowstorage", nstage=3, sig=sig, gam=gmm, c=c)
     raise ValueError(name)
 
 
