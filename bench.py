@@ -219,6 +219,134 @@ def _full_field_errors(np, got, ref, dens_hyd_norm_sq, dens_hyd, therm_hyd):
     return out
 
 
+TRC_DT = 0.5  # tracer step on the C5 mesh: |u| ~ 6 m/s, element 100 m at p = 7 (stable up to ~1 s)
+
+
+def tracer_bench(args, torch, np, fl, cases, peaks, peak_src, steps, warmup):
+    """Tracer advection (FElib's trcadvect3d_heve + tracer driver; the advection-test configuration
+    ONLY_TRACERADV_FLAG) on the bench mesh: one cosine-bell tracer carried by the mass flux of the C5
+    state with (u, v) = (5, -3) m/s, FCT + TMAR, ERK_SSP_3s3o, FP64.  DOF = one tracer value per node."""
+    from dataclasses import replace
+
+    base = cases.C5().scaled(32, 32, 16) if args.small else cases.C5()
+    x0, x1, y0, y1, z0, z1 = base.dom
+    case = replace(base, v0=-3.0, filter_on=False,
+                   tracer=dict(qmax=1.0, rx=0.25 * (x1 - x0), ry=0.25 * (y1 - y0), rz=0.3 * (z1 - z0),
+                               xc=0.5 * (x0 + x1), yc=0.5 * (y0 + y1), zc=0.35 * (z1 - z0)))
+    q, b = cases.initial_state(case)
+    Q = cases.tracer_state(case)
+    ctx = fl.Context(case)
+    ctx.set_base_state(b["dens_hyd"], b["pres_hyd"], b["therm_hyd"])
+    qd = [ctx.tensor(a) for a in q[:4]]
+    del q
+    Qh = torch.from_numpy(np.ascontiguousarray(Q)).pin_memory()
+    Qd = ctx.tensor(Q)
+    mf = qd[1:4]
+    aM, aP = ctx.trc_alphdens_advtest(qd[0], qd[1], qd[2], qd[3])
+    stream = torch.cuda.ExternalStream(ctx.stream_handle)
+
+    def timed(prec, Qt):
+        ctx.trc_update(Qt, mf, aM, aP, qd[0], qd[0], TRC_DT, nsteps=warmup, prec=prec)
+        fl.prof_reset(ctx)
+        fl.prof_enable(ctx, True)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.trc_update(Qt, mf, aM, aP, qd[0], qd[0], TRC_DT, nsteps=steps, sync=False, prec=prec)
+        e1.record(stream)
+        ctx.sync()
+        torch.cuda.synchronize()
+        fl.prof_enable(ctx, False)
+        pr = {k: v for k, v in fl.prof_read(ctx).items() if k.startswith("trc") and v[1]}
+        return e0.elapsed_time(e1), pr
+
+    # FP64 (FElib's arithmetic) on a copy, then the float-pair path on Qd: same state, same steps
+    Q64 = Qd.clone()
+    ms64, prof64 = timed(fl.PREC_FP64, Q64)
+    ms, prof = timed(fl.PREC_PAIR, Qd)
+    pair_vs_fp64 = float((Qd - Q64).norm().item() / max(Q64.norm().item(), 1e-300))
+    del Q64
+    nodes = case.Np * case.Ne
+    value = nodes * 3 * steps / (ms * 1e-3)
+    nf_per_node = 6 * case.N1 ** 2 / case.Np  # face nodes per volume node
+    # algorithmic bytes per node of one launch (one read or write per array element; pairs and FP64
+    # values are both 8 bytes):
+    #   trc_fct:   Q, MFLX x3, DDENS_TRC, DDENS0_TRC + alph_dens M/P on the faces
+    #   trc_stage: the same inputs, the stage output, and var0 / varTmp (mean of the three stages)
+    algo = {"trc_fct": 8 * 6 + 16 * nf_per_node, "trc_stage": 8 * 6 + 16 * nf_per_node + (24 + 16 + 16) / 3}
+
+    def kern_table(pr):
+        out = {}
+        for k, (kms, kn) in pr.items():
+            avg = kms / kn
+            ach = algo.get(k, 0.0) * nodes / (avg * 1e-3) / 1e9
+            out[k] = {"ms": kms, "launches": kn, "avg_launch_ms": avg, "algorithmic_bytes_per_node": algo.get(k),
+                      "achieved_gbs": ach, "frac_of_hbm": ach / peaks.get("hbm_gbs", 6800.0)}
+        return out
+
+    kern = kern_table(prof)
+    top = max(kern, key=lambda k: kern[k]["ms"]) if kern else None
+    roof = None
+    if top:
+        roof = {"bound": "hbm", "kernel": top, "achieved": kern[top]["achieved_gbs"], "peak": peaks.get("hbm_gbs", 6800.0),
+                "unit": "GB/s", "frac": kern[top]["frac_of_hbm"], "peak_source": peak_src,
+                "note": "float-pair kernels; see profiles/trc_kernels_C5small_p7_32x32x16.md"}
+    # end to end: the step's inputs (QTRC, MFLX x3, alph_dens M/P, DDENS_TRC, DDENS0_TRC) from pinned host
+    # memory, one tracer step, QTRC back to the host
+    e2e = None
+    if not args.no_e2e:
+        hs = [Qh] + [t.cpu().pin_memory() for t in (mf[0], mf[1], mf[2], aM, aP, qd[0], qd[0])]
+        ds = [torch.empty_like(Qd)] + [torch.empty_like(t) for t in (mf[0], mf[1], mf[2], aM, aP, qd[0], qd[0])]
+        ke = max(1, min(steps, 3))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            for d_, h_ in zip(ds, hs):
+                d_.copy_(h_, non_blocking=True)
+            torch.cuda.synchronize()
+            ctx.trc_update(ds[0], ds[1:4], ds[4], ds[5], ds[6], ds[7], TRC_DT, nsteps=1, sync=False,
+                           prec=fl.PREC_PAIR)
+            ctx.sync()
+            Qh.copy_(ds[0], non_blocking=True)
+            torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        e2e = {"value": nodes * 3 * ke / (t1 - t0), "unit": UNIT,
+               "h2d_bytes_per_step": int(sum(h.numel() * 8 for h in hs)), "d2h_bytes_per_step": int(Qd.numel() * 8),
+               "steps": ke}
+        del hs, ds
+    finite = bool(torch.isfinite(Qd).all().item())
+    qmin = float(Qd.min().item())
+    cb = None
+    if not args.no_cpu:
+        import oracle as orc
+
+        sc = case.scaled(8, 8, 16)
+        qs, bs = cases.initial_state(sc)
+        o = orc.Oracle(sc.porder, sc.NeX, sc.NeY, sc.NeZ, sc.dom)
+        o.set_base_state(bs["dens_hyd"], bs["pres_hyd"])
+        am, ap = o.trc_alphdens_advtest(qs[0], qs[1], qs[2], qs[3])
+        Qs = cases.tracer_state(sc)
+        t0 = time.perf_counter()
+        o.trc_step(Qs, qs[1:4], am, ap, qs[0], qs[0], TRC_DT, nsteps=1)
+        t1 = time.perf_counter()
+        ns = max(1, min(400, int(8.0 / max(t1 - t0, 1e-3))))
+        t2 = time.perf_counter()
+        o.trc_step(Qs, qs[1:4], am, ap, qs[0], qs[0], TRC_DT, nsteps=ns)
+        t3 = time.perf_counter()
+        cb = {"value": sc.Np * sc.Ne * 3 * ns / (t3 - t2), "unit": UNIT, "cores": orc.num_threads(), "kind": "port",
+              "sample": f"FP64 oracle tracer step (FCT + TMAR, SSP-RK3), {ns} steps of an 8x8x16-element p=7 "
+                        f"sample of the same workload, {t3 - t2:.1f} s"}
+    ctx.close()
+    return {"metric": "tracer DOF-stage/s (one tracer, FCT + TMAR, ERK_SSP_3s3o)", "value": value, "unit": UNIT,
+            "ms_per_step": ms / steps, "steps": steps, "dt": TRC_DT, "dtype": "f32x2", "path": "float pairs",
+            "fp64": {"value": nodes * 3 * steps / (ms64 * 1e-3), "ms_per_step": ms64 / steps,
+                     "kernels": kern_table(prof64)},
+            "rel_l2_pair_vs_fp64": pair_vs_fp64,
+            "workload": f"C5 mesh p=7 {case.NeX}x{case.NeY}x{case.NeZ}, cosine-bell tracer, (u, v) = (5, -3) m/s",
+            "kernels": kern, "roofline": roof, "e2e": e2e, "cpu_baseline": cb, "finite": finite, "min_q": qmin,
+            "gpu_launches": sum(v[1] for v in prof.values())}
+
+
 def run_fedg(args):
     import numpy as np
     import torch
@@ -388,6 +516,9 @@ def run_fedg(args):
     cb = None
     if rank == 0 and not args.no_cpu:
         cb = cpu_sample(path)
+    trc = None
+    if rank == 0 and not args.no_tracer:
+        trc = tracer_bench(args, torch, np, fl, cases, peaks, peak_src, args.steps, args.warmup)
 
     finite = all(bool(torch.isfinite(t).all().item()) for t in qd)
     if rank == 0:
@@ -413,6 +544,7 @@ def run_fedg(args):
             "plain_fp64": plain,
             "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
             "accuracy": acc,
+            "tracer_advection": trc,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -437,6 +569,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--no-other", action="store_true", help="skip the run of the other precision mode")
+    ap.add_argument("--no-tracer", action="store_true", help="skip the tracer-advection measurement")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -153,6 +153,10 @@ void build_ops_1d(int N, double etac_h, double alpha_h, int ord_h, double etac_v
 
 }  // namespace
 namespace fedg {
+void lgl_nodes_1d(int N, double* x) {
+  const std::vector<double> v = lgl(N);
+  for (int i = 0; i <= N; ++i) x[i] = v[i];
+}
 void modal_filter_1d(int N, double etac, double alpha, int ord, double* F) {
   const int n1 = N + 1;
   const std::vector<double> x = lgl(N);
@@ -321,6 +325,8 @@ void fedg_ctx_destroy(fedg_ctx* c) {
   cudaFree(c->d_cnt);
   cudaFree(c->work);
   cudaFree(c->trc_buf);
+  cudaFree(c->nd_buf);
+  cudaFree(c->sponge_coef);
   if (c->h_cnt) cudaFreeHost(c->h_cnt);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -395,6 +401,8 @@ static double* ensure_work(fedg_ctx* c, size_t ndouble) {
   if (c->work_doubles >= ndouble) return c->work;
   cudaFree(c->work);
   cudaFree(c->trc_buf);
+  cudaFree(c->nd_buf);
+  cudaFree(c->sponge_coef);
   c->work = nullptr;
   c->work_doubles = 0;
   if (cudaMalloc(&c->work, sizeof(double) * ndouble) != cudaSuccess) return nullptr;

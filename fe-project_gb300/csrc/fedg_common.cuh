@@ -53,6 +53,33 @@ __device__ __forceinline__ void face_node(int f, int a, int b, int& i, int& j, i
   }
 }
 
+// Exterior node of face node (f, a, b) of element ke on the flat cube: the periodic neighbour's
+// matching node (kn >= 0), or at a lid (kn = -1) the element's own node.  pM: the face node's index
+// in the element; gP: the exterior node's global index.
+template <int N1>
+__device__ __forceinline__ void face_exterior(const Ops& op, int f, int a, int b, long ke, int ex, int ey, int ez,
+                                              int nxy, int& pM, size_t& gP, long& kn) {
+  constexpr int Np = N1 * N1 * N1, NF = N1 * N1;
+  int iM, jM, kM;
+  face_node<N1>(f, a, b, iM, jM, kM);
+  pM = iM + N1 * jM + NF * kM;
+  switch (f) {
+    case 0: kn = ke + (ey > 0 ? -op.NeX : (long)(op.NeY - 1) * op.NeX); break;
+    case 1: kn = ke + (ex < op.NeX - 1 ? 1 : -(op.NeX - 1)); break;
+    case 2: kn = ke + (ey < op.NeY - 1 ? op.NeX : -(long)(op.NeY - 1) * op.NeX); break;
+    case 3: kn = ke + (ex > 0 ? -1 : op.NeX - 1); break;
+    case 4: kn = ez > 0 ? ke - nxy : -1; break;
+    default: kn = ez < op.NeZ - 1 ? ke + nxy : -1; break;
+  }
+  if (kn >= 0) {
+    int i2, j2, k2;
+    face_node<N1>(face_opp(f), a, b, i2, j2, k2);
+    gP = (size_t)kn * Np + i2 + N1 * j2 + NF * k2;
+  } else {
+    gP = (size_t)ke * Np + pM;
+  }
+}
+
 __device__ __forceinline__ double warp_max(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));

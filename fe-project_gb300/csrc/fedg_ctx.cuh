@@ -34,6 +34,8 @@ struct fedg_ctx {
   fedg_tint* upd_tint = nullptr;  // RK buffers of fedg_update, kept between calls
   MlpState* guess = nullptr;      // column-guess network attached with fedg_guess_load (not owned)
   double* trc_buf = nullptr;      // tracer update scratch: two stage fields, var0, varTmp, FCT per element
+  double* nd_buf = nullptr;       // numerical-diffusion scratch: gradient (3 fields), Laplacian (2 fields)
+  double* sponge_coef = nullptr;  // sponge-layer coefficient per level
   // kernel timers / launch counters
   bool prof_on = false;
   long long nlaunch[FEDG_K_COUNT] = {};
@@ -41,6 +43,13 @@ struct fedg_ctx {
   std::vector<Rec> recs;
   Prof prof() const { return Prof{d_prof, d_prof + L, d_prof + 2 * L, d_prof + 3 * L}; }
 };
+
+namespace fedg {
+// fedg_trc_update's tracer steps in float pairs (fedg_trc_pair.cu); scratch: 4 Np*Ne + Ne doubles
+int trc_update_pair(fedg_ctx* c, double* QTRC, const double* const mflx[3], const double* aM, const double* aP,
+                    const double* ddens_trc, const double* ddens0_trc, const double* ddens, const double* rhoq,
+                    const fedg_trc_opts* o, double* scratch);
+}  // namespace fedg
 
 // Runs one launch f() of kernel class id on the context stream, counting it and, when the
 // timers are on, bracketing it with a pair of CUDA events.

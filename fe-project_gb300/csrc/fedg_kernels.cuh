@@ -16,6 +16,8 @@ struct ViArgs {
 
 // host: 1D exponential modal filter matrix (row-major N1 x N1) of order N
 void modal_filter_1d(int N, double etac, double alpha, int ord, double* F);
+// host: the N+1 LGL nodes on [-1, 1]
+void lgl_nodes_1d(int N, double* x);
 
 int launch_tend_fp64(const Ops& op, const Prof& pf, const F5c& q, const double* dpres, const F5& t, int Ne,
                      int hevi, cudaStream_t s);

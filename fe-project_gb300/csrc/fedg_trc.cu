@@ -61,31 +61,6 @@ struct TrcFilt {
   double Fh[FEDG_MAXN1 * FEDG_MAXN1], Fv[FEDG_MAXN1 * FEDG_MAXN1];
 };
 
-// exterior node of face node (f, a, b) of element ke; lid: slip lid (own node)
-template <int N1>
-__device__ __forceinline__ void trc_face_nodes(const Ops& op, int f, int a, int b, long ke, int ex, int ey, int ez,
-                                               int nxy, int& pM, size_t& gP, long& kn) {
-  constexpr int Np = N1 * N1 * N1, NF = N1 * N1;
-  int iM, jM, kM;
-  face_node<N1>(f, a, b, iM, jM, kM);
-  pM = iM + N1 * jM + NF * kM;
-  switch (f) {
-    case 0: kn = ke + (ey > 0 ? -op.NeX : (long)(op.NeY - 1) * op.NeX); break;
-    case 1: kn = ke + (ex < op.NeX - 1 ? 1 : -(op.NeX - 1)); break;
-    case 2: kn = ke + (ey < op.NeY - 1 ? op.NeX : -(long)(op.NeY - 1) * op.NeX); break;
-    case 3: kn = ke + (ex > 0 ? -1 : op.NeX - 1); break;
-    case 4: kn = ez > 0 ? ke - nxy : -1; break;
-    default: kn = ez < op.NeZ - 1 ? ke + nxy : -1; break;
-  }
-  if (kn >= 0) {
-    int i2, j2, k2;
-    face_node<N1>(face_opp(f), a, b, i2, j2, k2);
-    gP = (size_t)kn * Np + i2 + N1 * j2 + NF * k2;
-  } else {
-    gP = (size_t)ke * Np + pM;
-  }
-}
-
 // outward normal component on face f of the vector field (vx, vy, vz) at node g; the normals are
 // axis-aligned, so only one component is loaded.  flip_z reflects the vertical component (the
 // exterior side of a slip lid).
@@ -158,7 +133,7 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
       int pM;
       size_t gP;
       long kn;
-      trc_face_nodes<N1>(op, f, a, b, ke, ex, ey, ez, nxy, pM, gP, kn);
+      face_exterior<N1>(op, f, a, b, ke, ex, ey, ez, nxy, pM, gP, kn);
       const size_t gM = (size_t)ke * Np + pM;
       const double mfM = normal_comp(f, in.mf[0], in.mf[1], in.mf[2], gM);
       const double mfP = normal_comp(f, in.mf[0], in.mf[1], in.mf[2], gP, kn < 0);
@@ -281,7 +256,7 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
       int pM;
       size_t gP;
       long kn;
-      trc_face_nodes<N1>(op, f, a, b, ke, ex, ey, ez, nxy, pM, gP, kn);
+      face_exterior<N1>(op, f, a, b, ke, ex, ey, ez, nxy, pM, gP, kn);
       const size_t gM = (size_t)ke * Np + pM;
       const double mfM = normal_comp(f, in.mf[0], in.mf[1], in.mf[2], gM);
       const double mfP = normal_comp(f, in.mf[0], in.mf[1], in.mf[2], gP, kn < 0);
@@ -411,7 +386,7 @@ __global__ void k_trc_alph_adv(const Ops op, const double* __restrict__ dens_pro
   int pM;
   size_t gP;
   long kn;
-  trc_face_nodes<N1>(op, f, a, b, ke, ex, ey, ez, nxy, pM, gP, kn);
+  face_exterior<N1>(op, f, a, b, ke, ex, ey, ez, nxy, pM, gP, kn);
   const size_t gM = (size_t)ke * Np + pM;
   const int kM = pM / NF, kP = (int)((gP % Np) / NF);
   const int ezP = kn >= 0 ? (int)(kn / nxy) : ez;
@@ -468,7 +443,7 @@ __global__ void k_trc_alph_dyn(const Ops op, const Prof pf, const MflxArgs A, lo
   int pM;
   size_t gP;
   long kn;
-  trc_face_nodes<N1>(op, f, a, b, ke, ex, ey, ez, nxy, pM, gP, kn);
+  face_exterior<N1>(op, f, a, b, ke, ex, ey, ez, nxy, pM, gP, kn);
   const size_t gM = (size_t)ke * Np + pM;
   const int levM = ez * N1 + pM / NF;
   const int levP = (kn >= 0 ? (int)(kn / nxy) : ez) * N1 + (int)((gP % Np) / NF);
@@ -696,6 +671,8 @@ int fedg_trc_update(fedg_ctx* c, double* QTRC, const double* const mflx[3], cons
   if (!c || !QTRC || !mflx || !mflx[0] || !mflx[1] || !mflx[2] || !alph_M || !alph_P || !DDENS_TRC || !DDENS0_TRC || !o)
     return api_fail("fedg_trc_update: null argument");
   if (o->scheme != FEDG_SSP_RK3) return api_fail("fedg_trc_update: the tracer scheme must be FEDG_SSP_RK3 (ERK_SSP_3s3o)");
+  if (o->prec != FEDG_PREC_FP64 && o->prec != FEDG_PREC_PAIR)
+    return api_fail("fedg_trc_update: prec must be FEDG_PREC_FP64 or FEDG_PREC_PAIR");
   if (!(o->dt > 0.0) || o->nsteps < 0) return api_fail("fedg_trc_update: dt must be positive and nsteps >= 0");
   if (int r = check_base(c, "fedg_trc_update")) return r;
   cudaSetDevice(c->d.device);
@@ -711,6 +688,8 @@ int fedg_trc_update(fedg_ctx* c, double* QTRC, const double* const mflx[3], cons
       return api_fail("fedg_trc_update: out of device memory (4 tracer fields of scratch)");
     }
   }
+  if (o->prec == FEDG_PREC_PAIR)
+    return trc_update_pair(c, QTRC, mflx, alph_M, alph_P, DDENS_TRC, DDENS0_TRC, DDENS, RHOQ_tp, o, c->trc_buf);
   double* bufA = c->trc_buf;
   double* bufB = bufA + n;
   double* var0 = bufB + n;

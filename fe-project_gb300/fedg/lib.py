@@ -33,14 +33,14 @@ EXPORTED = [
     "fedg_guess_set_params", "fedg_guess_get_params", "fedg_guess_train_step", "fedg_guess_loss_grad",
     "fedg_guess_predict", "fedg_guess_load", "fedg_cal_tend_ex_noalloc",
     "fedg_trc_alphdens_advtest", "fedg_trc_save_massflux", "fedg_trc_fct_coef", "fedg_trc_cal_tend",
-    "fedg_trc_tmar", "fedg_trc_modalfilter", "fedg_trc_update",
+    "fedg_trc_tmar", "fedg_trc_modalfilter", "fedg_trc_update", "fedg_numdiff_apply", "fedg_sponge_add_tend",
 ]
 
 # kernel classes of fedg_prof_read (include/fedg.h)
-K_TEND, K_VI, K_RK, K_FILTER, K_PRES, K_MTEND, K_MVI, K_MLP, K_AUX, K_TRC_FCT, K_TRC_TEND, K_TRC_AUX, K_COUNT = \
-    range(13)
+K_TEND, K_VI, K_RK, K_FILTER, K_PRES, K_MTEND, K_MVI, K_MLP, K_AUX, K_TRC_FCT, K_TRC_TEND, K_TRC_AUX, K_ND, \
+    K_COUNT = range(14)
 KERNEL_NAMES = ["tend_fp64", "vi_fp64", "rk", "filter", "drhot2pres", "stage_mixed", "vi_mixed", "mlp", "aux",
-                "trc_fct", "trc_stage", "trc_aux"]
+                "trc_fct", "trc_stage", "trc_aux", "numdiff"]
 
 
 class MeshDesc(ctypes.Structure):
@@ -64,7 +64,8 @@ class TrcOpts(ctypes.Structure):
     _fields_ = [("scheme", ctypes.c_int), ("dt", ctypes.c_double), ("nsteps", ctypes.c_int),
                 ("limiter", ctypes.c_int), ("tmar", ctypes.c_int), ("filter", ctypes.c_int),
                 ("mf_etac_h", ctypes.c_double), ("mf_alpha_h", ctypes.c_double), ("mf_order_h", ctypes.c_int),
-                ("mf_etac_v", ctypes.c_double), ("mf_alpha_v", ctypes.c_double), ("mf_order_v", ctypes.c_int)]
+                ("mf_etac_v", ctypes.c_double), ("mf_alpha_v", ctypes.c_double), ("mf_order_v", ctypes.c_int),
+                ("prec", ctypes.c_int)]
 
 
 class UpdateOpts(ctypes.Structure):
@@ -134,6 +135,8 @@ def load():
     lib.fedg_trc_modalfilter.argtypes = [_vp, _vp, _vp, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                          ctypes.c_double, ctypes.c_double, ctypes.c_int]
     lib.fedg_trc_update.argtypes = [_vp, _vp, _P3, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.POINTER(TrcOpts)]
+    lib.fedg_numdiff_apply.argtypes = [_vp, _P5, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double]
+    lib.fedg_sponge_add_tend.argtypes = [_vp, _P3, _P3, ctypes.c_double, ctypes.c_double, ctypes.c_int]
     lib.fedg_prof_enable.argtypes = [_vp, ctypes.c_int]
     lib.fedg_prof_reset.argtypes = [_vp]
     lib.fedg_prof_read.argtypes = [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
@@ -333,14 +336,15 @@ class Context:
         return Q
 
     def trc_update(self, Q, mflx, aM, aP, ddens_trc, ddens0_trc, dt, nsteps=1, ddens=None, rhoq_tp=None,
-                   limiter=True, tmar=True, filter=None, sync=True):
+                   limiter=True, tmar=True, filter=None, sync=True, prec=PREC_FP64):
         """nsteps tracer steps in place on Q (ERK_SSP_3s3o); filter = None or a dict of the six tracer
         filter parameters (etac_h, alpha_h, ord_h, etac_v, alpha_v, ord_v)."""
         fp = dict(etac_h=2.0 / 3.0, alpha_h=36.0, ord_h=16, etac_v=2.0 / 3.0, alpha_v=36.0, ord_v=16)
         if filter:
             fp.update(filter)
         o = TrcOpts(SSP_RK3, float(dt), int(nsteps), int(bool(limiter)), int(bool(tmar)), int(bool(filter)),
-                    fp["etac_h"], fp["alpha_h"], int(fp["ord_h"]), fp["etac_v"], fp["alpha_v"], int(fp["ord_v"]))
+                    fp["etac_h"], fp["alpha_h"], int(fp["ord_h"]), fp["etac_v"], fp["alpha_v"], int(fp["ord_v"]),
+                    int(prec))
         if sync:
             self.torch.cuda.synchronize()
         _check(self.lib.fedg_trc_update(self.h, _ptr(Q), (ctypes.c_void_p * 3)(*[m.data_ptr() for m in mflx]),
@@ -349,6 +353,22 @@ class Context:
         if sync:
             self.sync()
         return Q
+
+    # -- numerical diffusion (nonhydro3d_numdiff.F90) and sponge layer (dgm_spongelayer.F90) --
+    def numdiff_apply(self, q, nlap, coef_h, coef_v, dt):
+        self.torch.cuda.synchronize()
+        _check(self.lib.fedg_numdiff_apply(self.h, _p5(q), int(nlap), float(coef_h), float(coef_v), float(dt)),
+               "fedg_numdiff_apply")
+        self.sync()
+        return q
+
+    def sponge_add_tend(self, tend, mom, tau, height, hveldamp=False):
+        self.torch.cuda.synchronize()
+        _check(self.lib.fedg_sponge_add_tend(self.h, (ctypes.c_void_p * 3)(*[t.data_ptr() for t in tend]),
+                                             (ctypes.c_void_p * 3)(*[m.data_ptr() for m in mom]), float(tau),
+                                             float(height), int(bool(hveldamp))), "fedg_sponge_add_tend")
+        self.sync()
+        return tend
 
 
 def prof_enable(ctx, on=True):

@@ -29,6 +29,9 @@ module scale_atm_dyn_dgm_nonhydro3d_gb300
   public :: atm_dyn_dgm_nonhydro3d_gb300_cal_tend_hevi
   public :: atm_dyn_dgm_nonhydro3d_gb300_cal_vi
   public :: atm_dyn_dgm_nonhydro3d_gb300_ctx
+  public :: atm_dyn_dgm_nonhydro3d_gb300_numdiff_apply
+  public :: atm_dyn_dgm_nonhydro3d_gb300_sponge_init
+  public :: atm_dyn_dgm_nonhydro3d_gb300_sponge_add_tend
 
   integer(c_int), parameter :: FEDG_HEVE = 0, FEDG_HEVI = 1
 
@@ -74,9 +77,26 @@ module scale_atm_dyn_dgm_nonhydro3d_gb300
       import :: c_int, c_ptr
       type(c_ptr), value :: ctx
     end function
+    integer(c_int) function fedg_numdiff_apply(ctx, q, nlap, coef_h, coef_v, dt) bind(C, name="fedg_numdiff_apply")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      type(c_ptr), intent(in) :: q(5)
+      integer(c_int), value :: nlap
+      real(c_double), value :: coef_h, coef_v, dt
+    end function
+    integer(c_int) function fedg_sponge_add_tend(ctx, tend, mom, tau, height, hveldamp) &
+        bind(C, name="fedg_sponge_add_tend")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      type(c_ptr), intent(in) :: tend(3), mom(3)
+      real(c_double), value :: tau, height
+      integer(c_int), value :: hveldamp
+    end function
   end interface
 
   type(c_ptr), save :: ctx = c_null_ptr
+  real(RP), save :: sl_tau = -1.0_RP, sl_height = -1.0_RP
+  logical, save :: sl_hvel = .false.
   integer, save :: vi_max_iter = 1           ! 1: FElib's single linearised solve
   real(RP), save :: vi_tol = 1.0E-10_RP
 
@@ -219,5 +239,51 @@ contains
       LOG_INFO("atm_dyn_dgm_nonhydro3d_gb300_cal_vi",*) 'Newton not converged in columns:', ierr
     end if
   end subroutine atm_dyn_dgm_nonhydro3d_gb300_cal_vi
+
+  !> AtmDyn_Nonhydro3D_Numdiff%Apply (…_nonhydro3d_numdiff.F90:214-242) on the prognostic fields
+  subroutine atm_dyn_dgm_nonhydro3d_gb300_numdiff_apply( DDENS, MOMX, MOMY, MOMZ, THERM, &
+    ND_LAPLACIAN_NUM, ND_COEF_H, ND_COEF_V, dtsec, lmesh, elem )
+    class(LocalMesh3D), intent(in) :: lmesh
+    class(ElementBase3D), intent(in) :: elem
+    real(RP), intent(inout), target :: DDENS(elem%Np,lmesh%NeA), MOMX(elem%Np,lmesh%NeA), &
+      MOMY(elem%Np,lmesh%NeA), MOMZ(elem%Np,lmesh%NeA), THERM(elem%Np,lmesh%NeA)
+    integer, intent(in) :: ND_LAPLACIAN_NUM
+    real(RP), intent(in) :: ND_COEF_H, ND_COEF_V, dtsec
+    type(c_ptr) :: q(5)
+    integer(c_int) :: ierr
+    !$acc host_data use_device(DDENS, MOMX, MOMY, MOMZ, THERM)
+    q = [ c_loc(DDENS), c_loc(MOMX), c_loc(MOMY), c_loc(MOMZ), c_loc(THERM) ]
+    !$acc end host_data
+    ierr = fedg_numdiff_apply( ctx, q, ND_LAPLACIAN_NUM, ND_COEF_H, ND_COEF_V, dtsec )
+    if (ierr < 0) call PRC_abort
+    ierr = fedg_synchronize( ctx )
+  end subroutine atm_dyn_dgm_nonhydro3d_gb300_numdiff_apply
+
+  !> the &PARAM_ATMOS_DYN_SPONGELAYER settings (…_dgm_spongelayer.F90:57-123: tau defaults to 10 dt)
+  subroutine atm_dyn_dgm_nonhydro3d_gb300_sponge_init( wdamp_tau, wdamp_height, hveldamp_flag )
+    real(RP), intent(in) :: wdamp_tau, wdamp_height
+    logical, intent(in) :: hveldamp_flag
+    sl_tau = wdamp_tau
+    sl_height = wdamp_height
+    sl_hvel = hveldamp_flag
+  end subroutine atm_dyn_dgm_nonhydro3d_gb300_sponge_init
+
+  !> AtmDynSpongeLayer%AddTend (…_dgm_spongelayer.F90:134-185)
+  subroutine atm_dyn_dgm_nonhydro3d_gb300_sponge_add_tend( MOMX_dt, MOMY_dt, MOMZ_dt, MOMX_, MOMY_, MOMZ_, &
+    lmesh, elem )
+    class(LocalMesh3D), intent(in) :: lmesh
+    class(ElementBase3D), intent(in) :: elem
+    real(RP), intent(inout), target :: MOMX_dt(elem%Np,lmesh%NeA), MOMY_dt(elem%Np,lmesh%NeA), &
+      MOMZ_dt(elem%Np,lmesh%NeA)
+    real(RP), intent(in), target :: MOMX_(elem%Np,lmesh%NeA), MOMY_(elem%Np,lmesh%NeA), MOMZ_(elem%Np,lmesh%NeA)
+    type(c_ptr) :: tend(3), mom(3)
+    integer(c_int) :: ierr
+    !$acc host_data use_device(MOMX_dt, MOMY_dt, MOMZ_dt, MOMX_, MOMY_, MOMZ_)
+    tend = [ c_loc(MOMX_dt), c_loc(MOMY_dt), c_loc(MOMZ_dt) ]
+    mom = [ c_loc(MOMX_), c_loc(MOMY_), c_loc(MOMZ_) ]
+    !$acc end host_data
+    ierr = fedg_sponge_add_tend( ctx, tend, mom, sl_tau, sl_height, merge(1, 0, sl_hvel) )
+    if (ierr < 0) call PRC_abort
+  end subroutine atm_dyn_dgm_nonhydro3d_gb300_sponge_add_tend
 
 end module scale_atm_dyn_dgm_nonhydro3d_gb300

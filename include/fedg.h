@@ -232,10 +232,27 @@ typedef struct {
   int filter;          /* MODALFILTER_FLAG */
   double mf_etac_h, mf_alpha_h; int mf_order_h;
   double mf_etac_v, mf_alpha_v; int mf_order_v;
+  int prec;            /* FEDG_PREC_FP64 (FElib's arithmetic, default) or FEDG_PREC_PAIR (float pairs on
+                          the FP32 pipe: FP64-class, relative rounding ~1e-14) */
 } fedg_trc_opts;
 int fedg_trc_update(fedg_ctx* ctx, double* QTRC, const double* const mflx[3], const double* alph_M,
                     const double* alph_P, const double* DDENS_TRC, const double* DDENS0_TRC, const double* DDENS,
                     const double* RHOQ_tp, const fedg_trc_opts* opts);
+
+/* ---- Numerical diffusion and sponge layer ---------------------------------------------------
+ * atm_dyn_dgm_nonhydro3d_numdiff_Apply (FElib/src/fluid_dyn_solver/scale_atm_dyn_dgm_nonhydro3d_numdiff.F90:
+ * 214-376), applied by the model after the dynamics and tracer updates (mod_atmos_dyn.F90:340-348):
+ * q += dt (-1)^(nlap+1) nabla^(2 nlap) q with coefficients coef_h (horizontal) and coef_v (vertical),
+ * for DRHOT, MOMZ, MOMX, MOMY, DDENS in that order; all but DDENS are differentiated as q/dens and
+ * weighted by dens.  nlap = ND_LAPLACIAN_NUM, coef_h/v = ND_COEF_H/V, dt = the dynamics step.
+ * q[5] = DDENS, MOMX, MOMY, MOMZ, DRHOT, in place; lids are slip and adiabatic (dgm_bnd.F90:370-508). */
+int fedg_numdiff_apply(fedg_ctx* ctx, double* const q[5], int nlap, double coef_h, double coef_v, double dt);
+/* atm_dyn_dgm_spongelayer_add_tend (..._dgm_spongelayer.F90:134-219): Rayleigh damping of MOMZ (and of
+ * MOMX, MOMY when hveldamp) above `height`, rate 0.25/tau (1 + sign(z - h)) (1 - cos(pi (z - h)/(z_top - h))),
+ * subtracted from the explicit tendencies.  tend[3] = MOMX_dt, MOMY_dt, MOMZ_dt (in/out); mom[3] = MOMX,
+ * MOMY, MOMZ.  FElib's defaults: tau = 10 dt when SL_WDAMP_TAU < 0; height from SL_WDAMP_LAYER. */
+int fedg_sponge_add_tend(fedg_ctx* ctx, double* const tend[3], const double* const mom[3], double tau,
+                         double height, int hveldamp);
 
 /* Kernel timers: the analogue of FElib's PROF_rapstart/PROF_rapend regions
  * (e.g. 'ATM_DYN_cal_vi', 'cal_dyn_tend_interior'; scale_prof of the SCALE library).
@@ -255,7 +272,8 @@ enum {
   FEDG_K_TRC_FCT = 9,   /* tracer FCT coefficient (calc_fct_coef)                   */
   FEDG_K_TRC_TEND = 10, /* tracer tendency + RK stage (cal_tend, Advance_trcvar)    */
   FEDG_K_TRC_AUX = 11,  /* tracer Rusanov coefficients, mass flux, TMAR, filter     */
-  FEDG_K_COUNT = 12
+  FEDG_K_ND = 12,       /* numerical diffusion passes, sponge layer                 */
+  FEDG_K_COUNT = 13
 };
 int fedg_prof_enable(fedg_ctx* ctx, int on);
 int fedg_prof_reset(fedg_ctx* ctx);

@@ -28,6 +28,8 @@
 //   * driver stage loop        ..._driver_nonhydro3d.F90:614-963
 //   * tracer advection (FCT + TMAR, mass-flux averaging, tracer RK, tracer filter)
 //                              ..._trcadvect3d_heve.F90, ..._driver_trcadv3d.F90:330-560
+//   * numerical diffusion      ..._nonhydro3d_numdiff.F90:214-721, ..._dgm_bnd.F90:370-508
+//   * sponge layer             ..._dgm_spongelayer.F90:134-219
 //
 // Layout: every field is column-major (Np, Ne) like FElib, node n = i + N1*j + N1^2*k,
 // element ke = ex + NeX*ey + NeX*NeY*ez.  Exterior (halo) values are produced in place
@@ -1178,6 +1180,252 @@ static void trc_step(const Oracle& o, const TrcFilter& tf, const TrcStepArgs& A,
     QTRC[p] = (o.dens_hyd[p] + ddens_trc[p]) / (o.dens_hyd[p] + dd[p]) * q[p];
 }
 
+// ---------------------------------------------------------------------------------
+// Numerical diffusion: the hyperdiffusion filter of FElib, (-1)^(n+1) coef nabla^(2n) applied to each
+// prognostic variable after the dynamics step with LDG-type alternating one-sided fluxes.
+//   Apply / apply_numfilter     ..._nonhydro3d_numdiff.F90:214-376
+//   numdiff_tend                :379-440;  cal_del_flux_lap_with_coef :443-500
+//   numdiff_cal_laplacian       :505-558;  cal_del_flux_lap           :561-601
+//   numdiff_cal_flx             :606-665;  cal_del_gradDiffVar        :668-721
+//   lid boundary values         ..._dgm_bnd.F90:370-508 (ApplyBC_numdiff_odd_lc / _even_lc) for
+//                               slip velocity and adiabatic thermal lids
+// Flat cube: periodic faces take the neighbour's values; at a lid the exterior value is the own
+// node's, reflected as FElib's boundary routines do, and the face flux is centred (is_bound).
+// ---------------------------------------------------------------------------------
+static inline double fsign1(double x) { return std::signbit(x) ? -1.0 : 1.0; }  // Fortran sign(1, x)
+
+// exterior value of a scalar at a lid under the even boundary routine (slip: the wall-normal
+// momentum component is reflected; the other variables keep the own value)
+static inline double nd_even_ext(int var, double vM, double nx, double ny, double nz) {
+  switch (var) {
+    case VMX: { const double g = vM * nx; return vM - 2.0 * g * nx; }
+    case VMY: { const double g = vM * ny; return vM - 2.0 * g * ny; }
+    case VMZ: { const double g = vM * nz; return vM - 2.0 * g * nz; }
+    default: return vM;
+  }
+}
+// exterior gradient at a lid under the odd boundary routine
+static inline void nd_odd_ext(int var, const double gM[3], double nx, double ny, double nz, double gP[3]) {
+  const double gn = gM[0] * nx + gM[1] * ny + gM[2] * nz;
+  gP[0] = gM[0]; gP[1] = gM[1]; gP[2] = gM[2];
+  switch (var) {
+    case VMX: gP[1] = gM[1] - 2.0 * gn * ny; gP[2] = gM[2] - 2.0 * gn * nz; break;
+    case VMY: gP[0] = gM[0] - 2.0 * gn * nx; gP[2] = gM[2] - 2.0 * gn * nz; break;
+    case VMZ: gP[0] = gM[0] - 2.0 * gn * nx; gP[1] = gM[1] - 2.0 * gn * ny; break;
+    default:  // DENS, RHOT: adiabatic
+      gP[0] = gM[0] - 2.0 * gn * nx; gP[1] = gM[1] - 2.0 * gn * ny; gP[2] = gM[2] - 2.0 * gn * nz; break;
+  }
+}
+
+// tensor-product Lift of per-face values fv[6][Nfp] at node (i, j, k)
+static inline double nd_lift(const Oracle& o, const double* fv, int i, int j, int k) {
+  const int N1 = o.N1, Nfp = o.Nfp, N = N1 - 1;
+  const std::vector<double>& Mi = o.e.Minv;
+  return Mi[j * N1 + 0] * fv[0 * Nfp + i + N1 * k] + Mi[i * N1 + N] * fv[1 * Nfp + j + N1 * k] +
+         Mi[j * N1 + N] * fv[2 * Nfp + i + N1 * k] + Mi[i * N1 + 0] * fv[3 * Nfp + j + N1 * k] +
+         Mi[k * N1 + 0] * fv[4 * Nfp + i + N1 * j] + Mi[k * N1 + N] * fv[5 * Nfp + i + N1 * j];
+}
+static inline double nd_dx(const Oracle& o, const double* u, int dir, int i, int j, int k) {
+  const int N1 = o.N1;
+  const std::vector<double>& D = o.e.D;
+  double s = 0.0;
+  for (int l = 0; l < N1; ++l) {
+    const size_t p = dir == 0 ? o.nid(l, j, k) : (dir == 1 ? o.nid(i, l, k) : o.nid(i, j, l));
+    s += D[(dir == 0 ? i : (dir == 1 ? j : k)) * N1 + l] * u[p];
+  }
+  return s;
+}
+
+// numdiff_cal_flx: G = grad(Vh, Vh, Vv) (divided by the density if dens_div); the even boundary
+// routine supplies the lid exterior of Vh (and of Vv when bc_v)
+static void nd_grad(const Oracle& o, int var, const double* Vh, const double* Vv, const double* ddens, bool dens_div,
+                    bool bc_v, double* Gx, double* Gy, double* Gz) {
+  const int N1 = o.N1, Np = o.Np, Nfp = o.Nfp;
+  const double E[3] = {2.0 / o.dx, 2.0 / o.dy, 2.0 / o.dz};
+  const double FS[6] = {2.0 / o.dy, 2.0 / o.dx, 2.0 / o.dy, 2.0 / o.dx, 2.0 / o.dz, 2.0 / o.dz};
+#pragma omp parallel
+  {
+    std::vector<double> df(3 * 6 * Nfp), vh(Np), vv(Np);
+#pragma omp for schedule(static)
+    for (long ke = 0; ke < o.Ne; ++ke) {
+      for (int f = 0; f < 6; ++f)
+        for (int b = 0; b < N1; ++b)
+          for (int a = 0; a < N1; ++a) {
+            int i, j, k; face_node(N1, f, a, b, i, j, k);
+            const size_t iM = (size_t)ke * Np + o.nid(i, j, k);
+            bool lid; const size_t iP = ext_node(o, ke, f, a, b, lid);
+            const double nx = NX[f], ny = NY[f], nz = NZ[f];
+            double wP = 1.0, wM = 1.0;
+            if (dens_div) { wP = 1.0 / (ddens[iP] + o.dens_hyd[iP]); wM = 1.0 / (ddens[iM] + o.dens_hyd[iM]); }
+            double hP = Vh[iP], vP = Vv[iP];
+            if (lid) { hP = nd_even_ext(var, Vh[iM], nx, ny, nz); if (bc_v) vP = nd_even_ext(var, Vv[iM], nx, ny, nz); }
+            const double dh = 0.5 * (hP * wP - Vh[iM] * wM);
+            const double dv = 0.5 * (vP * wP - Vv[iM] * wM);
+            const int fp = f * Nfp + a + N1 * b;
+            if (lid) {
+              df[0 * 6 * Nfp + fp] = FS[f] * (dh * nx);
+              df[1 * 6 * Nfp + fp] = FS[f] * (dh * ny);
+              df[2 * 6 * Nfp + fp] = FS[f] * (dv * nz);
+            } else {
+              df[0 * 6 * Nfp + fp] = FS[f] * ((1.0 - fsign1(nx)) * dh * nx);
+              df[1 * 6 * Nfp + fp] = FS[f] * ((1.0 - fsign1(ny)) * dh * ny);
+              df[2 * 6 * Nfp + fp] = FS[f] * ((1.0 - fsign1(nz)) * dv * nz);
+            }
+          }
+      for (int p = 0; p < Np; ++p) {
+        const size_t g = (size_t)ke * Np + p;
+        if (dens_div) { vh[p] = Vh[g] / (ddens[g] + o.dens_hyd[g]); vv[p] = Vv[g] / (ddens[g] + o.dens_hyd[g]); }
+        else { vh[p] = Vh[g]; vv[p] = Vv[g]; }
+      }
+      for (int k = 0; k < N1; ++k)
+        for (int j = 0; j < N1; ++j)
+          for (int i = 0; i < N1; ++i) {
+            const size_t g = (size_t)ke * Np + o.nid(i, j, k);
+            Gx[g] = E[0] * nd_dx(o, vh.data(), 0, i, j, k) + nd_lift(o, &df[0], i, j, k);
+            Gy[g] = E[1] * nd_dx(o, vh.data(), 1, i, j, k) + nd_lift(o, &df[6 * Nfp], i, j, k);
+            Gz[g] = E[2] * nd_dx(o, vv.data(), 2, i, j, k) + nd_lift(o, &df[12 * Nfp], i, j, k);
+          }
+    }
+  }
+}
+
+// numdiff_cal_laplacian with the odd boundary routine on G: horizontal and vertical parts
+static void nd_lap(const Oracle& o, int var, const double* Gx, const double* Gy, const double* Gz, double* lh,
+                   double* lv) {
+  const int N1 = o.N1, Np = o.Np, Nfp = o.Nfp;
+  const double E[3] = {2.0 / o.dx, 2.0 / o.dy, 2.0 / o.dz};
+  const double FS[6] = {2.0 / o.dy, 2.0 / o.dx, 2.0 / o.dy, 2.0 / o.dx, 2.0 / o.dz, 2.0 / o.dz};
+#pragma omp parallel
+  {
+    std::vector<double> dfh(6 * Nfp), dfv(6 * Nfp);
+#pragma omp for schedule(static)
+    for (long ke = 0; ke < o.Ne; ++ke) {
+      for (int f = 0; f < 6; ++f)
+        for (int b = 0; b < N1; ++b)
+          for (int a = 0; a < N1; ++a) {
+            int i, j, k; face_node(N1, f, a, b, i, j, k);
+            const size_t iM = (size_t)ke * Np + o.nid(i, j, k);
+            bool lid; const size_t iP = ext_node(o, ke, f, a, b, lid);
+            const double nx = NX[f], ny = NY[f], nz = NZ[f];
+            double gM[3] = {Gx[iM], Gy[iM], Gz[iM]}, gP[3] = {Gx[iP], Gy[iP], Gz[iP]};
+            if (lid) nd_odd_ext(var, gM, nx, ny, nz, gP);
+            const int fp = f * Nfp + a + N1 * b;
+            if (lid) {
+              dfh[fp] = FS[f] * (0.5 * ((gP[0] - gM[0]) * nx + (gP[1] - gM[1]) * ny));
+              dfv[fp] = FS[f] * (0.5 * (gP[2] - gM[2]) * nz);
+            } else {
+              dfh[fp] = FS[f] * (0.5 * ((1.0 + fsign1(nx)) * (gP[0] - gM[0]) * nx + (1.0 + fsign1(ny)) * (gP[1] - gM[1]) * ny));
+              dfv[fp] = FS[f] * (0.5 * (1.0 + fsign1(nz)) * (gP[2] - gM[2]) * nz);
+            }
+          }
+      const double* gx = Gx + (size_t)ke * Np;
+      const double* gy = Gy + (size_t)ke * Np;
+      const double* gz = Gz + (size_t)ke * Np;
+      for (int k = 0; k < N1; ++k)
+        for (int j = 0; j < N1; ++j)
+          for (int i = 0; i < N1; ++i) {
+            const size_t g = (size_t)ke * Np + o.nid(i, j, k);
+            lh[g] = E[0] * nd_dx(o, gx, 0, i, j, k) + E[1] * nd_dx(o, gy, 1, i, j, k) + nd_lift(o, dfh.data(), i, j, k);
+            lv[g] = E[2] * nd_dx(o, gz, 2, i, j, k) + nd_lift(o, dfv.data(), i, j, k);
+          }
+    }
+  }
+}
+
+// numdiff_tend with the odd boundary routine on G, then var += dt tend
+static void nd_tend_update(const Oracle& o, int var, const double* Gx, const double* Gy, const double* Gz,
+                           const double* ddens, bool mul_dens, double ch, double cv, double dt, double* V) {
+  const int N1 = o.N1, Np = o.Np, Nfp = o.Nfp;
+  const double E[3] = {2.0 / o.dx, 2.0 / o.dy, 2.0 / o.dz};
+  const double FS[6] = {2.0 / o.dy, 2.0 / o.dx, 2.0 / o.dy, 2.0 / o.dx, 2.0 / o.dz, 2.0 / o.dz};
+#pragma omp parallel
+  {
+    std::vector<double> df(6 * Nfp), fx(Np), fy(Np), fz(Np);
+#pragma omp for schedule(static)
+    for (long ke = 0; ke < o.Ne; ++ke) {
+      for (int f = 0; f < 6; ++f)
+        for (int b = 0; b < N1; ++b)
+          for (int a = 0; a < N1; ++a) {
+            int i, j, k; face_node(N1, f, a, b, i, j, k);
+            const size_t iM = (size_t)ke * Np + o.nid(i, j, k);
+            bool lid; const size_t iP = ext_node(o, ke, f, a, b, lid);
+            const double nx = NX[f], ny = NY[f], nz = NZ[f];
+            double gM[3] = {Gx[iM], Gy[iM], Gz[iM]}, gP[3] = {Gx[iP], Gy[iP], Gz[iP]};
+            if (lid) nd_odd_ext(var, gM, nx, ny, nz, gP);
+            double wM = 0.5, wP = 0.5;
+            if (mul_dens) { wM = 0.5 * (o.dens_hyd[iM] + ddens[iM]); wP = 0.5 * (o.dens_hyd[iP] + ddens[iP]); }
+            double d;
+            if (lid) {
+              d = ch * (wP * gP[0] - wM * gM[0]) * nx + ch * (wP * gP[1] - wM * gM[1]) * ny + cv * (wP * gP[2] - wM * gM[2]) * nz;
+            } else {
+              d = (1.0 + fsign1(nx)) * ch * (wP * gP[0] - wM * gM[0]) * nx +
+                  (1.0 + fsign1(ny)) * ch * (wP * gP[1] - wM * gM[1]) * ny +
+                  (1.0 + fsign1(nz)) * cv * (wP * gP[2] - wM * gM[2]) * nz;
+            }
+            df[f * Nfp + a + N1 * b] = FS[f] * d;
+          }
+      for (int p = 0; p < Np; ++p) {
+        const size_t g = (size_t)ke * Np + p;
+        double h = ch, v = cv;
+        if (mul_dens) { h = ch * (o.dens_hyd[g] + ddens[g]); v = cv * (o.dens_hyd[g] + ddens[g]); }
+        fx[p] = h * Gx[g]; fy[p] = h * Gy[g]; fz[p] = v * Gz[g];
+      }
+      for (int k = 0; k < N1; ++k)
+        for (int j = 0; j < N1; ++j)
+          for (int i = 0; i < N1; ++i) {
+            const size_t g = (size_t)ke * Np + o.nid(i, j, k);
+            const double t = E[0] * nd_dx(o, fx.data(), 0, i, j, k) + E[1] * nd_dx(o, fy.data(), 1, i, j, k) +
+                             E[2] * nd_dx(o, fz.data(), 2, i, j, k) + nd_lift(o, df.data(), i, j, k);
+            V[g] = V[g] + dt * t;
+          }
+    }
+  }
+}
+
+// Apply: THERM, MOMZ, MOMX, MOMY, DENS in FElib's order (DDENS, the density weight of the others,
+// changes last); nlap = ND_LAPLACIAN_NUM, coef_h/v = ND_COEF_H/V, dt = the dynamics step
+static void numdiff_apply(const Oracle& o, double* const q[5], int nlap, double coef_h, double coef_v, double dt) {
+  const size_t n = (size_t)o.Np * o.Ne;
+  std::vector<double> Gx(n), Gy(n), Gz(n), lh(n), lv(n);
+  const double sgn = ((nlap + 1) % 2 == 0) ? 1.0 : -1.0;  // (-1)^mod(nlap+1, 2)
+  const int order[5] = {VRT, VMZ, VMX, VMY, VD};
+  for (int vi = 0; vi < 5; ++vi) {
+    const int var = order[vi];
+    const bool dw = var != VD;
+    nd_grad(o, var, q[var], q[var], q[VD], dw, true, Gx.data(), Gy.data(), Gz.data());
+    for (int it = 1; it < nlap; ++it) {
+      nd_lap(o, var, Gx.data(), Gy.data(), Gz.data(), lh.data(), lv.data());
+      nd_grad(o, var, lh.data(), lv.data(), q[VD], false, false, Gx.data(), Gy.data(), Gz.data());
+    }
+    nd_tend_update(o, var, Gx.data(), Gy.data(), Gz.data(), q[VD], dw, sgn * coef_h, sgn * coef_v, dt, q[var]);
+  }
+}
+
+// ---------------------------------------------------------------------------------
+// Sponge layer: Rayleigh damping of w (and optionally u, v) towards zero above a height
+//   ..._dgm_spongelayer.F90:134-219 (add_tend, calc_wdampcoef)
+// ---------------------------------------------------------------------------------
+static void sponge_add_tend(const Oracle& o, double* const tend[3], const double* const mom[3], double tau,
+                            double height, int hvel) {
+  const int N1 = o.N1, Np = o.Np;
+  const double s = hvel ? 1.0 : 0.0;
+  const double ztop = o.zmax, rt = 1.0 / tau;
+#pragma omp parallel for schedule(static)
+  for (long ke = 0; ke < o.Ne; ++ke) {
+    const int ez = (int)(ke / ((long)o.NeX * o.NeY));
+    for (int k = 0; k < N1; ++k) {
+      const double z = o.zmin + (ez + 0.5 * (o.e.x[k] + 1.0)) * o.dz;
+      const double c = 0.25 * rt * (1.0 + fsign1(z - height)) * (1.0 - std::cos(M_PI * (z - height) / (ztop - height)));
+      for (int p = k * N1 * N1; p < (k + 1) * N1 * N1; ++p) {
+        const size_t g = (size_t)ke * Np + p;
+        tend[0][g] = tend[0][g] - s * c * mom[0][g];
+        tend[1][g] = tend[1][g] - s * c * mom[1][g];
+        tend[2][g] = tend[2][g] - c * mom[2][g];
+      }
+    }
+  }
+}
+
 }  // namespace
 
 // =================================================================================
@@ -1428,6 +1676,18 @@ void orc_trc_step(void* h, double* QTRC, const double* const* mflx, const double
   }
   TrcStepArgs A{nstage, sig, gam, c, dt, limiter, tmar, filter};
   for (int s = 0; s < nsteps; ++s) trc_step(*o, tf, A, QTRC, mflx, aM, aP, ddens_trc, ddens0_trc, ddens, rhoq_tp);
+}
+
+
+// ---- numerical diffusion and sponge layer ----
+// q = {DDENS, MOMX, MOMY, MOMZ, DRHOT}, updated in place
+void orc_numdiff_apply(void* h, double* const* q, int nlap, double coef_h, double coef_v, double dt) {
+  numdiff_apply(*static_cast<Oracle*>(h), q, nlap, coef_h, coef_v, dt);
+}
+// tend = {MOMX_dt, MOMY_dt, MOMZ_dt} (in/out), mom = {MOMX, MOMY, MOMZ}
+void orc_sponge_add_tend(void* h, double* const* tend, const double* const* mom, double tau, double height,
+                         int hvel) {
+  sponge_add_tend(*static_cast<Oracle*>(h), tend, mom, tau, height, hvel);
 }
 
 }  // extern "C"

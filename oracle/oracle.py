@@ -84,6 +84,9 @@ def _load():
                                    ctypes.c_double, ctypes.c_double, ctypes.c_int]
     lib.orc_trc_step.argtypes = [ctypes.c_void_p, _dp, pp, _dp, _dp, _dp, _dp, _dp, _dp, ctypes.c_int, _dp, _dp,
                                  _dp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, ctypes.c_int]
+    lib.orc_numdiff_apply.argtypes = [ctypes.c_void_p, pp, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                      ctypes.c_double]
+    lib.orc_sponge_add_tend.argtypes = [ctypes.c_void_p, pp, pp, ctypes.c_double, ctypes.c_double, ctypes.c_int]
     _lib = lib
     return lib
 
@@ -287,3 +290,20 @@ class Oracle:
                               _ptr(sig), _ptr(gam), _ptr(c), float(dt), int(bool(limiter)), int(bool(tmar)),
                               int(bool(filter)), _ptr(filt), int(nsteps))
         return q
+
+    # ---- numerical diffusion (nonhydro3d_numdiff.F90) and sponge layer (dgm_spongelayer.F90) ----
+    def numdiff_apply(self, q, nlap, coef_h, coef_v, dt):
+        """returns a copy of the 5 fields after the hyperdiffusion filter"""
+        qs = [np.array(a, np.float64, copy=True, order="C") for a in q]
+        pq, _k = _pp(qs)
+        self.lib.orc_numdiff_apply(self._h, pq, int(nlap), float(coef_h), float(coef_v), float(dt))
+        return qs
+
+    def sponge_add_tend(self, tend, mom, tau, height, hvel=False):
+        """returns copies of (MOMX_dt, MOMY_dt, MOMZ_dt) with the Rayleigh damping added"""
+        ts = [np.array(a, np.float64, copy=True, order="C") for a in tend]
+        ms = [_c64(a) for a in mom]
+        pt, _k1 = _pp(ts)
+        pm, _k2 = _pp(ms)
+        self.lib.orc_sponge_add_tend(self._h, pt, pm, float(tau), float(height), int(bool(hvel)))
+        return ts

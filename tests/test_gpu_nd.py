@@ -1,0 +1,63 @@
+"""GPU parity of the numerical diffusion (FElib's hyperdiffusion filter,
+FElib/src/fluid_dyn_solver/scale_atm_dyn_dgm_nonhydro3d_numdiff.F90:214-721 with the lid values of
+..._dgm_bnd.F90:370-508) and of the sponge layer (..._dgm_spongelayer.F90:134-219) against the FP64
+CPU oracle, through the C ABI.
+
+Tolerance: the change each call makes to a field, relative (max norm) to the largest change, 1e-11
+(FP64 on both sides; only the summation order inside the contractions differs); sponge 1e-14.
+"""
+import numpy as np
+import pytest
+
+from conftest import have_gpu
+
+pytestmark = [pytest.mark.gpu, pytest.mark.skipif(not have_gpu(), reason="needs a CUDA GPU")]
+
+import oracle as orc  # noqa: E402
+from fedg import cases  # noqa: E402
+from fedg import lib as fl  # noqa: E402
+
+VARS = ("DDENS", "MOMX", "MOMY", "MOMZ", "DRHOT")
+
+
+def setup(case, seed):
+    q, b = cases.initial_state(case)
+    rng = np.random.default_rng(seed)
+    sc = [1e-3 * b["dens_hyd"], 2.0, 2.0, 1.0, 0.3]
+    q = [q[v] + sc[v] * rng.standard_normal(q[v].shape) for v in range(5)]
+    o = orc.Oracle(case.porder, case.NeX, case.NeY, case.NeZ, case.dom, grav=case.grav)
+    o.set_base_state(b["dens_hyd"], b["pres_hyd"])
+    ctx = fl.Context(case)
+    ctx.set_base_state(b["dens_hyd"], b["pres_hyd"], b["therm_hyd"])
+    return o, ctx, q, b
+
+
+@pytest.mark.parametrize("porder,ne", [(3, (4, 3, 4)), (7, (2, 2, 3)), (2, (3, 4, 3))])
+@pytest.mark.parametrize("nlap", [1, 2, 3])
+def test_numdiff_apply(porder, ne, nlap):
+    case = cases.C1().scaled(*ne, porder=porder)
+    o, ctx, q, b = setup(case, seed=10 + nlap)
+    coef = {1: 2.0e2, 2: 5.0e5, 3: 1.0e9}[nlap]
+    ref = o.numdiff_apply(q, nlap, coef, 0.5 * coef, 0.01)
+    qd = [ctx.tensor(a) for a in q]
+    ctx.numdiff_apply(qd, nlap, coef, 0.5 * coef, 0.01)
+    for v in range(5):
+        got = qd[v].cpu().numpy()
+        dref = ref[v] - q[v]
+        err = np.max(np.abs((got - q[v]) - dref)) / max(np.max(np.abs(dref)), 1e-300)
+        assert err < 1e-11, (VARS[v], err)
+
+
+def test_sponge_add_tend():
+    case = cases.C1().scaled(3, 3, 8)
+    o, ctx, q, b = setup(case, seed=3)
+    rng = np.random.default_rng(4)
+    tend = [rng.standard_normal(o.shape) for _ in range(3)]
+    mom = [q[1], q[2], q[3]]
+    for hv in (False, True):
+        ref = o.sponge_add_tend(tend, mom, 20.0, 600.0, hv)
+        td = [ctx.tensor(a) for a in tend]
+        ctx.sponge_add_tend(td, [ctx.tensor(a) for a in mom], 20.0, 600.0, hv)
+        for d in range(3):
+            got = td[d].cpu().numpy()
+            assert np.max(np.abs(got - ref[d])) <= 1e-14 * max(1.0, np.max(np.abs(ref[d]))), (d, hv)

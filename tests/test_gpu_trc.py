@@ -220,3 +220,50 @@ def test_update_properties_at_size():
     ctx.trc_update(Qbd, mf, aM, aP, qd[0], qd[0], case.dt, nsteps=10, limiter=True, tmar=True)
     got = np_(Qbd)
     assert got.min() >= -1e-14 and got.max() > 0.01
+
+
+# ---- the float-pair tracer step (fedg_trc_opts.prec = FEDG_PREC_PAIR) ----
+PAIR_TOL = 1e-11  # FP64-class float pairs (relative rounding ~1e-14 per operation) against the FP64 oracle
+
+
+@pytest.mark.parametrize("porder,ne,steps", [(3, (6, 6, 3), 20), (7, (3, 3, 2), 6), (2, (5, 4, 3), 10)])
+@pytest.mark.parametrize("limiter", [True, False])
+def test_update_pair_advection_test(porder, ne, steps, limiter):
+    case = t1(ne, porder)
+    o, ctx, q, b, Q = setup(case)
+    mf = [q[1], q[2], q[3]]
+    aM, aP = o.trc_alphdens_advtest(q[0], q[1], q[2], q[3])
+    ref = o.trc_step(Q, mf, aM, aP, q[0], q[0], case.dt, nsteps=steps, limiter=limiter, tmar=True)
+    qd = [ctx.tensor(a) for a in q]
+    Qd = ctx.tensor(Q)
+    ctx.trc_update(Qd, [qd[1], qd[2], qd[3]], ctx.tensor(aM), ctx.tensor(aP), qd[0], qd[0], case.dt, nsteps=steps,
+                   limiter=limiter, tmar=True, prec=fl.PREC_PAIR)
+    got = np_(Qd)
+    assert rel_l2(got, ref) < PAIR_TOL, rel_l2(got, ref)
+    if limiter:
+        assert got.min() >= -1e-14
+
+
+def test_update_pair_coupled_densities_filter_and_source():
+    case = cases.C1().scaled(4, 4, 3)
+    case = cases.replace(case, tracer=dict(qmax=2.0, rx=200.0, ry=200.0, rz=150.0, xc=250.0, yc=250.0, zc=180.0))
+    o, ctx, q, b, Q = setup(case, seed=8, wobble=0.3)
+    rng = np.random.default_rng(9)
+    mf_o = [np.zeros(o.shape) for _ in range(3)]
+    aM, aP = np.zeros(o.face_shape), np.zeros(o.face_shape)
+    for s, w in enumerate((1 / 6, 1 / 6, 2 / 3), start=1):
+        qs = [a.copy() for a in q]
+        qs[1] = qs[1] + 2.0 * s
+        o.trc_save_massflux(s, qs, w, w, 0, mf_o, aM, aP)
+    ddens0 = q[0]
+    ddens_trc = q[0] + 1e-4 * b["dens_hyd"] * rng.standard_normal(o.shape)
+    ddens = q[0] + 2e-4 * b["dens_hyd"] * rng.standard_normal(o.shape)
+    rhoq = 1e-5 * np.abs(rng.standard_normal(o.shape))
+    filt = dict(etac_h=2.0 / 3.0, alpha_h=36.0, ord_h=16, etac_v=0.5, alpha_v=30.0, ord_v=12)
+    ref = o.trc_step(Q, mf_o, aM, aP, ddens_trc, ddens0, 0.02, nsteps=8, ddens=ddens, rhoq_tp=rhoq, limiter=True,
+                     tmar=True, filter=filt)
+    Qd = ctx.tensor(Q)
+    ctx.trc_update(Qd, [ctx.tensor(m) for m in mf_o], ctx.tensor(aM), ctx.tensor(aP), ctx.tensor(ddens_trc),
+                   ctx.tensor(ddens0), 0.02, nsteps=8, ddens=ctx.tensor(ddens), rhoq_tp=ctx.tensor(rhoq),
+                   limiter=True, tmar=True, filter=filt, prec=fl.PREC_PAIR)
+    assert rel_l2(np_(Qd), ref) < PAIR_TOL

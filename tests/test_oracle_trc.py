@@ -183,3 +183,100 @@ def test_ssp3_tables_consistent():
         for j in range(ns):
             A[i, j] = gam[i, j] + sum(sig[i, k] * A[k, j] for k in range(i))
     assert np.allclose(A[:ns].sum(axis=1), tb["c"], atol=1e-15)
+
+
+# ---- numerical diffusion (nonhydro3d_numdiff.F90) and sponge layer (dgm_spongelayer.F90) ----
+def _nd_case(porder=3, ne=(8, 2, 4)):
+    return cases.Case("nd", porder, *ne, (0.0, 8000.0, 0.0, 2000.0, 0.0, 4000.0), "HEVE", dt=1.0, nsteps=1,
+                      base="constPT", grav=0.0, filter_on=False)
+
+
+def _nd_setup(case):
+    q, b = cases.initial_state(case)
+    o = orc.Oracle(case.porder, case.NeX, case.NeY, case.NeZ, case.dom, grav=case.grav)
+    o.set_base_state(b["dens_hyd"], b["pres_hyd"])
+    return o, q, b
+
+
+@pytest.mark.parametrize("nlap,porder", [(1, 5), (2, 7)])
+def test_numdiff_damps_a_fourier_mode_at_its_rate(nlap, porder):
+    """(-1)^(n+1) coef nabla^(2n) on sin(2 pi x / L): one application multiplies the mode by
+    1 - coef dt (2 pi / L)^(2n) (uniform density, 8 elements per wavelength).  The iterated
+    operator needs the higher order: the one-sided LDG Laplacian's nodal error sits in high modes,
+    which the second application amplifies."""
+    case = _nd_case(porder=porder)
+    o, q, b = _nd_setup(case)
+    L = case.dom[1]
+    kx = 2 * np.pi / L
+    dt = 1.0
+    coef = 0.02 / (kx ** (2 * nlap) * dt)  # 2 % damping per application
+    q[4] = 0.5 * np.sin(kx * b["x"])
+    out = o.numdiff_apply(q, nlap, coef, coef, dt)
+    ratio = (out[4] * q[4]).sum() / (q[4] * q[4]).sum()
+    assert abs(ratio - (1.0 - 0.02)) < (1e-5 if nlap == 1 else 5e-5), ratio
+    # the other variables (uniform momentum in x only, zero elsewhere) do not move
+    for v in (0, 1, 2, 3):
+        assert np.max(np.abs(out[v] - q[v])) < 1e-12 * max(1.0, np.max(np.abs(q[v])))
+
+
+def test_numdiff_biharmonic_is_the_laplacian_twice():
+    """ND_LAPLACIAN_NUM = 2 applies the one-sided LDG Laplacian twice (apply_numfilter's loop,
+    numdiff.F90:313-357), with the sign (-1)^(n+1): B u = -L(L u) for a smooth x-mode"""
+    case = _nd_case(porder=3, ne=(8, 2, 2))
+    o, q, b = _nd_setup(case)
+    u = 0.5 * np.sin(2 * np.pi * b["x"] / case.dom[1])
+    q[4] = u
+    Lu = o.numdiff_apply(q, 1, 1.0, 1.0, 1.0)[4] - u
+    q2 = list(q)
+    q2[4] = Lu
+    LLu = o.numdiff_apply(q2, 1, 1.0, 1.0, 1.0)[4] - Lu
+    Bu = o.numdiff_apply(q, 2, 1.0, 1.0, 1.0)[4] - u
+    assert np.max(np.abs(Bu + LLu)) < 1e-5 * np.max(np.abs(LLu))
+
+
+def test_numdiff_conserves_and_is_dissipative():
+    """random fields: the exact-mass integrals of DRHOT and DDENS are kept (zero flux through the
+    periodic faces and the lids), and the L2 norm of DRHOT decreases"""
+    case = _nd_case(porder=3, ne=(4, 3, 3))
+    o, q, b = _nd_setup(case)
+    rng = np.random.default_rng(0)
+    q[4] = rng.standard_normal(o.shape)
+    q[0] = 1e-3 * rng.standard_normal(o.shape)
+    q[3] = rng.standard_normal(o.shape)
+    ones = np.zeros(o.shape)
+    for nlap in (1, 2):
+        out = o.numdiff_apply(q, nlap, 1.0e3 if nlap == 1 else 1.0e5, 1.0e3 if nlap == 1 else 1.0e5, 0.05)
+        for v in (0, 4):
+            m0 = _mass_exact(o, np.ones(o.shape), q[v])
+            m1 = _mass_exact(o, np.ones(o.shape), out[v])
+            assert abs(m1 - m0) < 1e-12 * np.abs(q[v]).sum() * (o.Np ** 0), (v, m0, m1)
+        assert np.linalg.norm(out[4]) < np.linalg.norm(q[4])
+    del ones
+
+
+def test_numdiff_constant_state_unchanged():
+    case = _nd_case(porder=3, ne=(3, 3, 3))
+    o, q, b = _nd_setup(case)
+    q[4] = q[4] + 7.0
+    q[1] = 3.0 * (b["dens_hyd"] + q[0])  # constant velocity: MOMX/dens is uniform
+    out = o.numdiff_apply(q, 2, 1e5, 1e5, 0.1)
+    for v in range(5):
+        assert np.max(np.abs(out[v] - q[v])) < 1e-11 * max(1.0, np.max(np.abs(q[v])))
+
+
+def test_sponge_matches_formula():
+    case = _nd_case(porder=3, ne=(2, 2, 6))
+    o, q, b = _nd_setup(case)
+    rng = np.random.default_rng(1)
+    mom = [rng.standard_normal(o.shape) for _ in range(3)]
+    tend = [rng.standard_normal(o.shape) for _ in range(3)]
+    tau, h = 30.0, 2500.0
+    ztop = case.dom[5]
+    z = b["z"]
+    c = 0.25 / tau * (1.0 + np.where(z - h >= 0, 1.0, -1.0)) * (1.0 - np.cos(np.pi * (z - h) / (ztop - h)))
+    for hv in (False, True):
+        out = o.sponge_add_tend(tend, mom, tau, h, hv)
+        s = 1.0 if hv else 0.0
+        assert np.allclose(out[2], tend[2] - c * mom[2], rtol=1e-14, atol=1e-14)
+        assert np.allclose(out[0], tend[0] - s * c * mom[0], rtol=1e-14, atol=1e-14)
+    assert np.all(c[z < h] == 0.0) and c.max() > 0
