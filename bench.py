@@ -456,20 +456,29 @@ def run_fedg(args):
         ke = max(1, min(args.steps, 2))
         q_e = [torch.empty_like(t) for t in qd]
         torch.cuda.synchronize()
+        ph = [0.0, 0.0, 0.0]  # seconds in H2D, the step, D2H
         t0 = time.perf_counter()
         for _ in range(ke):
+            ta = time.perf_counter()
             for dst, src in zip(q_e, q_host):
                 dst.copy_(src, non_blocking=True)
             torch.cuda.synchronize()
+            tb = time.perf_counter()
             ctx.update(q_e, 1, sync=False, **opts)
             ctx.sync()
+            tc = time.perf_counter()
             for dst, src in zip(q_host, q_e):
                 dst.copy_(src, non_blocking=True)
             torch.cuda.synchronize()
+            td = time.perf_counter()
+            ph[0] += tb - ta
+            ph[1] += tc - tb
+            ph[2] += td - tc
         t1 = time.perf_counter()
         nb = sum(t.numel() * 8 for t in qd)
         e2e = {"value": dofs_stage * ke / (t1 - t0), "unit": UNIT, "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb,
-               "steps": ke}
+               "steps": ke, "ms_per_step": {"h2d": 1e3 * ph[0] / ke, "update": 1e3 * ph[1] / ke, "d2h": 1e3 * ph[2] / ke},
+               "copy_gbs": {"h2d": nb * ke / max(ph[0], 1e-9) / 1e9, "d2h": nb * ke / max(ph[2], 1e-9) / 1e9}}
         del q_e
 
     # the headline path without the learned guess, the other precision mode, and the plain FP64 path, on

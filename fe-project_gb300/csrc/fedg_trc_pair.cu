@@ -119,6 +119,29 @@ __device__ __forceinline__ f2 elem_sum_p(f2 v, float2* s_red, int le, int p) {
   }
 }
 
+// per-face sums of the weighted integrands sf[6][NF] of element le into s_out[le][0..5]: one warp
+// per face when the element has at least 6 warps, else one thread per face (the caller synchronises)
+template <int N1>
+__device__ __forceinline__ void face_sums_p(const float2* sf, float2* s_out, int le, int p, bool valid) {
+  constexpr int Np = N1 * N1 * N1, NF = N1 * N1;
+  if constexpr (Np >= 6 * 32) {
+    const int f = p >> 5, lane = p & 31;
+    if (f < 6) {
+      f2 s = zero2();
+      for (int q = lane; q < NF; q += 32) s = s + f2_of(sf[f * NF + q]);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s = s + shfl_xor(s, o);
+      if (valid && lane == 0) s_out[le * 8 + f] = f2_pack(s);
+    }
+  } else {
+    if (valid && p < 6) {
+      f2 s = zero2();
+      for (int q = 0; q < NF; ++q) s = s + f2_of(sf[p * NF + q]);
+      s_out[le * 8 + p] = f2_pack(s);
+    }
+  }
+}
+
 template <int N1>
 __device__ __forceinline__ void face_nodes_p(const TrcOpsP& op, int f, int a, int b, long ke, int ex, int ey, int ez,
                                              int nxy, int& pM, size_t& gP, long& kn) {
@@ -200,11 +223,7 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
     v = f2_of(op.J) * ((f2_of(op.w[i]) * f2_of(op.w[j])) * f2_of(op.w[k])) * m;
   }
   const f2 qe = elem_sum_p<N1, EPB>(v, s_red, le, p);
-  if (valid && p < 6) {
-    f2 s = zero2();
-    for (int q = 0; q < NF; ++q) s = s + f2_of(sf[p * NF + q]);
-    s_out[le * 8 + p] = f2_pack(s);
-  }
+  face_sums_p<N1>(sf, s_out, le, p, valid);
   __syncthreads();
   if (valid && p == 0) {
     f2 net = zero2();
@@ -216,7 +235,7 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
 }
 
 template <int N1, int EPB>
-__global__ void __launch_bounds__(EPB* N1* N1* N1)
+__global__ void __launch_bounds__(EPB* N1* N1* N1, (N1 == 8 ? 3 : 1))
     k_trc_stage_p(const TrcOpsP op, const double* __restrict__ dens_prof, const InP in, const StageP st, int Ne) {
   constexpr int Np = N1 * N1 * N1, NF = N1 * N1;
   extern __shared__ float2 smp[];
@@ -261,11 +280,7 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
     }
   }
   __syncthreads();
-  if (valid && p < 6) {
-    f2 s = zero2();
-    for (int qq = 0; qq < NF; ++qq) s = s + f2_of(sf[p * NF + qq]);
-    s_out[le * 8 + p] = f2_pack(s);
-  }
+  face_sums_p<N1>(sf, s_out, le, p, valid);
   __syncthreads();
   if (valid) {  // del_flux = Fscale (numflux R - q- m-), R = R- on outflow faces, R+ on inflow faces
     for (int fi = p; fi < 6 * NF; fi += Np) {
