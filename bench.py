@@ -395,6 +395,8 @@ def run_fedg(args):
     if net is not None:
         net.attach(ctx)
     stream = torch.cuda.ExternalStream(ctx.stream_handle)
+    if args.tol is not None:
+        PATH_TOL[path] = args.tol
     opts = dict(prec=prec, dt=DT_STABLE, max_iter=PATH_ITER[path], tol=PATH_TOL[path], use_guess=use_guess)
 
     # warm-up
@@ -450,7 +452,11 @@ def run_fedg(args):
     fp64_tf = fp64_dgemm_tflops(torch, ctx.dev) if rank == 0 else 0.0
     gpu_launches = sum(v[1] for v in prof.values())
 
-    # end to end through the public API with host buffers: H2D of the state, one step, D2H
+    # end to end through the public API with host buffers: H2D of the state, one step, D2H.  It starts
+    # from the state the timed region ended at (the same point of the same simulation), copied to the
+    # pinned host buffers; the comparisons below start from there too.
+    for h_, t_ in zip(q_host, qd):
+        h_.copy_(t_)
     e2e = None
     if rank == 0 and not args.no_e2e:
         ke = max(1, min(args.steps, 2))
@@ -570,6 +576,7 @@ def main():
     ap.add_argument("--impl", choices=["fedg", "reference"], default="fedg")
     ap.add_argument("--path", choices=["pair", "mixed", "fp64"], default=os.environ.get("FEDG_BENCH_PATH", "pair"))
     ap.add_argument("--guess", type=int, default=1)
+    ap.add_argument("--tol", type=float, default=None, help="Newton tolerance of the timed path (default per path)")
     ap.add_argument("--train-steps", type=int, default=2000)
     ap.add_argument("--compare-steps", type=int, default=4,
                     help="steps of the accuracy comparison against the plain FP64 path")

@@ -623,7 +623,12 @@ int fedg_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_o
   if (!c->base_set) return fail("fedg_update: base state not set");
   if (o->eqs != FEDG_HEVE && o->eqs != FEDG_HEVI) return fail("fedg_update: bad eqs");
   CK(cudaSetDevice(c->d.device));
-  if (o->prec == FEDG_PREC_MIXED || o->prec == FEDG_PREC_PAIR) return mixed_update(c, q, nsteps, o, iters_out);
+  if (o->prec == FEDG_PREC_MIXED || o->prec == FEDG_PREC_PAIR) {
+    if (c->trc_flux[0])
+      return fail("fedg_update: tracer flux outputs (fedg_update_set_tracer_flux) need prec FEDG_PREC_FP64");
+    if (c->sl_tau > 0.0) return fail("fedg_update: the sponge layer (fedg_update_set_sponge) needs prec FEDG_PREC_FP64");
+    return mixed_update(c, q, nsteps, o, iters_out);
+  }
   if (o->prec != FEDG_PREC_FP64) return fail("fedg_update: bad prec");
   const int scheme = o->eqs == FEDG_HEVE ? FEDG_SSP_RK3 : FEDG_IMEX_ARK232;
   int r = 0;
@@ -641,7 +646,11 @@ int fedg_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_o
   const double* base[16] = {};
   long long nsum = 0, ncnt = 0;
   int nfail = 0;
+  double* const* tf = c->trc_flux;
+  const size_t nb64 = sizeof(double) * c->n;
   for (int step = 0; step < nsteps && r >= 0; ++step) {
+    if (tf[0] && cudaMemcpyAsync(tf[6], q[0], nb64, cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess)
+      return fail("fedg_update: DDENS0_TRC copy");
     if (o->eqs == FEDG_HEVI) r = fedg_tint_store_var0(t, q);
     for (int s = 1; s <= t->nstage && r >= 0; ++s) {
       if (o->eqs == FEDG_HEVI) {
@@ -671,14 +680,54 @@ int fedg_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_o
               fedg_tint_tend_ex(t, s, 3), fedg_tint_tend_ex(t, s, 4)}};
       r = tracked(c, FEDG_K_TEND, [&] { return launch_tend_fp64(c->op, c->prof(), qc, dp, tex, c->Ne, o->eqs, c->stream); });
       if (r) return cuda_fail((cudaError_t)r, "fedg_update: cal_tend");
+      if (c->sl_tau > 0.0) {  // sponge layer on the explicit tendency (driver_nonhydro3d.F90:831-841)
+        double* const tm[3] = {tex.v[1], tex.v[2], tex.v[3]};
+        const double* const mm[3] = {q[1], q[2], q[3]};
+        r = fedg_sponge_add_tend(c, tm, mm, c->sl_tau, c->sl_height, c->sl_hvel);
+        if (r) return r;
+      }
+      if (tf[0]) {  // save_massflux of the stage state (driver_nonhydro3d.F90:900-917)
+        static const double b_ssp3[3] = {1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0};
+        const double w_h = o->eqs == FEDG_HEVI ? t->b_ex[s - 1] : b_ssp3[s - 1];
+        const double w_v = o->eqs == FEDG_HEVI ? t->b_im[s - 1] : b_ssp3[s - 1];
+        double* const mf[3] = {tf[0], tf[1], tf[2]};
+        r = fedg_trc_save_massflux(c, s, q, dp, w_h, w_v, o->eqs == FEDG_HEVI, mf, tf[3], tf[4]);
+        if (r) return r;
+      }
       r = fedg_tint_advance(t, s, q);
     }
+    // DENS_TRC: the density before the modal filter (driver_nonhydro3d.F90:920-935)
+    if (r >= 0 && tf[0] && cudaMemcpyAsync(tf[5], q[0], nb64, cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess)
+      return fail("fedg_update: DDENS_TRC copy");
     if (r >= 0 && c->d.mf_on) r = fedg_modalfilter(c, q);
   }
   (void)base;
   if (r < 0) return r;
   if (iters_out) *iters_out = ncnt ? double(nsum) / double(ncnt) : 0.0;
   return nfail;
+}
+
+int fedg_update_set_sponge(fedg_ctx* c, double tau, double height, int hveldamp) {
+  if (!c) return fail("fedg_update_set_sponge: null context");
+  if (tau > 0.0 && !(height < c->d.zmax)) return fail("fedg_update_set_sponge: the damping height must be below the top");
+  c->sl_tau = tau > 0.0 ? tau : 0.0;
+  c->sl_height = height;
+  c->sl_hvel = hveldamp != 0;
+  return 0;
+}
+
+int fedg_update_set_tracer_flux(fedg_ctx* c, double* const mflx[3], double* alph_M, double* alph_P,
+                                double* DDENS_TRC, double* DDENS0_TRC) {
+  if (!c) return fail("fedg_update_set_tracer_flux: null context");
+  if (!mflx) {
+    for (int i = 0; i < 7; ++i) c->trc_flux[i] = nullptr;
+    return 0;
+  }
+  if (!mflx[0] || !mflx[1] || !mflx[2] || !alph_M || !alph_P || !DDENS_TRC || !DDENS0_TRC)
+    return fail("fedg_update_set_tracer_flux: null field");
+  double* const v[7] = {mflx[0], mflx[1], mflx[2], alph_M, alph_P, DDENS_TRC, DDENS0_TRC};
+  for (int i = 0; i < 7; ++i) c->trc_flux[i] = v[i];
+  return 0;
 }
 
 // ---------------- column-guess network ----------------

@@ -36,6 +36,13 @@ struct fedg_ctx {
   double* trc_buf = nullptr;      // tracer update scratch: two stage fields, var0, varTmp, FCT per element
   double* nd_buf = nullptr;       // numerical-diffusion scratch: gradient (3 fields), Laplacian (2 fields)
   double* sponge_coef = nullptr;  // sponge-layer coefficient per level
+  double sponge_key[2] = {-1.0, -1.0};  // (tau, height) of the uploaded profile
+  // tracer transport outputs of fedg_update (fedg_update_set_tracer_flux): MFLX_x/y/z, alph_dens_M/P,
+  // DDENS_TRC, DDENS0_TRC (caller's device arrays; none when trc_flux[0] is null)
+  double* trc_flux[7] = {};
+  // sponge layer inside fedg_update (fedg_update_set_sponge; off when sl_tau <= 0)
+  double sl_tau = 0.0, sl_height = 0.0;
+  int sl_hvel = 0;
   // kernel timers / launch counters
   bool prof_on = false;
   long long nlaunch[FEDG_K_COUNT] = {};

@@ -373,9 +373,14 @@ int fedg_sponge_add_tend(fedg_ctx* c, double* const tend[3], const double* const
     c->sponge_coef = nullptr;
     return api_fail("fedg_sponge_add_tend: out of device memory");
   }
-  if (cudaMemcpyAsync(c->sponge_coef, coef.data(), sizeof(double) * c->L, cudaMemcpyHostToDevice, c->stream) !=
-      cudaSuccess)
-    return api_fail("fedg_sponge_add_tend: coefficient upload");
+  const bool upload = !(c->sponge_key[0] == tau && c->sponge_key[1] == height);
+  if (upload) {  // the profile is uploaded only when (tau, height) change
+    if (cudaMemcpyAsync(c->sponge_coef, coef.data(), sizeof(double) * c->L, cudaMemcpyHostToDevice, c->stream) !=
+        cudaSuccess)
+      return api_fail("fedg_sponge_add_tend: coefficient upload");
+    c->sponge_key[0] = tau;
+    c->sponge_key[1] = height;
+  }
   const int r = tracked(c, FEDG_K_ND, [&] {
     k_sponge<<<(unsigned)((c->n + 255) / 256), 256, 0, c->stream>>>(c->sponge_coef, tend[0], tend[1], tend[2], mom[0],
                                                                    mom[1], mom[2], hveldamp ? 1.0 : 0.0, c->N1, c->Np,
@@ -384,7 +389,7 @@ int fedg_sponge_add_tend(fedg_ctx* c, double* const tend[3], const double* const
   });
   if (r) return api_cuda_fail((cudaError_t)r, "fedg_sponge_add_tend");
   // the host coefficient array must outlive the asynchronous copy
-  if (cudaStreamSynchronize(c->stream) != cudaSuccess) return api_fail("fedg_sponge_add_tend: synchronise");
+  if (upload && cudaStreamSynchronize(c->stream) != cudaSuccess) return api_fail("fedg_sponge_add_tend: synchronise");
   return 0;
 }
 

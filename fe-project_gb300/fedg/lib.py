@@ -34,6 +34,7 @@ EXPORTED = [
     "fedg_guess_predict", "fedg_guess_load", "fedg_cal_tend_ex_noalloc",
     "fedg_trc_alphdens_advtest", "fedg_trc_save_massflux", "fedg_trc_fct_coef", "fedg_trc_cal_tend",
     "fedg_trc_tmar", "fedg_trc_modalfilter", "fedg_trc_update", "fedg_numdiff_apply", "fedg_sponge_add_tend",
+    "fedg_update_set_tracer_flux", "fedg_update_set_sponge",
 ]
 
 # kernel classes of fedg_prof_read (include/fedg.h)
@@ -135,6 +136,8 @@ def load():
     lib.fedg_trc_modalfilter.argtypes = [_vp, _vp, _vp, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                          ctypes.c_double, ctypes.c_double, ctypes.c_int]
     lib.fedg_trc_update.argtypes = [_vp, _vp, _P3, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.POINTER(TrcOpts)]
+    lib.fedg_update_set_tracer_flux.argtypes = [_vp, _P3, _vp, _vp, _vp, _vp]
+    lib.fedg_update_set_sponge.argtypes = [_vp, ctypes.c_double, ctypes.c_double, ctypes.c_int]
     lib.fedg_numdiff_apply.argtypes = [_vp, _P5, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double]
     lib.fedg_sponge_add_tend.argtypes = [_vp, _P3, _P3, ctypes.c_double, ctypes.c_double, ctypes.c_int]
     lib.fedg_prof_enable.argtypes = [_vp, ctypes.c_int]
@@ -353,6 +356,24 @@ class Context:
         if sync:
             self.sync()
         return Q
+
+    def set_sponge(self, tau, height=0.0, hveldamp=False):
+        """sponge layer inside update() (FP64 path); tau <= 0 turns it off"""
+        _check(self.lib.fedg_update_set_sponge(self.h, float(tau), float(height), int(bool(hveldamp))),
+               "fedg_update_set_sponge")
+
+    def set_tracer_flux(self, outs):
+        """outs = [MFLX_x, MFLX_y, MFLX_z, alph_M, alph_P, DDENS_TRC, DDENS0_TRC] device tensors filled by
+        update() (FP64 path), or None to clear"""
+        if outs is None:
+            _check(self.lib.fedg_update_set_tracer_flux(self.h, None, None, None, None, None),
+                   "fedg_update_set_tracer_flux")
+            self._trc_keep = None
+            return
+        self._trc_keep = outs
+        _check(self.lib.fedg_update_set_tracer_flux(self.h, (ctypes.c_void_p * 3)(*[m.data_ptr() for m in outs[:3]]),
+                                                    _ptr(outs[3]), _ptr(outs[4]), _ptr(outs[5]), _ptr(outs[6])),
+               "fedg_update_set_tracer_flux")
 
     # -- numerical diffusion (nonhydro3d_numdiff.F90) and sponge layer (dgm_spongelayer.F90) --
     def numdiff_apply(self, q, nlap, coef_h, coef_v, dt):

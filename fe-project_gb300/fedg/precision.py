@@ -74,6 +74,8 @@ PATHS = {
     "plain_fp64_tol1e-13": (fl.PREC_FP64, 1e-13, False),
     "plain_fp64_tol1e-10": (fl.PREC_FP64, 1e-10, False),
     "learned_pair_tol1e-13": (fl.PREC_PAIR, 1e-13, True),
+    "learned_pair_tol1e-12": (fl.PREC_PAIR, 1e-12, True),
+    "learned_pair_tol1e-11": (fl.PREC_PAIR, 1e-11, True),
     "learned_fp32_tol1e-10": (fl.PREC_MIXED, 1e-10, True),
 }
 REFS = ("plain_fp64_tol1e-13", "plain_fp64_tol1e-10")

@@ -239,6 +239,21 @@ int fedg_trc_update(fedg_ctx* ctx, double* QTRC, const double* const mflx[3], co
                     const double* alph_P, const double* DDENS_TRC, const double* DDENS0_TRC, const double* DDENS,
                     const double* RHOQ_tp, const fedg_trc_opts* opts);
 
+/* Tracer transport outputs of fedg_update (FEDG_PREC_FP64), the coupling of FElib's dynamics driver to
+ * its tracer driver (driver_nonhydro3d.F90:900-935): during each step, after every stage's explicit
+ * tendency, the stage-weighted mass flux and the dynamics' Rusanov coefficients are accumulated into
+ * mflx/alph_M/alph_P (fedg_trc_save_massflux with the scheme's b weights); DDENS0_TRC receives DDENS at
+ * the step's start and DDENS_TRC the DDENS before the modal filter.  After fedg_update they hold the
+ * last step's values, ready for fedg_trc_update.  mflx == NULL clears the registration.  The caller
+ * owns the arrays (FElib layout, device). */
+int fedg_update_set_tracer_flux(fedg_ctx* ctx, double* const mflx[3], double* alph_M, double* alph_P,
+                                double* DDENS_TRC, double* DDENS0_TRC);
+
+/* The sponge layer inside fedg_update (FEDG_PREC_FP64): after every stage's explicit tendency,
+ * fedg_sponge_add_tend on MOMX/MOMY/MOMZ_dt (SPONGELAYER_FLAG, driver_nonhydro3d.F90:831-841).
+ * tau <= 0 turns it off (the default). */
+int fedg_update_set_sponge(fedg_ctx* ctx, double tau, double height, int hveldamp);
+
 /* ---- Numerical diffusion and sponge layer ---------------------------------------------------
  * atm_dyn_dgm_nonhydro3d_numdiff_Apply (FElib/src/fluid_dyn_solver/scale_atm_dyn_dgm_nonhydro3d_numdiff.F90:
  * 214-376), applied by the model after the dynamics and tracer updates (mod_atmos_dyn.F90:340-348):

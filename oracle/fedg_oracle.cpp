@@ -187,6 +187,12 @@ struct Oracle {
   // base state, (Np, Ne)
   std::vector<double> dens_hyd, pres_hyd, therm_hyd;
   double newton_cref = 340.0;  // velocity scale of the MOMZ convergence test
+  // tracer transport outputs of the dynamics step when set (save_massflux, driver_nonhydro3d.F90:900-935):
+  // MFLX_x/y/z, alph_dens_M/P, DDENS_TRC, DDENS0_TRC
+  double* trc_out[7] = {};
+  // sponge layer in the dynamics step when tau > 0 (driver_nonhydro3d.F90:831-841)
+  double sl_tau = 0.0, sl_height = 0.0;
+  int sl_hvel = 0;
 
   size_t nid(int i, int j, int k) const { return (size_t)i + (size_t)N1 * j + (size_t)N1 * N1 * k; }
   size_t eid(int ex, int ey, int ez) const { return (size_t)ex + (size_t)NeX * ey + (size_t)NeX * NeY * ez; }
@@ -1559,6 +1565,15 @@ void orc_step_heve(void* h, double* const* q, double dt, int nsteps) {
     for (int st = 1; st <= 3; ++st) {
       drhot2pres(*o, q[VRT], nullptr, dp.data());
       cal_tend(*o, 0, q, dp.data(), tp);
+      if (o->sl_tau > 0.0) {
+        double* const tm[3] = {tp[VMX], tp[VMY], tp[VMZ]};
+        const double* const mm[3] = {q[VMX], q[VMY], q[VMZ]};
+        sponge_add_tend(*o, tm, mm, o->sl_tau, o->sl_height, o->sl_hvel);
+      }
+      if (o->trc_out[0]) {  // ERK_SSP_3s3o weights b = (1/6, 1/6, 2/3)
+        const double w = st == 3 ? 2.0 / 3.0 : 1.0 / 6.0;
+        trc_save_massflux(*o, st, q, dp.data(), w, w, 0, o->trc_out, o->trc_out[3], o->trc_out[4]);
+      }
       for (int v = 0; v < 5; ++v) {
         double* x = q[v]; const double* x0 = q0[v].data(); double* vt = tmp[v].data(); const double* tt = t[v].data();
 #pragma omp parallel for
@@ -1568,6 +1583,10 @@ void orc_step_heve(void* h, double* const* q, double dt, int nsteps) {
           else { x[p] = vt[p] + (2.0 / 3.0) * x[p] + (2.0 / 3.0) * dt * tt[p]; }
         }
       }
+    }
+    if (o->trc_out[0]) {
+      std::memcpy(o->trc_out[5], q[VD], n * sizeof(double));
+      std::memcpy(o->trc_out[6], q0[VD].data(), n * sizeof(double));
     }
     if (o->filter_on) modal_filter(*o, q);
   }
@@ -1606,6 +1625,13 @@ long orc_step_hevi(void* h, double* const* q, double dt, int nsteps, int max_ite
       }
       drhot2pres(*o, q[VRT], nullptr, dp.data());
       cal_tend(*o, 1, q, dp.data(), tep);
+      if (o->sl_tau > 0.0) {
+        double* const tm[3] = {tep[VMX], tep[VMY], tep[VMZ]};
+        const double* const mm[3] = {q[VMX], q[VMY], q[VMZ]};
+        sponge_add_tend(*o, tm, mm, o->sl_tau, o->sl_height, o->sl_hvel);
+      }
+      if (o->trc_out[0])  // IMEX: horizontal weight b_ex, vertical b_im (driver_nonhydro3d.F90:900-917)
+        trc_save_massflux(*o, st, q, dp.data(), bb[st], bb[st], 1, o->trc_out, o->trc_out[3], o->trc_out[4]);
       for (int v = 0; v < 5; ++v) {  // Advance (rk_advance_general2D, timeint_rk.F90:2201-2360)
         double* x = q[v]; double* vt = vtmp[v].data(); const double* x0 = var0[v].data();
         const double* te = tex[st][v].data(); const double* ti = tim[st][v].data();
@@ -1622,6 +1648,10 @@ long orc_step_hevi(void* h, double* const* q, double dt, int nsteps, int max_ite
           }
         }
       }
+    }
+    if (o->trc_out[0]) {
+      std::memcpy(o->trc_out[5], q[VD], n * sizeof(double));
+      std::memcpy(o->trc_out[6], var0[VD].data(), n * sizeof(double));
     }
     if (o->filter_on) modal_filter(*o, q);
   }
@@ -1688,6 +1718,21 @@ void orc_numdiff_apply(void* h, double* const* q, int nlap, double coef_h, doubl
 void orc_sponge_add_tend(void* h, double* const* tend, const double* const* mom, double tau, double height,
                          int hvel) {
   sponge_add_tend(*static_cast<Oracle*>(h), tend, mom, tau, height, hvel);
+}
+
+
+// tracer transport outputs of orc_step_heve/orc_step_hevi (NULL clears): out = {MFLX_x, MFLX_y, MFLX_z,
+// alph_dens_M, alph_dens_P, DDENS_TRC, DDENS0_TRC}
+void orc_set_trc_flux(void* h, double* const* out) {
+  Oracle* o = static_cast<Oracle*>(h);
+  for (int i = 0; i < 7; ++i) o->trc_out[i] = out ? out[i] : nullptr;
+}
+
+
+// sponge layer inside orc_step_heve/orc_step_hevi (tau <= 0: off)
+void orc_set_sponge(void* h, double tau, double height, int hvel) {
+  Oracle* o = static_cast<Oracle*>(h);
+  o->sl_tau = tau; o->sl_height = height; o->sl_hvel = hvel;
 }
 
 }  // extern "C"

@@ -84,6 +84,8 @@ def _load():
                                    ctypes.c_double, ctypes.c_double, ctypes.c_int]
     lib.orc_trc_step.argtypes = [ctypes.c_void_p, _dp, pp, _dp, _dp, _dp, _dp, _dp, _dp, ctypes.c_int, _dp, _dp,
                                  _dp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, ctypes.c_int]
+    lib.orc_set_trc_flux.argtypes = [ctypes.c_void_p, pp]
+    lib.orc_set_sponge.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_int]
     lib.orc_numdiff_apply.argtypes = [ctypes.c_void_p, pp, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                       ctypes.c_double]
     lib.orc_sponge_add_tend.argtypes = [ctypes.c_void_p, pp, pp, ctypes.c_double, ctypes.c_double, ctypes.c_int]
@@ -307,3 +309,20 @@ class Oracle:
         pm, _k2 = _pp(ms)
         self.lib.orc_sponge_add_tend(self._h, pt, pm, float(tau), float(height), int(bool(hvel)))
         return ts
+
+    def set_trc_flux(self, outs):
+        """outs = [MFLX_x, MFLX_y, MFLX_z, alph_M, alph_P, DDENS_TRC, DDENS0_TRC] (filled by step_heve /
+        step_hevi in place) or None"""
+        if outs is None:
+            self.lib.orc_set_trc_flux(self._h, None)
+            self._trc_keep = None
+            return
+        for a in outs:
+            assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+        pq, keep = _pp(outs)
+        self._trc_keep = (pq, keep)
+        self.lib.orc_set_trc_flux(self._h, pq)
+
+    def set_sponge(self, tau, height=0.0, hvel=False):
+        """sponge layer inside step_heve / step_hevi (tau <= 0: off)"""
+        self.lib.orc_set_sponge(self._h, float(tau), float(height), int(bool(hvel)))

@@ -267,3 +267,32 @@ def test_update_pair_coupled_densities_filter_and_source():
                    ctx.tensor(ddens0), 0.02, nsteps=8, ddens=ctx.tensor(ddens), rhoq_tp=ctx.tensor(rhoq),
                    limiter=True, tmar=True, filter=filt, prec=fl.PREC_PAIR)
     assert rel_l2(np_(Qd), ref) < PAIR_TOL
+
+
+@pytest.mark.parametrize("hevi", [0, 1])
+def test_update_accumulates_tracer_flux(hevi):
+    """fedg_update (FP64) with fedg_update_set_tracer_flux: the stage-weighted mass flux, the dynamics'
+    Rusanov coefficients, DDENS_TRC and DDENS0_TRC of the last step, against the oracle's dynamics
+    step with the same outputs (driver_nonhydro3d.F90:900-935)"""
+    case = cases.C2().scaled(2, 2, 3) if hevi else cases.C1().scaled(3, 3, 3)
+    dt = 0.04 if hevi else 0.02
+    o, ctx, q, b, _ = setup(case, seed=12, wobble=0.5)
+    outs_o = [np.zeros(o.shape) for _ in range(3)] + [np.zeros(o.face_shape) for _ in range(2)] + \
+             [np.zeros(o.shape) for _ in range(2)]
+    o.set_trc_flux(outs_o)
+    if hevi:
+        ref, _, _ = o.step_hevi(q, dt, 2, max_iter=1)
+    else:
+        ref = o.step_heve(q, dt, 2)
+    o.set_trc_flux(None)
+    outs_g = [ctx.empty() for _ in range(3)] + [ctx.empty_face() for _ in range(2)] + [ctx.empty() for _ in range(2)]
+    ctx.set_tracer_flux(outs_g)
+    qd = [ctx.tensor(a) for a in q]
+    ctx.update(qd, 2, eqs=fl.HEVI if hevi else fl.HEVE, dt=dt, max_iter=1)
+    ctx.set_tracer_flux(None)
+    names = ["MFLX_x", "MFLX_y", "MFLX_z", "alph_M", "alph_P", "DDENS_TRC", "DDENS0_TRC"]
+    for nm, g, r in zip(names, outs_g, outs_o):
+        e = rel_max(np_(g), r)
+        assert e < 1e-10, (nm, e)
+    # the dynamics state itself is unchanged by the registration
+    assert rel_max(np_(qd[3]), ref[3]) < 1e-9
