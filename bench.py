@@ -347,6 +347,57 @@ def tracer_bench(args, torch, np, fl, cases, peaks, peak_src, steps, warmup):
             "gpu_launches": sum(v[1] for v in prof.values())}
 
 
+def numdiff_bench(args, torch, np, fl, ctx, qd, peaks, peak_src, case):
+    """Numerical diffusion (FElib's hyperdiffusion filter, nonhydro3d_numdiff.F90) and the sponge layer
+    (dgm_spongelayer.F90) on the bench state: one application each, FP64.  DOF = one value of one
+    prognostic variable; the filter touches 5 variables per application."""
+    stream = torch.cuda.ExternalStream(ctx.stream_handle)
+    nodes = case.Np * case.Ne
+    out = {}
+    q = [t.clone() for t in qd]
+    for nlap, coef in ((1, 1.0e2), (2, 1.0e5)):
+        ctx.numdiff_apply(q, nlap, coef, coef, 1e-3)  # warm-up (allocates the scratch)
+        fl.prof_reset(ctx)
+        fl.prof_enable(ctx, True)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            ctx.lib.fedg_numdiff_apply(ctx.h, fl._p5(q), nlap, coef, coef, 1e-3)
+        e1.record(stream)
+        ctx.sync()
+        torch.cuda.synchronize()
+        fl.prof_enable(ctx, False)
+        ms = e0.elapsed_time(e1) / args.steps
+        launches = fl.prof_read(ctx)["numdiff"][1] // args.steps
+        # algorithmic bytes per node and variable: gradient pass reads q (+ DDENS) and writes G (3);
+        # each extra Laplacian pass reads G (3), writes 2, reads 2, writes 3; the tendency pass reads
+        # G (3) + DDENS and updates q (read + write)
+        bpn = 8 * ((2 + 3) + (nlap - 1) * (3 + 2 + 2 + 3) + (3 + 1 + 2))
+        gbs = 5 * bpn * nodes / (ms * 1e-3) / 1e9
+        out[f"nlap{nlap}"] = {"value": 5 * nodes / (ms * 1e-3), "unit": "DOF/s", "ms_per_apply": ms,
+                              "launches_per_apply": launches, "algorithmic_bytes_per_node_var": bpn,
+                              "achieved_gbs": gbs, "frac_of_hbm": gbs / peaks.get("hbm_gbs", 6800.0),
+                              "peak_source": peak_src}
+    del q
+    tend = [torch.zeros_like(qd[1]) for _ in range(3)]
+    ztop = case.dom[5]
+    ctx.sponge_add_tend(tend, qd[1:4], 30.0, 0.5 * ztop, True)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        ctx.lib.fedg_sponge_add_tend(ctx.h, (fl.ctypes.c_void_p * 3)(*[x.data_ptr() for x in tend]),
+                                     (fl.ctypes.c_void_p * 3)(*[x.data_ptr() for x in qd[1:4]]), 30.0, 0.5 * ztop, 1)
+    e1.record(stream)
+    ctx.sync()
+    ms = e0.elapsed_time(e1) / args.steps
+    gbs = 8 * 9 * nodes / (ms * 1e-3) / 1e9  # 3 tendencies read + written, 3 momenta read
+    out["sponge"] = {"ms_per_call": ms, "achieved_gbs": gbs, "frac_of_hbm": gbs / peaks.get("hbm_gbs", 6800.0)}
+    del tend
+    return out
+
+
 def run_fedg(args):
     import numpy as np
     import torch
@@ -534,6 +585,9 @@ def run_fedg(args):
     trc = None
     if rank == 0 and not args.no_tracer:
         trc = tracer_bench(args, torch, np, fl, cases, peaks, peak_src, args.steps, args.warmup)
+    ndf = None
+    if rank == 0 and not args.no_numdiff:
+        ndf = numdiff_bench(args, torch, np, fl, ctx, qd, peaks, peak_src, case)
 
     finite = all(bool(torch.isfinite(t).all().item()) for t in qd)
     if rank == 0:
@@ -560,6 +614,7 @@ def run_fedg(args):
             "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
             "accuracy": acc,
             "tracer_advection": trc,
+            "numdiff_sponge": ndf,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -586,6 +641,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--no-other", action="store_true", help="skip the run of the other precision mode")
     ap.add_argument("--no-tracer", action="store_true", help="skip the tracer-advection measurement")
+    ap.add_argument("--no-numdiff", action="store_true", help="skip the numerical-diffusion / sponge measurement")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -136,7 +136,7 @@ def load():
     lib.fedg_trc_modalfilter.argtypes = [_vp, _vp, _vp, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                          ctypes.c_double, ctypes.c_double, ctypes.c_int]
     lib.fedg_trc_update.argtypes = [_vp, _vp, _P3, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.POINTER(TrcOpts)]
-    lib.fedg_update_set_tracer_flux.argtypes = [_vp, _P3, _vp, _vp, _vp, _vp]
+    lib.fedg_update_set_tracer_flux.argtypes = [_vp, ctypes.POINTER(ctypes.c_void_p), _vp, _vp, _vp, _vp]
     lib.fedg_update_set_sponge.argtypes = [_vp, ctypes.c_double, ctypes.c_double, ctypes.c_int]
     lib.fedg_numdiff_apply.argtypes = [_vp, _P5, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double]
     lib.fedg_sponge_add_tend.argtypes = [_vp, _P3, _P3, ctypes.c_double, ctypes.c_double, ctypes.c_int]
