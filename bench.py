@@ -355,15 +355,16 @@ def numdiff_bench(args, torch, np, fl, ctx, qd, peaks, peak_src, case):
     nodes = case.Np * case.Ne
     out = {}
     q = [t.clone() for t in qd]
-    for nlap, coef in ((1, 1.0e2), (2, 1.0e5)):
-        ctx.numdiff_apply(q, nlap, coef, coef, 1e-3)  # warm-up (allocates the scratch)
+    for nlap, coef, prec in ((1, 1.0e2, fl.PREC_FP64), (2, 1.0e5, fl.PREC_FP64), (1, 1.0e2, fl.PREC_PAIR),
+                             (2, 1.0e5, fl.PREC_PAIR)):
+        ctx.numdiff_apply(q, nlap, coef, coef, 1e-3, prec=prec)  # warm-up (allocates the scratch)
         fl.prof_reset(ctx)
         fl.prof_enable(ctx, True)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(args.steps):
-            ctx.lib.fedg_numdiff_apply(ctx.h, fl._p5(q), nlap, coef, coef, 1e-3)
+            ctx.lib.fedg_numdiff_apply_prec(ctx.h, fl._p5(q), nlap, coef, coef, 1e-3, prec)
         e1.record(stream)
         ctx.sync()
         torch.cuda.synchronize()
@@ -375,7 +376,8 @@ def numdiff_bench(args, torch, np, fl, ctx, qd, peaks, peak_src, case):
         # G (3) + DDENS and updates q (read + write)
         bpn = 8 * ((2 + 3) + (nlap - 1) * (3 + 2 + 2 + 3) + (3 + 1 + 2))
         gbs = 5 * bpn * nodes / (ms * 1e-3) / 1e9
-        out[f"nlap{nlap}"] = {"value": 5 * nodes / (ms * 1e-3), "unit": "DOF/s", "ms_per_apply": ms,
+        out[f"nlap{nlap}_{'pair' if prec == fl.PREC_PAIR else 'fp64'}"] = {
+                              "value": 5 * nodes / (ms * 1e-3), "unit": "DOF/s", "ms_per_apply": ms,
                               "launches_per_apply": launches, "algorithmic_bytes_per_node_var": bpn,
                               "achieved_gbs": gbs, "frac_of_hbm": gbs / peaks.get("hbm_gbs", 6800.0),
                               "peak_source": peak_src}

@@ -56,6 +56,9 @@ namespace fedg {
 int trc_update_pair(fedg_ctx* c, double* QTRC, const double* const mflx[3], const double* aM, const double* aP,
                     const double* ddens_trc, const double* ddens0_trc, const double* ddens, const double* rhoq,
                     const fedg_trc_opts* o, double* scratch);
+// fedg_numdiff_apply_prec in float pairs (fedg_nd_pair.cu); scratch: 5 Np*Ne doubles
+int numdiff_apply_pair(fedg_ctx* c, double* const q[5], int nlap, double coef_h, double coef_v, double dt,
+                       double* scratch);
 }  // namespace fedg
 
 // Runs one launch f() of kernel class id on the context stream, counting it and, when the

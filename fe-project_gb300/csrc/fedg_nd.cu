@@ -303,7 +303,14 @@ int nd_pass(int pass, const Ops& op, const double* dp, const double* a, const do
 extern "C" {
 
 int fedg_numdiff_apply(fedg_ctx* c, double* const q[5], int nlap, double coef_h, double coef_v, double dt) {
+  return fedg_numdiff_apply_prec(c, q, nlap, coef_h, coef_v, dt, FEDG_PREC_FP64);
+}
+
+int fedg_numdiff_apply_prec(fedg_ctx* c, double* const q[5], int nlap, double coef_h, double coef_v, double dt,
+                            int prec) {
   if (!c || !q) return api_fail("fedg_numdiff_apply: null argument");
+  if (prec != FEDG_PREC_FP64 && prec != FEDG_PREC_PAIR)
+    return api_fail("fedg_numdiff_apply: prec must be FEDG_PREC_FP64 or FEDG_PREC_PAIR");
   for (int v = 0; v < 5; ++v)
     if (!q[v]) return api_fail("fedg_numdiff_apply: null field");
   if (nlap < 1) return api_fail("fedg_numdiff_apply: ND_LAPLACIAN_NUM must be >= 1");
@@ -316,6 +323,7 @@ int fedg_numdiff_apply(fedg_ctx* c, double* const q[5], int nlap, double coef_h,
       return api_fail("fedg_numdiff_apply: out of device memory (5 fields of scratch)");
     }
   }
+  if (prec == FEDG_PREC_PAIR) return numdiff_apply_pair(c, q, nlap, coef_h, coef_v, dt, c->nd_buf);
   double* Gx = c->nd_buf;
   double* Gy = Gx + n;
   double* Gz = Gy + n;

@@ -34,7 +34,7 @@ EXPORTED = [
     "fedg_guess_predict", "fedg_guess_load", "fedg_cal_tend_ex_noalloc",
     "fedg_trc_alphdens_advtest", "fedg_trc_save_massflux", "fedg_trc_fct_coef", "fedg_trc_cal_tend",
     "fedg_trc_tmar", "fedg_trc_modalfilter", "fedg_trc_update", "fedg_numdiff_apply", "fedg_sponge_add_tend",
-    "fedg_update_set_tracer_flux", "fedg_update_set_sponge",
+    "fedg_update_set_tracer_flux", "fedg_update_set_sponge", "fedg_numdiff_apply_prec",
 ]
 
 # kernel classes of fedg_prof_read (include/fedg.h)
@@ -139,6 +139,8 @@ def load():
     lib.fedg_update_set_tracer_flux.argtypes = [_vp, ctypes.POINTER(ctypes.c_void_p), _vp, _vp, _vp, _vp]
     lib.fedg_update_set_sponge.argtypes = [_vp, ctypes.c_double, ctypes.c_double, ctypes.c_int]
     lib.fedg_numdiff_apply.argtypes = [_vp, _P5, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double]
+    lib.fedg_numdiff_apply_prec.argtypes = [_vp, _P5, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                            ctypes.c_double, ctypes.c_int]
     lib.fedg_sponge_add_tend.argtypes = [_vp, _P3, _P3, ctypes.c_double, ctypes.c_double, ctypes.c_int]
     lib.fedg_prof_enable.argtypes = [_vp, ctypes.c_int]
     lib.fedg_prof_reset.argtypes = [_vp]
@@ -376,10 +378,10 @@ class Context:
                "fedg_update_set_tracer_flux")
 
     # -- numerical diffusion (nonhydro3d_numdiff.F90) and sponge layer (dgm_spongelayer.F90) --
-    def numdiff_apply(self, q, nlap, coef_h, coef_v, dt):
+    def numdiff_apply(self, q, nlap, coef_h, coef_v, dt, prec=PREC_FP64):
         self.torch.cuda.synchronize()
-        _check(self.lib.fedg_numdiff_apply(self.h, _p5(q), int(nlap), float(coef_h), float(coef_v), float(dt)),
-               "fedg_numdiff_apply")
+        _check(self.lib.fedg_numdiff_apply_prec(self.h, _p5(q), int(nlap), float(coef_h), float(coef_v), float(dt),
+                                                int(prec)), "fedg_numdiff_apply")
         self.sync()
         return q
 

@@ -262,6 +262,10 @@ int fedg_update_set_sponge(fedg_ctx* ctx, double tau, double height, int hveldam
  * weighted by dens.  nlap = ND_LAPLACIAN_NUM, coef_h/v = ND_COEF_H/V, dt = the dynamics step.
  * q[5] = DDENS, MOMX, MOMY, MOMZ, DRHOT, in place; lids are slip and adiabatic (dgm_bnd.F90:370-508). */
 int fedg_numdiff_apply(fedg_ctx* ctx, double* const q[5], int nlap, double coef_h, double coef_v, double dt);
+/* the same with a precision: FEDG_PREC_FP64 (fedg_numdiff_apply) or FEDG_PREC_PAIR (the passes in float
+ * pairs on the FP32 pipe, FP64-class; the increment is added to the FP64 fields in FP64) */
+int fedg_numdiff_apply_prec(fedg_ctx* ctx, double* const q[5], int nlap, double coef_h, double coef_v, double dt,
+                            int prec);
 /* atm_dyn_dgm_spongelayer_add_tend (..._dgm_spongelayer.F90:134-219): Rayleigh damping of MOMZ (and of
  * MOMX, MOMY when hveldamp) above `height`, rate 0.25/tau (1 + sign(z - h)) (1 - cos(pi (z - h)/(z_top - h))),
  * subtracted from the explicit tendencies.  tend[3] = MOMX_dt, MOMY_dt, MOMZ_dt (in/out); mom[3] = MOMX,

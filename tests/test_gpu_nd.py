@@ -90,3 +90,21 @@ def test_update_with_sponge(hevi):
     # and the sponge did something: the same steps without it differ
     ref0 = o.step_hevi(q, dt, 2, max_iter=1)[0] if hevi else o.step_heve(q, dt, 2)
     assert np.max(np.abs(ref0[3] - ref[3])) > 1e-6 * max(1.0, np.max(np.abs(ref[3])))
+
+
+@pytest.mark.parametrize("porder,ne", [(3, (4, 3, 4)), (7, (2, 2, 3)), (2, (3, 4, 3))])
+@pytest.mark.parametrize("nlap", [1, 2, 3])
+def test_numdiff_apply_pair(porder, ne, nlap):
+    """the float-pair passes (FEDG_PREC_PAIR) against the FP64 oracle: the change of each field,
+    relative to the largest change, <= 1e-10 (FP64-class pairs)"""
+    case = cases.C1().scaled(*ne, porder=porder)
+    o, ctx, q, b = setup(case, seed=30 + nlap)
+    coef = {1: 2.0e2, 2: 5.0e5, 3: 1.0e9}[nlap]
+    ref = o.numdiff_apply(q, nlap, coef, 0.5 * coef, 0.01)
+    qd = [ctx.tensor(a) for a in q]
+    ctx.numdiff_apply(qd, nlap, coef, 0.5 * coef, 0.01, prec=fl.PREC_PAIR)
+    for v in range(5):
+        got = qd[v].cpu().numpy()
+        dref = ref[v] - q[v]
+        err = np.max(np.abs((got - q[v]) - dref)) / max(np.max(np.abs(dref)), 1e-300)
+        assert err < 1e-10, (VARS[v], err)
