@@ -516,6 +516,7 @@ def run_fedg(args):
         q_e = [torch.empty_like(t) for t in qd]
         torch.cuda.synchronize()
         ph = [0.0, 0.0, 0.0]  # seconds in H2D, the step, D2H
+        h2d_each = []
         t0 = time.perf_counter()
         for _ in range(ke):
             ta = time.perf_counter()
@@ -533,11 +534,13 @@ def run_fedg(args):
             ph[0] += tb - ta
             ph[1] += tc - tb
             ph[2] += td - tc
+            h2d_each.append(1e3 * (tb - ta))
         t1 = time.perf_counter()
         nb = sum(t.numel() * 8 for t in qd)
         e2e = {"value": dofs_stage * ke / (t1 - t0), "unit": UNIT, "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb,
                "steps": ke, "ms_per_step": {"h2d": 1e3 * ph[0] / ke, "update": 1e3 * ph[1] / ke, "d2h": 1e3 * ph[2] / ke},
-               "copy_gbs": {"h2d": nb * ke / max(ph[0], 1e-9) / 1e9, "d2h": nb * ke / max(ph[2], 1e-9) / 1e9}}
+               "copy_gbs": {"h2d": nb * ke / max(ph[0], 1e-9) / 1e9, "d2h": nb * ke / max(ph[2], 1e-9) / 1e9},
+               "h2d_ms_each": h2d_each}
         del q_e
 
     # the headline path without the learned guess, the other precision mode, and the plain FP64 path, on

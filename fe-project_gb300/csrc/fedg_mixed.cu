@@ -614,8 +614,92 @@ static int pair_setup(fedg_ctx* c, MixedState* m) {
   return 0;
 }
 
+// reference wind of the deviations = domain-mean velocity of the first state seen
+static int set_ref_wind(fedg_ctx* c, MixedState* m, double* const q[5]) {
+  if (m->wind_set) return 0;
+  int r;
+  double* d_s = reinterpret_cast<double*>(m->fbuf);  // TI area, free before the first step
+  if (cudaMemsetAsync(d_s, 0, 3 * sizeof(double), c->stream) != cudaSuccess) return api_fail("memset");
+  r = tracked(c, FEDG_K_AUX, [&] {
+    k_wind_sums<<<1024, 256, 0, c->stream>>>(q[1], q[2], q[0], c->d_prof, c->Np, c->N1, c->nxy, c->n, d_s);
+    return (int)cudaGetLastError();
+  });
+  if (r) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): wind sums");
+  double hs[3];
+  if (cudaMemcpyAsync(hs, d_s, sizeof(hs), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+      cudaStreamSynchronize(c->stream) != cudaSuccess)
+    return api_fail("fedg_update(mixed): wind readback");
+  m->Uref = hs[2] != 0.0 ? hs[0] / hs[2] : 0.0;
+  m->Vref = hs[2] != 0.0 ? hs[1] / hs[2] : 0.0;
+  m->opf.Uref = (float)m->Uref;
+  m->opf.Vref = (float)m->Vref;
+  m->opx.Uref = split_host(m->Uref);
+  m->opx.Vref = split_host(m->Vref);
+  m->wind_set = true;
+  return 0;
+}
+
+// HEVE in float pairs: three explicit ERK_SSP_3s3o stages per step (timeint_rk.F90:1182-1278 with
+// the ERK_SSP_3s3o table of scale_timeint_rk_butcher.F90), each one k_stage_pair<HEVE> launch that
+// computes the explicit HEVE tendency of its input deviation state and applies the stage update;
+// stage 3 also applies the modal filter and writes q^{n+1} in FP64.  No implicit solve, so no guess
+// network and no Newton iterations.
+static int pair_update_heve(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_opts* o,
+                            double* iters_out) {
+  if (o->use_guess) return api_fail("fedg_update: use_guess needs eqs FEDG_HEVI (HEVE has no implicit solve)");
+  int r = mixed_setup(c);
+  if (r) return r;
+  MixedState* m = c->mixed;
+  if ((r = pair_setup(c, m))) return r;
+  if ((r = set_ref_wind(c, m, q))) return r;
+  m->opp.Uref = m->opx.Uref;
+  m->opp.Vref = m->opx.Vref;
+  PairCoef pc;
+  std::memset(&pc, 0, sizeof(pc));
+  pc.dt = split_host(o->dt);
+  pc.ssp[0] = split_host(0.75);
+  pc.ssp[1] = split_host(0.25);
+  pc.ssp[2] = split_host(1.0 / 3.0);
+  pc.ssp[3] = split_host(2.0 / 3.0);
+  const ProfP pfp{m->prof5, m->prof5 + c->L, m->prof5 + 2 * c->L, m->prof5 + 3 * c->L, m->prof5 + 4 * c->L,
+                  m->prof + c->L};
+  StagePairBufs BP;
+  std::memset(&BP, 0, sizeof(BP));
+  for (int v = 0; v < 5; ++v) {
+    BP.qn[v] = q[v];
+    BP.qnf[v] = m->QNFp(v);
+  }
+  F5c qc{{q[0], q[1], q[2], q[3], q[4]}};
+  Dev5p dv{{m->QNFp(0), m->QNFp(1), m->QNFp(2), m->QNFp(3), m->QNFp(4)}};
+  r = tracked(c, FEDG_K_AUX, [&] {
+    k_to_dev2<<<(unsigned)((c->n + 255) / 256), 256, 0, c->stream>>>(qc, dv, c->d_prof, m->opx.Uref, m->opx.Vref,
+                                                                    c->Np, c->N1, c->nxy, c->n);
+    return (int)cudaGetLastError();
+  });
+  if (r) return api_cuda_fail((cudaError_t)r, "fedg_update(pair, HEVE): deviation copy");
+  const int filt = c->d.mf_on;
+  // stage inputs and outputs: q^n deviation (QNFp) -> q1 (qi) -> q2 (QSFp) -> q^{n+1} (q, QNFp)
+  for (int step = 0; step < nsteps; ++step) {
+    for (int s = 1; s <= 3; ++s) {
+      for (int v = 0; v < 5; ++v) {
+        BP.qs[v] = s == 1 ? m->QNFp(v) : (s == 2 ? m->qi(v) : m->QSFp(v));
+        BP.qi[v] = s == 1 ? m->qi(v) : m->QSFp(v);
+      }
+      r = tracked(c, FEDG_K_MTEND, [&] {
+        return launch_stage_pair_heve(c->N1, s, m->opp, pfp, c->d_prof, BP, pc, c->Ne, filt, c->stream);
+      });
+      if (r) return api_cuda_fail((cudaError_t)r, "fedg_update(pair, HEVE): stage");
+    }
+  }
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) return api_fail("fedg_update(pair, HEVE): synchronize");
+  if (iters_out) *iters_out = 0.0;
+  return 0;
+}
+
 int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_opts* o, double* iters_out) {
-  if (o->eqs != FEDG_HEVI) return api_fail("fedg_update: the mixed-precision path implements HEVI (IMEX ARK232)");
+  if (o->eqs == FEDG_HEVE && o->prec == FEDG_PREC_PAIR) return pair_update_heve(c, q, nsteps, o, iters_out);
+  if (o->eqs != FEDG_HEVI)
+    return api_fail("fedg_update: the FP32 mixed-precision path implements HEVI (IMEX ARK232); HEVE runs in FP64 or float pairs");
   if (o->max_iter < 1) return api_fail("fedg_update: max_iter must be >= 1");
   int r = mixed_setup(c);
   if (r) return r;
@@ -636,26 +720,7 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
     B.SF[v] = m->SF(v);
     B.TI[v] = m->TI(v);
   }
-  if (!m->wind_set) {  // reference wind = domain-mean velocity of the first state seen
-    double* d_s = reinterpret_cast<double*>(m->fbuf);  // TI area, free before the first step
-    if (cudaMemsetAsync(d_s, 0, 3 * sizeof(double), c->stream) != cudaSuccess) return api_fail("memset");
-    r = tracked(c, FEDG_K_AUX, [&] {
-      k_wind_sums<<<1024, 256, 0, c->stream>>>(q[1], q[2], q[0], c->d_prof, c->Np, c->N1, c->nxy, c->n, d_s);
-      return (int)cudaGetLastError();
-    });
-    if (r) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): wind sums");
-    double hs[3];
-    if (cudaMemcpyAsync(hs, d_s, sizeof(hs), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
-        cudaStreamSynchronize(c->stream) != cudaSuccess)
-      return api_fail("fedg_update(mixed): wind readback");
-    m->Uref = hs[2] != 0.0 ? hs[0] / hs[2] : 0.0;
-    m->Vref = hs[2] != 0.0 ? hs[1] / hs[2] : 0.0;
-    m->opf.Uref = (float)m->Uref;
-    m->opf.Vref = (float)m->Vref;
-    m->opx.Uref = split_host(m->Uref);
-    m->opx.Vref = split_host(m->Vref);
-    m->wind_set = true;
-  }
+  if ((r = set_ref_wind(c, m, q))) return r;
   cf.Uref = m->Uref;
   cf.Vref = m->Vref;
   cf.Uref2 = m->opx.Uref;

@@ -78,6 +78,7 @@ struct ProfP {
 };
 struct PairCoef {
   float2 dt, a21e, a21i, a31e, a31i, a32e, a32i, b1, b2, b3;
+  float2 ssp[4];  // ERK_SSP_3s3o: 3/4, 1/4, 1/3, 2/3 (HEVE)
 };
 struct StagePairBufs {
   const float2* qs[5];  // deviation state of the explicit tendency (q^n at stage 1, Q_s after)
@@ -91,6 +92,8 @@ struct StagePairBufs {
   int xdinp;
   float xs[3];
 };
+int launch_stage_pair_heve(int N1, int stage, const OpsP& op, const ProfP& pf, const double* dens64,
+                           const StagePairBufs& B, const PairCoef& cf, int Ne, int filt, cudaStream_t s);
 int launch_stage_pair(int N1, int stage, const OpsP& op, const ProfP& pf, const double* dens64,
                       const StagePairBufs& B, const PairCoef& cf, int Ne, int filt, cudaStream_t s);
 

@@ -66,7 +66,10 @@ __device__ __forceinline__ void face_nb(const OpsP& op, int f, int ke, int ex, i
   }
 }
 
-template <int N1, int EPB, int STAGE>
+// HEVE: the explicit HEVE operator (heve.F90:292-489, heve_numflux.F90:946-1139: vertical DENS/RHOT
+// fluxes, the vertical pressure gradient and -g VFilterPM1(DDENS) explicit, unmasked wave speed) with
+// the SSP-RK3 low-storage update (timeint_rk.F90:1182-1278) in place of the IMEX ARK232 stages
+template <int N1, int EPB, int STAGE, bool HEVE = false>
 __global__ void __launch_bounds__(EPB* N1* N1* N1)
     k_stage_pair(const OpsP op, const ProfP pf, const double* __restrict__ dens64, const StagePairBufs B,
                  const PairCoef cf, int Ne, int filter_on) {
@@ -117,7 +120,7 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
     fl[(2 * 5 + VRT) * Np + p] = f2_pack(mz * pt);
     fl[(0 * 5 + VMZ) * Np + p] = f2_pack((mxr + mxd) * w);
     fl[(1 * 5 + VMZ) * Np + p] = f2_pack((myr + myd) * w);
-    fl[(2 * 5 + VMZ) * Np + p] = f2_pack(mz * w);
+    fl[(2 * 5 + VMZ) * Np + p] = f2_pack(HEVE ? mz * w + dp : mz * w);
     fl[(0 * 5 + VMX) * Np + p] = f2_pack(mxr * ud + mxd * u + dp);
     fl[(1 * 5 + VMX) * Np + p] = f2_pack(myr * ud + myd * u);
     fl[(2 * 5 + VMX) * Np + p] = f2_pack(mz * u);
@@ -170,12 +173,18 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
       const float velM = uM.h * nx + vM.h * ny + wM.h * nz, velP = uP.h * nx + vP.h * ny + wP.h * nz;
       const float csM = sqrtf(gamm * (__ldg(pf.phf + levM) + dpM.h) * rdM.h);
       const float csP = sqrtf(gamm * (__ldg(pf.phf + levP) + dpP.h) * rdP.h);
-      const float swV = 1.f - nz * nz;
+      const float swV = HEVE ? 1.f : 1.f - nz * nz;
       const float alpha = swV * fmaxf(csM + fabsf(velM), csP + fabsf(velP));
       // normal flux deviations F.n (the reference parts cancel: same level on both sides)
-      const f2 fD_M = mxM * nx + myM * ny, fD_P = mxP * nx + myP * ny;
-      const f2 fR_M = (mxrM * ptdM + mxM * (ptrM + ptdM)) * nx + (myrM * ptdM + myM * (ptrM + ptdM)) * ny;
-      const f2 fR_P = (mxrP * ptdP + mxP * (ptrP + ptdP)) * nx + (myrP * ptdP + myP * (ptrP + ptdP)) * ny;
+      f2 fD_M = mxM * nx + myM * ny, fD_P = mxP * nx + myP * ny;
+      f2 fR_M = (mxrM * ptdM + mxM * (ptrM + ptdM)) * nx + (myrM * ptdM + myM * (ptrM + ptdM)) * ny;
+      f2 fR_P = (mxrP * ptdP + mxP * (ptrP + ptdP)) * nx + (myrP * ptdP + myP * (ptrP + ptdP)) * ny;
+      if (HEVE) {  // vertical mass and RHOT fluxes (the reference state has no vertical flux)
+        fD_M = fD_M + mzM * nz;
+        fD_P = fD_P + mzP * nz;
+        fR_M = fR_M + mzM * (ptrM + ptdM) * nz;
+        fR_P = fR_P + mzP * (ptrP + ptdP) * nz;
+      }
       const f2 velM2 = uM * nx + vM * ny + wM * nz, velP2 = uP * nx + vP * ny + wP * nz;
       const f2 fZ_M = mzM * velM2, fZ_P = mzP * velP2;
       const f2 fX_M = (mxrM * udM + mxM * uM) * nx + (myrM * udM + myM * uM) * ny + mzM * uM * nz;
@@ -187,10 +196,11 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
       const int S = 6 * NF;
       o[VD * S] = f2_pack(tmp1 * (fD_P - fD_M - (ddP - ddM) * alpha));
       o[VRT * S] = f2_pack(tmp1 * (fR_P - fR_M - (drP - drM) * alpha));
-      o[VMZ * S] = f2_pack(tmp1 * (fZ_P - fZ_M - (mzP - mzM) * alpha));
+      o[VMZ * S] = f2_pack(HEVE ? tmp1 * (fZ_P - fZ_M + (dpP - dpM) * nz - (mzP - mzM) * alpha)
+                                : tmp1 * (fZ_P - fZ_M - (mzP - mzM) * alpha));
       o[VMX * S] = f2_pack(tmp1 * (fX_P - fX_M + (dpP - dpM) * nx - (mxP - mxM) * alpha));
       o[VMY * S] = f2_pack(tmp1 * (fY_P - fY_M + (dpP - dpM) * ny - (myP - myM) * alpha));
-      if (STAGE == 1 && f >= 4) {
+      if (!HEVE && STAGE == 1 && f >= 4) {
         // vertical faces of the implicit operator at var0 = q^n (hevi_common_2.F90:1016-1328)
         const float al = fmaxf(fabsf(wM.h) + csM, fabsf(wP.h) + csP);
         const f2 tm = f2_of(op.FSz) * 0.5f;
@@ -229,14 +239,21 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
       lf.add(f2_of(op.Lb[i]), f2_of(d[3 * NF + j + N1 * k]));
       lf.add(f2_of(op.Lb[k]), f2_of(d[4 * NF + i + N1 * j]));
       lf.add(f2_of(op.Lt[k]), f2_of(d[5 * NF + i + N1 * j]));
-      const bool horiz_only = (v == VD || v == VRT);
+      const bool horiz_only = !HEVE && (v == VD || v == VRT);
       f2 s = f2_of(op.E11) * sx.get() + f2_of(op.E22) * sy.get() + lf.get();
       if (!horiz_only) s = s + f2_of(op.E33) * szv[v];
       tex[v] = -s;
     }
     tex[VMX] = tex[VMX] + f2_of(op.cor) * (qv[VMY] + dh * V);
     tex[VMY] = tex[VMY] - f2_of(op.cor) * (qv[VMX] + dh * U);
-    if (STAGE == 1) {
+    if (HEVE) {  // -g VFilterPM1(DDENS) (heve.F90:447-452)
+      f2acc drho;
+#pragma unroll
+      for (int l = 0; l < N1; ++l) drho.add(f2_of(op.T[k * N1 + l]), f2_of(st[VD * Np + i + N1 * j + NF * l]));
+      tex[VMZ] = tex[VMZ] - f2_of(op.grav) * drho.get();
+#pragma unroll
+      for (int v = 0; v < 5; ++v) tim[v] = Z2;
+    } else if (STAGE == 1) {
       f2acc sdp, drho;
 #pragma unroll
       for (int l = 0; l < N1; ++l) {
@@ -259,6 +276,71 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
 
   // --- fused RK epilogue in pairs ---
   const f2 dt = f2_of(cf.dt);
+  if constexpr (HEVE) {
+    // ERK_SSP_3s3o on the deviations (the reference state does not change in time): q1 = qn + dt t(qn),
+    // q2 = 3/4 qn + 1/4 (q1 + dt t(q1)), q3 = 1/3 qn + 2/3 (q2 + dt t(q2)); the stage inputs and
+    // outputs are deviation pairs, qn is split from the FP64 state
+    f2 dev[5], ref[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      ref[v] = v == VMX ? dh * U : (v == VMY ? dh * V : Z2);
+      dev[v] = Z2;
+      if (valid) {
+        const f2 qnd = f2_split(__ldg(B.qn[v] + g)) - ref[v];
+        const f2 up = qv[v] + dt * tex[v];
+        dev[v] = STAGE == 1 ? up
+                            : (STAGE == 2 ? f2_of(cf.ssp[0]) * qnd + f2_of(cf.ssp[1]) * up
+                                          : f2_of(cf.ssp[2]) * qnd + f2_of(cf.ssp[3]) * up);
+      }
+    }
+    if (STAGE < 3) {
+      if (valid) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) B.qi[v][g] = f2_pack(dev[v]);
+      }
+      return;
+    }
+    if (!filter_on) {
+      if (valid) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+          const f2 out = ref[v] + dev[v];
+          B.qn[v][g] = (double)out.h + (double)out.l;
+          B.qnf[v][g] = f2_pack(dev[v]);
+        }
+      }
+      return;
+    }
+    __syncthreads();  // everyone is done with the shared arrays
+    float2* fa = s_st + le * 6 * Np;
+    float2* fb = fa + Np;
+    for (int v = 0; v < 5; ++v) {
+      fa[p] = f2_pack(dev[v]);
+      __syncthreads();
+      f2acc s1;
+#pragma unroll
+      for (int l = 0; l < N1; ++l) s1.add(f2_of(op.F[i * N1 + l]), f2_of(fa[l + N1 * j + NF * k]));
+      fb[p] = f2_pack(s1.get());
+      __syncthreads();
+      f2acc s2;
+#pragma unroll
+      for (int l = 0; l < N1; ++l) s2.add(f2_of(op.F[j * N1 + l]), f2_of(fb[i + N1 * l + NF * k]));
+      __syncthreads();
+      fa[p] = f2_pack(s2.get());
+      __syncthreads();
+      f2acc s3;
+#pragma unroll
+      for (int l = 0; l < N1; ++l) s3.add(f2_of(op.Fv[k * N1 + l]), f2_of(fa[i + N1 * j + NF * l]));
+      if (valid) {
+        const f2 fil = s3.get();
+        const f2 out = ref[v] + fil;
+        B.qn[v][g] = (double)out.h + (double)out.l;
+        B.qnf[v][g] = f2_pack(fil);
+      }
+      __syncthreads();
+    }
+    return;
+  }
   if (STAGE == 1 || STAGE == 2) {
     float xq[3] = {0.f, 0.f, 0.f};
     if (valid) {
@@ -353,18 +435,33 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
 template <int N1>
 constexpr int epb_p() { return N1 == 4 ? 4 : 1; }
 
-template <int N1, int STAGE>
+template <int N1, int STAGE, bool HEVE = false>
 int launch_pair_n(const OpsP& op, const ProfP& pf, const double* dens64, const StagePairBufs& B, const PairCoef& cf,
                   int Ne, int filt, cudaStream_t s) {
   constexpr int EPB = epb_p<N1>(), Np = N1 * N1 * N1, NF = N1 * N1;
   const size_t smem = sizeof(float2) * EPB * (21 * Np + 5 * 6 * NF + 5 * 2 * NF);
-  auto kfn = k_stage_pair<N1, EPB, STAGE>;
+  auto kfn = k_stage_pair<N1, EPB, STAGE, HEVE>;
   cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   kfn<<<(Ne + EPB - 1) / EPB, EPB * Np, smem, s>>>(op, pf, dens64, B, cf, Ne, filt);
   return (int)cudaGetLastError();
 }
 
 }  // namespace
+
+int launch_stage_pair_heve(int N1, int stage, const OpsP& op, const ProfP& pf, const double* dens64,
+                           const StagePairBufs& B, const PairCoef& cf, int Ne, int filt, cudaStream_t s) {
+  if (N1 == 8) {
+    if (stage == 1) return launch_pair_n<8, 1, true>(op, pf, dens64, B, cf, Ne, filt, s);
+    if (stage == 2) return launch_pair_n<8, 2, true>(op, pf, dens64, B, cf, Ne, filt, s);
+    return launch_pair_n<8, 3, true>(op, pf, dens64, B, cf, Ne, filt, s);
+  }
+  if (N1 == 4) {
+    if (stage == 1) return launch_pair_n<4, 1, true>(op, pf, dens64, B, cf, Ne, filt, s);
+    if (stage == 2) return launch_pair_n<4, 2, true>(op, pf, dens64, B, cf, Ne, filt, s);
+    return launch_pair_n<4, 3, true>(op, pf, dens64, B, cf, Ne, filt, s);
+  }
+  return (int)cudaErrorInvalidValue;
+}
 
 int launch_stage_pair(int N1, int stage, const OpsP& op, const ProfP& pf, const double* dens64,
                       const StagePairBufs& B, const PairCoef& cf, int Ne, int filt, cudaStream_t s) {

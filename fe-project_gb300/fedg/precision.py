@@ -35,6 +35,9 @@ Errors are computed on the full fields DENS, MOMX, MOMY, MOMZ, RHOT, with moment
 at least 1 m/s of hydrostatic momentum. The deviation fields DDENS and DRHOT are also reported
 against their own norms.
 
+With --case C1 --eqs HEVE the warm bubble runs with its own explicit HEVE scheme (ERK_SSP_3s3o),
+plain FP64 (plain_fp64_heve) against the float-pair mode (pair_heve).
+
 Usage (from the repository root):  PYTHONPATH=fe-project_gb300 python -m fedg.precision [--nex 8 ...]
 """
 from __future__ import annotations
@@ -79,24 +82,33 @@ PATHS = {
     "learned_fp32_tol1e-10": (fl.PREC_MIXED, 1e-10, True),
 }
 REFS = ("plain_fp64_tol1e-13", "plain_fp64_tol1e-10")
+# HEVE (explicit ERK_SSP_3s3o, no implicit solve): FP64 against float pairs
+HEVE_PATHS = {
+    "plain_fp64_heve": (fl.PREC_FP64, 0.0, False),
+    "pair_heve": (fl.PREC_PAIR, 0.0, False),
+}
+HEVE_REFS = ("plain_fp64_heve",)
 
 
 def run(nex=8, ney=8, nez=8, dt=0.04, hours=1.0, checkpoint_min=10.0, chunk=250, paths=tuple(PATHS), seeds=20,
-        train_steps=2000, case_name="C2", out=sys.stdout):
+        train_steps=2000, case_name="C2", eqs="HEVI", out=sys.stdout):
     import dataclasses
 
     import torch
 
     # C2: the density current (default); C1: the +2 K warm bubble of the small case, run with the
-    # HEVI IMEX scheme of the precision form
-    base = cases.C2() if case_name == "C2" else dataclasses.replace(cases.C1(), eqs="HEVI")
+    # HEVI IMEX scheme of the precision form or (eqs="HEVE") with its own explicit HEVE scheme
+    heve = eqs == "HEVE"
+    table, refs = (HEVE_PATHS, HEVE_REFS) if heve else (PATHS, REFS)
+    base = cases.C2() if case_name == "C2" else dataclasses.replace(cases.C1(), eqs=eqs)
     case = base.scaled(nex, ney, nez)
     nsteps = int(round(hours * 3600.0 / dt))
     ck_every = max(1, int(round(checkpoint_min * 60.0 / dt)))
-    info = {"workload": f"{case_name} recipe p={case.porder} {nex}x{ney}x{nez} elements, HEVI IMEX-ARK232",
+    scheme = "HEVE ERK_SSP_3s3o" if heve else "HEVI IMEX-ARK232"
+    info = {"workload": f"{case_name} recipe p={case.porder} {nex}x{ney}x{nez} elements, {scheme}",
             "dt": dt, "steps": nsteps, "simulated_s": nsteps * dt, "paths": list(paths)}
     net = None
-    if any(PATHS[p][2] for p in paths):
+    if any(table[p][2] for p in paths):
         t0 = time.perf_counter()
         # learned-guess recipe: about 200k (stage input, converged increment) pairs from 20 seeds
         # of 4x4x8 slices; 5 steps x 2 implicit stages x 1024 columns per seed
@@ -120,10 +132,11 @@ def run(nex=8, ney=8, nez=8, dt=0.04, hours=1.0, checkpoint_min=10.0, chunk=250,
     while done < nsteps:
         n = min(chunk, nsteps - done, ck_every - done % ck_every)
         for p in paths:
-            prec, tol, guess = PATHS[p]
+            prec, tol, guess = table[p]
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            nf, its = ctx.update(states[p], n, prec=prec, dt=dt, max_iter=30, tol=tol, use_guess=guess)
+            nf, its = ctx.update(states[p], n, eqs=fl.HEVE if heve else fl.HEVI, prec=prec, dt=dt, max_iter=30,
+                                 tol=tol, use_guess=guess)
             torch.cuda.synchronize()
             s = stats[p]
             s["s"] += time.perf_counter() - t0
@@ -133,7 +146,7 @@ def run(nex=8, ney=8, nez=8, dt=0.04, hours=1.0, checkpoint_min=10.0, chunk=250,
         if done % ck_every == 0 or done == nsteps:
             finite = all(bool(torch.isfinite(t).all().item()) for st in states.values() for t in st)
             rec = {"step": done, "t_s": done * dt, "finite": finite, "errors": {}}
-            for ref in REFS:
+            for ref in refs:
                 if ref not in states:
                     continue
                 for p in paths:
@@ -154,6 +167,8 @@ def run(nex=8, ney=8, nez=8, dt=0.04, hours=1.0, checkpoint_min=10.0, chunk=250,
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--case", choices=["C2", "C1"], default="C2")
+    ap.add_argument("--eqs", choices=["HEVI", "HEVE"], default="HEVI",
+                    help="HEVE: C1 with its explicit scheme, paths " + ", ".join(HEVE_PATHS))
     ap.add_argument("--nex", type=int, default=8)
     ap.add_argument("--ney", type=int, default=8)
     ap.add_argument("--nez", type=int, default=8)
@@ -161,18 +176,21 @@ def main(argv=None):
     ap.add_argument("--hours", type=float, default=1.0)
     ap.add_argument("--checkpoint-min", type=float, default=10.0)
     ap.add_argument("--chunk", type=int, default=250)
-    ap.add_argument("--paths", default=",".join(PATHS), help="comma-separated subset of " + ", ".join(PATHS))
+    ap.add_argument("--paths", default=None, help="comma-separated subset of " + ", ".join(PATHS))
     ap.add_argument("--seeds", type=int, default=20)
     ap.add_argument("--train-steps", type=int, default=2000)
     a = ap.parse_args(argv)
     import __graft_entry__ as ge  # noqa: F401  (repository root on sys.path when run from it)
 
     ge.build()
-    paths = tuple(p for p in a.paths.split(",") if p)
-    unknown = [p for p in paths if p not in PATHS]
+    table = HEVE_PATHS if a.eqs == "HEVE" else PATHS
+    if a.eqs == "HEVE" and a.case != "C1":
+        ap.error("--eqs HEVE runs the C1 case")
+    paths = tuple(p for p in (a.paths or ",".join(table)).split(",") if p)
+    unknown = [p for p in paths if p not in table]
     if unknown:
         ap.error(f"unknown paths {unknown}")
-    run(a.nex, a.ney, a.nez, a.dt, a.hours, a.checkpoint_min, a.chunk, paths, a.seeds, a.train_steps, a.case)
+    run(a.nex, a.ney, a.nez, a.dt, a.hours, a.checkpoint_min, a.chunk, paths, a.seeds, a.train_steps, a.case, a.eqs)
     return 0
 
 

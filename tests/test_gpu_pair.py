@@ -60,3 +60,53 @@ def test_pair_vs_fp64_gpu_density_current():
     fe, de = report("pair density current 450 steps", to_np(qp), to_np(q64), b)
     assert max(fe) < FULL_TOL_LONG, fe
     assert max(de) < DEV_TOL, de
+
+
+@pytest.mark.parametrize("name,case,dt,nst", [
+    ("p3_C1", cases.C1(), 0.02, 20),
+    ("p7_C2_4x4x4", cases.replace(cases.C2().scaled(4, 4, 4), eqs="HEVE"), 0.01, 10),
+])
+def test_pair_heve_vs_oracle(name, case, dt, nst):
+    """HEVE (explicit ERK_SSP_3s3o) in float pairs against the oracle's FP64 HEVE steps; the C2
+    slice carries a 10 m/s mean wind, so the reference-wind deviations are exercised."""
+    q, b = cases.initial_state(case)
+    o = orc.Oracle(case.porder, case.NeX, case.NeY, case.NeZ, case.dom)
+    o.set_base_state(b["dens_hyd"], b["pres_hyd"])
+    ref = o.step_heve(q, dt, nst)
+    ctx = fl.Context(case)
+    ctx.set_base_state(b["dens_hyd"], b["pres_hyd"], b["therm_hyd"])
+    qd = [ctx.tensor(a) for a in q]
+    nfail, _ = ctx.update(qd, nst, eqs=fl.HEVE, prec=fl.PREC_PAIR, dt=dt)
+    fe, de = report("pair HEVE " + name, to_np(qd), ref, b)
+    assert nfail == 0
+    assert max(fe) < FULL_TOL, fe
+    assert max(de) < DEV_TOL, de
+
+
+def test_pair_heve_vs_fp64_gpu_long():
+    """1500 HEVE steps (30 s) of the C1 thermal against the FP64 GPU path, at dt = 0.02 s (the
+    largest step that stays stable for this mesh with ERK_SSP_3s3o is between 0.025 and 0.03 s)."""
+    case = cases.C1()
+    q, b = cases.initial_state(case)
+    ctx = fl.Context(case)
+    ctx.set_base_state(b["dens_hyd"], b["pres_hyd"], b["therm_hyd"])
+    q64 = [ctx.tensor(a) for a in q]
+    qp = [ctx.tensor(a) for a in q]
+    ctx.update(q64, 1500, eqs=fl.HEVE, prec=fl.PREC_FP64, dt=0.02)
+    nf, _ = ctx.update(qp, 1500, eqs=fl.HEVE, prec=fl.PREC_PAIR, dt=0.02)
+    assert nf == 0
+    fe, de = report("pair HEVE C1 1500 steps", to_np(qp), to_np(q64), b)
+    assert max(fe) < FULL_TOL_LONG, fe
+    assert max(de) < DEV_TOL, de
+
+
+def test_pair_heve_rejects_guess_and_mixed():
+    case = cases.C1().scaled(2, 2, 2)
+    q, b = cases.initial_state(case)
+    ctx = fl.Context(case)
+    ctx.set_base_state(b["dens_hyd"], b["pres_hyd"], b["therm_hyd"])
+    qd = [ctx.tensor(a) for a in q]
+    with pytest.raises(fl.FedgError, match="HEVE"):
+        ctx.update(qd, 1, eqs=fl.HEVE, prec=fl.PREC_MIXED, dt=case.dt)
+    with pytest.raises(fl.FedgError, match="use_guess"):
+        ctx.update(qd, 1, eqs=fl.HEVE, prec=fl.PREC_PAIR, dt=case.dt, use_guess=True)
