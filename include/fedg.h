@@ -137,14 +137,15 @@ int fedg_tint_advance(fedg_tint* t, int stage, double* const q[5]);           /*
 /* AtmDynDGMDriver_nonhydro3d_update (driver_nonhydro3d.F90:614-963): nsteps full time steps
  * of q (5 device fields) with the fused GPU stage kernels.  eqs FEDG_HEVE uses SSP-RK3,
  * FEDG_HEVI uses IMEX ARK232 with the column Newton solve (max_iter, tol).
- * prec (HEVI only for the last two):
+ * prec (FEDG_PREC_MIXED: HEVI only):
  *   FEDG_PREC_FP64: FElib's arithmetic in FP64.
  *   FEDG_PREC_MIXED: FP32 explicit arithmetic on deviations from the hydrostatic state and the
  *     reference wind; the Newton iterate, its certifying residual and the RK accumulation in
  *     float pairs (about 48 bits); FP32 Jacobian and LU.
  *   FEDG_PREC_PAIR: as FEDG_PREC_MIXED with the explicit operator also in float pairs.
  *     It is FP64-class end to end; use it with a Newton tol near 1e-13, so the FP32
- *     corrections are refined to pair accuracy.
+ *     corrections are refined to pair accuracy.  With eqs FEDG_HEVE: the three SSP-RK3 stages in
+ *     float pairs (no implicit solve; use_guess must be 0, iters_out is 0).
  * use_guess != 0 takes the initial Newton iterate from the column-guess network loaded with
  * fedg_guess_load.
  * iters_out (optional, host): mean Newton solves per implicit column solve. */
