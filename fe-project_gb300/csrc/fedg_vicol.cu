@@ -661,14 +661,16 @@ __global__ void __launch_bounds__(32, 9) k_vi_cols(const Ops op, const OpsX ox, 
   __syncwarp();
   const size_t gcolumn = (size_t)col, glayer = (size_t)ncol;  // G history rows of this column
   const float cref = (float)args.cref;
-  col_residual<N1, false>(ox, c, px, qin, args.impl2, cref);
-  col_solve<N1>(op, px, kapf, c, args.impl_fac, gsc, gcolumn, glayer, true);
-  int nsolve = 1, st = 0;
+  // One call site per routine (the first residual is the FP32 one and is not tested; every
+  // column takes the first correction), which keeps the kernel's code small enough for the
+  // instruction caches.
+  int nsolve = 0, st = 0;
   bool active = true;
   while (true) {
-    const float err = args.check64 ? col_residual<N1, true>(ox, c, px, qin, args.impl2, cref)
-                                   : col_residual<N1, false>(ox, c, px, qin, args.impl2, cref);
-    if (active) {
+    const bool cert = nsolve > 0 && args.check64;
+    const float err = cert ? col_residual<N1, true>(ox, c, px, qin, args.impl2, cref)
+                           : col_residual<N1, false>(ox, c, px, qin, args.impl2, cref);
+    if (active && nsolve > 0) {
       if (err != err) { st = -2; active = false; }
       else if ((double)err <= args.tol) { st = nsolve; active = false; }
       else if (nsolve >= args.max_iter) { st = -1; active = false; }
