@@ -257,52 +257,96 @@ __device__ float col_residual(const OpsX& ox, const Col<N1>& c, const ProfX& px,
 }
 
 // ---------------------------------------------------------------------------------------------
-// Element LU without pivoting of the 3*N1 rows held 3 per lane (row 3k+v in lane k), with four
-// right-hand sides; on return r = A^-1 r.  The pivot row reaches the other lanes of the column
-// group by shuffles (width N1), and rows that a step does not touch get a zero multiplier, so
-// the factorisation is branch-free and needs neither shared memory nor barriers.  The pivot
-// index is a template parameter so every register index is a compile-time constant.
-template <int N1, int kk>
+// Element LU without pivoting of the 3*N1 rows held 3 per lane (row 3k+v in lane k: v = DENS,
+// MOMZ, RHOT of node k), with four right-hand sides; on return r = A^-1 r.  The pivot row reaches
+// the other lanes of the column group by shuffles (width N1); every register index is a
+// compile-time constant.
+//
+// Pivot order and sparsity.  The DENS rows of an element block are
+//   I + (Lift face terms in the DENS columns of nodes 0 and N)
+//     + impl_fac E33 D (MOMZ columns) + (block-Thomas update: node-0 columns, RHOT_0 included),
+// so a DENS row has nonzeros only in DENS_k, DENS_0, DENS_N, the MOMZ columns and RHOT_0.  The
+// DENS pivots go first (DENS_0 .. DENS_N), then MOMZ/RHOT node by node.  A DENS pivot row then
+// carries at most DENS_N, the N1 MOMZ columns and RHOT_0 to the right, and eliminating DENS_i
+// (0 < i < N) leaves the other DENS rows untouched (their DENS_i entry is zero); what remains is
+// the dense 2*N1 system of the MOMZ/RHOT Schur complement.  Against the natural order this
+// issues about a quarter fewer shuffles and half the FMAs.
+template <int N1>
+struct PivOrder {
+  // column (3 node + var) of pivot step s, and the step at which column c is pivoted
+  __host__ __device__ static constexpr int col(int s) { return s < N1 ? 3 * s : 3 * ((s - N1) / 2) + 1 + ((s - N1) & 1); }
+  __host__ __device__ static constexpr int pos(int c) { return c % 3 == 0 ? c / 3 : N1 + 2 * (c / 3) + (c % 3 - 1); }
+  // can the pivot row of step s hold a nonzero in column c (c not yet pivoted)?
+  __host__ __device__ static constexpr bool nz(int s, int c) {
+    if (pos(c) <= s) return false;
+    if (s >= N1) return true;  // MOMZ/RHOT phase: dense
+    return c == 3 * (N1 - 1) || c % 3 == 1 || c == 2;
+  }
+};
+
+template <int N1, int s>
 __device__ __forceinline__ void shfl_fwd(float (&a)[3][3 * N1], float (&r)[3][4], int k) {
   constexpr int n = 3 * N1;
-  if constexpr (kk < n) {
-    constexpr int owner = kk / 3, vv = kk % 3;
-    const float piv = __shfl_sync(FULL, a[vv][kk], owner, N1);
+  using O = PivOrder<N1>;
+  if constexpr (s < n) {
+    constexpr int pc = O::col(s), owner = pc / 3, vv = pc % 3;
+    // rows still to eliminate: DENS rows only at the first step (the DENS_0 column), MOMZ/RHOT
+    // rows until their own pivot
+    constexpr bool drows = s == 0;
+    const float piv = __shfl_sync(FULL, a[vv][pc], owner, N1);
     const float inv = __fdividef(1.f, piv);
     float f[3];
+    f[0] = (drows && k > 0) ? a[0][pc] * inv : 0.f;
 #pragma unroll
-    for (int v = 0; v < 3; ++v) f[v] = (3 * k + v > kk) ? a[v][kk] * inv : 0.f;
+    for (int v = 1; v < 3; ++v) f[v] = (O::pos(3 * k + v) > s) ? a[v][pc] * inv : 0.f;
 #pragma unroll
-    for (int cc = kk + 1; cc < n; ++cc) {
-      const float p = __shfl_sync(FULL, a[vv][cc], owner, N1);
+    for (int cc = 0; cc < n; ++cc) {
+      if (O::nz(s, cc)) {  // constant after unrolling
+        const float p = __shfl_sync(FULL, a[vv][cc], owner, N1);
+        if (drows) a[0][cc] = fmaf(-f[0], p, a[0][cc]);
 #pragma unroll
-      for (int v = 0; v < 3; ++v) a[v][cc] = fmaf(-f[v], p, a[v][cc]);
+        for (int v = 1; v < 3; ++v) a[v][cc] = fmaf(-f[v], p, a[v][cc]);
+      }
     }
 #pragma unroll
     for (int m = 0; m < 4; ++m) {
       const float p = __shfl_sync(FULL, r[vv][m], owner, N1);
+      if (drows) r[0][m] = fmaf(-f[0], p, r[0][m]);
 #pragma unroll
-      for (int v = 0; v < 3; ++v) r[v][m] = fmaf(-f[v], p, r[v][m]);
+      for (int v = 1; v < 3; ++v) r[v][m] = fmaf(-f[v], p, r[v][m]);
     }
-    shfl_fwd<N1, kk + 1>(a, r, k);
+    shfl_fwd<N1, s + 1>(a, r, k);
   }
 }
-template <int N1, int kk>
+template <int N1, int s>
 __device__ __forceinline__ void shfl_bwd(float (&a)[3][3 * N1], float (&r)[3][4], int k) {
-  if constexpr (kk >= 0) {
-    constexpr int owner = kk / 3, vv = kk % 3;
-    const float inv = __fdividef(1.f, __shfl_sync(FULL, a[vv][kk], owner, N1));
+  using O = PivOrder<N1>;
+  if constexpr (s >= 0) {
+    constexpr int pc = O::col(s), owner = pc / 3, vv = pc % 3;
+    const float inv = __fdividef(1.f, __shfl_sync(FULL, a[vv][pc], owner, N1));
     float x[4];
 #pragma unroll
     for (int m = 0; m < 4; ++m) x[m] = __shfl_sync(FULL, r[vv][m], owner, N1) * inv;
+    // rows pivoted before step s that can hold a nonzero in column pc: DENS rows for the MOMZ
+    // columns, RHOT_0 and DENS_N; MOMZ/RHOT rows in the MOMZ/RHOT phase
+    constexpr bool dcol = (pc % 3 == 1) || pc == 2 || pc == 3 * (N1 - 1);
 #pragma unroll
     for (int v = 0; v < 3; ++v) {
-      const int row = 3 * k + v;
-      const float g = row < kk ? a[v][kk] : 0.f;
+      if (v == 0 && !dcol) {
+        if (k == owner && vv == 0) {
 #pragma unroll
-      for (int m = 0; m < 4; ++m) r[v][m] = row == kk ? x[m] : fmaf(-g, x[m], r[v][m]);
+          for (int m = 0; m < 4; ++m) r[0][m] = x[m];
+        }
+        continue;
+      }
+      if (v > 0 && s < N1) continue;  // DENS pivots: MOMZ/RHOT rows come later in the order
+      const int row = 3 * k + v;
+      const bool before = O::pos(row) < s;
+      const float g = before ? a[v][pc] : 0.f;
+#pragma unroll
+      for (int m = 0; m < 4; ++m) r[v][m] = row == pc ? x[m] : fmaf(-g, x[m], r[v][m]);
     }
-    shfl_bwd<N1, kk - 1>(a, r, k);
+    shfl_bwd<N1, s - 1>(a, r, k);
   }
 }
 template <int N1>
