@@ -66,6 +66,47 @@ __device__ __forceinline__ void face_nb(const OpsP& op, int f, int ke, int ex, i
   }
 }
 
+// stage-3 output: modal filter (tensorprod3D_kernel.F90:2555-2618) of the five deviation fields,
+// all five per pass (three barriers), then q^{n+1} = ref + F(dev) in FP64 and its deviation pair.
+// fa, fb: [5][Np] float2 of this element (free shared memory at this point).
+template <int N1>
+__device__ __forceinline__ void filter_store(const OpsP& op, float2* fa, float2* fb, const f2 (&dev)[5],
+                                             const f2 (&ref)[5], const StagePairBufs& B, size_t g, bool valid,
+                                             int i, int j, int k, int p) {
+  constexpr int Np = N1 * N1 * N1, NF = N1 * N1;
+#pragma unroll
+  for (int v = 0; v < 5; ++v) fa[v * Np + p] = f2_pack(dev[v]);
+  __syncthreads();
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    f2acc s1;
+#pragma unroll
+    for (int l = 0; l < N1; ++l) s1.add(f2_of(op.F[i * N1 + l]), f2_of(fa[v * Np + l + N1 * j + NF * k]));
+    fb[v * Np + p] = f2_pack(s1.get());
+  }
+  __syncthreads();
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    f2acc s2;
+#pragma unroll
+    for (int l = 0; l < N1; ++l) s2.add(f2_of(op.F[j * N1 + l]), f2_of(fb[v * Np + i + N1 * l + NF * k]));
+    fa[v * Np + p] = f2_pack(s2.get());
+  }
+  __syncthreads();
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    f2acc s3;
+#pragma unroll
+    for (int l = 0; l < N1; ++l) s3.add(f2_of(op.Fv[k * N1 + l]), f2_of(fa[v * Np + i + N1 * j + NF * l]));
+    if (valid) {
+      const f2 fil = s3.get();
+      const f2 out = ref[v] + fil;
+      B.qn[v][g] = (double)out.h + (double)out.l;
+      B.qnf[v][g] = f2_pack(fil);
+    }
+  }
+}
+
 // HEVE: the explicit HEVE operator (heve.F90:292-489, heve_numflux.F90:946-1139: vertical DENS/RHOT
 // fluxes, the vertical pressure gradient and -g VFilterPM1(DDENS) explicit, unmasked wave speed) with
 // the SSP-RK3 low-storage update (timeint_rk.F90:1182-1278) in place of the IMEX ARK232 stages
@@ -312,33 +353,7 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
       return;
     }
     __syncthreads();  // everyone is done with the shared arrays
-    float2* fa = s_st + le * 6 * Np;
-    float2* fb = fa + Np;
-    for (int v = 0; v < 5; ++v) {
-      fa[p] = f2_pack(dev[v]);
-      __syncthreads();
-      f2acc s1;
-#pragma unroll
-      for (int l = 0; l < N1; ++l) s1.add(f2_of(op.F[i * N1 + l]), f2_of(fa[l + N1 * j + NF * k]));
-      fb[p] = f2_pack(s1.get());
-      __syncthreads();
-      f2acc s2;
-#pragma unroll
-      for (int l = 0; l < N1; ++l) s2.add(f2_of(op.F[j * N1 + l]), f2_of(fb[i + N1 * l + NF * k]));
-      __syncthreads();
-      fa[p] = f2_pack(s2.get());
-      __syncthreads();
-      f2acc s3;
-#pragma unroll
-      for (int l = 0; l < N1; ++l) s3.add(f2_of(op.Fv[k * N1 + l]), f2_of(fa[i + N1 * j + NF * l]));
-      if (valid) {
-        const f2 fil = s3.get();
-        const f2 out = ref[v] + fil;
-        B.qn[v][g] = (double)out.h + (double)out.l;
-        B.qnf[v][g] = f2_pack(fil);
-      }
-      __syncthreads();
-    }
+    filter_store<N1>(op, s_st + le * 6 * Np, s_fl + le * 15 * Np, dev, ref, B, g, valid, i, j, k, p);
     return;
   }
   if (STAGE == 1 || STAGE == 2) {
@@ -403,33 +418,7 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
     return;
   }
   __syncthreads();  // everyone is done with the shared arrays
-  float2* fa = s_st + le * 6 * Np;
-  float2* fb = fa + Np;
-  for (int v = 0; v < 5; ++v) {
-    fa[p] = f2_pack(dev[v]);
-    __syncthreads();
-    f2acc s1;
-#pragma unroll
-    for (int l = 0; l < N1; ++l) s1.add(f2_of(op.F[i * N1 + l]), f2_of(fa[l + N1 * j + NF * k]));
-    fb[p] = f2_pack(s1.get());
-    __syncthreads();
-    f2acc s2;
-#pragma unroll
-    for (int l = 0; l < N1; ++l) s2.add(f2_of(op.F[j * N1 + l]), f2_of(fb[i + N1 * l + NF * k]));
-    __syncthreads();
-    fa[p] = f2_pack(s2.get());
-    __syncthreads();
-    f2acc s3;
-#pragma unroll
-    for (int l = 0; l < N1; ++l) s3.add(f2_of(op.Fv[k * N1 + l]), f2_of(fa[i + N1 * j + NF * l]));
-    if (valid) {
-      const f2 fil = s3.get();
-      const f2 out = ref[v] + fil;
-      B.qn[v][g] = (double)out.h + (double)out.l;
-      B.qnf[v][g] = f2_pack(fil);
-    }
-    __syncthreads();
-  }
+  filter_store<N1>(op, s_st + le * 6 * Np, s_fl + le * 15 * Np, dev, ref, B, g, valid, i, j, k, p);
 }
 
 template <int N1>
