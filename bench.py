@@ -347,6 +347,37 @@ def tracer_bench(args, torch, np, fl, cases, peaks, peak_src, steps, warmup):
             "gpu_launches": sum(v[1] for v in prof.values())}
 
 
+def heve_bench(args, torch, np, fl, ctx, q_host, dofs_stage, dnorm2, dens_hyd, therm_hyd):
+    """The HEVE scheme (config 1's explicit SSP-RK3 with the vertical terms explicit) on the bench
+    workload: plain FP64 against the float-pair mode, from the same state, dt half the HEVI step.
+    DOF-stage/s as for the headline (3 stages per step); the full-field relative L2 of the pair
+    path against FP64 after the timed steps."""
+    stream = torch.cuda.ExternalStream(ctx.stream_handle)
+    dt = 0.5 * DT_STABLE
+    out = {"dt": dt, "steps": args.steps}
+    qs = {}
+    for name, prec in (("fp64", fl.PREC_FP64), ("pair", fl.PREC_PAIR)):
+        q = [torch.empty(h.shape, dtype=h.dtype, device=ctx.dev) for h in q_host]
+        for a, h in zip(q, q_host):
+            a.copy_(h)
+        o = dict(eqs=fl.HEVE, prec=prec, dt=dt)
+        ctx.update(q, 1, **o)  # warm-up step (also allocates the pair scratch)
+        for a, h in zip(q, q_host):
+            a.copy_(h)
+        fl.prof_reset(ctx)
+        fl.prof_enable(ctx, True)
+        ms, _, _ = _timed_update(ctx, torch, stream, q, args.steps, o)
+        fl.prof_enable(ctx, False)
+        launches = sum(v[1] for v in fl.prof_read(ctx).values())
+        out[name] = {"value": dofs_stage * args.steps / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms / args.steps,
+                     "gpu_launches_per_step": launches / args.steps}
+        qs[name] = q
+    out["speedup_pair_vs_fp64"] = out["pair"]["value"] / out["fp64"]["value"]
+    out["pair_rel_l2_vs_fp64"] = _full_field_errors(np, qs["pair"], qs["fp64"], dnorm2, dens_hyd, therm_hyd)
+    del qs
+    return out
+
+
 def numdiff_bench(args, torch, np, fl, ctx, qd, peaks, peak_src, case):
     """Numerical diffusion (FElib's hyperdiffusion filter, nonhydro3d_numdiff.F90) and the sponge layer
     (dgm_spongelayer.F90) on the bench state: one application each, FP64.  DOF = one value of one
@@ -593,6 +624,9 @@ def run_fedg(args):
     ndf = None
     if rank == 0 and not args.no_numdiff:
         ndf = numdiff_bench(args, torch, np, fl, ctx, qd, peaks, peak_src, case)
+    hv = None
+    if rank == 0 and not args.no_heve:
+        hv = heve_bench(args, torch, np, fl, ctx, q_host, dofs_stage, dnorm2, dens_hyd, therm_hyd)
 
     finite = all(bool(torch.isfinite(t).all().item()) for t in qd)
     if rank == 0:
@@ -620,6 +654,7 @@ def run_fedg(args):
             "accuracy": acc,
             "tracer_advection": trc,
             "numdiff_sponge": ndf,
+            "heve": hv,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -643,6 +678,7 @@ def main():
     ap.add_argument("--small", action="store_true", help="32x32x16 elements instead of 128x128x16 (profiling)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-heve", action="store_true", help="skip the HEVE (FP64 vs float pairs) side measurement")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--no-other", action="store_true", help="skip the run of the other precision mode")
     ap.add_argument("--no-tracer", action="store_true", help="skip the tracer-advection measurement")

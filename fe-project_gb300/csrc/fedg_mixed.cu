@@ -330,31 +330,38 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
     return;
   }
   __syncthreads();  // everyone is done with the shared arrays
-  float* fa = s_st + le * 6 * Np;
-  float* fb = fa + Np;
+  // the five fields per pass: three barriers
+  float* fa = s_st + le * 6 * Np;   // [5][Np]
+  float* fb = s_fl + le * 15 * Np;  // [5][Np]
+#pragma unroll
+  for (int v = 0; v < 5; ++v) fa[v * Np + p] = dev[v];
+  __syncthreads();
+#pragma unroll
   for (int v = 0; v < 5; ++v) {
-    fa[p] = dev[v];
-    __syncthreads();
     float sacc = 0.f;
 #pragma unroll
-    for (int l = 0; l < N1; ++l) sacc = fmaf(op.F[i * N1 + l], fa[l + N1 * j + NF * k], sacc);
-    fb[p] = sacc;
-    __syncthreads();
-    sacc = 0.f;
+    for (int l = 0; l < N1; ++l) sacc = fmaf(op.F[i * N1 + l], fa[v * Np + l + N1 * j + NF * k], sacc);
+    fb[v * Np + p] = sacc;
+  }
+  __syncthreads();
 #pragma unroll
-    for (int l = 0; l < N1; ++l) sacc = fmaf(op.F[j * N1 + l], fb[i + N1 * l + NF * k], sacc);
-    __syncthreads();
-    fa[p] = sacc;
-    __syncthreads();
-    sacc = 0.f;
+  for (int v = 0; v < 5; ++v) {
+    float sacc = 0.f;
 #pragma unroll
-    for (int l = 0; l < N1; ++l) sacc = fmaf(op.Fv[k * N1 + l], fa[i + N1 * j + NF * l], sacc);
+    for (int l = 0; l < N1; ++l) sacc = fmaf(op.F[j * N1 + l], fb[v * Np + i + N1 * l + NF * k], sacc);
+    fa[v * Np + p] = sacc;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    float sacc = 0.f;
+#pragma unroll
+    for (int l = 0; l < N1; ++l) sacc = fmaf(op.Fv[k * N1 + l], fa[v * Np + i + N1 * j + NF * l], sacc);
     if (valid) {
       const double ref = v == VMX ? dh64 * cf.Uref : (v == VMY ? dh64 * cf.Vref : 0.0);
       B.qn[v][g] = ref + (double)sacc;
       B.qnf[v][g] = sacc;
     }
-    __syncthreads();
   }
 }
 
