@@ -52,7 +52,7 @@ PATH_DTYPE = {"pair": "f32x2", "mixed": "f32+f32x2", "fp64": "f64"}
 # DRAM bytes per node of one launch of the dominant kernel from ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum on the 32x32x16-element slice, 8,388,608 nodes; profiles/), per path
 NCU_BYTES_PER_NODE = {
-    "pair": {"vi_mixed": (936.96e6 + 1159.80e6) / (32 * 32 * 16 * 512)},
+    "pair": {"vi_mixed": (895.11e6 + 1128.88e6) / (32 * 32 * 16 * 512)},
     "mixed": {"vi_mixed": (847.3e6 + 728.2e6) / (32 * 32 * 16 * 512)},
 }
 
