@@ -197,6 +197,7 @@ class Context:
         self.shape = (case.Ne, case.Np)
         self.ncol = case.NeX * case.NeY * case.N1 * case.N1
         self._base = None
+        self._coriolis = None
 
     def close(self):
         if getattr(self, "h", None):
@@ -225,12 +226,20 @@ class Context:
         return self.lib.fedg_ctx_stream(self.h)
 
     # -- FElib interface --
-    def set_base_state(self, dens_hyd, pres_hyd, therm_hyd):
+    def set_base_state(self, dens_hyd, pres_hyd, therm_hyd, coriolis_f=0.0):
+        """Registers the base state; coriolis_f != 0 passes a constant 2D CORIOLIS(Np2D, NeA2D) field
+        (an f-plane), as FElib's AUX_VARS2D would hold it."""
         b = [self.tensor(dens_hyd), self.tensor(pres_hyd), self.tensor(therm_hyd)]
+        cor = None
+        if coriolis_f:
+            c = self.case
+            cor = self.torch.full((c.NeX * c.NeY, c.N1 * c.N1), float(coriolis_f), dtype=self.torch.float64,
+                                  device=self.dev)
         self.torch.cuda.synchronize()
         _check(self.lib.fedg_set_base_state(self.h, _ptr(b[0]), _ptr(b[1]), _ptr(b[2]), None, None, None, None,
-                                            None, None), "fedg_set_base_state")
+                                            None, _ptr(cor) if cor is not None else None), "fedg_set_base_state")
         self._base = b
+        self._coriolis = cor
         return b
 
     def drhot2pres(self, drhot):
@@ -243,9 +252,10 @@ class Context:
     def cal_tend_ex(self, q, eqs, dpres=None):
         out = [self.empty() for _ in range(5)]
         b = self._base
+        cor = getattr(self, "_coriolis", None)
         ins = (ctypes.c_void_p * 16)(*[t.data_ptr() for t in q], dpres.data_ptr() if dpres is not None else None,
                                      b[0].data_ptr(), b[1].data_ptr(), None, b[2].data_ptr(),
-                                     None, None, None, None, None, None)
+                                     cor.data_ptr() if cor is not None else None, None, None, None, None, None)
         self.torch.cuda.synchronize()
         _check(self.lib.fedg_cal_tend_ex(self.h, ins, _p5(out), int(eqs)), "fedg_cal_tend_ex")
         self.sync()

@@ -28,6 +28,8 @@ NEWTON_TOL = 1e-13
     ("p7_C2_4x4x4", cases.C2().scaled(4, 4, 4), 0.04, 10),
     ("p3_C1", cases.C1(), 0.02, 20),
     ("p7_C5_4x4x8", cases.C5().scaled(4, 4, 8), 0.005, 10),
+    # 27 elements: the last block of four p=3 elements is partly empty
+    ("p3_C1_3x3x3_ragged", cases.replace(cases.C1().scaled(3, 3, 3), eqs="HEVI"), 0.02, 10),
 ])
 def test_pair_vs_oracle(name, case, dt, nst):
     q, b = cases.initial_state(case)
@@ -65,6 +67,7 @@ def test_pair_vs_fp64_gpu_density_current():
 @pytest.mark.parametrize("name,case,dt,nst", [
     ("p3_C1", cases.C1(), 0.02, 20),
     ("p7_C2_4x4x4", cases.replace(cases.C2().scaled(4, 4, 4), eqs="HEVE"), 0.01, 10),
+    ("p3_C1_3x3x3_ragged", cases.C1().scaled(3, 3, 3), 0.02, 10),
 ])
 def test_pair_heve_vs_oracle(name, case, dt, nst):
     """HEVE (explicit ERK_SSP_3s3o) in float pairs against the oracle's FP64 HEVE steps; the C2
