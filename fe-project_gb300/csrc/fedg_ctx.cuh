@@ -59,6 +59,9 @@ int trc_update_pair(fedg_ctx* c, double* QTRC, const double* const mflx[3], cons
 // fedg_numdiff_apply_prec in float pairs (fedg_nd_pair.cu); scratch: 5 Np*Ne doubles
 int numdiff_apply_pair(fedg_ctx* c, double* const q[5], int nlap, double coef_h, double coef_v, double dt,
                        double* scratch);
+// sponge-layer coefficient at the L LGL levels of the column (dgm_spongelayer.F90): 0.25/tau
+// (1 + sign(z - h)) (1 - cos(pi (z - h) / (z_top - h)))
+void sponge_coef_host(const fedg_ctx* c, double tau, double height, double* coef);
 }  // namespace fedg
 
 // Runs one launch f() of kernel class id on the context stream, counting it and, when the

@@ -239,6 +239,14 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
     }
     tex[VMX] += op.coriolis_f * (qv[VMY] + dh * op.Vref);
     tex[VMY] -= op.coriolis_f * (qv[VMX] + dh * op.Uref);
+    if (pf.sl) {  // sponge layer on the explicit tendency (driver_nonhydro3d.F90:831-841)
+      const float cz = __ldg(pf.sl + lev);
+      tex[VMZ] -= cz * qv[VMZ];
+      if (pf.sl_h != 0.f) {
+        tex[VMX] -= cz * (qv[VMX] + dh * op.Uref);
+        tex[VMY] -= cz * (qv[VMY] + dh * op.Vref);
+      }
+    }
     if (STAGE == 1) {
       float sdp = 0.f, drho = 0.f;
 #pragma unroll
@@ -444,6 +452,9 @@ struct MixedState {
   float2* pbuf = nullptr;
   void** d_pptrs = nullptr;  // device arrays of pointers: TI[5], QSF[5] (pairs)
   float2* prof5 = nullptr;   // [5][L] DENS_hyd, PRES_hyd, THERM_hyd, 1/THERM_hyd, THERM_hyd/DENS_hyd
+  // sponge-layer coefficient per level, pairs then FP32 ([L] each), for the (tau, height) in sl_key
+  float2* sl2 = nullptr;
+  double sl_key[2] = {0.0, 0.0};
   OpsP opp;
   OpsF opf;
   OpsX opx;
@@ -479,6 +490,7 @@ void mixed_free(MixedState* m) {
   cudaFree(m->pbuf);
   cudaFree(m->d_pptrs);
   cudaFree(m->prof5);
+  cudaFree(m->sl2);
   delete m;
 }
 
@@ -621,6 +633,38 @@ static int pair_setup(fedg_ctx* c, MixedState* m) {
   return 0;
 }
 
+// sponge-layer coefficient of the registered sponge (fedg_update_set_sponge) as float pairs and
+// FP32, uploaded when (tau, height) change; the profile pointers stay NULL without a sponge
+static int set_sponge_prof(fedg_ctx* c, MixedState* m, ProfF* pff, ProfP* pfp) {
+  if (!(c->sl_tau > 0.0)) return 0;
+  const int L = c->L;
+  if (!m->sl2 && cudaMalloc(&m->sl2, sizeof(float2) * L + sizeof(float) * L) != cudaSuccess) {
+    m->sl2 = nullptr;
+    return api_fail("fedg_update: out of device memory (sponge profile)");
+  }
+  float* slf = reinterpret_cast<float*>(m->sl2 + L);
+  if (!(m->sl_key[0] == c->sl_tau && m->sl_key[1] == c->sl_height)) {
+    std::vector<double> coef(L);
+    sponge_coef_host(c, c->sl_tau, c->sl_height, coef.data());
+    std::vector<float2> h2(L);
+    std::vector<float> hf(L);
+    for (int l = 0; l < L; ++l) {
+      h2[l] = split_host(coef[l]);
+      hf[l] = (float)coef[l];
+    }
+    // synchronous copies: the host vectors go out of scope here
+    if (cudaMemcpy(m->sl2, h2.data(), sizeof(float2) * L, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(slf, hf.data(), sizeof(float) * L, cudaMemcpyHostToDevice) != cudaSuccess)
+      return api_fail("fedg_update: sponge profile upload");
+    m->sl_key[0] = c->sl_tau;
+    m->sl_key[1] = c->sl_height;
+  }
+  const float h = c->sl_hvel ? 1.f : 0.f;
+  if (pff) { pff->sl = slf; pff->sl_h = h; }
+  if (pfp) { pfp->sl = m->sl2; pfp->sl_h = h; }
+  return 0;
+}
+
 // reference wind of the deviations = domain-mean velocity of the first state seen
 static int set_ref_wind(fedg_ctx* c, MixedState* m, double* const q[5]) {
   if (m->wind_set) return 0;
@@ -668,8 +712,9 @@ static int pair_update_heve(fedg_ctx* c, double* const q[5], int nsteps, const f
   pc.ssp[1] = split_host(0.25);
   pc.ssp[2] = split_host(1.0 / 3.0);
   pc.ssp[3] = split_host(2.0 / 3.0);
-  const ProfP pfp{m->prof5, m->prof5 + c->L, m->prof5 + 2 * c->L, m->prof5 + 3 * c->L, m->prof5 + 4 * c->L,
-                  m->prof + c->L};
+  ProfP pfp{m->prof5, m->prof5 + c->L, m->prof5 + 2 * c->L, m->prof5 + 3 * c->L, m->prof5 + 4 * c->L,
+            m->prof + c->L};
+  if ((r = set_sponge_prof(c, m, nullptr, &pfp))) return r;
   StagePairBufs BP;
   std::memset(&BP, 0, sizeof(BP));
   for (int v = 0; v < 5; ++v) {
@@ -716,7 +761,7 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
   if (o->use_guess && !mlp_ready(c->guess)) return api_fail("fedg_update: use_guess set but no trained column-guess network is loaded (fedg_guess_load)");
   const double alp = (3.0 + 2.0 * std::sqrt(2.0)) / 6.0, gam = 1.0 - 1.0 / std::sqrt(2.0), del = 1.0 / (2.0 * std::sqrt(2.0));
   MixCoef cf{o->dt, 2.0 * gam, gam, 1.0 - alp, del, alp, del, del, del, gam, 0.0, 0.0, {0.f, 0.f}, {0.f, 0.f}};
-  const ProfF pff{m->prof, m->prof + c->L, m->prof + 2 * c->L, m->prof + 3 * c->L};
+  ProfF pff{m->prof, m->prof + c->L, m->prof + 2 * c->L, m->prof + 3 * c->L};
   StageBufs B;
   std::memset(&B, 0, sizeof(B));
   for (int v = 0; v < 5; ++v) {
@@ -738,8 +783,9 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
   MixViArgs va{impl_fac, 1.0 / impl_fac, o->tol, 340.0, split_host(impl_fac), split_host(1.0 / impl_fac), o->max_iter, 1};
   const PairCoef pc{split_host(o->dt), split_host(2.0 * gam), split_host(gam), split_host(1.0 - alp), split_host(del),
                     split_host(alp), split_host(del), split_host(del), split_host(del), split_host(gam)};
-  const ProfP pfp{m->prof5, m->prof5 + c->L, m->prof5 + 2 * c->L, m->prof5 + 3 * c->L, m->prof5 + 4 * c->L,
-                  m->prof + c->L};
+  ProfP pfp{m->prof5, m->prof5 + c->L, m->prof5 + 2 * c->L, m->prof5 + 3 * c->L, m->prof5 + 4 * c->L,
+            m->prof + c->L};
+  if ((r = set_sponge_prof(c, m, &pff, &pfp))) return r;
   StagePairBufs BP;
   std::memset(&BP, 0, sizeof(BP));
   if (pair) {

@@ -25,7 +25,9 @@ struct ProfF {
   const float* dens;
   const float* pres;
   const float* therm;
-  const float* rtherm;  // 1 / THERM_hyd
+  const float* rtherm;       // 1 / THERM_hyd
+  const float* sl = nullptr; // sponge-layer coefficient per level (NULL: no sponge)
+  float sl_h = 0.f;          // 1: the sponge also damps MOMX/MOMY
 };
 
 
@@ -75,6 +77,8 @@ struct OpsP {
 struct ProfP {
   const float2 *dh, *ph, *th, *rth, *ptr;  // DENS_hyd, PRES_hyd, THERM_hyd, 1/THERM_hyd, THERM_hyd/DENS_hyd
   const float* phf;                         // PRES_hyd in FP32 (wave speed)
+  const float2* sl = nullptr;               // sponge-layer coefficient per level (NULL: no sponge)
+  float sl_h = 0.f;                         // 1: the sponge also damps MOMX/MOMY
 };
 struct PairCoef {
   float2 dt, a21e, a21i, a31e, a31i, a32e, a32i, b1, b2, b3;

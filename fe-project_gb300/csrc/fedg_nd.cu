@@ -300,6 +300,20 @@ int nd_pass(int pass, const Ops& op, const double* dp, const double* a, const do
 }  // namespace
 }  // namespace fedg
 
+namespace fedg {
+void sponge_coef_host(const fedg_ctx* c, double tau, double height, double* coef) {
+  std::vector<double> xs(c->N1);
+  lgl_nodes_1d(c->N1 - 1, xs.data());
+  const double dz = (c->d.zmax - c->d.zmin) / c->d.NeZ, rt = 1.0 / tau, ztop = c->d.zmax;
+  for (int l = 0; l < c->L; ++l) {
+    const int ez = l / c->N1, k = l - ez * c->N1;
+    const double z = c->d.zmin + (ez + 0.5 * (xs[k] + 1.0)) * dz;
+    coef[l] = 0.25 * rt * (1.0 + (std::signbit(z - height) ? -1.0 : 1.0)) *
+              (1.0 - std::cos(M_PI * (z - height) / (ztop - height)));
+  }
+}
+}  // namespace fedg
+
 extern "C" {
 
 int fedg_numdiff_apply(fedg_ctx* c, double* const q[5], int nlap, double coef_h, double coef_v, double dt) {
@@ -365,18 +379,8 @@ int fedg_sponge_add_tend(fedg_ctx* c, double* const tend[3], const double* const
   if (!(tau > 0.0)) return api_fail("fedg_sponge_add_tend: tau must be positive");
   if (!(height < c->d.zmax)) return api_fail("fedg_sponge_add_tend: the damping height must be below the top");
   cudaSetDevice(c->d.device);
-  // per-level coefficient 0.25/tau (1 + sign(z - h)) (1 - cos(pi (z - h)/(z_top - h))) at the LGL levels
-  const int N = c->N1 - 1;
-  std::vector<double> xs(c->N1);
-  lgl_nodes_1d(N, xs.data());
   std::vector<double> coef(c->L);
-  const double dz = (c->d.zmax - c->d.zmin) / c->d.NeZ, rt = 1.0 / tau, ztop = c->d.zmax;
-  for (int l = 0; l < c->L; ++l) {
-    const int ez = l / c->N1, k = l - ez * c->N1;
-    const double z = c->d.zmin + (ez + 0.5 * (xs[k] + 1.0)) * dz;
-    coef[l] = 0.25 * rt * (1.0 + (std::signbit(z - height) ? -1.0 : 1.0)) *
-              (1.0 - std::cos(M_PI * (z - height) / (ztop - height)));
-  }
+  sponge_coef_host(c, tau, height, coef.data());
   if (!c->sponge_coef && cudaMalloc(&c->sponge_coef, sizeof(double) * c->L) != cudaSuccess) {
     c->sponge_coef = nullptr;
     return api_fail("fedg_sponge_add_tend: out of device memory");

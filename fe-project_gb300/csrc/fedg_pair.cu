@@ -287,6 +287,14 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
     }
     tex[VMX] = tex[VMX] + f2_of(op.cor) * (qv[VMY] + dh * V);
     tex[VMY] = tex[VMY] - f2_of(op.cor) * (qv[VMX] + dh * U);
+    if (pf.sl) {  // sponge layer on the explicit tendency (driver_nonhydro3d.F90:831-841)
+      const f2 cz = ld2(pf.sl + lev);
+      tex[VMZ] = tex[VMZ] - cz * qv[VMZ];
+      if (pf.sl_h != 0.f) {
+        tex[VMX] = tex[VMX] - cz * (qv[VMX] + dh * U);
+        tex[VMY] = tex[VMY] - cz * (qv[VMY] + dh * V);
+      }
+    }
     if (HEVE) {  // -g VFilterPM1(DDENS) (heve.F90:447-452)
       f2acc drho;
 #pragma unroll

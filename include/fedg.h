@@ -250,8 +250,9 @@ int fedg_trc_update(fedg_ctx* ctx, double* QTRC, const double* const mflx[3], co
 int fedg_update_set_tracer_flux(fedg_ctx* ctx, double* const mflx[3], double* alph_M, double* alph_P,
                                 double* DDENS_TRC, double* DDENS0_TRC);
 
-/* The sponge layer inside fedg_update (FEDG_PREC_FP64): after every stage's explicit tendency,
- * fedg_sponge_add_tend on MOMX/MOMY/MOMZ_dt (SPONGELAYER_FLAG, driver_nonhydro3d.F90:831-841).
+/* The sponge layer inside fedg_update (every prec): after every stage's explicit tendency, the
+ * damping of fedg_sponge_add_tend on MOMX/MOMY/MOMZ_dt (SPONGELAYER_FLAG, driver_nonhydro3d.F90:
+ * 831-841); the FP32 and float-pair paths apply it inside their fused stage kernels.
  * tau <= 0 turns it off (the default). */
 int fedg_update_set_sponge(fedg_ctx* ctx, double tau, double height, int hveldamp);
 

@@ -92,6 +92,36 @@ def test_update_with_sponge(hevi):
     assert np.max(np.abs(ref0[3] - ref[3])) > 1e-6 * max(1.0, np.max(np.abs(ref[3])))
 
 
+@pytest.mark.parametrize("eqs,prec,bar", [("HEVI", "pair", 1e-9), ("HEVE", "pair", 1e-9), ("HEVI", "mixed", 1e-6)])
+def test_update_with_sponge_fast_paths(eqs, prec, bar):
+    """The float-pair and FP32 update paths with the sponge layer (applied inside their stage
+    kernels) against the oracle's converged steps with the same sponge; full fields, momentum
+    against at least 1 m/s of hydrostatic momentum"""
+    hevi = eqs == "HEVI"
+    case = cases.C2().scaled(2, 2, 4) if hevi else cases.C1().scaled(3, 3, 4)
+    dt = 0.04 if hevi else 0.02
+    o, ctx, _, b = setup(case, seed=22)
+    q, _ = cases.initial_state(case)  # unperturbed: the FP32 mode's bar is for smooth states
+    ztop = case.dom[5]
+    o.set_sponge(50 * dt, 0.5 * ztop, True)
+    ctx.set_sponge(50 * dt, 0.5 * ztop, True)
+    p = fl.PREC_PAIR if prec == "pair" else fl.PREC_MIXED
+    qd = [ctx.tensor(a) for a in q]
+    if hevi:
+        ref, rfail, _ = o.step_hevi(q, dt, 3, max_iter=30, tol=1e-13)
+        nf, _ = ctx.update(qd, 3, eqs=fl.HEVI, prec=p, dt=dt, max_iter=30, tol=1e-13 if prec == "pair" else 1e-10)
+        assert rfail == 0 and nf == 0
+    else:
+        ref = o.step_heve(q, dt, 3)
+        ctx.update(qd, 3, eqs=fl.HEVE, prec=p, dt=dt)
+    o.set_sponge(0.0)
+    ctx.set_sponge(0.0)
+    dn = np.linalg.norm(b["dens_hyd"])
+    hyd = [b["dens_hyd"], 0.0, 0.0, 0.0, b["therm_hyd"]]
+    errs = [float(np.linalg.norm(g.cpu().numpy() - r) / max(np.linalg.norm(r + h), dn)) for g, r, h in zip(qd, ref, hyd)]
+    assert max(errs) < bar, dict(zip(VARS, errs))
+
+
 @pytest.mark.parametrize("porder,ne", [(3, (4, 3, 4)), (7, (2, 2, 3)), (2, (3, 4, 3))])
 @pytest.mark.parametrize("nlap", [1, 2, 3])
 def test_numdiff_apply_pair(porder, ne, nlap):
