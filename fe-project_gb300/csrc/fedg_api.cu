@@ -624,8 +624,6 @@ int fedg_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_o
   if (o->eqs != FEDG_HEVE && o->eqs != FEDG_HEVI) return fail("fedg_update: bad eqs");
   CK(cudaSetDevice(c->d.device));
   if (o->prec == FEDG_PREC_MIXED || o->prec == FEDG_PREC_PAIR) {
-    if (c->trc_flux[0])
-      return fail("fedg_update: tracer flux outputs (fedg_update_set_tracer_flux) need prec FEDG_PREC_FP64");
     return mixed_update(c, q, nsteps, o, iters_out);
   }
   if (o->prec != FEDG_PREC_FP64) return fail("fedg_update: bad prec");

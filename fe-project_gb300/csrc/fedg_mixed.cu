@@ -43,6 +43,7 @@ struct StageBufs {
   __nv_bfloat16* X;     // stages 1, 2: feature rows of the column-guess network (NULL: none)
   int xdinp;            // row length of X
   float xs[3];          // feature scales of DDENS', MOMZ, DRHOT'
+  double* dtrc;         // stage 3: DDENS before the modal filter (DDENS_TRC of the tracer flux; NULL: none)
 };
 
 // PRES - PRES_hyd = PRES_hyd ((1 + DRHOT/THERM_hyd)^kappa - 1)   (nonhydro3d_common.F90:470-474)
@@ -327,6 +328,7 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
       dev[v] = f2_to_f(f2_sub(qnew[v], ref));
     }
   }
+  if (B.dtrc && valid) B.dtrc[g] = (double)qnew[VD].h + (double)qnew[VD].l;  // DDENS_TRC: before the filter
   if (!filter_on) {
     if (valid) {
 #pragma unroll
@@ -730,8 +732,13 @@ static int pair_update_heve(fedg_ctx* c, double* const q[5], int nsteps, const f
   });
   if (r) return api_cuda_fail((cudaError_t)r, "fedg_update(pair, HEVE): deviation copy");
   const int filt = c->d.mf_on;
+  double* const* tf = c->trc_flux;  // registered tracer-flux outputs (fedg_update_set_tracer_flux)
+  BP.dtrc = tf[0] ? tf[5] : nullptr;
+  static const double b_ssp3[3] = {1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0};
   // stage inputs and outputs: q^n deviation (QNFp) -> q1 (qi) -> q2 (QSFp) -> q^{n+1} (q, QNFp)
   for (int step = 0; step < nsteps; ++step) {
+    if (tf[0] && cudaMemcpyAsync(tf[6], q[0], sizeof(double) * c->n, cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess)
+      return api_fail("fedg_update(pair, HEVE): DDENS0_TRC copy");
     for (int s = 1; s <= 3; ++s) {
       for (int v = 0; v < 5; ++v) {
         BP.qs[v] = s == 1 ? m->QNFp(v) : (s == 2 ? m->qi(v) : m->QSFp(v));
@@ -741,6 +748,10 @@ static int pair_update_heve(fedg_ctx* c, double* const q[5], int nsteps, const f
         return launch_stage_pair_heve(c->N1, s, m->opp, pfp, c->d_prof, BP, pc, c->Ne, filt, c->stream);
       });
       if (r) return api_cuda_fail((cudaError_t)r, "fedg_update(pair, HEVE): stage");
+      if (tf[0]) {  // save_massflux of the stage state (driver_nonhydro3d.F90:900-917)
+        r = save_massflux_dev(c, s, BP.qs, nullptr, m->Uref, m->Vref, b_ssp3[s - 1], b_ssp3[s - 1], 0);
+        if (r) return api_cuda_fail((cudaError_t)r, "fedg_update(pair, HEVE): save_massflux");
+      }
     }
   }
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) return api_fail("fedg_update(pair, HEVE): synchronize");
@@ -857,20 +868,30 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
                             c->stream);
     });
   };
+  double* const* tf = c->trc_flux;  // registered tracer-flux outputs (fedg_update_set_tracer_flux)
+  B.dtrc = BP.dtrc = tf[0] ? tf[5] : nullptr;
+  const double bw[3] = {cf.b1, cf.b2, cf.b3};  // ARK232 b (explicit = implicit)
+  auto save = [&](int s) -> int {  // save_massflux of the stage state (driver_nonhydro3d.F90:900-917)
+    if (!tf[0]) return 0;
+    return save_massflux_dev(c, s, pair ? BP.qs : nullptr, pair ? nullptr : B.qsf, m->Uref, m->Vref, bw[s - 1],
+                             bw[s - 1], 1);
+  };
   for (int step = 0; step < nsteps; ++step) {
+    if (tf[0] && cudaMemcpyAsync(tf[6], q[0], sizeof(double) * c->n, cudaMemcpyDeviceToDevice, c->stream) != cudaSuccess)
+      return api_fail("fedg_update(mixed): DDENS0_TRC copy");
     for (int v = 0; v < 5; ++v) {
       B.qsf[v] = m->QNF(v);
       BP.qs[v] = pair ? m->QNFp(v) : nullptr;
     }
-    if ((r = stage(1))) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): stage 1");
+    if ((r = stage(1)) || (r = save(1))) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): stage 1");
     if ((r = vi())) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): column solve 2");
     for (int v = 0; v < 5; ++v) {
       B.qsf[v] = m->QSF(v);
       BP.qs[v] = pair ? m->QSFp(v) : nullptr;
     }
-    if ((r = stage(2))) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): stage 2");
+    if ((r = stage(2)) || (r = save(2))) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): stage 2");
     if ((r = vi())) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): column solve 3");
-    if ((r = stage(3))) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): stage 3");
+    if ((r = stage(3)) || (r = save(3))) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): stage 3");
   }
   if (cudaMemcpyAsync(c->h_cnt, c->d_cnt, sizeof(unsigned long long) * 3, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
       cudaStreamSynchronize(c->stream) != cudaSuccess)

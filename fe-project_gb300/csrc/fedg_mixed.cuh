@@ -95,6 +95,7 @@ struct StagePairBufs {
   __nv_bfloat16* X;     // stages 1, 2: feature rows of the column-guess network (NULL: none)
   int xdinp;
   float xs[3];
+  double* dtrc;         // stage 3: DDENS before the modal filter (DDENS_TRC of the tracer flux; NULL: none)
 };
 int launch_stage_pair_heve(int N1, int stage, const OpsP& op, const ProfP& pf, const double* dens64,
                            const StagePairBufs& B, const PairCoef& cf, int Ne, int filt, cudaStream_t s);

@@ -349,6 +349,7 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
       }
       return;
     }
+    if (B.dtrc && valid) B.dtrc[g] = (double)dev[VD].h + (double)dev[VD].l;  // DDENS_TRC: before the filter
     if (!filter_on) {
       if (valid) {
 #pragma unroll
@@ -415,6 +416,7 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
       dev[v] = qnew[v] - ref[v];
     }
   }
+  if (B.dtrc && valid) B.dtrc[g] = (double)qnew[VD].h + (double)qnew[VD].l;  // DDENS_TRC: before the filter
   if (!filter_on) {
     if (valid) {
 #pragma unroll

@@ -217,7 +217,7 @@ template <int N1, int EPB>
 __global__ void __launch_bounds__(EPB* N1* N1* N1)
     k_trc_stage(const Ops op, const double* __restrict__ dens_prof, const TrcIn in, const TrcStage st,
                 const TrcFilt tf, int Ne) {
-  constexpr int Np = N1 * N1 * N1, NF = N1 * N1, N = N1 - 1;
+  constexpr int Np = N1 * N1 * N1, NF = N1 * N1;
   extern __shared__ double sm[];
   double* s_fl = sm;                       // [EPB][3][Np] volume fluxes MFLX_d q
   double* s_nf = s_fl + EPB * 3 * Np;      // [EPB][6NF] numflux
@@ -399,8 +399,40 @@ __global__ void k_trc_alph_adv(const Ops op, const double* __restrict__ dens_pro
   aP[t] = alpha * densP;
 }
 
+// Stage state of save_massflux in the three representations the update paths hold it in:
+// FP64 fields (FElib's), float-pair deviations and FP32 deviations (from the hydrostatic state and
+// the reference-wind momentum DENS_hyd (Uref, Vref) of MOMX/MOMY).  get() returns the FP64 value.
+struct StF64 {
+  const double* q[5];
+  __device__ double get(int v, size_t g, int) const { return __ldg(q[v] + g); }
+};
+struct StPair {
+  const float2* q[5];
+  const double* dens;  // DENS_hyd per level
+  double U, V;
+  __device__ double get(int v, size_t g, int lev) const {
+    const float2 x = __ldg(q[v] + g);
+    double d = (double)x.x + (double)x.y;
+    if (v == VMX) d = fma(__ldg(dens + lev), U, d);
+    if (v == VMY) d = fma(__ldg(dens + lev), V, d);
+    return d;
+  }
+};
+struct StF32 {
+  const float* q[5];
+  const double* dens;
+  double U, V;
+  __device__ double get(int v, size_t g, int lev) const {
+    double d = (double)__ldg(q[v] + g);
+    if (v == VMX) d = fma(__ldg(dens + lev), U, d);
+    if (v == VMY) d = fma(__ldg(dens + lev), V, d);
+    return d;
+  }
+};
+
+template <class S>
 struct MflxArgs {
-  const double* q[5];   // DDENS, MOMX, MOMY, MOMZ, DRHOT
+  S q;                  // DDENS, MOMX, MOMY, MOMZ, DRHOT of the stage
   const double* dpres;  // DPRES or NULL (formed from DRHOT)
   double* mf[3];
   double* aM;
@@ -409,30 +441,49 @@ struct MflxArgs {
   int first, hevi;
 };
 
-__device__ __forceinline__ double dpres_of(const Ops& op, const Prof& pf, const MflxArgs& A, size_t g, int lev) {
+template <class S>
+__device__ __forceinline__ double dpres_of(const Ops& op, const Prof& pf, const MflxArgs<S>& A, size_t g, int lev) {
   if (A.dpres) return __ldg(A.dpres + g);
-  const double rhot = __ldg(pf.therm + lev) + __ldg(A.q[VRT] + g);
+  const double rhot = __ldg(pf.therm + lev) + A.q.get(VRT, g, lev);
   return op.pres00 * pow(op.rdry / op.pres00 * rhot, op.kap) - __ldg(pf.pres + lev);
 }
 
-// save_massflux: stage-weighted mass flux (one thread per node)
-__global__ void k_trc_mflx(const MflxArgs A, size_t n) {
+// normal momentum component (axis-aligned faces); flip_z: the exterior side of a slip lid
+template <class S>
+__device__ __forceinline__ double normal_mom(const S& q, int f, size_t g, int lev, bool flip_z = false) {
+  switch (f) {
+    case 0: return -q.get(VMY, g, lev);
+    case 1: return q.get(VMX, g, lev);
+    case 2: return q.get(VMY, g, lev);
+    case 3: return -q.get(VMX, g, lev);
+    case 4: return flip_z ? q.get(VMZ, g, lev) : -q.get(VMZ, g, lev);
+    default: return flip_z ? -q.get(VMZ, g, lev) : q.get(VMZ, g, lev);
+  }
+}
+
+// save_massflux (driver_nonhydro3d.F90:900-917): MFLX += w MOM of the stage
+template <class S>
+__global__ void k_trc_mflx(const MflxArgs<S> A, int Np, int N1, size_t nxy, size_t n) {
   const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= n) return;
+  const size_t ke = g / Np;
+  const int lev = (int)(ke / nxy) * N1 + (int)(g - ke * Np) / (N1 * N1);
+  const double mx = A.w_h * A.q.get(VMX, g, lev), my = A.w_h * A.q.get(VMY, g, lev);
+  const double mz = A.w_v * A.q.get(VMZ, g, lev);
   if (A.first) {
-    A.mf[0][g] = A.w_h * A.q[VMX][g];
-    A.mf[1][g] = A.w_h * A.q[VMY][g];
-    A.mf[2][g] = A.w_v * A.q[VMZ][g];
+    A.mf[0][g] = mx;
+    A.mf[1][g] = my;
+    A.mf[2][g] = mz;
   } else {
-    A.mf[0][g] += A.w_h * A.q[VMX][g];
-    A.mf[1][g] += A.w_h * A.q[VMY][g];
-    A.mf[2][g] += A.w_v * A.q[VMZ][g];
+    A.mf[0][g] += mx;
+    A.mf[1][g] += my;
+    A.mf[2][g] += mz;
   }
 }
 
 // cal_alphdens_dyn (trcadvect3d_heve.F90:460-551): one thread per face node
-template <int N1>
-__global__ void k_trc_alph_dyn(const Ops op, const Prof pf, const MflxArgs A, long Ne) {
+template <int N1, class S>
+__global__ void k_trc_alph_dyn(const Ops op, const Prof pf, const MflxArgs<S> A, long Ne) {
   constexpr int Np = N1 * N1 * N1, NF = N1 * N1;
   const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (size_t)Ne * 6 * NF) return;
@@ -447,11 +498,11 @@ __global__ void k_trc_alph_dyn(const Ops op, const Prof pf, const MflxArgs A, lo
   const size_t gM = (size_t)ke * Np + pM;
   const int levM = ez * N1 + pM / NF;
   const int levP = (kn >= 0 ? (int)(kn / nxy) : ez) * N1 + (int)((gP % Np) / NF);
-  const double densM = __ldg(A.q[VD] + gM) + __ldg(pf.dens + levM);
-  const double densP = __ldg(A.q[VD] + gP) + __ldg(pf.dens + levP);
+  const double densM = A.q.get(VD, gM, levM) + __ldg(pf.dens + levM);
+  const double densP = A.q.get(VD, gP, levP) + __ldg(pf.dens + levP);
   const double gnn = (f < 4 || !A.hevi) ? 1.0 : 0.0;  // |nx| + |ny| (+ |nz| for HEVE) on axis-aligned faces
-  const double velM = normal_comp(f, A.q[VMX], A.q[VMY], A.q[VMZ], gM) / densM;
-  const double velP = normal_comp(f, A.q[VMX], A.q[VMY], A.q[VMZ], gP, kn < 0) / densP;
+  const double velM = normal_mom(A.q, f, gM, levM) / densM;
+  const double velP = normal_mom(A.q, f, gP, levP, kn < 0) / densP;
   const double gamm = op.kap;
   const double alpha = fmax(sqrt(gnn * gamm * (__ldg(pf.pres + levM) + dpres_of(op, pf, A, gM, levM)) / densM) + fabs(velM),
                             sqrt(gnn * gamm * (__ldg(pf.pres + levP) + dpres_of(op, pf, A, gP, levP)) / densP) + fabs(velP));
@@ -514,10 +565,10 @@ int launch_alph_adv_n(const Ops& op, const double* dp, const double* dd, const d
   k_trc_alph_adv<N1><<<(unsigned)((nt + 255) / 256), 256, 0, s>>>(op, dp, dd, mx, my, mz, aM, aP, Ne);
   return (int)cudaGetLastError();
 }
-template <int N1>
-int launch_alph_dyn_n(const Ops& op, const Prof& pf, const MflxArgs& A, int Ne, cudaStream_t s) {
+template <int N1, class S>
+int launch_alph_dyn_n(const Ops& op, const Prof& pf, const MflxArgs<S>& A, int Ne, cudaStream_t s) {
   const size_t nt = (size_t)Ne * 6 * N1 * N1;
-  k_trc_alph_dyn<N1><<<(unsigned)((nt + 255) / 256), 256, 0, s>>>(op, pf, A, Ne);
+  k_trc_alph_dyn<N1, S><<<(unsigned)((nt + 255) / 256), 256, 0, s>>>(op, pf, A, Ne);
   return (int)cudaGetLastError();
 }
 
@@ -548,8 +599,20 @@ int launch_alph_adv(const Ops& op, const double* dp, const double* dd, const dou
                     const double* mz, double* aM, double* aP, int Ne, cudaStream_t s) {
   FEDG_TRC_DISPATCH(op.N1, launch_alph_adv_n<NN>(op, dp, dd, mx, my, mz, aM, aP, Ne, s))
 }
-int launch_alph_dyn(const Ops& op, const Prof& pf, const MflxArgs& A, int Ne, cudaStream_t s) {
-  FEDG_TRC_DISPATCH(op.N1, launch_alph_dyn_n<NN>(op, pf, A, Ne, s))
+template <class S>
+int launch_alph_dyn(const Ops& op, const Prof& pf, const MflxArgs<S>& A, int Ne, cudaStream_t s) {
+  FEDG_TRC_DISPATCH(op.N1, (launch_alph_dyn_n<NN, S>(op, pf, A, Ne, s)))
+}
+
+// both save_massflux kernels of one stage
+template <class S>
+int save_massflux_launch(fedg_ctx* c, const MflxArgs<S>& A) {
+  int r = tracked(c, FEDG_K_TRC_AUX, [&] {
+    k_trc_mflx<S><<<(unsigned)((c->n + 255) / 256), 256, 0, c->stream>>>(A, c->Np, c->N1, c->nxy, c->n);
+    return (int)cudaGetLastError();
+  });
+  if (!r) r = tracked(c, FEDG_K_TRC_AUX, [&] { return launch_alph_dyn(c->op, c->prof(), A, c->Ne, c->stream); });
+  return r;
 }
 
 TrcFilt make_filter(const fedg_ctx* c, double etac_h, double alpha_h, int ord_h, double etac_v, double alpha_v,
@@ -567,6 +630,39 @@ int check_base(const fedg_ctx* c, const char* who) {
 }
 
 }  // namespace
+
+// save_massflux of a stage that the FP32 or float-pair update holds as deviations (qp: pairs, or
+// qf: FP32), into the tracer-flux outputs registered with fedg_update_set_tracer_flux
+int save_massflux_dev(fedg_ctx* c, int rkstage, const float2* const qp[5], const float* const qf[5], double U,
+                      double V, double w_h, double w_v, int is_hevi) {
+  double* const* tf = c->trc_flux;
+  auto fill = [&](auto& A) {
+    A.dpres = nullptr;
+    for (int d = 0; d < 3; ++d) A.mf[d] = tf[d];
+    A.aM = tf[3];
+    A.aP = tf[4];
+    A.w_h = w_h;
+    A.w_v = w_v;
+    A.first = rkstage == 1;
+    A.hevi = is_hevi != 0;
+  };
+  if (qp) {
+    MflxArgs<StPair> A;
+    for (int v = 0; v < 5; ++v) A.q.q[v] = qp[v];
+    A.q.dens = c->d_prof;
+    A.q.U = U;
+    A.q.V = V;
+    fill(A);
+    return save_massflux_launch(c, A);
+  }
+  MflxArgs<StF32> A;
+  for (int v = 0; v < 5; ++v) A.q.q[v] = qf[v];
+  A.q.dens = c->d_prof;
+  A.q.U = U;
+  A.q.V = V;
+  fill(A);
+  return save_massflux_launch(c, A);
+}
 }  // namespace fedg
 
 // ---------------------------------------------------------------------------------------
@@ -596,8 +692,8 @@ int fedg_trc_save_massflux(fedg_ctx* c, int rkstage, const double* const q[5], c
   if (rkstage < 1) return api_fail("fedg_trc_save_massflux: rkstage is 1-based");
   if (int r = check_base(c, "fedg_trc_save_massflux")) return r;
   cudaSetDevice(c->d.device);
-  MflxArgs A;
-  for (int v = 0; v < 5; ++v) A.q[v] = q[v];
+  MflxArgs<StF64> A;
+  for (int v = 0; v < 5; ++v) A.q.q[v] = q[v];
   A.dpres = DPRES;
   for (int d = 0; d < 3; ++d) A.mf[d] = mflx[d];
   A.aM = alph_M;
@@ -606,11 +702,7 @@ int fedg_trc_save_massflux(fedg_ctx* c, int rkstage, const double* const q[5], c
   A.w_v = w_v;
   A.first = rkstage == 1;
   A.hevi = is_hevi != 0;
-  int r = tracked(c, FEDG_K_TRC_AUX, [&] {
-    k_trc_mflx<<<(unsigned)((c->n + 255) / 256), 256, 0, c->stream>>>(A, c->n);
-    return (int)cudaGetLastError();
-  });
-  if (!r) r = tracked(c, FEDG_K_TRC_AUX, [&] { return launch_alph_dyn(c->op, c->prof(), A, c->Ne, c->stream); });
+  const int r = save_massflux_launch(c, A);
   return r ? api_cuda_fail((cudaError_t)r, "fedg_trc_save_massflux") : 0;
 }
 

@@ -240,13 +240,15 @@ int fedg_trc_update(fedg_ctx* ctx, double* QTRC, const double* const mflx[3], co
                     const double* alph_P, const double* DDENS_TRC, const double* DDENS0_TRC, const double* DDENS,
                     const double* RHOQ_tp, const fedg_trc_opts* opts);
 
-/* Tracer transport outputs of fedg_update (FEDG_PREC_FP64), the coupling of FElib's dynamics driver to
+/* Tracer transport outputs of fedg_update (every prec), the coupling of FElib's dynamics driver to
  * its tracer driver (driver_nonhydro3d.F90:900-935): during each step, after every stage's explicit
  * tendency, the stage-weighted mass flux and the dynamics' Rusanov coefficients are accumulated into
  * mflx/alph_M/alph_P (fedg_trc_save_massflux with the scheme's b weights); DDENS0_TRC receives DDENS at
  * the step's start and DDENS_TRC the DDENS before the modal filter.  After fedg_update they hold the
- * last step's values, ready for fedg_trc_update.  mflx == NULL clears the registration.  The caller
- * owns the arrays (FElib layout, device). */
+ * last step's values, ready for fedg_trc_update.  The FP32 and float-pair paths accumulate them from
+ * the stage states they hold as deviations, and their fused stage-3 kernel writes DDENS_TRC before
+ * its filter.  mflx == NULL clears the registration.  The caller owns the arrays (FElib layout,
+ * device). */
 int fedg_update_set_tracer_flux(fedg_ctx* ctx, double* const mflx[3], double* alph_M, double* alph_P,
                                 double* DDENS_TRC, double* DDENS0_TRC);
 

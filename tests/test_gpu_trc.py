@@ -296,3 +296,42 @@ def test_update_accumulates_tracer_flux(hevi):
         assert e < 1e-10, (nm, e)
     # the dynamics state itself is unchanged by the registration
     assert rel_max(np_(qd[3]), ref[3]) < 1e-9
+
+
+@pytest.mark.parametrize("eqs,prec,bar", [("HEVI", "pair", 1e-9), ("HEVE", "pair", 1e-9), ("HEVI", "mixed", 1e-6)])
+def test_update_tracer_flux_fast_paths(eqs, prec, bar):
+    """The float-pair (HEVI and HEVE) and FP32 updates with registered tracer-flux outputs: the
+    stage-weighted mass flux and Rusanov coefficients from the stage states they hold as deviations,
+    DDENS_TRC written by the fused stage-3 kernel before its modal filter, DDENS0_TRC; against the
+    oracle's converged steps with the same outputs.  Maximum error relative to the field's maximum,
+    with floors: the mass fluxes against at least 1 m/s of hydrostatic momentum (a component that
+    stays near zero, MFLX_y of a flow along x, is not measured against its own roundoff), the DDENS
+    fields against the hydrostatic density."""
+    hevi = eqs == "HEVI"
+    case = cases.C2().scaled(2, 2, 3) if hevi else cases.C1().scaled(3, 3, 3)
+    dt = 0.04 if hevi else 0.02
+    o, ctx, q, b, _ = setup(case)
+    outs_o = [np.zeros(o.shape) for _ in range(3)] + [np.zeros(o.face_shape) for _ in range(2)] + \
+             [np.zeros(o.shape) for _ in range(2)]
+    o.set_trc_flux(outs_o)
+    if hevi:
+        ref, rfail, _ = o.step_hevi(q, dt, 2, max_iter=30, tol=1e-13)
+        assert rfail == 0
+    else:
+        ref = o.step_heve(q, dt, 2)
+    o.set_trc_flux(None)
+    outs_g = [ctx.empty() for _ in range(3)] + [ctx.empty_face() for _ in range(2)] + [ctx.empty() for _ in range(2)]
+    ctx.set_tracer_flux(outs_g)
+    qd = [ctx.tensor(a) for a in q]
+    p = fl.PREC_PAIR if prec == "pair" else fl.PREC_MIXED
+    nf, _ = ctx.update(qd, 2, eqs=fl.HEVI if hevi else fl.HEVE, prec=p, dt=dt, max_iter=30,
+                       tol=1e-13 if prec == "pair" else 1e-10)
+    ctx.set_tracer_flux(None)
+    assert nf == 0
+    names = ["MFLX_x", "MFLX_y", "MFLX_z", "alph_M", "alph_P", "DDENS_TRC", "DDENS0_TRC"]
+    dmax = float(np.max(np.abs(b["dens_hyd"])))
+    for nm, g, r in zip(names, outs_g, outs_o):
+        g = np_(g)
+        floor = dmax if (nm.startswith("DDENS") or nm.startswith("MFLX")) else 0.0
+        e = float(np.max(np.abs(g - r))) / max(np.max(np.abs(r)), floor, 1e-300)
+        assert e < bar, (nm, e)
