@@ -38,24 +38,29 @@ namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
 
-// per-column shared-memory layout (bytes); the column stride is padded so that the C columns
-// of a warp start on different banks
+// per-column shared-memory layout (bytes).  Three scratch areas whose phases never overlap share
+// one region: the residual's ring of level quantities, the correction's Jacobian quantities and
+// block coupling, and the MOMX/MOMY phase's tridiagonal arrays.  The column stride is the
+// smallest one whose residue puts the C columns of a warp on different banks.
 struct ColLayout {
   int oP, oRing, oDel, oBf, oBc, oAl, oJb, oSJ, stride;
   __host__ __device__ ColLayout(int N1, int NeZ) {
     const int L = N1 * NeZ;
     int o = 0;
     oP = o;    o += 24 * L;                    // float2 P[3L] (uv phase: var0 pairs [2L])
-    oRing = o; o += 96 * N1;                   // 3 element slots x 4 quantities x N1 nodes x float2
-    oDel = o;  o += 48;                        // 6 face fluxes (float2) of the current element
     oBf = o;   o += 12 * L;                    // float b / y / x [3L] (uv phase: [2L])
-    oBc = o;   o += 64;                        // block-Thomas coupling from the element below
+    oDel = o;  o += 48;                        // 6 face fluxes (float2) of the current element
     oAl = o;   o += ((8 * NeZ + 15) / 16) * 16; // alB, alT per element
-    oJb = o;   o += ((12 * (NeZ + 1) + 15) / 16) * 16;  // uv: c' and the two interface jumps
-    oSJ = o;   o += 16 * (N1 + 2);             // float4: pot, wt, dpd of the element's nodes + 2 neighbours
+    const int u_ring = 96 * N1;                            // 3 element slots x 4 quantities x N1 x float2
+    const int u_solve = 16 * (N1 + 2) + 64;                // float4 pot, wt, dpd of the element's nodes
+                                                           // + 2 neighbours; coupling from below
+    const int u_jb = ((12 * (NeZ + 1) + 15) / 16) * 16;    // uv: c' and the two interface jumps
+    oRing = oSJ = oJb = o;
+    oBc = o + 16 * (N1 + 2);
+    o += u_ring > u_solve ? (u_ring > u_jb ? u_ring : u_jb) : (u_solve > u_jb ? u_solve : u_jb);
     const int words = o / 4;
-    const int C = 32 / N1;
-    stride = 4 * (((words + 31) / 32) * 32 + 32 / C);
+    const int C = 32 / N1, r = 32 / C, m = 2 * r;  // stride = r (mod 2r) words
+    stride = 4 * (((words - r + m - 1) / m) * m + r);
   }
 };
 
@@ -516,20 +521,22 @@ __device__ void col_solve(const Ops& op, const ProfX& px, float kapf, const Col<
 
 // ---------------------------------------------------------------------------------------------
 template <int N1, bool PO>
-__global__ void __launch_bounds__(32, 9) k_vi_cols(const Ops op, const OpsX ox, const ProfX px, const X5 qin, const F5c z,
+__global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, const ProfX px, const X5 qin, const F5c z,
                                                 const float* const* guess, void* const* qsf, void* const* tout,
                                                 float* __restrict__ gsc, int* status, unsigned long long* cnt,
                                                 const MixViArgs args, int ncol) {
   constexpr int N = N1 - 1, C = 32 / N1, NF = N1 * N1, Np = N1 * N1 * N1;
   extern __shared__ __align__(16) unsigned char smraw[];
-  const int lane = threadIdx.x & 31;
+  // two warps per block (C columns each): with the one-warp blocks the per-block shared-memory
+  // reservation cost a whole warp of occupancy per SM
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int grp = lane / N1, k = lane % N1;
-  const int col0 = blockIdx.x * C;
-  if (col0 >= ncol) return;  // ncol is a multiple of C: warps are all-valid or all-invalid
+  const int col0 = (blockIdx.x * 2 + wib) * C;
+  if (col0 >= ncol) return;  // ncol is a multiple of C: warps are all-valid or all-invalid (no block barriers)
   const int col = col0 + grp;
   const int NeZ = op.NeZ, L = op.L;
   const ColLayout lay(N1, NeZ);
-  unsigned char* base = smraw + (size_t)grp * lay.stride;
+  unsigned char* base = smraw + (size_t)(wib * C + grp) * lay.stride;
   Col<N1> c;
   c.P = reinterpret_cast<float2*>(base + lay.oP);
   c.sJ = reinterpret_cast<float4*>(base + lay.oSJ);
@@ -758,12 +765,12 @@ int launch_n(const Ops& op, const OpsX& ox, const ProfX& px, const X5& qin, cons
              const MixViArgs& a, cudaStream_t s) {
   constexpr int C = 32 / N1;
   const ColLayout lay(N1, op.NeZ);
-  const size_t smem = (size_t)lay.stride * C;
+  const size_t smem = (size_t)lay.stride * 2 * C;
   if (smem > 227 * 1024) return (int)cudaErrorInvalidValue;
   const int ncol = op.NeX * op.NeY * N1 * N1;
   auto kfn = k_vi_cols<N1, PO>;
   cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  kfn<<<(ncol + C - 1) / C, 32, smem, s>>>(op, ox, px, qin, z, guess, qsf, tout, gsc, status, cnt, a, ncol);
+  kfn<<<(ncol + 2 * C - 1) / (2 * C), 64, smem, s>>>(op, ox, px, qin, z, guess, qsf, tout, gsc, status, cnt, a, ncol);
   return (int)cudaGetLastError();
 }
 
