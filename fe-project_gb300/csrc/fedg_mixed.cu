@@ -1,20 +1,27 @@
-// fedg_mixed.cu -- the mixed-precision fused HEVI update (IMEX ARK232), the headline path.
+// fedg_mixed.cu -- the fused update paths of the two fast precision modes: FP32 explicit
+// arithmetic (FEDG_PREC_MIXED, k_stage_mixed here) and float pairs (FEDG_PREC_PAIR, k_stage_pair
+// in fedg_pair.cu), with the column Newton solve of fedg_vicol.cu.
 //
-// Per time step five launches, each stage's RK arithmetic fused into its kernel:
+// HEVI (IMEX ARK232), per time step five launches (plus the guess network's GEMMs), each stage's
+// RK arithmetic fused into its kernel:
 //   K1  stage-1 explicit tendency E(q^n) and implicit operator A(q^n) (impl_fac = 0),
-//       writes the stage-2 input q*_2 (FP64) and two FP32 tendency accumulators
-//   V2  column Newton solve of Q - q*_2 - impl_fac A(Q) = 0  -> Q_2 (FP64), t_im2 (FP32)
-//   K2  E(Q_2), writes q*_3 (FP64), updates the final accumulator
+//       writes the stage-2 input q*_2 (float pairs) and two tendency accumulators
+//   V2  column Newton solve of Q - q*_2 - impl_fac A(Q) = 0  -> Q_2, t_im2
+//   K2  E(Q_2), writes q*_3, updates the final accumulator
 //   V3  column Newton solve for stage 3 -> Q_3, t_im3
-//   K3  E(Q_3), q^{n+1} = q^n + dt*(accumulator + b3 (t_ex3 + t_im3)) in FP64, then the modal
-//       filter of the element, written in place over q^n
+//   K3  E(Q_3), q^{n+1} = q^n + dt*(accumulator + b3 (t_ex3 + t_im3)), then the modal filter of
+//       the element, written in FP64 in place over q^n
 // (FElib: driver_nonhydro3d.F90:727-951, timeint_rk.F90:2201-2565, butcher_tab.F90:260-274.)
+// HEVE (ERK_SSP_3s3o) in float pairs: three launches of k_stage_pair<HEVE> per step
+// (pair_update_heve).  Both paths apply the registered sponge layer inside the stage kernels and
+// accumulate the registered tracer mass flux from their stage states (save_massflux_dev).
 //
-// Precision: explicit volume/face arithmetic in FP32 on deviations from the hydrostatic state
-// (the pressure deviation is formed as PRES_hyd*((1 + DRHOT/THERM_hyd)^kappa - 1), never as a
-// difference of totals); FP64 for the prognostic state, every RK accumulation, the Newton
-// residual (DENS/MOMZ/RHOT and MOMX/MOMY) and the Newton update; the Jacobian and its LU in
-// FP32 (the FP64 residual judges convergence, so the converged state is FP64-accurate).
+// Precision: the explicit volume/face arithmetic on deviations from the hydrostatic state and a
+// reference wind (the pressure deviation is formed as PRES_hyd*((1 + DRHOT/THERM_hyd)^kappa - 1),
+// never as a difference of totals), in FP32 or in float pairs; FP64-class float pairs for every RK
+// accumulation, the Newton iterate and its certifying residual; the Jacobian and its LU in FP32
+// (the pair residual judges convergence, so the converged state is FP64-class); the prognostic
+// state stays FP64.
 #include <cmath>
 #include <cstring>
 #include <vector>

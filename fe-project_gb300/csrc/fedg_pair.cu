@@ -19,7 +19,11 @@
 // scale_atm_dyn_dgm_nonhydro3d_rhot_hevi.F90:289-482), the HEVI numerical flux
 // (scale_atm_dyn_dgm_nonhydro3d_rhot_hevi_numflux.F90:232-418), the implicit operator at var0
 // (scale_atm_dyn_dgm_nonhydro3d_hevi_common_2.F90:1016-1328), timeint_rk (FElib/src/common/
-// scale_timeint_rk.F90:2201-2565) and the modal filter (scale_atm_dyn_dgm_modalfilter.F90:49-130).
+// scale_timeint_rk.F90:2201-2565) and the modal filter (scale_atm_dyn_dgm_modalfilter.F90:49-130);
+// with HEVE = true, cal_tend for HEVE (…_rhot_heve.F90:292-489), its numerical flux
+// (…_rhot_heve_numflux.F90:946-1139) and the SSP-RK3 stages (scale_timeint_rk.F90:1182-1278).
+// The sponge layer (…_dgm_spongelayer.F90:134-219) is added to the explicit tendency when a
+// profile is given.
 #include "fedg_ctx.cuh"
 #include "fedg_f2.cuh"
 #include "fedg_mixed.cuh"
