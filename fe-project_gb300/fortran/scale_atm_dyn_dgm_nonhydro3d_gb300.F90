@@ -32,8 +32,17 @@ module scale_atm_dyn_dgm_nonhydro3d_gb300
   public :: atm_dyn_dgm_nonhydro3d_gb300_numdiff_apply
   public :: atm_dyn_dgm_nonhydro3d_gb300_sponge_init
   public :: atm_dyn_dgm_nonhydro3d_gb300_sponge_add_tend
+  public :: atm_dyn_dgm_nonhydro3d_gb300_set_base_state
+  public :: atm_dyn_dgm_nonhydro3d_gb300_load_guess
+  public :: atm_dyn_dgm_nonhydro3d_gb300_update
 
   integer(c_int), parameter :: FEDG_HEVE = 0, FEDG_HEVI = 1
+  integer(c_int), parameter, public :: FEDG_PREC_FP64 = 0, FEDG_PREC_MIXED = 1, FEDG_PREC_PAIR = 2
+
+  type, bind(C) :: fedg_update_opts
+    integer(c_int) :: eqs, prec, max_iter, use_guess
+    real(c_double) :: dt, tol
+  end type
 
   type, bind(C) :: fedg_mesh_desc
     integer(c_int) :: porder, NeX, NeY, NeZ
@@ -92,9 +101,49 @@ module scale_atm_dyn_dgm_nonhydro3d_gb300
       real(c_double), value :: tau, height
       integer(c_int), value :: hveldamp
     end function
+    integer(c_int) function fedg_set_base_state(ctx, dens_hyd, pres_hyd, therm_hyd, rtot, cvtot, cptot, &
+        dphyddx, dphyddy, coriolis) bind(C, name="fedg_set_base_state")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx, dens_hyd, pres_hyd, therm_hyd, rtot, cvtot, cptot, dphyddx, dphyddy, coriolis
+    end function
+    integer(c_int) function fedg_update_set_sponge(ctx, tau, height, hveldamp) bind(C, name="fedg_update_set_sponge")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), value :: tau, height
+      integer(c_int), value :: hveldamp
+    end function
+    integer(c_int) function fedg_update(ctx, q, nsteps, opts, iters_out) bind(C, name="fedg_update")
+      import :: c_int, c_ptr, c_double, fedg_update_opts
+      type(c_ptr), value :: ctx
+      type(c_ptr), intent(in) :: q(5)
+      integer(c_int), value :: nsteps
+      type(fedg_update_opts), intent(in) :: opts
+      real(c_double), intent(out) :: iters_out
+    end function
+    integer(c_int) function fedg_guess_create(levels, hidden, g) bind(C, name="fedg_guess_create")
+      import :: c_int, c_ptr
+      integer(c_int), value :: levels, hidden
+      type(c_ptr), intent(out) :: g
+    end function
+    integer(c_int) function fedg_guess_set_scales(g, in_scale, out_scale) bind(C, name="fedg_guess_set_scales")
+      import :: c_int, c_ptr, c_float
+      type(c_ptr), value :: g
+      real(c_float), intent(in) :: in_scale(4), out_scale(3)
+    end function
+    integer(c_int) function fedg_guess_set_params(g, host, n) bind(C, name="fedg_guess_set_params")
+      import :: c_int, c_ptr, c_float, c_long_long
+      type(c_ptr), value :: g
+      real(c_float), intent(in) :: host(*)
+      integer(c_long_long), value :: n
+    end function
+    integer(c_int) function fedg_guess_load(ctx, g) bind(C, name="fedg_guess_load")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx, g
+    end function
   end interface
 
   type(c_ptr), save :: ctx = c_null_ptr
+  type(c_ptr), save :: guess = c_null_ptr    ! column-guess network (atm_dyn_dgm_nonhydro3d_gb300_load_guess)
   real(RP), save :: sl_tau = -1.0_RP, sl_height = -1.0_RP
   logical, save :: sl_hvel = .false.
   integer, save :: vi_max_iter = 1           ! 1: FElib's single linearised solve
@@ -131,6 +180,65 @@ contains
     if (c_associated(ctx)) call fedg_ctx_destroy(ctx)
     ctx = c_null_ptr
   end subroutine atm_dyn_dgm_nonhydro3d_gb300_Final
+
+  !> Register the base state for the whole-step update (AUX_VARS DENS_hyd, PRES_hyd, THERM_hyd and
+  !! AUX_VARS2D CORIOLIS; the dry constants Rtot/CVtot/CPtot and DPhydDx/y = 0 are implied).
+  subroutine atm_dyn_dgm_nonhydro3d_gb300_set_base_state( DENS_hyd, PRES_hyd, THERM_hyd, CORIOLIS )
+    real(RP), intent(in), target :: DENS_hyd(:,:), PRES_hyd(:,:), THERM_hyd(:,:), CORIOLIS(:,:)
+    integer(c_int) :: ierr
+    !$acc host_data use_device(DENS_hyd, PRES_hyd, THERM_hyd, CORIOLIS)
+    ierr = fedg_set_base_state(ctx, c_loc(DENS_hyd), c_loc(PRES_hyd), c_loc(THERM_hyd), c_null_ptr, c_null_ptr, &
+                               c_null_ptr, c_null_ptr, c_null_ptr, c_loc(CORIOLIS))
+    !$acc end host_data
+    if (ierr < 0) call PRC_abort
+  end subroutine atm_dyn_dgm_nonhydro3d_gb300_set_base_state
+
+  !> Attach the column-guess network for update(use_guess = .true.): a (3L+1) -> hidden -> hidden -> 3L
+  !! GELU MLP (L = NeZ*(porder+1)) with its parameters in the library's logical order, as written by
+  !! the training (fe-project_gb300/fedg/guess.py).
+  subroutine atm_dyn_dgm_nonhydro3d_gb300_load_guess( levels, hidden, in_scale, out_scale, params )
+    integer, intent(in) :: levels, hidden
+    real(c_float), intent(in) :: in_scale(4), out_scale(3), params(:)
+    integer(c_int) :: ierr
+    if (.not. c_associated(guess)) then
+      ierr = fedg_guess_create(levels, hidden, guess)
+      if (ierr < 0) call PRC_abort
+    end if
+    if (fedg_guess_set_scales(guess, in_scale, out_scale) < 0) call PRC_abort
+    if (fedg_guess_set_params(guess, params, int(size(params), c_long_long)) < 0) call PRC_abort
+    if (fedg_guess_load(ctx, guess) < 0) call PRC_abort
+  end subroutine atm_dyn_dgm_nonhydro3d_gb300_load_guess
+
+  !> nsteps whole time steps of AtmDynDGMDriver_nonhydro3d_update's stage loop
+  !! (driver_nonhydro3d.F90:614-963) for the dry dynamics: HEVE (SSP-RK3) or HEVI (IMEX ARK232) with
+  !! the modal filter, the sponge layer when sponge_init set one, in FElib's FP64 arithmetic
+  !! (FEDG_PREC_FP64), or fused in float pairs (FEDG_PREC_PAIR, HEVI with tol ~1e-13) or FP32
+  !! (FEDG_PREC_MIXED, HEVI).  nfail returns the number of columns whose Newton solve did not converge.
+  subroutine atm_dyn_dgm_nonhydro3d_gb300_update( DDENS, MOMX, MOMY, MOMZ, DRHOT, nsteps, hevi, prec, dt, &
+      use_guess, nfail, mean_solves )
+    real(RP), intent(inout), target :: DDENS(:,:), MOMX(:,:), MOMY(:,:), MOMZ(:,:), DRHOT(:,:)
+    integer, intent(in) :: nsteps, prec
+    logical, intent(in) :: hevi, use_guess
+    real(RP), intent(in) :: dt
+    integer, intent(out) :: nfail
+    real(RP), intent(out), optional :: mean_solves
+    type(c_ptr) :: q(5)
+    type(fedg_update_opts) :: o
+    real(c_double) :: its
+    integer(c_int) :: ierr
+    o = fedg_update_opts(merge(FEDG_HEVI, FEDG_HEVE, hevi), prec, vi_max_iter, merge(1, 0, use_guess), dt, vi_tol)
+    if (sl_tau > 0.0_RP) then
+      ierr = fedg_update_set_sponge(ctx, sl_tau, sl_height, merge(1, 0, sl_hvel))
+      if (ierr < 0) call PRC_abort
+    end if
+    !$acc host_data use_device(DDENS, MOMX, MOMY, MOMZ, DRHOT)
+    q = [c_loc(DDENS), c_loc(MOMX), c_loc(MOMY), c_loc(MOMZ), c_loc(DRHOT)]
+    ierr = fedg_update(ctx, q, int(nsteps, c_int), o, its)
+    !$acc end host_data
+    if (ierr < 0) call PRC_abort
+    nfail = ierr
+    if (present(mean_solves)) mean_solves = its
+  end subroutine atm_dyn_dgm_nonhydro3d_gb300_update
 
   !> atm_dyn_nonhydro3d_cal_tend_ex for EQS_TYPE = "NONHYDRO3D_HEVE_GB300"
   subroutine atm_dyn_dgm_nonhydro3d_gb300_cal_tend_heve( &
