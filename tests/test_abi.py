@@ -55,3 +55,23 @@ def test_error_text_without_gpu():
     d.periodic_y = 1
     assert lib.fedg_ctx_create(ctypes.byref(d), ctypes.byref(h)) < 0
     assert b"periodic" in lib.fedg_last_error()
+
+
+def test_fortran_shims_bind_declared_symbols():
+    """Every bind(C, name=...) of the Fortran shims (not compiled in this image) names a function
+    that include/fedg.h declares, and the bind(C) mirrors of the option structs list the C fields
+    in the C order."""
+    names = set(declared())
+    fdir = os.path.join(ROOT, "fe-project_gb300", "fortran")
+    bound = []
+    for fn in sorted(os.listdir(fdir)):
+        if fn.endswith(".F90"):
+            bound += re.findall(r'bind\(C,\s*name="([A-Za-z0-9_]+)"\)', open(os.path.join(fdir, fn)).read())
+    assert bound
+    assert sorted(set(bound) - names) == []
+    src = open(os.path.join(fdir, "scale_atm_dyn_dgm_nonhydro3d_gb300.F90")).read()
+    hdr = open(HDR).read()
+    m = re.search(r"typedef struct \{\s*int eqs, prec, max_iter, use_guess;\s*double dt, tol;\s*\} fedg_update_opts;", hdr)
+    assert m, "fedg_update_opts layout changed: update the Fortran mirror"
+    assert re.search(r"type, bind\(C\) :: fedg_update_opts\s*integer\(c_int\) :: eqs, prec, max_iter, use_guess\s*"
+                     r"real\(c_double\) :: dt, tol\s*end type", src)
