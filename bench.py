@@ -4,7 +4,7 @@
 Workload (default): p=7, 128x128x16 elements over 12.8 x 12.8 x 3.2 km, periodic in x/y,
 slip lids, constant Brunt-Vaisala base state (N = 0.01 1/s, theta_sfc = 300 K), i.i.d.
 +-0.1 K potential-temperature noise below 500 m (seed 0), u = 5 m/s, HEVI with IMEX
-ARK(2,3,2) and the column Newton solve to tol 1e-10.  134,217,728 nodes x 5 variables.
+ARK(2,3,2) and the column Newton solve (tol per path, below).  134,217,728 nodes x 5 variables.
 
 A "step" is one full time step (3 RK stages) of the whole domain; the metric is
 DOF-stage updates per second = 5 * Np * Ne * 3 * steps / time.
@@ -16,7 +16,8 @@ Paths (--path):
   mixed  the learned guess with FP32 explicit arithmetic (FEDG_PREC_MIXED), Newton tol 1e-10;
   fp64   FElib's algorithm in FP64 on the GPU, Newton tol 1e-10.
 The default run also times learned+FP32, the headline path without the guess and the plain
-FP64 path on the same state, and reports the error of each against plain FP64.
+FP64 path on the same state, and reports the error of each against plain FP64; then HEVE (FP64
+and float pairs), the tracer advection and the numerical diffusion / sponge on the same mesh.
 
   python bench.py [--steps K] [--warmup W] [--path pair|mixed|fp64] [--impl fedg|reference]
 
@@ -55,6 +56,28 @@ NCU_BYTES_PER_NODE = {
     "pair": {"vi_mixed": (895.11e6 + 1128.88e6) / (32 * 32 * 16 * 512)},
     "mixed": {"vi_mixed": (847.3e6 + 728.2e6) / (32 * 32 * 16 * 512)},
 }
+
+
+# warp instructions per node of one launch of the dominant kernel from ncu (smsp__inst_executed.sum
+# on the 32x32x16-element slice; profiles/pair_step_C5small_p7_32x32x16.md), per path
+NCU_INST_PER_NODE = {
+    "pair": {"vi_mixed": 2.104868361e9 / (32 * 32 * 16 * 512)},
+}
+
+
+def issue_roofline(kname, path, nodes, avg_ms, sm_mhz, n_sm):
+    """The dominant kernel against the SM issue rate, the ceiling of a latency-bound kernel: ncu's
+    warp instructions per node times the nodes of one launch over the CUDA-event launch time,
+    against 4 schedulers x SMs x the SM clock sampled during the timed region."""
+    ipn = NCU_INST_PER_NODE.get(path, {}).get(kname)
+    if ipn is None or not avg_ms or avg_ms <= 0:
+        return None
+    mhz = sm_mhz or 2070.0
+    achieved = ipn * nodes / (avg_ms * 1e-3)
+    peak = 4.0 * n_sm * mhz * 1e6
+    return {"bound": "issue", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "warp instructions/s",
+            "frac": achieved / peak, "inst_per_node": ipn, "sm_mhz": mhz, "sms": n_sm,
+            "source": "ncu smsp__inst_executed.sum on the 32x32x16 slice, scaled by nodes; peak = 4 x SMs x SM clock"}
 
 
 def _env_rank():
@@ -533,6 +556,8 @@ def run_fedg(args):
             "unit": "GB/s", "frac": achieved / peaks.get("hbm_gbs", 6800.0), "traffic": traffic,
             "traffic_unit": "GB per launch (ncu DRAM read+write of the same path on the 32x32x16 slice, scaled by nodes)",
             "peak_source": peak_src, "avg_launch_ms": avg_ms, "algorithmic_bytes_per_node": bytes_per_node.get(kname)}
+    n_sm = torch.cuda.get_device_properties(ctx.dev).multi_processor_count
+    roof_issue = issue_roofline(kname, path, nodes, avg_ms, (clocks or {}).get("sm_mhz"), n_sm)
     fp64_tf = fp64_dgemm_tflops(torch, ctx.dev) if rank == 0 else 0.0
     gpu_launches = sum(v[1] for v in prof.values())
 
@@ -651,6 +676,7 @@ def run_fedg(args):
                        "l2": "inputs larger than L2 (FP64 state %.1f GB)" % (case.dofs * 8 / 1e9),
                        "parallelism": "replicas" if world > 1 else "single"},
             "roofline": roof,
+            "roofline_issue": roof_issue,
             "roofline_fp64": {"bound": "fp64", "peak_tflops": fp64_tf, "peak_source": "measured cuBLAS DGEMM 4096^3"},
             "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items() if v[1]},
             "cpu_baseline": cb, "e2e": e2e, "gpu_launches": gpu_launches, "clocks": clocks,
