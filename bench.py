@@ -80,6 +80,24 @@ def issue_roofline(kname, path, nodes, avg_ms, sm_mhz, n_sm):
             "source": "ncu smsp__inst_executed.sum on the 32x32x16 slice, scaled by nodes; peak = 4 x SMs x SM clock"}
 
 
+def max_over_ranks(value, world, device):
+    """The largest of the ranks' values (the slowest replica's time); one rank: the value."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_rank, steps, ms_max, world):
+    """Whole-job throughput of N independent replicas: the units all ranks processed over the
+    slowest rank's time."""
+    return units_per_rank * steps * world / (ms_max * 1e-3)
+
+
 def _env_rank():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(
         os.environ.get("LOCAL_RANK", "0"))
@@ -519,12 +537,9 @@ def run_fedg(args):
     clocks = clk.stop()
     fl.prof_enable(ctx, False)
     prof = fl.prof_read(ctx)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, world, "cuda")
     dofs_stage = case.dofs * 3
-    value = dofs_stage * args.steps / (ms * 1e-3) * world
+    value = replica_throughput(dofs_stage, args.steps, ms, world)
 
     # dominant kernel and its roofline
     peaks, peak_src = measured_peaks()

@@ -26,3 +26,42 @@ def test_issue_roofline_arithmetic():
     assert b.issue_roofline("vi_mixed", "fp64", nodes, 10.0, 2070.0, 152) is None
     # no clock sample: the maximum SM clock
     assert b.issue_roofline("vi_mixed", "pair", nodes, 78.0, None, 152)["sm_mhz"] == 2070.0
+
+
+def _replica(rank, world, port, out):
+    import os as _os
+
+    import torch.distributed as dist
+
+    _os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    b = _bench()
+    ms = b.max_over_ranks(10.0 + 5.0 * rank, world, "cpu")  # rank 1 is the slower replica
+    out[rank] = (ms, b.replica_throughput(1000, 3, ms, world))
+    dist.destroy_process_group()
+
+
+def test_replicas_take_the_slowest_rank_gloo():
+    """bench.py --gpus N runs N independent replicas; the timed region is the max over ranks and the
+    throughput counts all ranks' units (two gloo ranks on the CPU)."""
+    import socket
+
+    import torch.multiprocessing as mp
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    out = ctx.Manager().dict()
+    procs = [ctx.Process(target=_replica, args=(r, 2, port, out)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(120)
+        assert p.exitcode == 0
+    for r in range(2):
+        ms, v = out[r]
+        assert ms == 15.0
+        assert abs(v - 1000 * 3 * 2 / 0.015) < 1e-6 * v
+    b = _bench()
+    assert b.max_over_ranks(7.0, 1, "cpu") == 7.0
