@@ -4,7 +4,6 @@ import ctypes
 import os
 import re
 
-
 from conftest import ROOT
 
 HDR = os.path.join(ROOT, "include", "fedg.h")
