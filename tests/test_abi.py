@@ -4,6 +4,8 @@ import ctypes
 import os
 import re
 
+import pytest
+
 from conftest import ROOT
 
 HDR = os.path.join(ROOT, "include", "fedg.h")
@@ -73,3 +75,36 @@ def test_fortran_shims_bind_declared_symbols():
     assert m, "fedg_update_opts layout changed: update the Fortran mirror"
     assert re.search(r"type, bind\(C\) :: fedg_update_opts\s*integer\(c_int\) :: eqs, prec, max_iter, use_guess\s*"
                      r"real\(c_double\) :: dt, tol\s*end type", src)
+
+
+def test_c_host_compiles_and_links_every_symbol(tmp_path):
+    """A plain C99 host (what a cgo / Fortran / ctypes caller sees) compiles against include/fedg.h
+    with -pedantic -Werror and links every declared function from libfedg.so; no GPU call is made."""
+    import shutil
+    import subprocess
+
+    from fedg import lib as fl
+
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    if not os.path.exists(fl.LIB_PATH):
+        import __graft_entry__ as ge
+
+        ge.build()
+    names = declared()
+    src = ['#include <stdio.h>', '#include "fedg.h"', "typedef void (*fn)(void);", "int main(void) {",
+           "  const fn f[] = {"]
+    src += [f"    (fn)&{n}," for n in names]
+    src += ["  };", '  printf("%d\\n", (int)(sizeof f / sizeof f[0]));', "  return 0;", "}"]
+    c = tmp_path / "host.c"
+    c.write_text("\n".join(src) + "\n")
+    exe = tmp_path / "host"
+    libdir = os.path.dirname(fl.LIB_PATH)
+    cuda_lib = "/usr/local/cuda/lib64"
+    cmd = ["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-Wno-cast-function-type",
+           "-I", os.path.join(ROOT, "include"), str(c), "-o", str(exe), "-L", libdir, "-lfedg",
+           f"-Wl,-rpath,{libdir}", f"-Wl,-rpath-link,{cuda_lib}", f"-Wl,-rpath,{cuda_lib}"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0 and int(out.stdout.strip()) == len(names), out.stderr
