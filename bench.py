@@ -49,16 +49,16 @@ PATH_TOL = {"pair": 1e-13, "mixed": 1e-10, "fp64": 1e-10}
 PATH_ITER = {"pair": 30, "mixed": 20, "fp64": 20}
 PATH_NAME = {"pair": "learned+pair", "mixed": "learned+fp32", "fp64": "plain_fp64"}
 PATH_DTYPE = {"pair": "f32x2", "mixed": "f32+f32x2", "fp64": "f64"}
-# DRAM bytes per node of one launch of the dominant kernel from ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum on the 32x32x16-element slice, 8,388,608 nodes; profiles/), per path
+# DRAM bytes per node of one launch of the dominant kernel, measured by ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum of one launch on the 32x32x16-element slice, 8,388,608 nodes), per path
 NCU_BYTES_PER_NODE = {
     "pair": {"vi_mixed": (895.11e6 + 1128.88e6) / (32 * 32 * 16 * 512)},
     "mixed": {"vi_mixed": (847.3e6 + 728.2e6) / (32 * 32 * 16 * 512)},
 }
 
 
-# warp instructions per node of one launch of the dominant kernel from ncu (smsp__inst_executed.sum
-# on the 32x32x16-element slice; profiles/pair_step_C5small_p7_32x32x16.md), per path
+# warp instructions per node of one launch of the dominant kernel, measured by ncu
+# (smsp__inst_executed.sum of one launch on the 32x32x16-element slice), per path
 NCU_INST_PER_NODE = {
     "pair": {"vi_mixed": 2.104868361e9 / (32 * 32 * 16 * 512)},
 }
@@ -330,7 +330,7 @@ def tracer_bench(args, torch, np, fl, cases, peaks, peak_src, steps, warmup):
     if top:
         roof = {"bound": "hbm", "kernel": top, "achieved": kern[top]["achieved_gbs"], "peak": peaks.get("hbm_gbs", 6800.0),
                 "unit": "GB/s", "frac": kern[top]["frac_of_hbm"], "peak_source": peak_src,
-                "note": "float-pair kernels; see profiles/trc_kernels_C5small_p7_32x32x16.md"}
+                "note": "float-pair tracer kernels"}
     # end to end: the step's inputs (QTRC, MFLX x3, alph_dens M/P, DDENS_TRC, DDENS0_TRC) from pinned host
     # memory, one tracer step, QTRC back to the host
     e2e = None
@@ -561,9 +561,8 @@ def run_fedg(args):
     }
     avg_ms = ktime / max(klaunch, 1)
     achieved = bytes_per_node.get(kname, 0) * nodes / (avg_ms * 1e-3) / 1e9 if avg_ms > 0 else 0.0
-    # DRAM bytes per node of one launch from ncu (dram__bytes_read.sum + dram__bytes_write.sum of the
-    # kernel on the 32x32x16-element slice, profiles/mixed_kernels_C5small_p7_32x32x16.md), scaled to
-    # this workload's node count
+    # DRAM bytes per node of one launch measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum
+    # of the kernel on the 32x32x16-element slice), scaled to this workload's node count
     ncu_bytes_per_node = NCU_BYTES_PER_NODE.get(path, {})
     traffic = ncu_bytes_per_node[kname] * nodes / 1e9 if kname in ncu_bytes_per_node else None
     roof = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peaks.get("hbm_gbs", 6800.0),

@@ -310,6 +310,8 @@ int fedg_ctx_create(const fedg_mesh_desc* d, fedg_ctx** out) {
     fedg_ctx_destroy(c);
     return cuda_fail(e, "fedg_ctx_create");
   }
+  // set-up of fedg_cal_tend_ex_noalloc on this device (loads its static scratch now, not at call time)
+  noalloc_setup(d->device);
   *out = c;
   return 0;
 }
@@ -773,6 +775,10 @@ int fedg_guess_predict(fedg_guess* g, const float* X, float* Y, int n) {
   if (!g || !X || !Y || n < 1) return fail("fedg_guess_predict: bad argument");
   const int r = mlp_predict(reinterpret_cast<MlpState*>(g), X, Y, n, 0);
   return r ? cuda_fail((cudaError_t)r, "fedg_guess_predict") : 0;
+}
+int fedg_guess_set_wait_limit(fedg_guess* g, int polls) {
+  if (!g || polls < 0) return fail("fedg_guess_set_wait_limit: bad argument");
+  return mlp_set_poll_limit(reinterpret_cast<MlpState*>(g), polls) ? fail("fedg_guess_set_wait_limit") : 0;
 }
 int fedg_guess_load(fedg_ctx* c, fedg_guess* g) {
   if (!c) return fail("fedg_guess_load: null ctx");

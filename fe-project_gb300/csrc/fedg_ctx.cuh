@@ -62,6 +62,9 @@ int numdiff_apply_pair(fedg_ctx* c, double* const q[5], int nlap, double coef_h,
 // sponge-layer coefficient at the L LGL levels of the column (dgm_spongelayer.F90): 0.25/tau
 // (1 + sign(z - h)) (1 - cos(pi (z - h) / (z_top - h)))
 void sponge_coef_host(const fedg_ctx* c, double tau, double height, double* coef);
+// fedg_cal_tend_ex_noalloc's set-up (fedg_static.cu): looks up its static scratch array on device `dev`,
+// the current device, which loads the module holding it; called by fedg_ctx_create
+void noalloc_setup(int dev);
 // save_massflux of a stage held as float-pair (qp) or FP32 (qf) deviations from the hydrostatic
 // state and the reference-wind momentum (fedg_trc.cu), into the registered tracer-flux outputs
 int save_massflux_dev(fedg_ctx* c, int rkstage, const float2* const qp[5], const float* const qf[5], double U,

@@ -903,8 +903,14 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
   if (cudaMemcpyAsync(c->h_cnt, c->d_cnt, sizeof(unsigned long long) * 3, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
       cudaStreamSynchronize(c->stream) != cudaSuccess)
     return api_fail("fedg_update(mixed): status readback");
-  if (o->use_guess && mlp_take_error(c->guess, c->stream))
-    return api_fail("fedg_update(mixed): a column-guess tensor-core GEMM timed out waiting on its barrier");
+  if (o->use_guess) {
+    const int ge = mlp_take_error(c->guess, c->stream);
+    if (ge == -1) return api_fail("fedg_update(mixed): a column-guess tensor-core GEMM timed out waiting on its barrier");
+    if (ge == -2)
+      return api_fail("fedg_update(mixed): a column-guess tensor-core GEMM timed out waiting on its barrier, and "
+                      "waiting for its MMAs in flight timed out too");
+    if (ge) return api_cuda_fail((cudaError_t)ge, "fedg_update(mixed): column-guess error flag");
+  }
   if (iters_out) *iters_out = c->h_cnt[2] ? double(c->h_cnt[1]) / double(c->h_cnt[2]) : 0.0;
   return (int)c->h_cnt[0];
 }

@@ -47,10 +47,15 @@ struct ColIO {
 // matrices are 128 B apart (leading byte offset), 8-row groups 512 B apart (stride byte
 // offset).
 // One elected thread issues tcgen05.mma (M = 128, N = BN, K = 16) into a TMEM accumulator of
-// 128 lanes x BN columns and commits to an mbarrier.  Every wait on that barrier is bounded:
-// after the limit the kernel raises *err, skips the stores, waits once more (bounded) for
-// the MMAs in flight and releases its TMEM.  The epilogue reads the accumulator with
-// tcgen05.ld (warp w owns lanes 32w..32w+31, one output row per thread), adds the bias,
+// 128 lanes x BN columns and commits to an mbarrier.  Every wait on that barrier is bounded.
+// The waits of the normal path poll at most `poll_limit` times; when one runs out the kernel
+// raises *err (1), skips the epilogue's TMEM reads and stores, and drains: it waits for the
+// last commit, which arrives once every MMA issued before it has completed, with the full
+// limit DRAIN_POLLS.  If the drain runs out as well it raises *err (2) and still releases its
+// TMEM: a CTA that exits holding TMEM can leave later allocations on its SM waiting for ever,
+// while a release behind MMAs still in flight can only disturb accumulators of this launch,
+// whose outputs the raised flag has already discarded.  The epilogue reads the accumulator
+// with tcgen05.ld (warp w owns lanes 32w..32w+31, one output row per thread), adds the bias,
 // applies GELU and stores the row.
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -59,8 +64,11 @@ __device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint
          (1ull << 46);  // descriptor version 1, base offset 0, no swizzle
 }
 
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t parity) {
-  for (int it = 0; it < (1 << 20); ++it) {
+// polls of the drain wait, and the default limit of the normal path's waits
+constexpr int DRAIN_POLLS = 1 << 20;
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t parity, int limit) {
+  for (int it = 0; it < limit; ++it) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -84,7 +92,7 @@ __device__ __forceinline__ size_t col_off(const ColMap& cm, int l) {
 template <int BN, int OMODE, bool GELU>
 __global__ void __launch_bounds__(128) k_gemm_tc(const bf16* __restrict__ A, const bf16* __restrict__ W,
                                                  const float* __restrict__ bias, void* __restrict__ out, int M, int Np,
-                                                 int Kp, const ColIO io, int* err) {
+                                                 int Kp, const ColIO io, int* err, int poll_limit) {
   constexpr int TM = 128, TK = 32, NA = TM * (TK / 8) / 128, NB = BN * (TK / 8) / 128;
   constexpr uint32_t TCOLS = BN <= 32 ? 32 : (BN <= 64 ? 64 : (BN <= 128 ? 128 : 256));
   static_assert(BN % 32 == 0 && BN <= 256, "tcgen05 M=128 tile: N % 32 == 0 (16 for the MMA), N <= 256");
@@ -150,7 +158,7 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const bf16* __restrict__ A, con
   for (int c = 0; c < nch; ++c) {
     const int buf = c & 1;
     if (c >= 2) {  // the MMAs of chunk c-2 must have read this buffer
-      const bool got = mbar_wait_bounded(smem_u32(mbar + buf), (uint32_t)(((c - 2) >> 1) & 1));
+      const bool got = mbar_wait_bounded(smem_u32(mbar + buf), (uint32_t)(((c - 2) >> 1) & 1), poll_limit);
       ok = __syncthreads_and(got) != 0;
       if (!ok) break;
     }
@@ -178,18 +186,25 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const bf16* __restrict__ A, con
     if (c + 1 < nch) load_chunk((c + 1) * TK);
   }
   // the last commit arrives once every MMA before it has completed
-  if (last >= 0) {
-    const bool got = mbar_wait_bounded(smem_u32(mbar + (last & 1)), (uint32_t)((last >> 1) & 1));
-    ok = (__syncthreads_and(got) != 0) && ok;
+  if (last >= 0 && ok) {
+    const bool got = mbar_wait_bounded(smem_u32(mbar + (last & 1)), (uint32_t)((last >> 1) & 1), poll_limit);
+    ok = __syncthreads_and(got) != 0;
   }
-  if (!ok && tid == 0) atomicExch(err, 1);
+  if (!ok) {  // drain the MMAs in flight with the full limit before the TMEM is released
+    bool drained = true;
+    if (last >= 0) {
+      const bool got = mbar_wait_bounded(smem_u32(mbar + (last & 1)), (uint32_t)((last >> 1) & 1), DRAIN_POLLS);
+      drained = __syncthreads_and(got) != 0;
+    }
+    if (tid == 0) atomicMax(err, drained ? 1 : 2);
+  }
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   const int row = m0 + 32 * warp + lane;
   const uint32_t tl = tmem + ((uint32_t)(32 * warp) << 16);
   size_t rbase = 0;
   if constexpr (OMODE == 2) rbase = col_base(io.cm, row < M ? row : 0);
 #pragma unroll 1
-  for (int c0 = 0; c0 < BN; c0 += 16) {
+  for (int c0 = 0; ok && c0 < BN; c0 += 16) {  // ok is uniform over the CTA (__syncthreads_and)
     uint32_t r[16];
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
@@ -198,7 +213,7 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const bf16* __restrict__ A, con
         : "r"(tl + (uint32_t)c0)
         : "memory");
     asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-    if (ok && row < M) {
+    if (row < M) {
       if constexpr (OMODE == 2) {  // scatter: output feature -> (variable, level) of column `row`
         const int L = io.cm.L;
         int f = n0 + c0;
@@ -238,20 +253,21 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const bf16* __restrict__ A, con
 
 template <int BN, int OMODE, bool GELU>
 static void launch_tc_n(const bf16* A, const bf16* W, const float* bias, void* out, int M, int Np, int Kp,
-                        const ColIO& io, int* err, cudaStream_t s) {
+                        const ColIO& io, int* err, int poll_limit, cudaStream_t s) {
   const size_t smem = 2 * sizeof(bf16) * (128 * 32 + BN * 32) + 2 * sizeof(uint64_t) + 16;
   auto kfn = k_gemm_tc<BN, OMODE, GELU>;
   cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  kfn<<<dim3((unsigned)((M + 127) / 128), (unsigned)(Np / BN)), 128, smem, s>>>(A, W, bias, out, M, Np, Kp, io, err);
+  kfn<<<dim3((unsigned)((M + 127) / 128), (unsigned)(Np / BN)), 128, smem, s>>>(A, W, bias, out, M, Np, Kp, io, err,
+                                                                                  poll_limit);
 }
 
 template <int OMODE, bool GELU>
 static void launch_gemm_tc(const bf16* A, const bf16* W, const float* bias, void* out, int M, int Np, int Kp,
-                           const ColIO& io, int* err, cudaStream_t s) {
-  if (Np % 256 == 0) launch_tc_n<256, OMODE, GELU>(A, W, bias, out, M, Np, Kp, io, err, s);
-  else if (Np % 192 == 0) launch_tc_n<192, OMODE, GELU>(A, W, bias, out, M, Np, Kp, io, err, s);
-  else if (Np % 128 == 0) launch_tc_n<128, OMODE, GELU>(A, W, bias, out, M, Np, Kp, io, err, s);
-  else launch_tc_n<64, OMODE, GELU>(A, W, bias, out, M, Np, Kp, io, err, s);
+                           const ColIO& io, int* err, int poll_limit, cudaStream_t s) {
+  if (Np % 256 == 0) launch_tc_n<256, OMODE, GELU>(A, W, bias, out, M, Np, Kp, io, err, poll_limit, s);
+  else if (Np % 192 == 0) launch_tc_n<192, OMODE, GELU>(A, W, bias, out, M, Np, Kp, io, err, poll_limit, s);
+  else if (Np % 128 == 0) launch_tc_n<128, OMODE, GELU>(A, W, bias, out, M, Np, Kp, io, err, poll_limit, s);
+  else launch_tc_n<64, OMODE, GELU>(A, W, bias, out, M, Np, Kp, io, err, poll_limit, s);
 }
 
 // Generic FP32 SIMT GEMM for training: C(m,n) (+)= sum_k A(m,k) B(k,n) (+ bias[n]),
@@ -385,7 +401,8 @@ struct MlpState {
   size_t icap = 0;
   bf16 *Xh = nullptr, *H1 = nullptr, *H2 = nullptr;
   float* Yf = nullptr;
-  int* err = nullptr;  // raised by a tensor-core GEMM whose barrier wait ran out
+  int* err = nullptr;  // raised by a tensor-core GEMM whose barrier wait ran out (1), or whose drain did too (2)
+  int poll_limit = DRAIN_POLLS;  // polls of the tensor-core GEMMs' normal-path barrier waits
   int ready = 0;
 };
 
@@ -611,10 +628,11 @@ static int ensure_infer(MlpState* m, size_t n) {
 // scatters its outputs to the guess fields, otherwise it writes FP32 rows to m->Yf
 static int run_layers(MlpState* m, int n, const ColIO* io, cudaStream_t s) {
   const ColIO none{};
-  launch_gemm_tc<0, true>(m->Xh, m->Wh + m->hW1, m->P + m->ob1, m->H1, n, m->hp, m->dinp, none, m->err, s);
-  launch_gemm_tc<0, true>(m->H1, m->Wh + m->hW2, m->P + m->ob2, m->H2, n, m->hp, m->hp, none, m->err, s);
-  if (io) launch_gemm_tc<2, false>(m->H2, m->Wh + m->hW3, m->P + m->ob3, nullptr, n, m->doutp, m->hp, *io, m->err, s);
-  else launch_gemm_tc<1, false>(m->H2, m->Wh + m->hW3, m->P + m->ob3, m->Yf, n, m->doutp, m->hp, none, m->err, s);
+  const int pl = m->poll_limit;
+  launch_gemm_tc<0, true>(m->Xh, m->Wh + m->hW1, m->P + m->ob1, m->H1, n, m->hp, m->dinp, none, m->err, pl, s);
+  launch_gemm_tc<0, true>(m->H1, m->Wh + m->hW2, m->P + m->ob2, m->H2, n, m->hp, m->hp, none, m->err, pl, s);
+  if (io) launch_gemm_tc<2, false>(m->H2, m->Wh + m->hW3, m->P + m->ob3, nullptr, n, m->doutp, m->hp, *io, m->err, pl, s);
+  else launch_gemm_tc<1, false>(m->H2, m->Wh + m->hW3, m->P + m->ob3, m->Yf, n, m->doutp, m->hp, none, m->err, pl, s);
   return (int)cudaGetLastError();
 }
 
@@ -646,7 +664,13 @@ int mlp_take_error(MlpState* m, cudaStream_t s) {
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return (int)e;
   if (h) cudaMemsetAsync(m->err, 0, sizeof(int), s);
-  return h ? -1 : 0;
+  return h ? -h : 0;
+}
+
+int mlp_set_poll_limit(MlpState* m, int polls) {
+  if (!m || polls < 0) return (int)cudaErrorInvalidValue;
+  m->poll_limit = polls;
+  return 0;
 }
 
 int mlp_predict(MlpState* m, const float* X, float* Y, int n, cudaStream_t s) {

@@ -23,9 +23,12 @@ int mlp_rows(MlpState* m, int ncol, double impl_fac, MlpRows* out, cudaStream_t 
 // GEMMs on the tensor cores, the last scattering into three FP32 (Np, Ne) fields.
 int mlp_infer(MlpState* m, const fedg::Ops& op, float* gd, float* gm, float* gr, cudaStream_t s);
 
-// 0, or -1 if a tensor-core GEMM of this network gave up waiting on its barrier since the last
-// call (synchronises the stream; clears the flag)
+// 0; -1 if a tensor-core GEMM of this network gave up waiting on its barrier since the last call
+// (it then drained its MMAs and skipped its stores); -2 if the drain ran out too (synchronises the
+// stream; clears the flag)
 int mlp_take_error(MlpState* m, cudaStream_t s);
+// polls of the tensor-core GEMMs' normal-path barrier waits (the drain keeps its full limit)
+int mlp_set_poll_limit(MlpState* m, int polls);
 
 // host-side management used by the C ABI
 int mlp_create(int levels, int hidden, MlpState** out);

@@ -12,7 +12,10 @@
 // The array is part of the library image: every GPU that loads the library holds its
 // FEDG_NOALLOC_MAX_NODES doubles (16 MiB) until the process exits.  Host code cannot use the
 // symbol name as a device address; the device address is looked up with cudaGetSymbolAddress,
-// once per device, with that device current, on the first call on that device.
+// once per device, with that device current.  With CUDA's lazy module loading that lookup is what
+// loads this translation unit's module onto the device, and loading it reserves the 16 MiB.  So the
+// lookup runs during set-up: fedg_ctx_create calls noalloc_setup() on the context's device, and
+// the entry point itself only reads the address recorded then.
 #include <mutex>
 
 #include "fedg_ctx.cuh"
@@ -25,7 +28,41 @@ static __device__ __align__(256) double g_noalloc_dpres[FEDG_NOALLOC_MAX_NODES];
 namespace {
 std::mutex g_noalloc_mu;
 double* g_noalloc_ptr[FEDG_NOALLOC_MAX_DEVICES] = {};
+cudaError_t g_noalloc_err[FEDG_NOALLOC_MAX_DEVICES] = {};  // outcome of a failed set-up lookup
+
+// Makes `dev` current for the lifetime of the guard and restores the caller's device afterwards.
+struct DeviceGuard {
+  int prev = -1;
+  cudaError_t err = cudaSuccess;
+  explicit DeviceGuard(int dev) {
+    if ((err = cudaGetDevice(&prev)) == cudaSuccess && prev != dev) err = cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int now = -1;
+    if (prev >= 0 && cudaGetDevice(&now) == cudaSuccess && now != prev) cudaSetDevice(prev);
+  }
+};
 }  // namespace
+
+namespace fedg {
+// Looks up the static array's device address on `dev` (the current device) and records it.  Called
+// by fedg_ctx_create.  A failure is recorded, not returned: the context stays usable, and
+// fedg_cal_tend_ex_noalloc reports the recorded error instead of trying again at call time.
+void noalloc_setup(int dev) {
+  if (dev < 0 || dev >= FEDG_NOALLOC_MAX_DEVICES) return;
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (g_noalloc_ptr[dev]) return;
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_dpres);
+  if (e != cudaSuccess) {
+    g_noalloc_err[dev] = e;
+    cudaGetLastError();  // the failure is reported by the entry point, not by the next call
+    return;
+  }
+  g_noalloc_ptr[dev] = static_cast<double*>(p);
+  g_noalloc_err[dev] = cudaSuccess;
+}
+}  // namespace fedg
 
 extern "C" int fedg_cal_tend_ex_noalloc(fedg_ctx* c, const double* const in[16], double* const out[5], int eqs) {
   if (!c || !in || !out) return api_fail("fedg_cal_tend_ex_noalloc: null argument");
@@ -40,28 +77,26 @@ extern "C" int fedg_cal_tend_ex_noalloc(fedg_ctx* c, const double* const in[16],
     return api_fail("fedg_cal_tend_ex_noalloc: register this base state with fedg_set_base_state first");
   const int dev = c->d.device;
   if (dev < 0 || dev >= FEDG_NOALLOC_MAX_DEVICES) return api_fail("fedg_cal_tend_ex_noalloc: device ordinal out of range");
-  cudaError_t e = cudaSetDevice(dev);
-  if (e != cudaSuccess) return api_cuda_fail(e, "fedg_cal_tend_ex_noalloc: cudaSetDevice");
   double* scratch = nullptr;
+  cudaError_t setup_err = cudaSuccess;
   {
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {  // first call on this device: look up the array's device address
-      void* p = nullptr;
-      e = cudaGetSymbolAddress(&p, g_noalloc_dpres);
-      if (e != cudaSuccess) return api_cuda_fail(e, "fedg_cal_tend_ex_noalloc: cudaGetSymbolAddress");
-      g_noalloc_ptr[dev] = static_cast<double*>(p);
-    }
     scratch = g_noalloc_ptr[dev];
+    setup_err = g_noalloc_err[dev];
   }
+  if (!scratch)
+    return api_fail(std::string("fedg_cal_tend_ex_noalloc: the static scratch was not loaded on this device when the "
+                                "context was created (") +
+                    (setup_err != cudaSuccess ? cudaGetErrorString(setup_err) : "no lookup") + ")");
+  DeviceGuard guard(dev);
+  if (guard.err != cudaSuccess) return api_cuda_fail(guard.err, "fedg_cal_tend_ex_noalloc: cudaSetDevice");
   // Every entry the tendency kernel reads (own and face-neighbour nodes, all inside [0, Np*Ne))
   // is written by the DPRES kernel first, so nothing needs clearing between calls.
-  c->nlaunch[FEDG_K_PRES]++;
-  int r = launch_drhot2pres(c->op, c->prof(), in[4], nullptr, scratch, c->n, c->stream);
+  int r = tracked(c, FEDG_K_PRES, [&] { return launch_drhot2pres(c->op, c->prof(), in[4], nullptr, scratch, c->n, c->stream); });
   if (r) return api_cuda_fail((cudaError_t)r, "fedg_cal_tend_ex_noalloc: DRHOT2PRES");
   F5c q{{in[0], in[1], in[2], in[3], in[4]}};
   F5 t{{out[0], out[1], out[2], out[3], out[4]}};
-  c->nlaunch[FEDG_K_TEND]++;
-  r = launch_tend_fp64(c->op, c->prof(), q, scratch, t, c->Ne, eqs, c->stream);
+  r = tracked(c, FEDG_K_TEND, [&] { return launch_tend_fp64(c->op, c->prof(), q, scratch, t, c->Ne, eqs, c->stream); });
   if (r) return api_cuda_fail((cudaError_t)r, "fedg_cal_tend_ex_noalloc: tendency");
   return 0;
 }

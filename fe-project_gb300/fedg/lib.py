@@ -35,6 +35,7 @@ EXPORTED = [
     "fedg_trc_alphdens_advtest", "fedg_trc_save_massflux", "fedg_trc_fct_coef", "fedg_trc_cal_tend",
     "fedg_trc_tmar", "fedg_trc_modalfilter", "fedg_trc_update", "fedg_numdiff_apply", "fedg_sponge_add_tend",
     "fedg_update_set_tracer_flux", "fedg_update_set_sponge", "fedg_numdiff_apply_prec",
+    "fedg_guess_set_wait_limit",
 ]
 
 # kernel classes of fedg_prof_read (include/fedg.h)
@@ -126,6 +127,7 @@ def load():
     lib.fedg_guess_loss_grad.argtypes = [_vp, _vp, _vp, ctypes.c_int, _fp, _fp]
     lib.fedg_guess_predict.argtypes = [_vp, _vp, _vp, ctypes.c_int]
     lib.fedg_guess_load.argtypes = [_vp, _vp]
+    lib.fedg_guess_set_wait_limit.argtypes = [_vp, ctypes.c_int]
     _P3 = ctypes.c_void_p * 3
     lib.fedg_trc_alphdens_advtest.argtypes = [_vp] + [_vp] * 6
     lib.fedg_trc_save_massflux.argtypes = [_vp, ctypes.c_int, _P5, _vp, ctypes.c_double, ctypes.c_double,
@@ -559,6 +561,10 @@ class Guess:
         _check(self.lib.fedg_guess_predict(self.h, _ptr(X), _ptr(Y), int(X.shape[0])), "fedg_guess_predict")
         torch.cuda.synchronize()
         return Y
+
+    def set_wait_limit(self, polls):
+        """polls of the tensor-core GEMMs' barrier waits before they give up (default 1 << 20)"""
+        _check(self.lib.fedg_guess_set_wait_limit(self.h, int(polls)), "fedg_guess_set_wait_limit")
 
     def attach(self, ctx):
         _check(self.lib.fedg_guess_load(ctx.h, self.h), "fedg_guess_load")

@@ -99,10 +99,14 @@ int fedg_cal_tend_ex(fedg_ctx* ctx, const double* const in[16], double* const ou
  * device allocator has already claimed the memory): it forms DPRES in a static device array of
  * 2,097,152 doubles (16 MiB, held by every GPU that loads the library) and returns < 0 with a
  * message if Np*Ne exceeds that.  Same arguments as fedg_cal_tend_ex (in[5] is ignored); the
- * base state must already be registered with fedg_set_base_state.  The first call on a device
- * looks up the array's device address (cudaGetSymbolAddress), so make that first call before
- * any stream capture.  All calls share the one array: calls whose kernels overlap on the GPU
- * (two contexts, two streams) race on it and must be ordered by the caller. */
+ * base state must already be registered with fedg_set_base_state.  The array's device address
+ * is looked up (cudaGetSymbolAddress) when the first context on a device is created: with CUDA's
+ * lazy module loading that lookup loads the library module that holds the array and reserves its
+ * 16 MiB, so it happens in fedg_ctx_create, during the caller's set-up, and the entry point only
+ * reads the recorded address.  If that lookup failed, the entry point returns < 0 with the error.
+ * The caller's current device is restored before returning.  All calls share the one array:
+ * calls whose kernels overlap on the GPU (two contexts, two streams) race on it and must be
+ * ordered by the caller. */
 int fedg_cal_tend_ex_noalloc(fedg_ctx* ctx, const double* const in[16], double* const out[5], int eqs);
 
 /* atm_dyn_nonhydro3d_cal_vi (driver_nonhydro3d.F90:201-250; rhot_hevi.F90:772-965).
@@ -178,6 +182,12 @@ int fedg_guess_train_step(fedg_guess* g, const float* X, const float* T, int bat
 int fedg_guess_loss_grad(fedg_guess* g, const float* X, const float* T, int batch, float* loss, float* grad);
 /* inference through the BF16 tensor-core GEMM path */
 int fedg_guess_predict(fedg_guess* g, const float* X, float* Y, int n);
+/* Bounded waits of the network's tensor-core GEMMs: each wait on the MMA completion barrier polls
+ * at most `polls` times (default 1048576) before the kernel gives up, drains the MMAs it issued
+ * (with the default limit), skips its stores and raises an error flag that the calling entry point
+ * returns as < 0 with fedg_last_error text.  No counterpart in FElib (no GPU waits there); a small
+ * limit makes the wait run out on purpose, which is how the error path is tested. */
+int fedg_guess_set_wait_limit(fedg_guess* g, int polls);
 /* attach (g != NULL) or detach (g == NULL) the network used by fedg_update(use_guess = 1) */
 int fedg_guess_load(fedg_ctx* ctx, fedg_guess* g);
 

@@ -93,3 +93,29 @@ def test_learned_guess_gain_c4_geometry():
     for v in range(5):
         d = float(torch.linalg.norm(qa[v] - qb[v]).item())
         assert d <= 1e-8 * dn, (v, d)
+
+
+def test_guess_wait_limit_reports_error_and_context_recovers():
+    """The tensor-core GEMMs' bounded barrier waits: with a wait limit of zero polls every wait of
+    the normal path runs out at once, the kernels drain their MMAs with the full limit, skip their
+    stores and raise the error flag, and fedg_update returns < 0 with the error text.  With the
+    default limit restored the same context steps normally."""
+    import torch
+
+    case = cases.C2().scaled(2, 2, 8)
+    q, b = cases.initial_state(case)
+    ctx = fl.Context(case)
+    ctx.set_base_state(b["dens_hyd"], b["pres_hyd"], b["therm_hyd"])
+    net = fl.Guess(case.NeZ * case.N1, 64)
+    net.set_params(np.zeros(net.n, np.float32))  # guess Q = q*: a valid iterate, whatever the training
+    net.attach(ctx)
+    qd = [ctx.tensor(a) for a in q]
+    net.set_wait_limit(0)
+    with pytest.raises(fl.FedgError, match="timed out waiting on its barrier"):
+        ctx.update(qd, 1, prec=fl.PREC_MIXED, dt=0.04, max_iter=20, tol=1e-10, use_guess=True)
+    torch.cuda.synchronize()
+    net.set_wait_limit(1 << 20)
+    qd = [ctx.tensor(a) for a in q]
+    nf, it = ctx.update(qd, 1, prec=fl.PREC_MIXED, dt=0.04, max_iter=20, tol=1e-10, use_guess=True)
+    assert nf == 0 and it >= 1.0
+    assert all(bool(torch.isfinite(t).all()) for t in qd)

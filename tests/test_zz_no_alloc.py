@@ -34,7 +34,6 @@ def test_noalloc_matches_cal_tend_ex_twice(name, case, eqs):
     sc = [1e-3 * b["dens_hyd"], 2.0, 2.0, 1.0, 0.3]
     ctx = fl.Context(case)
     ctx.set_base_state(b["dens_hyd"], b["pres_hyd"], b["therm_hyd"])
-    ref = [t.cpu().numpy() for t in ctx.cal_tend_ex([ctx.tensor(a) for a in q], eqs)]
     for call in range(2):
         qd = [ctx.tensor(q[v] + (call * 0.1) * sc[v] * rng.standard_normal(q[v].shape)) for v in range(5)]
         ref = [t.cpu().numpy() for t in ctx.cal_tend_ex(qd, eqs)]  # the allocating entry point
@@ -61,3 +60,34 @@ def test_noalloc_rejects_meshes_beyond_its_scratch():
     torch.cuda.synchronize()
     rc = ctx.lib.fedg_cal_tend_ex_noalloc(ctx.h, _inputs(ctx, qd), fl._p5(out), int(fl.HEVI))
     assert rc < 0 and "static scratch" in fl.last_error()
+
+
+def test_noalloc_first_on_a_fresh_context_allocates_nothing():
+    """On a context that has never run the allocating entry point, two calls leave the device's
+    free memory unchanged (a fallback to the context's cudaMalloc'd scratch would take at least
+    the 1 MiB DPRES field of this mesh), and both match fedg_cal_tend_ex afterwards."""
+    import torch
+
+    case = cases.C2().scaled(8, 8, 4)  # 256 elements x 512 nodes: DPRES is 1 MiB
+    q, b = cases.initial_state(case)
+    rng = np.random.default_rng(5)
+    ctx = fl.Context(case)
+    ctx.set_base_state(b["dens_hyd"], b["pres_hyd"], b["therm_hyd"])
+    sc = [1e-3 * b["dens_hyd"], 2.0, 2.0, 1.0, 0.3]
+    qs = [[ctx.tensor(q[v] + 0.1 * (call + 1) * sc[v] * rng.standard_normal(q[v].shape)) for v in range(5)]
+          for call in range(2)]
+    outs = [[ctx.empty() for _ in range(5)] for _ in range(2)]
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for call in range(2):
+        rc = ctx.lib.fedg_cal_tend_ex_noalloc(ctx.h, _inputs(ctx, qs[call]), fl._p5(outs[call]), int(fl.HEVI))
+        assert rc == 0, fl.last_error()
+        ctx.sync()
+        free1, _ = torch.cuda.mem_get_info()
+        assert free1 == free0, (call, free0, free1)
+    for call in range(2):
+        ref = [t.cpu().numpy() for t in ctx.cal_tend_ex(qs[call], fl.HEVI)]
+        for v in range(5):
+            g = outs[call][v].cpu().numpy()
+            err = np.linalg.norm(g - ref[v]) / max(np.linalg.norm(ref[v]), 1e-300)
+            assert err <= 1e-11, (call, v, err)
