@@ -553,17 +553,11 @@ static void column_eval_Ax_uv(const Oracle& o, ColumnWork& w, std::vector<double
   }
 }
 
-// returns the number of Newton iterations used (or -1 if not converged within max_iter)
-static int column_solve(const Oracle& o, ColumnWork& w, const ColumnParams& cp, double* tend_out[5], int L) {
-  const int N1 = o.N1, NeZ = o.NeZ, N = N1 - 1, n3 = 3 * N1;
-  const double E33 = 2.0 / o.dz, FSz = 2.0 / o.dz;
+// vertical-face Rusanov speed alph frozen at the guess var0 (w.Z) (vi_cal_del_flux_dyn_uv,
+// common_2.F90:1149-1155; Gnn = |nz| = 1 on vertical faces)
+static void column_alph(const Oracle& o, ColumnWork& w, int L) {
+  const int N1 = o.N1, NeZ = o.NeZ, N = N1 - 1;
   const double rP0 = 1.0 / o.c.pres00, kap = o.c.cpdry / o.c.cvdry;
-  const std::vector<double>& Dm = o.e.D;
-  const std::vector<double>& Mi = o.e.Minv;
-  const std::vector<double>& T = o.e.T;
-  const double impl_fac = cp.impl_fac;
-
-  // alph from var0 (vi_cal_del_flux_dyn_uv :1149-1155; Gnn = |nz| = 1 on vertical faces)
   std::vector<double> s0(L);
   for (int l = 0; l < L; ++l) {
     const double rdens0 = 1.0 / (w.dh[l] + w.Z[VD][l]);
@@ -578,7 +572,19 @@ static int column_solve(const Oracle& o, ColumnWork& w, const ColumnParams& cp, 
     w.alphB[ez] = std::max(s0[lb], s0[lbP]);
     w.alphT[ez] = std::max(s0[lt], s0[ltP]);
   }
+}
 
+// returns the number of Newton iterations used (or -1 if not converged within max_iter)
+static int column_solve(const Oracle& o, ColumnWork& w, const ColumnParams& cp, double* tend_out[5], int L) {
+  const int N1 = o.N1, NeZ = o.NeZ, N = N1 - 1, n3 = 3 * N1;
+  const double E33 = 2.0 / o.dz, FSz = 2.0 / o.dz;
+  const double rP0 = 1.0 / o.c.pres00, kap = o.c.cpdry / o.c.cvdry;
+  const std::vector<double>& Dm = o.e.D;
+  const std::vector<double>& Mi = o.e.Minv;
+  const std::vector<double>& T = o.e.T;
+  const double impl_fac = cp.impl_fac;
+
+  column_alph(o, w, L);
   for (int v = 0; v < 5; ++v) w.P[v] = w.Z[v];  // PROG_VARS = var0 (hevi.F90:852-872)
 
   std::vector<double> tx(L), ty(L);
@@ -831,6 +837,53 @@ static long cal_vi(const Oracle& o, const double* const q[5], const double* cons
     }
   }
   return nfail;
+}
+
+// The implicit operator A(P) of every column (eval_Ax for DENS/MOMZ/RHOT, eval_Ax_uv for MOMX/MOMY,
+// common_2.F90:111-326, 482-586) with the vertical Rusanov speed frozen at q0 and the iterate P free.
+// Test infrastructure for checking the Newton solve against a finite-difference Jacobian of A.
+static void vi_operator(const Oracle& o, const double* const P[5], const double* const q0[5], double* const out[5]) {
+  const int N1 = o.N1, NeZ = o.NeZ, L = NeZ * N1;
+  const double rgamm = o.c.cvdry / o.c.cpdry;
+  const long ncol = (long)o.NeX * o.NeY * N1 * N1;
+#pragma omp parallel
+  {
+    ColumnWork w;
+    for (int v = 0; v < 5; ++v) { w.P[v].resize(L); w.Z[v].resize(L); }
+    w.dh.resize(L); w.ph.resize(L); w.rh.resize(L);
+    w.alphB.resize(NeZ); w.alphT.resize(NeZ);
+    w.A3.resize(3 * L);
+    w.W.resize(L); w.WT.resize(L); w.POT.resize(L); w.DPDRHOT.resize(L);
+    std::vector<double> tx(L), ty(L);
+    std::vector<size_t> gidx(L);
+#pragma omp for schedule(dynamic, 16)
+    for (long c = 0; c < ncol; ++c) {
+      const int ij = c % (N1 * N1);
+      const long exy = c / (N1 * N1);
+      const int i = ij % N1, j = ij / N1;
+      const int ex = exy % o.NeX, ey = exy / o.NeX;
+      for (int ez = 0; ez < NeZ; ++ez)
+        for (int k = 0; k < N1; ++k) gidx[ez * N1 + k] = o.eid(ex, ey, ez) * o.Np + o.nid(i, j, k);
+      for (int l = 0; l < L; ++l) {
+        const size_t g = gidx[l];
+        for (int v = 0; v < 5; ++v) { w.P[v][l] = P[v][g]; w.Z[v][l] = q0[v][g]; }
+        w.dh[l] = o.dens_hyd[g];
+        w.ph[l] = o.pres_hyd[g];
+        w.rh[l] = o.c.pres00 / o.c.rdry * std::pow(w.ph[l] / o.c.pres00, rgamm);
+      }
+      column_alph(o, w, L);
+      column_eval_Ax_uv(o, w, tx, ty);
+      column_eval_Ax(o, w);
+      for (int l = 0; l < L; ++l) {
+        const size_t g = gidx[l];
+        out[VD][g] = w.A3[0 * L + l];
+        out[VMZ][g] = w.A3[1 * L + l];
+        out[VRT][g] = w.A3[2 * L + l];
+        out[VMX][g] = tx[l];
+        out[VMY][g] = ty[l];
+      }
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------------
@@ -1549,6 +1602,10 @@ void orc_cal_tend(void* h, int hevi, const double* const* q, const double* dpres
 long orc_cal_vi(void* h, const double* const* q, const double* const* q0, double impl_fac, double dt,
                 int max_iter, double tol, double* const* tend, int* col_iters) {
   return cal_vi(*static_cast<Oracle*>(h), q, q0, impl_fac, dt, max_iter, tol, tend, col_iters);
+}
+
+void orc_vi_operator(void* h, const double* const* P, const double* const* q0, double* const* out) {
+  vi_operator(*static_cast<Oracle*>(h), P, q0, out);
 }
 
 void orc_modalfilter(void* h, double* const* q) { modal_filter(*static_cast<Oracle*>(h), q); }

@@ -69,6 +69,7 @@ def _load():
     lib.orc_cal_vi.argtypes = [ctypes.c_void_p, pp, pp, ctypes.c_double, ctypes.c_double,
                                ctypes.c_int, ctypes.c_double, pp, ctypes.POINTER(ctypes.c_int)]
     lib.orc_modalfilter.argtypes = [ctypes.c_void_p, pp]
+    lib.orc_vi_operator.argtypes = [ctypes.c_void_p, pp, pp, pp]
     lib.orc_step_heve.argtypes = [ctypes.c_void_p, pp, ctypes.c_double, ctypes.c_int]
     lib.orc_step_hevi.restype = ctypes.c_long
     lib.orc_step_hevi.argtypes = [ctypes.c_void_p, pp, ctypes.c_double, ctypes.c_int, ctypes.c_int,
@@ -195,6 +196,18 @@ class Oracle:
                                     its.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
         if want_iters:
             return out, int(nfail), its
+        return out
+
+    def vi_operator(self, P, q0):
+        """The implicit (vertical) operator A(P) of cal_vi on every column, with its Rusanov speed
+        frozen at q0: the operator whose Newton solve cal_vi performs."""
+        ps = [np.ascontiguousarray(a, np.float64) for a in P]
+        q0s = [np.ascontiguousarray(a, np.float64) for a in q0]
+        out = [np.zeros(self.shape) for _ in range(5)]
+        pp_, _k1 = _pp(ps)
+        pz, _k2 = _pp(q0s)
+        po, _k3 = _pp(out)
+        self.lib.orc_vi_operator(self._h, pp_, pz, po)
         return out
 
     def modalfilter(self, q):
