@@ -776,6 +776,11 @@ int fedg_guess_predict(fedg_guess* g, const float* X, float* Y, int n) {
   const int r = mlp_predict(reinterpret_cast<MlpState*>(g), X, Y, n, 0);
   return r ? cuda_fail((cudaError_t)r, "fedg_guess_predict") : 0;
 }
+int fedg_update_set_vi_neumann(fedg_ctx* c, int nterm) {
+  if (!c || nterm < 0 || nterm > 8) return fail("fedg_update_set_vi_neumann: nterm must be 0..8");
+  c->vi_neumann = nterm;
+  return 0;
+}
 int fedg_guess_set_wait_limit(fedg_guess* g, int polls) {
   if (!g || polls < 0) return fail("fedg_guess_set_wait_limit: bad argument");
   return mlp_set_poll_limit(reinterpret_cast<MlpState*>(g), polls) ? fail("fedg_guess_set_wait_limit") : 0;

@@ -43,6 +43,9 @@ struct fedg_ctx {
   // sponge layer inside fedg_update (fedg_update_set_sponge; off when sl_tau <= 0)
   double sl_tau = 0.0, sl_height = 0.0;
   int sl_hvel = 0;
+  // Jacobian-vector products of the Neumann corrections of the float-pair/FP32 column solve
+  // (fedg_update_set_vi_neumann; 0: LU corrections only)
+  int vi_neumann = 2;
   // kernel timers / launch counters
   bool prof_on = false;
   long long nlaunch[FEDG_K_COUNT] = {};

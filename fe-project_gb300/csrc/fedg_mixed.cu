@@ -798,7 +798,8 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
   m->opp.Uref = m->opx.Uref;
   m->opp.Vref = m->opx.Vref;
   const double impl_fac = gam * o->dt;
-  MixViArgs va{impl_fac, 1.0 / impl_fac, o->tol, 340.0, split_host(impl_fac), split_host(1.0 / impl_fac), o->max_iter, 1};
+  MixViArgs va{impl_fac, 1.0 / impl_fac, o->tol, 340.0, split_host(impl_fac), split_host(1.0 / impl_fac), o->max_iter, 1,
+               c->vi_neumann};
   const PairCoef pc{split_host(o->dt), split_host(2.0 * gam), split_host(gam), split_host(1.0 - alp), split_host(del),
                     split_host(alp), split_host(del), split_host(del), split_host(del), split_host(gam)};
   ProfP pfp{m->prof5, m->prof5 + c->L, m->prof5 + 2 * c->L, m->prof5 + 3 * c->L, m->prof5 + 4 * c->L,

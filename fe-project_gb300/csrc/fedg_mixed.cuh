@@ -60,6 +60,8 @@ struct MixViArgs {
   float2 inv_impl2; // 1/impl_fac as a float pair
   int max_iter;
   int check64;  // 1: convergence judged by the float-pair residual; 0: by the split residual
+  int neumann;  // > 0: corrections after an LU correction use this many Jacobian-vector products
+                // of a truncated Neumann series while it contracts (0: LU corrections only)
 };
 
 // ---- float-pair precision mode (FEDG_PREC_PAIR, fedg_pair.cu) ----

@@ -371,12 +371,35 @@ __device__ __forceinline__ float4 jac_level(const ProfX& px, const float2* P, in
   return make_float4(rhotf * rdf, Pm * rdf, kapf * (phf + fmf) / rhotf, 0.f);
 }
 
+// Block-Thomas history G_e = A_e^-1 U_e of the column solve: per node the 3 rows x 3 coupling
+// columns (9 floats), in three planes of n nodes (float4, float4, float) so that every lane's
+// stores and loads are 16-byte vectors and a warp's 32 nodes fill whole 128-byte lines: per
+// element, 4 + 4 + 1 lines.  Node index: (column + element * ncol) * N1 + k.
+struct GHist {
+  float* base;
+  size_t n;  // nodes
+  __device__ float4* p0(size_t g) const { return reinterpret_cast<float4*>(base) + g; }
+  __device__ float4* p1(size_t g) const { return reinterpret_cast<float4*>(base + 4 * n) + g; }
+  __device__ float* p2(size_t g) const { return base + 8 * n + g; }
+  // The history is written and read back within one correction while it sits in L2.  Once the
+  // back sweep has read an element's lines they are dead, and discarding them drops the dirty
+  // lines without a write-back to DRAM.  g0: first node of the warp's 32 nodes of the element
+  // (128-byte aligned: the warp's columns are C consecutive ones starting at a multiple of C).
+  __device__ void discard(size_t g0, int lane) const {
+    const char* a = nullptr;
+    if (lane < 4) a = reinterpret_cast<const char*>(p0(g0)) + 128 * lane;
+    else if (lane < 8) a = reinterpret_cast<const char*>(p1(g0)) + 128 * (lane - 4);
+    else if (lane == 8) a = reinterpret_cast<const char*>(p2(g0));
+    if (a) asm volatile("discard.global.L2 [%0], 128;" ::"l"(a) : "memory");
+  }
+};
+
 // one Newton correction of the DENS/MOMZ/RHOT system from the residual in c.Bf and the Jacobian
 // quantities of the iterate: construct_matbnd (hevi_common_2.F90:1325-1480), block-Thomas with the
-// 3x3 couplings of the face nodes, element LU; P += correction where apply.  G history in gscr.
+// 3x3 couplings of the face nodes, element LU; P += correction where apply.  G history in gh.
 template <int N1>
 __device__ void col_solve(const Ops& op, const ProfX& px, float kapf, const Col<N1>& c, double impl_fac,
-                          float* __restrict__ gsc, size_t gcol, size_t glayer, bool apply) {
+                          const GHist& gh, size_t gcol, size_t gcol0, size_t glayer, int lane, bool apply) {
   constexpr int N = N1 - 1, n3 = 3 * N1;
   const int k = c.k;
   const float fi = (float)impl_fac;
@@ -485,10 +508,12 @@ __device__ void col_solve(const Ops& op, const ProfX& px, float kapf, const Col<
     lu_rows<N1>(a, r, k);
 #pragma unroll
     for (int v = 0; v < 3; ++v) c.Bf[3 * l + v] = r[v][0];
-    float4* gp = reinterpret_cast<float4*>(gsc + (gcol + (size_t)e * glayer) * 12 * N1 + 12 * k);
-    gp[0] = make_float4(r[0][1], r[0][2], r[0][3], r[1][1]);
-    gp[1] = make_float4(r[1][2], r[1][3], r[2][1], r[2][2]);
-    gp[2] = make_float4(r[2][3], 0.f, 0.f, 0.f);
+    if (!last) {  // the last element's G is zero and never read
+      const size_t gn = (gcol + (size_t)e * glayer) * N1 + k;
+      *gh.p0(gn) = make_float4(r[0][1], r[0][2], r[0][3], r[1][1]);
+      *gh.p1(gn) = make_float4(r[1][2], r[1][3], r[2][1], r[2][2]);
+      *gh.p2(gn) = r[2][3];
+    }
     if (k == N) {
       float4* b4 = reinterpret_cast<float4*>(c.bc);
       b4[0] = make_float4(r[0][1], r[0][2], r[0][3], r[0][0]);
@@ -502,12 +527,14 @@ __device__ void col_solve(const Ops& op, const ProfX& px, float kapf, const Col<
     const int l = e * N1 + k;
     const float* x1 = c.Bf + 3 * (e + 1) * N1;
     const float xa = x1[0], xb = x1[1], xc = x1[2];
-    const float4* gp = reinterpret_cast<const float4*>(gsc + (gcol + (size_t)e * glayer) * 12 * N1 + 12 * k);
-    const float4 g0 = gp[0], g1 = gp[1], g2 = gp[2];
+    const size_t gn = (gcol + (size_t)e * glayer) * N1 + k;
+    const float4 g0 = *gh.p0(gn), g1 = *gh.p1(gn);
+    const float g2 = *gh.p2(gn);
     c.Bf[3 * l + 0] -= g0.x * xa + g0.y * xb + g0.z * xc;
     c.Bf[3 * l + 1] -= g0.w * xa + g1.x * xb + g1.y * xc;
-    c.Bf[3 * l + 2] -= g1.z * xa + g1.w * xb + g2.x * xc;
-    __syncwarp();
+    c.Bf[3 * l + 2] -= g1.z * xa + g1.w * xb + g2 * xc;
+    __syncwarp();  // every lane has read element e's history: its lines are dead
+    gh.discard((gcol0 + (size_t)e * glayer) * N1, lane);
   }
   if (apply) {
     for (int e = 0; e < c.NeZ; ++e) {
@@ -519,12 +546,114 @@ __device__ void col_solve(const Ops& op, const ProfX& px, float kapf, const Col<
   __syncwarp();
 }
 
+// One Newton correction by a truncated Neumann series, for a residual b (in c.Bf) that an LU
+// correction has already made small.  With J = I + K (K: the Jacobian of the DENS/MOMZ/RHOT system
+// without its identity, the same entries col_solve assembles), delta = (I - K + K^2 - ...) b with
+// nterm products K v; its error is K^(nterm+1) J^-1 b.  At small vertical Courant numbers ||K|| is
+// well below one (about 0.26 on the 128x128x16 p = 7 mesh at dt 0.005 s), so two products bring
+// the residual down by ~50x at the cost of two Jacobian-vector products (no assembly, no LU), where
+// an LU correction would be exact to FP32.  The caller checks the new certifying residual and
+// falls back to LU corrections when the series did not contract.
+// K v element by element, in place on c.Bf: lane k forms its node's three rows from the element's
+// v (c.Bf), the face nodes of the neighbours (vb: node N of element e-1, saved before it was
+// overwritten; node 0 of element e+1, not yet overwritten) and the level quantities of the iterate.
+template <int N1>
+__device__ void col_jvp(const Ops& op, const ProfX& px, float kapf, const Col<N1>& c, double impl_fac) {
+  constexpr int N = N1 - 1;
+  const int k = c.k;
+  const float fi = (float)impl_fac;
+  const float fdzs = (float)op.E33 * fi;
+  float Dk[N1], Tk[N1];
+#pragma unroll
+  for (int m = 0; m < N1; ++m) {
+    Dk[m] = fdzs * (float)op.D[k * N1 + m];
+    Tk[m] = fi * (float)op.grav * (float)op.T[k * N1 + m];
+  }
+  const float facB = 0.5f * fi * (float)op.Lb[k] * (float)op.FSz;
+  const float facT = 0.5f * fi * (float)op.Lt[k] * (float)op.FSz;
+  float vb[3] = {0.f, 0.f, 0.f};  // v at node N of element e-1
+  for (int e = 0; e < c.NeZ; ++e) {
+    const int l = e * N1 + k;
+    {
+      const float4 own = jac_level(px, c.P, l, kapf);
+      const bool below = k == 0 && e > 0, above = k == N && e < c.NeZ - 1;
+      const float4 nb = jac_level(px, c.P, below ? l - 1 : (above ? l + 1 : l), kapf);
+      __syncwarp();
+      c.sJ[k] = own;
+      if (below) c.sJ[N1] = nb;
+      if (above) c.sJ[N1 + 1] = nb;
+      __syncwarp();
+    }
+    const float* ve = c.Bf + 3 * e * N1;
+    float y[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int m = 0; m < N1; ++m) {
+      const float4 Jm = c.sJ[m];
+      const float vr = ve[3 * m], vm = ve[3 * m + 1], vt = ve[3 * m + 2];
+      y[0] = fmaf(Dk[m], vm, y[0]);
+      y[1] = fmaf(Tk[m], vr, fmaf(Dk[m] * Jm.z, vt, y[1]));
+      y[2] = fmaf(Dk[m], Jm.x * (vm - Jm.y * vr) + Jm.y * vt, y[2]);
+    }
+#pragma unroll
+    for (int f = 0; f < 2; ++f) {
+      const bool bnd = f == 0 ? (e == 0) : (e == c.NeZ - 1);
+      const int pv1 = f == 0 ? 0 : N;
+      const float nz = f == 0 ? -1.f : 1.f;
+      const float al = f == 0 ? c.alB(e) : c.alT(e);
+      const float fac = f == 0 ? facB : facT;
+      const float t1 = fac * al, t2 = fac * nz;
+      const float4 J1 = c.sJ[pv1];
+      const float pot1 = J1.x, wt1 = J1.y, dpd1 = J1.z;
+      const float r1 = ve[3 * pv1], m1 = ve[3 * pv1 + 1], h1 = ve[3 * pv1 + 2];
+      if (bnd) {  // slip lid: exterior MOMZ = -interior
+        y[0] -= 2.f * t2 * m1;
+        y[1] += 2.f * t1 * m1;
+        y[2] += 2.f * t2 * (pot1 * wt1 * r1 - pot1 * m1 - wt1 * h1);
+      } else {
+        const float4 Jn = c.sJ[f == 0 ? N1 : N1 + 1];
+        const float* vn = f == 0 ? vb : ve + 3 * N1;  // node 0 of element e+1 (not yet overwritten)
+        const float rn = vn[0], mn = vn[1], hn = vn[2];
+        y[0] += t1 * (r1 - rn) - t2 * (m1 - mn);
+        y[1] += t1 * (m1 - mn) - t2 * (dpd1 * h1 - Jn.z * hn);
+        y[2] += t2 * (pot1 * wt1 * r1 - Jn.x * Jn.y * rn) - t2 * (pot1 * m1 - Jn.x * mn) + t1 * (h1 - hn) -
+                t2 * (wt1 * h1 - Jn.y * hn);
+      }
+    }
+    const float vN0 = ve[3 * N], vN1 = ve[3 * N + 1], vN2 = ve[3 * N + 2];
+    __syncwarp();  // every lane has read element e's v
+    vb[0] = vN0; vb[1] = vN1; vb[2] = vN2;
+#pragma unroll
+    for (int v = 0; v < 3; ++v) c.Bf[3 * l + v] = y[v];
+    __syncwarp();
+  }
+}
+
+// P += (I - K + K^2 - ... +- K^nterm) b for b in c.Bf (destroyed) where apply.
+template <int N1>
+__device__ void col_neumann(const Ops& op, const ProfX& px, float kapf, const Col<N1>& c, double impl_fac, int nterm,
+                            bool apply) {
+  const int k = c.k;
+  for (int t = 0; t <= nterm; ++t) {
+    if (t > 0) col_jvp<N1>(op, px, kapf, c, impl_fac);
+    if (apply) {
+      const float sgn = (t & 1) ? -1.f : 1.f;
+      for (int e = 0; e < c.NeZ; ++e) {
+        const int l = e * N1 + k;
+#pragma unroll
+        for (int v = 0; v < 3; ++v) c.P[3 * l + v] = f2_pack(f2_add_f(f2_of(c.P[3 * l + v]), sgn * c.Bf[3 * l + v]));
+      }
+    }
+    __syncwarp();
+  }
+}
+
 // ---------------------------------------------------------------------------------------------
 template <int N1, bool PO>
 __global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, const ProfX px, const X5 qin, const F5c z,
                                                 const float* const* guess, void* const* qsf, void* const* tout,
                                                 float* __restrict__ gsc, int* status, unsigned long long* cnt,
                                                 const MixViArgs args, int ncol) {
+  static_assert(32 / N1 * N1 == 32, "a warp's columns cover 32 nodes of a level (whole G-history lines)");
   constexpr int N = N1 - 1, C = 32 / N1, NF = N1 * N1, Np = N1 * N1 * N1;
   extern __shared__ __align__(16) unsigned char smraw[];
   // two warps per block (C columns each): with the one-warp blocks the per-block shared-memory
@@ -711,12 +840,19 @@ __global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, 
   }
   __syncwarp();
   const size_t gcolumn = (size_t)col, glayer = (size_t)ncol;  // G history rows of this column
+  const GHist gh{gsc, (size_t)ncol * (size_t)L};
   const float cref = (float)args.cref;
   // One call site per routine (the first residual is the FP32 one and is not tested; every
   // column takes the first correction), which keeps the kernel's code small enough for the
   // instruction caches.
+  // Corrections: the first is an LU correction (col_solve); after an LU correction the next one
+  // is a truncated Neumann series (col_neumann, when args.neumann > 0), which keeps going while
+  // each one cuts the certifying residual at least fourfold; a column whose residual did not
+  // contract asks for LU corrections again.  The warp runs an LU correction if any of its active
+  // columns asks for one.
   int nsolve = 0, st = 0;
-  bool active = true;
+  bool active = true, want_lu = true, last_lu = true;
+  float err_prev = 0.f;
   while (true) {
     const bool cert = nsolve > 0 && args.check64;
     const float err = cert ? col_residual<N1, true>(ox, c, px, qin, args.impl2, cref)
@@ -727,7 +863,11 @@ __global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, 
       else if (nsolve >= args.max_iter) { st = -1; active = false; }
     }
     if (!__any_sync(FULL, active)) break;
-    col_solve<N1>(op, px, kapf, c, args.impl_fac, gsc, gcolumn, glayer, active);
+    if (nsolve > 0) want_lu = args.neumann <= 0 || (!last_lu && !(err <= 0.25f * err_prev));
+    err_prev = err;
+    last_lu = __any_sync(FULL, active && want_lu);
+    if (last_lu) col_solve<N1>(op, px, kapf, c, args.impl_fac, gh, gcolumn, (size_t)col0, glayer, lane, active);
+    else col_neumann<N1>(op, px, kapf, c, args.impl_fac, args.neumann, active);
     ++nsolve;
   }
   for (int e = 0; e < NeZ; ++e) {
@@ -776,7 +916,7 @@ int launch_n(const Ops& op, const OpsX& ox, const ProfX& px, const X5& qin, cons
 
 }  // namespace
 
-size_t vi_cols_scratch_floats(size_t nodes) { return (size_t)12 * nodes; }
+size_t vi_cols_scratch_floats(size_t nodes) { return (size_t)9 * nodes; }
 
 int launch_vi_cols(int N1, const Ops& op, const OpsX& ox, const ProfX& px, const X5& qin, const F5c& z,
                    const float* const* guess, void* const* qsf, void* const* tout, float* gsc, int* status,

@@ -35,7 +35,7 @@ EXPORTED = [
     "fedg_trc_alphdens_advtest", "fedg_trc_save_massflux", "fedg_trc_fct_coef", "fedg_trc_cal_tend",
     "fedg_trc_tmar", "fedg_trc_modalfilter", "fedg_trc_update", "fedg_numdiff_apply", "fedg_sponge_add_tend",
     "fedg_update_set_tracer_flux", "fedg_update_set_sponge", "fedg_numdiff_apply_prec",
-    "fedg_guess_set_wait_limit",
+    "fedg_guess_set_wait_limit", "fedg_update_set_vi_neumann",
 ]
 
 # kernel classes of fedg_prof_read (include/fedg.h)
@@ -128,6 +128,7 @@ def load():
     lib.fedg_guess_predict.argtypes = [_vp, _vp, _vp, ctypes.c_int]
     lib.fedg_guess_load.argtypes = [_vp, _vp]
     lib.fedg_guess_set_wait_limit.argtypes = [_vp, ctypes.c_int]
+    lib.fedg_update_set_vi_neumann.argtypes = [_vp, ctypes.c_int]
     _P3 = ctypes.c_void_p * 3
     lib.fedg_trc_alphdens_advtest.argtypes = [_vp] + [_vp] * 6
     lib.fedg_trc_save_massflux.argtypes = [_vp, ctypes.c_int, _P5, _vp, ctypes.c_double, ctypes.c_double,
@@ -296,6 +297,10 @@ class Context:
         if sync:
             self.sync()
         return nfail, float(mi.value)
+
+    def set_vi_neumann(self, nterm):
+        """Jacobian-vector products of the column solve's Neumann corrections (0: LU only)."""
+        _check(self.lib.fedg_update_set_vi_neumann(self.h, int(nterm)), "fedg_update_set_vi_neumann")
 
     # -- tracer advection (trcadvect3d_heve.F90, driver_trcadv3d.F90) --
     @property

@@ -160,6 +160,17 @@ typedef struct {
 int fedg_update(fedg_ctx* ctx, double* const q[5], int nsteps, const fedg_update_opts* opts,
                 double* iters_out);
 
+/* Newton corrections of the FEDG_PREC_MIXED / FEDG_PREC_PAIR column solve.  Every column's first
+ * correction solves the FP32 Jacobian by block-Thomas and element LU, like FElib's solve
+ * (hevi_common_2.F90:329-479).  Later corrections, which only refine that FP32 solution, use a
+ * truncated Neumann series of the same Jacobian J = I + K: delta = (I - K + K^2 - ...) b with nterm
+ * products K v (default 2), as long as each one cuts the certifying residual fourfold; a column
+ * whose residual does not contract (large vertical Courant numbers, where ||K|| is not small) goes
+ * back to LU corrections.  The converged state is the same: convergence is judged by the
+ * float-pair residual to tol either way.  nterm = 0: LU corrections only.  No counterpart in
+ * FElib, whose solve is a single LU correction. */
+int fedg_update_set_vi_neumann(fedg_ctx* ctx, int nterm);
+
 /* Column-guess network for the HEVI Newton solve (the learned initial iterate): a GELU MLP
  * (3L+1) -> hidden -> hidden -> 3L mapping a column's stage input (DDENS', MOMZ, DRHOT' at its
  * L = NeZ*N1 levels, then impl_fac, each times in_scale[var]) to the implicit increment
