@@ -80,6 +80,30 @@ __device__ __forceinline__ void face_exterior(const Ops& op, int f, int a, int b
   }
 }
 
+// Pivot order of the column solves' element LU (3*N1 rows: DENS, MOMZ, RHOT of node k are rows
+// 3k, 3k+1, 3k+2).
+// Pivot order and sparsity.  The DENS rows of an element block are
+//   I + (Lift face terms in the DENS columns of nodes 0 and N)
+//     + impl_fac E33 D (MOMZ columns) + (block-Thomas update: node-0 columns, RHOT_0 included),
+// so a DENS row has nonzeros only in DENS_k, DENS_0, DENS_N, the MOMZ columns and RHOT_0.  The
+// DENS pivots go first (DENS_0 .. DENS_N), then MOMZ/RHOT node by node.  A DENS pivot row then
+// carries at most DENS_N, the N1 MOMZ columns and RHOT_0 to the right, and eliminating DENS_i
+// (0 < i < N) leaves the other DENS rows untouched (their DENS_i entry is zero); what remains is
+// the dense 2*N1 system of the MOMZ/RHOT Schur complement.
+template <int N1>
+struct PivOrder {
+  // column (3 node + var) of pivot step s, and the step at which column c is pivoted
+  __host__ __device__ static constexpr int col(int s) { return s < N1 ? 3 * s : 3 * ((s - N1) / 2) + 1 + ((s - N1) & 1); }
+  __host__ __device__ static constexpr int pos(int c) { return c % 3 == 0 ? c / 3 : N1 + 2 * (c / 3) + (c % 3 - 1); }
+  // can the pivot row of step s hold a nonzero in column c (c not yet pivoted)?
+  __host__ __device__ static constexpr bool nz(int s, int c) {
+    if (pos(c) <= s) return false;
+    if (s >= N1) return true;  // MOMZ/RHOT phase: dense
+    return c == 3 * (N1 - 1) || c % 3 == 1 || c == 2;
+  }
+};
+
+
 __device__ __forceinline__ double warp_max(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));

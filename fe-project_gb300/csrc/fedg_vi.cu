@@ -32,11 +32,12 @@ __device__ __forceinline__ void warp_lu(double (&a)[n], double (&rhs)[nr], doubl
   mypiv = -1;
 #pragma unroll
   for (int k = 0; k < n; ++k) {
-    double bv = done ? -1.0 : fabs(a[k]);
+    // |a| compared as the integer bit pattern of a non-negative double: no FP64 instructions
+    long long bv = done ? -1LL : (__double_as_longlong(a[k]) & 0x7fffffffffffffffLL);
     int best = lane;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      const double ov = __shfl_xor_sync(0xffffffffu, bv, o);
+      const long long ov = __shfl_xor_sync(0xffffffffu, bv, o);
       const int ol = __shfl_xor_sync(0xffffffffu, best, o);
       if (ov > bv || (ov == bv && ol < best)) { bv = ov; best = ol; }
     }
@@ -76,6 +77,91 @@ __device__ __forceinline__ void warp_lu(double (&a)[n], double (&rhs)[nr], doubl
       if (mypiv >= 0 && mypiv < k) rhs[m] = fma(-a[k], xk, rhs[m]);
     }
   }
+  __syncwarp();
+}
+
+// Element-block LU of the column Newton solve in FP64: lane r < 3*N1 holds row r (DENS, MOMZ, RHOT
+// of node r/3) and its nr right-hand sides.  Pivot order PivOrder<N1> (fedg_common.cuh): the DENS
+// columns first, each pivoted on its own DENS row without a search (the DENS block is the identity
+// plus the small Lift face terms), then the MOMZ/RHOT columns of the dense Schur complement with
+// partial pivoting over the remaining rows.  The pivot search compares |a| as the bit pattern of a
+// non-negative double (monotonic as an integer), so it runs on the integer pipes, not on GB300's
+// scarce FP64 pipe; only the structurally nonzero columns of a pivot row are broadcast and
+// eliminated; each pivot's reciprocal is formed once and kept for the back substitution.
+// On return the lane that pivoted step s (plane[s]) holds x of column PivOrder::col(s) in rhs[].
+template <int N1, int nr, int s>
+__device__ __forceinline__ void lu_d_fwd(double (&a)[3 * N1], double (&rhs)[nr], double* prow, int* plane, int lane,
+                                         bool& done, int& mypiv, double& rpiv) {
+  constexpr int n = 3 * N1;
+  using O = PivOrder<N1>;
+  if constexpr (s < n) {
+    constexpr int pc = O::col(s);
+    int best;
+    if constexpr (s < N1) {
+      best = 3 * s;
+    } else {
+      long long bv = done ? -1LL : (__double_as_longlong(a[pc]) & 0x7fffffffffffffffLL);
+      best = lane;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const long long ov = __shfl_xor_sync(0xffffffffu, bv, o);
+        const int ol = __shfl_xor_sync(0xffffffffu, best, o);
+        if (ov > bv || (ov == bv && ol < best)) { bv = ov; best = ol; }
+      }
+    }
+    const bool piv = lane == best;
+    if (piv) {
+#pragma unroll
+      for (int c = 0; c < n; ++c)
+        if (O::nz(s, c)) prow[c] = a[c];
+#pragma unroll
+      for (int m = 0; m < nr; ++m) prow[n + m] = rhs[m];
+      rpiv = 1.0 / a[pc];
+      prow[n + nr] = rpiv;
+      plane[s] = lane;
+      mypiv = s;
+    }
+    __syncwarp();
+    if (!done && !piv) {
+      const double f = a[pc] * prow[n + nr];
+#pragma unroll
+      for (int c = 0; c < n; ++c)
+        if (O::nz(s, c)) a[c] = fma(-f, prow[c], a[c]);
+#pragma unroll
+      for (int m = 0; m < nr; ++m) rhs[m] = fma(-f, prow[n + m], rhs[m]);
+    }
+    done = done || piv;
+    __syncwarp();
+    lu_d_fwd<N1, nr, s + 1>(a, rhs, prow, plane, lane, done, mypiv, rpiv);
+  }
+}
+template <int N1, int nr, int s>
+__device__ __forceinline__ void lu_d_bwd(const double (&a)[3 * N1], double (&rhs)[nr], const int* plane, int mypiv,
+                                         double rpiv) {
+  using O = PivOrder<N1>;
+  if constexpr (s >= 0) {
+    constexpr int pc = O::col(s);
+    if (mypiv == s) {
+#pragma unroll
+      for (int m = 0; m < nr; ++m) rhs[m] *= rpiv;
+    }
+    const int src = plane[s];
+#pragma unroll
+    for (int m = 0; m < nr; ++m) {
+      const double xk = __shfl_sync(0xffffffffu, rhs[m], src);
+      if (mypiv >= 0 && mypiv < s) rhs[m] = fma(-a[pc], xk, rhs[m]);
+    }
+    lu_d_bwd<N1, nr, s - 1>(a, rhs, plane, mypiv, rpiv);
+  }
+}
+template <int N1, int nr>
+__device__ __forceinline__ void warp_lu_dfirst(double (&a)[3 * N1], double (&rhs)[nr], double* prow, int* plane,
+                                               int lane, int& mypiv) {
+  bool done = lane >= 3 * N1;
+  double rpiv = 0.0;
+  mypiv = -1;
+  lu_d_fwd<N1, nr, 0>(a, rhs, prow, plane, lane, done, mypiv, rpiv);
+  lu_d_bwd<N1, nr, 3 * N1 - 1>(a, rhs, plane, mypiv, rpiv);
   __syncwarp();
 }
 
@@ -254,12 +340,13 @@ __device__ void col_solve(ColCtx<N1>& c, double impl_fac) {
     }
     __syncwarp();
     int mypiv;
-    warp_lu<n3, 4>(a, rhs, c.prow, c.plane, lane, mypiv);
+    warp_lu_dfirst<N1, 4>(a, rhs, c.prow, c.plane, lane, mypiv);
     if (mypiv >= 0) {
-      c.bh[ez * n3 + mypiv] = rhs[0];
-      c.Gh[(ez * n3 + mypiv) * 3 + 0] = rhs[1];
-      c.Gh[(ez * n3 + mypiv) * 3 + 1] = rhs[2];
-      c.Gh[(ez * n3 + mypiv) * 3 + 2] = rhs[3];
+      const int xc = PivOrder<N1>::col(mypiv);  // the unknown this lane solved for
+      c.bh[ez * n3 + xc] = rhs[0];
+      c.Gh[(ez * n3 + xc) * 3 + 0] = rhs[1];
+      c.Gh[(ez * n3 + xc) * 3 + 1] = rhs[2];
+      c.Gh[(ez * n3 + xc) * 3 + 2] = rhs[3];
     }
     __syncwarp();
   }

@@ -37,6 +37,7 @@ namespace fedg {
 namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
+constexpr f2 Z2F{0.f, 0.f};
 
 // per-column shared-memory layout (bytes).  Three scratch areas whose phases never overlap share
 // one region: the residual's ring of level quantities, the correction's Jacobian quantities and
@@ -156,8 +157,18 @@ __device__ float col_residual(const OpsX& ox, const Col<N1>& c, const ProfX& px,
   __syncwarp();
   float errf = 0.f;
   const int gv[3] = {VD, VMZ, VRT};
+  // the stage input q* of the lane's node, loaded one element ahead so that the load latency
+  // overlaps the current element's work
+  float2 qcur[3], qnxt[3];
+#pragma unroll
+  for (int v = 0; v < 3; ++v) qcur[v] = __ldg(qin.v[gv[v]] + c.g(0));
   for (int e = 0; e < c.NeZ; ++e) {
     const int sc = e % 3, sb = (e + 2) % 3, st = (e + 1) % 3;
+    {
+      const size_t gn = c.g(e + 1 < c.NeZ ? e + 1 : e);
+#pragma unroll
+      for (int v = 0; v < 3; ++v) qnxt[v] = __ldg(qin.v[gv[v]] + gn);
+    }
     // vertical-face fluxes of element e: lanes over (side, variable)
     for (int t = k; t < 6; t += N1) {
       const int s = t / 3, v = t - 3 * s;
@@ -204,7 +215,6 @@ __device__ float col_residual(const OpsX& ox, const Col<N1>& c, const ProfX& px,
     __syncwarp();
     {
       const int l = e * N1 + k;
-      const size_t gi = c.g(e);
       const float isc[3] = {1.f / __ldg(px.dhf + l), 1.f / (__ldg(px.dhf + l) * cref), 1.f / __ldg(px.rhf + l)};
       float bfl[3];
       if constexpr (CERT) {
@@ -224,7 +234,7 @@ __device__ float col_residual(const OpsX& ox, const Col<N1>& c, const ProfX& px,
         A[2] = f2_add(f2_add(f2_mul(E33, sr.get()), f2_mul(lbk, f2_of(dl[2]))), f2_mul(ltk, f2_of(dl[5])));
 #pragma unroll
         for (int v = 0; v < 3; ++v) {  // A[v] holds -A: b = q* - P - impl_fac (-A)
-          const f2 qmp = f2_sub(f2_of(__ldg(qin.v[gv[v]] + gi)), f2_of(c.P[3 * l + v]));
+          const f2 qmp = f2_sub(f2_of(qcur[v]), f2_of(c.P[3 * l + v]));
           bfl[v] = f2_to_f(f2_sub(qmp, f2_mul(impl, A[v])));
         }
       } else {
@@ -243,7 +253,7 @@ __device__ float col_residual(const OpsX& ox, const Col<N1>& c, const ProfX& px,
         A[2] = E33.h * sr + lbk.h * dl[2] + ltk.h * dl[5];
 #pragma unroll
         for (int v = 0; v < 3; ++v) {
-          const float qmp = f2_to_f(f2_sub(f2_of(__ldg(qin.v[gv[v]] + gi)), f2_of(c.P[3 * l + v])));
+          const float qmp = f2_to_f(f2_sub(f2_of(qcur[v]), f2_of(c.P[3 * l + v])));
           bfl[v] = fmaf(-impl.h, A[v], qmp);
         }
       }
@@ -257,6 +267,8 @@ __device__ float col_residual(const OpsX& ox, const Col<N1>& c, const ProfX& px,
     __syncwarp();
     if (e + 2 < c.NeZ) fill(e + 2);
     __syncwarp();
+#pragma unroll
+    for (int v = 0; v < 3; ++v) qcur[v] = qnxt[v];
   }
   return grp_max_nan(errf, N1);
 }
@@ -267,28 +279,8 @@ __device__ float col_residual(const OpsX& ox, const Col<N1>& c, const ProfX& px,
 // the other lanes of the column group by shuffles (width N1); every register index is a
 // compile-time constant.
 //
-// Pivot order and sparsity.  The DENS rows of an element block are
-//   I + (Lift face terms in the DENS columns of nodes 0 and N)
-//     + impl_fac E33 D (MOMZ columns) + (block-Thomas update: node-0 columns, RHOT_0 included),
-// so a DENS row has nonzeros only in DENS_k, DENS_0, DENS_N, the MOMZ columns and RHOT_0.  The
-// DENS pivots go first (DENS_0 .. DENS_N), then MOMZ/RHOT node by node.  A DENS pivot row then
-// carries at most DENS_N, the N1 MOMZ columns and RHOT_0 to the right, and eliminating DENS_i
-// (0 < i < N) leaves the other DENS rows untouched (their DENS_i entry is zero); what remains is
-// the dense 2*N1 system of the MOMZ/RHOT Schur complement.  Against the natural order this
-// issues about a quarter fewer shuffles and half the FMAs.
-template <int N1>
-struct PivOrder {
-  // column (3 node + var) of pivot step s, and the step at which column c is pivoted
-  __host__ __device__ static constexpr int col(int s) { return s < N1 ? 3 * s : 3 * ((s - N1) / 2) + 1 + ((s - N1) & 1); }
-  __host__ __device__ static constexpr int pos(int c) { return c % 3 == 0 ? c / 3 : N1 + 2 * (c / 3) + (c % 3 - 1); }
-  // can the pivot row of step s hold a nonzero in column c (c not yet pivoted)?
-  __host__ __device__ static constexpr bool nz(int s, int c) {
-    if (pos(c) <= s) return false;
-    if (s >= N1) return true;  // MOMZ/RHOT phase: dense
-    return c == 3 * (N1 - 1) || c % 3 == 1 || c == 2;
-  }
-};
-
+// Pivot order and sparsity of the element blocks: PivOrder (fedg_common.cuh).  Against the natural
+// order the DENS-first order issues about a quarter fewer shuffles and half the FMAs.
 template <int N1, int s>
 __device__ __forceinline__ void shfl_fwd(float (&a)[3][3 * N1], float (&r)[3][4], int k) {
   constexpr int n = 3 * N1;
@@ -358,6 +350,177 @@ template <int N1>
 __device__ __forceinline__ void lu_rows(float (&a)[3][3 * N1], float (&r)[3][4], int k) {
   shfl_fwd<N1, 0>(a, r, k);
   shfl_bwd<N1, 3 * N1 - 1>(a, r, k);
+}
+
+// The same elimination in blocked form, which shortens its chain of dependent steps from 3*N1
+// pivots forward and back to about N1 + 3 (restated and checked against a dense solve in numpy:
+// tests/test_lu_order.py, blocked_solve):
+//   - DENS_0, then DENS_1 .. DENS_{N-1} together: once DENS_0 is eliminated their pivot rows and
+//     the other rows' multipliers are final (a DENS pivot row carries only DENS_N, the MOMZ columns
+//     and RHOT_0, none of which is a DENS_1 .. DENS_{N-1} column), so their updates are independent
+//     sums; then DENS_N;
+//   - the MOMZ/RHOT Schur complement node by node with 2x2 pivot blocks (MOMZ_k, RHOT_k), whose
+//     inverse lane k forms and keeps for the back substitution;
+//   - back substitution block by block, then DENS_N, then DENS_0 .. DENS_{N-1} in parallel.
+// Rows 3k+v live in lane k (a[v][.], right-hand sides r[v][.]); no pivoting, as in lu_rows.
+template <int N1>
+struct DensCols {  // the columns a DENS pivot row can hold: the MOMZ columns, RHOT_0, DENS_N
+  static constexpr int count = N1 + 2;
+  __host__ __device__ static constexpr int at(int i) { return i < N1 ? 3 * i + 1 : (i == N1 ? 2 : 3 * (N1 - 1)); }
+};
+template <int N1, int kb>
+__device__ __forceinline__ void blk_fwd(float (&a)[3][3 * N1], float (&r)[3][4], int k, float (&pinv)[4]) {
+  if constexpr (kb < N1) {
+    constexpr int c1 = 3 * kb + 1, c2 = 3 * kb + 2;
+    if (k == kb) {  // 2x2 pivot block of node kb
+      const float p11 = a[1][c1], p12 = a[1][c2], p21 = a[2][c1], p22 = a[2][c2];
+      const float id = __fdividef(1.f, fmaf(p11, p22, -p12 * p21));
+      pinv[0] = p22 * id; pinv[1] = -p12 * id; pinv[2] = -p21 * id; pinv[3] = p11 * id;
+    }
+    float q[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) q[i] = __shfl_sync(FULL, pinv[i], kb, N1);
+    // multipliers [f1 f2] = [a_c1 a_c2] P^-1 of this lane's MOMZ/RHOT rows (nodes after kb)
+    float f1[3], f2[3];
+    const bool el = k > kb;
+#pragma unroll
+    for (int v = 1; v < 3; ++v) {
+      f1[v] = el ? fmaf(a[v][c1], q[0], a[v][c2] * q[2]) : 0.f;
+      f2[v] = el ? fmaf(a[v][c1], q[1], a[v][c2] * q[3]) : 0.f;
+    }
+#pragma unroll
+    for (int m = kb + 1; m < N1; ++m) {
+#pragma unroll
+      for (int u = 1; u < 3; ++u) {
+        const int cc = 3 * m + u;
+        const float p1 = __shfl_sync(FULL, a[1][cc], kb, N1), p2 = __shfl_sync(FULL, a[2][cc], kb, N1);
+#pragma unroll
+        for (int v = 1; v < 3; ++v) a[v][cc] = fmaf(-f1[v], p1, fmaf(-f2[v], p2, a[v][cc]));
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const float p1 = __shfl_sync(FULL, r[1][m], kb, N1), p2 = __shfl_sync(FULL, r[2][m], kb, N1);
+#pragma unroll
+      for (int v = 1; v < 3; ++v) r[v][m] = fmaf(-f1[v], p1, fmaf(-f2[v], p2, r[v][m]));
+    }
+    blk_fwd<N1, kb + 1>(a, r, k, pinv);
+  }
+}
+template <int N1, int kb>
+__device__ __forceinline__ void blk_bwd(const float (&a)[3][3 * N1], float (&r)[3][4], int k, const float (&pinv)[4]) {
+  if constexpr (kb >= 0) {
+    constexpr int c1 = 3 * kb + 1, c2 = 3 * kb + 2;
+    if (k == kb) {  // x of the block: P^-1 times the reduced right-hand side
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        const float y1 = r[1][m], y2 = r[2][m];
+        r[1][m] = fmaf(pinv[0], y1, pinv[1] * y2);
+        r[2][m] = fmaf(pinv[2], y1, pinv[3] * y2);
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const float x1 = __shfl_sync(FULL, r[1][m], kb, N1), x2 = __shfl_sync(FULL, r[2][m], kb, N1);
+      // DENS rows: the MOMZ columns, and RHOT_0 (column 2) for block 0
+      r[0][m] = fmaf(-a[0][c1], x1, kb == 0 ? fmaf(-a[0][2], x2, r[0][m]) : r[0][m]);
+      if (k < kb) {
+#pragma unroll
+        for (int v = 1; v < 3; ++v) r[v][m] = fmaf(-a[v][c1], x1, fmaf(-a[v][c2], x2, r[v][m]));
+      }
+    }
+    blk_bwd<N1, kb - 1>(a, r, k, pinv);
+  }
+}
+template <int N1>
+__device__ __forceinline__ void lu_blocked(float (&a)[3][3 * N1], float (&r)[3][4], int k) {
+  constexpr int N = N1 - 1;
+  using DC = DensCols<N1>;
+  // DENS_0: every other row, the DENS_0 pivot row's columns only
+  {
+    const float inv = __fdividef(1.f, __shfl_sync(FULL, a[0][0], 0, N1));
+    const float f[3] = {k > 0 ? a[0][0] * inv : 0.f, a[1][0] * inv, a[2][0] * inv};
+#pragma unroll
+    for (int i = 0; i < DC::count; ++i) {
+      const int cc = DC::at(i);
+      const float p = __shfl_sync(FULL, a[0][cc], 0, N1);
+#pragma unroll
+      for (int v = 0; v < 3; ++v) a[v][cc] = fmaf(-f[v], p, a[v][cc]);
+    }
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const float p = __shfl_sync(FULL, r[0][m], 0, N1);
+#pragma unroll
+      for (int v = 0; v < 3; ++v) r[v][m] = fmaf(-f[v], p, r[v][m]);
+    }
+  }
+  // this lane's DENS pivot reciprocal (final once DENS_0 is eliminated; lane 0's is the DENS_0 pivot)
+  float dg = a[0][0];
+#pragma unroll
+  for (int j = 1; j < N1; ++j) dg = k == j ? a[0][3 * j] : dg;
+  const float rdk = __fdividef(1.f, dg);
+  // DENS_1 .. DENS_{N-1} together: MOMZ/RHOT rows only (the DENS rows hold no DENS_j, 0 < j < N)
+  if constexpr (N1 > 2) {
+    float f1[N1], f2[N1];
+#pragma unroll
+    for (int j = 1; j < N; ++j) {
+      const float inv = __shfl_sync(FULL, rdk, j, N1);
+      f1[j] = a[1][3 * j] * inv;
+      f2[j] = a[2][3 * j] * inv;
+    }
+#pragma unroll
+    for (int i = 0; i < DC::count; ++i) {
+      const int cc = DC::at(i);
+      float s1 = a[1][cc], s2 = a[2][cc];
+#pragma unroll
+      for (int j = 1; j < N; ++j) {
+        const float p = __shfl_sync(FULL, a[0][cc], j, N1);
+        s1 = fmaf(-f1[j], p, s1);
+        s2 = fmaf(-f2[j], p, s2);
+      }
+      a[1][cc] = s1;
+      a[2][cc] = s2;
+    }
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      float s1 = r[1][m], s2 = r[2][m];
+#pragma unroll
+      for (int j = 1; j < N; ++j) {
+        const float p = __shfl_sync(FULL, r[0][m], j, N1);
+        s1 = fmaf(-f1[j], p, s1);
+        s2 = fmaf(-f2[j], p, s2);
+      }
+      r[1][m] = s1;
+      r[2][m] = s2;
+    }
+  }
+  // DENS_N: MOMZ/RHOT rows, the MOMZ columns and RHOT_0
+  {
+    const float inv = __shfl_sync(FULL, rdk, N, N1);
+    const float f1 = a[1][3 * N] * inv, f2 = a[2][3 * N] * inv;
+#pragma unroll
+    for (int i = 0; i < DC::count - 1; ++i) {
+      const int cc = DC::at(i);
+      const float p = __shfl_sync(FULL, a[0][cc], N, N1);
+      a[1][cc] = fmaf(-f1, p, a[1][cc]);
+      a[2][cc] = fmaf(-f2, p, a[2][cc]);
+    }
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const float p = __shfl_sync(FULL, r[0][m], N, N1);
+      r[1][m] = fmaf(-f1, p, r[1][m]);
+      r[2][m] = fmaf(-f2, p, r[2][m]);
+    }
+  }
+  float pinv[4] = {0.f, 0.f, 0.f, 0.f};
+  blk_fwd<N1, 0>(a, r, k, pinv);
+  blk_bwd<N1, N>(a, r, k, pinv);
+  // DENS_N, then the other DENS unknowns in parallel
+#pragma unroll
+  for (int m = 0; m < 4; ++m) {
+    const float xn = __shfl_sync(FULL, r[0][m] * rdk, N, N1);
+    r[0][m] = k == N ? xn : fmaf(-a[0][3 * N], xn, r[0][m]) * rdk;
+  }
 }
 
 // FP32 Jacobian level quantities of level l from the iterate: pot = RHOT/DENS, wt = MOMZ/DENS,
@@ -522,14 +685,24 @@ __device__ void col_solve(const Ops& op, const ProfX& px, float kapf, const Col<
     }
     __syncwarp();
   }
-  // back sweep: x_e = y_e - G_e x_{e+1}(node 0)
+  // back sweep: x_e = y_e - G_e x_{e+1}(node 0); the history of element e-1 is loaded while e is
+  // processed
+  float4 g0n = make_float4(0.f, 0.f, 0.f, 0.f), g1n = g0n;
+  float g2n = 0.f;
+  if (c.NeZ >= 2) {
+    const size_t gn = (gcol + (size_t)(c.NeZ - 2) * glayer) * N1 + k;
+    g0n = *gh.p0(gn); g1n = *gh.p1(gn); g2n = *gh.p2(gn);
+  }
   for (int e = c.NeZ - 2; e >= 0; --e) {
     const int l = e * N1 + k;
     const float* x1 = c.Bf + 3 * (e + 1) * N1;
     const float xa = x1[0], xb = x1[1], xc = x1[2];
-    const size_t gn = (gcol + (size_t)e * glayer) * N1 + k;
-    const float4 g0 = *gh.p0(gn), g1 = *gh.p1(gn);
-    const float g2 = *gh.p2(gn);
+    const float4 g0 = g0n, g1 = g1n;
+    const float g2 = g2n;
+    if (e > 0) {
+      const size_t gn = (gcol + (size_t)(e - 1) * glayer) * N1 + k;
+      g0n = *gh.p0(gn); g1n = *gh.p1(gn); g2n = *gh.p2(gn);
+    }
     c.Bf[3 * l + 0] -= g0.x * xa + g0.y * xb + g0.z * xc;
     c.Bf[3 * l + 1] -= g0.w * xa + g1.x * xb + g1.y * xc;
     c.Bf[3 * l + 2] -= g1.z * xa + g1.w * xb + g2 * xc;
@@ -688,12 +861,17 @@ __global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, 
 
   // ---- frozen vertical Rusanov speed |w| + c of var0 (hevi_common_2.F90:1149-1155) ----
   float* atmp = c.Bf;  // [L]
+  // global loads one element ahead of their use, here and in the loops below
+  double zc[3] = {__ldg(z.v[VD] + c.g(0)), __ldg(z.v[VMZ] + c.g(0)), __ldg(z.v[VRT] + c.g(0))};
   for (int e = 0; e < NeZ; ++e) {
     const int l = e * N1 + k;
-    const size_t gi = c.g(e);
-    const float dd0 = f2_split(__ldg(z.v[VD] + gi)).h, dr0 = f2_split(__ldg(z.v[VRT] + gi)).h;
+    const size_t gn = c.g(e + 1 < NeZ ? e + 1 : e);
+    const double zn[3] = {__ldg(z.v[VD] + gn), __ldg(z.v[VMZ] + gn), __ldg(z.v[VRT] + gn)};
+    const float dd0 = f2_split(zc[0]).h, dr0 = f2_split(zc[2]).h;
     const float rdens0 = 1.f / (__ldg(px.dhf + l) + dd0);
-    const float wt0 = f2_split(__ldg(z.v[VMZ] + gi)).h * rdens0;
+    const float wt0 = f2_split(zc[1]).h * rdens0;
+#pragma unroll
+    for (int v = 0; v < 3; ++v) zc[v] = zn[v];
     const float pres0 = __ldg(px.phf + l) * (1.f + expm1f(kapf * log1pf(dr0 * __ldg(px.rthf + l))));
     atmp[l] = fabsf(wt0) + sqrtf(kapf * pres0 * rdens0);
   }
@@ -714,20 +892,31 @@ __global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, 
     float2* E = reinterpret_cast<float2*>(c.P);         // [2L] P - q* (float pair)
     float* jq = reinterpret_cast<float*>(c.P) + 4 * L;  // [4 NeZ] face jumps of q*
     float* bu = c.Bf;                                   // [2L] residual
-    const size_t g0 = c.gb - (size_t)NF * k;            // node (0, 0) of this column
-    auto gl = [&](int l) { return g0 + (size_t)(l / N1) * c.gs + (size_t)NF * (l % N1); };
+    // E = var0 - q* at every node; the bottom/top jumps (neighbour - own) of q* MOMX/MOMY from the
+    // face nodes' values, passed between lanes by shuffles: jq[4e + m] = q*(e-1, N) - q*(e, 0),
+    // jq[4e + 2 + m] = q*(e+1, 0) - q*(e, N), zero at the lids
+    double zu[2] = {__ldg(z.v[VMX] + c.g(0)), __ldg(z.v[VMY] + c.g(0))};
+    float2 qu[2] = {__ldg(qin.v[VMX] + c.g(0)), __ldg(qin.v[VMY] + c.g(0))};
+    f2 qtop[2] = {Z2F, Z2F};  // q*(e-1, N)
     for (int e = 0; e < NeZ; ++e) {
       const int l = e * N1 + k;
-      const size_t gi = c.g(e);
+      const size_t gn = c.g(e + 1 < NeZ ? e + 1 : e);
+      const double zn[2] = {__ldg(z.v[VMX] + gn), __ldg(z.v[VMY] + gn)};
+      const float2 qnx[2] = {__ldg(qin.v[VMX] + gn), __ldg(qin.v[VMY] + gn)};
 #pragma unroll
-      for (int m = 0; m < 2; ++m)
-        E[2 * l + m] = f2_pack(f2_sub(f2_split(__ldg(z.v[VMX + m] + gi)), f2_of(__ldg(qin.v[VMX + m] + gi))));
-      for (int t = k; t < 4; t += N1) {  // bottom/top jump (neighbour - own) of q* MOMX/MOMY
-        const int s = t >> 1, m = t & 1;
-        const int lM = e * N1 + (s == 0 ? 0 : N);
-        const bool lid = s == 0 ? (e == 0) : (e == NeZ - 1);
-        const int lP = lid ? lM : (s == 0 ? lM - 1 : lM + 1);
-        jq[4 * e + t] = lid ? 0.f : f2_to_f(f2_sub(f2_of(__ldg(qin.v[VMX + m] + gl(lP))), f2_of(__ldg(qin.v[VMX + m] + gl(lM)))));
+      for (int m = 0; m < 2; ++m) {
+        const f2 qs = f2_of(qu[m]);
+        E[2 * l + m] = f2_pack(f2_sub(f2_split(zu[m]), qs));
+        const f2 q0{__shfl_sync(FULL, qs.h, 0, N1), __shfl_sync(FULL, qs.l, 0, N1)};
+        const f2 qN{__shfl_sync(FULL, qs.h, N, N1), __shfl_sync(FULL, qs.l, N, N1)};
+        if (k == 0) {
+          jq[4 * e + m] = e == 0 ? 0.f : f2_to_f(f2_sub(qtop[m], q0));
+          if (e > 0) jq[4 * (e - 1) + 2 + m] = f2_to_f(f2_sub(q0, qtop[m]));
+          if (e == NeZ - 1) jq[4 * e + 2 + m] = 0.f;
+        }
+        qtop[m] = qN;
+        zu[m] = zn[m];
+        qu[m] = qnx[m];
       }
     }
     __syncwarp();
@@ -807,15 +996,22 @@ __global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, 
       active = need;
       __syncwarp();
     }
+    float2 qo[2] = {__ldg(qin.v[VMX] + c.g(0)), __ldg(qin.v[VMY] + c.g(0))};
     for (int e = 0; e < NeZ; ++e) {
       const int l = e * N1 + k;
       const size_t gi = c.g(e);
+      const float2 qc[2] = {qo[0], qo[1]};
+      {
+        const size_t gn = c.g(e + 1 < NeZ ? e + 1 : e);
+        qo[0] = __ldg(qin.v[VMX] + gn);
+        qo[1] = __ldg(qin.v[VMY] + gn);
+      }
       const f2 dh = f2_of(__ldg(px.dh + l));
 #pragma unroll
       for (int m = 0; m < 2; ++m) {
         const f2 ref = f2_mul(dh, f2_of(m == 0 ? ox.Uref : ox.Vref));
         const f2 inc = f2_of(E[2 * l + m]);  // P - q*
-        const f2 pdev = f2_add(f2_sub(f2_of(__ldg(qin.v[VMX + m] + gi)), ref), inc);
+        const f2 pdev = f2_add(f2_sub(f2_of(qc[m]), ref), inc);
         if constexpr (PO) {
           static_cast<float2*>(qsf[VMX + m])[gi] = f2_pack(pdev);
           static_cast<float2*>(tout[VMX + m])[gi] = f2_pack(f2_mul(inc, f2_of(args.inv_impl2)));
@@ -830,6 +1026,7 @@ __global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, 
 
   // ---- DENS/MOMZ/RHOT Newton ----
   const int gv[3] = {VD, VMZ, VRT};
+#pragma unroll 4
   for (int e = 0; e < NeZ; ++e) {
     const int l = e * N1 + k;
     const size_t gi = c.g(e);
@@ -870,13 +1067,22 @@ __global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, 
     else col_neumann<N1>(op, px, kapf, c, args.impl_fac, args.neumann, active);
     ++nsolve;
   }
+  float2 qo[3];
+#pragma unroll
+  for (int m = 0; m < 3; ++m) qo[m] = __ldg(qin.v[gv[m]] + c.g(0));
   for (int e = 0; e < NeZ; ++e) {
     const int l = e * N1 + k;
     const size_t gi = c.g(e);
+    const float2 qc[3] = {qo[0], qo[1], qo[2]};
+    {
+      const size_t gn = c.g(e + 1 < NeZ ? e + 1 : e);
+#pragma unroll
+      for (int m = 0; m < 3; ++m) qo[m] = __ldg(qin.v[gv[m]] + gn);
+    }
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
       const f2 pnew = f2_of(c.P[3 * l + m]);
-      const f2 inc = f2_sub(pnew, f2_of(__ldg(qin.v[gv[m]] + gi)));
+      const f2 inc = f2_sub(pnew, f2_of(qc[m]));
       if constexpr (PO) {
         static_cast<float2*>(qsf[gv[m]])[gi] = f2_pack(pnew);
         static_cast<float2*>(tout[gv[m]])[gi] = f2_pack(f2_mul(inc, f2_of(args.inv_impl2)));
