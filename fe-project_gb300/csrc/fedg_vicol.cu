@@ -275,86 +275,12 @@ __device__ float col_residual(const OpsX& ox, const Col<N1>& c, const ProfX& px,
 
 // ---------------------------------------------------------------------------------------------
 // Element LU without pivoting of the 3*N1 rows held 3 per lane (row 3k+v in lane k: v = DENS,
-// MOMZ, RHOT of node k), with four right-hand sides; on return r = A^-1 r.  The pivot row reaches
-// the other lanes of the column group by shuffles (width N1); every register index is a
-// compile-time constant.
-//
-// Pivot order and sparsity of the element blocks: PivOrder (fedg_common.cuh).  Against the natural
-// order the DENS-first order issues about a quarter fewer shuffles and half the FMAs.
-template <int N1, int s>
-__device__ __forceinline__ void shfl_fwd(float (&a)[3][3 * N1], float (&r)[3][4], int k) {
-  constexpr int n = 3 * N1;
-  using O = PivOrder<N1>;
-  if constexpr (s < n) {
-    constexpr int pc = O::col(s), owner = pc / 3, vv = pc % 3;
-    // rows still to eliminate: DENS rows only at the first step (the DENS_0 column), MOMZ/RHOT
-    // rows until their own pivot
-    constexpr bool drows = s == 0;
-    const float piv = __shfl_sync(FULL, a[vv][pc], owner, N1);
-    const float inv = __fdividef(1.f, piv);
-    float f[3];
-    f[0] = (drows && k > 0) ? a[0][pc] * inv : 0.f;
-#pragma unroll
-    for (int v = 1; v < 3; ++v) f[v] = (O::pos(3 * k + v) > s) ? a[v][pc] * inv : 0.f;
-#pragma unroll
-    for (int cc = 0; cc < n; ++cc) {
-      if (O::nz(s, cc)) {  // constant after unrolling
-        const float p = __shfl_sync(FULL, a[vv][cc], owner, N1);
-        if (drows) a[0][cc] = fmaf(-f[0], p, a[0][cc]);
-#pragma unroll
-        for (int v = 1; v < 3; ++v) a[v][cc] = fmaf(-f[v], p, a[v][cc]);
-      }
-    }
-#pragma unroll
-    for (int m = 0; m < 4; ++m) {
-      const float p = __shfl_sync(FULL, r[vv][m], owner, N1);
-      if (drows) r[0][m] = fmaf(-f[0], p, r[0][m]);
-#pragma unroll
-      for (int v = 1; v < 3; ++v) r[v][m] = fmaf(-f[v], p, r[v][m]);
-    }
-    shfl_fwd<N1, s + 1>(a, r, k);
-  }
-}
-template <int N1, int s>
-__device__ __forceinline__ void shfl_bwd(float (&a)[3][3 * N1], float (&r)[3][4], int k) {
-  using O = PivOrder<N1>;
-  if constexpr (s >= 0) {
-    constexpr int pc = O::col(s), owner = pc / 3, vv = pc % 3;
-    const float inv = __fdividef(1.f, __shfl_sync(FULL, a[vv][pc], owner, N1));
-    float x[4];
-#pragma unroll
-    for (int m = 0; m < 4; ++m) x[m] = __shfl_sync(FULL, r[vv][m], owner, N1) * inv;
-    // rows pivoted before step s that can hold a nonzero in column pc: DENS rows for the MOMZ
-    // columns, RHOT_0 and DENS_N; MOMZ/RHOT rows in the MOMZ/RHOT phase
-    constexpr bool dcol = (pc % 3 == 1) || pc == 2 || pc == 3 * (N1 - 1);
-#pragma unroll
-    for (int v = 0; v < 3; ++v) {
-      if (v == 0 && !dcol) {
-        if (k == owner && vv == 0) {
-#pragma unroll
-          for (int m = 0; m < 4; ++m) r[0][m] = x[m];
-        }
-        continue;
-      }
-      if (v > 0 && s < N1) continue;  // DENS pivots: MOMZ/RHOT rows come later in the order
-      const int row = 3 * k + v;
-      const bool before = O::pos(row) < s;
-      const float g = before ? a[v][pc] : 0.f;
-#pragma unroll
-      for (int m = 0; m < 4; ++m) r[v][m] = row == pc ? x[m] : fmaf(-g, x[m], r[v][m]);
-    }
-    shfl_bwd<N1, s - 1>(a, r, k);
-  }
-}
-template <int N1>
-__device__ __forceinline__ void lu_rows(float (&a)[3][3 * N1], float (&r)[3][4], int k) {
-  shfl_fwd<N1, 0>(a, r, k);
-  shfl_bwd<N1, 3 * N1 - 1>(a, r, k);
-}
-
-// The same elimination in blocked form, which shortens its chain of dependent steps from 3*N1
-// pivots forward and back to about N1 + 3 (restated and checked against a dense solve in numpy:
-// tests/test_lu_order.py, blocked_solve):
+// MOMZ, RHOT of node k), with four right-hand sides; on return r = A^-1 r.  Pivot rows reach the
+// other lanes of the column group by shuffles (width N1); every register index is a compile-time
+// constant.  The elimination follows the DENS-first order of PivOrder (fedg_common.cuh) in blocked
+// form, which shortens the chain of dependent steps from 3*N1 pivots forward and back to about
+// N1 + 3 (restated and checked against a dense solve in numpy: tests/test_lu_order.py,
+// blocked_solve):
 //   - DENS_0, then DENS_1 .. DENS_{N-1} together: once DENS_0 is eliminated their pivot rows and
 //     the other rows' multipliers are final (a DENS pivot row carries only DENS_N, the MOMZ columns
 //     and RHOT_0, none of which is a DENS_1 .. DENS_{N-1} column), so their updates are independent
@@ -362,7 +288,8 @@ __device__ __forceinline__ void lu_rows(float (&a)[3][3 * N1], float (&r)[3][4],
 //   - the MOMZ/RHOT Schur complement node by node with 2x2 pivot blocks (MOMZ_k, RHOT_k), whose
 //     inverse lane k forms and keeps for the back substitution;
 //   - back substitution block by block, then DENS_N, then DENS_0 .. DENS_{N-1} in parallel.
-// Rows 3k+v live in lane k (a[v][.], right-hand sides r[v][.]); no pivoting, as in lu_rows.
+// No pivoting: I + impl_fac J is diagonally dominant at stable time steps; a failure shows as a
+// non-converging or non-finite certifying residual, reported per column.
 template <int N1>
 struct DensCols {  // the columns a DENS pivot row can hold: the MOMZ columns, RHOT_0, DENS_N
   static constexpr int count = N1 + 2;
@@ -668,7 +595,7 @@ __device__ void col_solve(const Ops& op, const ProfX& px, float kapf, const Col<
 #pragma unroll
       for (int j = 0; j < 3; ++j) r[v][1 + j] = last ? 0.f : Uc[v][j];
     __syncwarp();  // everyone has read c.bc
-    lu_rows<N1>(a, r, k);
+    lu_blocked<N1>(a, r, k);
 #pragma unroll
     for (int v = 0; v < 3; ++v) c.Bf[3 * l + v] = r[v][0];
     if (!last) {  // the last element's G is zero and never read

@@ -1,12 +1,14 @@
-"""The pivot order and skip rules of the column solve's element LU (fe-project_gb300/csrc/fedg_vicol.cu,
-PivOrder / shfl_fwd / shfl_bwd), restated step for step in numpy and checked against a dense solve.
+"""The pivot order and skip rules of the column solves' element LU (PivOrder, fe-project_gb300/csrc/
+fedg_common.cuh), restated step for step in numpy and checked against a dense solve, with the two forms
+the kernels use: the blocked form of the FP32 column solve (fedg_vicol.cu, lu_blocked) and the FP64 one
+with partial pivoting in the MOMZ/RHOT phase (fedg_vi.cu, warp_lu_dfirst).
 
 The element block of the DENS/MOMZ/RHOT system has rows 3k+v (node k, variable v = DENS, MOMZ,
 RHOT).  A DENS row has nonzeros only in DENS_k, DENS_0, DENS_N, the MOMZ columns and RHOT_0, so the
-kernel pivots on DENS_0 .. DENS_N first (updating the other DENS rows only at the DENS_0 step, and
-shuffling only DENS_N, the MOMZ columns and RHOT_0 of a DENS pivot row), then on MOMZ/RHOT node by
+order pivots on DENS_0 .. DENS_N first (updating the other DENS rows only at the DENS_0 step, and
+carrying only DENS_N, the MOMZ columns and RHOT_0 of a DENS pivot row), then on MOMZ/RHOT node by
 node; the back substitution skips the same structural zeros.  Matrices with that sparsity and a
-dominant diagonal (no pivoting, as in the kernel) must be solved to roundoff.
+dominant diagonal (no pivoting, as in the FP32 kernel) must be solved to roundoff.
 """
 import numpy as np
 import pytest
@@ -31,7 +33,7 @@ def nz(s, c, N1):
 def structured_solve(A, R, N1):
     n = 3 * N1
     a, r = A.copy(), R.copy()
-    for s in range(n):  # forward elimination (shfl_fwd)
+    for s in range(n):  # forward elimination, one pivot at a time
         pc = col(s, N1)
         inv = 1.0 / a[pc, pc]
         prow, pr = a[pc].copy(), r[pc].copy()
@@ -50,7 +52,7 @@ def structured_solve(A, R, N1):
                     if nz(s, c, N1):
                         a[row, c] -= f * prow[c]
                 r[row] -= f * pr
-    for s in range(n - 1, -1, -1):  # back substitution (shfl_bwd)
+    for s in range(n - 1, -1, -1):  # back substitution
         pc = col(s, N1)
         x = r[pc] / a[pc, pc]
         dcol = pc % 3 == 1 or pc == 2 or pc == 3 * (N1 - 1)
