@@ -781,6 +781,11 @@ int fedg_update_set_vi_neumann(fedg_ctx* c, int nterm) {
   c->vi_neumann = nterm;
   return 0;
 }
+int fedg_update_set_wait_limit(fedg_ctx* c, int polls) {
+  if (!c || polls < 0) return fail("fedg_update_set_wait_limit: bad argument");
+  c->tc_polls = polls;
+  return 0;
+}
 int fedg_guess_set_wait_limit(fedg_guess* g, int polls) {
   if (!g || polls < 0) return fail("fedg_guess_set_wait_limit: bad argument");
   return mlp_set_poll_limit(reinterpret_cast<MlpState*>(g), polls) ? fail("fedg_guess_set_wait_limit") : 0;

@@ -46,6 +46,12 @@ struct fedg_ctx {
   // Jacobian-vector products of the Neumann corrections of the float-pair/FP32 column solve
   // (fedg_update_set_vi_neumann; 0: LU corrections only)
   int vi_neumann = 2;
+  // poll limit of the update path's tensor-core barrier waits (fedg_update_set_wait_limit)
+  int tc_polls = 1 << 20;
+  // reference wind of the fast paths given by a restart file (fedg_restart_read) instead of taken
+  // from the first state they see
+  bool wind_given = false;
+  double wind[2] = {0.0, 0.0};
   // kernel timers / launch counters
   bool prof_on = false;
   long long nlaunch[FEDG_K_COUNT] = {};
@@ -65,6 +71,10 @@ int numdiff_apply_pair(fedg_ctx* c, double* const q[5], int nlap, double coef_h,
 // sponge-layer coefficient at the L LGL levels of the column (dgm_spongelayer.F90): 0.25/tau
 // (1 + sign(z - h)) (1 - cos(pi (z - h) / (z_top - h)))
 void sponge_coef_host(const fedg_ctx* c, double tau, double height, double* coef);
+// the fast update paths' reference wind (fedg_mixed.cu): false if none has been fixed yet
+bool ref_wind(const fedg_ctx* c, double out[2]);
+// fixes the reference wind of the fast update paths (from a restart file)
+void set_ref_wind_given(fedg_ctx* c, double U, double V);
 // fedg_cal_tend_ex_noalloc's set-up (fedg_static.cu): looks up its static scratch array on device `dev`,
 // the current device, which loads the module holding it; called by fedg_ctx_create
 void noalloc_setup(int dev);

@@ -22,6 +22,7 @@
 // accumulation, the Newton iterate and its certifying residual; the Jacobian and its LU in FP32
 // (the pair residual judges convergence, so the converged state is FP64-class); the prognostic
 // state stays FP64.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -29,6 +30,7 @@
 #include "fedg_ctx.cuh"
 #include "fedg_f2.cuh"
 #include "fedg_mlp.cuh"
+#include "fedg_umma.cuh"
 
 namespace fedg {
 
@@ -51,7 +53,44 @@ struct StageBufs {
   int xdinp;            // row length of X
   float xs[3];          // feature scales of DDENS', MOMZ, DRHOT'
   double* dtrc;         // stage 3: DDENS before the modal filter (DDENS_TRC of the tracer flux; NULL: none)
+  int* tc_err;          // raised when a tensor-core contraction's barrier wait runs out
+  int tc_polls;         // poll limit of that wait
 };
+
+// ---- derivative contractions on the tensor cores (BF16x3 split, FP32 accumulation) ----
+// The 15 flux components of an element group are each differentiated along one direction (F_x
+// along x, F_y along y, F_z along z): with D the 1D derivative matrix, one GEMM
+//   C[row, o] = sum_l F[row, l] D[o, l]
+// whose rows are (direction, component, element, line of N1 nodes along the direction) and whose
+// K index is the node l along the line.  Each FP32 flux value f is split exactly into three BF16
+// slices f0 + f1 + f2 (f0 = bf16(f), f1 = bf16(f - f0), f2 = bf16(f - f0 - f1)), and so is D; the
+// six slice products with i + j <= 2 are accumulated in FP32 by the tensor core, which reproduces
+// FP32-class products (the dropped terms are below 2^-32 of |f||D|), as the 3xTF32 split does with
+// TF32 slices.  A row holds its three slices in K slots [8 s, 8 s + N1) of a K = 32 operand (the
+// remaining slots zero); B (K = 32 x N = 32) holds in column group g (N slots [8 g, 8 g + N1)) the
+// D slice g for the A slices s <= 2 - g, so out[o] = C[o] + C[8 + o] + C[16 + o].
+// tcgen05.mma kind::f16, M = 128, N = 32, K = 16 (two K steps per 128-row tile), FP32 accumulators
+// in TMEM (32 columns per tile), operands in shared memory in the no-swizzle K-major canonical
+// layout (8-row x 16-byte core matrices: K neighbours 128 B apart, 8-row groups 512 B apart).
+template <int N1, int EPB>
+struct TcGeom {
+  static constexpr int NF = N1 * N1, Np = N1 * N1 * N1;
+  static constexpr int ROWS = 15 * EPB * NF;           // 960 for (N1, EPB) = (8, 1) and (4, 4)
+  static constexpr int TILES = (ROWS + 127) / 128;
+  static constexpr int A_BYTES = TILES * 128 * 64;    // BF16, K = 32
+  static constexpr int B_BYTES = 32 * 64;
+  static constexpr uint32_t TMEM_COLS = 256;          // 32 per tile, power of two >= TILES * 32
+  static_assert(TILES * 32 <= (int)TMEM_COLS, "accumulator columns");
+  static_assert(15 * EPB * Np * 4 <= A_BYTES, "the derivative outputs reuse the operand region");
+};
+// BF16 element index of (row r, K slot kk) in the canonical layout
+__device__ __forceinline__ int tc_idx(int r, int kk) { return ((r >> 3) * 4 + (kk >> 3)) * 64 + (r & 7) * 8 + (kk & 7); }
+__device__ __forceinline__ void bf16x3(float f, __nv_bfloat16& a, __nv_bfloat16& b, __nv_bfloat16& c) {
+  a = __float2bfloat16_rn(f);
+  const float r1 = f - __bfloat162float(a);
+  b = __float2bfloat16_rn(r1);
+  c = __float2bfloat16_rn(r1 - __bfloat162float(b));
+}
 
 // PRES - PRES_hyd = PRES_hyd ((1 + DRHOT/THERM_hyd)^kappa - 1)   (nonhydro3d_common.F90:470-474)
 __device__ __forceinline__ float dpres_f(float dr, float rth, float ph, float kap) {
@@ -78,13 +117,18 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
     k_stage_mixed(const OpsF op, const ProfF pf, const double* __restrict__ dens64, const StageBufs B,
                   const MixCoef cf, int Ne, int filter_on) {
   constexpr int Np = N1 * N1 * N1, NF = N1 * N1, N = N1 - 1;
-  constexpr int NW = Np / 32;  // warps per element (N1 >= 4)
-  extern __shared__ float smf[];
-  float* s_st = smf;                        // [EPB][6][Np]
-  float* s_fl = s_st + EPB * 6 * Np;        // [EPB][15][Np]
-  float* s_df = s_fl + EPB * 15 * Np;       // [EPB][5][6NF]
+  using G = TcGeom<N1, EPB>;
+  extern __shared__ __align__(1024) unsigned char smraw[];
+  __nv_bfloat16* s_a = reinterpret_cast<__nv_bfloat16*>(smraw);            // contraction operand A
+  __nv_bfloat16* s_b = reinterpret_cast<__nv_bfloat16*>(smraw + G::A_BYTES);  // operand B (D slices)
+  float* s_st = reinterpret_cast<float*>(smraw + G::A_BYTES + G::B_BYTES);    // [EPB][6][Np]
+  float* s_df = s_st + EPB * 6 * Np;        // [EPB][5][6NF]
   float* s_di = s_df + EPB * 5 * 6 * NF;    // [EPB][5][2NF] (stage 1: implicit operator faces)
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(s_di + EPB * 5 * 2 * NF);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 1);
+  float* s_der = reinterpret_cast<float*>(smraw);  // [15][EPB][Np] derivatives, after the MMAs
   const int tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
   const int le = tid / Np, p = tid - le * Np;
   const int ke = blockIdx.x * EPB + le;
   const bool valid = ke < Ne;
@@ -94,12 +138,56 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
   const int ey = valid ? (ke - ez * nxy) / op.NeX : 0;
   const int ex = valid ? ke - ez * nxy - ey * op.NeX : 0;
   float* st = s_st + le * 6 * Np;
-  float* fl = s_fl + le * 15 * Np;
   float* df = s_df + le * 5 * 6 * NF;
   float* di = s_di + le * 5 * 2 * NF;
   const size_t g = (size_t)ke * Np + p;
   const int lev = ez * N1 + k;
   const double dh64 = valid ? __ldg(dens64 + lev) : 1.0;
+
+  // tensor-core set-up: TMEM for the accumulators, the MMA barrier, operand B, zero K slots of A
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
+                 "r"(G::TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(mbar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  for (int e = tid; e < 32 * 32; e += EPB * Np) {  // B[kk][n]: kk = 8 sa + l, n = 8 g + o
+    const int kk = e >> 5, n = e & 31, sa = kk >> 3, l = kk & 7, gg = n >> 3, o = n & 7;
+    float v = 0.f;
+    if (sa <= 2 - gg && l < N1 && o < N1 && gg < 3) {
+      __nv_bfloat16 d0, d1, d2;
+      bf16x3(op.D[o * N1 + l], d0, d1, d2);
+      v = __bfloat162float(gg == 0 ? d0 : (gg == 1 ? d1 : d2));
+    }
+    s_b[tc_idx(n, kk)] = __float2bfloat16_rn(v);
+  }
+  if constexpr (N1 < 8) {  // the unused K slots of every row are zero (NaN bit patterns times zero are not)
+    for (int e = tid; e < G::TILES * 128 * 4; e += EPB * Np) {
+      const int r = e >> 2, sl = e & 3;
+#pragma unroll
+      for (int x = 0; x < 8; ++x)
+        if (sl == 3 || x >= N1) s_a[tc_idx(r, 8 * sl + x)] = __float2bfloat16_rn(0.f);
+    }
+  } else {
+    for (int r = tid; r < G::TILES * 128; r += EPB * Np)
+#pragma unroll
+      for (int x = 0; x < 8; ++x) s_a[tc_idx(r, 24 + x)] = __float2bfloat16_rn(0.f);
+  }
+  // flux value of component (direction d, variable v) at this node -> its three BF16 slices in A
+  auto put = [&](int d, int v, float f) {
+    const int line = d == 0 ? j + N1 * k : (d == 1 ? i + N1 * k : i + N1 * j);
+    const int slot = d == 0 ? i : (d == 1 ? j : k);
+    const int r = (d * 5 + v) * (EPB * NF) + le * NF + line;
+    __nv_bfloat16 a0, a1, a2;
+    bf16x3(f, a0, a1, a2);
+    s_a[tc_idx(r, slot)] = a0;
+    s_a[tc_idx(r, 8 + slot)] = a1;
+    s_a[tc_idx(r, 16 + slot)] = a2;
+  };
 
   // The state arrives as FP32 deviations: DDENS, DRHOT are deviations already; MOMX/MOMY are
   // taken relative to the horizontally uniform reference DENS_hyd(z)*(Uref, Vref) (subtracted in
@@ -122,23 +210,47 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
     const float ptd = (qv[VRT] - ptr * dd) * rdens, pt = ptr + ptd;
     const float ud = (mxd - Uf * dd) * rdens, vd = (myd - Vf * dd) * rdens;
     const float u = Uf + ud, vv = Vf + vd, w = mz * rdens;
-    fl[(0 * 5 + VD) * Np + p] = mxd;
-    fl[(1 * 5 + VD) * Np + p] = myd;
-    fl[(2 * 5 + VD) * Np + p] = mz;
-    fl[(0 * 5 + VRT) * Np + p] = mxr * ptd + mxd * pt;
-    fl[(1 * 5 + VRT) * Np + p] = myr * ptd + myd * pt;
-    fl[(2 * 5 + VRT) * Np + p] = mz * pt;  // used by the implicit operator only (stage 1)
-    fl[(0 * 5 + VMZ) * Np + p] = (mxr + mxd) * w;
-    fl[(1 * 5 + VMZ) * Np + p] = (myr + myd) * w;
-    fl[(2 * 5 + VMZ) * Np + p] = mz * w;
-    fl[(0 * 5 + VMX) * Np + p] = mxr * ud + mxd * u + dp;
-    fl[(1 * 5 + VMX) * Np + p] = myr * ud + myd * u;
-    fl[(2 * 5 + VMX) * Np + p] = mz * u;
-    fl[(0 * 5 + VMY) * Np + p] = mxr * vd + mxd * vv;
-    fl[(1 * 5 + VMY) * Np + p] = myr * vd + myd * vv + dp;
-    fl[(2 * 5 + VMY) * Np + p] = mz * vv;
+    put(0, VD, mxd);
+    put(1, VD, myd);
+    put(2, VD, mz);
+    put(0, VRT, mxr * ptd + mxd * pt);
+    put(1, VRT, myr * ptd + myd * pt);
+    put(2, VRT, mz * pt);  // used by the implicit operator only (stage 1)
+    put(0, VMZ, (mxr + mxd) * w);
+    put(1, VMZ, (myr + myd) * w);
+    put(2, VMZ, mz * w);
+    put(0, VMX, mxr * ud + mxd * u + dp);
+    put(1, VMX, myr * ud + myd * u);
+    put(2, VMX, mz * u);
+    put(0, VMY, mxr * vd + mxd * vv);
+    put(1, VMY, myr * vd + myd * vv + dp);
+    put(2, VMY, mz * vv);
   }
+  // the contractions run on the tensor cores while the threads compute the face fluxes
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // generic stores -> tensor-core reads
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  if (tid == 0) {
+    constexpr uint32_t idesc = umma_idesc_bf16(128, 32);
+#pragma unroll 1
+    for (int t = 0; t < G::TILES; ++t) {
+#pragma unroll
+      for (int ks = 0; ks < 2; ++ks) {
+        const uint64_t ad = umma_desc(smem_u32(s_a) + t * 8192 + ks * 256, 128, 512);
+        const uint64_t bd = umma_desc(smem_u32(s_b) + ks * 256, 128, 512);
+        const uint32_t acc = ks > 0 ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem + 32u * t),
+            "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+            : "memory");
+      }
+    }
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(smem_u32(mbar))
+                 : "memory");
+  }
 
   // --- HEVI Rusanov face flux (hevi_numflux.F90:232-418) in FP32 ---
   if (valid) {
@@ -222,7 +334,50 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
       }
     }
   }
+  // the MMAs' results: wait for the commit (bounded: on expiry raise tc_err and drain with the
+  // full limit, the tendencies of this launch being discarded by the caller), then each warp reads
+  // TMEM lanes 32 (warp % 4) .. +31 of its tiles (one row per thread, 32 accumulator columns) and
+  // writes the N1 derivatives of the row's line into s_der
+  {
+    bool ok = __syncthreads_and(mbar_wait_bounded(smem_u32(mbar), 0u, B.tc_polls)) != 0;
+    if (!ok) {
+      const bool drained = __syncthreads_and(mbar_wait_bounded(smem_u32(mbar), 0u, DRAIN_POLLS)) != 0;
+      if (tid == 0) atomicMax(B.tc_err, drained ? 1 : 2);
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    constexpr int NWARP = EPB * Np / 32;
+    for (int u = warp; ok && u < G::TILES * 4; u += NWARP) {  // (tile, lane quarter); u % 4 == warp % 4
+      const int t = u >> 2, q = u & 3;
+      uint32_t rr[32];
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+          "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+          : "=r"(rr[0]), "=r"(rr[1]), "=r"(rr[2]), "=r"(rr[3]), "=r"(rr[4]), "=r"(rr[5]), "=r"(rr[6]), "=r"(rr[7]),
+            "=r"(rr[8]), "=r"(rr[9]), "=r"(rr[10]), "=r"(rr[11]), "=r"(rr[12]), "=r"(rr[13]), "=r"(rr[14]),
+            "=r"(rr[15]), "=r"(rr[16]), "=r"(rr[17]), "=r"(rr[18]), "=r"(rr[19]), "=r"(rr[20]), "=r"(rr[21]),
+            "=r"(rr[22]), "=r"(rr[23]), "=r"(rr[24]), "=r"(rr[25]), "=r"(rr[26]), "=r"(rr[27]), "=r"(rr[28]),
+            "=r"(rr[29]), "=r"(rr[30]), "=r"(rr[31])
+          : "r"(tmem + ((uint32_t)(32 * q) << 16) + 32u * t)
+          : "memory");
+      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+      const int r = t * 128 + 32 * q + lane;
+      if (r < G::ROWS) {
+        const int dv = r / (EPB * NF), rem = r - dv * (EPB * NF), d = dv / 5;
+        const int e2 = rem / NF, line = rem - e2 * NF;
+        float* out = s_der + (size_t)dv * (EPB * Np) + e2 * Np;
+#pragma unroll
+        for (int o = 0; o < N1; ++o) {
+          const float val = __uint_as_float(rr[o]) + __uint_as_float(rr[8 + o]) + __uint_as_float(rr[16 + o]);
+          const int po = d == 0 ? o + N1 * line : (d == 1 ? (line % N1) + N1 * o + NF * (line / N1) : line + NF * o);
+          out[po] = val;
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   __syncthreads();
+  if (warp == 0)  // the accumulators are in s_der now
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(G::TMEM_COLS) : "memory");
 
   float tex[5], tim[5];
   if (valid) {
@@ -230,13 +385,9 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
     float szv[5];
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
-      float sx = 0.f, sy = 0.f, sz = 0.f;
-#pragma unroll
-      for (int l = 0; l < N1; ++l) {
-        sx = fmaf(op.D[i * N1 + l], fl[(0 * 5 + v) * Np + l + N1 * j + NF * k], sx);
-        sy = fmaf(op.D[j * N1 + l], fl[(1 * 5 + v) * Np + i + N1 * l + NF * k], sy);
-        sz = fmaf(op.D[k * N1 + l], fl[(2 * 5 + v) * Np + i + N1 * j + NF * l], sz);
-      }
+      const float sx = s_der[(size_t)(0 * 5 + v) * (EPB * Np) + le * Np + p];
+      const float sy = s_der[(size_t)(1 * 5 + v) * (EPB * Np) + le * Np + p];
+      const float sz = s_der[(size_t)(2 * 5 + v) * (EPB * Np) + le * Np + p];
       szv[v] = sz;
       const float* d = df + v * S;
       const float lf = op.Lb[j] * d[0 * NF + i + N1 * k] + op.Lt[i] * d[1 * NF + j + N1 * k] +
@@ -349,7 +500,7 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
   __syncthreads();  // everyone is done with the shared arrays
   // the five fields per pass: three barriers
   float* fa = s_st + le * 6 * Np;   // [5][Np]
-  float* fb = s_fl + le * 15 * Np;  // [5][Np]
+  float* fb = s_der + le * 5 * Np;  // [5][Np] (the operand region, free by now)
 #pragma unroll
   for (int v = 0; v < 5; ++v) fa[v * Np + p] = dev[v];
   __syncthreads();
@@ -398,10 +549,15 @@ __global__ void k_to_dev(F5c q, Dev5 out, const double* __restrict__ dens_prof, 
   out.v[VRT][g] = (float)q.v[VRT][g];
 }
 
-// sums of MOMX, MOMY and DENS over the domain (FP64) for the reference wind
-__global__ void k_wind_sums(const double* __restrict__ mx, const double* __restrict__ my,
-                            const double* __restrict__ dd, const double* __restrict__ dens_prof, int Np, int N1,
-                            size_t nxy, size_t n, double* out) {
+// sums of MOMX, MOMY and DENS over the domain (FP64) for the reference wind, in a fixed order so
+// that the reference wind, and with it every later step of the fast paths, is reproducible bit for
+// bit: each block sums a fixed grid-stride subset (warp shuffles, then its warps in order) into
+// part[block][3]; k_wind_final adds the block sums in order.
+constexpr int WIND_BLOCKS = 1024;
+__global__ void __launch_bounds__(256) k_wind_sums(const double* __restrict__ mx, const double* __restrict__ my,
+                                                   const double* __restrict__ dd, const double* __restrict__ dens_prof,
+                                                   int Np, int N1, size_t nxy, size_t n, double* part) {
+  __shared__ double ws[8][3];
   double s0 = 0.0, s1 = 0.0, s2 = 0.0;
   for (size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x; g < n; g += (size_t)gridDim.x * blockDim.x) {
     const size_t ke = g / Np;
@@ -416,10 +572,24 @@ __global__ void k_wind_sums(const double* __restrict__ mx, const double* __restr
     s1 += __shfl_xor_sync(0xffffffffu, s1, o);
     s2 += __shfl_xor_sync(0xffffffffu, s2, o);
   }
+  const int w = threadIdx.x >> 5;
   if ((threadIdx.x & 31) == 0) {
-    atomicAdd(out + 0, s0);
-    atomicAdd(out + 1, s1);
-    atomicAdd(out + 2, s2);
+    ws[w][0] = s0;
+    ws[w][1] = s1;
+    ws[w][2] = s2;
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double t = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += ws[q][threadIdx.x];
+    part[(size_t)blockIdx.x * 3 + threadIdx.x] = t;
+  }
+}
+__global__ void k_wind_final(const double* __restrict__ part, int nblocks, double* out) {
+  if (threadIdx.x < 3) {
+    double t = 0.0;
+    for (int b = 0; b < nblocks; ++b) t += part[(size_t)b * 3 + threadIdx.x];
+    out[threadIdx.x] = t;
   }
 }
 
@@ -431,7 +601,8 @@ template <int N1, int STAGE>
 static int launch_stage_n(const OpsF& op, const ProfF& pf, const double* dens64, const StageBufs& B,
                           const MixCoef& cf, int Ne, int filt, cudaStream_t s) {
   constexpr int EPB = epb_m<N1>(), Np = N1 * N1 * N1, NF = N1 * N1;
-  const size_t smem = sizeof(float) * EPB * (21 * Np + 5 * 6 * NF + 5 * 2 * NF);
+  using G = TcGeom<N1, EPB>;
+  const size_t smem = G::A_BYTES + G::B_BYTES + sizeof(float) * EPB * (6 * Np + 5 * 6 * NF + 5 * 2 * NF) + 16;
   auto kfn = k_stage_mixed<N1, EPB, STAGE>;
   cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   kfn<<<(Ne + EPB - 1) / EPB, EPB * Np, smem, s>>>(op, pf, dens64, B, cf, Ne, filt);
@@ -457,6 +628,7 @@ struct MixedState {
   float2* prof2 = nullptr;  // [4][L] float pairs DENS_hyd, PRES_hyd, RHOT_hyd, 1/RHOT_hyd
   float** d_ptrs = nullptr; // device arrays of float pointers: TI[5], guess[3], QSF[5]
   float* gsc = nullptr;     // block-Thomas history of the column solve
+  int* tc_err = nullptr;    // raised by a stage kernel whose tensor-core barrier wait ran out
   // float-pair mode (FEDG_PREC_PAIR), allocated on first use: S3 | SF | TI | QSF | QNF as pairs
   float2* pbuf = nullptr;
   void** d_pptrs = nullptr;  // device arrays of pointers: TI[5], QSF[5] (pairs)
@@ -496,6 +668,7 @@ void mixed_free(MixedState* m) {
   cudaFree(m->prof2);
   cudaFree(m->d_ptrs);
   cudaFree(m->gsc);
+  cudaFree(m->tc_err);
   cudaFree(m->pbuf);
   cudaFree(m->d_pptrs);
   cudaFree(m->prof5);
@@ -515,7 +688,9 @@ static int mixed_setup(fedg_ctx* c) {
       (e = cudaMalloc(&m->prof, sizeof(float) * 4 * L)) != cudaSuccess ||
       (e = cudaMalloc(&m->prof2, sizeof(float2) * 4 * L)) != cudaSuccess ||
       (e = cudaMalloc(&m->d_ptrs, sizeof(float*) * 13)) != cudaSuccess ||
-      (e = cudaMalloc(&m->gsc, sizeof(float) * vi_cols_scratch_floats(c->n))) != cudaSuccess) {
+      (e = cudaMalloc(&m->gsc, sizeof(float) * vi_cols_scratch_floats(c->n))) != cudaSuccess ||
+      (e = cudaMalloc(&m->tc_err, sizeof(int))) != cudaSuccess ||
+      (e = cudaMemset(m->tc_err, 0, sizeof(int))) != cudaSuccess) {
     mixed_free(m);
     return api_cuda_fail(e, "fedg_update(mixed): allocation");
   }
@@ -675,13 +850,50 @@ static int set_sponge_prof(fedg_ctx* c, MixedState* m, ProfF* pff, ProfP* pfp) {
 }
 
 // reference wind of the deviations = domain-mean velocity of the first state seen
+static void apply_ref_wind(MixedState* m, double U, double V) {
+  m->Uref = U;
+  m->Vref = V;
+  m->opf.Uref = (float)U;
+  m->opf.Vref = (float)V;
+  m->opx.Uref = split_host(U);
+  m->opx.Vref = split_host(V);
+  m->wind_set = true;
+}
+
+bool fedg::ref_wind(const fedg_ctx* c, double out[2]) {
+  if (c->mixed && c->mixed->wind_set) {
+    out[0] = c->mixed->Uref;
+    out[1] = c->mixed->Vref;
+    return true;
+  }
+  if (c->wind_given) {
+    out[0] = c->wind[0];
+    out[1] = c->wind[1];
+    return true;
+  }
+  return false;
+}
+
+void fedg::set_ref_wind_given(fedg_ctx* c, double U, double V) {
+  c->wind_given = true;
+  c->wind[0] = U;
+  c->wind[1] = V;
+  if (c->mixed) apply_ref_wind(c->mixed, U, V);
+}
+
 static int set_ref_wind(fedg_ctx* c, MixedState* m, double* const q[5]) {
   if (m->wind_set) return 0;
+  if (c->wind_given) {
+    apply_ref_wind(m, c->wind[0], c->wind[1]);
+    return 0;
+  }
   int r;
-  double* d_s = reinterpret_cast<double*>(m->fbuf);  // TI area, free before the first step
-  if (cudaMemsetAsync(d_s, 0, 3 * sizeof(double), c->stream) != cudaSuccess) return api_fail("memset");
+  double* d_s = reinterpret_cast<double*>(m->fbuf);  // TI area, free before the first step: 3 sums, then
+  double* d_part = d_s + 4;                          // the block sums [WIND_BLOCKS][3]
+  const int nb = (int)std::min<size_t>(WIND_BLOCKS, (c->n + 255) / 256);  // 3 nb + 4 doubles fit the TI area
   r = tracked(c, FEDG_K_AUX, [&] {
-    k_wind_sums<<<1024, 256, 0, c->stream>>>(q[1], q[2], q[0], c->d_prof, c->Np, c->N1, c->nxy, c->n, d_s);
+    k_wind_sums<<<nb, 256, 0, c->stream>>>(q[1], q[2], q[0], c->d_prof, c->Np, c->N1, c->nxy, c->n, d_part);
+    k_wind_final<<<1, 32, 0, c->stream>>>(d_part, nb, d_s);
     return (int)cudaGetLastError();
   });
   if (r) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): wind sums");
@@ -689,13 +901,7 @@ static int set_ref_wind(fedg_ctx* c, MixedState* m, double* const q[5]) {
   if (cudaMemcpyAsync(hs, d_s, sizeof(hs), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
       cudaStreamSynchronize(c->stream) != cudaSuccess)
     return api_fail("fedg_update(mixed): wind readback");
-  m->Uref = hs[2] != 0.0 ? hs[0] / hs[2] : 0.0;
-  m->Vref = hs[2] != 0.0 ? hs[1] / hs[2] : 0.0;
-  m->opf.Uref = (float)m->Uref;
-  m->opf.Vref = (float)m->Vref;
-  m->opx.Uref = split_host(m->Uref);
-  m->opx.Vref = split_host(m->Vref);
-  m->wind_set = true;
+  apply_ref_wind(m, hs[2] != 0.0 ? hs[0] / hs[2] : 0.0, hs[2] != 0.0 ? hs[1] / hs[2] : 0.0);
   return 0;
 }
 
@@ -782,6 +988,8 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
   ProfF pff{m->prof, m->prof + c->L, m->prof + 2 * c->L, m->prof + 3 * c->L};
   StageBufs B;
   std::memset(&B, 0, sizeof(B));
+  B.tc_err = m->tc_err;
+  B.tc_polls = c->tc_polls;
   for (int v = 0; v < 5; ++v) {
     B.qn[v] = q[v];
     B.qnf[v] = m->QNF(v);
@@ -904,6 +1112,17 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
   if (cudaMemcpyAsync(c->h_cnt, c->d_cnt, sizeof(unsigned long long) * 3, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
       cudaStreamSynchronize(c->stream) != cudaSuccess)
     return api_fail("fedg_update(mixed): status readback");
+  if (!pair) {
+    int h = 0;
+    if (cudaMemcpy(&h, m->tc_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+      return api_fail("fedg_update(mixed): error-flag readback");
+    if (h) {
+      cudaMemset(m->tc_err, 0, sizeof(int));
+      return api_fail(h == 1 ? "fedg_update(mixed): a stage kernel's tensor-core contraction timed out waiting on its barrier"
+                             : "fedg_update(mixed): a stage kernel's tensor-core contraction timed out waiting on its "
+                               "barrier, and waiting for its MMAs in flight timed out too");
+    }
+  }
   if (o->use_guess) {
     const int ge = mlp_take_error(c->guess, c->stream);
     if (ge == -1) return api_fail("fedg_update(mixed): a column-guess tensor-core GEMM timed out waiting on its barrier");

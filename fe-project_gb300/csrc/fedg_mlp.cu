@@ -10,10 +10,16 @@
 #include <vector>
 
 #include "fedg_mlp.cuh"
+#include "fedg_umma.cuh"
 
 using bf16 = __nv_bfloat16;
 
 namespace {
+
+using fedg::DRAIN_POLLS;
+using fedg::mbar_wait_bounded;
+using fedg::smem_u32;
+using fedg::umma_desc;
 
 // padding of the inference buffers: rows to the 128-row GEMM tile, inputs to the 32-wide K chunk,
 // outputs to a multiple of 64 columns
@@ -57,29 +63,6 @@ struct ColIO {
 // whose outputs the raised flag has already discarded.  The epilogue reads the accumulator
 // with tcgen05.ld (warp w owns lanes 32w..32w+31, one output row per thread), adds the bias,
 // applies GELU and stores the row.
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
-         (1ull << 46);  // descriptor version 1, base offset 0, no swizzle
-}
-
-// polls of the drain wait, and the default limit of the normal path's waits
-constexpr int DRAIN_POLLS = 1 << 20;
-
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t parity, int limit) {
-  for (int it = 0; it < limit; ++it) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(mbar), "r"(parity)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
-}
-
 // element offset of level l of column c within an (Np, Ne) field, from the column's base index
 __device__ __forceinline__ size_t col_base(const ColMap& cm, int c) {
   const int ij = c & ((1 << (2 * cm.lgN1)) - 1), exy = c >> (2 * cm.lgN1);
@@ -119,7 +102,7 @@ __global__ void __launch_bounds__(128) k_gemm_tc(const bf16* __restrict__ A, con
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   const uint32_t tmem = *tmem_slot;
   // instruction descriptor: D f32, A/B bf16, both K-major, N/8, M/16
-  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
+  constexpr uint32_t idesc = fedg::umma_idesc_bf16(TM, BN);
 
   // one K chunk of this thread's A and B pieces in registers: prefetched while the previous
   // chunk's MMAs run

@@ -35,7 +35,8 @@ EXPORTED = [
     "fedg_trc_alphdens_advtest", "fedg_trc_save_massflux", "fedg_trc_fct_coef", "fedg_trc_cal_tend",
     "fedg_trc_tmar", "fedg_trc_modalfilter", "fedg_trc_update", "fedg_numdiff_apply", "fedg_sponge_add_tend",
     "fedg_update_set_tracer_flux", "fedg_update_set_sponge", "fedg_numdiff_apply_prec",
-    "fedg_guess_set_wait_limit", "fedg_update_set_vi_neumann",
+    "fedg_guess_set_wait_limit", "fedg_update_set_vi_neumann", "fedg_update_set_wait_limit",
+    "fedg_restart_write", "fedg_restart_read",
 ]
 
 # kernel classes of fedg_prof_read (include/fedg.h)
@@ -78,6 +79,11 @@ class UpdateOpts(ctypes.Structure):
 _lib = None
 _vp = ctypes.c_void_p
 _P5 = ctypes.c_void_p * 5
+
+
+class RestartInfo(ctypes.Structure):
+    _fields_ = [("step", ctypes.c_longlong), ("time", ctypes.c_double), ("dt", ctypes.c_double),
+                ("scheme", ctypes.c_char * 32)]
 
 
 def load():
@@ -129,6 +135,9 @@ def load():
     lib.fedg_guess_load.argtypes = [_vp, _vp]
     lib.fedg_guess_set_wait_limit.argtypes = [_vp, ctypes.c_int]
     lib.fedg_update_set_vi_neumann.argtypes = [_vp, ctypes.c_int]
+    lib.fedg_update_set_wait_limit.argtypes = [_vp, ctypes.c_int]
+    lib.fedg_restart_write.argtypes = [_vp, ctypes.c_char_p, _P5, ctypes.POINTER(RestartInfo)]
+    lib.fedg_restart_read.argtypes = [_vp, ctypes.c_char_p, _P5, ctypes.c_void_p, ctypes.POINTER(RestartInfo)]
     _P3 = ctypes.c_void_p * 3
     lib.fedg_trc_alphdens_advtest.argtypes = [_vp] + [_vp] * 6
     lib.fedg_trc_save_massflux.argtypes = [_vp, ctypes.c_int, _P5, _vp, ctypes.c_double, ctypes.c_double,
@@ -297,6 +306,27 @@ class Context:
         if sync:
             self.sync()
         return nfail, float(mi.value)
+
+    # -- restart files (scale_file_restart_meshfield.F90) --
+    def restart_write(self, path, q, step=0, time=0.0, dt=0.0, scheme=""):
+        info = RestartInfo(int(step), float(time), float(dt), scheme.encode()[:31])
+        self.torch.cuda.synchronize()
+        _check(self.lib.fedg_restart_write(self.h, str(path).encode(), _p5(q), ctypes.byref(info)),
+               "fedg_restart_write")
+
+    def restart_read(self, path, q, base=None):
+        """fills the five device fields q (and, when given, the three base-state fields); returns
+        (step, time, dt, scheme)"""
+        info = RestartInfo()
+        bp = (ctypes.c_void_p * 3)(*[t.data_ptr() for t in base]) if base is not None else None
+        self.torch.cuda.synchronize()
+        _check(self.lib.fedg_restart_read(self.h, str(path).encode(), _p5(q), bp, ctypes.byref(info)),
+               "fedg_restart_read")
+        return int(info.step), float(info.time), float(info.dt), info.scheme.decode()
+
+    def set_wait_limit(self, polls):
+        """polls of the update path's tensor-core barrier waits before they give up (default 1 << 20)"""
+        _check(self.lib.fedg_update_set_wait_limit(self.h, int(polls)), "fedg_update_set_wait_limit")
 
     def set_vi_neumann(self, nterm):
         """Jacobian-vector products of the column solve's Neumann corrections (0: LU only)."""
@@ -566,6 +596,23 @@ class Guess:
         _check(self.lib.fedg_guess_predict(self.h, _ptr(X), _ptr(Y), int(X.shape[0])), "fedg_guess_predict")
         torch.cuda.synchronize()
         return Y
+
+    # -- restart files (scale_file_restart_meshfield.F90) --
+    def restart_write(self, path, q, step=0, time=0.0, dt=0.0, scheme=""):
+        info = RestartInfo(int(step), float(time), float(dt), scheme.encode()[:31])
+        self.torch.cuda.synchronize()
+        _check(self.lib.fedg_restart_write(self.h, str(path).encode(), _p5(q), ctypes.byref(info)),
+               "fedg_restart_write")
+
+    def restart_read(self, path, q, base=None):
+        """fills the five device fields q (and, when given, the three base-state fields); returns
+        (step, time, dt, scheme)"""
+        info = RestartInfo()
+        bp = (ctypes.c_void_p * 3)(*[t.data_ptr() for t in base]) if base is not None else None
+        self.torch.cuda.synchronize()
+        _check(self.lib.fedg_restart_read(self.h, str(path).encode(), _p5(q), bp, ctypes.byref(info)),
+               "fedg_restart_read")
+        return int(info.step), float(info.time), float(info.dt), info.scheme.decode()
 
     def set_wait_limit(self, polls):
         """polls of the tensor-core GEMMs' barrier waits before they give up (default 1 << 20)"""

@@ -171,6 +171,13 @@ int fedg_update(fedg_ctx* ctx, double* const q[5], int nsteps, const fedg_update
  * FElib, whose solve is a single LU correction. */
 int fedg_update_set_vi_neumann(fedg_ctx* ctx, int nterm);
 
+/* Bounded waits of the update path's tensor-core contractions (the FEDG_PREC_MIXED stage kernels):
+ * each wait on the MMA completion barrier polls at most `polls` times (default 1048576) before the
+ * kernel gives up, drains its MMAs with the default limit and raises an error flag; fedg_update then
+ * returns < 0 with fedg_last_error text.  No counterpart in FElib (no GPU waits there); a small
+ * limit makes the wait run out on purpose, which is how the error path is tested. */
+int fedg_update_set_wait_limit(fedg_ctx* ctx, int polls);
+
 /* Column-guess network for the HEVI Newton solve (the learned initial iterate): a GELU MLP
  * (3L+1) -> hidden -> hidden -> 3L mapping a column's stage input (DDENS', MOMZ, DRHOT' at its
  * L = NeZ*N1 levels, then impl_fac, each times in_scale[var]) to the implicit increment
@@ -297,6 +304,27 @@ int fedg_numdiff_apply_prec(fedg_ctx* ctx, double* const q[5], int nlap, double 
  * MOMY, MOMZ.  FElib's defaults: tau = 10 dt when SL_WDAMP_TAU < 0; height from SL_WDAMP_LAYER. */
 int fedg_sponge_add_tend(fedg_ctx* ctx, double* const tend[3], const double* const mom[3], double tau,
                          double height, int hveldamp);
+
+/* ---- Restart files -------------------------------------------------------------------------
+ * The restart state FElib writes through NetCDF (FElib/src/file/scale_file_restart_meshfield.F90:
+ * 136-186; read back by model/atm_nonhydro3d/src/atmos/mod_atmos_vars.F90:580-633), in a flat
+ * little-endian file: a header (mesh, step, time, dt, time-integration scheme name, the fast paths'
+ * reference wind) and the fields DDENS, MOMX, MOMY, MOMZ, DRHOT, DENS_hyd, PRES_hyd, THERM_hyd in
+ * FElib's (Np, Ne) order as float64.  fedg_restart_write takes the five prognostic fields (device)
+ * and writes the registered base state with them; fedg_restart_read checks the mesh, fills the five
+ * fields and, when base is not NULL, DENS_hyd, PRES_hyd, THERM_hyd (device arrays; register them with
+ * fedg_set_base_state), and fixes the context's reference wind, so that a run restored into a new
+ * context continues bit for bit.  The layout is documented in fe-project_gb300/csrc/fedg_restart.cu
+ * and read and written by fe-project_gb300/fedg/restart.py. */
+typedef struct {
+  long long step;   /* time steps taken */
+  double time;      /* simulated time [s] */
+  double dt;        /* time step [s] */
+  char scheme[32];  /* time-integration scheme (FElib's TINTEG_TYPE, e.g. "IMEX_ARK232") */
+} fedg_restart_info;
+int fedg_restart_write(fedg_ctx* ctx, const char* path, const double* const q[5], const fedg_restart_info* info);
+int fedg_restart_read(fedg_ctx* ctx, const char* path, double* const q[5], double* const base[3],
+                      fedg_restart_info* info);
 
 /* Kernel timers: the analogue of FElib's PROF_rapstart/PROF_rapend regions
  * (e.g. 'ATM_DYN_cal_vi', 'cal_dyn_tend_interior'; scale_prof of the SCALE library).

@@ -95,3 +95,26 @@ def test_mixed_rejects_heve_and_low_order():
     ctx2.set_base_state(b2["dens_hyd"], b2["pres_hyd"], b2["therm_hyd"])
     with pytest.raises(fl.FedgError):
         ctx2.update([ctx2.tensor(a) for a in q2], 1, eqs=fl.HEVI, prec=fl.PREC_MIXED, dt=0.02)
+
+
+def test_tensor_core_wait_limit_reports_error_and_context_recovers():
+    """The FP32 mode's stage kernels differentiate the fluxes on the tensor cores and wait on the MMA
+    barrier with a bounded poll count.  With a limit of zero polls every wait runs out at once: the
+    kernels drain their MMAs with the full limit, raise the error flag, and fedg_update returns < 0
+    with the error text; with the default limit restored the same context steps normally."""
+    import torch
+
+    case = cases.C2().scaled(2, 2, 4)
+    q, b = cases.initial_state(case)
+    ctx = fl.Context(case)
+    ctx.set_base_state(b["dens_hyd"], b["pres_hyd"], b["therm_hyd"])
+    qd = [ctx.tensor(a) for a in q]
+    ctx.set_wait_limit(0)
+    with pytest.raises(fl.FedgError, match="tensor-core contraction timed out"):
+        ctx.update(qd, 1, prec=fl.PREC_MIXED, dt=0.04, max_iter=20, tol=1e-10)
+    torch.cuda.synchronize()
+    ctx.set_wait_limit(1 << 20)
+    qd = [ctx.tensor(a) for a in q]
+    nf, _ = ctx.update(qd, 1, prec=fl.PREC_MIXED, dt=0.04, max_iter=20, tol=1e-10)
+    assert nf == 0
+    assert all(bool(torch.isfinite(t).all()) for t in qd)
