@@ -57,40 +57,43 @@ struct StageBufs {
   int tc_polls;         // poll limit of that wait
 };
 
-// ---- derivative contractions on the tensor cores (BF16x3 split, FP32 accumulation) ----
+// ---- derivative contractions on the tensor cores (3xTF32 split, FP32 accumulation) ----
 // The 15 flux components of an element group are each differentiated along one direction (F_x
 // along x, F_y along y, F_z along z): with D the 1D derivative matrix, one GEMM
 //   C[row, o] = sum_l F[row, l] D[o, l]
 // whose rows are (direction, component, element, line of N1 nodes along the direction) and whose
-// K index is the node l along the line.  Each FP32 flux value f is split exactly into three BF16
-// slices f0 + f1 + f2 (f0 = bf16(f), f1 = bf16(f - f0), f2 = bf16(f - f0 - f1)), and so is D; the
-// six slice products with i + j <= 2 are accumulated in FP32 by the tensor core, which reproduces
-// FP32-class products (the dropped terms are below 2^-32 of |f||D|), as the 3xTF32 split does with
-// TF32 slices.  A row holds its three slices in K slots [8 s, 8 s + N1) of a K = 32 operand (the
-// remaining slots zero); B (K = 32 x N = 32) holds in column group g (N slots [8 g, 8 g + N1)) the
-// D slice g for the A slices s <= 2 - g, so out[o] = C[o] + C[8 + o] + C[16 + o].
-// tcgen05.mma kind::f16, M = 128, N = 32, K = 16 (two K steps per 128-row tile), FP32 accumulators
-// in TMEM (32 columns per tile), operands in shared memory in the no-swizzle K-major canonical
-// layout (8-row x 16-byte core matrices: K neighbours 128 B apart, 8-row groups 512 B apart).
+// K index is the node l along the line (K = 8, N1 = 4 pads with zeros).  Each FP32 value is split
+// into a TF32 head and the TF32-rounded remainder, f = f_hi + f_lo, and so is D; the products
+// f_hi D_hi + f_hi D_lo + f_lo D_hi are accumulated in FP32 by the tensor core (the 3xTF32 scheme:
+// the dropped f_lo D_lo is below 2^-22 of |f||D|), which keeps the contraction FP32-class.
+// Per 128-row tile two tcgen05.mma kind::tf32 (M = 128, N = 16, K = 8) into 16 TMEM columns:
+//   A_hi x [D_hi | D_lo]  -> columns 0..7: f_hi D_hi, columns 8..15: f_hi D_lo
+//   A_lo x [D_hi | 0   ]  -> columns 0..7: + f_lo D_hi
+// so out[o] = C[o] + C[8 + o].  Operands in shared memory in the no-swizzle K-major canonical
+// layout (8-row x 16-byte core matrices: the two K halves 128 B apart, 8-row groups 256 B apart).
 template <int N1, int EPB>
 struct TcGeom {
   static constexpr int NF = N1 * N1, Np = N1 * N1 * N1;
-  static constexpr int ROWS = 15 * EPB * NF;           // 960 for (N1, EPB) = (8, 1) and (4, 4)
+  static constexpr int ROWS = 15 * EPB * NF;          // 960 for (N1, EPB) = (8, 1) and (4, 4)
   static constexpr int TILES = (ROWS + 127) / 128;
-  static constexpr int A_BYTES = TILES * 128 * 64;    // BF16, K = 32
-  static constexpr int B_BYTES = 32 * 64;
-  static constexpr uint32_t TMEM_COLS = 256;          // 32 per tile, power of two >= TILES * 32
-  static_assert(TILES * 32 <= (int)TMEM_COLS, "accumulator columns");
+  static constexpr int A_BYTES = 2 * TILES * 128 * 32;  // A_hi, then A_lo: 32-bit, K = 8
+  static constexpr int B_BYTES = 2 * 16 * 32;           // [D_hi | D_lo], then [D_hi | 0]
+  static constexpr uint32_t TMEM_COLS = 128;            // 16 per tile, power of two >= TILES * 16
+  static_assert(TILES * 16 <= (int)TMEM_COLS, "accumulator columns");
   static_assert(15 * EPB * Np * 4 <= A_BYTES, "the derivative outputs reuse the operand region");
 };
-// BF16 element index of (row r, K slot kk) in the canonical layout
-__device__ __forceinline__ int tc_idx(int r, int kk) { return ((r >> 3) * 4 + (kk >> 3)) * 64 + (r & 7) * 8 + (kk & 7); }
-__device__ __forceinline__ void bf16x3(float f, __nv_bfloat16& a, __nv_bfloat16& b, __nv_bfloat16& c) {
-  a = __float2bfloat16_rn(f);
-  const float r1 = f - __bfloat162float(a);
-  b = __float2bfloat16_rn(r1);
-  c = __float2bfloat16_rn(r1 - __bfloat162float(b));
+// 32-bit element index of (row r, K slot kk) in the canonical layout
+__device__ __forceinline__ int tc_idx(int r, int kk) { return ((r >> 3) * 2 + (kk >> 2)) * 32 + (r & 7) * 4 + (kk & 3); }
+__device__ __forceinline__ uint32_t tf32_rna(float f) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(f));
+  return r;
 }
+__device__ __forceinline__ void tf32x2(float f, uint32_t& hi, uint32_t& lo) {
+  hi = tf32_rna(f);
+  lo = tf32_rna(f - __uint_as_float(hi));
+}
+
 
 // PRES - PRES_hyd = PRES_hyd ((1 + DRHOT/THERM_hyd)^kappa - 1)   (nonhydro3d_common.F90:470-474)
 __device__ __forceinline__ float dpres_f(float dr, float rth, float ph, float kap) {
@@ -119,8 +122,8 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
   constexpr int Np = N1 * N1 * N1, NF = N1 * N1, N = N1 - 1;
   using G = TcGeom<N1, EPB>;
   extern __shared__ __align__(1024) unsigned char smraw[];
-  __nv_bfloat16* s_a = reinterpret_cast<__nv_bfloat16*>(smraw);            // contraction operand A
-  __nv_bfloat16* s_b = reinterpret_cast<__nv_bfloat16*>(smraw + G::A_BYTES);  // operand B (D slices)
+  uint32_t* s_a = reinterpret_cast<uint32_t*>(smraw);                 // A_hi [TILES*128][8], then A_lo
+  uint32_t* s_b = reinterpret_cast<uint32_t*>(smraw + G::A_BYTES);    // [D_hi | D_lo] [16][8], then [D_hi | 0]
   float* s_st = reinterpret_cast<float*>(smraw + G::A_BYTES + G::B_BYTES);    // [EPB][6][Np]
   float* s_df = s_st + EPB * 6 * Np;        // [EPB][5][6NF]
   float* s_di = s_df + EPB * 5 * 6 * NF;    // [EPB][5][2NF] (stage 1: implicit operator faces)
@@ -155,38 +158,27 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(mbar)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
-  for (int e = tid; e < 32 * 32; e += EPB * Np) {  // B[kk][n]: kk = 8 sa + l, n = 8 g + o
-    const int kk = e >> 5, n = e & 31, sa = kk >> 3, l = kk & 7, gg = n >> 3, o = n & 7;
-    float v = 0.f;
-    if (sa <= 2 - gg && l < N1 && o < N1 && gg < 3) {
-      __nv_bfloat16 d0, d1, d2;
-      bf16x3(op.D[o * N1 + l], d0, d1, d2);
-      v = __bfloat162float(gg == 0 ? d0 : (gg == 1 ? d1 : d2));
-    }
-    s_b[tc_idx(n, kk)] = __float2bfloat16_rn(v);
+  for (int e = tid; e < 2 * 16 * 8; e += EPB * Np) {  // B rows n (output node, hi/lo half), K slot l
+    const int h = e >> 7, n = (e >> 3) & 15, l = e & 7, o = n & 7;
+    uint32_t dh = 0u, dl = 0u;
+    if (o < N1 && l < N1) tf32x2(op.D[o * N1 + l], dh, dl);
+    s_b[h * 128 + tc_idx(n, l)] = n < 8 ? dh : (h == 0 ? dl : 0u);
   }
-  if constexpr (N1 < 8) {  // the unused K slots of every row are zero (NaN bit patterns times zero are not)
-    for (int e = tid; e < G::TILES * 128 * 4; e += EPB * Np) {
-      const int r = e >> 2, sl = e & 3;
-#pragma unroll
-      for (int x = 0; x < 8; ++x)
-        if (sl == 3 || x >= N1) s_a[tc_idx(r, 8 * sl + x)] = __float2bfloat16_rn(0.f);
+  if constexpr (N1 < 8) {  // K slots N1..7 of every row are zero (NaN bit patterns times zero are not)
+    for (int r = tid; r < G::TILES * 128; r += EPB * Np) {
+      *reinterpret_cast<uint4*>(s_a + tc_idx(r, 4)) = make_uint4(0u, 0u, 0u, 0u);
+      *reinterpret_cast<uint4*>(s_a + G::TILES * 128 * 8 + tc_idx(r, 4)) = make_uint4(0u, 0u, 0u, 0u);
     }
-  } else {
-    for (int r = tid; r < G::TILES * 128; r += EPB * Np)
-#pragma unroll
-      for (int x = 0; x < 8; ++x) s_a[tc_idx(r, 24 + x)] = __float2bfloat16_rn(0.f);
   }
   // flux value of component (direction d, variable v) at this node -> its three BF16 slices in A
   auto put = [&](int d, int v, float f) {
     const int line = d == 0 ? j + N1 * k : (d == 1 ? i + N1 * k : i + N1 * j);
     const int slot = d == 0 ? i : (d == 1 ? j : k);
     const int r = (d * 5 + v) * (EPB * NF) + le * NF + line;
-    __nv_bfloat16 a0, a1, a2;
-    bf16x3(f, a0, a1, a2);
-    s_a[tc_idx(r, slot)] = a0;
-    s_a[tc_idx(r, 8 + slot)] = a1;
-    s_a[tc_idx(r, 16 + slot)] = a2;
+    uint32_t hi, lo;
+    tf32x2(f, hi, lo);
+    s_a[tc_idx(r, slot)] = hi;
+    s_a[G::TILES * 128 * 8 + tc_idx(r, slot)] = lo;
   };
 
   // The state arrives as FP32 deviations: DDENS, DRHOT are deviations already; MOMX/MOMY are
@@ -233,17 +225,17 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   const uint32_t tmem = *tmem_slot;
   if (tid == 0) {
-    constexpr uint32_t idesc = umma_idesc_bf16(128, 32);
+    constexpr uint32_t idesc = umma_idesc_tf32(128, 16);
 #pragma unroll 1
     for (int t = 0; t < G::TILES; ++t) {
 #pragma unroll
-      for (int ks = 0; ks < 2; ++ks) {
-        const uint64_t ad = umma_desc(smem_u32(s_a) + t * 8192 + ks * 256, 128, 512);
-        const uint64_t bd = umma_desc(smem_u32(s_b) + ks * 256, 128, 512);
-        const uint32_t acc = ks > 0 ? 1u : 0u;
+      for (int h = 0; h < 2; ++h) {  // A_hi x [D_hi | D_lo], then A_lo x [D_hi | 0]
+        const uint64_t ad = umma_desc(smem_u32(s_a) + h * (G::TILES * 128 * 32) + t * 4096, 128, 256);
+        const uint64_t bd = umma_desc(smem_u32(s_b) + h * 512, 128, 256);
+        const uint32_t acc = h > 0 ? 1u : 0u;
         asm volatile(
             "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem + 32u * t),
+            " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem + 16u * t),
             "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
             : "memory");
       }
@@ -348,16 +340,13 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
     constexpr int NWARP = EPB * Np / 32;
     for (int u = warp; ok && u < G::TILES * 4; u += NWARP) {  // (tile, lane quarter); u % 4 == warp % 4
       const int t = u >> 2, q = u & 3;
-      uint32_t rr[32];
+      uint32_t rr[16];
       asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-          "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
           : "=r"(rr[0]), "=r"(rr[1]), "=r"(rr[2]), "=r"(rr[3]), "=r"(rr[4]), "=r"(rr[5]), "=r"(rr[6]), "=r"(rr[7]),
             "=r"(rr[8]), "=r"(rr[9]), "=r"(rr[10]), "=r"(rr[11]), "=r"(rr[12]), "=r"(rr[13]), "=r"(rr[14]),
-            "=r"(rr[15]), "=r"(rr[16]), "=r"(rr[17]), "=r"(rr[18]), "=r"(rr[19]), "=r"(rr[20]), "=r"(rr[21]),
-            "=r"(rr[22]), "=r"(rr[23]), "=r"(rr[24]), "=r"(rr[25]), "=r"(rr[26]), "=r"(rr[27]), "=r"(rr[28]),
-            "=r"(rr[29]), "=r"(rr[30]), "=r"(rr[31])
-          : "r"(tmem + ((uint32_t)(32 * q) << 16) + 32u * t)
+            "=r"(rr[15])
+          : "r"(tmem + ((uint32_t)(32 * q) << 16) + 16u * t)
           : "memory");
       asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
       const int r = t * 128 + 32 * q + lane;
@@ -367,7 +356,7 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
         float* out = s_der + (size_t)dv * (EPB * Np) + e2 * Np;
 #pragma unroll
         for (int o = 0; o < N1; ++o) {
-          const float val = __uint_as_float(rr[o]) + __uint_as_float(rr[8 + o]) + __uint_as_float(rr[16 + o]);
+          const float val = __uint_as_float(rr[o]) + __uint_as_float(rr[8 + o]);
           const int po = d == 0 ? o + N1 * line : (d == 1 ? (line % N1) + N1 * o + NF * (line / N1) : line + NF * o);
           out[po] = val;
         }

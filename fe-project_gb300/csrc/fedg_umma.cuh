@@ -20,6 +20,12 @@ __host__ __device__ constexpr uint32_t umma_idesc_bf16(int M, int N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
+// Instruction descriptor of tcgen05.mma kind::tf32: FP32 accumulator, TF32 A and B (format 2), both
+// K-major, M x N tile.
+__host__ __device__ constexpr uint32_t umma_idesc_tf32(int M, int N) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
 // polls of a drain wait, and the default limit of the normal-path waits
 constexpr int DRAIN_POLLS = 1 << 20;
 
