@@ -47,7 +47,15 @@ DT_STABLE = 0.005  # C5 geometry (h = 100 m, p = 7): the oracle is stable at 0.0
 PATH_PREC = {"pair": 2, "mixed": 1, "fp64": 0}
 PATH_TOL = {"pair": 1e-13, "mixed": 1e-10, "fp64": 1e-10}
 PATH_ITER = {"pair": 30, "mixed": 20, "fp64": 20}
-PATH_NAME = {"pair": "learned+pair", "mixed": "learned+fp32", "fp64": "plain_fp64"}
+PATH_NAME = {"pair": "pair", "mixed": "fp32", "fp64": "plain_fp64"}
+# FP64 flops of the plain column solve per node and launch, counted on FElib's algorithm (dense
+# block LU with partial pivoting of the 3N1 x 3N1 element blocks, hevi_common_linalgebra.F90:2296-2445):
+# per element column (n = 24 at p = 7) 2n^3/3 for the factorisation plus 4 right-hand sides x 2n^2
+# for the substitutions, per node (/ N1); the MOMX/MOMY element solves (N1 x N1, 3 right-hand sides)
+# and two residual evaluations (Dz of three fluxes, VPOrdM1, Lift: ~100 flop per node each)
+def fp64_vi_flops_per_node(N1):
+    n = 3 * N1
+    return (2 * n ** 3 / 3 + 4 * 2 * n * n) / N1 + (2 * N1 ** 3 / 3 + 3 * 2 * N1 * N1) / N1 + 2 * 100
 PATH_DTYPE = {"pair": "f32x2", "mixed": "f32+f32x2", "fp64": "f64"}
 # DRAM bytes per node of one launch of the dominant kernel, measured by ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum of one launch on the 32x32x16-element slice, 8,388,608 nodes), per path
@@ -229,6 +237,40 @@ def fp64_dgemm_tflops(torch, dev):
         best = min(best, e0.elapsed_time(e1))
     del a, b
     return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def c4_guess_bench(np, torch, fl, cases, stream, nsteps=10):
+    """BASELINE's learned-guess configuration: the C2 geometry (p = 7, 800 m elements, 64 levels per
+    column: 193 -> 256 -> 256 -> 192), trained with Adam (lr 1e-3, batch 4096) on 204,800 (column state,
+    converged increment) pairs that the plain solver generates from 20 seeds of random bubbles and
+    winds; then, on a held-out seed, the mean Newton solves per implicit column solve and ms per step
+    with and without the learned iterate, in the FP32 mode (tol 1e-10) and the float-pair mode (tol
+    1e-13), on a 16x16x8-element slice at dt 0.04 s (the stable step of this mesh)."""
+    from fedg import guess
+
+    dt = 0.04
+    base = cases.C2().scaled(8, 8, 8)
+    t0 = time.perf_counter()
+    net, info = guess.build_guess(base, dt, seeds=range(20), nsteps=2, per_stage_keep=2560, train_steps=2000,
+                                  batch=4096, lr=1e-3)
+    info["build_s"] = time.perf_counter() - t0
+    case = guess.random_case(cases.C2().scaled(16, 16, 8), np.random.default_rng(1000))
+    q, b = cases.initial_state(case)
+    ctx = fl.Context(case)
+    ctx.set_base_state(b["dens_hyd"], b["pres_hyd"], b["therm_hyd"])
+    net.attach(ctx)
+    out = {"training": info, "workload": f"C2 geometry, {case.NeX}x{case.NeY}x{case.NeZ} elements, dt {dt} s, "
+                                          f"{nsteps} steps, held-out seed", "paths": {}}
+    for name, prec, tol in (("fp32", fl.PREC_MIXED, 1e-10), ("pair", fl.PREC_PAIR, 1e-13)):
+        for g in (False, True):
+            qd = [ctx.tensor(a) for a in q]
+            ctx.update(qd, 1, prec=prec, dt=dt, max_iter=30, tol=tol, use_guess=g)
+            ms, nf, its = _timed_update(ctx, torch, torch.cuda.ExternalStream(ctx.stream_handle), qd, nsteps,
+                                        dict(prec=prec, dt=dt, max_iter=30, tol=tol, use_guess=g))
+            out["paths"][name + ("_learned" if g else "_plain")] = {
+                "mean_newton_solves": its, "ms_per_step": ms / nsteps, "nonconverged_columns": nf, "newton_tol": tol}
+    ctx.close()
+    return out
 
 
 def _timed_update(ctx, torch, stream, qd, steps, opts):
@@ -495,8 +537,9 @@ def run_fedg(args):
     path = args.path
     prec = PATH_PREC[path]
     use_guess = path != "fp64" and bool(args.guess)
+    guess_side = path != "fp64" and not use_guess and not args.no_guess_side
     net, ginfo = None, None
-    if use_guess:
+    if use_guess or guess_side:
         # the C5 column network (128 levels: 385 -> 256 -> 256 -> 384), trained on the GPU with the
         # library's kernels on (stage input, converged increment) pairs of the plain solver on a
         # 16x16x16-element slice of the same geometry, 8 noise/wind seeds
@@ -517,7 +560,7 @@ def run_fedg(args):
     q_host = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory() for a in q]
     del q
     if net is not None:
-        net.attach(ctx)
+        net.attach(ctx)  # used by the headline only with --guess 1; otherwise by the with_guess side run
     stream = torch.cuda.ExternalStream(ctx.stream_handle)
     if args.tol is not None:
         PATH_TOL[path] = args.tol
@@ -622,12 +665,28 @@ def run_fedg(args):
 
     # the headline path without the learned guess, the other precision mode, and the plain FP64 path, on
     # the same state
-    noguess, plain, acc, other = None, None, None, None
+    noguess, withguess, plain, acc, other = None, None, None, None, None
     if rank == 0 and use_guess:
         o2 = dict(opts, use_guess=False)
         ms2, nf2, its2 = _timed_update(ctx, torch, stream, qd, args.steps, o2)
         noguess = {"value": dofs_stage * args.steps / (ms2 * 1e-3), "unit": UNIT, "ms_per_step": ms2 / args.steps,
                    "newton_tol": opts["tol"], "mean_newton_solves": its2, "nonconverged_columns": nf2}
+    if rank == 0 and guess_side:
+        # the headline path with the learned initial iterate, on the same state
+        o2 = dict(opts, use_guess=True)
+        ctx.update(qd, 1, **o2)
+        fl.prof_reset(ctx)
+        fl.prof_enable(ctx, True)
+        ms2, nf2, its2 = _timed_update(ctx, torch, stream, qd, args.steps, o2)
+        fl.prof_enable(ctx, False)
+        pg = fl.prof_read(ctx)
+        withguess = {"value": dofs_stage * args.steps / (ms2 * 1e-3), "unit": UNIT, "ms_per_step": ms2 / args.steps,
+                     "newton_tol": opts["tol"], "mean_newton_solves": its2, "nonconverged_columns": nf2,
+                     "guess_network_ms_per_step": pg["mlp"][0] / args.steps,
+                     "column_solve_ms_per_step": pg["vi_mixed"][0] / args.steps}
+    c4 = None
+    if rank == 0 and path != "fp64" and not args.no_c4:
+        c4 = c4_guess_bench(np, torch, fl, cases, stream)
     other_path = {"pair": "mixed", "mixed": "pair"}.get(path)
     if rank == 0 and other_path and not args.no_other:
         op_ = dict(opts, prec=PATH_PREC[other_path], tol=PATH_TOL[other_path], max_iter=PATH_ITER[other_path])
@@ -635,7 +694,7 @@ def run_fedg(args):
         mso, nfo, itso = _timed_update(ctx, torch, stream, qd, args.steps, op_)
         other = {"value": dofs_stage * args.steps / (mso * 1e-3), "unit": UNIT, "ms_per_step": mso / args.steps,
                  "newton_tol": op_["tol"], "mean_newton_solves": itso, "nonconverged_columns": nfo,
-                 "path": PATH_NAME[other_path] if use_guess else PATH_NAME[other_path].replace("learned+", "")}
+                 "path": ("learned+" if use_guess else "") + PATH_NAME[other_path]}
     if rank == 0 and prec != fl.PREC_FP64 and not args.no_plain:
         # FElib's algorithm in FP64 on the GPU from the same initial state, and the error of each
         # precision mode against it after the same number of steps
@@ -648,9 +707,23 @@ def run_fedg(args):
         ncmp = args.compare_steps
         o64 = dict(opts, prec=fl.PREC_FP64, use_guess=False, tol=1e-10, max_iter=20)
         ctx.update(q_ref, max(ncmp - 2, 0), **o64)
+        fl.prof_reset(ctx)
+        fl.prof_enable(ctx, True)
         pms, nf64, its64 = _timed_update(ctx, torch, stream, q_ref, 2, o64)
+        fl.prof_enable(ctx, False)
+        p64 = fl.prof_read(ctx)
         plain = {"value": dofs_stage * 2 / (pms * 1e-3), "unit": UNIT, "ms_per_step": pms / 2, "steps": 2,
-                 "newton_tol": 1e-10, "mean_newton_solves": its64, "nonconverged_columns": nf64}
+                 "newton_tol": 1e-10, "mean_newton_solves": its64, "nonconverged_columns": nf64,
+                 "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in p64.items() if v[1]}}
+        vt, vn = p64.get("vi_fp64", (0.0, 0))
+        if vn and fp64_tf > 0:
+            fpn = fp64_vi_flops_per_node(case.N1) * max(its64, 1.0)
+            ach = fpn * nodes / (vt / vn * 1e-3) / 1e12
+            plain["roofline_fp64_column_solve"] = {
+                "bound": "fp64", "kernel": "vi_fp64", "achieved_tflops": ach, "peak_tflops": fp64_tf,
+                "frac": ach / fp64_tf, "flop_per_node": fpn, "avg_launch_ms": vt / vn,
+                "flop_count": "FElib's dense block LU with partial pivoting, its substitutions and the residuals, "
+                              "per Newton solve; the kernel itself skips the DENS rows' structural zeros"}
         ctx.update(q_mix, ncmp, **opts)
         acc = {"steps": ncmp, "rel_l2_vs_plain_fp64": _full_field_errors(np, q_mix, q_ref, dnorm2, dens_hyd, therm_hyd)}
         if other is not None:
@@ -682,7 +755,7 @@ def run_fedg(args):
             "vs_baseline": None, "dtype": PATH_DTYPE[path], "data": "synthetic",
             "config": {"workload": f"{case.name}: p=7 {case.NeX}x{case.NeY}x{case.NeZ} elements, HEVI IMEX-ARK232, "
                                    f"constBVFreq N=0.01, +-0.1K noise below 500 m, u=5 m/s",
-                       "path": PATH_NAME[path] if use_guess or path == "fp64" else PATH_NAME[path].replace("learned+", ""),
+                       "path": ("learned+" if use_guess else "") + PATH_NAME[path],
                        "one_hour_accuracy": "fe-project_gb300/fedg/precision.py (C1 warm bubble and C2 density current)",
                        "dt": DT_STABLE, "dt_baseline": 0.5, "newton_tol": opts["tol"], "newton_max_iter": opts["max_iter"],
                        "mean_newton_solves": its, "nonconverged_columns": nfail, "finite": finite,
@@ -695,7 +768,9 @@ def run_fedg(args):
             "cpu_baseline": cb, "e2e": e2e, "gpu_launches": gpu_launches, "clocks": clocks,
             "guess_training": ginfo,
             "without_guess": noguess,
-            ("learned_fp32" if other_path == "mixed" else "learned_pair"): other,
+            "with_guess": withguess,
+            "learned_guess_c4": c4,
+            ("fp32_mode" if other_path == "mixed" else "pair_mode"): other,
             "plain_fp64": plain,
             "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
             "accuracy": acc,
@@ -717,7 +792,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["fedg", "reference"], default="fedg")
     ap.add_argument("--path", choices=["pair", "mixed", "fp64"], default=os.environ.get("FEDG_BENCH_PATH", "pair"))
-    ap.add_argument("--guess", type=int, default=1)
+    ap.add_argument("--guess", type=int, default=0, help="1: the headline path uses the learned Newton iterate")
+    ap.add_argument("--no-guess-side", action="store_true", help="skip the with_guess side measurement")
+    ap.add_argument("--no-c4", action="store_true", help="skip the C4 learned-guess measurement")
     ap.add_argument("--tol", type=float, default=None, help="Newton tolerance of the timed path (default per path)")
     ap.add_argument("--train-steps", type=int, default=2000)
     ap.add_argument("--compare-steps", type=int, default=4,
