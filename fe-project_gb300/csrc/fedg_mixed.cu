@@ -55,6 +55,7 @@ struct StageBufs {
   double* dtrc;         // stage 3: DDENS before the modal filter (DDENS_TRC of the tracer flux; NULL: none)
   int* tc_err;          // raised when a tensor-core contraction's barrier wait runs out
   int tc_polls;         // poll limit of that wait
+  float2* a0[3];        // stage 1: A(q^n) of DENS, MOMZ, RHOT (FP32, lo = 0) for the column solves
 };
 
 // ---- derivative contractions on the tensor cores (3xTF32 split, FP32 accumulation) ----
@@ -409,6 +410,11 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
       tim[VRT] = -(op.E33 * szv[VRT] + lb * di[VRT * S2 + fb] + lt * di[VRT * S2 + ft]);
       tim[VMX] = -(lb * di[VMX * S2 + fb] + lt * di[VMX * S2 + ft]);
       tim[VMY] = -(lb * di[VMY * S2 + fb] + lt * di[VMY * S2 + ft]);
+      if (B.a0[0]) {
+        B.a0[0][g] = make_float2(tim[VD], 0.f);
+        B.a0[1][g] = make_float2(tim[VMZ], 0.f);
+        B.a0[2][g] = make_float2(tim[VRT], 0.f);
+      }
     } else {
 #pragma unroll
       for (int v = 0; v < 5; ++v) tim[v] = __ldg(B.TI[v] + g);
@@ -618,6 +624,7 @@ struct MixedState {
   float** d_ptrs = nullptr; // device arrays of float pointers: TI[5], guess[3], QSF[5]
   float* gsc = nullptr;     // block-Thomas history of the column solve
   int* tc_err = nullptr;    // raised by a stage kernel whose tensor-core barrier wait ran out
+  float2* a0buf = nullptr;  // [3][n] A(q^n) of DENS, MOMZ, RHOT from stage 1 (first Newton residual)
   // float-pair mode (FEDG_PREC_PAIR), allocated on first use: S3 | SF | TI | QSF | QNF as pairs
   float2* pbuf = nullptr;
   void** d_pptrs = nullptr;  // device arrays of pointers: TI[5], QSF[5] (pairs)
@@ -658,6 +665,7 @@ void mixed_free(MixedState* m) {
   cudaFree(m->d_ptrs);
   cudaFree(m->gsc);
   cudaFree(m->tc_err);
+  cudaFree(m->a0buf);
   cudaFree(m->pbuf);
   cudaFree(m->d_pptrs);
   cudaFree(m->prof5);
@@ -679,6 +687,7 @@ static int mixed_setup(fedg_ctx* c) {
       (e = cudaMalloc(&m->d_ptrs, sizeof(float*) * 13)) != cudaSuccess ||
       (e = cudaMalloc(&m->gsc, sizeof(float) * vi_cols_scratch_floats(c->n))) != cudaSuccess ||
       (e = cudaMalloc(&m->tc_err, sizeof(int))) != cudaSuccess ||
+      (e = cudaMalloc(&m->a0buf, sizeof(float2) * 3 * c->n)) != cudaSuccess ||
       (e = cudaMemset(m->tc_err, 0, sizeof(int))) != cudaSuccess) {
     mixed_free(m);
     return api_cuda_fail(e, "fedg_update(mixed): allocation");
@@ -979,6 +988,7 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
   std::memset(&B, 0, sizeof(B));
   B.tc_err = m->tc_err;
   B.tc_polls = c->tc_polls;
+  for (int v = 0; v < 3; ++v) B.a0[v] = m->a0buf + (size_t)v * c->n;
   for (int v = 0; v < 5; ++v) {
     B.qn[v] = q[v];
     B.qnf[v] = m->QNF(v);
@@ -1013,6 +1023,7 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
       BP.SF[v] = m->SFp(v);
       BP.TI[v] = m->TIp(v);
     }
+    for (int v = 0; v < 3; ++v) BP.a0[v] = m->a0buf + (size_t)v * c->n;
     F5c qc{{q[0], q[1], q[2], q[3], q[4]}};
     Dev5p dv{{m->QNFp(0), m->QNFp(1), m->QNFp(2), m->QNFp(3), m->QNFp(4)}};
     r = tracked(c, FEDG_K_AUX, [&] {
@@ -1069,7 +1080,8 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
       gptr = (const float* const*)(m->d_ptrs + 5);
     }
     return tracked(c, FEDG_K_MVI, [&] {
-      return launch_vi_cols(c->N1, c->op, m->opx, px, qin, z, gptr, qo, to, m->gsc, c->d_status, c->d_cnt, va, pair,
+      const A3 a0{{m->a0buf, m->a0buf + c->n, m->a0buf + 2 * c->n}};
+      return launch_vi_cols(c->N1, c->op, m->opx, px, qin, z, a0, gptr, qo, to, m->gsc, c->d_status, c->d_cnt, va, pair,
                             c->stream);
     });
   };

@@ -52,6 +52,10 @@ struct ProfX {
 struct X5 {
   const float2* v[5];
 };
+// the implicit operator A(var0) of DENS, MOMZ, RHOT as float pairs, written by the stage-1 kernel
+struct A3 {
+  const float2* v[3];
+};
 
 // controls of the mixed-precision column solve
 struct MixViArgs {
@@ -98,6 +102,7 @@ struct StagePairBufs {
   int xdinp;
   float xs[3];
   double* dtrc;         // stage 3: DDENS before the modal filter (DDENS_TRC of the tracer flux; NULL: none)
+  float2* a0[3];        // stage 1 (HEVI): A(q^n) of DENS, MOMZ, RHOT for the column solves' first residual
 };
 int launch_stage_pair_heve(int N1, int stage, const OpsP& op, const ProfP& pf, const double* dens64,
                            const StagePairBufs& B, const PairCoef& cf, int Ne, int filt, cudaStream_t s);
@@ -106,14 +111,15 @@ int launch_stage_pair(int N1, int stage, const OpsP& op, const ProfP& pf, const 
 
 // Mixed-precision column solve (fedg_vicol.cu).  qin: stage input q* (float pairs); z: var0
 // (FP64; alph and the plain initial iterate); guess: FP32 increments of (DENS, MOMZ, RHOT) over
-// q*, or NULL.
+// q*, or NULL; a0: the implicit operator at var0 from the stage-1 kernel (the first residual when
+// the iterate starts at var0).
 // qsf: FP32 deviation copy of Q (MOMX/MOMY relative to DENS_hyd*(Uref, Vref)); tout: (Q - q*)/
 // impl_fac in FP32; gsc: vi_cols_scratch_floats(n) floats of block-Thomas history; status[ncol]:
 // solves used, -1 not converged, -2 non-finite; cnt[3]: failed columns, solves, converged columns.
 size_t vi_cols_scratch_floats(size_t nodes);
 // pair_out: qsf and tout are float-pair (float2) arrays instead of FP32 ones
 int launch_vi_cols(int N1, const Ops& op, const OpsX& ox, const ProfX& px, const X5& qin, const F5c& z,
-                   const float* const* guess, void* const* qsf, void* const* tout, float* gsc, int* status,
+                   const A3& a0, const float* const* guess, void* const* qsf, void* const* tout, float* gsc, int* status,
                    unsigned long long* cnt, const MixViArgs& a, bool pair_out, cudaStream_t s);
 
 }  // namespace fedg

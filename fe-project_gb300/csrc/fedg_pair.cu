@@ -321,6 +321,11 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
       tim[VRT] = -(E33 * szv[VRT] + lb * dv(VRT, fb) + lt * dv(VRT, ft));
       tim[VMX] = -(lb * dv(VMX, fb) + lt * dv(VMX, ft));
       tim[VMY] = -(lb * dv(VMY, fb) + lt * dv(VMY, ft));
+      if (B.a0[0]) {
+        B.a0[0][g] = f2_pack(tim[VD]);
+        B.a0[1][g] = f2_pack(tim[VMZ]);
+        B.a0[2][g] = f2_pack(tim[VRT]);
+      }
     } else {
 #pragma unroll
       for (int v = 0; v < 5; ++v) tim[v] = ld2(B.TI[v] + g);

@@ -274,6 +274,30 @@ __device__ float col_residual(const OpsX& ox, const Col<N1>& c, const ProfX& px,
 }
 
 // ---------------------------------------------------------------------------------------------
+// First residual of a column whose iterate starts at var0: b = q* - var0 + impl_fac A(var0), with
+// A(var0) the implicit operator that the stage-1 kernel evaluated at q^n = var0 for its own
+// implicit tendency (both implicit stages of an ARK232 step start at var0, so one evaluation
+// serves both).  Formed in float pairs and rounded into c.Bf; no operator evaluation here.  The
+// first correction is never judged by it (convergence is tested on the certifying residual).
+template <int N1>
+__device__ void col_first_residual(const Col<N1>& c, const X5& qin, const A3& a0, float2 impl2) {
+  const int k = c.k;
+  const int gv[3] = {VD, VMZ, VRT};
+  const f2 impl = f2_of(impl2);
+#pragma unroll 4
+  for (int e = 0; e < c.NeZ; ++e) {
+    const int l = e * N1 + k;
+    const size_t gi = c.g(e);
+#pragma unroll
+    for (int v = 0; v < 3; ++v) {
+      const f2 b = f2_add(f2_sub(f2_of(__ldg(qin.v[gv[v]] + gi)), f2_of(c.P[3 * l + v])),
+                          f2_mul(impl, f2_of(__ldg(a0.v[v] + gi))));
+      c.Bf[3 * l + v] = f2_to_f(b);
+    }
+  }
+  __syncwarp();
+}
+
 // Element LU without pivoting of the 3*N1 rows held 3 per lane (row 3k+v in lane k: v = DENS,
 // MOMZ, RHOT of node k), with four right-hand sides; on return r = A^-1 r.  Pivot rows reach the
 // other lanes of the column group by shuffles (width N1); every register index is a compile-time
@@ -750,7 +774,7 @@ __device__ void col_neumann(const Ops& op, const ProfX& px, float kapf, const Co
 // ---------------------------------------------------------------------------------------------
 template <int N1, bool PO>
 __global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, const ProfX px, const X5 qin, const F5c z,
-                                                const float* const* guess, void* const* qsf, void* const* tout,
+                                                const A3 a0, const float* const* guess, void* const* qsf, void* const* tout,
                                                 float* __restrict__ gsc, int* status, unsigned long long* cnt,
                                                 const MixViArgs args, int ncol) {
   static_assert(32 / N1 * N1 == 32, "a warp's columns cover 32 nodes of a level (whole G-history lines)");
@@ -966,9 +990,9 @@ __global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, 
   const size_t gcolumn = (size_t)col, glayer = (size_t)ncol;  // G history rows of this column
   const GHist gh{gsc, (size_t)ncol * (size_t)L};
   const float cref = (float)args.cref;
-  // One call site per routine (the first residual is the FP32 one and is not tested; every
-  // column takes the first correction), which keeps the kernel's code small enough for the
-  // instruction caches.
+  // One call site per routine, which keeps the kernel's code small enough for the instruction
+  // caches.  The first residual is not tested (every column takes the first correction); from
+  // var0 it is formed from the stage kernel's A(var0) instead of a second operator evaluation.
   // Corrections: the first is an LU correction (col_solve); after an LU correction the next one
   // is a truncated Neumann series (col_neumann, when args.neumann > 0), which keeps going while
   // each one cuts the certifying residual at least fourfold; a column whose residual did not
@@ -978,9 +1002,11 @@ __global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, 
   bool active = true, want_lu = true, last_lu = true;
   float err_prev = 0.f;
   while (true) {
-    const bool cert = nsolve > 0 && args.check64;
-    const float err = cert ? col_residual<N1, true>(ox, c, px, qin, args.impl2, cref)
-                           : col_residual<N1, false>(ox, c, px, qin, args.impl2, cref);
+    // the first residual comes from the stage's A(var0) when the iterate starts at var0; every
+    // other one is the certifying float-pair residual
+    float err = 0.f;
+    if (nsolve == 0 && !guess && a0.v[0]) col_first_residual<N1>(c, qin, a0, args.impl2);
+    else err = col_residual<N1, true>(ox, c, px, qin, args.impl2, cref);
     if (active && nsolve > 0) {
       if (err != err) { st = -2; active = false; }
       else if ((double)err <= args.tol) { st = nsolve; active = false; }
@@ -1033,7 +1059,8 @@ __global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, 
 }
 
 template <int N1, bool PO>
-int launch_n(const Ops& op, const OpsX& ox, const ProfX& px, const X5& qin, const F5c& z, const float* const* guess,
+int launch_n(const Ops& op, const OpsX& ox, const ProfX& px, const X5& qin, const F5c& z, const A3& a0,
+             const float* const* guess,
              void* const* qsf, void* const* tout, float* gsc, int* status, unsigned long long* cnt,
              const MixViArgs& a, cudaStream_t s) {
   constexpr int C = 32 / N1;
@@ -1043,7 +1070,8 @@ int launch_n(const Ops& op, const OpsX& ox, const ProfX& px, const X5& qin, cons
   const int ncol = op.NeX * op.NeY * N1 * N1;
   auto kfn = k_vi_cols<N1, PO>;
   cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  kfn<<<(ncol + 2 * C - 1) / (2 * C), 64, smem, s>>>(op, ox, px, qin, z, guess, qsf, tout, gsc, status, cnt, a, ncol);
+  kfn<<<(ncol + 2 * C - 1) / (2 * C), 64, smem, s>>>(op, ox, px, qin, z, a0, guess, qsf, tout, gsc, status, cnt, a,
+                                                     ncol);
   return (int)cudaGetLastError();
 }
 
@@ -1052,13 +1080,13 @@ int launch_n(const Ops& op, const OpsX& ox, const ProfX& px, const X5& qin, cons
 size_t vi_cols_scratch_floats(size_t nodes) { return (size_t)9 * nodes; }
 
 int launch_vi_cols(int N1, const Ops& op, const OpsX& ox, const ProfX& px, const X5& qin, const F5c& z,
-                   const float* const* guess, void* const* qsf, void* const* tout, float* gsc, int* status,
+                   const A3& a0, const float* const* guess, void* const* qsf, void* const* tout, float* gsc, int* status,
                    unsigned long long* cnt, const MixViArgs& a, bool pair_out, cudaStream_t s) {
   switch (N1 * 2 + (pair_out ? 1 : 0)) {
-    case 8: return launch_n<4, false>(op, ox, px, qin, z, guess, qsf, tout, gsc, status, cnt, a, s);
-    case 9: return launch_n<4, true>(op, ox, px, qin, z, guess, qsf, tout, gsc, status, cnt, a, s);
-    case 16: return launch_n<8, false>(op, ox, px, qin, z, guess, qsf, tout, gsc, status, cnt, a, s);
-    case 17: return launch_n<8, true>(op, ox, px, qin, z, guess, qsf, tout, gsc, status, cnt, a, s);
+    case 8: return launch_n<4, false>(op, ox, px, qin, z, a0, guess, qsf, tout, gsc, status, cnt, a, s);
+    case 9: return launch_n<4, true>(op, ox, px, qin, z, a0, guess, qsf, tout, gsc, status, cnt, a, s);
+    case 16: return launch_n<8, false>(op, ox, px, qin, z, a0, guess, qsf, tout, gsc, status, cnt, a, s);
+    case 17: return launch_n<8, true>(op, ox, px, qin, z, a0, guess, qsf, tout, gsc, status, cnt, a, s);
   }
   return (int)cudaErrorInvalidValue;
 }
