@@ -594,11 +594,13 @@ def run_fedg(args):
         "rk": 8 * 20,                        # general IMEX advance (upper bound of the stage kinds)
         # fused stage kernels, mean of the three (FP32 deviation state in, FP64 q^n / q* ):
         # S1 q^n(f32) + q^n(f64) in -> q*_2, S3, SF out; S2 Q_2(f32), t_im, q^n, S3, SF in -> q*_3, SF out;
-        # S3 Q_3(f32), t_im, q^n, SF in -> q^n+1 (f64) + its f32 copy out
-        "stage_mixed": (20 + 40 + 40 + 20 + 20 + 20 + 20 + 40 + 20 + 20 + 40 + 20 + 20 + 40 + 20 + 40 + 20) / 3,
+        # S3 Q_3(f32), t_im, q^n, SF in -> q^n+1 (f64) + its f32 copy out; S1 also writes A(q^n) of
+        # DENS, MOMZ, RHOT (3 pairs) for the column solve's first residual
+        "stage_mixed": (20 + 40 + 40 + 20 + 20 + 20 + 20 + 40 + 20 + 20 + 40 + 20 + 20 + 40 + 20 + 40 + 20 + 24) / 3,
         # column solve: q* (float pairs) and var0 (FP64) in -> Q and t_im out, FP32 in the FP32 mode and
-        # float pairs in the pair mode; plus the three guess fields (FP32) when the guess is on
-        "vi_mixed": 8 * 5 + 8 * 5 + (8 if prec == fl.PREC_PAIR else 4) * 10 + (12 if use_guess else 0),
+        # float pairs in the pair mode; plus the three guess fields (FP32) when the guess is on, else
+        # the stage-1 kernel's A(var0) of DENS, MOMZ, RHOT (pairs) for the first residual
+        "vi_mixed": 8 * 5 + 8 * 5 + (8 if prec == fl.PREC_PAIR else 4) * 10 + (12 if use_guess else 24),
         "filter": 8 * 10, "drhot2pres": 8 * 2, "mlp": 0, "aux": 0,
     }
     avg_ms = ktime / max(klaunch, 1)
@@ -635,7 +637,7 @@ def run_fedg(args):
             dst.copy_(src, non_blocking=True)
         torch.cuda.synchronize()
         ph = [0.0, 0.0, 0.0]  # seconds in H2D, the step, D2H
-        h2d_each = []
+        h2d_each, d2h_each = [], []
         t0 = time.perf_counter()
         for _ in range(ke):
             ta = time.perf_counter()
@@ -654,12 +656,13 @@ def run_fedg(args):
             ph[1] += tc - tb
             ph[2] += td - tc
             h2d_each.append(1e3 * (tb - ta))
+            d2h_each.append(1e3 * (td - tc))
         t1 = time.perf_counter()
         nb = sum(t.numel() * 8 for t in qd)
         e2e = {"value": dofs_stage * ke / (t1 - t0), "unit": UNIT, "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb,
                "steps": ke, "ms_per_step": {"h2d": 1e3 * ph[0] / ke, "update": 1e3 * ph[1] / ke, "d2h": 1e3 * ph[2] / ke},
                "copy_gbs": {"h2d": nb * ke / max(ph[0], 1e-9) / 1e9, "d2h": nb * ke / max(ph[2], 1e-9) / 1e9},
-               "h2d_ms_each": h2d_each}
+               "h2d_ms_each": h2d_each, "d2h_ms_each": d2h_each}
         del q_e
 
     # the headline path without the learned guess, the other precision mode, and the plain FP64 path, on

@@ -18,13 +18,19 @@ elements of 800 m. One simulated hour is therefore 90,000 steps.
 
 Paths (all from the same initial state; the four HEVI paths at the same dt):
 
-  plain_fp64_tol1e-13   FP64 fused update (FElib's algorithm), Newton to tol 1e-13: the
+  plain_fp64_tol1e-14   FP64 fused update (FElib's algorithm), Newton to tol 1e-14: the
                         implicit stages converged to roundoff; the reference of the comparison.
+  plain_fp64_tol1e-13   the same at tol 1e-13 (its distance from the tol 1e-14 run is how far a
+                        1e-13 Newton tolerance alone carries a state over the run).
   plain_fp64_tol1e-10   the same at the plain method's tolerance 1e-10.
   learned_pair_tol1e-13 float-pair precision mode (FEDG_PREC_PAIR: explicit operator, Newton
                         residual and RK accumulation in float pairs, FP32 Jacobian/LU), Newton from
                         the column-guess MLP to tol 1e-13.
   learned_fp32_tol1e-10 FP32 explicit mode (FEDG_PREC_MIXED), Newton from the MLP to tol 1e-10.
+  pair_tol1e-13/1e-14,  the float-pair and FP32 modes from FElib's guess var0 (no MLP).
+  fp32_tol1e-10
+
+Each path is compared with each of the plain FP64 runs that ran (tol 1e-14, 1e-13, 1e-10).
 
 The MLP follows the learned-guess recipe:
   - 193 -> 256 -> 256 -> 192;
@@ -37,6 +43,9 @@ against their own norms.
 
 With --case C1 --eqs HEVE the warm bubble runs with its own explicit HEVE scheme (ERK_SSP_3s3o),
 plain FP64 (plain_fp64_heve) against the float-pair mode (pair_heve).
+
+With --case C5 the stably stratified C5 workload (p = 7, 100 m elements, 16 vertical elements)
+runs on --nex x --ney x --nez elements at dt 0.005 s, e.g. a 720-step window on 32 x 32 x 16.
 
 Usage (from the repository root):  PYTHONPATH=fe-project_gb300 python -m fedg.precision [--nex 8 ...]
 """
@@ -74,14 +83,18 @@ def _errors(torch, got, ref, dens_hyd, therm_hyd):
 
 
 PATHS = {
+    "plain_fp64_tol1e-14": (fl.PREC_FP64, 1e-14, False),
     "plain_fp64_tol1e-13": (fl.PREC_FP64, 1e-13, False),
     "plain_fp64_tol1e-10": (fl.PREC_FP64, 1e-10, False),
     "learned_pair_tol1e-13": (fl.PREC_PAIR, 1e-13, True),
     "learned_pair_tol1e-12": (fl.PREC_PAIR, 1e-12, True),
     "learned_pair_tol1e-11": (fl.PREC_PAIR, 1e-11, True),
     "learned_fp32_tol1e-10": (fl.PREC_MIXED, 1e-10, True),
+    "pair_tol1e-14": (fl.PREC_PAIR, 1e-14, False),
+    "pair_tol1e-13": (fl.PREC_PAIR, 1e-13, False),
+    "fp32_tol1e-10": (fl.PREC_MIXED, 1e-10, False),
 }
-REFS = ("plain_fp64_tol1e-13", "plain_fp64_tol1e-10")
+REFS = ("plain_fp64_tol1e-14", "plain_fp64_tol1e-13", "plain_fp64_tol1e-10")
 # HEVE (explicit ERK_SSP_3s3o, no implicit solve): FP64 against float pairs
 HEVE_PATHS = {
     "plain_fp64_heve": (fl.PREC_FP64, 0.0, False),
@@ -91,7 +104,7 @@ HEVE_REFS = ("plain_fp64_heve",)
 
 
 def run(nex=8, ney=8, nez=8, dt=0.04, hours=1.0, checkpoint_min=10.0, chunk=250, paths=tuple(PATHS), seeds=20,
-        train_steps=2000, case_name="C2", eqs="HEVI", out=sys.stdout):
+        train_steps=2000, case_name="C2", eqs="HEVI", out=sys.stdout, steps=None, concurrent=False, max_iter=30):
     import dataclasses
 
     import torch
@@ -100,13 +113,16 @@ def run(nex=8, ney=8, nez=8, dt=0.04, hours=1.0, checkpoint_min=10.0, chunk=250,
     # HEVI IMEX scheme of the precision form or (eqs="HEVE") with its own explicit HEVE scheme
     heve = eqs == "HEVE"
     table, refs = (HEVE_PATHS, HEVE_REFS) if heve else (PATHS, REFS)
-    base = cases.C2() if case_name == "C2" else dataclasses.replace(cases.C1(), eqs=eqs)
+    if case_name == "C1":
+        base = dataclasses.replace(cases.C1(), eqs=eqs)
+    else:
+        base = cases.C2() if case_name == "C2" else cases.C5()
     case = base.scaled(nex, ney, nez)
-    nsteps = int(round(hours * 3600.0 / dt))
+    nsteps = steps if steps else int(round(hours * 3600.0 / dt))
     ck_every = max(1, int(round(checkpoint_min * 60.0 / dt)))
     scheme = "HEVE ERK_SSP_3s3o" if heve else "HEVI IMEX-ARK232"
     info = {"workload": f"{case_name} recipe p={case.porder} {nex}x{ney}x{nez} elements, {scheme}",
-            "dt": dt, "steps": nsteps, "simulated_s": nsteps * dt, "paths": list(paths)}
+            "dt": dt, "steps": nsteps, "simulated_s": nsteps * dt, "paths": list(paths), "max_iter": max_iter}
     net = None
     if any(table[p][2] for p in paths):
         t0 = time.perf_counter()
@@ -123,25 +139,50 @@ def run(nex=8, ney=8, nez=8, dt=0.04, hours=1.0, checkpoint_min=10.0, chunk=250,
     therm_hyd = ctx.tensor(b["therm_hyd"])
     q0 = [ctx.tensor(a) for a in q]
     states = {p: [t.clone() for t in q0] for p in paths}
+    # concurrent: one context (own stream and scratch) and one host thread per path, so that the
+    # small launch-bound cases of different paths share the GPU; ms_per_step is then wall time
+    # under that sharing, not a per-path speed
+    ctxs = {p: ctx for p in paths}
+    if concurrent and sum(1 for p in paths if table[p][2]) > 1:
+        raise ValueError("concurrent paths share one guess network: run at most one learned path")
+    if concurrent:
+        for p in paths[1:]:
+            c2 = fl.Context(case)
+            c2.set_base_state(b["dens_hyd"], b["pres_hyd"], b["therm_hyd"])
+            ctxs[p] = c2
+    info["concurrent_paths"] = bool(concurrent)
     if net is not None:
-        net.attach(ctx)
+        for c2 in {id(c): c for c in ctxs.values()}.values():
+            net.attach(c2)
     stats = {p: {"s": 0.0, "fail": 0, "its": 0.0} for p in paths}
     done = 0
     print(json.dumps({"setup": info}), file=out, flush=True)
     rec = None
+
+    def advance(p, n):
+        prec, tol, guess = table[p]
+        t0 = time.perf_counter()
+        nf, its = ctxs[p].update(states[p], n, eqs=fl.HEVE if heve else fl.HEVI, prec=prec, dt=dt, max_iter=max_iter,
+                                 tol=tol, use_guess=guess, sync=not concurrent)
+        ctxs[p].sync()
+        s = stats[p]
+        s["s"] += time.perf_counter() - t0
+        s["fail"] += nf
+        s["its"] += its * n
+
     while done < nsteps:
         n = min(chunk, nsteps - done, ck_every - done % ck_every)
-        for p in paths:
-            prec, tol, guess = table[p]
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            nf, its = ctx.update(states[p], n, eqs=fl.HEVE if heve else fl.HEVI, prec=prec, dt=dt, max_iter=30,
-                                 tol=tol, use_guess=guess)
-            torch.cuda.synchronize()
-            s = stats[p]
-            s["s"] += time.perf_counter() - t0
-            s["fail"] += nf
-            s["its"] += its * n
+        torch.cuda.synchronize()
+        if concurrent:
+            import concurrent.futures as cf
+
+            with cf.ThreadPoolExecutor(max_workers=len(paths)) as ex:
+                for fut in [ex.submit(advance, p, n) for p in paths]:
+                    fut.result()
+        else:
+            for p in paths:
+                advance(p, n)
+        torch.cuda.synchronize()
         done += n
         if done % ck_every == 0 or done == nsteps:
             finite = all(bool(torch.isfinite(t).all().item()) for st in states.values() for t in st)
@@ -160,13 +201,14 @@ def run(nex=8, ney=8, nez=8, dt=0.04, hours=1.0, checkpoint_min=10.0, chunk=250,
             print(json.dumps(rec), file=out, flush=True)
             if not finite:
                 break
-    ctx.close()
+    for c2 in {id(c): c for c in ctxs.values()}.values():
+        c2.close()
     return rec
 
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
-    ap.add_argument("--case", choices=["C2", "C1"], default="C2")
+    ap.add_argument("--case", choices=["C2", "C1", "C5"], default="C2")
     ap.add_argument("--eqs", choices=["HEVI", "HEVE"], default="HEVI",
                     help="HEVE: C1 with its explicit scheme, paths " + ", ".join(HEVE_PATHS))
     ap.add_argument("--nex", type=int, default=8)
@@ -174,6 +216,10 @@ def main(argv=None):
     ap.add_argument("--nez", type=int, default=8)
     ap.add_argument("--dt", type=float, default=0.04)
     ap.add_argument("--hours", type=float, default=1.0)
+    ap.add_argument("--steps", type=int, default=None, help="number of steps (overrides --hours)")
+    ap.add_argument("--max-iter", type=int, default=30, help="Newton solves per implicit stage at most")
+    ap.add_argument("--concurrent", action="store_true",
+                    help="run the paths at the same time, one context and host thread each")
     ap.add_argument("--checkpoint-min", type=float, default=10.0)
     ap.add_argument("--chunk", type=int, default=250)
     ap.add_argument("--paths", default=None, help="comma-separated subset of " + ", ".join(PATHS))
@@ -190,7 +236,8 @@ def main(argv=None):
     unknown = [p for p in paths if p not in table]
     if unknown:
         ap.error(f"unknown paths {unknown}")
-    run(a.nex, a.ney, a.nez, a.dt, a.hours, a.checkpoint_min, a.chunk, paths, a.seeds, a.train_steps, a.case, a.eqs)
+    run(a.nex, a.ney, a.nez, a.dt, a.hours, a.checkpoint_min, a.chunk, paths, a.seeds, a.train_steps, a.case, a.eqs,
+        steps=a.steps, concurrent=a.concurrent, max_iter=a.max_iter)
     return 0
 
 
