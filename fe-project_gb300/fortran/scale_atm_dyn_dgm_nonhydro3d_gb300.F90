@@ -35,6 +35,8 @@ module scale_atm_dyn_dgm_nonhydro3d_gb300
   public :: atm_dyn_dgm_nonhydro3d_gb300_set_base_state
   public :: atm_dyn_dgm_nonhydro3d_gb300_load_guess
   public :: atm_dyn_dgm_nonhydro3d_gb300_update
+  public :: atm_dyn_dgm_nonhydro3d_gb300_restart_write
+  public :: atm_dyn_dgm_nonhydro3d_gb300_restart_read
 
   integer(c_int), parameter :: FEDG_HEVE = 0, FEDG_HEVI = 1
   integer(c_int), parameter, public :: FEDG_PREC_FP64 = 0, FEDG_PREC_MIXED = 1, FEDG_PREC_PAIR = 2
@@ -42,6 +44,12 @@ module scale_atm_dyn_dgm_nonhydro3d_gb300
   type, bind(C) :: fedg_update_opts
     integer(c_int) :: eqs, prec, max_iter, use_guess
     real(c_double) :: dt, tol
+  end type
+
+  type, bind(C) :: fedg_restart_info
+    integer(c_long_long) :: step
+    real(c_double) :: time, dt
+    character(kind=c_char) :: scheme(32)
   end type
 
   type, bind(C) :: fedg_mesh_desc
@@ -139,6 +147,21 @@ module scale_atm_dyn_dgm_nonhydro3d_gb300
     integer(c_int) function fedg_guess_load(ctx, g) bind(C, name="fedg_guess_load")
       import :: c_int, c_ptr
       type(c_ptr), value :: ctx, g
+    end function
+    integer(c_int) function fedg_restart_write(ctx, path, q, info) bind(C, name="fedg_restart_write")
+      import :: c_int, c_ptr, c_char, fedg_restart_info
+      type(c_ptr), value :: ctx
+      character(kind=c_char), intent(in) :: path(*)
+      type(c_ptr), intent(in) :: q(5)
+      type(fedg_restart_info), intent(in) :: info
+    end function
+    integer(c_int) function fedg_restart_read(ctx, path, q, base, info) bind(C, name="fedg_restart_read")
+      import :: c_int, c_ptr, c_char, fedg_restart_info
+      type(c_ptr), value :: ctx
+      character(kind=c_char), intent(in) :: path(*)
+      type(c_ptr), intent(in) :: q(5)
+      type(c_ptr), value :: base
+      type(fedg_restart_info), intent(out) :: info
     end function
   end interface
 
@@ -239,6 +262,52 @@ contains
     nfail = ierr
     if (present(mean_solves)) mean_solves = its
   end subroutine atm_dyn_dgm_nonhydro3d_gb300_update
+
+  !> Write the restart state (scale_file_restart_meshfield.F90:136-186): the five prognostic fields, the
+  !! registered base state and the fast paths' reference wind, in the library's flat format.
+  subroutine atm_dyn_dgm_nonhydro3d_gb300_restart_write( path, DDENS, MOMX, MOMY, MOMZ, DRHOT, step, time, dt, &
+      scheme )
+    character(len=*), intent(in) :: path, scheme
+    real(RP), intent(in), target :: DDENS(:,:), MOMX(:,:), MOMY(:,:), MOMZ(:,:), DRHOT(:,:)
+    integer, intent(in) :: step
+    real(RP), intent(in) :: time, dt
+    type(fedg_restart_info) :: info
+    type(c_ptr) :: q(5)
+    integer :: i
+    integer(c_int) :: ierr
+    info%step = int(step, c_long_long)
+    info%time = time
+    info%dt = dt
+    info%scheme = c_null_char
+    do i = 1, min(len_trim(scheme), 31)
+      info%scheme(i) = scheme(i:i)
+    end do
+    !$acc host_data use_device(DDENS, MOMX, MOMY, MOMZ, DRHOT)
+    q = [c_loc(DDENS), c_loc(MOMX), c_loc(MOMY), c_loc(MOMZ), c_loc(DRHOT)]
+    ierr = fedg_restart_write(ctx, trim(path)//c_null_char, q, info)
+    !$acc end host_data
+    if (ierr < 0) call PRC_abort
+  end subroutine atm_dyn_dgm_nonhydro3d_gb300_restart_write
+
+  !> Read a restart file written by restart_write into the five prognostic fields (mod_atmos_vars.F90:
+  !! 580-633); the mesh must match the context's.  The base state stays the registered one.
+  subroutine atm_dyn_dgm_nonhydro3d_gb300_restart_read( path, DDENS, MOMX, MOMY, MOMZ, DRHOT, step, time, dt )
+    character(len=*), intent(in) :: path
+    real(RP), intent(inout), target :: DDENS(:,:), MOMX(:,:), MOMY(:,:), MOMZ(:,:), DRHOT(:,:)
+    integer, intent(out) :: step
+    real(RP), intent(out) :: time, dt
+    type(fedg_restart_info) :: info
+    type(c_ptr) :: q(5)
+    integer(c_int) :: ierr
+    !$acc host_data use_device(DDENS, MOMX, MOMY, MOMZ, DRHOT)
+    q = [c_loc(DDENS), c_loc(MOMX), c_loc(MOMY), c_loc(MOMZ), c_loc(DRHOT)]
+    ierr = fedg_restart_read(ctx, trim(path)//c_null_char, q, c_null_ptr, info)
+    !$acc end host_data
+    if (ierr < 0) call PRC_abort
+    step = int(info%step)
+    time = info%time
+    dt = info%dt
+  end subroutine atm_dyn_dgm_nonhydro3d_gb300_restart_read
 
   !> atm_dyn_nonhydro3d_cal_tend_ex for EQS_TYPE = "NONHYDRO3D_HEVE_GB300"
   subroutine atm_dyn_dgm_nonhydro3d_gb300_cal_tend_heve( &
