@@ -533,10 +533,17 @@ def run_fedg(args):
     case = cases.C5()
     if args.small:
         case = case.scaled(32, 32, 16)
+    if world > 1:
+        # one slab of a domain split along x (weak scaling: every rank holds a whole C5 mesh, the
+        # domain is world times as long in x); the x faces are exchanged over NCCL before every stage
+        from fedg import slabs
+
+        case = slabs.slab_case(case, rank, world, weak=True)
+    side = rank == 0 and world == 1  # the side measurements run on one GPU only
     path = args.path
     prec = PATH_PREC[path]
     use_guess = path != "fp64" and bool(args.guess)
-    guess_side = path != "fp64" and not use_guess and not args.no_guess_side
+    guess_side = path != "fp64" and not use_guess and not args.no_guess_side and side
     net, ginfo = None, None
     if use_guess or guess_side:
         # the C5 column network (128 levels: 385 -> 256 -> 256 -> 384), trained on the GPU with the
@@ -549,8 +556,17 @@ def run_fedg(args):
                                        per_stage_keep=4096, train_steps=args.train_steps, batch=4096, lr=1e-3)
         ginfo["build_s"] = time.perf_counter() - t0
     q, b = cases.initial_state(case)
-    ctx = fl.Context(case, device=local)
+    ctx = fl.Context(case, device=local, periodic_x=fl.HALO if world > 1 else 1)
     ctx.set_base_state(b["dens_hyd"], b["pres_hyd"], b["therm_hyd"])
+    halo = None
+    if world > 1:
+        # the slabs share the case's mean wind as the reference of the momentum deviations
+        ctx.set_ref_wind(case.u0, case.v0)
+        nbh = ctx.halo_bytes()
+        hsend = [torch.empty(nbh, dtype=torch.uint8, device=ctx.dev) for _ in range(2)]
+        hrecv = [torch.zeros(nbh, dtype=torch.uint8, device=ctx.dev) for _ in range(2)]
+        halo = slabs.HaloExchange(hsend, hrecv, rank, world)
+        ctx.set_halo(hsend, hrecv, halo)
     dens_hyd = ctx.tensor(b["dens_hyd"])
     therm_hyd = ctx.tensor(b["therm_hyd"])
     dnorm2 = float((dens_hyd * dens_hyd).sum().item())
@@ -624,7 +640,7 @@ def run_fedg(args):
     for h_, t_ in zip(q_host, qd):
         h_.copy_(t_)
     e2e = None
-    if rank == 0 and not args.no_e2e:
+    if not args.no_e2e:  # every rank: each slab's state crosses its own host link
         ke = max(1, min(args.steps, 3))
         q_e = [torch.empty_like(t) for t in qd]
         # one untimed round trip first, identical to the timed ones (the copy path's warm-up)
@@ -638,6 +654,8 @@ def run_fedg(args):
         torch.cuda.synchronize()
         ph = [0.0, 0.0, 0.0]  # seconds in H2D, the step, D2H
         h2d_each, d2h_each = [], []
+        if world > 1:
+            dist.barrier()
         t0 = time.perf_counter()
         for _ in range(ke):
             ta = time.perf_counter()
@@ -658,8 +676,9 @@ def run_fedg(args):
             h2d_each.append(1e3 * (tb - ta))
             d2h_each.append(1e3 * (td - tc))
         t1 = time.perf_counter()
+        e2e_ms = max_over_ranks(1e3 * (t1 - t0), world, "cuda")
         nb = sum(t.numel() * 8 for t in qd)
-        e2e = {"value": dofs_stage * ke / (t1 - t0), "unit": UNIT, "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb,
+        e2e = {"value": replica_throughput(dofs_stage, ke, e2e_ms, world), "unit": UNIT, "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb,
                "steps": ke, "ms_per_step": {"h2d": 1e3 * ph[0] / ke, "update": 1e3 * ph[1] / ke, "d2h": 1e3 * ph[2] / ke},
                "copy_gbs": {"h2d": nb * ke / max(ph[0], 1e-9) / 1e9, "d2h": nb * ke / max(ph[2], 1e-9) / 1e9},
                "h2d_ms_each": h2d_each, "d2h_ms_each": d2h_each}
@@ -668,12 +687,12 @@ def run_fedg(args):
     # the headline path without the learned guess, the other precision mode, and the plain FP64 path, on
     # the same state
     noguess, withguess, plain, acc, other = None, None, None, None, None
-    if rank == 0 and use_guess:
+    if side and use_guess:
         o2 = dict(opts, use_guess=False)
         ms2, nf2, its2 = _timed_update(ctx, torch, stream, qd, args.steps, o2)
         noguess = {"value": dofs_stage * args.steps / (ms2 * 1e-3), "unit": UNIT, "ms_per_step": ms2 / args.steps,
                    "newton_tol": opts["tol"], "mean_newton_solves": its2, "nonconverged_columns": nf2}
-    if rank == 0 and guess_side:
+    if side and guess_side:
         # the headline path with the learned initial iterate, on the same state
         o2 = dict(opts, use_guess=True)
         ctx.update(qd, 1, **o2)
@@ -687,17 +706,17 @@ def run_fedg(args):
                      "guess_network_ms_per_step": pg["mlp"][0] / args.steps,
                      "column_solve_ms_per_step": pg["vi_mixed"][0] / args.steps}
     c4 = None
-    if rank == 0 and path != "fp64" and not args.no_c4:
+    if side and path != "fp64" and not args.no_c4:
         c4 = c4_guess_bench(np, torch, fl, cases, stream)
     other_path = {"pair": "mixed", "mixed": "pair"}.get(path)
-    if rank == 0 and other_path and not args.no_other:
+    if side and other_path and not args.no_other:
         op_ = dict(opts, prec=PATH_PREC[other_path], tol=PATH_TOL[other_path], max_iter=PATH_ITER[other_path])
         ctx.update(qd, 1, **op_)
         mso, nfo, itso = _timed_update(ctx, torch, stream, qd, args.steps, op_)
         other = {"value": dofs_stage * args.steps / (mso * 1e-3), "unit": UNIT, "ms_per_step": mso / args.steps,
                  "newton_tol": op_["tol"], "mean_newton_solves": itso, "nonconverged_columns": nfo,
                  "path": ("learned+" if use_guess else "") + PATH_NAME[other_path]}
-    if rank == 0 and prec != fl.PREC_FP64 and not args.no_plain:
+    if side and prec != fl.PREC_FP64 and not args.no_plain:
         # FElib's algorithm in FP64 on the GPU from the same initial state, and the error of each
         # precision mode against it after the same number of steps
         q_ref = [torch.empty_like(t) for t in qd]
@@ -737,16 +756,16 @@ def run_fedg(args):
         del q_ref, q_mix
 
     cb = None
-    if rank == 0 and not args.no_cpu:
+    if side and not args.no_cpu:
         cb = cpu_sample(path)
     trc = None
-    if rank == 0 and not args.no_tracer:
+    if side and not args.no_tracer:
         trc = tracer_bench(args, torch, np, fl, cases, peaks, peak_src, args.steps, args.warmup)
     ndf = None
-    if rank == 0 and not args.no_numdiff:
+    if side and not args.no_numdiff:
         ndf = numdiff_bench(args, torch, np, fl, ctx, qd, peaks, peak_src, case)
     hv = None
-    if rank == 0 and not args.no_heve:
+    if side and not args.no_heve:
         hv = heve_bench(args, torch, np, fl, ctx, q_host, dofs_stage, dnorm2, dens_hyd, therm_hyd)
 
     finite = all(bool(torch.isfinite(t).all().item()) for t in qd)
@@ -762,7 +781,8 @@ def run_fedg(args):
                        "dt": DT_STABLE, "dt_baseline": 0.5, "newton_tol": opts["tol"], "newton_max_iter": opts["max_iter"],
                        "mean_newton_solves": its, "nonconverged_columns": nfail, "finite": finite,
                        "l2": "inputs larger than L2 (FP64 state %.1f GB)" % (case.dofs * 8 / 1e9),
-                       "parallelism": "replicas" if world > 1 else "single"},
+                       "parallelism": "slabs" if world > 1 else "single",
+                       "halo_bytes_sent_per_stage": 2 * halo.send[0].numel() if halo else 0},
             "roofline": roof,
             "roofline_issue": roof_issue,
             "roofline_fp64": {"bound": "fp64", "peak_tflops": fp64_tf, "peak_source": "measured cuBLAS DGEMM 4096^3"},

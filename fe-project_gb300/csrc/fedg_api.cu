@@ -276,7 +276,8 @@ int fedg_ctx_create(const fedg_mesh_desc* d, fedg_ctx** out) {
   if (!d || !out) return fail("fedg_ctx_create: null argument");
   if (d->porder < 1 || d->porder > FEDG_MAXN1 - 1) return fail("fedg_ctx_create: porder must be 1..7");
   if (d->NeX < 1 || d->NeY < 1 || d->NeZ < 1) return fail("fedg_ctx_create: element counts must be >= 1");
-  if (!d->periodic_x || !d->periodic_y) return fail("fedg_ctx_create: only periodic lateral boundaries are supported");
+  if ((d->periodic_x != 1 && d->periodic_x != FEDG_HALO) || d->periodic_y != 1)
+    return fail("fedg_ctx_create: lateral boundaries must be periodic (periodic_x = 1 or FEDG_HALO for a slab, periodic_y = 1)");
   if (!(d->xmax > d->xmin && d->ymax > d->ymin && d->zmax > d->zmin)) return fail("fedg_ctx_create: empty domain");
   if (d->NeZ > 64) return fail("fedg_ctx_create: NeZ > 64 is not supported by the column solver");
   CK(cudaSetDevice(d->device));
@@ -424,6 +425,8 @@ int fedg_cal_tend_ex(fedg_ctx* c, const double* const in[16], double* const out[
     if (r) return r;
   }
   if (!c->base_set) return fail("fedg_cal_tend_ex: base state not set");
+  if (fedg::slab(c) && !c->hrecv[0])
+    return fail("fedg_cal_tend_ex: a slab (periodic_x = FEDG_HALO) needs its halo buffers (fedg_update_set_halo)");
   const double* dpres = in[5];
   if (!dpres) {
     double* w = ensure_work(c, c->n);
@@ -674,6 +677,8 @@ int fedg_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_o
       }
       r = tracked(c, FEDG_K_PRES, [&] { return launch_drhot2pres(c->op, c->prof(), q[4], nullptr, dp, c->n, c->stream); });
       if (r) return cuda_fail((cudaError_t)r, "fedg_update: drhot2pres");
+      // a slab exchanges the face layers of the stage state and DPRES (driver_nonhydro3d.F90:768-787)
+      if (fedg::slab(c) && (r = fedg::halo_exchange_fp64(c, q, dp, s))) return r;
       F5c qc{{q[0], q[1], q[2], q[3], q[4]}};
       F5 tex{{fedg_tint_tend_ex(t, s, 0), fedg_tint_tend_ex(t, s, 1), fedg_tint_tend_ex(t, s, 2),
               fedg_tint_tend_ex(t, s, 3), fedg_tint_tend_ex(t, s, 4)}};
@@ -722,6 +727,7 @@ int fedg_update_set_tracer_flux(fedg_ctx* c, double* const mflx[3], double* alph
     for (int i = 0; i < 7; ++i) c->trc_flux[i] = nullptr;
     return 0;
   }
+  if (fedg::slab(c)) return fail("fedg_update_set_tracer_flux: not available on a slab (periodic_x = FEDG_HALO)");
   if (!mflx[0] || !mflx[1] || !mflx[2] || !alph_M || !alph_P || !DDENS_TRC || !DDENS0_TRC)
     return fail("fedg_update_set_tracer_flux: null field");
   double* const v[7] = {mflx[0], mflx[1], mflx[2], alph_M, alph_P, DDENS_TRC, DDENS0_TRC};

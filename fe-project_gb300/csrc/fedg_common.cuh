@@ -28,6 +28,9 @@ struct Ops {
   double coriolis_f;
   int NeX, NeY, NeZ;
   int N1, Np, L;  // L = NeZ*N1 levels
+  // slab of a decomposed domain: the x- and x+ exterior face layers (receive buffers of the halo
+  // exchange, [6 fields][NeY*NeZ][N1*N1] doubles); NULL on a periodic mesh
+  const double* hx[2];
 };
 
 // column profiles of the horizontally homogeneous base state, [L] each
@@ -39,6 +42,14 @@ struct Prof {
 };
 
 __host__ __device__ inline int face_opp(int f) { return f ^ ((f < 4) ? 2 : 1); }
+
+// DPRES of one node (nonhydro3d_common.F90:428-479): PRES = P00 (Rd/P00 RHOT)^(cp/cv), minus
+// PRES_hyd; explicit roundings, so every kernel that forms it (the field, a slab's halo) agrees
+__device__ __forceinline__ double dpres_of(const Ops& op, double rhot, double pres_hyd, double* pres = nullptr) {
+  const double pr = __dmul_rn(op.pres00, pow(__dmul_rn(op.rdry / op.pres00, rhot), op.kap));
+  if (pres) *pres = pr;
+  return __dsub_rn(pr, pres_hyd);
+}
 
 template <int N1>
 __device__ __forceinline__ void face_node(int f, int a, int b, int& i, int& j, int& k) {

@@ -52,6 +52,12 @@ struct fedg_ctx {
   // from the first state they see
   bool wind_given = false;
   double wind[2] = {0.0, 0.0};
+  // slab of a decomposed domain (periodic_x = FEDG_HALO): the caller's halo buffers and exchange
+  // (fedg_update_set_halo)
+  void* hsend[2] = {};
+  void* hrecv[2] = {};
+  fedg_halo_fn hfn = nullptr;
+  void* huser = nullptr;
   // kernel timers / launch counters
   bool prof_on = false;
   long long nlaunch[FEDG_K_COUNT] = {};
@@ -75,6 +81,11 @@ void sponge_coef_host(const fedg_ctx* c, double tau, double height, double* coef
 bool ref_wind(const fedg_ctx* c, double out[2]);
 // fixes the reference wind of the fast update paths (from a restart file)
 void set_ref_wind_given(fedg_ctx* c, double U, double V);
+// slab of a decomposed domain (fedg_halo.cu): packs the stage state's x face layers, synchronises
+// and calls the caller's exchange; FP64 fields (+ DPRES, NULL: formed) or float-pair deviations
+bool slab(const fedg_ctx* c);
+int halo_exchange_fp64(fedg_ctx* c, const double* const q[5], const double* dpres, int stage);
+int halo_exchange_pair(fedg_ctx* c, const float2* const qs[5], int stage);
 // fedg_cal_tend_ex_noalloc's set-up (fedg_static.cu): looks up its static scratch array on device `dev`,
 // the current device, which loads the module holding it; called by fedg_ctx_create
 void noalloc_setup(int dev);

@@ -885,6 +885,8 @@ static int set_ref_wind(fedg_ctx* c, MixedState* m, double* const q[5]) {
     apply_ref_wind(m, c->wind[0], c->wind[1]);
     return 0;
   }
+  if (slab(c))  // the slabs of one domain must share one reference wind
+    return api_fail("fedg_update: a slab (periodic_x = FEDG_HALO) needs the domain's reference wind (fedg_update_set_ref_wind)");
   int r;
   double* d_s = reinterpret_cast<double*>(m->fbuf);  // TI area, free before the first step: 3 sums, then
   double* d_part = d_s + 4;                          // the block sums [WIND_BLOCKS][3]
@@ -918,6 +920,8 @@ static int pair_update_heve(fedg_ctx* c, double* const q[5], int nsteps, const f
   if ((r = set_ref_wind(c, m, q))) return r;
   m->opp.Uref = m->opx.Uref;
   m->opp.Vref = m->opx.Vref;
+  m->opp.hx[0] = slab(c) ? static_cast<const float2*>(c->hrecv[0]) : nullptr;
+  m->opp.hx[1] = slab(c) ? static_cast<const float2*>(c->hrecv[1]) : nullptr;
   PairCoef pc;
   std::memset(&pc, 0, sizeof(pc));
   pc.dt = split_host(o->dt);
@@ -955,6 +959,7 @@ static int pair_update_heve(fedg_ctx* c, double* const q[5], int nsteps, const f
         BP.qs[v] = s == 1 ? m->QNFp(v) : (s == 2 ? m->qi(v) : m->QSFp(v));
         BP.qi[v] = s == 1 ? m->qi(v) : m->QSFp(v);
       }
+      if (slab(c) && (r = halo_exchange_pair(c, BP.qs, s))) return r;
       r = tracked(c, FEDG_K_MTEND, [&] {
         return launch_stage_pair_heve(c->N1, s, m->opp, pfp, c->d_prof, BP, pc, c->Ne, filt, c->stream);
       });
@@ -979,6 +984,8 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
   if (r) return r;
   MixedState* m = c->mixed;
   const bool pair = o->prec == FEDG_PREC_PAIR;
+  if (!pair && slab(c))
+    return api_fail("fedg_update: the FP32 mode needs a periodic mesh; a slab (periodic_x = FEDG_HALO) runs FEDG_PREC_FP64 or FEDG_PREC_PAIR");
   if (pair && (r = pair_setup(c, m))) return r;
   if (o->use_guess && !mlp_ready(c->guess)) return api_fail("fedg_update: use_guess set but no trained column-guess network is loaded (fedg_guess_load)");
   const double alp = (3.0 + 2.0 * std::sqrt(2.0)) / 6.0, gam = 1.0 - 1.0 / std::sqrt(2.0), del = 1.0 / (2.0 * std::sqrt(2.0));
@@ -1004,6 +1011,8 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
   cf.Vref2 = m->opx.Vref;
   m->opp.Uref = m->opx.Uref;
   m->opp.Vref = m->opx.Vref;
+  m->opp.hx[0] = slab(c) ? static_cast<const float2*>(c->hrecv[0]) : nullptr;
+  m->opp.hx[1] = slab(c) ? static_cast<const float2*>(c->hrecv[1]) : nullptr;
   const double impl_fac = gam * o->dt;
   MixViArgs va{impl_fac, 1.0 / impl_fac, o->tol, 340.0, split_host(impl_fac), split_host(1.0 / impl_fac), o->max_iter, 1,
                c->vi_neumann};
@@ -1100,14 +1109,18 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
       B.qsf[v] = m->QNF(v);
       BP.qs[v] = pair ? m->QNFp(v) : nullptr;
     }
+    // a slab exchanges the face layers of each stage state before its tendency (pair mode only)
+    if (slab(c) && (r = halo_exchange_pair(c, BP.qs, 1))) return r;
     if ((r = stage(1)) || (r = save(1))) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): stage 1");
     if ((r = vi())) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): column solve 2");
     for (int v = 0; v < 5; ++v) {
       B.qsf[v] = m->QSF(v);
       BP.qs[v] = pair ? m->QSFp(v) : nullptr;
     }
+    if (slab(c) && (r = halo_exchange_pair(c, BP.qs, 2))) return r;
     if ((r = stage(2)) || (r = save(2))) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): stage 2");
     if ((r = vi())) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): column solve 3");
+    if (slab(c) && (r = halo_exchange_pair(c, BP.qs, 3))) return r;
     if ((r = stage(3)) || (r = save(3))) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): stage 3");
   }
   if (cudaMemcpyAsync(c->h_cnt, c->d_cnt, sizeof(unsigned long long) * 3, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||

@@ -102,7 +102,13 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
       double ddM = st[VD * Np + pM], mxM = st[VMX * Np + pM], myM = st[VMY * Np + pM];
       double mzM = st[VMZ * Np + pM], drM = st[VRT * Np + pM], dpM = st[5 * Np + pM];
       double ddP, mxP, myP, mzP, drP, dpP;
-      if (kn >= 0) {
+      // a slab's x boundary: the exterior face layer comes from the halo exchange
+      const double* hxs = (f == 3 && ex == 0) ? op.hx[0] : ((f == 1 && ex == op.NeX - 1) ? op.hx[1] : nullptr);
+      if (hxs) {
+        const size_t per = (size_t)op.NeY * op.NeZ * NF, h = (size_t)(ey + op.NeY * ez) * NF + ab;
+        ddP = __ldg(hxs + h); mxP = __ldg(hxs + per + h); myP = __ldg(hxs + 2 * per + h);
+        mzP = __ldg(hxs + 3 * per + h); drP = __ldg(hxs + 4 * per + h); dpP = __ldg(hxs + 5 * per + h);
+      } else if (kn >= 0) {
         int i2, j2, k2;
         face_node<N1>(face_opp(f), a, b, i2, j2, k2);
         const size_t gP = (size_t)kn * Np + i2 + N1 * j2 + NF * k2;
@@ -228,9 +234,9 @@ __global__ void k_drhot2pres(const Ops op, const Prof pf, const double* __restri
   const int ez = (int)(ke / ((size_t)op.NeX * op.NeY));
   const int lev = ez * op.N1 + p / (op.N1 * op.N1);
   const double rhot = __ldg(pf.therm + lev) + drhot[g];
-  const double pr = op.pres00 * pow(op.rdry / op.pres00 * rhot, op.kap);
+  double pr;
+  dpres[g] = dpres_of(op, rhot, __ldg(pf.pres + lev), &pr);
   if (pres) pres[g] = pr;
-  dpres[g] = pr - __ldg(pf.pres + lev);
 }
 
 // ---------------------------------------------------------------------------------------

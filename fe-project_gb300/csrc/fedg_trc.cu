@@ -629,6 +629,12 @@ int check_base(const fedg_ctx* c, const char* who) {
   return 0;
 }
 
+// the tracer kernels read lateral neighbours of a periodic mesh only (no slab halo)
+int check_periodic(const fedg_ctx* c, const char* who) {
+  if (fedg::slab(c)) return api_fail(std::string(who) + ": not available on a slab (periodic_x = FEDG_HALO)");
+  return 0;
+}
+
 }  // namespace
 
 // save_massflux of a stage that the FP32 or float-pair update holds as deviations (qp: pairs, or
@@ -675,6 +681,7 @@ int fedg_trc_alphdens_advtest(fedg_ctx* c, const double* DDENS, const double* MO
   if (!c || !DDENS || !MOMX || !MOMY || !MOMZ || !alph_M || !alph_P)
     return api_fail("fedg_trc_alphdens_advtest: null argument");
   if (int r = check_base(c, "fedg_trc_alphdens_advtest")) return r;
+  if (int r = check_periodic(c, "fedg_trc_alphdens_advtest")) return r;
   cudaSetDevice(c->d.device);
   const int r = tracked(c, FEDG_K_TRC_AUX, [&] {
     return launch_alph_adv(c->op, c->d_prof, DDENS, MOMX, MOMY, MOMZ, alph_M, alph_P, c->Ne, c->stream);
@@ -691,6 +698,7 @@ int fedg_trc_save_massflux(fedg_ctx* c, int rkstage, const double* const q[5], c
     if (!mflx[d]) return api_fail("fedg_trc_save_massflux: null mass-flux field");
   if (rkstage < 1) return api_fail("fedg_trc_save_massflux: rkstage is 1-based");
   if (int r = check_base(c, "fedg_trc_save_massflux")) return r;
+  if (int r = check_periodic(c, "fedg_trc_save_massflux")) return r;
   cudaSetDevice(c->d.device);
   MflxArgs<StF64> A;
   for (int v = 0; v < 5; ++v) A.q.q[v] = q[v];
@@ -714,6 +722,7 @@ int fedg_trc_fct_coef(fedg_ctx* c, const double* QTRC, const double* const mflx[
     return api_fail("fedg_trc_fct_coef: null argument");
   if (!(dt > 0.0)) return api_fail("fedg_trc_fct_coef: dt must be positive");
   if (int r = check_base(c, "fedg_trc_fct_coef")) return r;
+  if (int r = check_periodic(c, "fedg_trc_fct_coef")) return r;
   cudaSetDevice(c->d.device);
   const TrcIn in{QTRC, {mflx[0], mflx[1], mflx[2]}, alph_M, alph_P, RHOQ_tp, DDENS_TRC, DDENS0_TRC};
   const TrcFct fc{rk_c_ssm1, dt, nullptr, fct_coef};
@@ -725,6 +734,7 @@ int fedg_trc_cal_tend(fedg_ctx* c, const double* QTRC, const double* const mflx[
                       const double* alph_P, const double* fct_coef, const double* RHOQ_tp, double* QTRC_dt) {
   if (!c || !QTRC || !mflx || !mflx[0] || !mflx[1] || !mflx[2] || !alph_M || !alph_P || !QTRC_dt)
     return api_fail("fedg_trc_cal_tend: null argument");
+  if (int r = check_periodic(c, "fedg_trc_cal_tend")) return r;
   cudaSetDevice(c->d.device);
   const TrcIn in{QTRC, {mflx[0], mflx[1], mflx[2]}, alph_M, alph_P, RHOQ_tp, nullptr, nullptr};
   TrcStage st;
@@ -767,6 +777,7 @@ int fedg_trc_update(fedg_ctx* c, double* QTRC, const double* const mflx[3], cons
     return api_fail("fedg_trc_update: prec must be FEDG_PREC_FP64 or FEDG_PREC_PAIR");
   if (!(o->dt > 0.0) || o->nsteps < 0) return api_fail("fedg_trc_update: dt must be positive and nsteps >= 0");
   if (int r = check_base(c, "fedg_trc_update")) return r;
+  if (int r = check_periodic(c, "fedg_trc_update")) return r;
   cudaSetDevice(c->d.device);
   // ERK_SSP_3s3o in Shu-Osher form (scale_timeint_rk_butcher_tab.F90:200-210) and its stage nodes
   constexpr int ns = 3;

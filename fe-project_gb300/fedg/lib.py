@@ -37,7 +37,13 @@ EXPORTED = [
     "fedg_update_set_tracer_flux", "fedg_update_set_sponge", "fedg_numdiff_apply_prec",
     "fedg_guess_set_wait_limit", "fedg_update_set_vi_neumann", "fedg_update_set_wait_limit",
     "fedg_restart_write", "fedg_restart_read",
+    "fedg_halo_bytes", "fedg_update_set_halo", "fedg_halo_pack", "fedg_update_set_ref_wind",
+    "fedg_update_get_ref_wind",
 ]
+
+HALO = 2  # fedg_mesh_desc.periodic_x of a slab (FEDG_HALO)
+# fedg_halo_fn: int (*)(void* user, int stage)
+HALO_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int)
 
 # kernel classes of fedg_prof_read (include/fedg.h)
 K_TEND, K_VI, K_RK, K_FILTER, K_PRES, K_MTEND, K_MVI, K_MLP, K_AUX, K_TRC_FCT, K_TRC_TEND, K_TRC_AUX, K_ND, \
@@ -158,6 +164,12 @@ def load():
     lib.fedg_prof_reset.argtypes = [_vp]
     lib.fedg_prof_read.argtypes = [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                    ctypes.POINTER(ctypes.c_longlong)]
+    lib.fedg_halo_bytes.restype = ctypes.c_size_t
+    lib.fedg_halo_bytes.argtypes = [_vp]
+    lib.fedg_update_set_halo.argtypes = [_vp, ctypes.c_void_p * 2, ctypes.c_void_p * 2, HALO_FN, ctypes.c_void_p]
+    lib.fedg_halo_pack.argtypes = [_vp, _P5, _vp]
+    lib.fedg_update_set_ref_wind.argtypes = [_vp, ctypes.c_double, ctypes.c_double]
+    lib.fedg_update_get_ref_wind.argtypes = [_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
     _lib = lib
     return lib
 
@@ -187,7 +199,7 @@ def _p5(ts):
 class Context:
     """One fedg context (mesh, operators, base state, CUDA stream) on one GPU."""
 
-    def __init__(self, case, device: int = 0, filter_on=None):
+    def __init__(self, case, device: int = 0, filter_on=None, periodic_x: int = 1):
         import torch
 
         if not torch.cuda.is_available():
@@ -200,7 +212,7 @@ class Context:
         from .cases import CPDRY, CVDRY, GRAV, PRES00, RDRY
 
         fo = case.filter_on if filter_on is None else filter_on
-        d = MeshDesc(case.porder, case.NeX, case.NeY, case.NeZ, xmin, xmax, ymin, ymax, zmin, zmax, 1, 1,
+        d = MeshDesc(case.porder, case.NeX, case.NeY, case.NeZ, xmin, xmax, ymin, ymax, zmin, zmax, int(periodic_x), 1,
                      getattr(case, "grav", GRAV), RDRY, CPDRY, CVDRY, PRES00, int(fo), 2.0 / 3.0, 36.0, 16,
                      2.0 / 3.0, 36.0, 16, device)
         h = _vp()
@@ -306,6 +318,39 @@ class Context:
         if sync:
             self.sync()
         return nfail, float(mi.value)
+
+    # -- slab of a decomposed domain (MeshFieldComm exchange, scale_meshfieldcomm_base.F90:340-470) --
+    def halo_bytes(self) -> int:
+        return int(self.lib.fedg_halo_bytes(self.h))
+
+    def set_halo(self, send, recv, exchange=None):
+        """send, recv: two device buffers each (torch tensors of halo_bytes() bytes, kept alive by the
+        caller); exchange(stage) -> None moves this slab's send[1] to the x+ neighbour's recv[0] and
+        its send[0] to the x- neighbour's recv[1] and returns once recv holds the neighbours' data."""
+        def fn(_user, stage):
+            try:
+                exchange(int(stage))
+                return 0
+            except Exception as e:  # the C caller only sees the status; keep the reason
+                self.halo_error = e
+                return 1
+        self._halo_fn = HALO_FN(fn) if exchange is not None else ctypes.cast(None, HALO_FN)
+        self._halo_bufs = (send, recv)
+        sp = (ctypes.c_void_p * 2)(*[t.data_ptr() for t in send])
+        rp = (ctypes.c_void_p * 2)(*[t.data_ptr() for t in recv])
+        _check(self.lib.fedg_update_set_halo(self.h, sp, rp, self._halo_fn, None), "fedg_update_set_halo")
+
+    def halo_pack(self, q, dpres=None):
+        self.torch.cuda.synchronize()
+        _check(self.lib.fedg_halo_pack(self.h, _p5(q), _ptr(dpres)), "fedg_halo_pack")
+
+    def set_ref_wind(self, u, v):
+        _check(self.lib.fedg_update_set_ref_wind(self.h, float(u), float(v)), "fedg_update_set_ref_wind")
+
+    def get_ref_wind(self):
+        u, v = ctypes.c_double(), ctypes.c_double()
+        r = _check(self.lib.fedg_update_get_ref_wind(self.h, ctypes.byref(u), ctypes.byref(v)), "fedg_update_get_ref_wind")
+        return (u.value, v.value) if r else None
 
     # -- restart files (scale_file_restart_meshfield.F90) --
     def restart_write(self, path, q, step=0, time=0.0, dt=0.0, scheme=""):
@@ -596,6 +641,39 @@ class Guess:
         _check(self.lib.fedg_guess_predict(self.h, _ptr(X), _ptr(Y), int(X.shape[0])), "fedg_guess_predict")
         torch.cuda.synchronize()
         return Y
+
+    # -- slab of a decomposed domain (MeshFieldComm exchange, scale_meshfieldcomm_base.F90:340-470) --
+    def halo_bytes(self) -> int:
+        return int(self.lib.fedg_halo_bytes(self.h))
+
+    def set_halo(self, send, recv, exchange=None):
+        """send, recv: two device buffers each (torch tensors of halo_bytes() bytes, kept alive by the
+        caller); exchange(stage) -> None moves this slab's send[1] to the x+ neighbour's recv[0] and
+        its send[0] to the x- neighbour's recv[1] and returns once recv holds the neighbours' data."""
+        def fn(_user, stage):
+            try:
+                exchange(int(stage))
+                return 0
+            except Exception as e:  # the C caller only sees the status; keep the reason
+                self.halo_error = e
+                return 1
+        self._halo_fn = HALO_FN(fn) if exchange is not None else ctypes.cast(None, HALO_FN)
+        self._halo_bufs = (send, recv)
+        sp = (ctypes.c_void_p * 2)(*[t.data_ptr() for t in send])
+        rp = (ctypes.c_void_p * 2)(*[t.data_ptr() for t in recv])
+        _check(self.lib.fedg_update_set_halo(self.h, sp, rp, self._halo_fn, None), "fedg_update_set_halo")
+
+    def halo_pack(self, q, dpres=None):
+        self.torch.cuda.synchronize()
+        _check(self.lib.fedg_halo_pack(self.h, _p5(q), _ptr(dpres)), "fedg_halo_pack")
+
+    def set_ref_wind(self, u, v):
+        _check(self.lib.fedg_update_set_ref_wind(self.h, float(u), float(v)), "fedg_update_set_ref_wind")
+
+    def get_ref_wind(self):
+        u, v = ctypes.c_double(), ctypes.c_double()
+        r = _check(self.lib.fedg_update_get_ref_wind(self.h, ctypes.byref(u), ctypes.byref(v)), "fedg_update_get_ref_wind")
+        return (u.value, v.value) if r else None
 
     # -- restart files (scale_file_restart_meshfield.F90) --
     def restart_write(self, path, q, step=0, time=0.0, dt=0.0, scheme=""):

@@ -193,6 +193,13 @@ struct Oracle {
   // sponge layer in the dynamics step when tau > 0 (driver_nonhydro3d.F90:831-841)
   double sl_tau = 0.0, sl_height = 0.0;
   int sl_hvel = 0;
+  // slab of a domain decomposed along x (FElib's MeshFieldComm exchange, scale_meshfieldcomm_base.F90:
+  // 340-470, called by the driver before each tendency, driver_nonhydro3d.F90:768-787): the x- and x+
+  // exterior face layers [6 fields: DDENS, MOMX, MOMY, MOMZ, DRHOT, DPRES][NeY*NeZ][Nfp], filled by
+  // halo_cb before every tendency of a step; NULL on a periodic mesh
+  const double* hx[2] = {nullptr, nullptr};
+  void (*halo_cb)(void* user, int stage, const double* const* q, const double* dpres) = nullptr;
+  void* halo_user = nullptr;
 
   size_t nid(int i, int j, int k) const { return (size_t)i + (size_t)N1 * j + (size_t)N1 * N1 * k; }
   size_t eid(int ex, int ey, int ez) const { return (size_t)ex + (size_t)NeX * ey + (size_t)NeX * NeY * ez; }
@@ -277,12 +284,17 @@ static void cal_tend(const Oracle& o, int hevi, const double* const q[5], const 
             size_t iP; double msign = 1.0;
             if (kn >= 0) { int i2, j2, k2; face_node(N1, fo, a, b, i2, j2, k2); iP = (size_t)kn * Np + o.nid(i2, j2, k2); }
             else { iP = iM; msign = -1.0; }  // slip lid: MOMZ reflected (dgm_bnd.F90:323-341)
-            const double ddM = q[VD][iM], ddP = q[VD][iP];
-            const double mxM = q[VMX][iM], mxP = q[VMX][iP];
-            const double myM = q[VMY][iM], myP = q[VMY][iP];
-            const double mzM = q[VMZ][iM], mzP = msign * q[VMZ][iP];
-            const double drM = q[VRT][iM], drP = q[VRT][iP];
-            const double dpM = dpres[iM], dpP = dpres[iP];
+            // a slab's x boundary: the exterior values come from the exchanged face layer (the base
+            // state is horizontally homogeneous, so the exterior node's base values are the own node's)
+            const double* hs = (f == 3 && ex == 0) ? o.hx[0] : ((f == 1 && ex == o.NeX - 1) ? o.hx[1] : nullptr);
+            const size_t hper = (size_t)o.NeY * o.NeZ * Nfp, hi = (size_t)(ey + o.NeY * ez) * Nfp + a + N1 * b;
+            if (hs) iP = iM;
+            const double ddM = q[VD][iM], ddP = hs ? hs[hi] : q[VD][iP];
+            const double mxM = q[VMX][iM], mxP = hs ? hs[hper + hi] : q[VMX][iP];
+            const double myM = q[VMY][iM], myP = hs ? hs[2 * hper + hi] : q[VMY][iP];
+            const double mzM = q[VMZ][iM], mzP = hs ? hs[3 * hper + hi] : msign * q[VMZ][iP];
+            const double drM = q[VRT][iM], drP = hs ? hs[4 * hper + hi] : q[VRT][iP];
+            const double dpM = dpres[iM], dpP = hs ? hs[5 * hper + hi] : dpres[iP];
             const double densM = ddM + o.dens_hyd[iM], densP = ddP + o.dens_hyd[iP];
             const double rhotM = o.therm_hyd[iM] + drM, rhotP = o.therm_hyd[iP] + drP;
             const double phM = o.pres_hyd[iM], phP = o.pres_hyd[iP];
@@ -1523,6 +1535,17 @@ void* orc_create(const orc_desc* d) {
 
 void orc_destroy(void* h) { delete static_cast<Oracle*>(h); }
 
+// a slab of a domain decomposed along x: exterior x face layers recv0 (x-) and recv1 (x+), and the
+// exchange the step functions call before every tendency (after DPRES is formed)
+void orc_set_halo(void* h, const double* recv0, const double* recv1,
+                  void (*cb)(void* user, int stage, const double* const* q, const double* dpres), void* user) {
+  Oracle* o = static_cast<Oracle*>(h);
+  o->hx[0] = recv0;
+  o->hx[1] = recv1;
+  o->halo_cb = cb;
+  o->halo_user = user;
+}
+
 int orc_num_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();
@@ -1621,6 +1644,7 @@ void orc_step_heve(void* h, double* const* q, double dt, int nsteps) {
     for (int v = 0; v < 5; ++v) std::memcpy(q0[v].data(), q[v], n * sizeof(double));
     for (int st = 1; st <= 3; ++st) {
       drhot2pres(*o, q[VRT], nullptr, dp.data());
+      if (o->halo_cb) o->halo_cb(o->halo_user, st, q, dp.data());
       cal_tend(*o, 0, q, dp.data(), tp);
       if (o->sl_tau > 0.0) {
         double* const tm[3] = {tp[VMX], tp[VMY], tp[VMZ]};
@@ -1681,6 +1705,7 @@ long orc_step_hevi(void* h, double* const* q, double dt, int nsteps, int max_ite
         for (size_t p = 0; p < n; ++p) x[p] = x[p] + impl_fac * ti[p];
       }
       drhot2pres(*o, q[VRT], nullptr, dp.data());
+      if (o->halo_cb) o->halo_cb(o->halo_user, st, q, dp.data());
       cal_tend(*o, 1, q, dp.data(), tep);
       if (o->sl_tau > 0.0) {
         double* const tm[3] = {tep[VMX], tep[VMY], tep[VMZ]};

@@ -38,6 +38,11 @@ class OrcDesc(ctypes.Structure):
     ]
 
 
+# void (*)(void* user, int stage, const double* const* q, const double* dpres)
+HALO_CB = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.POINTER(ctypes.c_double)),
+                           ctypes.POINTER(ctypes.c_double))
+
+
 def build() -> str:
     """Compile the oracle with its Makefile (gcc + OpenMP); returns the .so path."""
     subprocess.run(["make", "-s", "-C", _HERE], check=True)
@@ -56,6 +61,7 @@ def _load():
     lib.orc_create.restype = ctypes.c_void_p
     lib.orc_create.argtypes = [ctypes.POINTER(OrcDesc)]
     lib.orc_destroy.argtypes = [ctypes.c_void_p]
+    lib.orc_set_halo.argtypes = [ctypes.c_void_p, _dp, _dp, HALO_CB, ctypes.c_void_p]
     lib.orc_num_threads.restype = ctypes.c_int
     lib.orc_set_num_threads.argtypes = [ctypes.c_int]
     lib.orc_get_1d.argtypes = [ctypes.c_void_p] + [_dp] * 8
@@ -229,6 +235,38 @@ class Oracle:
         nfail = self.lib.orc_step_hevi(self._h, pq, float(dt), int(nsteps), int(max_iter), float(tol),
                                        ctypes.byref(mi))
         return qs, int(nfail), float(mi.value)
+
+    # ---- slab of a domain decomposed along x (scale_meshfieldcomm_base.F90:340-470) ----
+    def halo_pack(self, q, dpres):
+        """The x face layers of this slab, [2 sides][6 fields][NeY*NeZ*N1*N1]: side 0 the nodes (0, a, b)
+        of the elements ex = 0, side 1 the nodes (N, a, b) of ex = NeX-1, in the order (ey + NeY ez,
+        a + N1 b); fields DDENS, MOMX, MOMY, MOMZ, DRHOT, DPRES (the library's buffer layout)."""
+        N1 = self.N1
+        out = np.empty((2, 6, self.NeY * self.NeZ * N1 * N1))
+        for v, a in enumerate(list(q) + [dpres]):
+            x = np.asarray(a, np.float64).reshape(self.NeZ, self.NeY, self.NeX, N1, N1, N1)  # ez ey ex k j i
+            out[0, v] = x[:, :, 0, :, :, 0].reshape(-1)
+            out[1, v] = x[:, :, self.NeX - 1, :, :, N1 - 1].reshape(-1)
+        return out
+
+    def set_halo(self, exchange):
+        """Makes this oracle a slab: before every tendency of step_hevi/step_heve, exchange(stage, send,
+        recv) gets this slab's packed face layers (send, as halo_pack) and must fill recv[0] with the
+        x- neighbour's send[1] and recv[1] with the x+ neighbour's send[0], in place."""
+        n = self.Np * self.Ne
+        self._hrecv = np.zeros((2, 6, self.NeY * self.NeZ * self.N1 * self.N1))
+        self.halo_errors = []
+
+        def cb(_user, stage, qpp, dpp):
+            try:
+                q = [np.ctypeslib.as_array(qpp[v], shape=(n,)) for v in range(5)]
+                dp = np.ctypeslib.as_array(dpp, shape=(n,))
+                exchange(int(stage), self.halo_pack(q, dp), self._hrecv)
+            except Exception as e:  # a ctypes callback cannot raise into C
+                self.halo_errors.append(e)
+
+        self._halo_cb = HALO_CB(cb)
+        self.lib.orc_set_halo(self._h, _ptr(self._hrecv[0]), _ptr(self._hrecv[1]), self._halo_cb, None)
 
     # ---- tracer advection (trcadvect3d_heve.F90, driver_trcadv3d.F90) ----
     # Face-node arrays (alph_dens) have shape (Ne, 6, N1*N1): FElib's (NfpTot, Ne).
