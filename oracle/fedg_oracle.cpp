@@ -30,6 +30,10 @@
 //                              ..._trcadvect3d_heve.F90, ..._driver_trcadv3d.F90:330-560
 //   * numerical diffusion      ..._nonhydro3d_numdiff.F90:214-721, ..._dgm_bnd.F90:370-508
 //   * sponge layer             ..._dgm_spongelayer.F90:134-219
+//   * slab of a domain split along x (orc_set_halo): the x faces of the boundary elements
+//     read the exchanged face layers, filled by a callback before every tendency, as the
+//     driver's MeshFieldComm_Exchange does (..._driver_nonhydro3d.F90:768-787,
+//     FElib/src/data/scale_meshfieldcomm_base.F90:340-470)
 //
 // Layout: every field is column-major (Np, Ne) like FElib, node n = i + N1*j + N1^2*k,
 // element ke = ex + NeX*ey + NeX*NeY*ez.  Exterior (halo) values are produced in place
