@@ -327,6 +327,7 @@ void fedg_ctx_destroy(fedg_ctx* c) {
   cudaFree(c->d_status);
   cudaFree(c->d_cnt);
   cudaFree(c->work);
+  cudaFree(c->host_state);
   cudaFree(c->trc_buf);
   cudaFree(c->nd_buf);
   cudaFree(c->sponge_coef);
@@ -403,6 +404,7 @@ int fedg_drhot2pres(fedg_ctx* c, const double* DRHOT, double* PRES, double* DPRE
 static double* ensure_work(fedg_ctx* c, size_t ndouble) {
   if (c->work_doubles >= ndouble) return c->work;
   cudaFree(c->work);
+  cudaFree(c->host_state);
   cudaFree(c->trc_buf);
   cudaFree(c->nd_buf);
   cudaFree(c->sponge_coef);
@@ -623,13 +625,16 @@ int fedg_tint_advance(fedg_tint* t, int stage, double* const q[5]) {
 }
 
 // ---------------- driver update loop (driver_nonhydro3d.F90:614-963) ----------------
-int fedg_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_opts* o, double* iters_out) {
+// hout: device-mapped page-locked host arrays that the float-pair path's last stage kernel also
+// writes the result to (fedg_update_host), or NULL
+static int update_impl(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_opts* o, double* iters_out,
+                       double* const* hout) {
   if (!c || !q || !o) return fail("fedg_update: null argument");
   if (!c->base_set) return fail("fedg_update: base state not set");
   if (o->eqs != FEDG_HEVE && o->eqs != FEDG_HEVI) return fail("fedg_update: bad eqs");
   CK(cudaSetDevice(c->d.device));
   if (o->prec == FEDG_PREC_MIXED || o->prec == FEDG_PREC_PAIR) {
-    return mixed_update(c, q, nsteps, o, iters_out);
+    return mixed_update(c, q, nsteps, o, iters_out, hout);
   }
   if (o->prec != FEDG_PREC_FP64) return fail("fedg_update: bad prec");
   const int scheme = o->eqs == FEDG_HEVE ? FEDG_SSP_RK3 : FEDG_IMEX_ARK232;
@@ -709,6 +714,48 @@ int fedg_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_o
   if (r < 0) return r;
   if (iters_out) *iters_out = ncnt ? double(nsum) / double(ncnt) : 0.0;
   return nfail;
+}
+
+int fedg_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_opts* o, double* iters_out) {
+  return update_impl(c, q, nsteps, o, iters_out, nullptr);
+}
+
+// fedg_update for fields in page-locked host memory: H2D into the context's device copy of the
+// state, the steps, and the result back into the host arrays.  In the float-pair paths the last
+// stage kernel stores q^{n+1} through the arrays' device mapping while it runs (the device-to-host
+// transfer overlaps its arithmetic); the FP64 and FP32 paths copy the result back after the step.
+int fedg_update_host(fedg_ctx* c, double* const host_q[5], int nsteps, const fedg_update_opts* o,
+                     double* iters_out) {
+  if (!c || !host_q || !o) return fail("fedg_update_host: null argument");
+  CK(cudaSetDevice(c->d.device));
+  double* hd[5];
+  for (int v = 0; v < 5; ++v) {
+    unsigned flags = 0;
+    void* dp = nullptr;
+    if (!host_q[v] || cudaHostGetFlags(&flags, host_q[v]) != cudaSuccess ||
+        cudaHostGetDevicePointer(&dp, host_q[v], 0) != cudaSuccess || !dp) {
+      cudaGetLastError();  // clear the lookup's error
+      return fail("fedg_update_host: the fields must be page-locked host memory (cudaHostAlloc or cudaHostRegister)");
+    }
+    hd[v] = static_cast<double*>(dp);
+  }
+  const size_t nb = sizeof(double) * c->n;
+  if (!c->host_state && cudaMalloc(&c->host_state, 5 * nb) != cudaSuccess) {
+    c->host_state = nullptr;
+    return fail("fedg_update_host: out of device memory");
+  }
+  double* dq[5];
+  for (int v = 0; v < 5; ++v) {
+    dq[v] = c->host_state + (size_t)v * c->n;
+    CK(cudaMemcpyAsync(dq[v], host_q[v], nb, cudaMemcpyHostToDevice, c->stream));
+  }
+  const bool direct = o->prec == FEDG_PREC_PAIR && nsteps > 0;
+  const int r = update_impl(c, dq, nsteps, o, iters_out, direct ? hd : nullptr);
+  if (r < 0) return r;
+  if (!direct)
+    for (int v = 0; v < 5; ++v) CK(cudaMemcpyAsync(host_q[v], dq[v], nb, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return r;
 }
 
 int fedg_update_set_sponge(fedg_ctx* c, double tau, double height, int hveldamp) {

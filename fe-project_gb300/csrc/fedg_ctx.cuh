@@ -33,6 +33,7 @@ struct fedg_ctx {
   MixedState* mixed = nullptr;
   fedg_tint* upd_tint = nullptr;  // RK buffers of fedg_update, kept between calls
   MlpState* guess = nullptr;      // column-guess network attached with fedg_guess_load (not owned)
+  double* host_state = nullptr;   // device copy of the state of fedg_update_host (5 Np*Ne doubles)
   double* trc_buf = nullptr;      // tracer update scratch: two stage fields, var0, varTmp, FCT per element
   double* nd_buf = nullptr;       // numerical-diffusion scratch: gradient (3 fields), Laplacian (2 fields)
   double* sponge_coef = nullptr;  // sponge-layer coefficient per level

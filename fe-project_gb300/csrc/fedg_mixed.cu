@@ -911,7 +911,7 @@ static int set_ref_wind(fedg_ctx* c, MixedState* m, double* const q[5]) {
 // stage 3 also applies the modal filter and writes q^{n+1} in FP64.  No implicit solve, so no guess
 // network and no Newton iterations.
 static int pair_update_heve(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_opts* o,
-                            double* iters_out) {
+                            double* iters_out, double* const* hout) {
   if (o->use_guess) return api_fail("fedg_update: use_guess needs eqs FEDG_HEVI (HEVE has no implicit solve)");
   int r = mixed_setup(c);
   if (r) return r;
@@ -960,6 +960,7 @@ static int pair_update_heve(fedg_ctx* c, double* const q[5], int nsteps, const f
         BP.qi[v] = s == 1 ? m->qi(v) : m->QSFp(v);
       }
       if (slab(c) && (r = halo_exchange_pair(c, BP.qs, s))) return r;
+      for (int v = 0; v < 5; ++v) BP.qh[v] = (hout && s == 3 && step == nsteps - 1) ? hout[v] : nullptr;
       r = tracked(c, FEDG_K_MTEND, [&] {
         return launch_stage_pair_heve(c->N1, s, m->opp, pfp, c->d_prof, BP, pc, c->Ne, filt, c->stream);
       });
@@ -975,8 +976,10 @@ static int pair_update_heve(fedg_ctx* c, double* const q[5], int nsteps, const f
   return 0;
 }
 
-int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_opts* o, double* iters_out) {
-  if (o->eqs == FEDG_HEVE && o->prec == FEDG_PREC_PAIR) return pair_update_heve(c, q, nsteps, o, iters_out);
+int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_opts* o, double* iters_out,
+                 double* const* hout) {
+  if (o->eqs == FEDG_HEVE && o->prec == FEDG_PREC_PAIR) return pair_update_heve(c, q, nsteps, o, iters_out, hout);
+  if (hout && o->prec != FEDG_PREC_PAIR) return api_fail("fedg_update_host: direct host output needs FEDG_PREC_PAIR");
   if (o->eqs != FEDG_HEVI)
     return api_fail("fedg_update: the FP32 mixed-precision path implements HEVI (IMEX ARK232); HEVE runs in FP64 or float pairs");
   if (o->max_iter < 1) return api_fail("fedg_update: max_iter must be >= 1");
@@ -1121,6 +1124,7 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
     if ((r = stage(2)) || (r = save(2))) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): stage 2");
     if ((r = vi())) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): column solve 3");
     if (slab(c) && (r = halo_exchange_pair(c, BP.qs, 3))) return r;
+    for (int v = 0; v < 5; ++v) BP.qh[v] = (hout && step == nsteps - 1) ? hout[v] : nullptr;
     if ((r = stage(3)) || (r = save(3))) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): stage 3");
   }
   if (cudaMemcpyAsync(c->h_cnt, c->d_cnt, sizeof(unsigned long long) * 3, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||

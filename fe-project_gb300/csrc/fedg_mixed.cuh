@@ -106,6 +106,7 @@ struct StagePairBufs {
   float xs[3];
   double* dtrc;         // stage 3: DDENS before the modal filter (DDENS_TRC of the tracer flux; NULL: none)
   float2* a0[3];        // stage 1 (HEVI): A(q^n) of DENS, MOMZ, RHOT for the column solves' first residual
+  double* qh[5];        // stage 3: also store q^{n+1} here (mapped page-locked host memory; NULL: none)
 };
 int launch_stage_pair_heve(int N1, int stage, const OpsP& op, const ProfP& pf, const double* dens64,
                            const StagePairBufs& B, const PairCoef& cf, int Ne, int filt, cudaStream_t s);
@@ -129,4 +130,7 @@ int launch_vi_cols(int N1, const Ops& op, const OpsX& ox, const ProfX& px, const
 
 struct MixedState;
 void mixed_free(MixedState* m);
-int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_opts* o, double* iters_out);
+// hout (optional): device-mapped page-locked host arrays that the last step's stage-3 kernel also
+// writes q^{n+1} to (fedg_update_host; float-pair paths only)
+int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_opts* o, double* iters_out,
+                 double* const* hout = nullptr);

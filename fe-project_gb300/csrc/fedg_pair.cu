@@ -105,7 +105,9 @@ __device__ __forceinline__ void filter_store(const OpsP& op, float2* fa, float2*
     if (valid) {
       const f2 fil = s3.get();
       const f2 out = ref[v] + fil;
-      B.qn[v][g] = (double)out.h + (double)out.l;
+      const double o64 = (double)out.h + (double)out.l;
+      B.qn[v][g] = o64;
+      if (B.qh[0]) B.qh[v][g] = o64;
       B.qnf[v][g] = f2_pack(fil);
     }
   }
@@ -371,7 +373,9 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
 #pragma unroll
         for (int v = 0; v < 5; ++v) {
           const f2 out = ref[v] + dev[v];
-          B.qn[v][g] = (double)out.h + (double)out.l;
+          const double o64 = (double)out.h + (double)out.l;
+          B.qn[v][g] = o64;
+          if (B.qh[0]) B.qh[v][g] = o64;
           B.qnf[v][g] = f2_pack(dev[v]);
         }
       }
@@ -437,7 +441,9 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
     if (valid) {
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
-        B.qn[v][g] = (double)qnew[v].h + (double)qnew[v].l;
+        const double o64 = (double)qnew[v].h + (double)qnew[v].l;
+        B.qn[v][g] = o64;
+        if (B.qh[0]) B.qh[v][g] = o64;
         B.qnf[v][g] = f2_pack(dev[v]);
       }
     }

@@ -38,7 +38,7 @@ EXPORTED = [
     "fedg_guess_set_wait_limit", "fedg_update_set_vi_neumann", "fedg_update_set_wait_limit",
     "fedg_restart_write", "fedg_restart_read",
     "fedg_halo_bytes", "fedg_update_set_halo", "fedg_halo_pack", "fedg_update_set_ref_wind",
-    "fedg_update_get_ref_wind",
+    "fedg_update_get_ref_wind", "fedg_update_host",
 ]
 
 HALO = 2  # fedg_mesh_desc.periodic_x of a slab (FEDG_HALO)
@@ -164,6 +164,7 @@ def load():
     lib.fedg_prof_reset.argtypes = [_vp]
     lib.fedg_prof_read.argtypes = [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                    ctypes.POINTER(ctypes.c_longlong)]
+    lib.fedg_update_host.argtypes = [_vp, _P5, ctypes.c_int, ctypes.POINTER(UpdateOpts), ctypes.POINTER(ctypes.c_double)]
     lib.fedg_halo_bytes.restype = ctypes.c_size_t
     lib.fedg_halo_bytes.argtypes = [_vp]
     lib.fedg_update_set_halo.argtypes = [_vp, ctypes.c_void_p * 2, ctypes.c_void_p * 2, HALO_FN, ctypes.c_void_p]
@@ -351,6 +352,17 @@ class Context:
         u, v = ctypes.c_double(), ctypes.c_double()
         r = _check(self.lib.fedg_update_get_ref_wind(self.h, ctypes.byref(u), ctypes.byref(v)), "fedg_update_get_ref_wind")
         return (u.value, v.value) if r else None
+
+    def update_host(self, q_host, nsteps, *, eqs=None, prec=PREC_FP64, dt=None, max_iter=1, tol=0.0,
+                    use_guess=False):
+        """fedg_update_host: q_host are five page-locked host tensors (torch pin_memory), updated in place"""
+        eqs = (HEVE if self.case.eqs == "HEVE" else HEVI) if eqs is None else eqs
+        o = UpdateOpts(int(eqs), int(prec), int(max_iter), int(bool(use_guess)),
+                       float(self.case.dt if dt is None else dt), float(tol))
+        mi = ctypes.c_double(0.0)
+        nfail = _check(self.lib.fedg_update_host(self.h, _p5(q_host), int(nsteps), ctypes.byref(o), ctypes.byref(mi)),
+                       "fedg_update_host")
+        return nfail, float(mi.value)
 
     # -- restart files (scale_file_restart_meshfield.F90) --
     def restart_write(self, path, q, step=0, time=0.0, dt=0.0, scheme=""):
@@ -674,6 +686,17 @@ class Guess:
         u, v = ctypes.c_double(), ctypes.c_double()
         r = _check(self.lib.fedg_update_get_ref_wind(self.h, ctypes.byref(u), ctypes.byref(v)), "fedg_update_get_ref_wind")
         return (u.value, v.value) if r else None
+
+    def update_host(self, q_host, nsteps, *, eqs=None, prec=PREC_FP64, dt=None, max_iter=1, tol=0.0,
+                    use_guess=False):
+        """fedg_update_host: q_host are five page-locked host tensors (torch pin_memory), updated in place"""
+        eqs = (HEVE if self.case.eqs == "HEVE" else HEVI) if eqs is None else eqs
+        o = UpdateOpts(int(eqs), int(prec), int(max_iter), int(bool(use_guess)),
+                       float(self.case.dt if dt is None else dt), float(tol))
+        mi = ctypes.c_double(0.0)
+        nfail = _check(self.lib.fedg_update_host(self.h, _p5(q_host), int(nsteps), ctypes.byref(o), ctypes.byref(mi)),
+                       "fedg_update_host")
+        return nfail, float(mi.value)
 
     # -- restart files (scale_file_restart_meshfield.F90) --
     def restart_write(self, path, q, step=0, time=0.0, dt=0.0, scheme=""):

@@ -162,6 +162,16 @@ typedef struct {
 int fedg_update(fedg_ctx* ctx, double* const q[5], int nsteps, const fedg_update_opts* opts,
                 double* iters_out);
 
+/* fedg_update for a caller whose fields live in host memory (FElib's CPU build keeps its MeshField
+ * arrays on the host): host_q[5] (DDENS, MOMX, MOMY, MOMZ, DRHOT in FElib layout) must be page-locked
+ * (cudaHostAlloc, or host memory registered with cudaHostRegister).  The fields are copied into the
+ * context's device copy of the state (allocated on first use), nsteps steps are taken, and the result
+ * is written back to host_q before the call returns.  With FEDG_PREC_PAIR the last stage kernel
+ * stores the result into host_q through its device mapping while it runs, so the device-to-host
+ * transfer overlaps its arithmetic; the other paths copy it back after the step. */
+int fedg_update_host(fedg_ctx* ctx, double* const host_q[5], int nsteps, const fedg_update_opts* opts,
+                     double* iters_out);
+
 /* Newton corrections of the FEDG_PREC_MIXED / FEDG_PREC_PAIR column solve.  Every column's first
  * correction solves the FP32 Jacobian by block-Thomas and element LU, like FElib's solve
  * (hevi_common_2.F90:329-479).  Later corrections, which only refine that FP32 solution, use a
