@@ -404,10 +404,6 @@ int fedg_drhot2pres(fedg_ctx* c, const double* DRHOT, double* PRES, double* DPRE
 static double* ensure_work(fedg_ctx* c, size_t ndouble) {
   if (c->work_doubles >= ndouble) return c->work;
   cudaFree(c->work);
-  cudaFree(c->host_state);
-  cudaFree(c->trc_buf);
-  cudaFree(c->nd_buf);
-  cudaFree(c->sponge_coef);
   c->work = nullptr;
   c->work_doubles = 0;
   if (cudaMalloc(&c->work, sizeof(double) * ndouble) != cudaSuccess) return nullptr;
@@ -752,7 +748,7 @@ int fedg_update_host(fedg_ctx* c, double* const host_q[5], int nsteps, const fed
   const bool direct = o->prec == FEDG_PREC_PAIR && nsteps > 0;
   const int r = update_impl(c, dq, nsteps, o, iters_out, direct ? hd : nullptr);
   if (r < 0) return r;
-  if (!direct)
+  if (!direct)  // the FP64 and FP32 paths copy the result back after the step
     for (int v = 0; v < 5; ++v) CK(cudaMemcpyAsync(host_q[v], dq[v], nb, cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   return r;

@@ -274,25 +274,72 @@ __device__ float col_residual(const OpsX& ox, const Col<N1>& c, const ProfX& px,
 }
 
 // ---------------------------------------------------------------------------------------------
-// First residual of a column whose iterate starts at var0: b = q* - var0 + impl_fac A(var0), with
-// A(var0) the implicit operator that the stage-1 kernel evaluated at q^n = var0 for its own
-// implicit tendency (both implicit stages of an ARK232 step start at var0, so one evaluation
-// serves both).  Formed in float pairs and rounded into c.Bf; no operator evaluation here.  The
-// first correction is never judged by it (convergence is tested on the certifying residual).
+// One pass over a column before its Newton solve, loads one element ahead:
+//  - the frozen vertical Rusanov speed |w| + c of var0 (hevi_common_2.F90:1149-1155) at the face
+//    nodes, combined over the two sides of every face into c.al (lanes 0 and N give the values,
+//    passed by shuffles; the element below's top value is carried to the next element);
+//  - the initial iterate P in c.P: var0, or q* plus the guess increment;
+//  - with a0 (the iterate starts at var0) the first residual b = (q* - var0) + impl_fac A(var0) in
+//    c.Bf, from the implicit operator the stage-1 kernel evaluated at q^n = var0 for its own
+//    implicit tendency (both implicit stages of an ARK232 step start at var0).  It is formed in
+//    float pairs and rounded; the first correction is never judged by it (convergence is tested
+//    on the certifying residual).
 template <int N1>
-__device__ void col_first_residual(const Col<N1>& c, const X5& qin, const A3& a0, float2 impl2) {
-  const int k = c.k;
+__device__ void col_start(const ProfX& px, float kapf, const Col<N1>& c, const F5c& z, const X5& qin,
+                          const float* const* guess, const A3& a0, float2 impl2) {
+  constexpr int N = N1 - 1;
+  const int k = c.k, NeZ = c.NeZ;
   const int gv[3] = {VD, VMZ, VRT};
+  const bool res = a0.v[0] != nullptr, useq = res || guess;
   const f2 impl = f2_of(impl2);
-#pragma unroll 4
-  for (int e = 0; e < c.NeZ; ++e) {
-    const int l = e * N1 + k;
-    const size_t gi = c.g(e);
+  double zc[3];
+  float2 qc[3] = {}, ac[3] = {};
+  float gc[3] = {};
+  {
+    const size_t g0 = c.g(0);
 #pragma unroll
     for (int v = 0; v < 3; ++v) {
-      const f2 b = f2_add(f2_sub(f2_of(__ldg(qin.v[gv[v]] + gi)), f2_of(c.P[3 * l + v])),
-                          f2_mul(impl, f2_of(__ldg(a0.v[v] + gi))));
-      c.Bf[3 * l + v] = f2_to_f(b);
+      zc[v] = __ldg(z.v[gv[v]] + g0);
+      if (useq) qc[v] = __ldg(qin.v[gv[v]] + g0);
+      if (res) ac[v] = __ldg(a0.v[v] + g0);
+      if (guess) gc[v] = __ldg(guess[v] + g0);
+    }
+  }
+  float aprev = 0.f;  // |w| + c at node N of the element below
+  for (int e = 0; e < NeZ; ++e) {
+    const int l = e * N1 + k;
+    const size_t gn = c.g(e + 1 < NeZ ? e + 1 : e);
+    double zn[3];
+    float2 qn[3] = {}, an[3] = {};
+    float gnx[3] = {};
+#pragma unroll
+    for (int v = 0; v < 3; ++v) {
+      zn[v] = __ldg(z.v[gv[v]] + gn);
+      if (useq) qn[v] = __ldg(qin.v[gv[v]] + gn);
+      if (res) an[v] = __ldg(a0.v[v] + gn);
+      if (guess) gnx[v] = __ldg(guess[v] + gn);
+    }
+    const float dd0 = f2_split(zc[0]).h, dr0 = f2_split(zc[2]).h;
+    const float rdens0 = 1.f / (__ldg(px.dhf + l) + dd0);
+    const float wt0 = f2_split(zc[1]).h * rdens0;
+    const float pres0 = __ldg(px.phf + l) * (1.f + expm1f(kapf * log1pf(dr0 * __ldg(px.rthf + l))));
+    const float at = fabsf(wt0) + sqrtf(kapf * pres0 * rdens0);
+    const float a0n = __shfl_sync(FULL, at, 0, N1), aNn = __shfl_sync(FULL, at, N, N1);
+    if (k == 0) {
+      c.al[2 * e] = fmaxf(a0n, e > 0 ? aprev : a0n);
+      if (e > 0) c.al[2 * e - 1] = fmaxf(aprev, a0n);
+      if (e == NeZ - 1) c.al[2 * e + 1] = fmaxf(aNn, aNn);
+    }
+    aprev = aNn;
+#pragma unroll
+    for (int v = 0; v < 3; ++v) {
+      const f2 p = guess ? f2_add_f(f2_of(qc[v]), gc[v]) : f2_split(zc[v]);
+      c.P[3 * l + v] = f2_pack(p);
+      if (res) c.Bf[3 * l + v] = f2_to_f(f2_add(f2_sub(f2_of(qc[v]), p), f2_mul(impl, f2_of(ac[v]))));
+      zc[v] = zn[v];
+      qc[v] = qn[v];
+      ac[v] = an[v];
+      gc[v] = gnx[v];
     }
   }
   __syncwarp();
@@ -810,31 +857,72 @@ __global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, 
   const float kapf = ox.kap.x;
   const float iif = (float)args.inv_impl_fac;
 
-  // ---- frozen vertical Rusanov speed |w| + c of var0 (hevi_common_2.F90:1149-1155) ----
-  float* atmp = c.Bf;  // [L]
-  // global loads one element ahead of their use, here and in the loops below
-  double zc[3] = {__ldg(z.v[VD] + c.g(0)), __ldg(z.v[VMZ] + c.g(0)), __ldg(z.v[VRT] + c.g(0))};
+  // ---- one pass over the column: alph, the initial iterate, the first residual ----
+  // (the MOMX/MOMY solve runs after the DENS/MOMZ/RHOT Newton: it reuses the Newton's shared memory)
+  const bool first_a0 = !guess && a0.v[0];
+  col_start<N1>(px, kapf, c, z, qin, guess, first_a0 ? a0 : A3{{nullptr, nullptr, nullptr}}, args.impl2);
+
+  // ---- DENS/MOMZ/RHOT Newton ----
+  const int gv[3] = {VD, VMZ, VRT};
+  const size_t gcolumn = (size_t)col, glayer = (size_t)ncol;  // G history rows of this column
+  const GHist gh{gsc, (size_t)ncol * (size_t)L};
+  const float cref = (float)args.cref;
+  // One call site per routine, which keeps the kernel's code small enough for the instruction
+  // caches.  The first residual is not tested (every column takes the first correction); from
+  // var0 it was formed by col_start from the stage kernel's A(var0), not by an operator evaluation.
+  // Corrections: the first is an LU correction (col_solve); after an LU correction the next one
+  // is a truncated Neumann series (col_neumann, when args.neumann > 0), which keeps going while
+  // each one cuts the certifying residual at least fourfold; a column whose residual did not
+  // contract asks for LU corrections again.  The warp runs an LU correction if any of its active
+  // columns asks for one.
+  int nsolve = 0, st = 0;
+  bool active = true, want_lu = true, last_lu = true;
+  float err_prev = 0.f;
+  while (true) {
+    // the first residual comes from the stage's A(var0) when the iterate starts at var0; every
+    // other one is the certifying float-pair residual
+    float err = 0.f;
+    if (!(nsolve == 0 && first_a0)) err = col_residual<N1, true>(ox, c, px, qin, args.impl2, cref);
+    if (active && nsolve > 0) {
+      if (err != err) { st = -2; active = false; }
+      else if ((double)err <= args.tol) { st = nsolve; active = false; }
+      else if (nsolve >= args.max_iter) { st = -1; active = false; }
+    }
+    if (!__any_sync(FULL, active)) break;
+    if (nsolve > 0) want_lu = args.neumann <= 0 || (!last_lu && !(err <= 0.25f * err_prev));
+    err_prev = err;
+    last_lu = __any_sync(FULL, active && want_lu);
+    if (last_lu) col_solve<N1>(op, px, kapf, c, args.impl_fac, gh, gcolumn, (size_t)col0, glayer, lane, active);
+    else col_neumann<N1>(op, px, kapf, c, args.impl_fac, args.neumann, active);
+    ++nsolve;
+  }
+  float2 qo[3];
+#pragma unroll
+  for (int m = 0; m < 3; ++m) qo[m] = __ldg(qin.v[gv[m]] + c.g(0));
   for (int e = 0; e < NeZ; ++e) {
     const int l = e * N1 + k;
-    const size_t gn = c.g(e + 1 < NeZ ? e + 1 : e);
-    const double zn[3] = {__ldg(z.v[VD] + gn), __ldg(z.v[VMZ] + gn), __ldg(z.v[VRT] + gn)};
-    const float dd0 = f2_split(zc[0]).h, dr0 = f2_split(zc[2]).h;
-    const float rdens0 = 1.f / (__ldg(px.dhf + l) + dd0);
-    const float wt0 = f2_split(zc[1]).h * rdens0;
+    const size_t gi = c.g(e);
+    const float2 qc[3] = {qo[0], qo[1], qo[2]};
+    {
+      const size_t gn = c.g(e + 1 < NeZ ? e + 1 : e);
 #pragma unroll
-    for (int v = 0; v < 3; ++v) zc[v] = zn[v];
-    const float pres0 = __ldg(px.phf + l) * (1.f + expm1f(kapf * log1pf(dr0 * __ldg(px.rthf + l))));
-    atmp[l] = fabsf(wt0) + sqrtf(kapf * pres0 * rdens0);
+      for (int m = 0; m < 3; ++m) qo[m] = __ldg(qin.v[gv[m]] + gn);
+    }
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      const f2 pnew = f2_of(c.P[3 * l + m]);
+      const f2 inc = f2_sub(pnew, f2_of(qc[m]));
+      if constexpr (PO) {
+        static_cast<float2*>(qsf[gv[m]])[gi] = f2_pack(pnew);
+        static_cast<float2*>(tout[gv[m]])[gi] = f2_pack(f2_mul(inc, f2_of(args.inv_impl2)));
+      } else {
+        static_cast<float*>(qsf[gv[m]])[gi] = f2_to_f(pnew);
+        static_cast<float*>(tout[gv[m]])[gi] = f2_to_f(inc) * iif;
+      }
+    }
   }
-  __syncwarp();
-  for (int e = k; e < NeZ; e += N1) {
-    const int lb = e * N1, lt = e * N1 + N;
-    c.al[2 * e] = fmaxf(atmp[lb], atmp[e > 0 ? lb - 1 : lb]);
-    c.al[2 * e + 1] = fmaxf(atmp[lt], atmp[e < NeZ - 1 ? lt + 1 : lt]);
-  }
-  __syncwarp();
-
-  // ---- MOMX/MOMY (eval_Ax_uv / solve_uv) ----
+  // ---- MOMX/MOMY (eval_Ax_uv / solve_uv), after the Newton: its scratch is the Newton's ----
+  __syncwarp();  // every lane has stored its DENS/MOMZ/RHOT nodes (c.P is overwritten below)
   // The operator is linear and acts on the face jumps only.  The unknown is E = P - q*, a float
   // pair per node, starting from var0 - q*: b(P) = impl_fac A(q* + E) - E.  The face jumps of q*
   // are formed in pairs once per column; the corrections are FP32 and accumulate into E in pairs,
@@ -975,76 +1063,6 @@ __global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, 
     __syncwarp();
   }
 
-  // ---- DENS/MOMZ/RHOT Newton ----
-  const int gv[3] = {VD, VMZ, VRT};
-#pragma unroll 4
-  for (int e = 0; e < NeZ; ++e) {
-    const int l = e * N1 + k;
-    const size_t gi = c.g(e);
-#pragma unroll
-    for (int m = 0; m < 3; ++m)
-      c.P[3 * l + m] = f2_pack(guess ? f2_add_f(f2_of(__ldg(qin.v[gv[m]] + gi)), __ldg(guess[m] + gi))
-                                     : f2_split(__ldg(z.v[gv[m]] + gi)));
-  }
-  __syncwarp();
-  const size_t gcolumn = (size_t)col, glayer = (size_t)ncol;  // G history rows of this column
-  const GHist gh{gsc, (size_t)ncol * (size_t)L};
-  const float cref = (float)args.cref;
-  // One call site per routine, which keeps the kernel's code small enough for the instruction
-  // caches.  The first residual is not tested (every column takes the first correction); from
-  // var0 it is formed from the stage kernel's A(var0) instead of a second operator evaluation.
-  // Corrections: the first is an LU correction (col_solve); after an LU correction the next one
-  // is a truncated Neumann series (col_neumann, when args.neumann > 0), which keeps going while
-  // each one cuts the certifying residual at least fourfold; a column whose residual did not
-  // contract asks for LU corrections again.  The warp runs an LU correction if any of its active
-  // columns asks for one.
-  int nsolve = 0, st = 0;
-  bool active = true, want_lu = true, last_lu = true;
-  float err_prev = 0.f;
-  while (true) {
-    // the first residual comes from the stage's A(var0) when the iterate starts at var0; every
-    // other one is the certifying float-pair residual
-    float err = 0.f;
-    if (nsolve == 0 && !guess && a0.v[0]) col_first_residual<N1>(c, qin, a0, args.impl2);
-    else err = col_residual<N1, true>(ox, c, px, qin, args.impl2, cref);
-    if (active && nsolve > 0) {
-      if (err != err) { st = -2; active = false; }
-      else if ((double)err <= args.tol) { st = nsolve; active = false; }
-      else if (nsolve >= args.max_iter) { st = -1; active = false; }
-    }
-    if (!__any_sync(FULL, active)) break;
-    if (nsolve > 0) want_lu = args.neumann <= 0 || (!last_lu && !(err <= 0.25f * err_prev));
-    err_prev = err;
-    last_lu = __any_sync(FULL, active && want_lu);
-    if (last_lu) col_solve<N1>(op, px, kapf, c, args.impl_fac, gh, gcolumn, (size_t)col0, glayer, lane, active);
-    else col_neumann<N1>(op, px, kapf, c, args.impl_fac, args.neumann, active);
-    ++nsolve;
-  }
-  float2 qo[3];
-#pragma unroll
-  for (int m = 0; m < 3; ++m) qo[m] = __ldg(qin.v[gv[m]] + c.g(0));
-  for (int e = 0; e < NeZ; ++e) {
-    const int l = e * N1 + k;
-    const size_t gi = c.g(e);
-    const float2 qc[3] = {qo[0], qo[1], qo[2]};
-    {
-      const size_t gn = c.g(e + 1 < NeZ ? e + 1 : e);
-#pragma unroll
-      for (int m = 0; m < 3; ++m) qo[m] = __ldg(qin.v[gv[m]] + gn);
-    }
-#pragma unroll
-    for (int m = 0; m < 3; ++m) {
-      const f2 pnew = f2_of(c.P[3 * l + m]);
-      const f2 inc = f2_sub(pnew, f2_of(qc[m]));
-      if constexpr (PO) {
-        static_cast<float2*>(qsf[gv[m]])[gi] = f2_pack(pnew);
-        static_cast<float2*>(tout[gv[m]])[gi] = f2_pack(f2_mul(inc, f2_of(args.inv_impl2)));
-      } else {
-        static_cast<float*>(qsf[gv[m]])[gi] = f2_to_f(pnew);
-        static_cast<float*>(tout[gv[m]])[gi] = f2_to_f(inc) * iif;
-      }
-    }
-  }
   if (k == 0 && status) status[col] = st;
   const unsigned nfail = __reduce_add_sync(FULL, (k == 0 && st < 0) ? 1u : 0u);
   const unsigned nsol = __reduce_add_sync(FULL, (k == 0 && st >= 0) ? (unsigned)st : 0u);
