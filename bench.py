@@ -562,9 +562,11 @@ def run_fedg(args):
     if world > 1:
         # the slabs share the case's mean wind as the reference of the momentum deviations
         ctx.set_ref_wind(case.u0, case.v0)
-        nbh = ctx.halo_bytes()
-        hsend = [torch.empty(nbh, dtype=torch.uint8, device=ctx.dev) for _ in range(2)]
-        hrecv = [torch.zeros(nbh, dtype=torch.uint8, device=ctx.dev) for _ in range(2)]
+        # slabs along x: halo buffers on the x- and x+ sides only
+        hsend = [torch.empty(ctx.halo_bytes(sd), dtype=torch.uint8, device=ctx.dev) if sd < 2 else None
+                 for sd in range(4)]
+        hrecv = [torch.zeros(ctx.halo_bytes(sd), dtype=torch.uint8, device=ctx.dev) if sd < 2 else None
+                 for sd in range(4)]
         halo = slabs.HaloExchange(hsend, hrecv, rank, world)
         ctx.set_halo(hsend, hrecv, halo)
     dens_hyd = ctx.tensor(b["dens_hyd"])

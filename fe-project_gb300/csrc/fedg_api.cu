@@ -276,8 +276,8 @@ int fedg_ctx_create(const fedg_mesh_desc* d, fedg_ctx** out) {
   if (!d || !out) return fail("fedg_ctx_create: null argument");
   if (d->porder < 1 || d->porder > FEDG_MAXN1 - 1) return fail("fedg_ctx_create: porder must be 1..7");
   if (d->NeX < 1 || d->NeY < 1 || d->NeZ < 1) return fail("fedg_ctx_create: element counts must be >= 1");
-  if ((d->periodic_x != 1 && d->periodic_x != FEDG_HALO) || d->periodic_y != 1)
-    return fail("fedg_ctx_create: lateral boundaries must be periodic (periodic_x = 1 or FEDG_HALO for a slab, periodic_y = 1)");
+  if ((d->periodic_x != 1 && d->periodic_x != FEDG_HALO) || (d->periodic_y != 1 && d->periodic_y != FEDG_HALO))
+    return fail("fedg_ctx_create: lateral boundaries must be periodic (1) or halo-exchanged parts of a decomposed domain (FEDG_HALO)");
   if (!(d->xmax > d->xmin && d->ymax > d->ymin && d->zmax > d->zmin)) return fail("fedg_ctx_create: empty domain");
   if (d->NeZ > 64) return fail("fedg_ctx_create: NeZ > 64 is not supported by the column solver");
   CK(cudaSetDevice(d->device));
@@ -423,8 +423,8 @@ int fedg_cal_tend_ex(fedg_ctx* c, const double* const in[16], double* const out[
     if (r) return r;
   }
   if (!c->base_set) return fail("fedg_cal_tend_ex: base state not set");
-  if (fedg::slab(c) && !c->hrecv[0])
-    return fail("fedg_cal_tend_ex: a slab (periodic_x = FEDG_HALO) needs its halo buffers (fedg_update_set_halo)");
+  if (fedg::slab(c) && !c->hrecv[fedg::halo_dir(c, 0) ? 0 : 2])
+    return fail("fedg_cal_tend_ex: a decomposed mesh (periodic_x/y = FEDG_HALO) needs its halo buffers (fedg_update_set_halo)");
   const double* dpres = in[5];
   if (!dpres) {
     double* w = ensure_work(c, c->n);
@@ -770,7 +770,7 @@ int fedg_update_set_tracer_flux(fedg_ctx* c, double* const mflx[3], double* alph
     for (int i = 0; i < 7; ++i) c->trc_flux[i] = nullptr;
     return 0;
   }
-  if (fedg::slab(c)) return fail("fedg_update_set_tracer_flux: not available on a slab (periodic_x = FEDG_HALO)");
+  if (fedg::slab(c)) return fail("fedg_update_set_tracer_flux: not available on a part of a decomposed mesh (periodic_x/y = FEDG_HALO)");
   if (!mflx[0] || !mflx[1] || !mflx[2] || !alph_M || !alph_P || !DDENS_TRC || !DDENS0_TRC)
     return fail("fedg_update_set_tracer_flux: null field");
   double* const v[7] = {mflx[0], mflx[1], mflx[2], alph_M, alph_P, DDENS_TRC, DDENS0_TRC};

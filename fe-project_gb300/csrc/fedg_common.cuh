@@ -28,10 +28,23 @@ struct Ops {
   double coriolis_f;
   int NeX, NeY, NeZ;
   int N1, Np, L;  // L = NeZ*N1 levels
-  // slab of a decomposed domain: the x- and x+ exterior face layers (receive buffers of the halo
-  // exchange, [6 fields][NeY*NeZ][N1*N1] doubles); NULL on a periodic mesh
-  const double* hx[2];
+  // part of a decomposed domain: the exterior face layers of the x-, x+, y-, y+ boundaries (receive
+  // buffers of the halo exchange, [6 fields][NeY*NeZ or NeX*NeZ][N1*N1] doubles); NULL where the
+  // mesh is periodic in that direction
+  const double* hx[4];
 };
+
+// halo side of face f of element (ex, ey) on a decomposed mesh: 0 x-, 1 x+, 2 y-, 3 y+, or -1 for a
+// face inside the mesh or a lid; the buffer index of face node ab of that side; the side's field stride
+__device__ __forceinline__ int halo_side(int f, int ex, int ey, int NeX, int NeY) {
+  return (f == 3 && ex == 0) ? 0 : (f == 1 && ex == NeX - 1) ? 1 : (f == 0 && ey == 0) ? 2 : (f == 2 && ey == NeY - 1) ? 3 : -1;
+}
+__device__ __forceinline__ size_t halo_index(int side, int ex, int ey, int ez, int ab, int NeX, int NeY, int NF) {
+  return (size_t)(side < 2 ? ey + NeY * ez : ex + NeX * ez) * NF + ab;
+}
+__device__ __forceinline__ size_t halo_stride(int side, int NeX, int NeY, int NeZ, int NF) {
+  return (size_t)(side < 2 ? NeY : NeX) * NeZ * NF;
+}
 
 // column profiles of the horizontally homogeneous base state, [L] each
 struct Prof {

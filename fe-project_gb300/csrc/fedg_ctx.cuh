@@ -53,10 +53,10 @@ struct fedg_ctx {
   // from the first state they see
   bool wind_given = false;
   double wind[2] = {0.0, 0.0};
-  // slab of a decomposed domain (periodic_x = FEDG_HALO): the caller's halo buffers and exchange
-  // (fedg_update_set_halo)
-  void* hsend[2] = {};
-  void* hrecv[2] = {};
+  // part of a decomposed domain (periodic_x and/or periodic_y = FEDG_HALO): the caller's halo
+  // buffers of the x-, x+, y-, y+ sides and its exchange (fedg_update_set_halo)
+  void* hsend[4] = {};
+  void* hrecv[4] = {};
   fedg_halo_fn hfn = nullptr;
   void* huser = nullptr;
   // kernel timers / launch counters
@@ -84,7 +84,8 @@ bool ref_wind(const fedg_ctx* c, double out[2]);
 void set_ref_wind_given(fedg_ctx* c, double U, double V);
 // slab of a decomposed domain (fedg_halo.cu): packs the stage state's x face layers, synchronises
 // and calls the caller's exchange; FP64 fields (+ DPRES, NULL: formed) or float-pair deviations
-bool slab(const fedg_ctx* c);
+bool slab(const fedg_ctx* c);  // true if either lateral direction exchanges a halo
+bool halo_dir(const fedg_ctx* c, int side);  // side 0..3 (x-, x+, y-, y+) is a halo side
 int halo_exchange_fp64(fedg_ctx* c, const double* const q[5], const double* dpres, int stage);
 int halo_exchange_pair(fedg_ctx* c, const float2* const qs[5], int stage);
 // fedg_cal_tend_ex_noalloc's set-up (fedg_static.cu): looks up its static scratch array on device `dev`,

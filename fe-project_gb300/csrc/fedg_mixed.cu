@@ -886,7 +886,7 @@ static int set_ref_wind(fedg_ctx* c, MixedState* m, double* const q[5]) {
     return 0;
   }
   if (slab(c))  // the slabs of one domain must share one reference wind
-    return api_fail("fedg_update: a slab (periodic_x = FEDG_HALO) needs the domain's reference wind (fedg_update_set_ref_wind)");
+    return api_fail("fedg_update: a part of a decomposed mesh (periodic_x/y = FEDG_HALO) needs the domain's reference wind (fedg_update_set_ref_wind)");
   int r;
   double* d_s = reinterpret_cast<double*>(m->fbuf);  // TI area, free before the first step: 3 sums, then
   double* d_part = d_s + 4;                          // the block sums [WIND_BLOCKS][3]
@@ -920,8 +920,7 @@ static int pair_update_heve(fedg_ctx* c, double* const q[5], int nsteps, const f
   if ((r = set_ref_wind(c, m, q))) return r;
   m->opp.Uref = m->opx.Uref;
   m->opp.Vref = m->opx.Vref;
-  m->opp.hx[0] = slab(c) ? static_cast<const float2*>(c->hrecv[0]) : nullptr;
-  m->opp.hx[1] = slab(c) ? static_cast<const float2*>(c->hrecv[1]) : nullptr;
+  for (int sd = 0; sd < 4; ++sd) m->opp.hx[sd] = halo_dir(c, sd) ? static_cast<const float2*>(c->hrecv[sd]) : nullptr;
   PairCoef pc;
   std::memset(&pc, 0, sizeof(pc));
   pc.dt = split_host(o->dt);
@@ -988,7 +987,7 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
   MixedState* m = c->mixed;
   const bool pair = o->prec == FEDG_PREC_PAIR;
   if (!pair && slab(c))
-    return api_fail("fedg_update: the FP32 mode needs a periodic mesh; a slab (periodic_x = FEDG_HALO) runs FEDG_PREC_FP64 or FEDG_PREC_PAIR");
+    return api_fail("fedg_update: the FP32 mode needs a periodic mesh; a part of a decomposed mesh (periodic_x/y = FEDG_HALO) runs FEDG_PREC_FP64 or FEDG_PREC_PAIR");
   if (pair && (r = pair_setup(c, m))) return r;
   if (o->use_guess && !mlp_ready(c->guess)) return api_fail("fedg_update: use_guess set but no trained column-guess network is loaded (fedg_guess_load)");
   const double alp = (3.0 + 2.0 * std::sqrt(2.0)) / 6.0, gam = 1.0 - 1.0 / std::sqrt(2.0), del = 1.0 / (2.0 * std::sqrt(2.0));
@@ -1014,8 +1013,7 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
   cf.Vref2 = m->opx.Vref;
   m->opp.Uref = m->opx.Uref;
   m->opp.Vref = m->opx.Vref;
-  m->opp.hx[0] = slab(c) ? static_cast<const float2*>(c->hrecv[0]) : nullptr;
-  m->opp.hx[1] = slab(c) ? static_cast<const float2*>(c->hrecv[1]) : nullptr;
+  for (int sd = 0; sd < 4; ++sd) m->opp.hx[sd] = halo_dir(c, sd) ? static_cast<const float2*>(c->hrecv[sd]) : nullptr;
   const double impl_fac = gam * o->dt;
   MixViArgs va{impl_fac, 1.0 / impl_fac, o->tol, 340.0, split_host(impl_fac), split_host(1.0 / impl_fac), o->max_iter, 1,
                c->vi_neumann};

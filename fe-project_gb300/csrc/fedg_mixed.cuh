@@ -78,9 +78,9 @@ struct OpsP {
   float rmax;
   double kap64;
   int NeX, NeY, NeZ, N1, Np, L;
-  // slab of a decomposed domain: the x- and x+ exterior face layers as deviation pairs
-  // ([6][NeY*NeZ][N1*N1], fields DDENS..DRHOT used); NULL on a periodic mesh
-  const float2* hx[2];
+  // part of a decomposed domain: the x-, x+, y-, y+ exterior face layers as deviation pairs
+  // ([6][NeY*NeZ or NeX*NeZ][N1*N1], fields DDENS..DRHOT used); NULL where periodic
+  const float2* hx[4];
 };
 // base-state profiles for the pair stage kernels, [L] each
 struct ProfP {

@@ -323,7 +323,7 @@ int fedg_numdiff_apply(fedg_ctx* c, double* const q[5], int nlap, double coef_h,
 int fedg_numdiff_apply_prec(fedg_ctx* c, double* const q[5], int nlap, double coef_h, double coef_v, double dt,
                             int prec) {
   if (!c || !q) return api_fail("fedg_numdiff_apply: null argument");
-  if (fedg::slab(c)) return api_fail("fedg_numdiff_apply: not available on a slab (periodic_x = FEDG_HALO)");
+  if (fedg::slab(c)) return api_fail("fedg_numdiff_apply: not available on a part of a decomposed mesh (periodic_x/y = FEDG_HALO)");
   if (prec != FEDG_PREC_FP64 && prec != FEDG_PREC_PAIR)
     return api_fail("fedg_numdiff_apply: prec must be FEDG_PREC_FP64 or FEDG_PREC_PAIR");
   for (int v = 0; v < 5; ++v)

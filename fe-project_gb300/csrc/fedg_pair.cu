@@ -188,14 +188,15 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
       long kn;
       int levP;
       face_nb<N1>(op, f, ke, ex, ey, ez, nxy, kn, levP, kM);
-      // a slab's x boundary: the exterior face layer comes from the halo exchange
-      const float2* hxs = (f == 3 && ex == 0) ? op.hx[0] : ((f == 1 && ex == op.NeX - 1) ? op.hx[1] : nullptr);
+      // a boundary of a decomposed mesh: the exterior face layer comes from the halo exchange
+      const int hsd = halo_side(f, ex, ey, op.NeX, op.NeY);
+      const float2* hxs = hsd >= 0 ? op.hx[hsd] : nullptr;
       const int levM = ez * N1 + kM;
       const f2 ddM = f2_of(st[VD * Np + pM]), mxM = f2_of(st[VMX * Np + pM]), myM = f2_of(st[VMY * Np + pM]);
       const f2 mzM = f2_of(st[VMZ * Np + pM]), drM = f2_of(st[VRT * Np + pM]), dpM = f2_of(st[5 * Np + pM]);
       f2 ddP, mxP, myP, mzP, drP, dpP;
       if (hxs) {
-        const size_t per = (size_t)op.NeY * op.NeZ * NF, h = (size_t)(ey + op.NeY * ez) * NF + ab;
+        const size_t per = halo_stride(hsd, op.NeX, op.NeY, op.NeZ, NF), h = halo_index(hsd, ex, ey, ez, ab, op.NeX, op.NeY, NF);
         ddP = ld2(hxs + h); mxP = ld2(hxs + per + h); myP = ld2(hxs + 2 * per + h);
         mzP = ld2(hxs + 3 * per + h); drP = ld2(hxs + 4 * per + h);
         dpP = dpres2(op, drP, ld2(pf.rth + levP), ld2(pf.ph + levP));

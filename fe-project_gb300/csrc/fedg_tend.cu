@@ -102,10 +102,11 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
       double ddM = st[VD * Np + pM], mxM = st[VMX * Np + pM], myM = st[VMY * Np + pM];
       double mzM = st[VMZ * Np + pM], drM = st[VRT * Np + pM], dpM = st[5 * Np + pM];
       double ddP, mxP, myP, mzP, drP, dpP;
-      // a slab's x boundary: the exterior face layer comes from the halo exchange
-      const double* hxs = (f == 3 && ex == 0) ? op.hx[0] : ((f == 1 && ex == op.NeX - 1) ? op.hx[1] : nullptr);
+      // a boundary of a decomposed mesh: the exterior face layer comes from the halo exchange
+      const int hsd = halo_side(f, ex, ey, op.NeX, op.NeY);
+      const double* hxs = hsd >= 0 ? op.hx[hsd] : nullptr;
       if (hxs) {
-        const size_t per = (size_t)op.NeY * op.NeZ * NF, h = (size_t)(ey + op.NeY * ez) * NF + ab;
+        const size_t per = halo_stride(hsd, op.NeX, op.NeY, op.NeZ, NF), h = halo_index(hsd, ex, ey, ez, ab, op.NeX, op.NeY, NF);
         ddP = __ldg(hxs + h); mxP = __ldg(hxs + per + h); myP = __ldg(hxs + 2 * per + h);
         mzP = __ldg(hxs + 3 * per + h); drP = __ldg(hxs + 4 * per + h); dpP = __ldg(hxs + 5 * per + h);
       } else if (kn >= 0) {

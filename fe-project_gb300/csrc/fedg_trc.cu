@@ -631,7 +631,7 @@ int check_base(const fedg_ctx* c, const char* who) {
 
 // the tracer kernels read lateral neighbours of a periodic mesh only (no slab halo)
 int check_periodic(const fedg_ctx* c, const char* who) {
-  if (fedg::slab(c)) return api_fail(std::string(who) + ": not available on a slab (periodic_x = FEDG_HALO)");
+  if (fedg::slab(c)) return api_fail(std::string(who) + ": not available on a part of a decomposed mesh (periodic_x/y = FEDG_HALO)");
   return 0;
 }
 

@@ -166,8 +166,8 @@ def load():
                                    ctypes.POINTER(ctypes.c_longlong)]
     lib.fedg_update_host.argtypes = [_vp, _P5, ctypes.c_int, ctypes.POINTER(UpdateOpts), ctypes.POINTER(ctypes.c_double)]
     lib.fedg_halo_bytes.restype = ctypes.c_size_t
-    lib.fedg_halo_bytes.argtypes = [_vp]
-    lib.fedg_update_set_halo.argtypes = [_vp, ctypes.c_void_p * 2, ctypes.c_void_p * 2, HALO_FN, ctypes.c_void_p]
+    lib.fedg_halo_bytes.argtypes = [_vp, ctypes.c_int]
+    lib.fedg_update_set_halo.argtypes = [_vp, ctypes.c_void_p * 4, ctypes.c_void_p * 4, HALO_FN, ctypes.c_void_p]
     lib.fedg_halo_pack.argtypes = [_vp, _P5, _vp]
     lib.fedg_update_set_ref_wind.argtypes = [_vp, ctypes.c_double, ctypes.c_double]
     lib.fedg_update_get_ref_wind.argtypes = [_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
@@ -200,7 +200,7 @@ def _p5(ts):
 class Context:
     """One fedg context (mesh, operators, base state, CUDA stream) on one GPU."""
 
-    def __init__(self, case, device: int = 0, filter_on=None, periodic_x: int = 1):
+    def __init__(self, case, device: int = 0, filter_on=None, periodic_x: int = 1, periodic_y: int = 1):
         import torch
 
         if not torch.cuda.is_available():
@@ -213,7 +213,7 @@ class Context:
         from .cases import CPDRY, CVDRY, GRAV, PRES00, RDRY
 
         fo = case.filter_on if filter_on is None else filter_on
-        d = MeshDesc(case.porder, case.NeX, case.NeY, case.NeZ, xmin, xmax, ymin, ymax, zmin, zmax, int(periodic_x), 1,
+        d = MeshDesc(case.porder, case.NeX, case.NeY, case.NeZ, xmin, xmax, ymin, ymax, zmin, zmax, int(periodic_x), int(periodic_y),
                      getattr(case, "grav", GRAV), RDRY, CPDRY, CVDRY, PRES00, int(fo), 2.0 / 3.0, 36.0, 16,
                      2.0 / 3.0, 36.0, 16, device)
         h = _vp()
@@ -320,14 +320,16 @@ class Context:
             self.sync()
         return nfail, float(mi.value)
 
-    # -- slab of a decomposed domain (MeshFieldComm exchange, scale_meshfieldcomm_base.F90:340-470) --
-    def halo_bytes(self) -> int:
-        return int(self.lib.fedg_halo_bytes(self.h))
+    # -- part of a decomposed domain (MeshFieldComm exchange, scale_meshfieldcomm_base.F90:340-470) --
+    def halo_bytes(self, side: int) -> int:
+        """bytes of the halo buffer of side 0..3 (x-, x+, y-, y+); 0 where the mesh is periodic"""
+        return int(self.lib.fedg_halo_bytes(self.h, int(side)))
 
     def set_halo(self, send, recv, exchange=None):
-        """send, recv: two device buffers each (torch tensors of halo_bytes() bytes, kept alive by the
-        caller); exchange(stage) -> None moves this slab's send[1] to the x+ neighbour's recv[0] and
-        its send[0] to the x- neighbour's recv[1] and returns once recv holds the neighbours' data."""
+        """send, recv: four device buffers each (torch tensors of halo_bytes(side) bytes, None on
+        periodic sides, kept alive here); exchange(stage) -> None moves send[1] to the x+ neighbour's
+        recv[0], send[0] to the x- neighbour's recv[1], send[3] to the y+ neighbour's recv[2] and
+        send[2] to the y- neighbour's recv[3], and returns once recv holds the neighbours' data."""
         def fn(_user, stage):
             try:
                 exchange(int(stage))
@@ -337,8 +339,8 @@ class Context:
                 return 1
         self._halo_fn = HALO_FN(fn) if exchange is not None else ctypes.cast(None, HALO_FN)
         self._halo_bufs = (send, recv)
-        sp = (ctypes.c_void_p * 2)(*[t.data_ptr() for t in send])
-        rp = (ctypes.c_void_p * 2)(*[t.data_ptr() for t in recv])
+        sp = (ctypes.c_void_p * 4)(*[None if t is None else t.data_ptr() for t in send])
+        rp = (ctypes.c_void_p * 4)(*[None if t is None else t.data_ptr() for t in recv])
         _check(self.lib.fedg_update_set_halo(self.h, sp, rp, self._halo_fn, None), "fedg_update_set_halo")
 
     def halo_pack(self, q, dpres=None):
@@ -654,14 +656,16 @@ class Guess:
         torch.cuda.synchronize()
         return Y
 
-    # -- slab of a decomposed domain (MeshFieldComm exchange, scale_meshfieldcomm_base.F90:340-470) --
-    def halo_bytes(self) -> int:
-        return int(self.lib.fedg_halo_bytes(self.h))
+    # -- part of a decomposed domain (MeshFieldComm exchange, scale_meshfieldcomm_base.F90:340-470) --
+    def halo_bytes(self, side: int) -> int:
+        """bytes of the halo buffer of side 0..3 (x-, x+, y-, y+); 0 where the mesh is periodic"""
+        return int(self.lib.fedg_halo_bytes(self.h, int(side)))
 
     def set_halo(self, send, recv, exchange=None):
-        """send, recv: two device buffers each (torch tensors of halo_bytes() bytes, kept alive by the
-        caller); exchange(stage) -> None moves this slab's send[1] to the x+ neighbour's recv[0] and
-        its send[0] to the x- neighbour's recv[1] and returns once recv holds the neighbours' data."""
+        """send, recv: four device buffers each (torch tensors of halo_bytes(side) bytes, None on
+        periodic sides, kept alive here); exchange(stage) -> None moves send[1] to the x+ neighbour's
+        recv[0], send[0] to the x- neighbour's recv[1], send[3] to the y+ neighbour's recv[2] and
+        send[2] to the y- neighbour's recv[3], and returns once recv holds the neighbours' data."""
         def fn(_user, stage):
             try:
                 exchange(int(stage))
@@ -671,8 +675,8 @@ class Guess:
                 return 1
         self._halo_fn = HALO_FN(fn) if exchange is not None else ctypes.cast(None, HALO_FN)
         self._halo_bufs = (send, recv)
-        sp = (ctypes.c_void_p * 2)(*[t.data_ptr() for t in send])
-        rp = (ctypes.c_void_p * 2)(*[t.data_ptr() for t in recv])
+        sp = (ctypes.c_void_p * 4)(*[None if t is None else t.data_ptr() for t in send])
+        rp = (ctypes.c_void_p * 4)(*[None if t is None else t.data_ptr() for t in recv])
         _check(self.lib.fedg_update_set_halo(self.h, sp, rp, self._halo_fn, None), "fedg_update_set_halo")
 
     def halo_pack(self, q, dpres=None):

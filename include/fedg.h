@@ -19,8 +19,8 @@
  *     DEVICE pointer (the Fortran side passes it under `!$acc host_data use_device`).
  *     Only the first Np*Ne entries (the local elements) are read or written: exterior
  *     values of periodic faces and of the slip lids are formed inside the kernels, so no
- *     halo exchange is needed on one GPU; a slab of a decomposed domain exchanges its x faces
- *     through caller-owned buffers (fedg_update_set_halo).
+ *     halo exchange is needed on one GPU; a part of a decomposed domain exchanges its boundary
+ *     faces through caller-owned buffers (fedg_update_set_halo).
  *   - Element order ke = i + (j-1)*NeX + (k-1)*NeX*NeY, node order p = i + (j-1)*N1 + (k-1)*N1^2.
  *   - Return codes: 0 ok; > 0 number of columns whose Newton iteration did not converge;
  *     < 0 error (fedg_last_error() gives the text).  No entry point traps the GPU.
@@ -46,8 +46,8 @@ typedef struct {
   int porder;                 /* PolyOrder_h == PolyOrder_v, 1..7                         */
   int NeX, NeY, NeZ;          /* local elements per direction                            */
   double xmin, xmax, ymin, ymax, zmin, zmax;
-  int periodic_x, periodic_y; /* 1: periodic lateral boundaries; periodic_x = FEDG_HALO:  */
-                              /* the mesh is one x-slab of a larger domain (see below)   */
+  int periodic_x, periodic_y; /* 1: periodic; FEDG_HALO: the mesh is one part of a domain */
+                              /* decomposed in that direction (see below)                */
   double grav, rdry, cpdry, cvdry, pres00;
   int mf_on;                  /* MODALFILTER_FLAG                                        */
   double mf_etac_h, mf_alpha_h; int mf_order_h;
@@ -190,42 +190,43 @@ int fedg_update_set_vi_neumann(fedg_ctx* ctx, int nterm);
  * limit makes the wait run out on purpose, which is how the error path is tested. */
 int fedg_update_set_wait_limit(fedg_ctx* ctx, int polls);
 
-/* ---- Horizontal slab decomposition ---------------------------------------------------------
+/* ---- Horizontal domain decomposition -------------------------------------------------------
  * FElib distributes its domain over MPI ranks and, before each tendency evaluation, exchanges the
  * face values of the prognostic fields (PROG_VARS%MeshFieldComm_Exchange, driver_nonhydro3d.F90:
  * 768-771) and of DPRES (AUXDYNVAR3D_manager%MeshFieldComm_Exchange, :783-787) through
  * MeshFieldCommBase_exchange_core / _wait_core (scale_meshfieldcomm_base.F90:340-470).
- * Here a context whose mesh has periodic_x = FEDG_HALO is one slab of a domain split along x into
- * slabs of full y extent and full-height columns (the column solves stay local).  Its two x
- * boundaries take their exterior values from halo buffers that the caller's transport (MPI,
- * NCCL, peer copies) fills; y stays periodic inside the slab and z has the slip lids.
- *   side 0 (x-): recv[0] holds the x- neighbour's last element layer (its x+ face nodes), which
- *                that neighbour packs into its send[1];
- *   side 1 (x+): recv[1] holds the x+ neighbour's first element layer (its x- face nodes), which
- *                that neighbour packs into its send[0].
- * Layout of each buffer: [6 fields][NeY*NeZ elements, ey + NeY*ez][N1*N1 face nodes, a + N1*b] of
- * 8-byte values; the fields are DDENS, MOMX, MOMY, MOMZ, DRHOT, DPRES and face node (a, b) of an x
- * face is node (i, a, b) of the element, i = 0 (x-) or N (x+).  FEDG_PREC_FP64 exchanges doubles;
- * FEDG_PREC_PAIR exchanges float pairs (hi, lo) of the deviations from the hydrostatic state and
- * the reference wind and leaves the DPRES slot unused (the receiving side forms it from DRHOT).
- * The FP32 mode (FEDG_PREC_MIXED), the tracer, numerical-diffusion and tracer-flux entry points
- * need a periodic mesh and refuse a slab. */
+ * Here the domain is split along x and/or y into parts with full-height columns (the column solves
+ * stay local): a context whose mesh has periodic_x = FEDG_HALO (periodic_y = FEDG_HALO) is one part
+ * whose x (y) boundaries take their exterior values from halo buffers that the caller's transport
+ * (MPI, NCCL, peer copies) fills; a direction left at 1 stays periodic inside the part, and z has
+ * the slip lids.  Sides: 0 x-, 1 x+, 2 y-, 3 y+.
+ *   recv[0] holds the x- neighbour's x+ face layer, which that neighbour packs into its send[1];
+ *   recv[1] holds the x+ neighbour's x- face layer (its send[0]); recv[2] and recv[3] the same in y.
+ * Layout of each buffer: [6 fields][boundary elements][N1*N1 face nodes] of 8-byte values; the
+ * fields are DDENS, MOMX, MOMY, MOMZ, DRHOT, DPRES, the boundary elements are numbered ey + NeY*ez on
+ * the x sides and ex + NeX*ez on the y sides, and face node a + N1*b is node (i, a, b) of the element
+ * on an x face (i = 0 or N) and node (a, j, b) on a y face (j = 0 or N).  FEDG_PREC_FP64 exchanges
+ * doubles; FEDG_PREC_PAIR exchanges float pairs (hi, lo) of the deviations from the hydrostatic
+ * state and the reference wind and leaves the DPRES slot unused (the receiving side forms it from
+ * DRHOT).  The FP32 mode (FEDG_PREC_MIXED), the tracer, numerical-diffusion and tracer-flux entry
+ * points need a periodic mesh and refuse a decomposed one. */
 enum { FEDG_HALO = 2 };
-/* bytes of one halo buffer (one side) */
-size_t fedg_halo_bytes(const fedg_ctx* ctx);
-/* The exchange fedg_update calls before every tendency evaluation of a slab: the library has
- * packed the stage state into send[0] and send[1] and synchronised its stream; the function moves
- * this rank's send[1] to the x+ neighbour's recv[0] and its send[0] to the x- neighbour's recv[1],
- * and returns 0 once this rank's recv[0] and recv[1] hold the neighbours' data (nonzero: fedg_update
- * returns < 0).  stage: the RK stage (1..3) of the tendency about to be evaluated. */
+/* bytes of the halo buffer of one side (0 for a side whose direction is periodic) */
+size_t fedg_halo_bytes(const fedg_ctx* ctx, int side);
+/* The exchange fedg_update calls before every tendency evaluation of a part: the library has
+ * packed the stage state into the send buffers of the halo sides and synchronised its stream; the
+ * function moves send[1] to the x+ neighbour's recv[0], send[0] to the x- neighbour's recv[1],
+ * send[3] to the y+ neighbour's recv[2] and send[2] to the y- neighbour's recv[3] (the halo sides
+ * only), and returns 0 once this part's receive buffers hold the neighbours' data (nonzero:
+ * fedg_update returns < 0).  stage: the RK stage (1..3) of the tendency about to be evaluated. */
 typedef int (*fedg_halo_fn)(void* user, int stage);
-/* Registers the slab's halo buffers (device, fedg_halo_bytes each; the caller owns them, so its
- * transport can use them directly) and the exchange (fn may be NULL for callers that only use
- * fedg_halo_pack and fedg_cal_tend_ex). */
-int fedg_update_set_halo(fedg_ctx* ctx, void* const send[2], void* const recv[2], fedg_halo_fn fn, void* user);
-/* Packs the FP64 face layers of q (5 fields) and DPRES (NULL: formed from DRHOT) into send[0] and
- * send[1] and synchronises: FElib's MeshFieldComm put before an exchange, for callers of
- * fedg_cal_tend_ex on a slab, which reads recv[0] and recv[1] as they are when it runs. */
+/* Registers the part's halo buffers (device, fedg_halo_bytes(ctx, side) each, NULL on periodic
+ * sides; the caller owns them, so its transport can use them directly) and the exchange (fn may be
+ * NULL for callers that only use fedg_halo_pack and fedg_cal_tend_ex). */
+int fedg_update_set_halo(fedg_ctx* ctx, void* const send[4], void* const recv[4], fedg_halo_fn fn, void* user);
+/* Packs the FP64 face layers of q (5 fields) and DPRES (NULL: formed from DRHOT) into the send
+ * buffers and synchronises: FElib's MeshFieldComm put before an exchange, for callers of
+ * fedg_cal_tend_ex on a part, which reads the receive buffers as they are when it runs. */
 int fedg_halo_pack(fedg_ctx* ctx, const double* const q[5], const double* DPRES);
 /* The reference wind (U, V) of the FP32 and float-pair paths' momentum deviations.  A periodic
  * context takes it from the domain mean of the first state it sees; slabs must share one, so a slab

@@ -30,7 +30,7 @@
 //                              ..._trcadvect3d_heve.F90, ..._driver_trcadv3d.F90:330-560
 //   * numerical diffusion      ..._nonhydro3d_numdiff.F90:214-721, ..._dgm_bnd.F90:370-508
 //   * sponge layer             ..._dgm_spongelayer.F90:134-219
-//   * slab of a domain split along x (orc_set_halo): the x faces of the boundary elements
+//   * part of a domain split along x and/or y (orc_set_halo): the faces of the boundary elements
 //     read the exchanged face layers, filled by a callback before every tendency, as the
 //     driver's MeshFieldComm_Exchange does (..._driver_nonhydro3d.F90:768-787,
 //     FElib/src/data/scale_meshfieldcomm_base.F90:340-470)
@@ -197,11 +197,12 @@ struct Oracle {
   // sponge layer in the dynamics step when tau > 0 (driver_nonhydro3d.F90:831-841)
   double sl_tau = 0.0, sl_height = 0.0;
   int sl_hvel = 0;
-  // slab of a domain decomposed along x (FElib's MeshFieldComm exchange, scale_meshfieldcomm_base.F90:
-  // 340-470, called by the driver before each tendency, driver_nonhydro3d.F90:768-787): the x- and x+
-  // exterior face layers [6 fields: DDENS, MOMX, MOMY, MOMZ, DRHOT, DPRES][NeY*NeZ][Nfp], filled by
-  // halo_cb before every tendency of a step; NULL on a periodic mesh
-  const double* hx[2] = {nullptr, nullptr};
+  // part of a domain decomposed along x and/or y (FElib's MeshFieldComm exchange,
+  // scale_meshfieldcomm_base.F90:340-470, called by the driver before each tendency,
+  // driver_nonhydro3d.F90:768-787): the x-, x+, y-, y+ exterior face layers [6 fields: DDENS, MOMX,
+  // MOMY, MOMZ, DRHOT, DPRES][NeY*NeZ (x sides) or NeX*NeZ (y sides)][Nfp], filled by halo_cb before
+  // every tendency of a step; NULL on a side whose direction is periodic
+  const double* hx[4] = {nullptr, nullptr, nullptr, nullptr};
   void (*halo_cb)(void* user, int stage, const double* const* q, const double* dpres) = nullptr;
   void* halo_user = nullptr;
 
@@ -290,8 +291,11 @@ static void cal_tend(const Oracle& o, int hevi, const double* const q[5], const 
             else { iP = iM; msign = -1.0; }  // slip lid: MOMZ reflected (dgm_bnd.F90:323-341)
             // a slab's x boundary: the exterior values come from the exchanged face layer (the base
             // state is horizontally homogeneous, so the exterior node's base values are the own node's)
-            const double* hs = (f == 3 && ex == 0) ? o.hx[0] : ((f == 1 && ex == o.NeX - 1) ? o.hx[1] : nullptr);
-            const size_t hper = (size_t)o.NeY * o.NeZ * Nfp, hi = (size_t)(ey + o.NeY * ez) * Nfp + a + N1 * b;
+            const int hsd = (f == 3 && ex == 0) ? 0 : (f == 1 && ex == o.NeX - 1) ? 1 : (f == 0 && ey == 0) ? 2
+                          : (f == 2 && ey == o.NeY - 1) ? 3 : -1;
+            const double* hs = hsd >= 0 ? o.hx[hsd] : nullptr;
+            const size_t hper = (size_t)(hsd < 2 ? o.NeY : o.NeX) * o.NeZ * Nfp;
+            const size_t hi = (size_t)(hsd < 2 ? ey + o.NeY * ez : ex + o.NeX * ez) * Nfp + a + N1 * b;
             if (hs) iP = iM;
             const double ddM = q[VD][iM], ddP = hs ? hs[hi] : q[VD][iP];
             const double mxM = q[VMX][iM], mxP = hs ? hs[hper + hi] : q[VMX][iP];
@@ -1539,13 +1543,13 @@ void* orc_create(const orc_desc* d) {
 
 void orc_destroy(void* h) { delete static_cast<Oracle*>(h); }
 
-// a slab of a domain decomposed along x: exterior x face layers recv0 (x-) and recv1 (x+), and the
-// exchange the step functions call before every tendency (after DPRES is formed)
-void orc_set_halo(void* h, const double* recv0, const double* recv1,
+// a part of a domain decomposed along x and/or y: the exterior face layers recv[4] (x-, x+, y-, y+;
+// NULL on the sides of a periodic direction), and the exchange the step functions call before every
+// tendency (after DPRES is formed)
+void orc_set_halo(void* h, const double* const* recv,
                   void (*cb)(void* user, int stage, const double* const* q, const double* dpres), void* user) {
   Oracle* o = static_cast<Oracle*>(h);
-  o->hx[0] = recv0;
-  o->hx[1] = recv1;
+  for (int s = 0; s < 4; ++s) o->hx[s] = recv[s];
   o->halo_cb = cb;
   o->halo_user = user;
 }

@@ -61,7 +61,7 @@ def _load():
     lib.orc_create.restype = ctypes.c_void_p
     lib.orc_create.argtypes = [ctypes.POINTER(OrcDesc)]
     lib.orc_destroy.argtypes = [ctypes.c_void_p]
-    lib.orc_set_halo.argtypes = [ctypes.c_void_p, _dp, _dp, HALO_CB, ctypes.c_void_p]
+    lib.orc_set_halo.argtypes = [ctypes.c_void_p, ctypes.POINTER(_dp), HALO_CB, ctypes.c_void_p]
     lib.orc_num_threads.restype = ctypes.c_int
     lib.orc_set_num_threads.argtypes = [ctypes.c_int]
     lib.orc_get_1d.argtypes = [ctypes.c_void_p] + [_dp] * 8
@@ -236,37 +236,48 @@ class Oracle:
                                        ctypes.byref(mi))
         return qs, int(nfail), float(mi.value)
 
-    # ---- slab of a domain decomposed along x (scale_meshfieldcomm_base.F90:340-470) ----
-    def halo_pack(self, q, dpres):
-        """The x face layers of this slab, [2 sides][6 fields][NeY*NeZ*N1*N1]: side 0 the nodes (0, a, b)
-        of the elements ex = 0, side 1 the nodes (N, a, b) of ex = NeX-1, in the order (ey + NeY ez,
-        a + N1 b); fields DDENS, MOMX, MOMY, MOMZ, DRHOT, DPRES (the library's buffer layout)."""
+    # ---- part of a domain decomposed along x and/or y (scale_meshfieldcomm_base.F90:340-470) ----
+    def halo_pack(self, q, dpres, sides=(0, 1)):
+        """The boundary face layers of this part, {side: [6 fields][boundary elements * N1*N1]} for the
+        halo sides (0 x-, 1 x+, 2 y-, 3 y+): side 0 the nodes (0, a, b) of the elements ex = 0, side 1
+        the nodes (N, a, b) of ex = NeX-1 (elements in the order ey + NeY ez), sides 2 and 3 the nodes
+        (a, 0, b) of ey = 0 and (a, N, b) of ey = NeY-1 (order ex + NeX ez); face node a + N1 b; fields
+        DDENS, MOMX, MOMY, MOMZ, DRHOT, DPRES (the library's buffer layout)."""
         N1 = self.N1
-        out = np.empty((2, 6, self.NeY * self.NeZ * N1 * N1))
-        for v, a in enumerate(list(q) + [dpres]):
-            x = np.asarray(a, np.float64).reshape(self.NeZ, self.NeY, self.NeX, N1, N1, N1)  # ez ey ex k j i
-            out[0, v] = x[:, :, 0, :, :, 0].reshape(-1)
-            out[1, v] = x[:, :, self.NeX - 1, :, :, N1 - 1].reshape(-1)
+        out = {}
+        fields = [np.asarray(a, np.float64).reshape(self.NeZ, self.NeY, self.NeX, N1, N1, N1)  # ez ey ex k j i
+                  for a in list(q) + [dpres]]
+        for sd in sides:
+            if sd < 2:
+                ex, i = (0, 0) if sd == 0 else (self.NeX - 1, N1 - 1)
+                out[sd] = np.stack([x[:, :, ex, :, :, i].reshape(-1) for x in fields])  # (ez, ey, b, a)
+            else:
+                ey, j = (0, 0) if sd == 2 else (self.NeY - 1, N1 - 1)
+                out[sd] = np.stack([x[:, ey, :, :, j, :].reshape(-1) for x in fields])  # (ez, ex, b, a)
         return out
 
-    def set_halo(self, exchange):
-        """Makes this oracle a slab: before every tendency of step_hevi/step_heve, exchange(stage, send,
-        recv) gets this slab's packed face layers (send, as halo_pack) and must fill recv[0] with the
-        x- neighbour's send[1] and recv[1] with the x+ neighbour's send[0], in place."""
+    def set_halo(self, exchange, sides=(0, 1)):
+        """Makes this oracle one part of a decomposed domain with halo exchanges on `sides`: before
+        every tendency of step_hevi/step_heve, exchange(stage, send, recv) gets the packed layers (send,
+        as halo_pack) and must fill recv[opposite side] of each neighbour's layer in place: recv[0] with
+        the x- neighbour's send[1], recv[1] with the x+ neighbour's send[0], recv[2] and recv[3] the
+        same in y."""
         n = self.Np * self.Ne
-        self._hrecv = np.zeros((2, 6, self.NeY * self.NeZ * self.N1 * self.N1))
+        Nfp = self.N1 * self.N1
+        self._hrecv = {sd: np.zeros((6, (self.NeY if sd < 2 else self.NeX) * self.NeZ * Nfp)) for sd in sides}
         self.halo_errors = []
 
         def cb(_user, stage, qpp, dpp):
             try:
                 q = [np.ctypeslib.as_array(qpp[v], shape=(n,)) for v in range(5)]
                 dp = np.ctypeslib.as_array(dpp, shape=(n,))
-                exchange(int(stage), self.halo_pack(q, dp), self._hrecv)
+                exchange(int(stage), self.halo_pack(q, dp, sides), self._hrecv)
             except Exception as e:  # a ctypes callback cannot raise into C
                 self.halo_errors.append(e)
 
         self._halo_cb = HALO_CB(cb)
-        self.lib.orc_set_halo(self._h, _ptr(self._hrecv[0]), _ptr(self._hrecv[1]), self._halo_cb, None)
+        self._hptrs = (_dp * 4)(*[_ptr(self._hrecv[sd]) if sd in self._hrecv else None for sd in range(4)])
+        self.lib.orc_set_halo(self._h, self._hptrs, self._halo_cb, None)
 
     # ---- tracer advection (trcadvect3d_heve.F90, driver_trcadv3d.F90) ----
     # Face-node arrays (alph_dens) have shape (Ne, 6, N1*N1): FElib's (NfpTot, Ne).
