@@ -332,6 +332,9 @@ void fedg_ctx_destroy(fedg_ctx* c) {
   cudaFree(c->nd_buf);
   cudaFree(c->sponge_coef);
   if (c->h_cnt) cudaFreeHost(c->h_cnt);
+  for (cudaEvent_t ev : c->chunk_ev)
+    if (ev) cudaEventDestroy(ev);
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -624,13 +627,13 @@ int fedg_tint_advance(fedg_tint* t, int stage, double* const q[5]) {
 // hout: device-mapped page-locked host arrays that the float-pair path's last stage kernel also
 // writes the result to (fedg_update_host), or NULL
 static int update_impl(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_opts* o, double* iters_out,
-                       double* const* hout) {
+                       double* const* hout, double* const* hin = nullptr) {
   if (!c || !q || !o) return fail("fedg_update: null argument");
   if (!c->base_set) return fail("fedg_update: base state not set");
   if (o->eqs != FEDG_HEVE && o->eqs != FEDG_HEVI) return fail("fedg_update: bad eqs");
   CK(cudaSetDevice(c->d.device));
   if (o->prec == FEDG_PREC_MIXED || o->prec == FEDG_PREC_PAIR) {
-    return mixed_update(c, q, nsteps, o, iters_out, hout);
+    return mixed_update(c, q, nsteps, o, iters_out, hout, hin);
   }
   if (o->prec != FEDG_PREC_FP64) return fail("fedg_update: bad prec");
   const int scheme = o->eqs == FEDG_HEVE ? FEDG_SSP_RK3 : FEDG_IMEX_ARK232;
@@ -741,12 +744,16 @@ int fedg_update_host(fedg_ctx* c, double* const host_q[5], int nsteps, const fed
     return fail("fedg_update_host: out of device memory");
   }
   double* dq[5];
-  for (int v = 0; v < 5; ++v) {
-    dq[v] = c->host_state + (size_t)v * c->n;
-    CK(cudaMemcpyAsync(dq[v], host_q[v], nb, cudaMemcpyHostToDevice, c->stream));
-  }
+  for (int v = 0; v < 5; ++v) dq[v] = c->host_state + (size_t)v * c->n;
   const bool direct = o->prec == FEDG_PREC_PAIR && nsteps > 0;
-  const int r = update_impl(c, dq, nsteps, o, iters_out, direct ? hd : nullptr);
+  // the float-pair HEVI path on a periodic mesh overlaps the H2D copies with its first stage, once the
+  // reference wind is fixed (the first call takes it from the state) and when no tracer-flux outputs
+  // read the state at the step's start
+  double wref[2];
+  const bool piped = direct && o->eqs == FEDG_HEVI && !fedg::slab(c) && fedg::ref_wind(c, wref) && !c->trc_flux[0];
+  if (!piped)
+    for (int v = 0; v < 5; ++v) CK(cudaMemcpyAsync(dq[v], host_q[v], nb, cudaMemcpyHostToDevice, c->stream));
+  const int r = update_impl(c, dq, nsteps, o, iters_out, direct ? hd : nullptr, piped ? host_q : nullptr);
   if (r < 0) return r;
   if (!direct)  // the FP64 and FP32 paths copy the result back after the step
     for (int v = 0; v < 5; ++v) CK(cudaMemcpyAsync(host_q[v], dq[v], nb, cudaMemcpyDeviceToHost, c->stream));

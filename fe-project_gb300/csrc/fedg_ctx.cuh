@@ -34,6 +34,8 @@ struct fedg_ctx {
   fedg_tint* upd_tint = nullptr;  // RK buffers of fedg_update, kept between calls
   MlpState* guess = nullptr;      // column-guess network attached with fedg_guess_load (not owned)
   double* host_state = nullptr;   // device copy of the state of fedg_update_host (5 Np*Ne doubles)
+  cudaStream_t copy_stream = nullptr;  // fedg_update_host's H2D copies, in z-ranges
+  cudaEvent_t chunk_ev[4] = {};        // one per z-range: the range has arrived
   double* trc_buf = nullptr;      // tracer update scratch: two stage fields, var0, varTmp, FCT per element
   double* nd_buf = nullptr;       // numerical-diffusion scratch: gradient (3 fields), Laplacian (2 fields)
   double* sponge_coef = nullptr;  // sponge-layer coefficient per level

@@ -753,9 +753,10 @@ static int mixed_setup(fedg_ctx* c) {
 
 // float-pair deviation copy of a state (DDENS, MOMX - DENS_hyd*Uref, MOMY - DENS_hyd*Vref, MOMZ, DRHOT)
 struct Dev5p { float2* v[5]; };
+// nodes [g0, n)
 __global__ void k_to_dev2(F5c q, Dev5p out, const double* __restrict__ dens_prof, float2 U, float2 V, int Np, int N1,
-                          size_t nxy, size_t n) {
-  const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+                          size_t nxy, size_t n, size_t g0 = 0) {
+  const size_t g = g0 + (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= n) return;
   const size_t ke = g / Np;
   const int ez = (int)(ke / nxy), k = (int)(g - ke * Np) / (N1 * N1);
@@ -975,8 +976,61 @@ static int pair_update_heve(fedg_ctx* c, double* const q[5], int nsteps, const f
   return 0;
 }
 
+// The first stage of a step whose state is still in page-locked host memory (fedg_update_host):
+// the H2D copies of the state go on the context's copy stream in kChunks ranges of element layers
+// (each a contiguous range of every field), each followed by an event; the context stream splits each
+// range into deviation pairs once it has arrived, and runs the stage-1 kernel on a range once the
+// range above it is split too (the kernel reads the face nodes of the layers below and above).
+template <class Stage1>
+static int pipelined_first_stage(fedg_ctx* c, MixedState* m, double* const q[5], double* const* hin, Stage1&& stage1) {
+  constexpr int kChunks = 4;
+  cudaError_t e;
+  if (!c->copy_stream) {
+    if ((e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking)) != cudaSuccess)
+      return api_cuda_fail(e, "fedg_update_host: copy stream");
+    for (int i = 0; i < kChunks; ++i)
+      if ((e = cudaEventCreateWithFlags(&c->chunk_ev[i], cudaEventDisableTiming)) != cudaSuccess)
+        return api_cuda_fail(e, "fedg_update_host: events");
+  }
+  const int NeZ = c->d.NeZ, nch = NeZ < kChunks ? NeZ : kChunks;
+  const size_t layer = c->nxy * (size_t)c->Np;  // nodes of one element layer
+  int zb[kChunks + 1];
+  for (int i = 0; i <= nch; ++i) zb[i] = (int)((long long)NeZ * i / nch);
+  // the copy stream must not start before the context stream's earlier work on q is done
+  if ((e = cudaEventRecord(c->chunk_ev[0], c->stream)) != cudaSuccess ||
+      (e = cudaStreamWaitEvent(c->copy_stream, c->chunk_ev[0], 0)) != cudaSuccess)
+    return api_cuda_fail(e, "fedg_update_host: stream order");
+  for (int i = 0; i < nch; ++i) {
+    const size_t off = (size_t)zb[i] * layer, cnt = (size_t)(zb[i + 1] - zb[i]) * layer;
+    for (int v = 0; v < 5; ++v)
+      if ((e = cudaMemcpyAsync(q[v] + off, hin[v] + off, sizeof(double) * cnt, cudaMemcpyHostToDevice,
+                               c->copy_stream)) != cudaSuccess)
+        return api_cuda_fail(e, "fedg_update_host: copy");
+    if ((e = cudaEventRecord(c->chunk_ev[i], c->copy_stream)) != cudaSuccess)
+      return api_cuda_fail(e, "fedg_update_host: event");
+  }
+  F5c qc{{q[0], q[1], q[2], q[3], q[4]}};
+  Dev5p dv{{m->QNFp(0), m->QNFp(1), m->QNFp(2), m->QNFp(3), m->QNFp(4)}};
+  const int nxy = (int)c->nxy;
+  for (int i = 0; i < nch; ++i) {
+    if ((e = cudaStreamWaitEvent(c->stream, c->chunk_ev[i], 0)) != cudaSuccess)
+      return api_cuda_fail(e, "fedg_update_host: wait");
+    const size_t g0 = (size_t)zb[i] * layer, g1 = (size_t)zb[i + 1] * layer;
+    int r = tracked(c, FEDG_K_AUX, [&] {
+      k_to_dev2<<<(unsigned)((g1 - g0 + 255) / 256), 256, 0, c->stream>>>(qc, dv, c->d_prof, m->opx.Uref, m->opx.Vref,
+                                                                         c->Np, c->N1, c->nxy, g1, g0);
+      return (int)cudaGetLastError();
+    });
+    if (r) return api_cuda_fail((cudaError_t)r, "fedg_update_host: deviation copy");
+    if (i > 0 && (r = stage1(zb[i - 1] * nxy, zb[i] * nxy)))  // the range below, now that this one is split
+      return api_cuda_fail((cudaError_t)r, "fedg_update_host: stage 1");
+  }
+  const int r = stage1(zb[nch - 1] * nxy, zb[nch] * nxy);
+  return r ? api_cuda_fail((cudaError_t)r, "fedg_update_host: stage 1") : 0;
+}
+
 int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_opts* o, double* iters_out,
-                 double* const* hout) {
+                 double* const* hout, double* const* hin) {
   if (o->eqs == FEDG_HEVE && o->prec == FEDG_PREC_PAIR) return pair_update_heve(c, q, nsteps, o, iters_out, hout);
   if (hout && o->prec != FEDG_PREC_PAIR) return api_fail("fedg_update_host: direct host output needs FEDG_PREC_PAIR");
   if (o->eqs != FEDG_HEVI)
@@ -1036,12 +1090,14 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
     for (int v = 0; v < 3; ++v) BP.a0[v] = m->a0buf + (size_t)v * c->n;
     F5c qc{{q[0], q[1], q[2], q[3], q[4]}};
     Dev5p dv{{m->QNFp(0), m->QNFp(1), m->QNFp(2), m->QNFp(3), m->QNFp(4)}};
-    r = tracked(c, FEDG_K_AUX, [&] {
-      k_to_dev2<<<(unsigned)((c->n + 255) / 256), 256, 0, c->stream>>>(qc, dv, c->d_prof, m->opx.Uref, m->opx.Vref,
-                                                                      c->Np, c->N1, c->nxy, c->n);
-      return (int)cudaGetLastError();
-    });
-    if (r) return api_cuda_fail((cudaError_t)r, "fedg_update(pair): deviation copy");
+    if (!hin) {  // with hin the deviation split runs range by range as the state arrives (below)
+      r = tracked(c, FEDG_K_AUX, [&] {
+        k_to_dev2<<<(unsigned)((c->n + 255) / 256), 256, 0, c->stream>>>(qc, dv, c->d_prof, m->opx.Uref, m->opx.Vref,
+                                                                        c->Np, c->N1, c->nxy, c->n);
+        return (int)cudaGetLastError();
+      });
+      if (r) return api_cuda_fail((cudaError_t)r, "fedg_update(pair): deviation copy");
+    }
   } else {  // FP32 deviation copy of the incoming state for the first stage-1 tendency
     F5c qc{{q[0], q[1], q[2], q[3], q[4]}};
     Dev5 dv{{m->QNF(0), m->QNF(1), m->QNF(2), m->QNF(3), m->QNF(4)}};
@@ -1112,7 +1168,17 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
     }
     // a slab exchanges the face layers of each stage state before its tendency (pair mode only)
     if (slab(c) && (r = halo_exchange_pair(c, BP.qs, 1))) return r;
-    if ((r = stage(1)) || (r = save(1))) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): stage 1");
+    if (step == 0 && hin) {
+      if ((r = pipelined_first_stage(c, m, q, hin, [&](int ke0, int ke1) {
+             return tracked(c, FEDG_K_MTEND, [&] {
+               return launch_stage_pair(c->N1, 1, m->opp, pfp, c->d_prof, BP, pc, ke1, filt, c->stream, ke0);
+             });
+           })))
+        return r;
+      if ((r = save(1))) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): stage 1");
+    } else if ((r = stage(1)) || (r = save(1))) {
+      return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): stage 1");
+    }
     if ((r = vi())) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): column solve 2");
     for (int v = 0; v < 5; ++v) {
       B.qsf[v] = m->QSF(v);

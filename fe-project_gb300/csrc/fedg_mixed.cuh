@@ -110,8 +110,9 @@ struct StagePairBufs {
 };
 int launch_stage_pair_heve(int N1, int stage, const OpsP& op, const ProfP& pf, const double* dens64,
                            const StagePairBufs& B, const PairCoef& cf, int Ne, int filt, cudaStream_t s);
+// elements [ke0, Ne) (ke0 > 0: one z-range of the mesh, for the pipelined first stage)
 int launch_stage_pair(int N1, int stage, const OpsP& op, const ProfP& pf, const double* dens64,
-                      const StagePairBufs& B, const PairCoef& cf, int Ne, int filt, cudaStream_t s);
+                      const StagePairBufs& B, const PairCoef& cf, int Ne, int filt, cudaStream_t s, int ke0 = 0);
 
 // Mixed-precision column solve (fedg_vicol.cu).  qin: stage input q* (float pairs); z: var0
 // (FP64; alph and the plain initial iterate); guess: FP32 increments of (DENS, MOMZ, RHOT) over
@@ -132,5 +133,8 @@ struct MixedState;
 void mixed_free(MixedState* m);
 // hout (optional): device-mapped page-locked host arrays that the last step's stage-3 kernel also
 // writes q^{n+1} to (fedg_update_host; float-pair paths only)
+// hin (optional, float-pair HEVI on a periodic mesh): page-locked host arrays holding the state; the
+// first step copies them into q in z-ranges on a second stream while the deviation split and the
+// stage-1 kernel run on the ranges that have arrived
 int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_opts* o, double* iters_out,
-                 double* const* hout = nullptr);
+                 double* const* hout = nullptr, double* const* hin = nullptr);

@@ -119,7 +119,7 @@ __device__ __forceinline__ void filter_store(const OpsP& op, float2* fa, float2*
 template <int N1, int EPB, int STAGE, bool HEVE = false>
 __global__ void __launch_bounds__(EPB* N1* N1* N1)
     k_stage_pair(const OpsP op, const ProfP pf, const double* __restrict__ dens64, const StagePairBufs B,
-                 const PairCoef cf, int Ne, int filter_on) {
+                 const PairCoef cf, int Ne, int filter_on, int ke0) {
   constexpr int Np = N1 * N1 * N1, NF = N1 * N1;
   extern __shared__ float2 smp[];
   float2* s_st = smp;                       // [EPB][6][Np]
@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
   float2* s_di = s_df + EPB * 5 * 6 * NF;   // [EPB][5][2NF]
   const int tid = threadIdx.x;
   const int le = tid / Np, p = tid - le * Np;
-  const int ke = blockIdx.x * EPB + le;
+  const int ke = ke0 + blockIdx.x * EPB + le;  // elements [ke0, Ne)
   const bool valid = ke < Ne;
   const int i = p % N1, j = (p / N1) % N1, k = p / NF;
   const int nxy = op.NeX * op.NeY;
@@ -459,12 +459,13 @@ constexpr int epb_p() { return N1 == 4 ? 4 : 1; }
 
 template <int N1, int STAGE, bool HEVE = false>
 int launch_pair_n(const OpsP& op, const ProfP& pf, const double* dens64, const StagePairBufs& B, const PairCoef& cf,
-                  int Ne, int filt, cudaStream_t s) {
+                  int Ne, int filt, cudaStream_t s, int ke0 = 0) {
   constexpr int EPB = epb_p<N1>(), Np = N1 * N1 * N1, NF = N1 * N1;
   const size_t smem = sizeof(float2) * EPB * (21 * Np + 5 * 6 * NF + 5 * 2 * NF);
   auto kfn = k_stage_pair<N1, EPB, STAGE, HEVE>;
   cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  kfn<<<(Ne + EPB - 1) / EPB, EPB * Np, smem, s>>>(op, pf, dens64, B, cf, Ne, filt);
+  if (Ne <= ke0) return (int)cudaSuccess;
+  kfn<<<(Ne - ke0 + EPB - 1) / EPB, EPB * Np, smem, s>>>(op, pf, dens64, B, cf, Ne, filt, ke0);
   return (int)cudaGetLastError();
 }
 
@@ -486,16 +487,16 @@ int launch_stage_pair_heve(int N1, int stage, const OpsP& op, const ProfP& pf, c
 }
 
 int launch_stage_pair(int N1, int stage, const OpsP& op, const ProfP& pf, const double* dens64,
-                      const StagePairBufs& B, const PairCoef& cf, int Ne, int filt, cudaStream_t s) {
+                      const StagePairBufs& B, const PairCoef& cf, int Ne, int filt, cudaStream_t s, int ke0) {
   if (N1 == 8) {
-    if (stage == 1) return launch_pair_n<8, 1>(op, pf, dens64, B, cf, Ne, filt, s);
-    if (stage == 2) return launch_pair_n<8, 2>(op, pf, dens64, B, cf, Ne, filt, s);
-    return launch_pair_n<8, 3>(op, pf, dens64, B, cf, Ne, filt, s);
+    if (stage == 1) return launch_pair_n<8, 1>(op, pf, dens64, B, cf, Ne, filt, s, ke0);
+    if (stage == 2) return launch_pair_n<8, 2>(op, pf, dens64, B, cf, Ne, filt, s, ke0);
+    return launch_pair_n<8, 3>(op, pf, dens64, B, cf, Ne, filt, s, ke0);
   }
   if (N1 == 4) {
-    if (stage == 1) return launch_pair_n<4, 1>(op, pf, dens64, B, cf, Ne, filt, s);
-    if (stage == 2) return launch_pair_n<4, 2>(op, pf, dens64, B, cf, Ne, filt, s);
-    return launch_pair_n<4, 3>(op, pf, dens64, B, cf, Ne, filt, s);
+    if (stage == 1) return launch_pair_n<4, 1>(op, pf, dens64, B, cf, Ne, filt, s, ke0);
+    if (stage == 2) return launch_pair_n<4, 2>(op, pf, dens64, B, cf, Ne, filt, s, ke0);
+    return launch_pair_n<4, 3>(op, pf, dens64, B, cf, Ne, filt, s, ke0);
   }
   return (int)cudaErrorInvalidValue;
 }

@@ -168,7 +168,10 @@ int fedg_update(fedg_ctx* ctx, double* const q[5], int nsteps, const fedg_update
  * context's device copy of the state (allocated on first use), nsteps steps are taken, and the result
  * is written back to host_q before the call returns.  With FEDG_PREC_PAIR the last stage kernel
  * stores the result into host_q through its device mapping while it runs, so the device-to-host
- * transfer overlaps its arithmetic; the other paths copy it back after the step. */
+ * transfer overlaps its arithmetic, and (HEVI on a periodic mesh, once the reference wind is fixed,
+ * without tracer-flux outputs) the host-to-device copies run in z-ranges on a second stream while
+ * the first stage works on the ranges that have arrived; the other paths copy the state in before
+ * and out after the step. */
 int fedg_update_host(fedg_ctx* ctx, double* const host_q[5], int nsteps, const fedg_update_opts* opts,
                      double* iters_out);
 
