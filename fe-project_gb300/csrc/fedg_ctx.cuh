@@ -90,6 +90,7 @@ bool slab(const fedg_ctx* c);  // true if either lateral direction exchanges a h
 bool halo_dir(const fedg_ctx* c, int side);  // side 0..3 (x-, x+, y-, y+) is a halo side
 int halo_exchange_fp64(fedg_ctx* c, const double* const q[5], const double* dpres, int stage);
 int halo_exchange_pair(fedg_ctx* c, const float2* const qs[5], int stage);
+int halo_exchange_f32(fedg_ctx* c, const float* const qs[5], int stage);  // FP32 stage state, value in .x
 // fedg_cal_tend_ex_noalloc's set-up (fedg_static.cu): looks up its static scratch array on device `dev`,
 // the current device, which loads the module holding it; called by fedg_ctx_create
 void noalloc_setup(int dev);

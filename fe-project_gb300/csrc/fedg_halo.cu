@@ -16,7 +16,8 @@
 // (MPI, NCCL or a peer copy: the library has no transport of its own); the stage kernels then read
 // the exterior values of the boundary faces from the receive buffers.  Sides 0..3 are x-, x+, y-,
 // y+; buffer layout per side: [6 fields][boundary elements][N1*N1 face nodes] of 8-byte values
-// (doubles in the FP64 path, float pairs of the deviations in the float-pair path), the boundary
+// (doubles in the FP64 path, float pairs of the deviations in the float-pair path, FP32 deviations
+// in .x in the FP32 mode), the boundary
 // elements numbered ey + NeY*ez on the x sides and ex + NeX*ez on the y sides, face node a + N1*b
 // being node (i, a, b) of the element on an x face and (a, j, b) on a y face.
 #include "fedg_ctx.cuh"
@@ -56,6 +57,7 @@ __device__ __forceinline__ bool halo_locate(const HaloGeom& hg, size_t t, int& s
 }
 
 struct Send4 { void* s[4]; };
+struct F5f { const float* v[5]; };
 
 __global__ void k_halo_pack_f64(const Ops op, const Prof pf, const HaloGeom hg, const F5c q,
                                 const double* __restrict__ dpres, Send4 out) {
@@ -86,6 +88,17 @@ __global__ void k_halo_pack_pair(const HaloGeom hg, const X5 qs, Send4 out) {
   const size_t per = hg.per(sd);
 #pragma unroll
   for (int v = 0; v < 5; ++v) o[(size_t)v * per + r] = __ldg(qs.v[v] + g);
+}
+
+// the same for the FP32 stage state of the FP32 mode: the value in .x of each 8-byte slot
+__global__ void k_halo_pack_f32(const HaloGeom hg, const F5f qs, Send4 out) {
+  int sd;
+  size_t r, g;
+  if (!halo_locate(hg, (size_t)blockIdx.x * blockDim.x + threadIdx.x, sd, r, g)) return;
+  float2* o = static_cast<float2*>(out.s[sd]);
+  const size_t per = hg.per(sd);
+#pragma unroll
+  for (int v = 0; v < 5; ++v) o[(size_t)v * per + r] = make_float2(__ldg(qs.v[v] + g), 0.f);
 }
 
 HaloGeom halo_geom(const fedg_ctx* c) {
@@ -139,6 +152,22 @@ int halo_exchange_pair(fedg_ctx* c, const float2* const qs[5], int stage) {
   const HaloGeom hg = halo_geom(c);
   int r = tracked(c, FEDG_K_AUX, [&] {
     k_halo_pack_pair<<<halo_blocks(hg), 256, 0, c->stream>>>(hg, x, send4(c));
+    return (int)cudaGetLastError();
+  });
+  if (r) return api_cuda_fail((cudaError_t)r, "fedg_update: halo pack");
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return api_cuda_fail(e, "fedg_update: halo pack");
+  if (c->hfn(c->huser, stage) != 0) return api_fail("fedg_update: the halo exchange function failed");
+  return 0;
+}
+
+int halo_exchange_f32(fedg_ctx* c, const float* const qs[5], int stage) {
+  if (!halo_ready(c) || !c->hfn)
+    return api_fail("fedg_update: a decomposed mesh (periodic_x/y = FEDG_HALO) needs its halo buffers and exchange (fedg_update_set_halo)");
+  const F5f x{{qs[0], qs[1], qs[2], qs[3], qs[4]}};
+  const HaloGeom hg = halo_geom(c);
+  int r = tracked(c, FEDG_K_AUX, [&] {
+    k_halo_pack_f32<<<halo_blocks(hg), 256, 0, c->stream>>>(hg, x, send4(c));
     return (int)cudaGetLastError();
   });
   if (r) return api_cuda_fail((cudaError_t)r, "fedg_update: halo pack");

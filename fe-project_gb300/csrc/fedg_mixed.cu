@@ -260,7 +260,15 @@ __global__ void __launch_bounds__(EPB* N1* N1* N1)
       const float ddM = st[VD * Np + pM], mxM = st[VMX * Np + pM], myM = st[VMY * Np + pM];
       const float mzM = st[VMZ * Np + pM], drM = st[VRT * Np + pM], dpM = st[5 * Np + pM];
       float ddP, mxP, myP, mzP, drP, dpP;
-      if (kn >= 0) {
+      // a boundary of a decomposed mesh: the exterior face layer comes from the halo exchange
+      const int hsd = halo_side(f, ex, ey, op.NeX, op.NeY);
+      const float2* hxs = hsd >= 0 ? op.hx[hsd] : nullptr;
+      if (hxs) {
+        const size_t per = halo_stride(hsd, op.NeX, op.NeY, op.NeZ, NF), h = halo_index(hsd, ex, ey, ez, ab, op.NeX, op.NeY, NF);
+        ddP = __ldg(hxs + h).x; mxP = __ldg(hxs + per + h).x; myP = __ldg(hxs + 2 * per + h).x;
+        mzP = __ldg(hxs + 3 * per + h).x; drP = __ldg(hxs + 4 * per + h).x;
+        dpP = dpres_f(drP, __ldg(pf.rtherm + levP), __ldg(pf.pres + levP), op.kap);
+      } else if (kn >= 0) {
         int i2, j2, k2;
         face_node<N1>(face_opp(f), a, b, i2, j2, k2);
         const size_t gP = (size_t)kn * Np + i2 + N1 * j2 + NF * k2;
@@ -1040,8 +1048,6 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
   if (r) return r;
   MixedState* m = c->mixed;
   const bool pair = o->prec == FEDG_PREC_PAIR;
-  if (!pair && slab(c))
-    return api_fail("fedg_update: the FP32 mode needs a periodic mesh; a part of a decomposed mesh (periodic_x/y = FEDG_HALO) runs FEDG_PREC_FP64 or FEDG_PREC_PAIR");
   if (pair && (r = pair_setup(c, m))) return r;
   if (o->use_guess && !mlp_ready(c->guess)) return api_fail("fedg_update: use_guess set but no trained column-guess network is loaded (fedg_guess_load)");
   const double alp = (3.0 + 2.0 * std::sqrt(2.0)) / 6.0, gam = 1.0 - 1.0 / std::sqrt(2.0), del = 1.0 / (2.0 * std::sqrt(2.0));
@@ -1067,7 +1073,10 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
   cf.Vref2 = m->opx.Vref;
   m->opp.Uref = m->opx.Uref;
   m->opp.Vref = m->opx.Vref;
-  for (int sd = 0; sd < 4; ++sd) m->opp.hx[sd] = halo_dir(c, sd) ? static_cast<const float2*>(c->hrecv[sd]) : nullptr;
+  for (int sd = 0; sd < 4; ++sd) {
+    m->opp.hx[sd] = halo_dir(c, sd) ? static_cast<const float2*>(c->hrecv[sd]) : nullptr;
+    m->opf.hx[sd] = m->opp.hx[sd];
+  }
   const double impl_fac = gam * o->dt;
   MixViArgs va{impl_fac, 1.0 / impl_fac, o->tol, 340.0, split_host(impl_fac), split_host(1.0 / impl_fac), o->max_iter, 1,
                c->vi_neumann};
@@ -1167,7 +1176,7 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
       BP.qs[v] = pair ? m->QNFp(v) : nullptr;
     }
     // a slab exchanges the face layers of each stage state before its tendency (pair mode only)
-    if (slab(c) && (r = halo_exchange_pair(c, BP.qs, 1))) return r;
+    if (slab(c) && (r = pair ? halo_exchange_pair(c, BP.qs, 1) : halo_exchange_f32(c, B.qsf, 1))) return r;
     if (step == 0 && hin) {
       if ((r = pipelined_first_stage(c, m, q, hin, [&](int ke0, int ke1) {
              return tracked(c, FEDG_K_MTEND, [&] {
@@ -1184,10 +1193,10 @@ int mixed_update(fedg_ctx* c, double* const q[5], int nsteps, const fedg_update_
       B.qsf[v] = m->QSF(v);
       BP.qs[v] = pair ? m->QSFp(v) : nullptr;
     }
-    if (slab(c) && (r = halo_exchange_pair(c, BP.qs, 2))) return r;
+    if (slab(c) && (r = pair ? halo_exchange_pair(c, BP.qs, 2) : halo_exchange_f32(c, B.qsf, 2))) return r;
     if ((r = stage(2)) || (r = save(2))) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): stage 2");
     if ((r = vi())) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): column solve 3");
-    if (slab(c) && (r = halo_exchange_pair(c, BP.qs, 3))) return r;
+    if (slab(c) && (r = pair ? halo_exchange_pair(c, BP.qs, 3) : halo_exchange_f32(c, B.qsf, 3))) return r;
     for (int v = 0; v < 5; ++v) BP.qh[v] = (hout && step == nsteps - 1) ? hout[v] : nullptr;
     if ((r = stage(3)) || (r = save(3))) return api_cuda_fail((cudaError_t)r, "fedg_update(mixed): stage 3");
   }

@@ -18,6 +18,9 @@ struct OpsF {
   float grav, kap, coriolis_f;
   float Uref, Vref;
   int NeX, NeY, NeZ, N1, Np, L;
+  // part of a decomposed domain: the x-, x+, y-, y+ exterior face layers of the FP32 stage state
+  // ([6][boundary elements][N1*N1] 8-byte slots, the value in .x); NULL where periodic
+  const float2* hx[4];
 };
 
 // column profiles of the base state in FP32, [L] each

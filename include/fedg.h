@@ -211,8 +211,9 @@ int fedg_update_set_wait_limit(fedg_ctx* ctx, int polls);
  * on an x face (i = 0 or N) and node (a, j, b) on a y face (j = 0 or N).  FEDG_PREC_FP64 exchanges
  * doubles; FEDG_PREC_PAIR exchanges float pairs (hi, lo) of the deviations from the hydrostatic
  * state and the reference wind and leaves the DPRES slot unused (the receiving side forms it from
- * DRHOT).  The FP32 mode (FEDG_PREC_MIXED), the tracer, numerical-diffusion and tracer-flux entry
- * points need a periodic mesh and refuse a decomposed one. */
+ * DRHOT); FEDG_PREC_MIXED exchanges its FP32 deviations in the first 4 bytes of each slot.  The
+ * tracer, numerical-diffusion and tracer-flux entry points need a periodic mesh and refuse a
+ * decomposed one. */
 enum { FEDG_HALO = 2 };
 /* bytes of the halo buffer of one side (0 for a side whose direction is periodic) */
 size_t fedg_halo_bytes(const fedg_ctx* ctx, int side);

@@ -1,5 +1,5 @@
 """Domain decomposition on one GPU: the library's face-layer packing and its halo reads in the FP64
-and float-pair stage kernels.  The part contexts of one domain (split along x, along y, or both)
+float-pair and FP32-mode stage kernels.  The part contexts of one domain (split along x, along y, or both)
 run their updates in host threads; their exchange function copies each part's packed layers into
 its neighbours' receive buffers (device copies, the threads meeting at a barrier: no kernel waits on
 another).  The result must equal the single-domain context bit for bit: every node's arithmetic is
@@ -98,13 +98,15 @@ def _slabs(fl, case, b, q, opts, nsteps, dims=(2, 1)):
 @pytest.mark.parametrize("eqs,prec,tol,dims", [("HEVI", "fp64", 1e-10, (2, 1)), ("HEVE", "fp64", 0.0, (2, 1)),
                                                ("HEVI", "pair", 1e-13, (2, 1)), ("HEVE", "pair", 0.0, (2, 1)),
                                                ("HEVI", "pair", 1e-13, (1, 2)), ("HEVI", "fp64", 1e-10, (2, 2)),
-                                               ("HEVI", "pair", 1e-13, (2, 2))])
+                                               ("HEVI", "pair", 1e-13, (2, 2)), ("HEVI", "fp32", 1e-10, (2, 1)),
+                                               ("HEVI", "fp32", 1e-10, (2, 2))])
 def test_parts_equal_one_domain(eqs, prec, tol, dims):
     from fedg import cases, lib as fl
 
     case = cases.C2().scaled(4, 4, 4)  # p = 7, the density current
     q, b = cases.initial_state(case)
-    opts = dict(eqs=fl.HEVI if eqs == "HEVI" else fl.HEVE, prec=fl.PREC_FP64 if prec == "fp64" else fl.PREC_PAIR,
+    precs = {"fp64": fl.PREC_FP64, "pair": fl.PREC_PAIR, "fp32": fl.PREC_MIXED}
+    opts = dict(eqs=fl.HEVI if eqs == "HEVI" else fl.HEVE, prec=precs[prec],
                 dt=0.04 if eqs == "HEVI" else 0.02, max_iter=30 if tol else 1, tol=tol)
     want = _full(fl, case, b, q, opts, 3)
     got = _slabs(fl, case, b, q, opts, 3, dims)
@@ -166,8 +168,6 @@ def test_slab_refusals():
     with pytest.raises(fl.FedgError, match="reference wind"):
         c.update(qd, 1, eqs=fl.HEVI, prec=fl.PREC_PAIR, dt=0.04, max_iter=30, tol=1e-13)
     c.set_ref_wind(*WIND)
-    with pytest.raises(fl.FedgError, match="FP32 mode"):
-        c.update(qd, 1, eqs=fl.HEVI, prec=fl.PREC_MIXED, dt=0.04, max_iter=30, tol=1e-10)
     with pytest.raises(fl.FedgError, match="decomposed"):
         c.numdiff_apply(qd, 1, 1.0, 1.0, 0.04)
 
