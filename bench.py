@@ -60,14 +60,14 @@ PATH_DTYPE = {"pair": "f32x2", "mixed": "f32+f32x2", "fp64": "f64"}
 # DRAM bytes per node of one launch of the dominant kernel, measured by ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum of one launch on the 32x32x16-element slice, 8,388,608 nodes), per path
 NCU_BYTES_PER_NODE = {
-    "pair": {"vi_mixed": (995.115776e6 + 647.497216e6) / (32 * 32 * 16 * 512)},
+    "pair": {"vi_mixed": (1109.730e6 + 657.106176e6) / (32 * 32 * 16 * 512)},
 }
 
 
 # warp instructions per node of one launch of the dominant kernel, measured by ncu
 # (smsp__inst_executed.sum of one launch on the 32x32x16-element slice), per path
 NCU_INST_PER_NODE = {
-    "pair": {"vi_mixed": 1.764025332e9 / (32 * 32 * 16 * 512)},
+    "pair": {"vi_mixed": 1.774784498e9 / (32 * 32 * 16 * 512)},
 }
 
 
