@@ -443,58 +443,58 @@ __global__ void __launch_bounds__(128) k_vi_fp64(const Ops op, const Prof pf, co
         if (qout.v[0]) { qout.v[VMX][g] = Qu[2 * l]; qout.v[VMY][g] = Qu[2 * l + 1]; }
       }
     } else {
-      for (int ez = 0; ez < NeZ; ++ez) {
-        double a[N1];
-        double rhs[3];
-        const bool act = lane < N1;
-        const int pv = act ? lane : 0;
+      // The element blocks are the identity plus the Lift face terms in columns 0 and N, coupled to
+      // the neighbours only through those, so the system reduces exactly to a scalar tridiagonal
+      // system in the interface jumps J_e = d(e, 0) - d(e-1, N), e = 1 .. NeZ-1 (J_0 = J_NeZ = 0 at the
+      // slip lids):  (1 + beta(e, 0) + tau(e-1, N)) J_e - beta(e-1, N) J_{e-1} - tau(e, 0) J_{e+1}
+      //            = b(e, 0) - b(e-1, N),  beta(e, p) = impl_fac Fz Lb[p] alB_e / 2, tau with Lt, alT,
+      // and then d(e, p) = b(e, p) - beta(e, p) J_e + tau(e, p) J_{e+1}: the same linear solve as the
+      // per-element LU of solve_Nnode8_uv (hevi_common_linalgebra.F90:2142-2294), in O(NeZ).
+      for (int l = lane; l < L; l += 32) {  // b = impl_fac A_uv(P) - P + q*
+        const int ez = l / N1, pv = l - ez * N1;
         const int lb = ez * N1, lt = ez * N1 + N;
         const int lbP = ez > 0 ? lb - 1 : lb, ltP = ez < NeZ - 1 ? lt + 1 : lt;
         const double dBx = tm * c.alB[ez] * (Pu[2 * lbP] - Pu[2 * lb]), dTx = tm * c.alT[ez] * (Pu[2 * ltP] - Pu[2 * lt]);
         const double dBy = tm * c.alB[ez] * (Pu[2 * lbP + 1] - Pu[2 * lb + 1]),
                      dTy = tm * c.alT[ez] * (Pu[2 * ltP + 1] - Pu[2 * lt + 1]);
-        const int l = ez * N1 + pv;
-        double bx = impl_fac * (-(op.Lb[pv] * dBx + op.Lt[pv] * dTx)) - Pu[2 * l] + Qu[2 * l];
-        double by = impl_fac * (-(op.Lb[pv] * dBy + op.Lt[pv] * dTy)) - Pu[2 * l + 1] + Qu[2 * l + 1];
-        const bool bcB = ez == 0, bcT = ez == NeZ - 1;
-        const double t1b = 0.5 * impl_fac * op.Lb[pv] * op.FSz * c.alB[ez];
-        const double t1t = 0.5 * impl_fac * op.Lt[pv] * op.FSz * c.alT[ez];
-#pragma unroll
-        for (int cc = 0; cc < N1; ++cc) a[cc] = (cc == pv) ? 1.0 : 0.0;
-        if (!bcB) a[0] += t1b;
-        if (!bcT) a[N] += t1t;
-        const double Lc = bcB ? 0.0 : -t1b;
-        const double Uc = bcT ? 0.0 : -t1t;
-        if (ez > 0) {
-          a[0] -= Lc * Gu[(ez - 1) * N1 + N];
-          bx -= Lc * bu[2 * ((ez - 1) * N1 + N)];
-          by -= Lc * bu[2 * ((ez - 1) * N1 + N) + 1];
-        }
-        rhs[0] = bx; rhs[1] = by; rhs[2] = bcT ? 0.0 : Uc;
-        if (!act) {
-#pragma unroll
-          for (int cc = 0; cc < N1; ++cc) a[cc] = 0.0;
-          rhs[0] = rhs[1] = rhs[2] = 0.0;
-        }
-        __syncwarp();
-        int mypiv;
-        warp_lu<N1, 3>(a, rhs, c.prow, c.plane, lane, mypiv);
-        if (mypiv >= 0) {
-          bu[2 * (ez * N1 + mypiv)] = rhs[0];
-          bu[2 * (ez * N1 + mypiv) + 1] = rhs[1];
-          Gu[ez * N1 + mypiv] = rhs[2];
-        }
-        __syncwarp();
+        bu[2 * l] = impl_fac * (-(op.Lb[pv] * dBx + op.Lt[pv] * dTx)) - Pu[2 * l] + Qu[2 * l];
+        bu[2 * l + 1] = impl_fac * (-(op.Lb[pv] * dBy + op.Lt[pv] * dTy)) - Pu[2 * l + 1] + Qu[2 * l + 1];
       }
-      for (int ez = NeZ - 2; ez >= 0; --ez) {
-        if (lane < N1) {
-          const int l = ez * N1 + lane;
-          const double gg = Gu[l];
-          bu[2 * l] -= gg * bu[2 * ((ez + 1) * N1)];
-          bu[2 * l + 1] -= gg * bu[2 * ((ez + 1) * N1) + 1];
+      __syncwarp();
+      const double cfs = 0.5 * impl_fac * op.FSz;
+      double* J = Gu;  // [2][NeZ + 1]: the jumps of MOMX and MOMY
+      if (lane < 2) {  // one Thomas sweep per momentum component
+        const int m = lane;
+        double* Jm = J + m * (NeZ + 1);
+        double cprev = 0.0, rprev = 0.0;
+        Jm[0] = 0.0;
+        Jm[NeZ] = 0.0;
+        for (int e = 1; e < NeZ; ++e) {
+          const double aa = e >= 2 ? -cfs * op.Lb[N] * c.alB[e - 1] : 0.0;
+          const double dd = 1.0 + cfs * op.Lb[0] * c.alB[e] + cfs * op.Lt[N] * c.alT[e - 1];
+          const double cc = e < NeZ - 1 ? -cfs * op.Lt[0] * c.alT[e] : 0.0;
+          const double ip = 1.0 / (dd - aa * cprev);
+          const double rr = bu[2 * (e * N1) + m] - bu[2 * ((e - 1) * N1 + N) + m];
+          cprev = cc * ip;
+          rprev = (rr - aa * rprev) * ip;
+          Jm[e] = rprev;
+          // forward coefficients kept in the jump slots' neighbours: store c' beside J
+          Gu[2 * (NeZ + 1) + m * (NeZ + 1) + e] = cprev;
         }
-        __syncwarp();
+        for (int e = NeZ - 2; e >= 1; --e) Jm[e] -= Gu[2 * (NeZ + 1) + m * (NeZ + 1) + e] * Jm[e + 1];
       }
+      __syncwarp();
+      for (int l = lane; l < L; l += 32) {
+        const int ez = l / N1, pv = l - ez * N1;
+        const double beta = ez > 0 ? cfs * op.Lb[pv] * c.alB[ez] : 0.0;
+        const double tau = ez < NeZ - 1 ? cfs * op.Lt[pv] * c.alT[ez] : 0.0;
+#pragma unroll
+        for (int m = 0; m < 2; ++m) {
+          const double* Jm = J + m * (NeZ + 1);
+          bu[2 * l + m] = bu[2 * l + m] - beta * Jm[ez] + tau * Jm[ez + 1];
+        }
+      }
+      __syncwarp();
       for (int l = lane; l < L; l += 32) {
         const double px = Pu[2 * l] + bu[2 * l], py = Pu[2 * l + 1] + bu[2 * l + 1];
         const size_t g = gidx(l);
