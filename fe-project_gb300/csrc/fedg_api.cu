@@ -327,6 +327,7 @@ void fedg_ctx_destroy(fedg_ctx* c) {
   cudaFree(c->d_status);
   cudaFree(c->d_cnt);
   cudaFree(c->work);
+  cudaFree(c->vi_gsc);
   cudaFree(c->host_state);
   cudaFree(c->trc_buf);
   cudaFree(c->nd_buf);
@@ -404,6 +405,20 @@ int fedg_drhot2pres(fedg_ctx* c, const double* DRHOT, double* PRES, double* DPRE
   return 0;
 }
 
+// the FP64 column solve's block-Thomas scratch (sized by its launch plan for this mesh)
+static double* vi_scratch(fedg_ctx* c, size_t* ndouble) {
+  const size_t need = vi_fp64_scratch_doubles(c->op);
+  *ndouble = need;
+  if (need == 0) return nullptr;
+  if (c->vi_gsc_doubles >= need) return c->vi_gsc;
+  cudaFree(c->vi_gsc);
+  c->vi_gsc = nullptr;
+  c->vi_gsc_doubles = 0;
+  if (cudaMalloc(&c->vi_gsc, sizeof(double) * need) != cudaSuccess) return nullptr;
+  c->vi_gsc_doubles = need;
+  return c->vi_gsc;
+}
+
 static double* ensure_work(fedg_ctx* c, size_t ndouble) {
   if (c->work_doubles >= ndouble) return c->work;
   cudaFree(c->work);
@@ -476,7 +491,12 @@ int fedg_cal_vi(fedg_ctx* c, const double* const in[12], double impl_fac, double
   F5 qo{{nullptr, nullptr, nullptr, nullptr, nullptr}};
   ViArgs a{impl_fac, dt, tol, max_iter, 340.0};
   int* st = col_status ? col_status : c->d_status;
-  CK((cudaError_t)tracked(c, FEDG_K_VI, [&] { return launch_vi_fp64(c->op, c->prof(), q, z, none, qo, t, st, a, c->stream); }));
+  size_t ngsc = 0;
+  double* gsc = vi_scratch(c, &ngsc);
+  if (!gsc) return fail(ngsc ? "fedg_cal_vi: out of device memory" : "fedg_cal_vi: the column does not fit in shared memory");
+  CK((cudaError_t)tracked(c, FEDG_K_VI, [&] {
+    return launch_vi_fp64(c->op, c->prof(), q, z, none, qo, t, st, a, gsc, ngsc, c->stream);
+  }));
   if (st != c->d_status) CK(cudaMemcpyAsync(c->d_status, st, sizeof(int) * c->ncol, cudaMemcpyDeviceToDevice, c->stream));
   return count_status(c, nullptr, nullptr);
 }
@@ -649,6 +669,10 @@ static int update_impl(fedg_ctx* c, double* const q[5], int nsteps, const fedg_u
   fedg_tint* t = c->upd_tint;
   double* dp = ensure_work(c, c->n);
   if (!dp) return fail("fedg_update: out of device memory");
+  size_t ngsc = 0;
+  double* gsc = nullptr;
+  if (o->eqs == FEDG_HEVI && !(gsc = vi_scratch(c, &ngsc)))
+    return fail(ngsc ? "fedg_update: out of device memory" : "fedg_update: the column does not fit in shared memory");
   const double* base[16] = {};
   long long nsum = 0, ncnt = 0;
   int nfail = 0;
@@ -669,7 +693,9 @@ static int update_impl(fedg_ctx* c, double* const q[5], int nsteps, const fedg_u
         // stage 1: var0 is the state itself (StoreImplicit copies it at stage 1)
         if (s == 1) z = qc;
         ViArgs a{fac, o->dt, o->tol, o->max_iter, 340.0};
-        r = tracked(c, FEDG_K_VI, [&] { return launch_vi_fp64(c->op, c->prof(), qc, z, none, qo, tim, c->d_status, a, c->stream); });
+        r = tracked(c, FEDG_K_VI, [&] {
+          return launch_vi_fp64(c->op, c->prof(), qc, z, none, qo, tim, c->d_status, a, gsc, ngsc, c->stream);
+        });
         if (r) return cuda_fail((cudaError_t)r, "fedg_update: cal_vi");
         if (fac != 0.0) {
           const int nb = count_status(c, &nsum, &ncnt);

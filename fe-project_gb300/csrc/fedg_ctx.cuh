@@ -30,6 +30,8 @@ struct fedg_ctx {
   // fused-update scratch
   double* work = nullptr;
   size_t work_doubles = 0;
+  double* vi_gsc = nullptr;  // block-Thomas scratch of the FP64 column solve
+  size_t vi_gsc_doubles = 0;
   MixedState* mixed = nullptr;
   fedg_tint* upd_tint = nullptr;  // RK buffers of fedg_update, kept between calls
   MlpState* guess = nullptr;      // column-guess network attached with fedg_guess_load (not owned)

@@ -29,8 +29,10 @@ int launch_drhot2pres(const Ops& op, const Prof& pf, const double* drhot, double
 // state alph is frozen at).  qout (may be NULL): new state; tout (may be NULL): tendency
 // (qout - qin)/impl_fac, or A(z) when impl_fac == 0.  status[ncol]: solves used, -1 not
 // converged, -2 non-finite.  guess (may be NULL): initial Newton iterate of the var3 part
-// (DDENS, MOMZ, DRHOT), overriding z for the iterate but not for alph.
+// (DDENS, MOMZ, DRHOT), overriding z for the iterate but not for alph.  gsc: block-Thomas scratch of
+// at least vi_fp64_scratch_doubles(op) doubles (0 when the column does not fit in shared memory).
+size_t vi_fp64_scratch_doubles(const Ops& op);
 int launch_vi_fp64(const Ops& op, const Prof& pf, const F5c& qin, const F5c& z, const F5c& guess, const F5& qout,
-                   const F5& tout, int* status, const ViArgs& a, cudaStream_t s);
+                   const F5& tout, int* status, const ViArgs& a, double* gsc, size_t gsc_doubles, cudaStream_t s);
 
 }  // namespace fedg

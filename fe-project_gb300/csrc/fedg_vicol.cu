@@ -1087,7 +1087,9 @@ int launch_n(const Ops& op, const OpsX& ox, const ProfX& px, const X5& qin, cons
   if (smem > 227 * 1024) return (int)cudaErrorInvalidValue;
   const int ncol = op.NeX * op.NeY * N1 * N1;
   auto kfn = k_vi_cols<N1, PO>;
-  cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  // the limit is raised to 227 KB, the same value from every caller: contexts of different column
+  // heights launching from several host threads never lower it under one another's launch
+  cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
   kfn<<<(ncol + 2 * C - 1) / (2 * C), 64, smem, s>>>(op, ox, px, qin, z, a0, guess, qsf, tout, gsc, status, cnt, a,
                                                      ncol);
   return (int)cudaGetLastError();
