@@ -58,16 +58,17 @@ def fp64_vi_flops_per_node(N1):
     return (2 * n ** 3 / 3 + 4 * 2 * n * n) / N1 + (2 * N1 ** 3 / 3 + 3 * 2 * N1 * N1) / N1 + 2 * 100
 PATH_DTYPE = {"pair": "f32x2", "mixed": "f32+f32x2", "fp64": "f64"}
 # DRAM bytes per node of one launch of the dominant kernel, measured by ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum of one launch on the 32x32x16-element slice, 8,388,608 nodes), per path
+# dram__bytes_write.sum on the 32x32x16-element slice, 8,388,608 nodes; the mean of the step's two
+# launches, one per implicit stage), per path
 NCU_BYTES_PER_NODE = {
-    "pair": {"vi_mixed": (1109.730e6 + 657.106176e6) / (32 * 32 * 16 * 512)},
+    "pair": {"vi_mixed": ((1063.248640e6 + 620.473856e6) + (995.027968e6 + 616.375808e6)) / 2 / (32 * 32 * 16 * 512)},
 }
 
 
 # warp instructions per node of one launch of the dominant kernel, measured by ncu
-# (smsp__inst_executed.sum of one launch on the 32x32x16-element slice), per path
+# (smsp__inst_executed.sum on the 32x32x16-element slice, the mean of the step's two launches), per path
 NCU_INST_PER_NODE = {
-    "pair": {"vi_mixed": 1.774784498e9 / (32 * 32 * 16 * 512)},
+    "pair": {"vi_mixed": (1.773631250e9 + 1.717718819e9) / 2 / (32 * 32 * 16 * 512)},
 }
 
 

@@ -83,6 +83,33 @@ struct Col {
   __device__ float alT(int e) const { return al[2 * e + 1]; }
 };
 
+// L2 eviction priority of the data the kernel reads or writes exactly once (var0, the stage
+// kernel's A(var0), the last read of q*, the outputs): evict-first.  What a column reads again
+// while the other columns stream past it (q* in every certifying residual, the block-Thomas
+// history) then keeps its lines in L2 instead of going back to DRAM.
+__device__ __forceinline__ unsigned long long l2_evict_first() {
+  unsigned long long p;
+  asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ double ld_once(const double* a, unsigned long long pol) {
+  double v;
+  asm("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(a), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ float2 ld_once(const float2* a, unsigned long long pol) {
+  float2 v;
+  asm("ld.global.nc.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(v.x), "=f"(v.y) : "l"(a), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ void st_once(float2* a, float2 v, unsigned long long pol) {
+  asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(a), "f"(v.x), "f"(v.y), "l"(pol)
+               : "memory");
+}
+__device__ __forceinline__ void st_once(float* a, float v, unsigned long long pol) {
+  asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(a), "f"(v), "l"(pol) : "memory");
+}
+
 __device__ __forceinline__ float grp_max_nan(float e, int width) {
   for (int o = width / 2; o > 0; o >>= 1) {
     const float oe = __shfl_xor_sync(FULL, e, o);
@@ -292,6 +319,7 @@ __device__ void col_start(const ProfX& px, float kapf, const Col<N1>& c, const F
   const int gv[3] = {VD, VMZ, VRT};
   const bool res = a0.v[0] != nullptr, useq = res || guess;
   const f2 impl = f2_of(impl2);
+  const unsigned long long once = l2_evict_first();
   double zc[3];
   float2 qc[3] = {}, ac[3] = {};
   float gc[3] = {};
@@ -299,9 +327,9 @@ __device__ void col_start(const ProfX& px, float kapf, const Col<N1>& c, const F
     const size_t g0 = c.g(0);
 #pragma unroll
     for (int v = 0; v < 3; ++v) {
-      zc[v] = __ldg(z.v[gv[v]] + g0);
+      zc[v] = ld_once(z.v[gv[v]] + g0, once);
       if (useq) qc[v] = __ldg(qin.v[gv[v]] + g0);
-      if (res) ac[v] = __ldg(a0.v[v] + g0);
+      if (res) ac[v] = ld_once(a0.v[v] + g0, once);
       if (guess) gc[v] = __ldg(guess[v] + g0);
     }
   }
@@ -314,9 +342,9 @@ __device__ void col_start(const ProfX& px, float kapf, const Col<N1>& c, const F
     float gnx[3] = {};
 #pragma unroll
     for (int v = 0; v < 3; ++v) {
-      zn[v] = __ldg(z.v[gv[v]] + gn);
+      zn[v] = ld_once(z.v[gv[v]] + gn, once);
       if (useq) qn[v] = __ldg(qin.v[gv[v]] + gn);
-      if (res) an[v] = __ldg(a0.v[v] + gn);
+      if (res) an[v] = ld_once(a0.v[v] + gn, once);
       if (guess) gnx[v] = __ldg(guess[v] + gn);
     }
     const float dd0 = f2_split(zc[0]).h, dr0 = f2_split(zc[2]).h;
@@ -896,9 +924,10 @@ __global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, 
     else col_neumann<N1>(op, px, kapf, c, args.impl_fac, args.neumann, active);
     ++nsolve;
   }
+  const unsigned long long once = l2_evict_first();
   float2 qo[3];
 #pragma unroll
-  for (int m = 0; m < 3; ++m) qo[m] = __ldg(qin.v[gv[m]] + c.g(0));
+  for (int m = 0; m < 3; ++m) qo[m] = ld_once(qin.v[gv[m]] + c.g(0), once);
   for (int e = 0; e < NeZ; ++e) {
     const int l = e * N1 + k;
     const size_t gi = c.g(e);
@@ -906,18 +935,18 @@ __global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, 
     {
       const size_t gn = c.g(e + 1 < NeZ ? e + 1 : e);
 #pragma unroll
-      for (int m = 0; m < 3; ++m) qo[m] = __ldg(qin.v[gv[m]] + gn);
+      for (int m = 0; m < 3; ++m) qo[m] = ld_once(qin.v[gv[m]] + gn, once);
     }
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
       const f2 pnew = f2_of(c.P[3 * l + m]);
       const f2 inc = f2_sub(pnew, f2_of(qc[m]));
       if constexpr (PO) {
-        static_cast<float2*>(qsf[gv[m]])[gi] = f2_pack(pnew);
-        static_cast<float2*>(tout[gv[m]])[gi] = f2_pack(f2_mul(inc, f2_of(args.inv_impl2)));
+        st_once(static_cast<float2*>(qsf[gv[m]]) + gi, f2_pack(pnew), once);
+        st_once(static_cast<float2*>(tout[gv[m]]) + gi, f2_pack(f2_mul(inc, f2_of(args.inv_impl2))), once);
       } else {
-        static_cast<float*>(qsf[gv[m]])[gi] = f2_to_f(pnew);
-        static_cast<float*>(tout[gv[m]])[gi] = f2_to_f(inc) * iif;
+        st_once(static_cast<float*>(qsf[gv[m]]) + gi, f2_to_f(pnew), once);
+        st_once(static_cast<float*>(tout[gv[m]]) + gi, f2_to_f(inc) * iif, once);
       }
     }
   }
@@ -934,13 +963,13 @@ __global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, 
     // E = var0 - q* at every node; the bottom/top jumps (neighbour - own) of q* MOMX/MOMY from the
     // face nodes' values, passed between lanes by shuffles: jq[4e + m] = q*(e-1, N) - q*(e, 0),
     // jq[4e + 2 + m] = q*(e+1, 0) - q*(e, N), zero at the lids
-    double zu[2] = {__ldg(z.v[VMX] + c.g(0)), __ldg(z.v[VMY] + c.g(0))};
+    double zu[2] = {ld_once(z.v[VMX] + c.g(0), once), ld_once(z.v[VMY] + c.g(0), once)};
     float2 qu[2] = {__ldg(qin.v[VMX] + c.g(0)), __ldg(qin.v[VMY] + c.g(0))};
     f2 qtop[2] = {Z2F, Z2F};  // q*(e-1, N)
     for (int e = 0; e < NeZ; ++e) {
       const int l = e * N1 + k;
       const size_t gn = c.g(e + 1 < NeZ ? e + 1 : e);
-      const double zn[2] = {__ldg(z.v[VMX] + gn), __ldg(z.v[VMY] + gn)};
+      const double zn[2] = {ld_once(z.v[VMX] + gn, once), ld_once(z.v[VMY] + gn, once)};
       const float2 qnx[2] = {__ldg(qin.v[VMX] + gn), __ldg(qin.v[VMY] + gn)};
 #pragma unroll
       for (int m = 0; m < 2; ++m) {
@@ -1035,15 +1064,15 @@ __global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, 
       active = need;
       __syncwarp();
     }
-    float2 qo[2] = {__ldg(qin.v[VMX] + c.g(0)), __ldg(qin.v[VMY] + c.g(0))};
+    float2 qo[2] = {ld_once(qin.v[VMX] + c.g(0), once), ld_once(qin.v[VMY] + c.g(0), once)};
     for (int e = 0; e < NeZ; ++e) {
       const int l = e * N1 + k;
       const size_t gi = c.g(e);
       const float2 qc[2] = {qo[0], qo[1]};
       {
         const size_t gn = c.g(e + 1 < NeZ ? e + 1 : e);
-        qo[0] = __ldg(qin.v[VMX] + gn);
-        qo[1] = __ldg(qin.v[VMY] + gn);
+        qo[0] = ld_once(qin.v[VMX] + gn, once);
+        qo[1] = ld_once(qin.v[VMY] + gn, once);
       }
       const f2 dh = f2_of(__ldg(px.dh + l));
 #pragma unroll
@@ -1052,11 +1081,11 @@ __global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, 
         const f2 inc = f2_of(E[2 * l + m]);  // P - q*
         const f2 pdev = f2_add(f2_sub(f2_of(qc[m]), ref), inc);
         if constexpr (PO) {
-          static_cast<float2*>(qsf[VMX + m])[gi] = f2_pack(pdev);
-          static_cast<float2*>(tout[VMX + m])[gi] = f2_pack(f2_mul(inc, f2_of(args.inv_impl2)));
+          st_once(static_cast<float2*>(qsf[VMX + m]) + gi, f2_pack(pdev), once);
+          st_once(static_cast<float2*>(tout[VMX + m]) + gi, f2_pack(f2_mul(inc, f2_of(args.inv_impl2))), once);
         } else {
-          static_cast<float*>(qsf[VMX + m])[gi] = f2_to_f(pdev);
-          static_cast<float*>(tout[VMX + m])[gi] = f2_to_f(inc) * iif;
+          st_once(static_cast<float*>(qsf[VMX + m]) + gi, f2_to_f(pdev), once);
+          st_once(static_cast<float*>(tout[VMX + m]) + gi, f2_to_f(inc) * iif, once);
         }
       }
     }
