@@ -33,7 +33,8 @@ EXPORTED = [
     "fedg_guess_set_params", "fedg_guess_get_params", "fedg_guess_train_step", "fedg_guess_loss_grad",
     "fedg_guess_predict", "fedg_guess_load", "fedg_cal_tend_ex_noalloc",
     "fedg_trc_alphdens_advtest", "fedg_trc_save_massflux", "fedg_trc_fct_coef", "fedg_trc_cal_tend",
-    "fedg_trc_tmar", "fedg_trc_modalfilter", "fedg_trc_update", "fedg_numdiff_apply", "fedg_sponge_add_tend",
+    "fedg_trc_tmar", "fedg_trc_modalfilter", "fedg_trc_update", "fedg_trc_negative_fixer", "fedg_numdiff_apply",
+    "fedg_sponge_add_tend",
     "fedg_update_set_tracer_flux", "fedg_update_set_sponge", "fedg_numdiff_apply_prec",
     "fedg_guess_set_wait_limit", "fedg_update_set_vi_neumann", "fedg_update_set_wait_limit",
     "fedg_restart_write", "fedg_restart_read",
@@ -151,6 +152,9 @@ def load():
     lib.fedg_trc_fct_coef.argtypes = [_vp, _vp, _P3, _vp, _vp, _vp, _vp, _vp, ctypes.c_double, ctypes.c_double, _vp]
     lib.fedg_trc_cal_tend.argtypes = [_vp, _vp, _P3, _vp, _vp, _vp, _vp, _vp]
     lib.fedg_trc_tmar.argtypes = [_vp, _vp, _vp]
+    _dp = ctypes.POINTER(ctypes.c_double)
+    lib.fedg_trc_negative_fixer.argtypes = [_vp, ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_int, _dp, _dp, _dp, _dp] + [_vp] * 8 + [ctypes.c_double]
     lib.fedg_trc_modalfilter.argtypes = [_vp, _vp, _vp, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                          ctypes.c_double, ctypes.c_double, ctypes.c_int]
     lib.fedg_trc_update.argtypes = [_vp, _vp, _P3, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.POINTER(TrcOpts)]
@@ -437,6 +441,20 @@ class Context:
         _check(self.lib.fedg_trc_tmar(self.h, _ptr(Q), _ptr(ddens)), "fedg_trc_tmar")
         self.sync()
         return Q
+
+    def trc_negative_fixer(self, qtrc, qla, qia, mass, r, cv, cp, ddens, pres, cvtot, cptot, rtot, dens_hyd,
+                           pres_hyd, drhot=None, dt=0.0):
+        """fedg_trc_negative_fixer in place on the device tensors qtrc (list of QA), ddens, pres, cvtot,
+        cptot, rtot and drhot (or None); mass/r/cv/cp: the QA tracer property values"""
+        qa = len(qtrc)
+        qp = (ctypes.c_void_p * qa)(*[t.data_ptr() for t in qtrc])
+        tab = [(ctypes.c_double * qa)(*[float(x) for x in a]) for a in (mass, r, cv, cp)]
+        self.torch.cuda.synchronize()
+        _check(self.lib.fedg_trc_negative_fixer(self.h, qp, qa, int(qla), int(qia), *tab, _ptr(ddens), _ptr(pres),
+                                                _ptr(cvtot), _ptr(cptot), _ptr(rtot), _ptr(dens_hyd),
+                                                _ptr(pres_hyd), _ptr(drhot), float(dt)),
+               "fedg_trc_negative_fixer")
+        self.sync()
 
     def trc_modalfilter(self, Q, ddens, etac_h=2.0 / 3.0, alpha_h=36.0, ord_h=16, etac_v=2.0 / 3.0, alpha_v=36.0,
                         ord_v=16):

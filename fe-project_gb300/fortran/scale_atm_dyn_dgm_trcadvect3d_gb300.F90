@@ -3,7 +3,9 @@
 !!
 !! ISO_C_BINDING shim with the argument lists of FElib's tracer-advection routines
 !! (FElib/src/fluid_dyn_solver/scale_atm_dyn_dgm_trcadvect3d_heve.F90: calc_fct_coef :234-306,
-!! cal_tend :149-231, TMAR :311-340, save_massflux :343-401), calling the GB300 library libfedg.so
+!! cal_tend :149-231, TMAR :311-340, save_massflux :343-401) and of the negative fixer the tracer
+!! driver runs after its step (FElib/src/microphysics/scale_atm_phy_mp_dgm_common.F90:429-556, called
+!! from fix_negative_val, ..._driver_trcadv3d.F90:596-651), calling the GB300 library libfedg.so
 !! (C ABI: include/fedg.h) on the driver's OpenACC-resident fields.  It shares the library context
 !! of scale_atm_dyn_dgm_nonhydro3d_gb300 (create that one first).  Not compiled in this repository
 !! (no Fortran compiler in its build image); built with the model by a maintainer, linked with -lfedg.
@@ -26,6 +28,7 @@ module scale_atm_dyn_dgm_trcadvect3d_gb300
   public :: atm_dyn_dgm_trcadvect3d_gb300_cal_tend
   public :: atm_dyn_dgm_trcadvect3d_gb300_TMAR
   public :: atm_dyn_dgm_trcadvect3d_gb300_save_massflux
+  public :: atm_phy_mp_dgm_common_gb300_negative_fixer
 
   interface
     integer(c_int) function fedg_trc_fct_coef(ctx, qtrc, mflx, rhoq_tp, alph_m, alph_p, ddens, ddens0, &
@@ -52,6 +55,15 @@ module scale_atm_dyn_dgm_trcadvect3d_gb300
       integer(c_int), value :: rkstage, is_hevi
       type(c_ptr), intent(in) :: q(5), mflx(3)
       real(c_double), value :: w_h, w_v
+    end function
+    integer(c_int) function fedg_trc_negative_fixer(ctx, qtrc, qa, qla, qia, mass, r, cv, cp, ddens, pres, &
+        cvtot, cptot, rtot, dens_hyd, pres_hyd, drhot, dt) bind(C, name="fedg_trc_negative_fixer")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx, ddens, pres, cvtot, cptot, rtot, dens_hyd, pres_hyd, drhot
+      type(c_ptr), intent(in) :: qtrc(*)
+      integer(c_int), value :: qa, qla, qia
+      real(c_double), intent(in) :: mass(*), r(*), cv(*), cp(*)
+      real(c_double), value :: dt
     end function
     integer(c_int) function fedg_synchronize(ctx) bind(C, name="fedg_synchronize")
       import :: c_int, c_ptr
@@ -168,5 +180,45 @@ contains
     if (ierr < 0) call PRC_abort
     ierr = fedg_synchronize( atm_dyn_dgm_nonhydro3d_gb300_ctx() )
   end subroutine atm_dyn_dgm_trcadvect3d_gb300_save_massflux
+
+  !> atm_phy_mp_dgm_common_negative_fixer with FElib's argument list (the tracer properties are
+  !! scale_tracer's; QA must equal 1 + QLA + QIA, the case in which FElib's routine defines every
+  !! tracer's result)
+  subroutine atm_phy_mp_dgm_common_gb300_negative_fixer( &
+    QTRC, DDENS, PRES, CVtot, CPtot, Rtot, DENS_hyd, PRES_hyd, &
+    dt, lmesh, elem, QA, QLA, QIA, DRHOT )
+    use openacc, only: acc_deviceptr
+    use scale_tracer, only: TRACER_MASS, TRACER_R, TRACER_CV, TRACER_CP
+    use scale_localmeshfield_base, only: LocalMeshFieldBaseList
+    class(LocalMesh3D), intent(in) :: lmesh
+    class(ElementBase3D), intent(in) :: elem
+    integer, intent(in) :: QA
+    type(LocalMeshFieldBaseList), intent(inout) :: QTRC(QA)
+    real(RP), intent(inout), target :: DDENS(elem%Np,lmesh%NeA)
+    real(RP), intent(inout), target :: PRES(elem%Np,lmesh%NeA)
+    real(RP), intent(inout), target :: CVtot(elem%Np,lmesh%NeA)
+    real(RP), intent(inout), target :: CPtot(elem%Np,lmesh%NeA)
+    real(RP), intent(inout), target :: Rtot(elem%Np,lmesh%NeA)
+    real(RP), intent(in), target :: DENS_hyd(elem%Np,lmesh%NeA)
+    real(RP), intent(in), target :: PRES_hyd(elem%Np,lmesh%NeA)
+    real(RP), intent(in) :: dt
+    integer, intent(in) :: QLA, QIA
+    real(RP), intent(inout), optional, target :: DRHOT(elem%Np,lmesh%NeA)
+
+    type(c_ptr) :: qp(QA), drp
+    integer :: iq
+    integer(c_int) :: ierr
+    do iq = 1, QA
+      qp(iq) = acc_deviceptr( QTRC(iq)%ptr%val )
+    end do
+    drp = c_null_ptr
+    if ( present(DRHOT) ) drp = acc_deviceptr( DRHOT )
+    ierr = fedg_trc_negative_fixer( atm_dyn_dgm_nonhydro3d_gb300_ctx(), qp, QA, QLA, QIA, &
+      TRACER_MASS, TRACER_R, TRACER_CV, TRACER_CP, &
+      acc_deviceptr(DDENS), acc_deviceptr(PRES), acc_deviceptr(CVtot), acc_deviceptr(CPtot), &
+      acc_deviceptr(Rtot), acc_deviceptr(DENS_hyd), acc_deviceptr(PRES_hyd), drp, dt )
+    if (ierr < 0) call PRC_abort
+    ierr = fedg_synchronize( atm_dyn_dgm_nonhydro3d_gb300_ctx() )
+  end subroutine atm_phy_mp_dgm_common_gb300_negative_fixer
 
 end module scale_atm_dyn_dgm_trcadvect3d_gb300

@@ -329,6 +329,26 @@ int fedg_trc_update(fedg_ctx* ctx, double* QTRC, const double* const mflx[3], co
                     const double* alph_P, const double* DDENS_TRC, const double* DDENS0_TRC, const double* DDENS,
                     const double* RHOQ_tp, const fedg_trc_opts* opts);
 
+/* atm_phy_mp_dgm_common_negative_fixer (FElib/src/microphysics/scale_atm_phy_mp_dgm_common.F90:429-556),
+ * which the tracer driver runs after the tracer step (fix_negative_val, driver_trcadv3d.F90:550,
+ * 596-651), in place, FP64.  Per element, each water species iq = 0 .. QLA+QIA has its mass DENS q
+ * clipped below at 1e-128 and rescaled to the element's mass max(M, 0); DDENS takes the mass change,
+ * the internal energy CVtot PRES / Rtot the change times TRACER_CV and the temperature; then the
+ * internal energy is rescaled to the element's old total, Rtot/CVtot/CPtot follow the new mixing
+ * ratios (SCALE's mixture specific heats: qdry = 1 - sum q TRACER_MASS, Rtot = sum q TRACER_R +
+ * qdry Rdry, likewise CV and CP), the potential energy of the mass change (DDENS - DDENS0) g z is taken
+ * out and PRES = IntEn Rtot / CVtot.  DRHOT (may be NULL: FElib's non-RHOT thermodynamic variable)
+ * is rebuilt as P00/Rtot (PRES/P00)^(CVtot/CPtot) - P00/Rdry (PRES_hyd/P00)^(CVdry/CPdry).
+ *   QTRC[QA]        device pointers of the tracers (Np, Ne); QA = 1 + QLA + QIA (<= 16): FElib's routine
+ *                   leaves the mixing ratios of any further tracer undefined, so it is refused here
+ *   trc_mass/r/cv/cp host arrays of QA: TRACER_MASS, TRACER_R, TRACER_CV, TRACER_CP (scale_tracer)
+ *   DENS_hyd, PRES_hyd (Np, Ne) device arrays; dt as in FElib's argument list (unused there too).
+ * Element integrals: the LGL quadrature of the flat cube; z of a node from the mesh descriptor. */
+int fedg_trc_negative_fixer(fedg_ctx* ctx, double* const* QTRC, int QA, int QLA, int QIA, const double* trc_mass,
+                            const double* trc_r, const double* trc_cv, const double* trc_cp, double* DDENS,
+                            double* PRES, double* CVtot, double* CPtot, double* Rtot, const double* DENS_hyd,
+                            const double* PRES_hyd, double* DRHOT, double dt);
+
 /* Tracer transport outputs of fedg_update (every prec), the coupling of FElib's dynamics driver to
  * its tracer driver (driver_nonhydro3d.F90:900-935): during each step, after every stage's explicit
  * tendency, the stage-weighted mass flux and the dynamics' Rusanov coefficients are accumulated into
