@@ -1,6 +1,7 @@
 """GPU parity of the tracer negative fixer (fedg_trc_negative_fixer, the C ABI) against its CPU
 restatement oracle/negfix_ref.py (FElib/src/microphysics/scale_atm_phy_mp_dgm_common.F90:429-556).
-Both are FP64; only the summation order of the element integrals differs: 1e-12 relative."""
+Both are FP64; only the summation order of the element integrals (and the pow of CUDA against the
+host's) differs: 1e-12 relative, DRHOT (a difference of two RHOT-sized terms) 1e-13 of RHOT."""
 import numpy as np
 import pytest
 
@@ -42,7 +43,10 @@ def test_negative_fixer_matches_oracle(porder, dims, with_drhot):
                        ("Rtot", rd, want[5])):
         assert rel(g.cpu().numpy(), w) <= TOL, name
     if with_drhot:
-        assert rel(drd.cpu().numpy(), want[6]) <= 1e-10, "DRHOT"  # a difference of two ~3e2 terms
+        # DRHOT is the difference of two RHOT-sized terms (~3e2): its rounding is measured against them
+        rhot = cases.PRES00 / want[5] * (want[2] / cases.PRES00) ** (want[3] / want[4])
+        assert np.abs(drd.cpu().numpy() - want[6]).max() <= 1e-13 * np.abs(rhot).max(), "DRHOT"
+
     ctx.close()
 
 
