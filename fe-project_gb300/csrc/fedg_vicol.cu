@@ -48,11 +48,12 @@ struct ColLayout {
   __host__ __device__ ColLayout(int N1, int NeZ) {
     const int L = N1 * NeZ;
     int o = 0;
-    oP = o;    o += 24 * L;                    // float2 P[3L] (uv phase: var0 pairs [2L])
+    oP = o;    o += 12 * L;                    // float P[3L]: the iterate's leading parts (uv phase:
+                                               // E [2L] and the face jumps of q*)
     oBf = o;   o += 12 * L;                    // float b / y / x [3L] (uv phase: [2L])
     oDel = o;  o += 48;                        // 6 face fluxes (float2) of the current element
     oAl = o;   o += ((8 * NeZ + 15) / 16) * 16; // alB, alT per element
-    const int u_ring = 96 * N1;                            // 3 element slots x 4 quantities x N1 x float2
+    const int u_ring = 120 * N1;                           // 3 element slots x 5 quantities x N1 x float2
     const int u_solve = 16 * (N1 + 2) + 64;                // float4 pot, wt, dpd of the element's nodes
                                                            // + 2 neighbours; coupling from below
     const int u_jb = ((12 * (NeZ + 1) + 15) / 16) * 16;    // uv: c' and the two interface jumps
@@ -67,7 +68,7 @@ struct ColLayout {
 
 template <int N1>
 struct Col {
-  float2* P;     // iterate, float pairs, row 3l+v (v: DENS, MOMZ, RHOT)
+  float* P;      // iterate: the leading parts of its float pairs, row 3l+v (v: DENS, MOMZ, RHOT)
   float4* sJ;    // Jacobian level quantities of the current element's nodes, then node N of the
                  // element below and node 0 of the element above
   void* ring;    // [3][4][N1]: slot, quantity (MOMZ, DDENS, fm, fr), node
@@ -76,8 +77,14 @@ struct Col {
   float* bc;
   float* al;
   float* jb;
+  // the trailing parts of the iterate's pairs, in global memory (L2-resident while the column is in
+  // flight): three planes of n nodes, node (column + element * ncol) * N1 + k, so that a warp's 32
+  // nodes of an element fill one 128-byte line per plane
+  float* lo;
+  size_t lo_n, lo_b, lo_s;
   int k, NeZ, L;
   size_t gb, gs;  // global index of node (0, k) of this column and the element-layer stride
+  __device__ float* plo(int v, int e) const { return lo + (size_t)v * lo_n + lo_b + (size_t)e * lo_s; }
   __device__ size_t g(int e) const { return gb + (size_t)e * gs; }
   __device__ float alB(int e) const { return al[2 * e]; }
   __device__ float alT(int e) const { return al[2 * e + 1]; }
@@ -121,21 +128,20 @@ __device__ __forceinline__ float grp_max_nan(float e, int width) {
 // ---------------------------------------------------------------------------------------------
 // residual b = impl_fac A(P) + q* - P of the DENS/MOMZ/RHOT system into c.Bf (FP32); returns the
 // column max of |b|/scale (NaN if not finite).
-// CERT: the operator A in float pairs (eval_Ax, hevi_common_2.F90:1177-1292, with the vertical
-// face flux vi_cal_del_flux_dyn :1294-1323); otherwise A in FP32 with only q* - P in pairs.
-// Element by element, with the level quantities of elements e-1, e, e+1 in a ring of 3 slots.
+// The operator A in float pairs (eval_Ax, hevi_common_2.F90:1177-1292, with the vertical face flux
+// vi_cal_del_flux_dyn :1294-1323).
+// Element by element, with the level quantities of elements e-1, e, e+1 in a ring of 3 slots
+// (MOMZ, DDENS, fm, fr and DRHOT of every node, the iterate's values as float pairs).
 // The pressure deviation PRES_hyd ((1 + r)^kappa - 1), r = DRHOT/RHOT_hyd, is the binomial
 // series: its leading term kappa r in pairs, the rest (relative size |r|) in FP32, which keeps
 // the pair precision for |r| <= rmax; beyond that pow() in FP64.
-template <int N1, bool CERT>
+template <int N1>
 __device__ float col_residual(const OpsX& ox, const Col<N1>& c, const ProfX& px, const X5& qin, float2 impl2,
                               float cref) {
   constexpr int N = N1 - 1;
   const int k = c.k;
-  const float kapf = ox.kap.x;
   float2* r2 = reinterpret_cast<float2*>(c.ring);
-  float* r1 = reinterpret_cast<float*>(c.ring);
-  auto ri = [](int s, int q, int m) { return (s * 4 + q) * N1 + m; };
+  auto ri = [](int s, int q, int m) { return (s * 5 + q) * N1 + m; };
   f2 Dk[N1], Tk[N1];
 #pragma unroll
   for (int m = 0; m < N1; ++m) {
@@ -145,42 +151,45 @@ __device__ float col_residual(const OpsX& ox, const Col<N1>& c, const ProfX& px,
   const f2 lbk = f2_of(ox.Lb[k]), ltk = f2_of(ox.Lt[k]);
   const f2 E33 = f2_of(ox.E33), grav = f2_of(ox.grav), tmp1 = f2_of(ox.tmp1), impl = f2_of(impl2);
 
-  auto fill = [&](int e) {  // level quantities of node (e, k) into slot e % 3 (all lanes)
-    const int l = e * N1 + k;
-    const f2 Pd = f2_of(c.P[3 * l]), Pm = f2_of(c.P[3 * l + 1]), Pr = f2_of(c.P[3 * l + 2]);
-    const int s = e % 3;
-    if constexpr (CERT) {
-      const f2 dens = f2_add(f2_of(__ldg(px.dh + l)), Pd);
-      const f2 rhot = f2_add(f2_of(__ldg(px.rh + l)), Pr);
-      const f2 rd = f2_recip(dens);
-      const f2 pot = f2_mul(rhot, rd);
-      const f2 rr = f2_mul(Pr, f2_of(__ldg(px.rhinv + l)));
-      f2 S;
-      if (fabsf(rr.h) <= ox.rmax) {
-        float tl = ox.cb[11];
+  auto lo3 = [&](int e, float (&o)[3]) {
 #pragma unroll
-        for (int m = 10; m >= 1; --m) tl = fmaf(tl, rr.h, ox.cb[m]);
-        S = f2_add_f(f2_mul(f2_of(ox.kap), rr), __fmul_rn(__fmul_rn(rr.h, rr.h), tl));
-      } else {
-        S = f2_split(pow(1.0 + ((double)rr.h + (double)rr.l), ox.kap64) - 1.0);
-      }
-      const f2 fm = f2_mul(f2_of(__ldg(px.ph + l)), S);
-      r2[ri(s, 0, k)] = f2_pack(Pm);
-      r2[ri(s, 1, k)] = f2_pack(Pd);
-      r2[ri(s, 2, k)] = f2_pack(fm);
-      r2[ri(s, 3, k)] = f2_pack(f2_mul(pot, Pm));
+    for (int v = 0; v < 3; ++v) o[v] = *c.plo(v, e);
+  };
+  auto fill = [&](int e, const float (&lo)[3]) {  // level quantities of node (e, k) into slot e % 3
+    const int l = e * N1 + k;
+    const f2 Pd{c.P[3 * l], lo[0]}, Pm{c.P[3 * l + 1], lo[1]}, Pr{c.P[3 * l + 2], lo[2]};
+    const int s = e % 3;
+    const f2 dens = f2_add(f2_of(__ldg(px.dh + l)), Pd);
+    const f2 rhot = f2_add(f2_of(__ldg(px.rh + l)), Pr);
+    const f2 rd = f2_recip(dens);
+    const f2 pot = f2_mul(rhot, rd);
+    const f2 rr = f2_mul(Pr, f2_of(__ldg(px.rhinv + l)));
+    f2 S;
+    if (fabsf(rr.h) <= ox.rmax) {
+      float tl = ox.cb[11];
+#pragma unroll
+      for (int m = 10; m >= 1; --m) tl = fmaf(tl, rr.h, ox.cb[m]);
+      S = f2_add_f(f2_mul(f2_of(ox.kap), rr), __fmul_rn(__fmul_rn(rr.h, rr.h), tl));
     } else {
-      const float rdf = 1.f / (__ldg(px.dhf + l) + Pd.h);
-      const float potf = (__ldg(px.rhf + l) + Pr.h) * rdf;
-      r1[ri(s, 0, k)] = Pm.h;
-      r1[ri(s, 1, k)] = Pd.h;
-      r1[ri(s, 2, k)] = __ldg(px.phf + l) * expm1f(kapf * log1pf(Pr.h * __ldg(px.rthf + l)));
-      r1[ri(s, 3, k)] = potf * Pm.h;
+      S = f2_split(pow(1.0 + ((double)rr.h + (double)rr.l), ox.kap64) - 1.0);
     }
+    const f2 fm = f2_mul(f2_of(__ldg(px.ph + l)), S);
+    r2[ri(s, 0, k)] = f2_pack(Pm);
+    r2[ri(s, 1, k)] = f2_pack(Pd);
+    r2[ri(s, 2, k)] = f2_pack(fm);
+    r2[ri(s, 3, k)] = f2_pack(f2_mul(pot, Pm));
+    r2[ri(s, 4, k)] = f2_pack(Pr);
   };
 
-  fill(0);
-  if (c.NeZ > 1) fill(1);
+  {
+    float lo[3];
+    lo3(0, lo);
+    fill(0, lo);
+    if (c.NeZ > 1) {
+      lo3(1, lo);
+      fill(1, lo);
+    }
+  }
   __syncwarp();
   float errf = 0.f;
   const int gv[3] = {VD, VMZ, VRT};
@@ -196,93 +205,59 @@ __device__ float col_residual(const OpsX& ox, const Col<N1>& c, const ProfX& px,
 #pragma unroll
       for (int v = 0; v < 3; ++v) qnxt[v] = __ldg(qin.v[gv[v]] + gn);
     }
+    float lon[3] = {0.f, 0.f, 0.f};  // the trailing parts of element e + 2's iterate, for its fill
+    if (e + 2 < c.NeZ) lo3(e + 2, lon);
     // vertical-face fluxes of element e: lanes over (side, variable)
     for (int t = k; t < 6; t += N1) {
       const int s = t / 3, v = t - 3 * s;
       const int nM = s == 0 ? 0 : N;
-      const int lM = e * N1 + nM;
       const bool lid = s == 0 ? (e == 0) : (e == c.NeZ - 1);
-      const int lP = lid ? lM : (s == 0 ? lM - 1 : lM + 1);
       const int sP = lid ? sc : (s == 0 ? sb : st), nP = lid ? nM : (s == 0 ? N : 0);
       const float nz = s == 0 ? -1.f : 1.f;
       const float al = s == 0 ? c.alB(e) : c.alT(e);
       // jump of RHOT (the slip lid's exterior state is the interior one: no jump)
-      const f2 dth = lid ? f2{0.f, 0.f} : f2_sub(f2_of(c.P[3 * lP + 2]), f2_of(c.P[3 * lM + 2]));
-      if constexpr (CERT) {
-        const f2 mzM = f2_of(r2[ri(sc, 0, nM)]);
-        const f2 dmz = lid ? f2_add(f2_neg(mzM), f2_neg(mzM)) : f2_sub(f2_of(r2[ri(sP, 0, nP)]), mzM);
-        f2 x;
-        if (v == 0) {
-          const f2 dr = lid ? f2{0.f, 0.f} : f2_sub(f2_of(r2[ri(sP, 1, nP)]), f2_of(r2[ri(sc, 1, nM)]));
-          x = f2_sub(f2_mul_f(dmz, nz), f2_mul_f(dr, al));
-        } else if (v == 1) {
-          const f2 dfm = lid ? f2{0.f, 0.f} : f2_sub(f2_of(r2[ri(sP, 2, nP)]), f2_of(r2[ri(sc, 2, nM)]));
-          x = f2_sub(f2_mul_f(dfm, nz), f2_mul_f(dmz, al));
-        } else {
-          const f2 frM = f2_of(r2[ri(sc, 3, nM)]);
-          const f2 dfr = lid ? f2_add(f2_neg(frM), f2_neg(frM)) : f2_sub(f2_of(r2[ri(sP, 3, nP)]), frM);
-          x = f2_sub(f2_mul_f(dfr, nz), f2_mul_f(dth, al));
-        }
-        reinterpret_cast<float2*>(c.del)[t] = f2_pack(f2_mul(tmp1, x));
+      const f2 dth = lid ? f2{0.f, 0.f} : f2_sub(f2_of(r2[ri(sP, 4, nP)]), f2_of(r2[ri(sc, 4, nM)]));
+      const f2 mzM = f2_of(r2[ri(sc, 0, nM)]);
+      const f2 dmz = lid ? f2_add(f2_neg(mzM), f2_neg(mzM)) : f2_sub(f2_of(r2[ri(sP, 0, nP)]), mzM);
+      f2 x;
+      if (v == 0) {
+        const f2 dr = lid ? f2{0.f, 0.f} : f2_sub(f2_of(r2[ri(sP, 1, nP)]), f2_of(r2[ri(sc, 1, nM)]));
+        x = f2_sub(f2_mul_f(dmz, nz), f2_mul_f(dr, al));
+      } else if (v == 1) {
+        const f2 dfm = lid ? f2{0.f, 0.f} : f2_sub(f2_of(r2[ri(sP, 2, nP)]), f2_of(r2[ri(sc, 2, nM)]));
+        x = f2_sub(f2_mul_f(dfm, nz), f2_mul_f(dmz, al));
       } else {
-        // MOMZ and density jumps from the float-pair iterate: the jumps of a DG solution are small
-        // against the values, so differencing FP32-rounded values would lose them
-        const float mzM = r1[ri(sc, 0, nM)];
-        const float dmz = lid ? -2.f * mzM : f2_to_f(f2_sub(f2_of(c.P[3 * lP + 1]), f2_of(c.P[3 * lM + 1])));
-        float x;
-        if (v == 0) x = dmz * nz - al * (lid ? 0.f : f2_to_f(f2_sub(f2_of(c.P[3 * lP]), f2_of(c.P[3 * lM]))));
-        else if (v == 1) x = (lid ? 0.f : r1[ri(sP, 2, nP)] - r1[ri(sc, 2, nM)]) * nz - al * dmz;
-        else {
-          const float frM = r1[ri(sc, 3, nM)];
-          x = (lid ? -2.f * frM : r1[ri(sP, 3, nP)] - frM) * nz - al * f2_to_f(dth);
-        }
-        reinterpret_cast<float*>(c.del)[t] = tmp1.h * x;
+        const f2 frM = f2_of(r2[ri(sc, 3, nM)]);
+        const f2 dfr = lid ? f2_add(f2_neg(frM), f2_neg(frM)) : f2_sub(f2_of(r2[ri(sP, 3, nP)]), frM);
+        x = f2_sub(f2_mul_f(dfr, nz), f2_mul_f(dth, al));
       }
+      reinterpret_cast<float2*>(c.del)[t] = f2_pack(f2_mul(tmp1, x));
     }
     __syncwarp();
     {
       const int l = e * N1 + k;
       const float isc[3] = {1.f / __ldg(px.dhf + l), 1.f / (__ldg(px.dhf + l) * cref), 1.f / __ldg(px.rhf + l)};
       float bfl[3];
-      if constexpr (CERT) {
-        f2acc sd, sm, sr, drho;
+      f2acc sd, sm, sr, drho;
 #pragma unroll
-        for (int m = 0; m < N1; ++m) {
-          sd.add(Dk[m], f2_of(r2[ri(sc, 0, m)]));
-          drho.add(Tk[m], f2_of(r2[ri(sc, 1, m)]));
-          sm.add(Dk[m], f2_of(r2[ri(sc, 2, m)]));
-          sr.add(Dk[m], f2_of(r2[ri(sc, 3, m)]));
-        }
-        const float2* dl = reinterpret_cast<const float2*>(c.del);
-        f2 A[3];
-        A[0] = f2_add(f2_add(f2_mul(E33, sd.get()), f2_mul(lbk, f2_of(dl[0]))), f2_mul(ltk, f2_of(dl[3])));
-        A[1] = f2_add(f2_add(f2_add(f2_mul(E33, sm.get()), f2_mul(lbk, f2_of(dl[1]))), f2_mul(ltk, f2_of(dl[4]))),
-                      f2_mul(grav, drho.get()));
-        A[2] = f2_add(f2_add(f2_mul(E33, sr.get()), f2_mul(lbk, f2_of(dl[2]))), f2_mul(ltk, f2_of(dl[5])));
+      for (int m = 0; m < N1; ++m) {
+        sd.add(Dk[m], f2_of(r2[ri(sc, 0, m)]));
+        drho.add(Tk[m], f2_of(r2[ri(sc, 1, m)]));
+        sm.add(Dk[m], f2_of(r2[ri(sc, 2, m)]));
+        sr.add(Dk[m], f2_of(r2[ri(sc, 3, m)]));
+      }
+      const float2* dl = reinterpret_cast<const float2*>(c.del);
+      f2 A[3];
+      A[0] = f2_add(f2_add(f2_mul(E33, sd.get()), f2_mul(lbk, f2_of(dl[0]))), f2_mul(ltk, f2_of(dl[3])));
+      A[1] = f2_add(f2_add(f2_add(f2_mul(E33, sm.get()), f2_mul(lbk, f2_of(dl[1]))), f2_mul(ltk, f2_of(dl[4]))),
+                    f2_mul(grav, drho.get()));
+      A[2] = f2_add(f2_add(f2_mul(E33, sr.get()), f2_mul(lbk, f2_of(dl[2]))), f2_mul(ltk, f2_of(dl[5])));
+      // this node's iterate from the ring: DDENS (quantity 1), MOMZ (0), DRHOT (4)
+      const f2 Pl[3] = {f2_of(r2[ri(sc, 1, k)]), f2_of(r2[ri(sc, 0, k)]), f2_of(r2[ri(sc, 4, k)])};
 #pragma unroll
-        for (int v = 0; v < 3; ++v) {  // A[v] holds -A: b = q* - P - impl_fac (-A)
-          const f2 qmp = f2_sub(f2_of(qcur[v]), f2_of(c.P[3 * l + v]));
-          bfl[v] = f2_to_f(f2_sub(qmp, f2_mul(impl, A[v])));
-        }
-      } else {
-        float sd = 0.f, sm = 0.f, sr = 0.f, drho = 0.f;
-#pragma unroll
-        for (int m = 0; m < N1; ++m) {
-          sd = fmaf(Dk[m].h, r1[ri(sc, 0, m)], sd);
-          drho = fmaf(Tk[m].h, r1[ri(sc, 1, m)], drho);
-          sm = fmaf(Dk[m].h, r1[ri(sc, 2, m)], sm);
-          sr = fmaf(Dk[m].h, r1[ri(sc, 3, m)], sr);
-        }
-        const float* dl = reinterpret_cast<const float*>(c.del);
-        float A[3];
-        A[0] = E33.h * sd + lbk.h * dl[0] + ltk.h * dl[3];
-        A[1] = E33.h * sm + lbk.h * dl[1] + ltk.h * dl[4] + grav.h * drho;
-        A[2] = E33.h * sr + lbk.h * dl[2] + ltk.h * dl[5];
-#pragma unroll
-        for (int v = 0; v < 3; ++v) {
-          const float qmp = f2_to_f(f2_sub(f2_of(qcur[v]), f2_of(c.P[3 * l + v])));
-          bfl[v] = fmaf(-impl.h, A[v], qmp);
-        }
+      for (int v = 0; v < 3; ++v) {  // A[v] holds -A: b = q* - P - impl_fac (-A)
+        const f2 qmp = f2_sub(f2_of(qcur[v]), Pl[v]);
+        bfl[v] = f2_to_f(f2_sub(qmp, f2_mul(impl, A[v])));
       }
 #pragma unroll
       for (int v = 0; v < 3; ++v) {
@@ -292,7 +267,7 @@ __device__ float col_residual(const OpsX& ox, const Col<N1>& c, const ProfX& px,
       }
     }
     __syncwarp();
-    if (e + 2 < c.NeZ) fill(e + 2);
+    if (e + 2 < c.NeZ) fill(e + 2, lon);
     __syncwarp();
 #pragma unroll
     for (int v = 0; v < 3; ++v) qcur[v] = qnxt[v];
@@ -362,7 +337,8 @@ __device__ void col_start(const ProfX& px, float kapf, const Col<N1>& c, const F
 #pragma unroll
     for (int v = 0; v < 3; ++v) {
       const f2 p = guess ? f2_add_f(f2_of(qc[v]), gc[v]) : f2_split(zc[v]);
-      c.P[3 * l + v] = f2_pack(p);
+      c.P[3 * l + v] = p.h;
+      *c.plo(v, e) = p.l;
       if (res) c.Bf[3 * l + v] = f2_to_f(f2_add(f2_sub(f2_of(qc[v]), p), f2_mul(impl, f2_of(ac[v]))));
       zc[v] = zn[v];
       qc[v] = qn[v];
@@ -551,13 +527,39 @@ __device__ __forceinline__ void lu_blocked(float (&a)[3][3 * N1], float (&r)[3][
 
 // FP32 Jacobian level quantities of level l from the iterate: pot = RHOT/DENS, wt = MOMZ/DENS,
 // dpd = dP/dRHOT = kappa PRES/RHOT
-__device__ __forceinline__ float4 jac_level(const ProfX& px, const float2* P, int l, float kapf) {
-  const float Pd = P[3 * l].x, Pm = P[3 * l + 1].x, Pr = P[3 * l + 2].x;
+__device__ __forceinline__ float4 jac_level(const ProfX& px, const float* P, int l, float kapf) {
+  const float Pd = P[3 * l], Pm = P[3 * l + 1], Pr = P[3 * l + 2];
   const float rdf = 1.f / (__ldg(px.dhf + l) + Pd);
   const float rhotf = __ldg(px.rhf + l) + Pr;
   const float phf = __ldg(px.phf + l);
   const float fmf = phf * expm1f(kapf * log1pf(Pr * __ldg(px.rthf + l)));
   return make_float4(rhotf * rdf, Pm * rdf, kapf * (phf + fmf) / rhotf, 0.f);
+}
+
+// P += sgn * b (b in c.Bf) in float pairs over the lane's levels; the trailing parts come from and go
+// back to their global planes, loaded four elements at a time so that their latency overlaps
+template <int N1>
+__device__ __forceinline__ void col_add(const Col<N1>& c, float sgn) {
+  const int k = c.k;
+  for (int e0 = 0; e0 < c.NeZ; e0 += 4) {
+    float lv[4][3];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int v = 0; v < 3; ++v) lv[j][v] = e0 + j < c.NeZ ? *c.plo(v, e0 + j) : 0.f;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (e0 + j < c.NeZ) {
+        const int l = (e0 + j) * N1 + k;
+#pragma unroll
+        for (int v = 0; v < 3; ++v) {
+          const f2 p = f2_add_f(f2{c.P[3 * l + v], lv[j][v]}, sgn * c.Bf[3 * l + v]);
+          c.P[3 * l + v] = p.h;
+          *c.plo(v, e0 + j) = p.l;
+        }
+      }
+    }
+  }
 }
 
 // Block-Thomas history G_e = A_e^-1 U_e of the column solve: per node the 3 rows x 3 coupling
@@ -735,13 +737,7 @@ __device__ void col_solve(const Ops& op, const ProfX& px, float kapf, const Col<
     __syncwarp();  // every lane has read element e's history: its lines are dead
     gh.discard((gcol0 + (size_t)e * glayer) * N1, lane);
   }
-  if (apply) {
-    for (int e = 0; e < c.NeZ; ++e) {
-      const int l = e * N1 + k;
-#pragma unroll
-      for (int v = 0; v < 3; ++v) c.P[3 * l + v] = f2_pack(f2_add_f(f2_of(c.P[3 * l + v]), c.Bf[3 * l + v]));
-    }
-  }
+  if (apply) col_add<N1>(c, 1.f);
   __syncwarp();
 }
 
@@ -831,24 +827,16 @@ __device__ void col_jvp(const Ops& op, const ProfX& px, float kapf, const Col<N1
 template <int N1>
 __device__ void col_neumann(const Ops& op, const ProfX& px, float kapf, const Col<N1>& c, double impl_fac, int nterm,
                             bool apply) {
-  const int k = c.k;
   for (int t = 0; t <= nterm; ++t) {
     if (t > 0) col_jvp<N1>(op, px, kapf, c, impl_fac);
-    if (apply) {
-      const float sgn = (t & 1) ? -1.f : 1.f;
-      for (int e = 0; e < c.NeZ; ++e) {
-        const int l = e * N1 + k;
-#pragma unroll
-        for (int v = 0; v < 3; ++v) c.P[3 * l + v] = f2_pack(f2_add_f(f2_of(c.P[3 * l + v]), sgn * c.Bf[3 * l + v]));
-      }
-    }
+    if (apply) col_add<N1>(c, (t & 1) ? -1.f : 1.f);
     __syncwarp();
   }
 }
 
 // ---------------------------------------------------------------------------------------------
 template <int N1, bool PO>
-__global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, const ProfX px, const X5 qin, const F5c z,
+__global__ void __launch_bounds__(64, 6) k_vi_cols(const Ops op, const OpsX ox, const ProfX px, const X5 qin, const F5c z,
                                                 const A3 a0, const float* const* guess, void* const* qsf, void* const* tout,
                                                 float* __restrict__ gsc, int* status, unsigned long long* cnt,
                                                 const MixViArgs args, int ncol) {
@@ -866,7 +854,7 @@ __global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, 
   const ColLayout lay(N1, NeZ);
   unsigned char* base = smraw + (size_t)(wib * C + grp) * lay.stride;
   Col<N1> c;
-  c.P = reinterpret_cast<float2*>(base + lay.oP);
+  c.P = reinterpret_cast<float*>(base + lay.oP);
   c.sJ = reinterpret_cast<float4*>(base + lay.oSJ);
   c.ring = base + lay.oRing;
   c.del = base + lay.oDel;
@@ -875,6 +863,10 @@ __global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, 
   c.al = reinterpret_cast<float*>(base + lay.oAl);
   c.jb = reinterpret_cast<float*>(base + lay.oJb);
   c.k = k; c.NeZ = NeZ; c.L = L;
+  c.lo_n = (size_t)ncol * L;
+  c.lo = gsc + 9 * c.lo_n;  // after the block-Thomas history planes
+  c.lo_b = (size_t)col * N1 + k;
+  c.lo_s = (size_t)ncol * N1;
   {
     const int ij = col % NF, exy = col / NF;
     const int ci = ij % N1, cj = ij / N1;
@@ -910,7 +902,7 @@ __global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, 
     // the first residual comes from the stage's A(var0) when the iterate starts at var0; every
     // other one is the certifying float-pair residual
     float err = 0.f;
-    if (!(nsolve == 0 && first_a0)) err = col_residual<N1, true>(ox, c, px, qin, args.impl2, cref);
+    if (!(nsolve == 0 && first_a0)) err = col_residual<N1>(ox, c, px, qin, args.impl2, cref);
     if (active && nsolve > 0) {
       if (err != err) { st = -2; active = false; }
       else if ((double)err <= args.tol) { st = nsolve; active = false; }
@@ -926,20 +918,29 @@ __global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, 
   }
   const unsigned long long once = l2_evict_first();
   float2 qo[3];
+  float po[3];  // the trailing parts of the iterate, one element ahead like q*
 #pragma unroll
-  for (int m = 0; m < 3; ++m) qo[m] = ld_once(qin.v[gv[m]] + c.g(0), once);
+  for (int m = 0; m < 3; ++m) {
+    qo[m] = ld_once(qin.v[gv[m]] + c.g(0), once);
+    po[m] = *c.plo(m, 0);
+  }
   for (int e = 0; e < NeZ; ++e) {
     const int l = e * N1 + k;
     const size_t gi = c.g(e);
     const float2 qc[3] = {qo[0], qo[1], qo[2]};
+    const float pc[3] = {po[0], po[1], po[2]};
     {
-      const size_t gn = c.g(e + 1 < NeZ ? e + 1 : e);
+      const int en = e + 1 < NeZ ? e + 1 : e;
+      const size_t gn = c.g(en);
 #pragma unroll
-      for (int m = 0; m < 3; ++m) qo[m] = ld_once(qin.v[gv[m]] + gn, once);
+      for (int m = 0; m < 3; ++m) {
+        qo[m] = ld_once(qin.v[gv[m]] + gn, once);
+        po[m] = *c.plo(m, en);
+      }
     }
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
-      const f2 pnew = f2_of(c.P[3 * l + m]);
+      const f2 pnew{c.P[3 * l + m], pc[m]};
       const f2 inc = f2_sub(pnew, f2_of(qc[m]));
       if constexpr (PO) {
         st_once(static_cast<float2*>(qsf[gv[m]]) + gi, f2_pack(pnew), once);
@@ -957,8 +958,9 @@ __global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, 
   // are formed in pairs once per column; the corrections are FP32 and accumulate into E in pairs,
   // so repeated corrections refine E to pair accuracy.
   {
-    float2* E = reinterpret_cast<float2*>(c.P);         // [2L] P - q* (float pair)
-    float* jq = reinterpret_cast<float*>(c.P) + 4 * L;  // [4 NeZ] face jumps of q*
+    float* Eh = c.P;          // [2L] P - q* (float pair): the leading parts; the trailing ones in the
+                              // iterate's global planes 0 and 1, free once DENS/MOMZ/RHOT are stored
+    float* jq = c.P + 2 * L;  // [4 NeZ] face jumps of q*
     float* bu = c.Bf;                                   // [2L] residual
     // E = var0 - q* at every node; the bottom/top jumps (neighbour - own) of q* MOMX/MOMY from the
     // face nodes' values, passed between lanes by shuffles: jq[4e + m] = q*(e-1, N) - q*(e, 0),
@@ -974,7 +976,9 @@ __global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, 
 #pragma unroll
       for (int m = 0; m < 2; ++m) {
         const f2 qs = f2_of(qu[m]);
-        E[2 * l + m] = f2_pack(f2_sub(f2_split(zu[m]), qs));
+        const f2 ev = f2_sub(f2_split(zu[m]), qs);
+        Eh[2 * l + m] = ev.h;
+        *c.plo(m, e) = ev.l;
         const f2 q0{__shfl_sync(FULL, qs.h, 0, N1), __shfl_sync(FULL, qs.l, 0, N1)};
         const f2 qN{__shfl_sync(FULL, qs.h, N, N1), __shfl_sync(FULL, qs.l, N, N1)};
         if (k == 0) {
@@ -996,13 +1000,19 @@ __global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, 
     bool active = true;
     for (int it = 0; it < 4; ++it) {
       float err = 0.f;
+      float el[2] = {*c.plo(0, 0), *c.plo(1, 0)};  // trailing parts of E, one element ahead
       for (int e = 0; e < NeZ; ++e) {
+        const float ec[2] = {el[0], el[1]};
+        if (e + 1 < NeZ) {
+          el[0] = *c.plo(0, e + 1);
+          el[1] = *c.plo(1, e + 1);
+        }
         for (int t = k; t < 4; t += N1) {
           const int s = t >> 1, m = t & 1;
           const int lM = e * N1 + (s == 0 ? 0 : N);
           const bool lid = s == 0 ? (e == 0) : (e == NeZ - 1);
           const int lP = lid ? lM : (s == 0 ? lM - 1 : lM + 1);
-          jdel[t] = jq[4 * e + t] + (E[2 * lP + m].x - E[2 * lM + m].x);
+          jdel[t] = jq[4 * e + t] + (Eh[2 * lP + m] - Eh[2 * lM + m]);
         }
         __syncwarp();
         const int l = e * N1 + k;
@@ -1011,7 +1021,7 @@ __global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, 
 #pragma unroll
         for (int m = 0; m < 2; ++m) {
           const float Af = cfs * (aB * jdel[m] + aT * jdel[2 + m]);  // impl_fac * A(P)
-          const float b = (Af - E[2 * l + m].x) - E[2 * l + m].y;
+          const float b = (Af - Eh[2 * l + m]) - ec[m];
           bu[2 * l + m] = b;
           err = fmaxf(err, fabsf(b) * iscu);
           if (!(fabsf(b) < 3.0e38f)) err = __int_as_float(0x7fc00000);
@@ -1053,32 +1063,52 @@ __global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, 
       }
       __syncwarp();
       if (need) {
-        for (int e = 0; e < NeZ; ++e) {
-          const int l = e * N1 + k;
-          const float beta = e > 0 ? cfs * lbk * c.alB(e) : 0.f;
-          const float tau = e < NeZ - 1 ? cfs * ltk * c.alT(e) : 0.f;
-          E[2 * l] = f2_pack(f2_add_f(f2_of(E[2 * l]), bu[2 * l] - beta * Jx[e] + tau * Jx[e + 1]));
-          E[2 * l + 1] = f2_pack(f2_add_f(f2_of(E[2 * l + 1]), bu[2 * l + 1] - beta * Jy[e] + tau * Jy[e + 1]));
+        for (int e0 = 0; e0 < NeZ; e0 += 4) {  // trailing parts loaded four elements at a time
+          float lv[4][2];
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int m = 0; m < 2; ++m) lv[j][m] = e0 + j < NeZ ? *c.plo(m, e0 + j) : 0.f;
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int e = e0 + j;
+            if (e < NeZ) {
+              const int l = e * N1 + k;
+              const float beta = e > 0 ? cfs * lbk * c.alB(e) : 0.f;
+              const float tau = e < NeZ - 1 ? cfs * ltk * c.alT(e) : 0.f;
+              const f2 ex = f2_add_f(f2{Eh[2 * l], lv[j][0]}, bu[2 * l] - beta * Jx[e] + tau * Jx[e + 1]);
+              const f2 ey = f2_add_f(f2{Eh[2 * l + 1], lv[j][1]}, bu[2 * l + 1] - beta * Jy[e] + tau * Jy[e + 1]);
+              Eh[2 * l] = ex.h;
+              *c.plo(0, e) = ex.l;
+              Eh[2 * l + 1] = ey.h;
+              *c.plo(1, e) = ey.l;
+            }
+          }
         }
       }
       active = need;
       __syncwarp();
     }
     float2 qo[2] = {ld_once(qin.v[VMX] + c.g(0), once), ld_once(qin.v[VMY] + c.g(0), once)};
+    float eo[2] = {*c.plo(0, 0), *c.plo(1, 0)};
     for (int e = 0; e < NeZ; ++e) {
       const int l = e * N1 + k;
       const size_t gi = c.g(e);
       const float2 qc[2] = {qo[0], qo[1]};
+      const float ec[2] = {eo[0], eo[1]};
       {
-        const size_t gn = c.g(e + 1 < NeZ ? e + 1 : e);
+        const int en = e + 1 < NeZ ? e + 1 : e;
+        const size_t gn = c.g(en);
         qo[0] = ld_once(qin.v[VMX] + gn, once);
         qo[1] = ld_once(qin.v[VMY] + gn, once);
+        eo[0] = *c.plo(0, en);
+        eo[1] = *c.plo(1, en);
       }
       const f2 dh = f2_of(__ldg(px.dh + l));
 #pragma unroll
       for (int m = 0; m < 2; ++m) {
         const f2 ref = f2_mul(dh, f2_of(m == 0 ? ox.Uref : ox.Vref));
-        const f2 inc = f2_of(E[2 * l + m]);  // P - q*
+        const f2 inc{Eh[2 * l + m], ec[m]};  // P - q*
         const f2 pdev = f2_add(f2_sub(f2_of(qc[m]), ref), inc);
         if constexpr (PO) {
           st_once(static_cast<float2*>(qsf[VMX + m]) + gi, f2_pack(pdev), once);
@@ -1090,6 +1120,13 @@ __global__ void __launch_bounds__(64, 5) k_vi_cols(const Ops op, const OpsX ox, 
       }
     }
     __syncwarp();
+  }
+  // the iterate's trailing-part lines of this warp's columns are dead: drop them from L2 without a
+  // write-back (one 128-byte line per plane and element)
+  for (int i = lane; i < 3 * NeZ; i += 32) {
+    const int v = i / NeZ, e = i - v * NeZ;
+    const float* a = c.lo + (size_t)v * c.lo_n + ((size_t)col0 + (size_t)e * ncol) * N1;
+    asm volatile("discard.global.L2 [%0], 128;" ::"l"(a) : "memory");
   }
 
   if (k == 0 && status) status[col] = st;
@@ -1126,7 +1163,7 @@ int launch_n(const Ops& op, const OpsX& ox, const ProfX& px, const X5& qin, cons
 
 }  // namespace
 
-size_t vi_cols_scratch_floats(size_t nodes) { return (size_t)9 * nodes; }
+size_t vi_cols_scratch_floats(size_t nodes) { return (size_t)12 * nodes; }  // G history 9, iterate 3
 
 int launch_vi_cols(int N1, const Ops& op, const OpsX& ox, const ProfX& px, const X5& qin, const F5c& z,
                    const A3& a0, const float* const* guess, void* const* qsf, void* const* tout, float* gsc, int* status,
