@@ -61,14 +61,14 @@ PATH_DTYPE = {"pair": "f32x2", "mixed": "f32+f32x2", "fp64": "f64"}
 # dram__bytes_write.sum on the 32x32x16-element slice, 8,388,608 nodes; the mean of the step's two
 # launches, one per implicit stage), per path
 NCU_BYTES_PER_NODE = {
-    "pair": {"vi_mixed": ((1063.248640e6 + 620.473856e6) + (995.027968e6 + 616.375808e6)) / 2 / (32 * 32 * 16 * 512)},
+    "pair": {"vi_mixed": ((1126.824704e6 + 656.262912e6) + (1039.029504e6 + 647.403264e6)) / 2 / (32 * 32 * 16 * 512)},
 }
 
 
 # warp instructions per node of one launch of the dominant kernel, measured by ncu
 # (smsp__inst_executed.sum on the 32x32x16-element slice, the mean of the step's two launches), per path
 NCU_INST_PER_NODE = {
-    "pair": {"vi_mixed": (1.773631250e9 + 1.717718819e9) / 2 / (32 * 32 * 16 * 512)},
+    "pair": {"vi_mixed": (1.841753748e9 + 1.782838923e9) / 2 / (32 * 32 * 16 * 512)},
 }
 
 
