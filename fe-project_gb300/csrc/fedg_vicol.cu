@@ -117,6 +117,12 @@ __device__ __forceinline__ void st_once(float* a, float v, unsigned long long po
   asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(a), "f"(v), "l"(pol) : "memory");
 }
 
+// the pressure deviation (1 + r)^kappa - 1 in FP64 where its series is out of range (|r| > rmax):
+// rare, so it is kept out of line, one copy for the whole kernel
+__device__ __noinline__ f2 pres_dev_pow(float rh, float rl, double kap64) {
+  return f2_split(pow(1.0 + ((double)rh + (double)rl), kap64) - 1.0);
+}
+
 __device__ __forceinline__ float grp_max_nan(float e, int width) {
   for (int o = width / 2; o > 0; o >>= 1) {
     const float oe = __shfl_xor_sync(FULL, e, o);
@@ -171,7 +177,7 @@ __device__ float col_residual(const OpsX& ox, const Col<N1>& c, const ProfX& px,
       for (int m = 10; m >= 1; --m) tl = fmaf(tl, rr.h, ox.cb[m]);
       S = f2_add_f(f2_mul(f2_of(ox.kap), rr), __fmul_rn(__fmul_rn(rr.h, rr.h), tl));
     } else {
-      S = f2_split(pow(1.0 + ((double)rr.h + (double)rr.l), ox.kap64) - 1.0);
+      S = pres_dev_pow(rr.h, rr.l, ox.kap64);
     }
     const f2 fm = f2_mul(f2_of(__ldg(px.ph + l)), S);
     r2[ri(s, 0, k)] = f2_pack(Pm);
@@ -181,16 +187,6 @@ __device__ float col_residual(const OpsX& ox, const Col<N1>& c, const ProfX& px,
     r2[ri(s, 4, k)] = f2_pack(Pr);
   };
 
-  {
-    float lo[3];
-    lo3(0, lo);
-    fill(0, lo);
-    if (c.NeZ > 1) {
-      lo3(1, lo);
-      fill(1, lo);
-    }
-  }
-  __syncwarp();
   float errf = 0.f;
   const int gv[3] = {VD, VMZ, VRT};
   // the stage input q* of the lane's node, loaded one element ahead so that the load latency
@@ -198,79 +194,87 @@ __device__ float col_residual(const OpsX& ox, const Col<N1>& c, const ProfX& px,
   float2 qcur[3], qnxt[3];
 #pragma unroll
   for (int v = 0; v < 3; ++v) qcur[v] = __ldg(qin.v[gv[v]] + c.g(0));
-  for (int e = 0; e < c.NeZ; ++e) {
-    const int sc = e % 3, sb = (e + 2) % 3, st = (e + 1) % 3;
-    {
-      const size_t gn = c.g(e + 1 < c.NeZ ? e + 1 : e);
+  // iterations e = -2, -1 only fill the ring with elements 0 and 1: one call site of fill for the
+  // whole loop (the kernel's code stays small for the instruction caches)
+  float lon[3];  // the trailing parts of the next element to fill, loaded one iteration ahead
+  lo3(0, lon);
+  for (int e = -2; e < c.NeZ; ++e) {
+    if (e >= 0) {
+      const int sc = e % 3, sb = (e + 2) % 3, st = (e + 1) % 3;
+      {
+        const size_t gn = c.g(e + 1 < c.NeZ ? e + 1 : e);
 #pragma unroll
-      for (int v = 0; v < 3; ++v) qnxt[v] = __ldg(qin.v[gv[v]] + gn);
-    }
-    float lon[3] = {0.f, 0.f, 0.f};  // the trailing parts of element e + 2's iterate, for its fill
-    if (e + 2 < c.NeZ) lo3(e + 2, lon);
-    // vertical-face fluxes of element e: lanes over (side, variable)
-    for (int t = k; t < 6; t += N1) {
-      const int s = t / 3, v = t - 3 * s;
-      const int nM = s == 0 ? 0 : N;
-      const bool lid = s == 0 ? (e == 0) : (e == c.NeZ - 1);
-      const int sP = lid ? sc : (s == 0 ? sb : st), nP = lid ? nM : (s == 0 ? N : 0);
-      const float nz = s == 0 ? -1.f : 1.f;
-      const float al = s == 0 ? c.alB(e) : c.alT(e);
-      // jump of RHOT (the slip lid's exterior state is the interior one: no jump)
-      const f2 dth = lid ? f2{0.f, 0.f} : f2_sub(f2_of(r2[ri(sP, 4, nP)]), f2_of(r2[ri(sc, 4, nM)]));
-      const f2 mzM = f2_of(r2[ri(sc, 0, nM)]);
-      const f2 dmz = lid ? f2_add(f2_neg(mzM), f2_neg(mzM)) : f2_sub(f2_of(r2[ri(sP, 0, nP)]), mzM);
-      f2 x;
-      if (v == 0) {
-        const f2 dr = lid ? f2{0.f, 0.f} : f2_sub(f2_of(r2[ri(sP, 1, nP)]), f2_of(r2[ri(sc, 1, nM)]));
-        x = f2_sub(f2_mul_f(dmz, nz), f2_mul_f(dr, al));
-      } else if (v == 1) {
-        const f2 dfm = lid ? f2{0.f, 0.f} : f2_sub(f2_of(r2[ri(sP, 2, nP)]), f2_of(r2[ri(sc, 2, nM)]));
-        x = f2_sub(f2_mul_f(dfm, nz), f2_mul_f(dmz, al));
-      } else {
-        const f2 frM = f2_of(r2[ri(sc, 3, nM)]);
-        const f2 dfr = lid ? f2_add(f2_neg(frM), f2_neg(frM)) : f2_sub(f2_of(r2[ri(sP, 3, nP)]), frM);
-        x = f2_sub(f2_mul_f(dfr, nz), f2_mul_f(dth, al));
+        for (int v = 0; v < 3; ++v) qnxt[v] = __ldg(qin.v[gv[v]] + gn);
       }
-      reinterpret_cast<float2*>(c.del)[t] = f2_pack(f2_mul(tmp1, x));
+      // vertical-face fluxes of element e: lanes over (side, variable)
+      for (int t = k; t < 6; t += N1) {
+        const int s = t / 3, v = t - 3 * s;
+        const int nM = s == 0 ? 0 : N;
+        const bool lid = s == 0 ? (e == 0) : (e == c.NeZ - 1);
+        const int sP = lid ? sc : (s == 0 ? sb : st), nP = lid ? nM : (s == 0 ? N : 0);
+        const float nz = s == 0 ? -1.f : 1.f;
+        const float al = s == 0 ? c.alB(e) : c.alT(e);
+        // jump of RHOT (the slip lid's exterior state is the interior one: no jump)
+        const f2 dth = lid ? f2{0.f, 0.f} : f2_sub(f2_of(r2[ri(sP, 4, nP)]), f2_of(r2[ri(sc, 4, nM)]));
+        const f2 mzM = f2_of(r2[ri(sc, 0, nM)]);
+        const f2 dmz = lid ? f2_add(f2_neg(mzM), f2_neg(mzM)) : f2_sub(f2_of(r2[ri(sP, 0, nP)]), mzM);
+        f2 x;
+        if (v == 0) {
+          const f2 dr = lid ? f2{0.f, 0.f} : f2_sub(f2_of(r2[ri(sP, 1, nP)]), f2_of(r2[ri(sc, 1, nM)]));
+          x = f2_sub(f2_mul_f(dmz, nz), f2_mul_f(dr, al));
+        } else if (v == 1) {
+          const f2 dfm = lid ? f2{0.f, 0.f} : f2_sub(f2_of(r2[ri(sP, 2, nP)]), f2_of(r2[ri(sc, 2, nM)]));
+          x = f2_sub(f2_mul_f(dfm, nz), f2_mul_f(dmz, al));
+        } else {
+          const f2 frM = f2_of(r2[ri(sc, 3, nM)]);
+          const f2 dfr = lid ? f2_add(f2_neg(frM), f2_neg(frM)) : f2_sub(f2_of(r2[ri(sP, 3, nP)]), frM);
+          x = f2_sub(f2_mul_f(dfr, nz), f2_mul_f(dth, al));
+        }
+        reinterpret_cast<float2*>(c.del)[t] = f2_pack(f2_mul(tmp1, x));
+      }
+      __syncwarp();
+      {
+        const int l = e * N1 + k;
+        const float isc[3] = {1.f / __ldg(px.dhf + l), 1.f / (__ldg(px.dhf + l) * cref), 1.f / __ldg(px.rhf + l)};
+        float bfl[3];
+        f2acc sd, sm, sr, drho;
+#pragma unroll
+        for (int m = 0; m < N1; ++m) {
+          sd.add(Dk[m], f2_of(r2[ri(sc, 0, m)]));
+          drho.add(Tk[m], f2_of(r2[ri(sc, 1, m)]));
+          sm.add(Dk[m], f2_of(r2[ri(sc, 2, m)]));
+          sr.add(Dk[m], f2_of(r2[ri(sc, 3, m)]));
+        }
+        const float2* dl = reinterpret_cast<const float2*>(c.del);
+        f2 A[3];
+        A[0] = f2_add(f2_add(f2_mul(E33, sd.get()), f2_mul(lbk, f2_of(dl[0]))), f2_mul(ltk, f2_of(dl[3])));
+        A[1] = f2_add(f2_add(f2_add(f2_mul(E33, sm.get()), f2_mul(lbk, f2_of(dl[1]))), f2_mul(ltk, f2_of(dl[4]))),
+                      f2_mul(grav, drho.get()));
+        A[2] = f2_add(f2_add(f2_mul(E33, sr.get()), f2_mul(lbk, f2_of(dl[2]))), f2_mul(ltk, f2_of(dl[5])));
+        // this node's iterate from the ring: DDENS (quantity 1), MOMZ (0), DRHOT (4)
+        const f2 Pl[3] = {f2_of(r2[ri(sc, 1, k)]), f2_of(r2[ri(sc, 0, k)]), f2_of(r2[ri(sc, 4, k)])};
+#pragma unroll
+        for (int v = 0; v < 3; ++v) {  // A[v] holds -A: b = q* - P - impl_fac (-A)
+          const f2 qmp = f2_sub(f2_of(qcur[v]), Pl[v]);
+          bfl[v] = f2_to_f(f2_sub(qmp, f2_mul(impl, A[v])));
+        }
+#pragma unroll
+        for (int v = 0; v < 3; ++v) {
+          c.Bf[3 * l + v] = bfl[v];
+          errf = fmaxf(errf, fabsf(bfl[v]) * isc[v]);
+          if (!(fabsf(bfl[v]) < 3.0e38f)) errf = __int_as_float(0x7fc00000);
+        }
+      }
+      __syncwarp();
+#pragma unroll
+      for (int v = 0; v < 3; ++v) qcur[v] = qnxt[v];
+    }
+    if (e + 2 < c.NeZ) {
+      const float lcur[3] = {lon[0], lon[1], lon[2]};
+      if (e + 3 < c.NeZ) lo3(e + 3, lon);
+      fill(e + 2, lcur);
     }
     __syncwarp();
-    {
-      const int l = e * N1 + k;
-      const float isc[3] = {1.f / __ldg(px.dhf + l), 1.f / (__ldg(px.dhf + l) * cref), 1.f / __ldg(px.rhf + l)};
-      float bfl[3];
-      f2acc sd, sm, sr, drho;
-#pragma unroll
-      for (int m = 0; m < N1; ++m) {
-        sd.add(Dk[m], f2_of(r2[ri(sc, 0, m)]));
-        drho.add(Tk[m], f2_of(r2[ri(sc, 1, m)]));
-        sm.add(Dk[m], f2_of(r2[ri(sc, 2, m)]));
-        sr.add(Dk[m], f2_of(r2[ri(sc, 3, m)]));
-      }
-      const float2* dl = reinterpret_cast<const float2*>(c.del);
-      f2 A[3];
-      A[0] = f2_add(f2_add(f2_mul(E33, sd.get()), f2_mul(lbk, f2_of(dl[0]))), f2_mul(ltk, f2_of(dl[3])));
-      A[1] = f2_add(f2_add(f2_add(f2_mul(E33, sm.get()), f2_mul(lbk, f2_of(dl[1]))), f2_mul(ltk, f2_of(dl[4]))),
-                    f2_mul(grav, drho.get()));
-      A[2] = f2_add(f2_add(f2_mul(E33, sr.get()), f2_mul(lbk, f2_of(dl[2]))), f2_mul(ltk, f2_of(dl[5])));
-      // this node's iterate from the ring: DDENS (quantity 1), MOMZ (0), DRHOT (4)
-      const f2 Pl[3] = {f2_of(r2[ri(sc, 1, k)]), f2_of(r2[ri(sc, 0, k)]), f2_of(r2[ri(sc, 4, k)])};
-#pragma unroll
-      for (int v = 0; v < 3; ++v) {  // A[v] holds -A: b = q* - P - impl_fac (-A)
-        const f2 qmp = f2_sub(f2_of(qcur[v]), Pl[v]);
-        bfl[v] = f2_to_f(f2_sub(qmp, f2_mul(impl, A[v])));
-      }
-#pragma unroll
-      for (int v = 0; v < 3; ++v) {
-        c.Bf[3 * l + v] = bfl[v];
-        errf = fmaxf(errf, fabsf(bfl[v]) * isc[v]);
-        if (!(fabsf(bfl[v]) < 3.0e38f)) errf = __int_as_float(0x7fc00000);
-      }
-    }
-    __syncwarp();
-    if (e + 2 < c.NeZ) fill(e + 2, lon);
-    __syncwarp();
-#pragma unroll
-    for (int v = 0; v < 3; ++v) qcur[v] = qnxt[v];
   }
   return grp_max_nan(errf, N1);
 }
