@@ -119,9 +119,27 @@ __device__ __forceinline__ void filter_store(const OpsP& op, float2* fa, float2*
 template <int N1, int EPB, int STAGE, bool HEVE = false>
 __global__ void __launch_bounds__(EPB* N1* N1* N1)
     k_stage_pair(const OpsP op, const ProfP pf, const double* __restrict__ dens64, const StagePairBufs B,
-                 const PairCoef cf, int Ne, int filter_on, int ke0) {
+                 const PairCoef cf, int Ne, int filter_on, int ke0, int pf_next) {
   constexpr int Np = N1 * N1 * N1, NF = N1 * N1;
   extern __shared__ float2 smp[];
+  // One block per SM leaves the latency of an element's loads uncovered when the block starts: ask
+  // L2 now for the fields of the block that will follow this one on the SM (pf_next elements on,
+  // the grid's resident width), one bulk prefetch per field and element range.
+  if (pf_next > 0 && threadIdx.x < 25) {
+    const int kn0 = ke0 + blockIdx.x * EPB + pf_next;
+    if (kn0 < Ne) {
+      const size_t off = (size_t)kn0 * Np;
+      const unsigned bytes = (unsigned)((Ne - kn0 < EPB ? Ne - kn0 : EPB) * Np * 8);
+      const int t = threadIdx.x, f = t % 5;
+      const void* src = nullptr;
+      if (t < 5) src = B.qs[f] + off;
+      else if (t < 10) src = B.qn[f] + off;
+      else if (t < 15 && !HEVE && STAGE >= 2) src = B.TI[f] + off;
+      else if (t < 20 && !HEVE && STAGE == 2) src = B.S3[f] + off;
+      else if (t < 25 && !HEVE && STAGE >= 2) src = B.SF[f] + off;
+      if (src) asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+    }
+  }
   float2* s_st = smp;                       // [EPB][6][Np]
   float2* s_fl = s_st + EPB * 6 * Np;       // [EPB][15][Np]
   float2* s_df = s_fl + EPB * 15 * Np;      // [EPB][5][6NF]
@@ -465,7 +483,14 @@ int launch_pair_n(const OpsP& op, const ProfP& pf, const double* dens64, const S
   auto kfn = k_stage_pair<N1, EPB, STAGE, HEVE>;
   cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (Ne <= ke0) return (int)cudaSuccess;
-  kfn<<<(Ne - ke0 + EPB - 1) / EPB, EPB * Np, smem, s>>>(op, pf, dens64, B, cf, Ne, filt, ke0);
+  // the grid's resident width in elements: the block that follows a block on its SM starts about
+  // that many elements further on
+  int dev = 0, nsm = 0, nb = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kfn, EPB * Np, smem);
+  const int pf_next = nsm * nb * EPB;
+  kfn<<<(Ne - ke0 + EPB - 1) / EPB, EPB * Np, smem, s>>>(op, pf, dens64, B, cf, Ne, filt, ke0, pf_next);
   return (int)cudaGetLastError();
 }
 
