@@ -119,9 +119,27 @@ __device__ __forceinline__ void face_neighbour(const OpsF& op, int f, int ke, in
 template <int N1, int EPB, int STAGE>
 __global__ void __launch_bounds__(EPB* N1* N1* N1)
     k_stage_mixed(const OpsF op, const ProfF pf, const double* __restrict__ dens64, const StageBufs B,
-                  const MixCoef cf, int Ne, int filter_on) {
+                  const MixCoef cf, int Ne, int filter_on, int pf_next) {
   constexpr int Np = N1 * N1 * N1, NF = N1 * N1, N = N1 - 1;
   using G = TcGeom<N1, EPB>;
+  // one bulk L2 prefetch per field of the block that will follow this one on its SM (pf_next
+  // elements on): its start-of-element loads then hit L2
+  if (pf_next > 0 && threadIdx.x < 25) {
+    const int kn0 = blockIdx.x * EPB + pf_next;
+    if (kn0 < Ne) {
+      const size_t off = (size_t)kn0 * Np;
+      const unsigned n = (unsigned)((Ne - kn0 < EPB ? Ne - kn0 : EPB) * Np);
+      const int t = threadIdx.x, f = t % 5;
+      const void* src = nullptr;
+      unsigned bytes = 4 * n;
+      if (t < 5) src = B.qsf[f] + off;
+      else if (t < 10) { src = B.qn[f] + off; bytes = 8 * n; }
+      else if (t < 15 && STAGE >= 2) src = B.TI[f] + off;
+      else if (t < 20 && STAGE == 2) src = B.S3[f] + off;
+      else if (t < 25 && STAGE >= 2) src = B.SF[f] + off;
+      if (src) asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+    }
+  }
   extern __shared__ __align__(1024) unsigned char smraw[];
   uint32_t* s_a = reinterpret_cast<uint32_t*>(smraw);                 // A_hi [TILES*128][8], then A_lo
   uint32_t* s_b = reinterpret_cast<uint32_t*>(smraw + G::A_BYTES);    // [D_hi | D_lo] [16][8], then [D_hi | 0]
@@ -608,7 +626,12 @@ static int launch_stage_n(const OpsF& op, const ProfF& pf, const double* dens64,
   const size_t smem = G::A_BYTES + G::B_BYTES + sizeof(float) * EPB * (6 * Np + 5 * 6 * NF + 5 * 2 * NF) + 16;
   auto kfn = k_stage_mixed<N1, EPB, STAGE>;
   cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  kfn<<<(Ne + EPB - 1) / EPB, EPB * Np, smem, s>>>(op, pf, dens64, B, cf, Ne, filt);
+  // the grid's resident width in elements (the next block on an SM starts about that far on)
+  int dev = 0, nsm = 0, nb = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kfn, EPB * Np, smem);
+  kfn<<<(Ne + EPB - 1) / EPB, EPB * Np, smem, s>>>(op, pf, dens64, B, cf, Ne, filt, nsm * nb * EPB);
   return (int)cudaGetLastError();
 }
 
