@@ -19,14 +19,20 @@
 //     fedg_f2.cuh); the convergence test is on the residual b = impl_fac A(P) + q* - P with the
 //     operator evaluated in float pairs ("certifying" residual), so the column reaches the
 //     FP64-class Newton solution while the kernel issues no FP64 arithmetic on its main path;
-//   - the first correction of every column uses the split residual (FP32 operator, q* - P in pairs);
+//   - from var0, the first residual comes from the stage-1 kernel's A(var0) (no operator pass);
 //   - Jacobian, block-Thomas and the element LU (no pivoting: I + impl_fac J is diagonally
-//     dominant at stable time steps; a failure shows as a non-converging or non-finite FP64
-//     residual, reported per column) are FP32;
+//     dominant at stable time steps; a failure shows as a non-converging or non-finite certifying
+//     residual, reported per column) are FP32; after an LU correction, Neumann corrections;
 //   - MOMX/MOMY: the element blocks are I plus two rank-one face terms, so the system reduces
 //     exactly to a scalar tridiagonal system in the NeZ-1 interface jumps, solved in FP32; the
 //     residual (FP64 jumps and q* - P, FP32 operator) is accurate far below the tolerance
 //     because the operator only sees the jumps.
+//
+// Memory: per column in shared memory the leading parts of P, the FP32 work vector and the
+// per-phase scratch (4.26 KB at p = 7, NeZ = 16: 12 warps per SM); in global memory, L2-resident
+// while the column is in flight and discarded from L2 after their last use, the block-Thomas
+// history and the trailing parts of P.  Data read or written once per launch carries an L2
+// evict-first policy.
 #include <algorithm>
 
 #include "fedg_ctx.cuh"
