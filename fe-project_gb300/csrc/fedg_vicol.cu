@@ -24,9 +24,10 @@
 //     dominant at stable time steps; a failure shows as a non-converging or non-finite certifying
 //     residual, reported per column) are FP32; after an LU correction, Neumann corrections;
 //   - MOMX/MOMY: the element blocks are I plus two rank-one face terms, so the system reduces
-//     exactly to a scalar tridiagonal system in the NeZ-1 interface jumps, solved in FP32; the
-//     residual (FP64 jumps and q* - P, FP32 operator) is accurate far below the tolerance
-//     because the operator only sees the jumps.
+//     exactly to a scalar tridiagonal system in the NeZ-1 interface jumps, solved in FP32 and
+//     accumulated into E = P - q* in pairs; the residual (the jumps of q* formed in pairs, E in
+//     pairs, the operator in FP32) is accurate far below the tolerance because the operator only
+//     sees the jumps.
 //
 // Memory: per column in shared memory the leading parts of P, the FP32 work vector and the
 // per-phase scratch (4.26 KB at p = 7, NeZ = 16: 12 warps per SM); in global memory, L2-resident
