@@ -108,7 +108,7 @@ def test_structured_lu_needs_the_sparsity():
 
 
 def dfirst_pivoting_solve(A, R, N1, rows_out=None):
-    """The FP64 kernel's variant (fe-project_gb300/csrc/fedg_vi.cu, warp_lu_dfirst): the same DENS-first
+    """The FP64 kernel's variant (fe-project_gb300/csrc/fedg_vi.cu, blk_fwd / blk_bwd): the same DENS-first
     column order, every DENS column pivoted on its own DENS row, the MOMZ/RHOT columns with partial
     pivoting over the rows not yet pivoted (largest |a|, lowest row on ties); the back substitution
     in reverse step order."""
@@ -167,6 +167,96 @@ def test_dfirst_lu_with_pivoting_solves_the_dens_sparse_block(N1, seed):
     ref = np.linalg.solve(A, R)
     assert np.max(np.abs(X - ref)) <= 1e-10 * max(1.0, np.max(np.abs(ref)))
     assert any(rows[s] != col(s, N1) for s in range(N1, n))  # rows were exchanged
+
+
+def dens_sparse_block(rng, N1):
+    """A random element block with the DENS rows' sparsity and an FP64-kernel-like conditioning: a
+    dominant DENS diagonal, a weak MOMZ diagonal (the MOMZ/RHOT phase exchanges rows)."""
+    n, N = 3 * N1, N1 - 1
+    A = rng.standard_normal((n, n))
+    for k in range(N1):
+        A[3 * k, :] *= 0.1
+        A[3 * k, 3 * k] = 3.0
+        for c in range(n):
+            if not (c == 3 * k or c == 0 or c == 3 * N or c % 3 == 1 or c == 2):
+                A[3 * k, c] = 0.0
+        A[3 * k + 1, 3 * k + 1] = 1e-9
+    return A
+
+
+def two_column_kernel_solve(A, R, N1, zeros_out=None):
+    """The FP64 kernel's elimination with the skips of its two-columns-per-warp form (fedg_vi.cu:
+    blk_fwd, blk_bwd): the DENS rows eliminate only at step 0; their pivots' reciprocals are formed
+    once their rows are final; the column-oriented back substitution updates a DENS row only at the
+    MOMZ columns, RHOT_0 and DENS_N, and scales the DENS rows of nodes below N together after the
+    DENS_N update.  zeros_out collects the entries the skips assume to be exact zeros."""
+    n, N = 3 * N1, N1 - 1
+    a, r = A.copy(), R.copy().astype(float)
+    done = np.zeros(n, bool)
+    piv_row = np.zeros(n, int)
+    for s in range(n):
+        pc = col(s, N1)
+        if s < N1:
+            p = pc
+        else:
+            cand = [row for row in range(n) if not done[row] and row % 3 != 0]
+            p = max(cand, key=lambda row: (abs(a[row, pc]), -row))
+        piv_row[s] = p
+        inv = 1.0 / a[p, pc]
+        for row in range(n):
+            if done[row] or row == p:
+                continue
+            if row % 3 == 0 and s > 0:  # a DENS row: skipped past step 0
+                if zeros_out is not None:
+                    zeros_out.append(a[row, pc])
+                continue
+            f = a[row, pc] * inv
+            for c in range(n):
+                if nz(s, c, N1):
+                    a[row, c] -= f * a[p, c]
+            r[row] -= f * r[p]
+        done[p] = True
+    mypiv = {piv_row[s]: s for s in range(n)}
+    for s in range(n - 1, -1, -1):  # column-oriented: scale the pivot row, then update the rows above it
+        pc, p = col(s, N1), piv_row[s]
+        if s >= N1 or s == N:
+            r[p] = r[p] / a[p, pc]
+        for row in range(n):
+            if mypiv[row] >= s:
+                continue
+            dens_row = row % 3 == 0
+            if dens_row and s >= N1 and not (pc % 3 == 1 or pc == 2):
+                if zeros_out is not None:
+                    zeros_out.append(a[row, pc])
+                continue
+            if dens_row and s < N and s > 0:
+                if zeros_out is not None:
+                    zeros_out.append(a[row, pc])
+                continue
+            r[row] -= a[row, pc] * r[p]
+        if s == N:  # the DENS rows of the nodes below N are final: scale them together
+            for k in range(N):
+                r[3 * k] = r[3 * k] / a[3 * k, 3 * k]
+    x = np.zeros_like(r)
+    for s in range(n):
+        x[col(s, N1)] = r[piv_row[s]]
+    return x
+
+
+@pytest.mark.parametrize("N1", [2, 3, 4, 8])
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_two_column_kernel_skips_only_exact_zeros(N1, seed):
+    """The skips of the two-columns-per-warp FP64 kernel touch only entries that are exactly zero, so
+    the kernel's arithmetic is the full DENS-first elimination's (its results are bit-identical to the
+    one-column kernel's); and the restated skips still solve the block to roundoff."""
+    rng = np.random.default_rng(seed)
+    A = dens_sparse_block(rng, N1)
+    R = rng.standard_normal((3 * N1, 4))
+    zeros = []
+    X = two_column_kernel_solve(A, R, N1, zeros_out=zeros)
+    assert zeros and all(z == 0.0 for z in zeros)
+    ref = np.linalg.solve(A, R)
+    assert np.max(np.abs(X - ref)) <= 1e-10 * max(1.0, np.max(np.abs(ref)))
 
 
 def blocked_solve(A, R, N1):
