@@ -195,6 +195,7 @@ __device__ float col_residual(const OpsX& ox, const Col<N1>& c, const ProfX& px,
   };
 
   float errf = 0.f;
+  bool bad = false;  // a non-finite entry anywhere makes the column's error NaN (fmaxf drops NaNs)
   const int gv[3] = {VD, VMZ, VRT};
   // the stage input q* of the lane's node, loaded one element ahead so that the load latency
   // overlaps the current element's work
@@ -269,7 +270,7 @@ __device__ float col_residual(const OpsX& ox, const Col<N1>& c, const ProfX& px,
         for (int v = 0; v < 3; ++v) {
           c.Bf[3 * l + v] = bfl[v];
           errf = fmaxf(errf, fabsf(bfl[v]) * isc[v]);
-          if (!(fabsf(bfl[v]) < 3.0e38f)) errf = __int_as_float(0x7fc00000);
+          bad = bad || !(fabsf(bfl[v]) < 3.0e38f);
         }
       }
       __syncwarp();
@@ -283,7 +284,7 @@ __device__ float col_residual(const OpsX& ox, const Col<N1>& c, const ProfX& px,
     }
     __syncwarp();
   }
-  return grp_max_nan(errf, N1);
+  return grp_max_nan(bad ? __int_as_float(0x7fc00000) : errf, N1);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1011,6 +1012,7 @@ __global__ void __launch_bounds__(64, 6) k_vi_cols(const Ops op, const OpsX ox, 
     bool active = true;
     for (int it = 0; it < 4; ++it) {
       float err = 0.f;
+      bool bad = false;
       float el[2] = {*c.plo(0, 0), *c.plo(1, 0)};  // trailing parts of E, one element ahead
       for (int e = 0; e < NeZ; ++e) {
         const float ec[2] = {el[0], el[1]};
@@ -1035,11 +1037,11 @@ __global__ void __launch_bounds__(64, 6) k_vi_cols(const Ops op, const OpsX ox, 
           const float b = (Af - Eh[2 * l + m]) - ec[m];
           bu[2 * l + m] = b;
           err = fmaxf(err, fabsf(b) * iscu);
-          if (!(fabsf(b) < 3.0e38f)) err = __int_as_float(0x7fc00000);
+          bad = bad || !(fabsf(b) < 3.0e38f);
         }
         __syncwarp();
       }
-      err = grp_max_nan(err, N1);
+      err = grp_max_nan(bad ? __int_as_float(0x7fc00000) : err, N1);
       const bool need = active && !(err <= args.tol) && it < 3;
       if (!__any_sync(FULL, need)) break;
       // interface jumps J_e = d_e0 - d_{e-1,N} (e = 1..NeZ-1) from the scalar tridiagonal system
