@@ -41,6 +41,9 @@ def small_cases():
         "p7_C2_4x4x4": cases.C2().scaled(4, 4, 4),
         "p7_C5_4x4x4": cases.C5().scaled(4, 4, 4),
         "p2_3x2x5": cases.C1().scaled(3, 2, 5, porder=2),
+        # 27 columns: the FP64 column solve's two-columns-per-warp mapping leaves the last half-warp
+        # without a column of its own
+        "p2_3x1x4_odd_columns": cases.C1().scaled(3, 1, 4, porder=2),
     }
 
 
@@ -99,7 +102,7 @@ def test_drhot2pres_and_filter(name):
     assert max(relerr(g, r) for g, r in zip(got, ref)) < 1e-13
 
 
-@pytest.mark.parametrize("name", ["p3_C1", "p7_C2_4x4x4", "p7_C5_4x4x4", "p2_3x2x5"])
+@pytest.mark.parametrize("name", ["p3_C1", "p7_C2_4x4x4", "p7_C5_4x4x4", "p2_3x2x5", "p2_3x1x4_odd_columns"])
 @pytest.mark.parametrize("mode", ["ref1", "iter", "zero"])
 def test_cal_vi(name, mode):
     case = small_cases()[name]
