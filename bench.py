@@ -240,7 +240,7 @@ def fp64_dgemm_tflops(torch, dev):
 
 
 def c4_guess_bench(np, torch, fl, cases, stream, nsteps=10):
-    """BASELINE's learned-guess configuration: the C2 geometry (p = 7, 800 m elements, 64 levels per
+    """The learned-guess workload (C4): the C2 geometry (p = 7, 800 m elements, 64 levels per
     column: 193 -> 256 -> 256 -> 192), trained with Adam (lr 1e-3, batch 4096) on 204,800 (column state,
     converged increment) pairs that the plain solver generates from 20 seeds of random bubbles and
     winds; then, on a held-out seed, the mean Newton solves per implicit column solve and ms per step
