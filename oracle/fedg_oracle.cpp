@@ -42,7 +42,7 @@
 //
 // The Newton solve of cal_vi has two modes: max_iter = 1 restates FElib exactly (one
 // linearised solve from the guess var0); max_iter > 1 iterates the same Newton step
-// until the scaled update is below tol (the iterated method this build adds).
+// until the scaled update is below tol (an iterated mode beyond FElib's single solve).
 
 #include <cmath>
 #include <cstdio>
