@@ -14,6 +14,12 @@
 // of SCALE, which the reference tree does not vendor): qdry = 1 - sum_q q MASS_q, Rtot = sum_q q R_q +
 // qdry Rdry, and the same for CV and CP.
 // Element integrals use the LGL quadrature of the flat cube: Gsqrt J w_i w_j w_k with Gsqrt = 1.
+//
+// Also the driver's update_pressure_specific_heat (driver_trcadv3d.F90:653-716), which precedes the
+// fixer: the mixture's Rtot, CVtot, CPtot from the tracers and PRES from DRHOT with them
+// (calc_pressure -> atm_dyn_dgm_nonhydro3d_common_DRHOT2PRES, nonhydro3d_common.F90:428-479:
+// PRES = P00 (Rtot (THERM_hyd + DRHOT) / P00)^(CPtot / CVtot), DPRES = PRES - PRES_hyd).
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -135,8 +141,79 @@ __global__ void __launch_bounds__(512) k_negative_fixer(const Ops op, const NegF
                  op.pres00 / op.rdry * pow(A.pres_hyd[g] / op.pres00, op.cvdry / op.cpdry);
 }
 
+struct HeatArgs {
+  const double* q[MAXQA];
+  double mass[MAXQA], r[MAXQA], cv[MAXQA], cp[MAXQA];
+  int QA;
+  const double* drhot;
+  const double* pres_hyd;
+  const double* therm_hyd;
+  double* rtot;
+  double* cvtot;
+  double* cptot;
+  double* pres;
+  double* dpres;  // or NULL
+};
+
+// update_pressure_specific_heat, node by node: the mixture's Rtot, CVtot, CPtot, then PRES from
+// RHOT = THERM_hyd + DRHOT with the mixture's exponent
+__global__ void __launch_bounds__(256) k_specific_heat_pressure(const Ops op, const HeatArgs A, size_t n) {
+  for (size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x; g < n; g += (size_t)gridDim.x * blockDim.x) {
+    double qdry = 1.0, r = 0.0, cv = 0.0, cp = 0.0;
+#pragma unroll
+    for (int iq = 0; iq < MAXQA; ++iq) {
+      if (iq < A.QA) {
+        const double q = A.q[iq][g];
+        qdry = qdry - q * A.mass[iq];
+        r = r + q * A.r[iq];
+        cv = cv + q * A.cv[iq];
+        cp = cp + q * A.cp[iq];
+      }
+    }
+    const double Rt = r + qdry * op.rdry, CVt = cv + qdry * op.cvdry, CPt = cp + qdry * op.cpdry;
+    A.rtot[g] = Rt;
+    A.cvtot[g] = CVt;
+    A.cptot[g] = CPt;
+    const double rhot = A.therm_hyd[g] + A.drhot[g];
+    const double pres = op.pres00 * pow(Rt * (1.0 / op.pres00) * rhot, CPt / CVt);
+    A.pres[g] = pres;
+    if (A.dpres) A.dpres[g] = pres - A.pres_hyd[g];
+  }
+}
+
 }  // namespace
 }  // namespace fedg
+
+extern "C" int fedg_trc_specific_heat_pressure(fedg_ctx* c, const double* const* QTRC, int QA, const double* trc_mass,
+                                               const double* trc_r, const double* trc_cv, const double* trc_cp,
+                                               const double* DRHOT, const double* PRES_hyd, const double* THERM_hyd,
+                                               double* Rtot, double* CVtot, double* CPtot, double* PRES,
+                                               double* DPRES) {
+  if (!c || !QTRC || !trc_mass || !trc_r || !trc_cv || !trc_cp || !DRHOT || !PRES_hyd || !THERM_hyd || !Rtot ||
+      !CVtot || !CPtot || !PRES)
+    return api_fail("fedg_trc_specific_heat_pressure: null argument");
+  if (QA < 0 || QA > MAXQA) return api_fail("fedg_trc_specific_heat_pressure: QA must be 0..16");
+  HeatArgs A{};
+  for (int iq = 0; iq < QA; ++iq) {
+    if (!QTRC[iq]) return api_fail("fedg_trc_specific_heat_pressure: null tracer field");
+    A.q[iq] = QTRC[iq];
+    A.mass[iq] = trc_mass[iq];
+    A.r[iq] = trc_r[iq];
+    A.cv[iq] = trc_cv[iq];
+    A.cp[iq] = trc_cp[iq];
+  }
+  A.QA = QA;
+  A.drhot = DRHOT; A.pres_hyd = PRES_hyd; A.therm_hyd = THERM_hyd;
+  A.rtot = Rtot; A.cvtot = CVtot; A.cptot = CPtot; A.pres = PRES; A.dpres = DPRES;
+  cudaSetDevice(c->d.device);
+  const size_t n = c->n;
+  const int grid = (int)std::min<size_t>((n + 255) / 256, (size_t)152 * 16);
+  const int r = tracked(c, FEDG_K_TRC_AUX, [&] {
+    k_specific_heat_pressure<<<grid, 256, 0, c->stream>>>(c->op, A, n);
+    return (int)cudaGetLastError();
+  });
+  return r ? api_cuda_fail((cudaError_t)r, "fedg_trc_specific_heat_pressure") : 0;
+}
 
 extern "C" int fedg_trc_negative_fixer(fedg_ctx* c, double* const* QTRC, int QA, int QLA, int QIA,
                                        const double* trc_mass, const double* trc_r, const double* trc_cv,

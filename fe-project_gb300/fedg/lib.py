@@ -33,7 +33,8 @@ EXPORTED = [
     "fedg_guess_set_params", "fedg_guess_get_params", "fedg_guess_train_step", "fedg_guess_loss_grad",
     "fedg_guess_predict", "fedg_guess_load", "fedg_cal_tend_ex_noalloc",
     "fedg_trc_alphdens_advtest", "fedg_trc_save_massflux", "fedg_trc_fct_coef", "fedg_trc_cal_tend",
-    "fedg_trc_tmar", "fedg_trc_modalfilter", "fedg_trc_update", "fedg_trc_negative_fixer", "fedg_numdiff_apply",
+    "fedg_trc_tmar", "fedg_trc_modalfilter", "fedg_trc_update", "fedg_trc_negative_fixer",
+    "fedg_trc_specific_heat_pressure", "fedg_numdiff_apply",
     "fedg_sponge_add_tend",
     "fedg_update_set_tracer_flux", "fedg_update_set_sponge", "fedg_numdiff_apply_prec",
     "fedg_guess_set_wait_limit", "fedg_update_set_vi_neumann", "fedg_update_set_wait_limit",
@@ -155,6 +156,8 @@ def load():
     _dp = ctypes.POINTER(ctypes.c_double)
     lib.fedg_trc_negative_fixer.argtypes = [_vp, ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int,
                                             ctypes.c_int, _dp, _dp, _dp, _dp] + [_vp] * 8 + [ctypes.c_double]
+    lib.fedg_trc_specific_heat_pressure.argtypes = [_vp, ctypes.POINTER(ctypes.c_void_p), ctypes.c_int,
+                                                    _dp, _dp, _dp, _dp] + [_vp] * 8
     lib.fedg_trc_modalfilter.argtypes = [_vp, _vp, _vp, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                          ctypes.c_double, ctypes.c_double, ctypes.c_int]
     lib.fedg_trc_update.argtypes = [_vp, _vp, _P3, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.POINTER(TrcOpts)]
@@ -448,12 +451,26 @@ class Context:
         cptot, rtot and drhot (or None); mass/r/cv/cp: the QA tracer property values"""
         qa = len(qtrc)
         qp = (ctypes.c_void_p * qa)(*[t.data_ptr() for t in qtrc])
-        tab = [(ctypes.c_double * qa)(*[float(x) for x in a]) for a in (mass, r, cv, cp)]
+        tab = [(ctypes.c_double * qa)(*[float(x) for x in list(a)[:qa]]) for a in (mass, r, cv, cp)]
         self.torch.cuda.synchronize()
         _check(self.lib.fedg_trc_negative_fixer(self.h, qp, qa, int(qla), int(qia), *tab, _ptr(ddens), _ptr(pres),
                                                 _ptr(cvtot), _ptr(cptot), _ptr(rtot), _ptr(dens_hyd),
                                                 _ptr(pres_hyd), _ptr(drhot), float(dt)),
                "fedg_trc_negative_fixer")
+        self.sync()
+
+    def trc_specific_heat_pressure(self, qtrc, mass, r, cv, cp, drhot, pres_hyd, therm_hyd, rtot, cvtot, cptot, pres,
+                                   dpres=None):
+        """fedg_trc_specific_heat_pressure: Rtot, CVtot, CPtot, PRES (and DPRES) from the device tensors
+        qtrc (list of QA) and DRHOT"""
+        qa = len(qtrc)
+        qp = (ctypes.c_void_p * max(qa, 1))(*[t.data_ptr() for t in qtrc])
+        tab = [(ctypes.c_double * max(qa, 1))(*[float(x) for x in list(a)[:qa]]) for a in (mass, r, cv, cp)]
+        self.torch.cuda.synchronize()
+        _check(self.lib.fedg_trc_specific_heat_pressure(self.h, qp, qa, *tab, _ptr(drhot), _ptr(pres_hyd),
+                                                        _ptr(therm_hyd), _ptr(rtot), _ptr(cvtot), _ptr(cptot),
+                                                        _ptr(pres), _ptr(dpres)),
+               "fedg_trc_specific_heat_pressure")
         self.sync()
 
     def trc_modalfilter(self, Q, ddens, etac_h=2.0 / 3.0, alpha_h=36.0, ord_h=16, etac_v=2.0 / 3.0, alpha_v=36.0,

@@ -329,6 +329,17 @@ int fedg_trc_update(fedg_ctx* ctx, double* QTRC, const double* const mflx[3], co
                     const double* alph_P, const double* DDENS_TRC, const double* DDENS0_TRC, const double* DDENS,
                     const double* RHOQ_tp, const fedg_trc_opts* opts);
 
+/* update_pressure_specific_heat (FElib/src/fluid_dyn_solver/scale_atm_dyn_dgm_driver_trcadv3d.F90:653-716),
+ * which the tracer driver runs after the tracer step and before the negative fixer: the mixture's Rtot,
+ * CVtot, CPtot from the QA tracers (SCALE's mixing rule, as for the fixer) and, through calc_pressure
+ * (atm_dyn_dgm_nonhydro3d_common_DRHOT2PRES, nonhydro3d_common.F90:428-479),
+ * PRES = P00 (Rtot (THERM_hyd + DRHOT) / P00)^(CPtot / CVtot) and DPRES = PRES - PRES_hyd (DPRES may be
+ * NULL).  QA <= 16 (0: the dry constants); tracer tables as for fedg_trc_negative_fixer; device arrays. */
+int fedg_trc_specific_heat_pressure(fedg_ctx* ctx, const double* const* QTRC, int QA, const double* trc_mass,
+                                    const double* trc_r, const double* trc_cv, const double* trc_cp,
+                                    const double* DRHOT, const double* PRES_hyd, const double* THERM_hyd,
+                                    double* Rtot, double* CVtot, double* CPtot, double* PRES, double* DPRES);
+
 /* atm_phy_mp_dgm_common_negative_fixer (FElib/src/microphysics/scale_atm_phy_mp_dgm_common.F90:429-556),
  * which the tracer driver runs after the tracer step (fix_negative_val, driver_trcadv3d.F90:550,
  * 596-651), in place, FP64.  Per element, each water species iq = 0 .. QLA+QIA has its mass DENS q

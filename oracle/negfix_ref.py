@@ -68,3 +68,17 @@ def negative_fixer(qtrc, ddens, pres, cvtot, cptot, rtot, dens_hyd, pres_hyd, dr
     if drhot is not None:                                     # :549-552
         dr = pres00 / rt * (p / pres00) ** (cvt / cpt) - pres00 / rdry * (pres_hyd / pres00) ** (cvdry / cpdry)
     return qnew, ddens, p, cvt, cpt, rt, dr
+
+
+def specific_heat_pressure(qtrc, drhot, pres_hyd, therm_hyd, mass, r, cv, cp, rdry, cvdry, cpdry, pres00):
+    """update_pressure_specific_heat (FElib/src/fluid_dyn_solver/scale_atm_dyn_dgm_driver_trcadv3d.F90:
+    653-716): the mixture's (Rtot, CVtot, CPtot) and, through atm_dyn_dgm_nonhydro3d_common_DRHOT2PRES
+    (nonhydro3d_common.F90:470-474), PRES = P00 (Rtot / P00 (THERM_hyd + DRHOT))^(CPtot / CVtot) and
+    DPRES = PRES - PRES_hyd.  qtrc: (QA, ...) or an empty list (the dry constants)."""
+    shape = np.shape(drhot)
+    q = np.asarray(qtrc, dtype=np.float64).reshape((len(qtrc),) + shape) if len(qtrc) else np.zeros((1,) + shape)
+    tabs = (mass, r, cv, cp) if len(qtrc) else ([0.0], [0.0], [0.0], [0.0])
+    _, rt, cvt, cpt = specific_heat(q, *tabs, rdry, cvdry, cpdry)
+    rhot = therm_hyd + drhot
+    pres = pres00 * (rt * (1.0 / pres00) * rhot) ** (cpt / cvt)
+    return rt, cvt, cpt, pres, pres - pres_hyd

@@ -60,3 +60,27 @@ def test_negative_fixer_refusals():
     with pytest.raises(fl.FedgError, match="1 \\+ QLA \\+ QIA"):
         ctx.trc_negative_fixer([t(a) for a in qtrc], 1, 3, MASS, R, CV, CP, *args)  # 5 species for 6 tracers
     ctx.close()
+
+
+@pytest.mark.parametrize("moist", [True, False])
+def test_specific_heat_pressure_matches_oracle(moist):
+    """fedg_trc_specific_heat_pressure (update_pressure_specific_heat) against its restatement:
+    the mixture exactly up to FMA contraction, PRES and DPRES to 1e-13 relative."""
+    from negfix_ref import specific_heat_pressure
+
+    case = cases.C2().scaled(3, 2, 4, porder=3)
+    qtrc, _, _, _, _, _, dh, ph, drhot = moist_state(case, seed=11)
+    therm_hyd = cases.PRES00 / cases.RDRY * (ph / cases.PRES00) ** (cases.CVDRY / cases.CPDRY)
+    tr = list(qtrc) if moist else []
+    want = specific_heat_pressure(tr, drhot, ph, therm_hyd, MASS, R, CV, CP, cases.RDRY, cases.CVDRY, cases.CPDRY,
+                                  cases.PRES00)
+    ctx = fl.Context(case)
+    t = ctx.tensor
+    outs = [ctx.empty() for _ in range(5)]
+    ctx.trc_specific_heat_pressure([t(a) for a in tr], MASS, R, CV, CP, t(drhot), t(ph), t(therm_hyd), *outs)
+    for name, g, w, tol in zip(("Rtot", "CVtot", "CPtot", "PRES", "DPRES"), outs, want,
+                               (1e-15, 1e-15, 1e-15, 1e-13, 1e-13)):
+        got = g.cpu().numpy()
+        scale = np.abs(want[3]).max() if name == "DPRES" else np.abs(w).max()  # DPRES: against PRES
+        assert np.abs(got - w).max() <= tol * scale, name
+    ctx.close()

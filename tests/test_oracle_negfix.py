@@ -69,3 +69,27 @@ def test_state_without_negatives_is_kept():
     np.testing.assert_allclose(pn, pres, rtol=1e-13)
     np.testing.assert_allclose(rn, rtot, rtol=1e-14)
     np.testing.assert_allclose(drn, drhot, rtol=0, atol=1e-9 * np.abs(drhot).max() + 1e-9)
+
+
+def test_specific_heat_pressure_restates_the_dry_and_moist_forms():
+    """update_pressure_specific_heat's restatement: with no tracers it is the dry DRHOT -> PRES of the
+    dynamics oracle; with the moist state's tracers it gives back the mixture and the pressure the
+    state was built from (PRES = P00 (Rtot RHOT / P00)^(CPtot / CVtot))."""
+    import oracle as orc
+    from negfix_ref import specific_heat_pressure
+
+    case = _case()
+    qtrc, ddens, pres, cvtot, cptot, rtot, dh, ph, drhot = moist_state(case, seed=4)
+    therm_hyd = cases.PRES00 / cases.RDRY * (ph / cases.PRES00) ** (cases.CVDRY / cases.CPDRY)
+    consts = (cases.RDRY, cases.CVDRY, cases.CPDRY, cases.PRES00)
+    rt, cvt, cpt, p, dp = specific_heat_pressure(qtrc, drhot, ph, therm_hyd, MASS, R, CV, CP, *consts)
+    np.testing.assert_array_equal(rt, rtot)
+    np.testing.assert_array_equal(cvt, cvtot)
+    np.testing.assert_allclose(p, pres, rtol=1e-14)
+    np.testing.assert_allclose(dp, p - ph, rtol=0, atol=0)
+    rt0, cvt0, cpt0, p0, dp0 = specific_heat_pressure([], drhot, ph, therm_hyd, MASS, R, CV, CP, *consts)
+    assert np.all(rt0 == cases.RDRY) and np.all(cvt0 == cases.CVDRY) and np.all(cpt0 == cases.CPDRY)
+    o = orc.Oracle(case.porder, case.NeX, case.NeY, case.NeZ, case.dom)
+    o.set_base_state(dh, ph)
+    pres_dry, dpres_dry = o.drhot2pres(drhot)
+    np.testing.assert_allclose(p0, np.asarray(pres_dry).reshape(p0.shape), rtol=1e-13)
