@@ -29,6 +29,7 @@ module scale_atm_dyn_dgm_trcadvect3d_gb300
   public :: atm_dyn_dgm_trcadvect3d_gb300_TMAR
   public :: atm_dyn_dgm_trcadvect3d_gb300_save_massflux
   public :: atm_phy_mp_dgm_common_gb300_negative_fixer
+  public :: atm_dyn_dgm_trcadvect3d_gb300_update_pressure_specific_heat
 
   interface
     integer(c_int) function fedg_trc_fct_coef(ctx, qtrc, mflx, rhoq_tp, alph_m, alph_p, ddens, ddens0, &
@@ -64,6 +65,14 @@ module scale_atm_dyn_dgm_trcadvect3d_gb300
       integer(c_int), value :: qa, qla, qia
       real(c_double), intent(in) :: mass(*), r(*), cv(*), cp(*)
       real(c_double), value :: dt
+    end function
+    integer(c_int) function fedg_trc_specific_heat_pressure(ctx, qtrc, qa, mass, r, cv, cp, drhot, pres_hyd, &
+        therm_hyd, rtot, cvtot, cptot, pres, dpres) bind(C, name="fedg_trc_specific_heat_pressure")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx, drhot, pres_hyd, therm_hyd, rtot, cvtot, cptot, pres, dpres
+      type(c_ptr), intent(in) :: qtrc(*)
+      integer(c_int), value :: qa
+      real(c_double), intent(in) :: mass(*), r(*), cv(*), cp(*)
     end function
     integer(c_int) function fedg_synchronize(ctx) bind(C, name="fedg_synchronize")
       import :: c_int, c_ptr
@@ -220,5 +229,41 @@ contains
     if (ierr < 0) call PRC_abort
     ierr = fedg_synchronize( atm_dyn_dgm_nonhydro3d_gb300_ctx() )
   end subroutine atm_phy_mp_dgm_common_gb300_negative_fixer
+
+  !> the tracer driver's update_pressure_specific_heat (driver_trcadv3d.F90:653-716) on one local
+  !! mesh's arrays: Rtot, CVtot, CPtot from the QA tracers and PRES (DPRES) from DRHOT through the
+  !! mixture's exponent
+  subroutine atm_dyn_dgm_trcadvect3d_gb300_update_pressure_specific_heat( &
+    PRES, DPRES, Rtot, CVtot, CPtot, QTRC, DRHOT, PRES_hyd, THERM_hyd, lmesh, elem, QA )
+    use openacc, only: acc_deviceptr
+    use scale_tracer, only: TRACER_MASS, TRACER_R, TRACER_CV, TRACER_CP
+    use scale_localmeshfield_base, only: LocalMeshFieldBaseList
+    class(LocalMesh3D), intent(in) :: lmesh
+    class(ElementBase3D), intent(in) :: elem
+    integer, intent(in) :: QA
+    real(RP), intent(inout), target :: PRES(elem%Np,lmesh%NeA)
+    real(RP), intent(inout), target :: DPRES(elem%Np,lmesh%NeA)
+    real(RP), intent(inout), target :: Rtot(elem%Np,lmesh%NeA)
+    real(RP), intent(inout), target :: CVtot(elem%Np,lmesh%NeA)
+    real(RP), intent(inout), target :: CPtot(elem%Np,lmesh%NeA)
+    type(LocalMeshFieldBaseList), intent(in) :: QTRC(QA)
+    real(RP), intent(in), target :: DRHOT(elem%Np,lmesh%NeA)
+    real(RP), intent(in), target :: PRES_hyd(elem%Np,lmesh%NeA)
+    real(RP), intent(in), target :: THERM_hyd(elem%Np,lmesh%NeA)
+
+    type(c_ptr) :: qp(max(QA, 1))
+    integer :: iq
+    integer(c_int) :: ierr
+    qp(1) = c_null_ptr
+    do iq = 1, QA
+      qp(iq) = acc_deviceptr( QTRC(iq)%ptr%val )
+    end do
+    ierr = fedg_trc_specific_heat_pressure( atm_dyn_dgm_nonhydro3d_gb300_ctx(), qp, QA, &
+      TRACER_MASS, TRACER_R, TRACER_CV, TRACER_CP, &
+      acc_deviceptr(DRHOT), acc_deviceptr(PRES_hyd), acc_deviceptr(THERM_hyd), &
+      acc_deviceptr(Rtot), acc_deviceptr(CVtot), acc_deviceptr(CPtot), acc_deviceptr(PRES), acc_deviceptr(DPRES) )
+    if (ierr < 0) call PRC_abort
+    ierr = fedg_synchronize( atm_dyn_dgm_nonhydro3d_gb300_ctx() )
+  end subroutine atm_dyn_dgm_trcadvect3d_gb300_update_pressure_specific_heat
 
 end module scale_atm_dyn_dgm_trcadvect3d_gb300
